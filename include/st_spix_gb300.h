@@ -1,0 +1,193 @@
+/*
+ * st_spix_gb300 — C ABI of the GB300 streaming-BASS ("BIST") superpixel engine.
+ *
+ * Every entry point takes caller-owned DEVICE pointers (unless a parameter says
+ * "host"), plain sizes and an explicit cudaStream_t (passed as void*), returns an
+ * int status (STSPIX_OK == 0) and never exits the process.  Work is enqueued on
+ * the given stream; entry points that must return a host-side value (a count)
+ * synchronise that stream and say so.  A context is NOT safe for concurrent use
+ * from several host threads; use one context per thread / per stream.
+ *
+ * Reference interfaces replaced (paths inside gauenk/st_spix):
+ *   stspix_bist_forward        st_spix/csrc/bist/pyapi.cu:200 bist_forward_cuda (+ :46 main_loop)
+ *   stspix_get_marked_video    st_spix/csrc/bist/pyapi.cu:260 get_marked_video
+ *   stspix_run_bass            st_spix/csrc/bist/bass.cu:221  run_bass
+ *   stspix_shift_and_fill      st_spix/csrc/bist/shift_and_fill.cu:108 shift_and_fill
+ *   stspix_run_prop            st_spix/csrc/bist/prop.cu:677  run_prop
+ *   stspix_find_border         st_spix/csrc/bist/seg_utils.cu:156,211 CudaFindBorderPixels(_end)
+ *   stspix_init_seg            st_spix/csrc/bist/init_seg.cu:20 init_seg
+ *   stspix_bass_partial        st_spix/csrc/bist/bass.cu:46 bass() stopped after k iterations
+ *                              (exposes update_params.cu:12 and update_seg.cu:281 state)
+ */
+#ifndef ST_SPIX_GB300_H
+#define ST_SPIX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define STSPIX_OK                 0
+#define STSPIX_ERR_ARG            1   /* bad argument (null pointer, size out of range)        */
+#define STSPIX_ERR_CUDA           2   /* a CUDA runtime call failed (see stspix_last_error)    */
+#define STSPIX_ERR_NOMEM          3   /* device allocation failed                               */
+#define STSPIX_ERR_NOPROGRESS     4   /* hole filling stopped shrinking (reference exits here)  */
+#define STSPIX_ERR_ITER_LIMIT     5   /* a bounded device loop hit its iteration cap            */
+#define STSPIX_ERR_CAPACITY       6   /* superpixel ids exceeded the parameter buffer           */
+#define STSPIX_ERR_BARRIER        7   /* a grid barrier timed out (kernel returned early)       */
+#define STSPIX_ERR_DEGENERATE     8   /* non-positive prior covariance determinant              */
+
+/* ---- configuration ------------------------------------------------------
+ * Defaults (stspix_default_config) are the reference's values:
+ *   niters_seg=4, sm_start=0, sigma2_size=0, merge_alpha=0 (pyapi.cu:63-73),
+ *   thresh_relabel=1e-5, thresh_new=1e-2 (pyapi.cu:72-73), split/merge period 4
+ *   (bass.cu:117-135), sp_size=15, sigma2_app=0.009^2, potts=0.5,
+ *   alpha_hastings=log(0.5), split_alpha=0 (demo.cu:45-57,141).            */
+typedef struct stspix_config {
+  int   niters;          /* outer BASS iterations (image mode / first frame)          */
+  int   niters_seg;      /* boundary sweeps per outer iteration                       */
+  int   sp_size;         /* hexagon side: sqrt of the initial superpixel area         */
+  int   sm_start;        /* split/merge only when iteration index > sm_start          */
+  int   sm_period;       /* split when idx%P==0, merge when idx%P==P/2                */
+  int   prop_niters;     /* >0: fixed iterations on propagated frames; 0: the
+                            reference's 4/8/12 ladder on the hole fraction            */
+  float sigma2_app;      /* appearance variance                                       */
+  float potts;           /* Potts weight per differing 8-neighbour                    */
+  float alpha_hastings;  /* log alpha of the merge Hastings ratio                     */
+  float split_alpha;     /* additive split bias                                       */
+  float merge_alpha;     /* additive merge bias                                       */
+  float sigma2_size;     /* kept for API parity (unused by the reference path)        */
+  float thresh_relabel;  /* revive a dead id when appearance distance < this          */
+  float thresh_new;      /* mint a new id when self distance > this                   */
+} stspix_config;
+
+void stspix_default_config(stspix_config* cfg);
+
+/* ---- superpixel parameters ----------------------------------------------
+ * Structure-of-arrays mirror of the reference's SuperpixelParams
+ * (st_spix/csrc/bist/structs.h:13-48).  `capacity` entries are allocated by the
+ * caller; entry i describes superpixel id i.  sigma_shape holds the INVERSE shape
+ * covariance (xx, xy, yy) as the reference stores it.                          */
+typedef struct stspix_params {
+  float*  mu_app;             /* [cap*3] */
+  float*  prior_mu_app;       /* [cap*3] */
+  double* mu_shape;           /* [cap*2] */
+  double* sigma_shape;        /* [cap*3] */
+  float*  logdet_sigma_shape; /* [cap]   */
+  double* prior_mu_shape;     /* [cap*2] */
+  double* prior_sigma_shape;  /* [cap*3] */
+  double* sample_sigma_shape; /* [cap*3] */
+  int*    counts;             /* [cap]   */
+  int*    sm_counts;          /* [cap]   */
+  float*  prior_counts;       /* [cap]   */
+  int*    ids;                /* [cap]   */
+  float*  invalid_counts;     /* [cap]   */
+  int     capacity;
+} stspix_params;
+
+/* Per-frame decision log (near-threshold ties are what label disagreements
+ * with the reference's racy FP32 path trace back to).                          */
+typedef struct stspix_frame_log {
+  int nsplits;        /* accepted splits                                   */
+  int nmerges;        /* accepted merges (superpixels removed)              */
+  int nrevived;       /* relabel: dead ids revived                          */
+  int nminted;        /* relabel: new ids minted                            */
+  int near_ties;      /* Hastings decisions with |ratio + 2| < 1e-6        */
+  int fill_iters;     /* hole-fill iterations (both fills)                  */
+  int niters;         /* outer iterations run                               */
+  int nspix;          /* superpixels after compaction                       */
+} stspix_frame_log;
+
+/* ---- context ------------------------------------------------------------ */
+typedef struct stspix_ctx stspix_ctx;
+
+int         stspix_create(stspix_ctx** ctx, int device);
+int         stspix_destroy(stspix_ctx* ctx);
+const char* stspix_last_error(const stspix_ctx* ctx);
+int         stspix_version(void);
+/* Number of kernels this context has launched since creation. */
+long long   stspix_kernel_launches(const stspix_ctx* ctx);
+/* Copy of the log of the last frame processed by this context (host). */
+int         stspix_get_frame_log(const stspix_ctx* ctx, stspix_frame_log* out);
+
+/* ---- drop-in surface ------------------------------------------------------ */
+
+/* bist_forward: vid f32 [T,H,W,3] contiguous; flows f32 [>=T-1,H,W,2]
+ * interleaved (dx,dy), read at index fidx-1 for frame fidx (may be NULL when
+ * video_mode==0); spix_out i32 [T,H,W].  rgb2lab is accepted and ignored, as in
+ * the reference (pyapi.cu:95-102).  Stream state stays on the device.          */
+int stspix_bist_forward(stspix_ctx* ctx, void* stream,
+                        const float* vid, const float* flows,
+                        int T, int H, int W, int nftrs,
+                        const stspix_config* cfg, int video_mode, int rgb2lab,
+                        int32_t* spix_out);
+
+/* get_marked_video: border (find_border_pixels_end) painted with `color`
+ * (3 floats, device), elsewhere the frame clipped to [0,1].                      */
+int stspix_get_marked_video(stspix_ctx* ctx, void* stream,
+                            const float* vid, const int32_t* spix,
+                            const float* color, int T, int H, int W, int nftrs,
+                            float* marked_out);
+
+/* ---- reference C++ entry points --------------------------------------------- */
+
+/* run_bass on one frame.  labels_out i32 [H*W]; params_out capacity must be >=
+ * the number of superpixels produced (<= 30 x initial hex count); *nspix_out
+ * (host) receives that number.  Synchronises the stream.                        */
+int stspix_run_bass(stspix_ctx* ctx, void* stream, const float* img, int H, int W,
+                    const stspix_config* cfg, int32_t* labels_out,
+                    stspix_params* params_out, int* nspix_out);
+
+/* shift_and_fill: prev labels + prev params (n_prev entries) + flow [H,W,2]
+ * -> filled and shifted labels; updates prev params' prior_counts and
+ * invalid_counts in place.                                                    */
+int stspix_shift_and_fill(stspix_ctx* ctx, void* stream, const int32_t* labels_prev,
+                          stspix_params* params_prev, int n_prev, const float* flow,
+                          int H, int W, int32_t* filled_out, int32_t* shifted_out);
+
+/* run_prop: propagated BASS on one frame given filled/shifted labels and the
+ * previous frame's params (n_prev entries).  niters as given (the ladder is
+ * applied by bist_forward).  Synchronises the stream.                          */
+int stspix_run_prop(stspix_ctx* ctx, void* stream, const float* img, int H, int W,
+                    const stspix_config* cfg, int niters,
+                    const int32_t* filled, const int32_t* shifted,
+                    const stspix_params* params_prev, int n_prev,
+                    int32_t* labels_out, stspix_params* params_out, int* nspix_out);
+
+/* ---- stage-level entry points (used by the parity tests) ------------------ */
+
+/* Hex-grid initialisation; returns the raw hex centre count in *nspix_out (host).
+ * Labels are NOT compacted (as the reference's init_seg).                     */
+int stspix_init_seg(stspix_ctx* ctx, void* stream, int32_t* labels, int H, int W,
+                    int sp_size, int* nspix_out);
+
+/* Border mask: mode 0 = find_border_pixels (image edge counts), mode 1 =
+ * find_border_pixels_end (only the larger label marks).                       */
+int stspix_find_border(stspix_ctx* ctx, void* stream, const int32_t* labels,
+                       uint8_t* border_out, int H, int W, int mode);
+
+/* Run a BASS frame (run_bass) but stop after `iters` outer iterations and dump
+ * the working state; with extra_update != 0 the next iteration's update_params
+ * (statistics + posterior, no split/merge, no sweep) also runs before the dump.  State arrays (device) have `nbuf` entries
+ * (nbuf = 30 x compacted hex count, returned in *nbuf_out):
+ *   count i32[nbuf], valid u8[nbuf], prior_count f32[nbuf],
+ *   mu_app f32[nbuf*3], mu_shape f64[nbuf*2], sigma_shape f64[nbuf*3],
+ *   logdet f64[nbuf], sums i64[nbuf*8] (sum r,g,b in 2^-28 units, sum x, y,
+ *   xx, xy, yy).  Any state pointer may be NULL.  Synchronises.               */
+typedef struct stspix_state_dump {
+  int32_t* count; uint8_t* valid; float* prior_count; float* mu_app;
+  double* mu_shape; double* sigma_shape; double* logdet; int64_t* sums;
+  int capacity;
+} stspix_state_dump;
+
+int stspix_bass_partial(stspix_ctx* ctx, void* stream, const float* img, int H, int W,
+                        const stspix_config* cfg, int iters, int extra_update,
+                        int32_t* labels_out, stspix_state_dump* dump,
+                        int* nbuf_out, int* max_spix_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ST_SPIX_GB300_H */

@@ -1,0 +1,1381 @@
+// ORACLE -- test infrastructure only.  Nothing in the st_spix_gb300 product links,
+// loads or calls this file; only tests/, __graft_entry__.smoke() and bench.py's CPU
+// baseline leg use it, as the checker and as the CPU baseline.
+//
+// CPU restatement of the reference's streaming-BASS ("BIST") per-frame path
+// (gauenk/st_spix, st_spix/csrc/bist/*, the `bist_cuda` extension).  Every function
+// cites the reference file:line it follows.  The reference is a CUDA program with
+// races; this restatement resolves each race by one fixed rule (the same rule the
+// GB300 engine implements), listed here:
+//   R1 sums: pixel colours are accumulated as int64 fixed point (2^-28 units, squares
+//      in 2^-20 units), positions as exact integers, so every sum is order-free.
+//      (reference: FP32 / FP64 atomicAdd, update_params.cu:115, split_merge.cu:874)
+//   R2 split ids: accepted splits get ids max_spix+1, +2, ... in ascending order of
+//      the split superpixel (reference: atomicAdd order, split_merge_orig.cu:968).
+//   R3 merge claims: among superpixels whose merge into f is accepted, the smallest
+//      id claims f (reference: first atomicMax caller, split_merge_orig.cu:635).
+//   R4 forward-warp collisions: smallest (size, id) wins (reference: smallest size,
+//      equal sizes racy, atomic_helpers.cu:90, shift_labels.cu:103).
+//   R5 relabel ties: smallest (distance, candidate id) wins (relabel.cu:275); relabel
+//      ids minted in ascending order; when several superpixels revive one dead id the
+//      copied count comes from the largest of them (last write in ascending order).
+//   R6 connected components keep, per label, the largest 8-connected region, ties to
+//      the region whose first pixel (raster order) comes first (split_disconnected.cu:248).
+//   R7 values the reference reads uninitialised are zero: sm_helper.ninvalid
+//      (split_merge_prop.cu:2000, never cleared) and ss_comps for ids >= nspix_prev
+//      (relabel.cu:236, never written).
+//   R8 floating point: IEEE binary32/64, no contraction into FMA (build with
+//      -ffp-contract=off); expression trees and float/double conversions follow the
+//      reference's source expressions.  The Hastings ratio (split/merge) is evaluated
+//      in FP64 with the lgamma(a_n) terms, which cancel exactly in the reference's
+//      formula, removed (split_merge_orig.cu:536-549, 845-877).
+//
+// Parity status: the reference has no CPU path, no tests and no golden vectors, and
+// its CUDA code cannot run here; this restatement is pinned only by the reference's
+// source (parity unpinned against reference outputs).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "../include/st_spix_gb300.h"
+
+namespace {
+
+constexpr int kFxAppShift = 28;   // colour sums:   round(v * 2^28)
+constexpr int kFxSqShift = 20;    // square sums:   round((v*v) * 2^20)
+constexpr int kFxFlowShift = 24;  // flow sums:     round(f * 2^24)
+
+inline int64_t fx(float v, int shift) {
+  return (int64_t)llrintf(ldexpf(v, shift));
+}
+inline double unfx(int64_t q, int shift) { return ldexp((double)q, -shift); }
+
+// Simple-point table: a 3x3 neighbourhood code (bit i set when neighbour i carries
+// the candidate label or lies outside the image; order NW,N,NE,W,E,SW,S,SE) maps to
+// 1 when relabelling the centre keeps both regions connected.  The table is data,
+// kept identical to the reference's bass_lut (seg_utils.h:15-27).
+const unsigned char kSimpleLut[256] = {
+    0, 0, 1, 1, 0, 0, 1, 1, 1, 1, 0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 0, 0,
+    0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0,
+    1, 1, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 1, 0, 1, 1, 0, 0, 0, 0,
+    0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+    1, 0, 0, 0, 1, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 1,
+    0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 1, 1, 0, 0, 1, 1, 0, 0};
+
+struct D2 { double x, y; };
+struct D3 { double x, y, z; };
+
+// -------------------------------------------------------------------------
+// Cross-frame parameters: SuperpixelParams (structs.h:13-48).
+struct Params {
+  int n = 0;
+  std::vector<float> mu_app, prior_mu_app;
+  std::vector<double> mu_shape, sigma_shape;
+  std::vector<float> logdet;
+  std::vector<double> prior_mu_shape, prior_sigma_shape, sample_sigma_shape;
+  std::vector<int> counts, sm_counts, ids;
+  std::vector<float> prior_counts, invalid_counts;
+  void resize(int m) {
+    n = m;
+    mu_app.assign(3 * m, 0.f); prior_mu_app.assign(3 * m, 0.f);
+    mu_shape.assign(2 * m, 0.0); sigma_shape.assign(3 * m, 0.0);
+    logdet.assign(m, 0.f);
+    prior_mu_shape.assign(2 * m, 0.0); prior_sigma_shape.assign(3 * m, 0.0);
+    sample_sigma_shape.assign(3 * m, 0.0);
+    counts.assign(m, 0); sm_counts.assign(m, 0); ids.assign(m, 0);
+    prior_counts.assign(m, 0.f); invalid_counts.assign(m, 0.f);
+  }
+};
+
+// Per-superpixel working state: spix_params (structs.h:71-106) + helper sums.
+struct Sp {
+  int nbuf = 0;
+  std::vector<int> count, sm_count;
+  std::vector<uint8_t> valid, prop;
+  std::vector<float> prior_count, icount, mu_app, prior_mu_app;
+  std::vector<double> mu_shape, prior_mu_shape, sigma_shape, prior_sigma_shape,
+      prior_icov, sample_sigma_shape, logdet;
+  std::vector<int64_t> acc;  // 8 per id: r,g,b (2^-28), x, y, xx, xy, yy
+  void init(int m) {
+    nbuf = m;
+    count.assign(m, 0); sm_count.assign(m, 0);
+    valid.assign(m, 0); prop.assign(m, 0);
+    prior_count.assign(m, 0.f); icount.assign(m, 0.f);
+    mu_app.assign(3 * m, 0.f); prior_mu_app.assign(3 * m, 0.f);
+    mu_shape.assign(2 * m, 0.0); prior_mu_shape.assign(2 * m, 0.0);
+    sigma_shape.assign(3 * m, 0.0); prior_sigma_shape.assign(3 * m, 0.0);
+    prior_icov.assign(3 * m, 0.0); sample_sigma_shape.assign(3 * m, 0.0);
+    logdet.assign(m, 0.0);
+    acc.assign(8 * (size_t)m, 0);
+  }
+};
+
+// Split/merge helper sums (spix_helper_sm, structs.h:115-156): per id
+// count, colour sums (2^-28), square sums (2^-20), invalid-pixel count.
+struct SmAcc {
+  std::vector<int> count, ninvalid;
+  std::vector<int64_t> s, sq;  // 3 per id each
+  void init(int m) {
+    count.assign(m, 0); ninvalid.assign(m, 0);
+    s.assign(3 * (size_t)m, 0); sq.assign(3 * (size_t)m, 0);
+  }
+};
+
+struct Frame {
+  int H = 0, W = 0, npix = 0;
+  const float* img = nullptr;
+  std::vector<int> seg;
+  std::vector<uint8_t> border;
+  Sp sp;
+  stspix_config cfg{};
+  int max_spix = 0;
+  int status = STSPIX_OK;
+  stspix_frame_log log{};
+};
+
+// -------------------------------------------------------------------------
+// init_seg.cu:11-46 nspix_from_spsize / init_seg host part.
+void hex_geometry(int sp_size, int W, int H, double* hh, double* ww, int* nx, int* ny) {
+  double Hh = sqrt(double(pow(sp_size, 2)) / (1.5 * sqrt(3.0)));
+  double w = sqrt(3.0) * Hh;
+  *hh = Hh; *ww = w;
+  *nx = (int)floor(double(W) / w) + 2;
+  *ny = (int)floor(double(H) / (1.5 * Hh)) + 2;
+}
+
+// init_seg.cu:48-75 InitHexCenter + InitHexSeg (brute force; last minimum wins).
+int init_seg(int* seg, int sp_size, int W, int H) {
+  double Hh, w; int nx, ny;
+  hex_geometry(sp_size, W, H, &Hh, &w, &nx, &ny);
+  int nspix = nx * ny;
+  std::vector<double> c(2 * (size_t)nspix);
+  for (int idx = 0; idx < nspix; idx++) {
+    int x = idx % nx, y = idx / nx;
+    double xx = double(x) * w;
+    double yy = double(y) * 1.5 * Hh;
+    if (y % 2 == 0) xx = xx + 0.5 * w;
+    c[2 * idx] = xx; c[2 * idx + 1] = yy;
+  }
+  int npix = H * W;
+  for (int idx = 0; idx < npix; idx++) {
+    int x = idx % W, y = idx / W;
+    double D2 = 1.7976931348623157e308;
+    int best = 0;
+    for (int j = 0; j < nspix; j++) {
+      double dx = (x - c[j * 2 + 0]);
+      double dy = (y - c[j * 2 + 1]);
+      double d2 = dx * dx + dy * dy;
+      if (d2 <= D2) { D2 = d2; best = j; }
+    }
+    seg[idx] = best;
+  }
+  return nspix;
+}
+
+// compact_spix.cu:41-122: live ids >= prev_nspix renumbered prev_nspix + rank
+// (rank in ascending id order).  Returns prev_nspix + #live new ids.  When sp is
+// given the selected parameter fields move with their ids
+// (fill_new_params_from_old / fill_old_params_from_new, compact_spix.cu:220-290).
+int compactify(std::vector<int>& seg, int prev_nspix, Sp* sp) {
+  int mx = -1;
+  for (int v : seg) mx = std::max(mx, v);
+  if (mx < prev_nspix) return prev_nspix;
+  std::vector<uint8_t> present(mx + 1, 0);
+  for (int v : seg) if (v >= prev_nspix) present[v] = 1;
+  std::vector<int> newid(mx + 1, -1);
+  std::vector<int> src;
+  int r = 0;
+  for (int v = prev_nspix; v <= mx; v++)
+    if (present[v]) { newid[v] = prev_nspix + r++; src.push_back(v); }
+  for (int& v : seg) if (v >= prev_nspix) v = newid[v];
+  if (sp && r > 0) {
+    // copy into a temporary first (the reference stages through new_params)
+    Sp tmp; tmp.init(r);
+    for (int j = 0; j < r; j++) {
+      int s = src[j];
+      for (int c = 0; c < 3; c++) {
+        tmp.mu_app[3 * j + c] = sp->mu_app[3 * s + c];
+        tmp.prior_mu_app[3 * j + c] = sp->prior_mu_app[3 * s + c];
+        tmp.sigma_shape[3 * j + c] = sp->sigma_shape[3 * s + c];
+        tmp.prior_sigma_shape[3 * j + c] = sp->prior_sigma_shape[3 * s + c];
+        tmp.sample_sigma_shape[3 * j + c] = sp->sample_sigma_shape[3 * s + c];
+      }
+      for (int c = 0; c < 2; c++) {
+        tmp.mu_shape[2 * j + c] = sp->mu_shape[2 * s + c];
+        tmp.prior_mu_shape[2 * j + c] = sp->prior_mu_shape[2 * s + c];
+      }
+      tmp.logdet[j] = sp->logdet[s];
+      tmp.count[j] = sp->count[s];
+      tmp.prior_count[j] = sp->prior_count[s];
+      tmp.valid[j] = sp->valid[s];
+    }
+    for (int j = 0; j < r; j++) {
+      int d = prev_nspix + j;
+      for (int c = 0; c < 3; c++) {
+        sp->mu_app[3 * d + c] = tmp.mu_app[3 * j + c];
+        sp->prior_mu_app[3 * d + c] = tmp.prior_mu_app[3 * j + c];
+        sp->sigma_shape[3 * d + c] = tmp.sigma_shape[3 * j + c];
+        sp->prior_sigma_shape[3 * d + c] = tmp.prior_sigma_shape[3 * j + c];
+        sp->sample_sigma_shape[3 * d + c] = tmp.sample_sigma_shape[3 * j + c];
+      }
+      for (int c = 0; c < 2; c++) {
+        sp->mu_shape[2 * d + c] = tmp.mu_shape[2 * j + c];
+        sp->prior_mu_shape[2 * d + c] = tmp.prior_mu_shape[2 * j + c];
+      }
+      sp->logdet[d] = tmp.logdet[j];
+      sp->count[d] = tmp.count[j];
+      sp->prior_count[d] = tmp.prior_count[j];
+      sp->valid[d] = tmp.valid[j];
+    }
+  }
+  return prev_nspix + r;
+}
+
+// -------------------------------------------------------------------------
+// seg_utils.cu:164-195 find_border_pixels: image edges are border.
+void find_border(const int* seg, uint8_t* border, int H, int W) {
+  for (int idx = 0; idx < H * W; idx++) {
+    int x = idx % W, y = idx / W;
+    if (y < 1 || x < 1 || y >= H - 1 || x >= W - 1) { border[idx] = 1; continue; }
+    int C = seg[idx];
+    border[idx] = (C != seg[idx - W] || C != seg[idx + W] || C != seg[idx + 1] ||
+                   C != seg[idx - 1]) ? 1 : 0;
+  }
+}
+
+// seg_utils.cu:218-257 find_border_pixels_end: only the larger label marks.
+void find_border_end(const int* seg, uint8_t* border, int H, int W) {
+  for (int idx = 0; idx < H * W; idx++) {
+    int x = idx % W, y = idx / W;
+    int C = seg[idx];
+    int N = -1, S = -1, E = -1, Wl = -1;
+    if (y > 0) N = seg[idx - W];
+    if (x > 0) Wl = seg[idx - 1];
+    if (y < H - 1) S = seg[idx + W];
+    if (x < W - 1) E = seg[idx + 1];
+    uint8_t b = 0;
+    if ((N >= 0 && C != N) || (S >= 0 && C != S) || (E >= 0 && C != E) ||
+        (Wl >= 0 && C != Wl)) {
+      if (N >= 0 && C > N) b = 1;
+      if (S >= 0 && C > S) b = 1;
+      if (E >= 0 && C > E) b = 1;
+      if (Wl >= 0 && C > Wl) b = 1;
+    }
+    border[idx] = b;
+  }
+}
+
+// -------------------------------------------------------------------------
+// update_params.cu:54-130 clear_fields + sum_by_label (R1 sums).
+void accumulate(Frame& f) {
+  Sp& sp = f.sp;
+  std::fill(sp.count.begin(), sp.count.end(), 0);
+  std::fill(sp.acc.begin(), sp.acc.end(), 0);
+  for (int k = 0; k < sp.nbuf; k++) {
+    for (int c = 0; c < 3; c++) { sp.mu_app[3 * k + c] = 0.f; sp.sigma_shape[3 * k + c] = 0.0; }
+    sp.mu_shape[2 * k] = 0.0; sp.mu_shape[2 * k + 1] = 0.0;
+  }
+  for (int t = 0; t < f.npix; t++) {
+    int k = f.seg[t];
+    if (k < 0) continue;
+    int64_t* a = &sp.acc[8 * (size_t)k];
+    sp.count[k] += 1;
+    for (int c = 0; c < 3; c++) a[c] += fx(f.img[3 * t + c], kFxAppShift);
+    int64_t x = t % f.W, y = t / f.W;
+    a[3] += x; a[4] += y; a[5] += x * x; a[6] += x * y; a[7] += y * y;
+  }
+}
+
+// update_params.cu:206-217 _add_sigma_smoothing (count arrives truncated to int).
+D3 add_sigma_smoothing(D3 in, int count, float pc, int sp_size) {
+  int nf = 50;
+  double total_count = 1. * (count + pc * nf);
+  D3 s;
+  s.x = (pc * sp_size + count * in.x) / (total_count + 3.0);
+  s.y = (count * in.y) / (total_count + 3.0);
+  s.z = (pc * sp_size + count * in.z) / (total_count + 3.0);
+  return s;
+}
+
+// update_params.cu:220-381 calc_simple_update.
+void posterior(Frame& f) {
+  Sp& sp = f.sp;
+  const int sp_size = f.cfg.sp_size;
+  for (int k = 0; k < sp.nbuf; k++) {
+    if (!sp.valid[k]) continue;
+    int count_int = sp.count[k];
+    float pc = sp.prior_count[k];
+    double count = count_int * 1.0;
+    double total_count = (double)count_int + pc * 50;
+    if (count_int <= 0) { sp.valid[k] = 0; continue; }
+    D3 pic;
+    if (sp.prop[k]) {
+      D3 s{sp.sample_sigma_shape[3 * k], sp.sample_sigma_shape[3 * k + 1],
+           sp.sample_sigma_shape[3 * k + 2]};
+      pic = add_sigma_smoothing(s, (int)pc, pc, sp_size);
+    } else {
+      pic = D3{sp.prior_icov[3 * k], sp.prior_icov[3 * k + 1], sp.prior_icov[3 * k + 2]};
+    }
+    double pr_det = pic.x * pic.z - pic.y * pic.y;
+    if (!(pr_det > 0)) f.status = STSPIX_ERR_DEGENERATE;
+    pr_det = sqrt(pr_det);
+    D3 psig;
+    psig.x = pc / pr_det * pic.x;
+    psig.y = pc / pr_det * pic.y;
+    psig.z = pc / pr_det * pic.z;
+    const int64_t* a = &sp.acc[8 * (size_t)k];
+    for (int c = 0; c < 3; c++)
+      sp.mu_app[3 * k + c] = (float)(unfx(a[c], kFxAppShift) / count);
+    double mx = a[3] / count, my = a[4] / count;
+    sp.mu_shape[2 * k] = mx; sp.mu_shape[2 * k + 1] = my;
+    D3 sg;
+    sg.x = a[5] - count * mx * mx;
+    sg.y = a[6] - count * mx * my;
+    sg.z = a[7] - count * my * my;
+    sg.x = (pc * psig.x + sg.x) / (total_count + 3.0);
+    sg.y = (pc * psig.y + sg.y) / (total_count + 3.0);
+    sg.z = (pc * psig.z + sg.z) / (total_count + 3.0);
+    double det = sg.x * sg.z - sg.y * sg.y;
+    if (det <= 0) {
+      sg.x = sg.x + 0.00001;
+      sg.z = sg.z + 0.00001;
+      det = sg.x * sg.z - sg.y * sg.y;
+      if (det <= 0) det = 0.00001;
+    }
+    sp.sigma_shape[3 * k] = sg.z / det;
+    sp.sigma_shape[3 * k + 1] = -sg.y / det;
+    sp.sigma_shape[3 * k + 2] = sg.x / det;
+    sp.logdet[k] = log(det);
+  }
+}
+
+// update_params.cu:12-31 update_params.
+void update_params(Frame& f) { accumulate(f); posterior(f); }
+
+// update_params.cu:385-438 store_sample_sigma_shape.
+void store_sample_sigma_shape(Frame& f) {
+  Sp& sp = f.sp;
+  for (int k = 0; k < sp.nbuf; k++) {
+    if (!sp.valid[k]) continue;
+    const int64_t* a = &sp.acc[8 * (size_t)k];
+    double count = sp.count[k] * 1.0;
+    double mx = a[3] / count, my = a[4] / count;
+    sp.mu_shape[2 * k] = mx; sp.mu_shape[2 * k + 1] = my;
+    D3 s;
+    if (count > 0) {
+      s.x = a[5] / count - mx * mx;
+      s.y = a[6] / count - mx * my;
+      s.z = a[7] / count - my * my;
+    } else {
+      s = D3{sp.prior_sigma_shape[3 * k], sp.prior_sigma_shape[3 * k + 1],
+             sp.prior_sigma_shape[3 * k + 2]};
+    }
+    sp.sample_sigma_shape[3 * k] = s.x;
+    sp.sample_sigma_shape[3 * k + 1] = s.y;
+    sp.sample_sigma_shape[3 * k + 2] = s.z;
+  }
+}
+
+// -------------------------------------------------------------------------
+// seg_utils.h:30-79 ischangbale_by_nbrs + set_nbrs_v1.
+inline bool simple_point(const int nb[8], int label, int* count_diff) {
+  int num = 0, diff = 0;
+  for (int i = 7; i >= 0; i--) {
+    num <<= 1;
+    bool b = (label == nb[i]) || (nb[i] == -1);
+    if (b) num++; else diff++;
+  }
+  *count_diff = diff;
+  return kSimpleLut[num] != 0;
+}
+
+struct Best { float v; int label; };
+
+// update_seg.cu:194-259 calc_joint (FP32 score).
+inline Best calc_joint(const float* imgC, int x, int y, const Sp& sp, int k,
+                       float sigma2_app, float neigh_neq, float beta, Best best) {
+  float res = -1000;
+  int count = sp.count[k];
+  const float x0 = imgC[0] - sp.mu_app[3 * k];
+  const float x1 = imgC[1] - sp.mu_app[3 * k + 1];
+  const float x2 = imgC[2] - sp.mu_app[3 * k + 2];
+  const int d0 = (int)(x - sp.mu_shape[2 * k]);
+  const int d1 = (int)(y - sp.mu_shape[2 * k + 1]);
+  const float sx = (float)sp.sigma_shape[3 * k];
+  const float sy = (float)sp.sigma_shape[3 * k + 1];
+  const float sz = (float)sp.sigma_shape[3 * k + 2];
+  const float ld = (float)sp.logdet[k];
+  res = res - (x0 * x0 + x1 * x1 + x2 * x2) / sigma2_app;
+  res = res - (float)(d0 * d0) * sx - (float)(d1 * d1) * sz - (float)(2 * d0 * d1) * sy;
+  res = res - ld;
+  res = res - beta * neigh_neq;
+  res = res - (float)(100 * (count <= 10));
+  if (res > best.v) { best.v = res; best.label = k; }
+  return best;
+}
+
+// update_seg.cu:30-190 update_seg_subset (one 2x2 parity class).
+void update_seg_subset(Frame& f, int xmod, int ymod) {
+  const int W = f.W, H = f.H;
+  int* seg = f.seg.data();
+  const float s2 = f.cfg.sigma2_app, potts = f.cfg.potts;
+  for (int y = ymod; y < H; y += 2) {
+    for (int x = xmod; x < W; x += 2) {
+      int idx = y * W + x;
+      if (!f.border[idx]) continue;
+      int C = seg[idx];
+      if (C < 0) continue;
+      int N = -1, S = -1, E = -1, Wl = -1, NE = -1, NW = -1, SE = -1, SW = -1;
+      if (x > 0) Wl = seg[idx - 1];
+      if (y > 0) N = seg[idx - W];
+      if (x < W - 1) E = seg[idx + 1];
+      if (y < H - 1) S = seg[idx + W];
+      if (y > 0 && x < W - 1) NE = seg[idx - W + 1];
+      if (y > 0 && x > 0) NW = seg[idx - W - 1];
+      if (x < W - 1 && y < H - 1) SE = seg[idx + W + 1];
+      if (x > 0 && y < H - 1) SW = seg[idx + W - 1];
+      const int nb[8] = {NW, N, NE, Wl, E, SW, S, SE};
+      int dN, dW, dS, dE;
+      bool vN = simple_point(nb, N, &dN);
+      bool vW = simple_point(nb, Wl, &dW);
+      bool vS = simple_point(nb, S, &dS);
+      bool vE = simple_point(nb, E, &dE);
+      if (!vN || !vW || !vS || !vE) continue;
+      const float* imgC = f.img + 3 * (size_t)idx;
+      Best best{-9999.f, C};
+      if (N >= 0) best = calc_joint(imgC, x, y, f.sp, N, s2, (float)dN, potts, best);
+      if (S != N && S >= 0) best = calc_joint(imgC, x, y, f.sp, S, s2, (float)dS, potts, best);
+      if (Wl != S && Wl != N && Wl >= 0)
+        best = calc_joint(imgC, x, y, f.sp, Wl, s2, (float)dW, potts, best);
+      if (E != Wl && E != S && E != N && E >= 0)
+        best = calc_joint(imgC, x, y, f.sp, E, s2, (float)dE, potts, best);
+      if (f.sp.count[C] <= 2 && best.label == C) {
+        if (N >= 0) best.label = N;
+        else if (E >= 0) best.label = E;
+        else if (S >= 0) best.label = S;
+        else if (Wl >= 0) best.label = Wl;
+      }
+      seg[idx] = best.label;
+    }
+  }
+}
+
+// update_seg.cu:281-311 update_seg.
+void update_seg(Frame& f) {
+  for (int it = 0; it < f.cfg.niters_seg; it++) {
+    find_border(f.seg.data(), f.border.data(), f.H, f.W);
+    for (int xm = 0; xm < 2; xm++)
+      for (int ym = 0; ym < 2; ym++) update_seg_subset(f, xm, ym);
+  }
+  find_border(f.seg.data(), f.border.data(), f.H, f.W);
+}
+
+// -------------------------------------------------------------------------
+// Split / merge helpers.
+
+// Per-channel marginal of the reference's Hastings terms
+// (split_merge_orig.cu:536-549 and 845-877): numerator - denominator with
+//   numerator   = a_n log b_0 + lgamma(a_n) + 0.5 log(1/n)
+//   denominator = a_n log b_n + 0.5 n log(pi) + n log 2 + lgamma(a_n)
+// where a_n = a_0 + n/2.  The lgamma(a_n) terms cancel exactly and are dropped.
+inline double marginal_channel(double n, double b0, double bn) {
+  const double a_n = 1e4 + n / 2;
+  return a_n * (log(b0) - log(bn)) + 0.5 * log(1.0 / n) -
+         (0.5 * n * log(M_PI) + n * log(2.0));
+}
+
+// b_n = b_0 + 0.5 * (sum v^2 - (sum v)^2 / n)   (split_merge_orig.cu:480-501)
+inline double bn_of(double b0, double n, int64_t s, int64_t sq) {
+  double S = unfx(s, kFxAppShift), Q = unfx(sq, kFxSqShift);
+  return b0 + 0.5 * (Q - S * S / n);
+}
+
+double total_marginal(double n, double b0, const int64_t* s, const int64_t* sq,
+                      bool clamp_negative, bool* ok) {
+  double t = 0;
+  for (int c = 0; c < 3; c++) {
+    double bn = bn_of(b0, n, s[c], sq[c]);
+    if (clamp_negative && bn < 0) bn = 0.1;
+    t += marginal_channel(n, b0, bn);
+  }
+  if (ok) *ok = true;
+  return t;
+}
+
+// Split/merge constants (split_merge_orig.cu:97-106, 240-251).
+struct SmConst { double b0; double log_alpha; };
+SmConst sm_const(const stspix_config& c) {
+  float i_std = (float)(sqrt(c.sigma2_app) * 2);
+  float a0 = 1e4f;
+  float b0 = i_std * a0;
+  float alpha = (float)exp((double)c.alpha_hastings);
+  return SmConst{(double)b0, log((double)alpha)};
+}
+
+// sum_by_label (split_merge.cu:862-891 / split_merge_prop.cu:1942-2018) over `lab`.
+void sm_accumulate(const Frame& f, const int* lab, const int* shifted, SmAcc& a) {
+  for (int t = 0; t < f.npix; t++) {
+    int k = lab[t];
+    if (k < 0) continue;
+    a.count[k] += 1;
+    for (int c = 0; c < 3; c++) {
+      float v = f.img[3 * t + c];
+      a.s[3 * (size_t)k + c] += fx(v, kFxAppShift);
+      a.sq[3 * (size_t)k + c] += fx(v * v, kFxSqShift);
+    }
+    if (shifted && shifted[t] < 0) a.ninvalid[k] += 1;
+  }
+}
+
+// BFS distance field (split_merge.cu:758-800 calc_split_candidate iterated to a
+// fixed point): 1 at the seed, +1 per 4-connected step inside the seed's label.
+void bfs_dist(const Frame& f, std::vector<int>& dist) {
+  const int W = f.W, H = f.H;
+  std::vector<int> frontier, next;
+  for (int i = 0; i < f.npix; i++) if (dist[i] == 1) frontier.push_back(i);
+  int d = 1;
+  while (!frontier.empty()) {
+    next.clear();
+    for (int idx : frontier) {
+      int x = idx % W, y = idx / W, C = f.seg[idx];
+      const int nbr[4] = {y > 0 ? idx - W : -1, x > 0 ? idx - 1 : -1,
+                          y < H - 1 ? idx + W : -1, x < W - 1 ? idx + 1 : -1};
+      for (int q : nbr) {
+        if (q < 0) continue;
+        if (dist[q] == -1 && f.seg[q] == C) { dist[q] = d + 1; next.push_back(q); }
+      }
+    }
+    frontier.swap(next);
+    d++;
+  }
+}
+
+// init_split (split_merge.cu:803-844): seed at the truncated mean shifted by
+// `direction` (+-1 in x, +-2 in y).
+void seed_split(const Frame& f, std::vector<int>& dist, int direction) {
+  const Sp& sp = f.sp;
+  for (int k = 0; k < sp.nbuf; k++) {
+    if (!sp.valid[k]) continue;
+    int x, y;
+    if (direction == 1 || direction == -1) {
+      x = int(sp.mu_shape[2 * k]) + direction;
+      y = int(sp.mu_shape[2 * k + 1]);
+    } else {
+      x = int(sp.mu_shape[2 * k]);
+      y = int(sp.mu_shape[2 * k + 1]) + direction;
+    }
+    long long ind = (long long)y * f.W + x;
+    if (ind < 0 || ind > (long long)f.W * f.H - 1) continue;
+    if (f.seg[ind] != k) continue;
+    dist[ind] = 1;
+  }
+}
+
+// Shared part of run_split_orig / run_split_p: bipartition labels.
+// Returns sm_seg (k or k + max_spix + 1 per pixel).
+std::vector<int> split_partition(const Frame& f, int direction) {
+  std::vector<int> d1(f.npix, -1), d2(f.npix, -1);
+  seed_split(f, d1, direction);
+  seed_split(f, d2, -direction);
+  bfs_dist(f, d1);
+  bfs_dist(f, d2);
+  std::vector<int> sm(f.npix);
+  for (int t = 0; t < f.npix; t++) {
+    int v = f.seg[t];
+    if (d1[t] > d2[t]) v += f.max_spix + 1;
+    sm[t] = v;
+  }
+  return sm;
+}
+
+inline bool near_tie(double h) { return fabs(h + 2.0) < 1e-6; }
+
+// split_merge_orig.cu:202-414 CudaCalcSplitCandidate_orig (and the prop variant,
+// split_merge_prop.cu:184-395 with update_split_flag_p :3026-3149 when prop_mode).
+void run_split(Frame& f, int direction, const int* shifted, bool prop_mode) {
+  Sp& sp = f.sp;
+  const int nbuf = sp.nbuf;
+  if (f.max_spix > nbuf / 2) return;
+  SmConst K = sm_const(f.cfg);
+  std::vector<int> sm = split_partition(f, direction);
+  SmAcc a; a.init(nbuf + 2);
+  sm_accumulate(f, sm.data(), prop_mode ? shifted : nullptr, a);
+  const int off = f.max_spix + 1;
+  std::vector<uint8_t> accept(nbuf, 0), select(nbuf, 1);
+  std::vector<int> newid(nbuf, -1);
+  int next = f.max_spix;
+  for (int k = 0; k < nbuf; k++) {
+    if (!sp.valid[k]) continue;
+    int s = k + off;
+    if (s >= nbuf) continue;
+    double count_f = sp.count[k], count_k = a.count[k], count_s = a.count[s];
+    if (count_f < 1 || count_k < 1 || count_s < 1) continue;
+    if (count_f != count_k + count_s) continue;
+    int64_t sq_f[3], s_f[3];
+    for (int c = 0; c < 3; c++) {
+      sq_f[c] = a.sq[3 * (size_t)k + c] + a.sq[3 * (size_t)s + c];
+      s_f[c] = sp.acc[8 * (size_t)k + c];
+    }
+    double mk = total_marginal(count_k, K.b0, &a.s[3 * (size_t)k], &a.sq[3 * (size_t)k], false, nullptr);
+    double ms = total_marginal(count_s, K.b0, &a.s[3 * (size_t)s], &a.sq[3 * (size_t)s], false, nullptr);
+    double mf = total_marginal(count_f, K.b0, s_f, sq_f, false, nullptr);
+    double h = mk + ms - mf + f.cfg.split_alpha;
+    bool prop_k = true;
+    if (prop_mode) {
+      bool is_prop = sp.prop[k];
+      int ninv_k = a.ninvalid[k], ninv_s = a.ninvalid[s];
+      prop_k = (ninv_k <= ninv_s);
+      select[k] = prop_k || !is_prop;
+      float iperc_k = (float)(ninv_k / (1.0 * count_k));
+      float iperc_s = (float)(ninv_k / (1.0 * count_s));  // reference uses ninvalid_k here
+      float iperc = prop_k ? iperc_k : iperc_s;
+      iperc = is_prop ? iperc : 1.0f;
+      h = h - 2 * (1.0 - iperc);
+    }
+    if (near_tie(h)) f.log.near_ties++;
+    if (!(h > -2)) continue;
+    accept[k] = 1;
+    int snew = ++next;
+    newid[k] = snew;
+    if (!prop_mode) {
+      float pcn = (float)std::max(sp.prior_count[k] / 2.0, 8.0);
+      sp.prior_count[k] = pcn;
+      sp.prior_count[snew] = pcn;
+    } else {
+      float pc = sp.prior_count[k];
+      float half = (float)std::max(pc / 2.0, 36.0);
+      if (prop_k) {
+        sp.prior_count[k] = pc;
+        sp.prior_count[snew] = (float)(pc / 2.);
+        sp.prop[snew] = 0;
+      } else {
+        sp.prior_count[k] = half;
+        sp.prior_count[snew] = half;
+        sp.prop[snew] = 0;
+        double pcs = sp.prior_count[snew];
+        sp.prior_icov[3 * k] = pcs; sp.prior_icov[3 * k + 1] = 0; sp.prior_icov[3 * k + 2] = pcs;
+      }
+      sp.icount[k] = (float)(sp.icount[k] / 2.0);
+      double pcs = sp.prior_count[snew];
+      sp.prior_icov[3 * snew] = pcs; sp.prior_icov[3 * snew + 1] = 0; sp.prior_icov[3 * snew + 2] = pcs;
+      sp.valid[snew] = 1;
+    }
+    f.log.nsplits++;
+  }
+  // split_sp (split_merge.cu:1002-1031) / split_sp_p (split_merge_prop.cu:2317-2350)
+  for (int t = 0; t < f.npix; t++) {
+    int k = f.seg[t];
+    if (k < 0 || !sp.valid[k] || !accept[k]) continue;
+    int s = newid[k];
+    int k2 = k + off;
+    if (!prop_mode || select[k]) {
+      if (sm[t] == k2) f.seg[t] = s;
+    } else {
+      if (sm[t] == k) f.seg[t] = s;
+    }
+    if (!prop_mode) sp.valid[s] = 1;
+  }
+  if (next >= nbuf) f.status = STSPIX_ERR_CAPACITY;
+  f.max_spix = next;
+}
+
+// split_merge_orig.cu:79-199 CudaCalcMergeCandidate_orig (prop_mode:
+// split_merge_prop.cu:87-181 with calc_merge_candidate_p :1808-1845 and
+// remove_sp_p :2353-2449).
+void run_merge(Frame& f, int direction, bool prop_mode) {
+  Sp& sp = f.sp;
+  const int nbuf = sp.nbuf, W = f.W, H = f.H;
+  SmConst K = sm_const(f.cfg);
+  std::vector<int> pair(nbuf, -1);
+  // calc_merge_candidate (split_merge.cu:719-755)
+  for (int idx = 0; idx < f.npix; idx++) {
+    if (!f.border[idx]) continue;
+    int x = idx % W, y = idx / W;
+    int C = f.seg[idx];
+    int Wl = -1;
+    if (!prop_mode) {
+      if (direction == 1) { if (y >= 0 && y < H - 1) Wl = f.seg[idx + W]; }
+      else { if (x > 0 && x < W) Wl = f.seg[idx - 1]; }
+      if (Wl >= 0 && C != Wl) pair[C] = std::max(pair[C], Wl);
+    } else {
+      if (direction == 1) { if (y > 1 && y < H - 2) Wl = f.seg[idx + W]; }
+      else { if (x > 1 && x < W - 2) Wl = f.seg[idx - 1]; }
+      bool pC = sp.prop[C];
+      bool pW = (Wl >= 0) ? sp.prop[Wl] : false;
+      if (Wl >= 0 && C != Wl && pC != pW) pair[C] = std::max(pair[C], Wl);
+    }
+  }
+  // Squares come from a pass over the current labels (sum_by_label_merge_p); the
+  // linear colour sums and counts are the ones of the last update_params, indexed
+  // by id (sp_helper / sp_params, split_merge_prop.cu:2572-2630).  They differ only
+  // for ids relabelled in between (prop frames), as in the reference.
+  SmAcc a; a.init(nbuf);
+  sm_accumulate(f, f.seg.data(), nullptr, a);
+  // calc_merge_stats_step0/1/2 + update_merge_flag (split_merge_orig.cu:456-656)
+  // m_single[k] exists only when k has its own candidate (b_n computed in step0).
+  std::vector<double> msingle(nbuf, 0);
+  std::vector<uint8_t> has_single(nbuf, 0);
+  for (int k = 0; k < nbuf; k++) {
+    if (!sp.valid[k] || pair[k] < 0) continue;
+    msingle[k] = total_marginal(sp.count[k], K.b0, &sp.acc[8 * (size_t)k], &a.sq[3 * (size_t)k], true, nullptr);
+    has_single[k] = 1;
+  }
+  std::vector<int> claim(nbuf, INT32_MAX);
+  std::vector<uint8_t> want(nbuf, 0);
+  for (int k = 0; k < nbuf; k++) {
+    if (!sp.valid[k]) continue;
+    int fk = pair[k];
+    if (fk < 0 || !sp.valid[fk]) continue;
+    double count_k = sp.count[k];
+    double count_f = sp.count[k] + sp.count[fk];
+    if (count_k < 1 || count_f < 1) continue;
+    int64_t s_f[3], sq_f[3];
+    for (int c = 0; c < 3; c++) {
+      s_f[c] = sp.acc[8 * (size_t)k + c] + sp.acc[8 * (size_t)fk + c];
+      sq_f[c] = a.sq[3 * (size_t)k + c] + a.sq[3 * (size_t)fk + c];
+    }
+    double m_merged = total_marginal(count_f, K.b0, s_f, sq_f, true, nullptr);
+    double h;
+    if (!has_single[fk]) {
+      h = -INFINITY;  // f's own b_n never computed: log(0) -> ratio -inf
+    } else {
+      h = m_merged - (K.log_alpha + msingle[k] + msingle[fk]) + f.cfg.merge_alpha;
+    }
+    if (near_tie(h)) f.log.near_ties++;
+    if (h > -2) { want[k] = 1; claim[fk] = std::min(claim[fk], k); }
+  }
+  std::vector<uint8_t> merge(nbuf, 0);
+  for (int k = 0; k < nbuf; k++)
+    if (want[k] && claim[pair[k]] == k) merge[k] = 1;
+  // remove_sp / remove_sp_p
+  std::vector<uint8_t> remove(nbuf, 0);
+  std::vector<int> target = pair;
+  std::vector<uint8_t> valid0 = sp.valid;
+  for (int k = 0; k < nbuf; k++) {
+    int s = pair[k];
+    if (s < 0) continue;
+    bool is_cycle = pair[s] == k;
+    if (!valid0[k] || !valid0[s]) continue;
+    if (!prop_mode) {
+      if (merge[k] && (!merge[s] || (is_cycle && k < s))) {
+        remove[k] = 1; sp.valid[k] = 0;
+        sp.prior_count[s] = sp.prior_count[k] + sp.prior_count[s];
+        f.log.nmerges++;
+      }
+    } else {
+      bool cond_c = is_cycle && sp.prop[k];
+      if (merge[k] && (!merge[s] || cond_c)) {
+        int r = k, t = s;
+        if (sp.prop[k]) { target[s] = k; r = s; t = k; }
+        remove[r] = 1; sp.valid[r] = 0;
+        sp.prior_count[t] = sp.prior_count[r] + sp.prior_count[t];
+        f.log.nmerges++;
+      }
+    }
+  }
+  // merge_sp (split_merge.cu:984-1000)
+  for (int t = 0; t < f.npix; t++) {
+    int k = f.seg[t];
+    if (k >= 0 && remove[k]) f.seg[t] = target[k];
+  }
+}
+
+// -------------------------------------------------------------------------
+// relabel.cu:126-409 relabel_spix (prop frames, before each merge).
+void relabel(Frame& f, const Params& prev, int nspix_prev) {
+  Sp& sp = f.sp;
+  const int nspix = f.max_spix + 1;
+  std::vector<uint8_t> living(nspix, 0);
+  for (int v : f.seg) if (v >= 0 && v < nspix) living[v] = 1;
+  std::vector<float> best_d(nspix, 10000.f);
+  std::vector<int> best_c(nspix, INT32_MAX);
+  std::vector<float> ss(nspix, 0.f);
+  for (int s = 0; s < nspix; s++) {
+    if (!living[s]) continue;
+    for (int c = 0; c < nspix_prev; c++) {
+      bool same = (c == s);
+      if (c < nspix && living[c] && !same) continue;
+      float dx = sp.mu_app[3 * s] - prev.prior_mu_app[3 * c];
+      float dy = sp.mu_app[3 * s + 1] - prev.prior_mu_app[3 * c + 1];
+      float dz = sp.mu_app[3 * s + 2] - prev.prior_mu_app[3 * c + 2];
+      float delta = (dx * dx + dy * dy + dz * dz);
+      if (same) ss[s] = delta;
+      if (delta < best_d[s] || (delta == best_d[s] && c < best_c[s])) {
+        best_d[s] = delta; best_c[s] = c;
+      }
+    }
+  }
+  std::vector<uint8_t> rel(nspix, 0);
+  std::vector<int> rid(nspix, -1);
+  int next = f.max_spix;
+  for (int s = 0; s < nspix; s++) {
+    if (!living[s]) continue;
+    int c = best_c[s];
+    bool revive = (best_d[s] < f.cfg.thresh_relabel) && (c < nspix) && (c != s);
+    if (revive) { rel[s] = 1; rid[s] = c; f.log.nrevived++; }
+    else if (ss[s] > f.cfg.thresh_new) { rel[s] = 1; rid[s] = ++next; f.log.nminted++; }
+  }
+  // relabel_spix_kernel (relabel.cu:86-120), applied in ascending old-id order.
+  for (int s = 0; s < nspix; s++) {
+    if (!rel[s]) continue;
+    int n = rid[s];
+    sp.count[n] = sp.count[s];
+    sp.icount[n] = sp.icount[s];
+    sp.valid[s] = 0;
+    sp.valid[n] = 1;
+    if (n >= nspix_prev) {
+      sp.prop[n] = 0;
+      sp.prior_count[n] = sp.prior_count[s];
+      for (int c = 0; c < 3; c++) {
+        sp.prior_sigma_shape[3 * n + c] = sp.prior_sigma_shape[3 * s + c];
+        sp.sample_sigma_shape[3 * n + c] = sp.sample_sigma_shape[3 * s + c];
+        sp.prior_mu_app[3 * n + c] = sp.prior_mu_app[3 * s + c];
+        sp.prior_icov[3 * n + c] = sp.prior_icov[3 * s + c];
+      }
+    }
+  }
+  for (int& v : f.seg) if (v >= 0 && v < nspix && rel[v]) v = rid[v];
+  if (next >= sp.nbuf) f.status = STSPIX_ERR_CAPACITY;
+  f.max_spix = next;
+}
+
+// -------------------------------------------------------------------------
+// Outer loop shared by bass (bass.cu:46-181) and prop_bass_v3 (prop.cu:326-468).
+void bass_loop(Frame& f, int niters, const int* shifted, bool prop_mode,
+               const Params* prev, int nspix_prev, int stop_after, int extra_update) {
+  int count = 1;
+  const int P = f.cfg.sm_period > 0 ? f.cfg.sm_period : 4;
+  for (int idx = 0; idx < niters; idx++) {
+    if (stop_after >= 0 && idx == stop_after) {
+      if (extra_update) update_params(f);
+      return;
+    }
+    update_params(f);
+    if (idx > f.cfg.sm_start) {
+      if (idx % P == 0) {
+        count += 1;
+        int direction = count % 2 + 1;
+        run_split(f, direction, shifted, prop_mode);
+        update_params(f);
+      }
+      if (idx % P == P / 2) {
+        int direction;
+        if (prop_mode) {
+          count += 1;
+          direction = count % 2;
+          relabel(f, *prev, nspix_prev);
+        } else {
+          direction = count % 2;
+        }
+        run_merge(f, direction, prop_mode);
+        update_params(f);
+      }
+    }
+    update_seg(f);
+  }
+  f.log.niters = niters;
+  if (stop_after >= 0) {
+    if (extra_update) update_params(f);
+    return;
+  }
+  update_params(f);
+  store_sample_sigma_shape(f);
+}
+
+// sparams_io.cu:142-286 read_params over the first n ids, then
+// sparams_io.cu:583-688 update_prior (prior := estimate for counts > 0).
+void read_params(const Sp& sp, int n, Params& out) {
+  out.resize(n);
+  for (int i = 0; i < n; i++) {
+    for (int c = 0; c < 3; c++) {
+      out.mu_app[3 * i + c] = sp.mu_app[3 * i + c];
+      out.prior_mu_app[3 * i + c] = sp.prior_mu_app[3 * i + c];
+      out.sigma_shape[3 * i + c] = sp.sigma_shape[3 * i + c];
+      out.prior_sigma_shape[3 * i + c] = sp.prior_sigma_shape[3 * i + c];
+      out.sample_sigma_shape[3 * i + c] = sp.sample_sigma_shape[3 * i + c];
+    }
+    for (int c = 0; c < 2; c++) {
+      out.mu_shape[2 * i + c] = sp.mu_shape[2 * i + c];
+      out.prior_mu_shape[2 * i + c] = sp.prior_mu_shape[2 * i + c];
+    }
+    out.logdet[i] = (float)sp.logdet[i];
+    out.counts[i] = sp.count[i];
+    out.invalid_counts[i] = sp.icount[i];
+    out.sm_counts[i] = sp.sm_count[i];
+    out.prior_counts[i] = sp.prior_count[i];
+    out.ids[i] = i;
+  }
+  for (int i = 0; i < n; i++) {
+    if (out.counts[i] <= 0) continue;
+    for (int c = 0; c < 3; c++) out.prior_mu_app[3 * i + c] = out.mu_app[3 * i + c];
+    for (int c = 0; c < 2; c++) out.prior_mu_shape[2 * i + c] = out.mu_shape[2 * i + c];
+    for (int c = 0; c < 3; c++) out.prior_sigma_shape[3 * i + c] = out.sigma_shape[3 * i + c];
+  }
+}
+
+// bass.cu:221-345 run_bass.  stop_after >= 0 stops the outer loop early (debug).
+int run_bass(Frame& f, const float* img, int H, int W, const stspix_config& cfg,
+             Params* out, int stop_after, int extra_update) {
+  f.H = H; f.W = W; f.npix = H * W; f.img = img; f.cfg = cfg;
+  f.seg.assign(f.npix, 0); f.border.assign(f.npix, 0);
+  f.status = STSPIX_OK; f.log = stspix_frame_log{};
+  int nspix_raw = init_seg(f.seg.data(), cfg.sp_size, W, H);
+  int nspix = compactify(f.seg, 0, nullptr);
+  int nbuf = nspix_raw * 30;  // bass.cu:245 sizes the buffer before compaction
+  f.sp.init(nbuf);
+  Sp& sp = f.sp;
+  // mark_active_contiguous + init_sp_params_kernel (init_sparams.cu:25-166, 195-286)
+  int count = (int)(f.npix / (1. * nspix));
+  for (int k = 0; k < nbuf; k++) {
+    sp.prior_sigma_shape[3 * k] = 1.0 / cfg.sp_size;
+    sp.prior_sigma_shape[3 * k + 1] = 0.;
+    sp.prior_sigma_shape[3 * k + 2] = 1.0 / cfg.sp_size;
+    sp.prior_icov[3 * k] = 1; sp.prior_icov[3 * k + 1] = 0; sp.prior_icov[3 * k + 2] = 1;
+    sp.prop[k] = 0;
+    if (k < nspix) { sp.valid[k] = 1; sp.prior_count[k] = (float)count; }
+    else sp.valid[k] = 0;
+  }
+  // prior_mu_app := initial mean (init_sp_params_kernel copies calc_summ_stats' mean)
+  accumulate(f);
+  for (int k = 0; k < nspix; k++) {
+    double c = sp.count[k];
+    for (int ch = 0; ch < 3; ch++)
+      sp.prior_mu_app[3 * k + ch] =
+          sp.count[k] > 0 ? (float)(unfx(sp.acc[8 * (size_t)k + ch], kFxAppShift) / c) : 0.f;
+  }
+  find_border(f.seg.data(), f.border.data(), H, W);
+  f.max_spix = nspix - 1;
+  bass_loop(f, cfg.niters, nullptr, false, nullptr, 0, stop_after, extra_update);
+  if (stop_after >= 0) return nspix;
+  find_border_end(f.seg.data(), f.border.data(), H, W);
+  int n = compactify(f.seg, 0, &f.sp);
+  if (out) read_params(f.sp, n, *out);
+  f.log.nspix = n;
+  return n;
+}
+
+// -------------------------------------------------------------------------
+// fill_missing.cu:35-130 + 288-441 + 617-647 (parity-scheduled hole fill).
+int fill_missing(std::vector<int>& seg, const std::vector<double>& centers, int H, int W,
+                 int break_iter, int* iters_out) {
+  const int npix = H * W;
+  std::vector<uint8_t> border(npix);
+  int iter = 0;
+  int prev_neg = (int)1410065408;  // (int)10000000000 as the reference truncates it
+  int num_neg = 1;
+  int status = STSPIX_OK;
+  while (num_neg > 0) {
+    if (break_iter > 0 && iter >= break_iter) break;
+    num_neg = 0;
+    for (int idx = 0; idx < npix; idx++) {
+      int x = idx % W, y = idx / W;
+      int N = -1, S = -1, E = -1, Wl = -1;
+      if (y > 0) N = seg[idx - W];
+      if (x > 0) Wl = seg[idx - 1];
+      if (y < H - 1) S = seg[idx + W];
+      if (x < W - 1) E = seg[idx + 1];
+      border[idx] = (N >= 0 || Wl >= 0 || S >= 0 || E >= 0) ? 1 : 0;
+      if (seg[idx] < 0) num_neg++;
+    }
+    for (int xm = 0; xm < 2; xm++) {
+      for (int ym = 0; ym < 2; ym++) {
+        for (int y = ym; y < H; y += 2) {
+          for (int x = xm; x < W; x += 2) {
+            int idx = y * W + x;
+            if (!border[idx] || seg[idx] != -1) continue;
+            int N = -1, S = -1, E = -1, Wl = -1;
+            if (x > 0) Wl = seg[idx - 1];
+            if (y > 0) N = seg[idx - W];
+            if (x < W - 1) E = seg[idx + 1];
+            if (y < H - 1) S = seg[idx + W];
+            float bx = -999999; int bl = -1;
+            auto consider = [&](int lab) {
+              const double* cp = &centers[2 * (size_t)lab];
+              float dx = (1.0f * x - cp[0]) / (1.0f * W);
+              float dy = (1.0f * y - cp[1]) / (1.0f * H);
+              float sim = -dx * dx - dy * dy;
+              if (sim > bx) { bx = sim; bl = lab; }
+            };
+            if (N >= 0) consider(N);
+            if (S >= 0 && S != N) consider(S);
+            if (Wl >= 0 && Wl != S && Wl != N) consider(Wl);
+            if (E >= 0 && E != Wl && E != S && E != N) consider(E);
+            seg[idx] = bl;
+          }
+        }
+      }
+    }
+    iter++;
+    if (iter > 0 && num_neg == prev_neg) { status = STSPIX_ERR_NOPROGRESS; break; }
+    prev_neg = num_neg;
+  }
+  if (iters_out) *iters_out += iter;
+  return status;
+}
+
+// split_disconnected.cu:33-96, 107-185, 248-311, 458-498: keep the largest
+// 8-connected region of each label, others -> -1 (R6).
+void invalidate_disconnected(std::vector<int>& seg, int H, int W, int nspix) {
+  const int npix = H * W;
+  std::vector<int> parent(npix);
+  std::iota(parent.begin(), parent.end(), 0);
+  auto find = [&](int a) {
+    while (parent[a] != a) { parent[a] = parent[parent[a]]; a = parent[a]; }
+    return a;
+  };
+  for (int idx = 0; idx < npix; idx++) {
+    int L = seg[idx];
+    if (L < 0) continue;
+    int y = idx / W, x = idx % W;
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) {
+        int yy = y + dy, xx = x + dx;
+        if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+        int q = yy * W + xx;
+        if (seg[q] != L) continue;
+        int a = find(idx), b = find(q);
+        if (a != b) { if (a < b) parent[b] = a; else parent[a] = b; }
+      }
+  }
+  std::vector<int> root(npix, -1), size(npix, 0);
+  for (int i = 0; i < npix; i++) if (seg[i] >= 0) { root[i] = find(i); size[root[i]]++; }
+  std::vector<int> best_root(std::max(nspix, 1), -1), best_size(std::max(nspix, 1), -1);
+  for (int r = 0; r < npix; r++) {
+    if (size[r] == 0) continue;  // r is a root iff size>0
+    int L = seg[r];
+    if (L >= nspix) continue;
+    if (size[r] > best_size[L]) { best_size[L] = size[r]; best_root[L] = r; }
+  }
+  for (int i = 0; i < npix; i++) {
+    int L = seg[i];
+    if (L < 0 || L >= nspix) continue;
+    if (root[i] != best_root[L]) seg[i] = -1;
+  }
+}
+
+// shift_and_fill.cu:108-339 (with sp_pooling.cu:27-71, shift_labels.cu:33-239).
+int shift_and_fill(const std::vector<int>& prev, Params& pp, const float* flow, int H, int W,
+                   std::vector<int>& filled, std::vector<int>& shifted, int* fill_iters) {
+  const int npix = H * W, nspix = pp.n;
+  // sp_downsample_kernel + normz_downsample_kernel: mean flow per superpixel
+  std::vector<int> cnt(nspix, 0);
+  std::vector<int64_t> fs(2 * (size_t)nspix, 0);
+  for (int t = 0; t < npix; t++) {
+    int k = prev[t];
+    if (k < 0 || k >= nspix) continue;
+    cnt[k]++;
+    fs[2 * (size_t)k] += fx(flow[2 * (size_t)t], kFxFlowShift);
+    fs[2 * (size_t)k + 1] += fx(flow[2 * (size_t)t + 1], kFxFlowShift);
+  }
+  std::vector<float> fds(2 * (size_t)nspix, 0.f);
+  for (int k = 0; k < nspix; k++)
+    for (int c = 0; c < 2; c++)
+      fds[2 * k + c] = (cnt[k] > 0) ? (float)(unfx(fs[2 * k + c], kFxFlowShift) / (1. * cnt[k])) : 0.f;
+  std::vector<double> centers(2 * (size_t)nspix);
+  for (int i = 0; i < 2 * nspix; i++) centers[i] = pp.mu_shape[i] + (double)fds[i];
+  // shift_labels_kernel + decode_kernel (R4)
+  std::vector<uint64_t> best(npix, UINT64_MAX);
+  std::vector<int> hits(npix, 0);
+  for (int t = 0; t < npix; t++) {
+    int k = prev[t];
+    if (k < 0 || k >= nspix) continue;
+    int size = cnt[k];
+    int fw = (int)roundf(fds[2 * k]);
+    int fh = (int)roundf(fds[2 * k + 1]);
+    int w = t % W + fw, h = t / W + fh;
+    if (w < 0 || w >= W || h < 0 || h >= H) continue;
+    int d = h * W + w;
+    hits[d]++;
+    uint64_t key = ((uint64_t)(uint32_t)size << 32) | (uint32_t)k;
+    if (key < best[d]) best[d] = key;
+  }
+  shifted.assign(npix, -1);
+  for (int t = 0; t < npix; t++) if (hits[t] > 0) shifted[t] = (int)(uint32_t)best[t];
+  filled = shifted;
+  std::vector<int> cs(nspix, 0), cf(nspix, 0);
+  for (int v : filled) if (v >= 0) cs[v]++;
+  int st = fill_missing(filled, centers, H, W, 1000, fill_iters);
+  if (st == STSPIX_OK) {
+    invalidate_disconnected(filled, H, W, nspix);
+    st = fill_missing(filled, centers, H, W, 1000, fill_iters);
+  }
+  for (int v : filled) if (v >= 0) cf[v]++;
+  for (int k = 0; k < nspix; k++) {
+    pp.invalid_counts[k] = (float)((cf[k] - cs[k]) / (static_cast<float>(cf[k]) + 1e-8));
+    if (cnt[k] > 0) pp.prior_counts[k] = (float)std::min(std::max(1.0 * cnt[k], 100.0), 10000.0);
+  }
+  return st;
+}
+
+// prop.cu:677-865 run_prop (with sparams_io.cu:123-140,353-520 write_params,
+// init_sparams.cu:195-286 mark_active).
+int run_prop(Frame& f, const float* img, int H, int W, const stspix_config& cfg, int niters,
+             const std::vector<int>& filled, const std::vector<int>& shifted,
+             const Params& prev, Params* out) {
+  f.H = H; f.W = W; f.npix = H * W; f.img = img; f.cfg = cfg;
+  f.status = STSPIX_OK;
+  int fill_iters = f.log.fill_iters;
+  f.log = stspix_frame_log{};
+  f.log.fill_iters = fill_iters;
+  const int nspix_prev = prev.n;
+  const int nbuf = nspix_prev * 10;
+  f.seg = filled;
+  f.border.assign(f.npix, 0);
+  f.sp.init(nbuf);
+  Sp& sp = f.sp;
+  for (int i = 0; i < nspix_prev; i++) {
+    for (int c = 0; c < 3; c++) {
+      sp.mu_app[3 * i + c] = prev.mu_app[3 * i + c];
+      sp.prior_mu_app[3 * i + c] = prev.prior_mu_app[3 * i + c];
+      sp.sigma_shape[3 * i + c] = prev.sigma_shape[3 * i + c];
+      sp.prior_sigma_shape[3 * i + c] = prev.prior_sigma_shape[3 * i + c];
+      sp.sample_sigma_shape[3 * i + c] = prev.sample_sigma_shape[3 * i + c];
+    }
+    for (int c = 0; c < 2; c++) {
+      sp.mu_shape[2 * i + c] = prev.mu_shape[2 * i + c];
+      sp.prior_mu_shape[2 * i + c] = prev.prior_mu_shape[2 * i + c];
+    }
+    sp.logdet[i] = prev.logdet[i];
+    double px = prev.prior_sigma_shape[3 * i], py = prev.prior_sigma_shape[3 * i + 1],
+           pz = prev.prior_sigma_shape[3 * i + 2];
+    double pr_det = px * pz - py * py;  // invert_cov (sparams_io.cu:505-520)
+    sp.prior_icov[3 * i] = pz / pr_det;
+    sp.prior_icov[3 * i + 1] = py / pr_det;
+    sp.prior_icov[3 * i + 2] = px / pr_det;
+    sp.count[i] = prev.counts[i];
+    sp.icount[i] = prev.invalid_counts[i];
+    sp.sm_count[i] = prev.sm_counts[i];
+    sp.prior_count[i] = prev.prior_counts[i];
+  }
+  // mark_active: all inactive, ids >= nspix get the default prior; present -> active+prop
+  for (int k = 0; k < nbuf; k++) {
+    sp.valid[k] = 0; sp.prop[k] = 0;
+    if (k >= nspix_prev) {
+      sp.prior_sigma_shape[3 * k] = 1.0 / cfg.sp_size;
+      sp.prior_sigma_shape[3 * k + 1] = 0;
+      sp.prior_sigma_shape[3 * k + 2] = 1.0 / cfg.sp_size;
+    }
+  }
+  for (int v : f.seg) if (v >= 0 && v < nbuf) { sp.valid[v] = 1; sp.prop[v] = 1; }
+  f.max_spix = nspix_prev - 1;
+  bass_loop(f, niters, shifted.data(), true, &prev, nspix_prev, -1, 0);
+  find_border_end(f.seg.data(), f.border.data(), H, W);
+  int n = compactify(f.seg, nspix_prev, &f.sp);
+  if (out) read_params(f.sp, n, *out);
+  f.log.nspix = n;
+  return n;
+}
+
+int ladder_niters(const std::vector<int>& shifted, int npix) {
+  int ninvalid = 0;
+  for (int v : shifted) if (v == -1) ninvalid++;
+  float iperc = ninvalid / (1.0 * npix);
+  if (iperc > 0.20) return 12;
+  if (iperc < 0.01) return 4;
+  return 8;
+}
+
+void params_to_c(const Params& p, stspix_params* o) {
+  if (!o) return;
+  int n = std::min(p.n, o->capacity);
+  auto cp = [&](auto* dst, const auto& src, int per) {
+    if (dst) std::copy(src.begin(), src.begin() + (size_t)per * n, dst);
+  };
+  cp(o->mu_app, p.mu_app, 3); cp(o->prior_mu_app, p.prior_mu_app, 3);
+  cp(o->mu_shape, p.mu_shape, 2); cp(o->sigma_shape, p.sigma_shape, 3);
+  cp(o->logdet_sigma_shape, p.logdet, 1); cp(o->prior_mu_shape, p.prior_mu_shape, 2);
+  cp(o->prior_sigma_shape, p.prior_sigma_shape, 3);
+  cp(o->sample_sigma_shape, p.sample_sigma_shape, 3);
+  cp(o->counts, p.counts, 1); cp(o->sm_counts, p.sm_counts, 1);
+  cp(o->prior_counts, p.prior_counts, 1); cp(o->ids, p.ids, 1);
+  cp(o->invalid_counts, p.invalid_counts, 1);
+}
+
+void params_from_c(const stspix_params* o, int n, Params& p) {
+  p.resize(n);
+  auto cp = [&](const auto* src, auto& dst, int per) {
+    if (src) std::copy(src, src + (size_t)per * n, dst.begin());
+  };
+  cp(o->mu_app, p.mu_app, 3); cp(o->prior_mu_app, p.prior_mu_app, 3);
+  cp(o->mu_shape, p.mu_shape, 2); cp(o->sigma_shape, p.sigma_shape, 3);
+  cp(o->logdet_sigma_shape, p.logdet, 1); cp(o->prior_mu_shape, p.prior_mu_shape, 2);
+  cp(o->prior_sigma_shape, p.prior_sigma_shape, 3);
+  cp(o->sample_sigma_shape, p.sample_sigma_shape, 3);
+  cp(o->counts, p.counts, 1); cp(o->sm_counts, p.sm_counts, 1);
+  cp(o->prior_counts, p.prior_counts, 1); cp(o->ids, p.ids, 1);
+  cp(o->invalid_counts, p.invalid_counts, 1);
+}
+
+stspix_frame_log g_last_log{};
+
+}  // namespace
+
+// =========================================================================
+// C ABI of the oracle (host pointers throughout).
+extern "C" {
+
+void oracle_default_config(stspix_config* c) {
+  c->niters = 15; c->niters_seg = 4; c->sp_size = 15; c->sm_start = 0; c->sm_period = 4;
+  c->prop_niters = 0;
+  c->sigma2_app = 0.009f * 0.009f; c->potts = 0.5f; c->alpha_hastings = (float)log(0.5);
+  c->split_alpha = 0.f; c->merge_alpha = 0.f; c->sigma2_size = 0.f;
+  c->thresh_relabel = 1e-5f; c->thresh_new = 1e-2f;
+}
+
+int oracle_hex_count(int H, int W, int sp_size) {
+  double hh, w; int nx, ny;
+  hex_geometry(sp_size, W, H, &hh, &w, &nx, &ny);
+  return nx * ny;
+}
+
+int oracle_init_seg(int32_t* labels, int H, int W, int sp_size) {
+  return init_seg(labels, sp_size, W, H);
+}
+
+void oracle_find_border(const int32_t* labels, uint8_t* border, int H, int W, int mode) {
+  if (mode == 0) find_border(labels, border, H, W);
+  else find_border_end(labels, border, H, W);
+}
+
+int oracle_run_bass(const float* img, int H, int W, const stspix_config* cfg,
+                    int32_t* labels_out, stspix_params* params_out, int* nspix_out) {
+  Frame f;
+  Params p;
+  int n = run_bass(f, img, H, W, *cfg, &p, -1, 0);
+  std::copy(f.seg.begin(), f.seg.end(), labels_out);
+  params_to_c(p, params_out);
+  if (nspix_out) *nspix_out = n;
+  g_last_log = f.log;
+  return f.status;
+}
+
+int oracle_bass_partial(const float* img, int H, int W, const stspix_config* cfg, int iters,
+                        int extra_update, int32_t* labels_out, stspix_state_dump* d,
+                        int* nbuf_out, int* max_spix_out) {
+  Frame f;
+  run_bass(f, img, H, W, *cfg, nullptr, iters, extra_update);
+  std::copy(f.seg.begin(), f.seg.end(), labels_out);
+  const Sp& sp = f.sp;
+  int n = d ? std::min(sp.nbuf, d->capacity) : 0;
+  if (d) {
+    if (d->count) std::copy(sp.count.begin(), sp.count.begin() + n, d->count);
+    if (d->valid) std::copy(sp.valid.begin(), sp.valid.begin() + n, d->valid);
+    if (d->prior_count) std::copy(sp.prior_count.begin(), sp.prior_count.begin() + n, d->prior_count);
+    if (d->mu_app) std::copy(sp.mu_app.begin(), sp.mu_app.begin() + 3 * n, d->mu_app);
+    if (d->mu_shape) std::copy(sp.mu_shape.begin(), sp.mu_shape.begin() + 2 * n, d->mu_shape);
+    if (d->sigma_shape) std::copy(sp.sigma_shape.begin(), sp.sigma_shape.begin() + 3 * n, d->sigma_shape);
+    if (d->logdet) std::copy(sp.logdet.begin(), sp.logdet.begin() + n, d->logdet);
+    if (d->sums) std::copy(sp.acc.begin(), sp.acc.begin() + 8 * (size_t)n, d->sums);
+  }
+  if (nbuf_out) *nbuf_out = sp.nbuf;
+  if (max_spix_out) *max_spix_out = f.max_spix;
+  return f.status;
+}
+
+int oracle_shift_and_fill(const int32_t* labels_prev, stspix_params* pprev, int n_prev,
+                          const float* flow, int H, int W, int32_t* filled_out,
+                          int32_t* shifted_out) {
+  Params p;
+  params_from_c(pprev, n_prev, p);
+  std::vector<int> prev(labels_prev, labels_prev + (size_t)H * W), filled, shifted;
+  int it = 0;
+  int st = shift_and_fill(prev, p, flow, H, W, filled, shifted, &it);
+  std::copy(filled.begin(), filled.end(), filled_out);
+  std::copy(shifted.begin(), shifted.end(), shifted_out);
+  params_to_c(p, pprev);
+  return st;
+}
+
+int oracle_run_prop(const float* img, int H, int W, const stspix_config* cfg, int niters,
+                    const int32_t* filled, const int32_t* shifted,
+                    const stspix_params* pprev, int n_prev, int32_t* labels_out,
+                    stspix_params* params_out, int* nspix_out) {
+  Params prev, out;
+  params_from_c(pprev, n_prev, prev);
+  std::vector<int> fl(filled, filled + (size_t)H * W), sh(shifted, shifted + (size_t)H * W);
+  Frame f;
+  int n = run_prop(f, img, H, W, *cfg, niters, fl, sh, prev, &out);
+  std::copy(f.seg.begin(), f.seg.end(), labels_out);
+  params_to_c(out, params_out);
+  if (nspix_out) *nspix_out = n;
+  g_last_log = f.log;
+  return f.status;
+}
+
+// pyapi.cu:46-195 main_loop (bist_forward).
+int oracle_bist_forward(const float* vid, const float* flows, int T, int H, int W,
+                        const stspix_config* cfg, int video_mode, int32_t* spix_out,
+                        int* niters_used) {
+  const int npix = H * W;
+  std::vector<int> prev;
+  Params pprev;
+  int status = STSPIX_OK;
+  for (int fi = 0; fi < T; fi++) {
+    const float* img = vid + (size_t)fi * npix * 3;
+    Frame f;
+    Params out;
+    if (fi == 0 || !video_mode) {
+      run_bass(f, img, H, W, *cfg, &out, -1, 0);
+      if (niters_used) niters_used[fi] = cfg->niters;
+    } else {
+      const float* flow = flows + (size_t)(fi - 1) * npix * 2;
+      std::vector<int> filled, shifted;
+      int st = shift_and_fill(prev, pprev, flow, H, W, filled, shifted, &f.log.fill_iters);
+      if (st != STSPIX_OK) status = st;
+      int niters = cfg->prop_niters > 0 ? cfg->prop_niters : ladder_niters(shifted, npix);
+      if (niters_used) niters_used[fi] = niters;
+      run_prop(f, img, H, W, *cfg, niters, filled, shifted, pprev, &out);
+    }
+    if (f.status != STSPIX_OK) status = f.status;
+    std::copy(f.seg.begin(), f.seg.end(), spix_out + (size_t)fi * npix);
+    prev = f.seg;
+    pprev = out;
+    g_last_log = f.log;
+  }
+  return status;
+}
+
+// pyapi.cu:221-303 get_marked_video.
+void oracle_get_marked_video(const float* vid, const int32_t* spix, const float* color,
+                             int T, int H, int W, float* out) {
+  const int npix = H * W;
+  std::vector<uint8_t> b(npix);
+  for (int fi = 0; fi < T; fi++) {
+    find_border_end(spix + (size_t)fi * npix, b.data(), H, W);
+    for (int t = 0; t < npix; t++) {
+      const float* s = vid + ((size_t)fi * npix + t) * 3;
+      float* o = out + ((size_t)fi * npix + t) * 3;
+      for (int c = 0; c < 3; c++)
+        o[c] = b[t] ? color[c] : (float)std::max(std::min((double)s[c], 1.), 0.0);
+    }
+  }
+}
+
+// Stage-level helpers used by the tests.
+int oracle_fill_missing(int32_t* seg, const double* centers, int ncenters, int H, int W,
+                        int break_iter, int* iters) {
+  std::vector<int> s(seg, seg + (size_t)H * W);
+  std::vector<double> c(centers, centers + 2 * (size_t)ncenters);
+  int it = 0;
+  int st = fill_missing(s, c, H, W, break_iter, &it);
+  std::copy(s.begin(), s.end(), seg);
+  if (iters) *iters = it;
+  return st;
+}
+
+void oracle_invalidate_disconnected(int32_t* seg, int H, int W, int nspix) {
+  std::vector<int> s(seg, seg + (size_t)H * W);
+  invalidate_disconnected(s, H, W, nspix);
+  std::copy(s.begin(), s.end(), seg);
+}
+
+void oracle_get_frame_log(stspix_frame_log* out) { *out = g_last_log; }
+
+}  // extern "C"

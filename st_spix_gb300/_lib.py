@@ -1,0 +1,160 @@
+"""ctypes binding of libstspix_gb300.so (the C ABI in include/st_spix_gb300.h).
+
+The library is the only compute path: if it is missing or fails to load this module
+raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+
+class Config(C.Structure):
+    """stspix_config."""
+    _fields_ = [("niters", C.c_int), ("niters_seg", C.c_int), ("sp_size", C.c_int),
+                ("sm_start", C.c_int), ("sm_period", C.c_int), ("prop_niters", C.c_int),
+                ("sigma2_app", C.c_float), ("potts", C.c_float),
+                ("alpha_hastings", C.c_float), ("split_alpha", C.c_float),
+                ("merge_alpha", C.c_float), ("sigma2_size", C.c_float),
+                ("thresh_relabel", C.c_float), ("thresh_new", C.c_float)]
+
+
+class ParamsC(C.Structure):
+    """stspix_params (device pointers)."""
+    _fields_ = [("mu_app", C.c_void_p), ("prior_mu_app", C.c_void_p),
+                ("mu_shape", C.c_void_p), ("sigma_shape", C.c_void_p),
+                ("logdet_sigma_shape", C.c_void_p), ("prior_mu_shape", C.c_void_p),
+                ("prior_sigma_shape", C.c_void_p), ("sample_sigma_shape", C.c_void_p),
+                ("counts", C.c_void_p), ("sm_counts", C.c_void_p),
+                ("prior_counts", C.c_void_p), ("ids", C.c_void_p),
+                ("invalid_counts", C.c_void_p), ("capacity", C.c_int)]
+
+
+class DumpC(C.Structure):
+    """stspix_state_dump (device pointers)."""
+    _fields_ = [("count", C.c_void_p), ("valid", C.c_void_p), ("prior_count", C.c_void_p),
+                ("mu_app", C.c_void_p), ("mu_shape", C.c_void_p),
+                ("sigma_shape", C.c_void_p), ("logdet", C.c_void_p), ("sums", C.c_void_p),
+                ("capacity", C.c_int)]
+
+
+class FrameLog(C.Structure):
+    """stspix_frame_log."""
+    _fields_ = [("nsplits", C.c_int), ("nmerges", C.c_int), ("nrevived", C.c_int),
+                ("nminted", C.c_int), ("near_ties", C.c_int), ("fill_iters", C.c_int),
+                ("niters", C.c_int), ("nspix", C.c_int)]
+
+
+# Every symbol declared in include/st_spix_gb300.h.
+EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_last_error",
+           "stspix_version", "stspix_kernel_launches", "stspix_get_frame_log",
+           "stspix_bist_forward", "stspix_get_marked_video", "stspix_run_bass",
+           "stspix_shift_and_fill", "stspix_run_prop", "stspix_init_seg",
+           "stspix_find_border", "stspix_bass_partial"]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first when needed and allowed) the engine library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if not os.path.exists(path) or not _build.up_to_date():
+            if not build_if_missing:
+                raise RuntimeError(f"st_spix_gb300 CUDA library not built: {path}")
+            _build.build()
+        lib = C.CDLL(path)
+        P, I = C.c_void_p, C.c_int
+        sig = {
+            "stspix_default_config": (None, [C.POINTER(Config)]),
+            "stspix_create": (I, [C.POINTER(C.c_void_p), I]),
+            "stspix_destroy": (I, [P]),
+            "stspix_last_error": (C.c_char_p, [P]),
+            "stspix_version": (I, []),
+            "stspix_kernel_launches": (C.c_longlong, [P]),
+            "stspix_get_frame_log": (I, [P, C.POINTER(FrameLog)]),
+            "stspix_bist_forward": (I, [P, P, P, P, I, I, I, I, C.POINTER(Config), I, I, P]),
+            "stspix_get_marked_video": (I, [P, P, P, P, P, I, I, I, I, P]),
+            "stspix_run_bass": (I, [P, P, P, I, I, C.POINTER(Config), P, C.POINTER(ParamsC),
+                                    C.POINTER(I)]),
+            "stspix_shift_and_fill": (I, [P, P, P, C.POINTER(ParamsC), I, P, I, I, P, P]),
+            "stspix_run_prop": (I, [P, P, P, I, I, C.POINTER(Config), I, P, P,
+                                    C.POINTER(ParamsC), I, P, C.POINTER(ParamsC),
+                                    C.POINTER(I)]),
+            "stspix_init_seg": (I, [P, P, P, I, I, I, C.POINTER(I)]),
+            "stspix_find_border": (I, [P, P, P, P, I, I, I]),
+            "stspix_bass_partial": (I, [P, P, P, I, I, C.POINTER(Config), I, I, P,
+                                        C.POINTER(DumpC), C.POINTER(I), C.POINTER(I)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return _lib
+
+
+class StspixError(RuntimeError):
+    """A non-zero status returned by the engine."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"st_spix_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class Context:
+    """One engine context (device workspace) bound to a CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.stspix_create(C.byref(h), int(device))
+        if st != 0:
+            raise StspixError(st, f"stspix_create(device={device}) failed")
+        self.handle = h
+        self.device = device
+
+    def check(self, st: int):
+        if st != 0:
+            msg = self.lib.stspix_last_error(self.handle)
+            raise StspixError(st, msg.decode() if msg else "")
+
+    def launches(self) -> int:
+        return int(self.lib.stspix_kernel_launches(self.handle))
+
+    def frame_log(self) -> FrameLog:
+        lg = FrameLog()
+        self.check(self.lib.stspix_get_frame_log(self.handle, C.byref(lg)))
+        return lg
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.stspix_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_config(**kw) -> Config:
+    c = Config()
+    load().stspix_default_config(C.byref(c))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c

@@ -1,0 +1,131 @@
+// Internal header of the GB300 streaming-BASS engine (device layout, kernels,
+// host workspace).  Public C ABI: include/st_spix_gb300.h.
+//
+// Deterministic rules shared with the CPU oracle (oracle/bass_oracle.cpp):
+//   R1 int64 fixed-point colour sums (2^-28; squares 2^-20; flow 2^-24), exact
+//      integer position sums.
+//   R2 split ids in ascending order of the split superpixel (exclusive scan).
+//   R3 merge claims: smallest claimant id wins (atomicMin).
+//   R4 forward-warp collisions: smallest packed (size, id) wins (64-bit atomicMin).
+//   R5 relabel: smallest packed (distance bits, candidate) wins; minted ids by scan;
+//      a revived id copies its count from the largest reviving superpixel.
+//   R6 connected components: per label keep the largest region, ties to the
+//      smallest root pixel index.
+//   R7 reference reads of uninitialised memory are zero.
+//   R8 IEEE FP32/FP64 with no FMA contraction (-fmad=false); Hastings in FP64.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/st_spix_gb300.h"
+
+namespace stspix {
+
+constexpr int kFxAppShift = 28;
+constexpr int kFxSqShift = 20;
+constexpr int kFxFlowShift = 24;
+constexpr int kMaxCoopRounds = 1 << 14;   // cap of the relaxation loops
+constexpr int kFillBreakIter = 1000;      // fill_missing.cu: break_iter
+constexpr long long kBarrierSpinLimit = 1LL << 24;
+
+// Packed record read by the boundary sweep: exactly the fields calc_joint reads
+// (update_seg.cu:194-259), already converted to the types it uses.
+struct __align__(16) SweepRec {
+  float mu_r, mu_g, mu_b, logdet;  // mean colour, (float) log det Sigma
+  double mu_x, mu_y;               // mean position (double: d0 is truncated from it)
+  float isx, isy, isz;             // (float) inverse shape covariance
+  int count;                       // pixel count
+};
+
+// Per-superpixel working state, structure of arrays, `cap` entries each.
+struct SpDev {
+  int cap;
+  int* count;
+  uint8_t* valid;
+  uint8_t* prop;
+  float* prior_count;
+  float* icount;
+  int* sm_count;
+  float* mu_app;           // [3*cap]
+  double* mu_shape;        // [2*cap]
+  double* sigma_shape;     // [3*cap]
+  double* logdet;          // [cap]
+  float* prior_mu_app;     // [3*cap]
+  double* prior_mu_shape;  // [2*cap]
+  double* prior_sigma_shape;   // [3*cap]
+  double* prior_icov;          // [3*cap]
+  double* sample_sigma_shape;  // [3*cap]
+  long long* acc;          // [8*cap]: r,g,b (2^-28), x, y, xx, xy, yy
+  SweepRec* rec;           // [cap]
+};
+
+// Split / merge scratch, cap+2 entries.
+struct SmDev {
+  int* count;
+  long long* s;      // [3*(cap+2)]
+  long long* sq;     // [3*(cap+2)]
+  int* ninvalid;
+  int* pair;         // merge candidate (sm_pairs[2k+1])
+  int* claim;        // merge claim (sm_pairs[2f])
+  int* target;
+  int* newid;
+  uint8_t* flag;     // bit0 accept/want, bit1 merge, bit2 remove, bit3 select, bit4 has_single
+  double* msingle;
+};
+
+// Frame-level device scalars.
+struct Scalars {
+  int max_spix;
+  int nspix;          // live superpixels after compaction / init
+  int nbuf_logical;   // reference's nspix_buffer (30 x hex count, or 10 x n_prev)
+  int status;
+  int nsplits, nmerges, nrevived, nminted, near_ties;
+  int fill_iters;
+  int ninvalid;       // -1 pixels after the shift
+  int tmp0, tmp1, tmp2;
+  unsigned int bar_count, bar_gen;   // grid barrier
+};
+
+// ---------------------------------------------------------------------------
+// Device helpers shared by the kernels.
+__device__ __forceinline__ long long fx_q(float v, int shift) {
+  return __float2ll_rn(ldexpf(v, shift));
+}
+__device__ __forceinline__ double fx_unq(long long q, int shift) {
+  return ldexp((double)q, -shift);
+}
+
+// Bounded grid barrier for cooperative launches: every block calls it; returns
+// false (and sets status) when the wait exceeded the spin limit.
+__device__ __forceinline__ bool grid_barrier(Scalars* sc) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &sc->bar_gen;
+    unsigned int my = *gen;
+    __threadfence();
+    unsigned int arrived = atomicAdd(&sc->bar_count, 1u);
+    ok = 1;
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&sc->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&sc->bar_gen, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == my) {
+        if (++spins > kBarrierSpinLimit) {
+          atomicExch(&sc->status, STSPIX_ERR_BARRIER);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)&sc->status == STSPIX_ERR_BARRIER) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+}  // namespace stspix

@@ -1,0 +1,514 @@
+// GB300 kernels of the per-frame BASS path: hex initialisation, compaction,
+// sufficient statistics + posterior, boundary sweep, parameter read-out.
+// Reference files cited per kernel (gauenk/st_spix, st_spix/csrc/bist/).
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "engine.h"
+#include "kernels.h"
+
+namespace stspix {
+
+// ---------------------------------------------------------------------------
+// Hex initialisation (init_seg.cu:48-75).  The reference tests every centre per
+// pixel and keeps the LAST centre at the minimum distance; the nearest centre of
+// this pointy-top hex lattice lies within one hexagon radius, so a 5x5 window of
+// lattice sites around the pixel, scanned in ascending id order with the same
+// `<=` rule and the same double arithmetic, gives the identical label.
+__global__ void k_init_hex(int* __restrict__ seg, int H, int W, double Hh, double w, int nx,
+                           int ny) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= H * W) return;
+  int x = idx % W, y = idx / W;
+  int r0 = (int)floor(y / (1.5 * Hh));
+  int c0 = (int)floor(x / w);
+  double D2 = 1.7976931348623157e308;
+  int best = 0;
+  for (int r = r0 - 2; r <= r0 + 2; r++) {
+    if (r < 0 || r >= ny) continue;
+    for (int c = c0 - 2; c <= c0 + 2; c++) {
+      if (c < 0 || c >= nx) continue;
+      double xx = double(c) * w;
+      double yy = double(r) * 1.5 * Hh;
+      if (r % 2 == 0) xx = xx + 0.5 * w;
+      double dx = (x - xx);
+      double dy = (y - yy);
+      double d2 = dx * dx + dy * dy;
+      if (d2 <= D2) { D2 = d2; best = r * nx + c; }
+    }
+  }
+  seg[idx] = best;
+}
+
+// ---------------------------------------------------------------------------
+// Compaction (compact_spix.cu:41-122, 196-290): flags of live ids in [lo, hi],
+// exclusive scan, remap.
+__global__ void k_mark_present(const int* __restrict__ seg, int npix, int lo,
+                               const int* __restrict__ hi_ptr, int hi_static,
+                               uint8_t* __restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  int hi = hi_ptr ? *hi_ptr : hi_static;
+  int v = seg[i];
+  if (v >= lo && v <= hi) flags[v - lo] = 1;
+}
+
+// Single-block exclusive scan of n byte flags (n up to a few 10^5).
+__global__ void k_scan_flags(const uint8_t* __restrict__ flags, const int* __restrict__ n_ptr,
+                             int n_static, int* __restrict__ excl, int* __restrict__ total) {
+  __shared__ int part[1024];
+  const int T = blockDim.x;
+  int n = n_ptr ? *n_ptr : n_static;
+  if (n < 0) n = 0;
+  int chunk = (n + T - 1) / T;
+  int b = threadIdx.x * chunk, e = min(n, b + chunk);
+  int s = 0;
+  for (int i = b; i < e; i++) s += flags[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 1; off < T; off <<= 1) {
+    int v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (int i = b; i < e; i++) { excl[i] = run; run += flags[i]; }
+  if (threadIdx.x == T - 1) *total = part[T - 1];
+}
+
+__global__ void k_remap(int* __restrict__ seg, int npix, int lo, const int* __restrict__ excl) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  int v = seg[i];
+  if (v >= lo) seg[i] = lo + excl[v - lo];
+}
+
+// fill_new_params_from_old (compact_spix.cu:220-265): gather moved fields.
+__global__ void k_compact_gather(SpDev sp, SpDev tmp, int lo, const int* __restrict__ hi_ptr,
+                                 const uint8_t* __restrict__ flags,
+                                 const int* __restrict__ excl) {
+  int v = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (v > *hi_ptr || v >= sp.cap) return;
+  if (!flags[v - lo]) return;
+  int j = excl[v - lo];
+  for (int c = 0; c < 3; c++) {
+    tmp.mu_app[3 * j + c] = sp.mu_app[3 * v + c];
+    tmp.prior_mu_app[3 * j + c] = sp.prior_mu_app[3 * v + c];
+    tmp.sigma_shape[3 * j + c] = sp.sigma_shape[3 * v + c];
+    tmp.prior_sigma_shape[3 * j + c] = sp.prior_sigma_shape[3 * v + c];
+    tmp.sample_sigma_shape[3 * j + c] = sp.sample_sigma_shape[3 * v + c];
+  }
+  for (int c = 0; c < 2; c++) {
+    tmp.mu_shape[2 * j + c] = sp.mu_shape[2 * v + c];
+    tmp.prior_mu_shape[2 * j + c] = sp.prior_mu_shape[2 * v + c];
+  }
+  tmp.logdet[j] = sp.logdet[v];
+  tmp.count[j] = sp.count[v];
+  tmp.prior_count[j] = sp.prior_count[v];
+  tmp.valid[j] = sp.valid[v];
+}
+
+// fill_old_params_from_new (compact_spix.cu:268-290).
+__global__ void k_compact_scatter(SpDev sp, SpDev tmp, int lo, const int* __restrict__ nnew) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *nnew) return;
+  int d = lo + j;
+  if (d >= sp.cap) return;
+  for (int c = 0; c < 3; c++) {
+    sp.mu_app[3 * d + c] = tmp.mu_app[3 * j + c];
+    sp.prior_mu_app[3 * d + c] = tmp.prior_mu_app[3 * j + c];
+    sp.sigma_shape[3 * d + c] = tmp.sigma_shape[3 * j + c];
+    sp.prior_sigma_shape[3 * d + c] = tmp.prior_sigma_shape[3 * j + c];
+    sp.sample_sigma_shape[3 * d + c] = tmp.sample_sigma_shape[3 * j + c];
+  }
+  for (int c = 0; c < 2; c++) {
+    sp.mu_shape[2 * d + c] = tmp.mu_shape[2 * j + c];
+    sp.prior_mu_shape[2 * d + c] = tmp.prior_mu_shape[2 * j + c];
+  }
+  sp.logdet[d] = tmp.logdet[j];
+  sp.count[d] = tmp.count[j];
+  sp.prior_count[d] = tmp.prior_count[j];
+  sp.valid[d] = tmp.valid[j];
+}
+
+// ---------------------------------------------------------------------------
+// init_sp_params_kernel + mark_active_contiguous (init_sparams.cu:45-166,
+// 195-286) for a BASS frame; *nspix live ids, count = npix / nspix.
+__global__ void k_init_bass_params(SpDev sp, const int* __restrict__ nspix_ptr, int npix,
+                                   int sp_size) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap) return;
+  int nspix = *nspix_ptr;
+  int count = (int)(npix / (1. * nspix));
+  sp.prior_sigma_shape[3 * k] = 1.0 / sp_size;
+  sp.prior_sigma_shape[3 * k + 1] = 0.;
+  sp.prior_sigma_shape[3 * k + 2] = 1.0 / sp_size;
+  sp.prior_icov[3 * k] = 1; sp.prior_icov[3 * k + 1] = 0; sp.prior_icov[3 * k + 2] = 1;
+  sp.prop[k] = 0;
+  sp.icount[k] = 0.f;
+  sp.sm_count[k] = 0;
+  for (int c = 0; c < 3; c++) {
+    sp.mu_app[3 * k + c] = 0.f; sp.prior_mu_app[3 * k + c] = 0.f;
+    sp.sigma_shape[3 * k + c] = 0.0; sp.sample_sigma_shape[3 * k + c] = 0.0;
+  }
+  for (int c = 0; c < 2; c++) { sp.mu_shape[2 * k + c] = 0.0; sp.prior_mu_shape[2 * k + c] = 0.0; }
+  sp.logdet[k] = 0.0;
+  sp.count[k] = 0;
+  if (k < nspix) { sp.valid[k] = 1; sp.prior_count[k] = (float)count; }
+  else { sp.valid[k] = 0; sp.prior_count[k] = 0.f; }
+}
+
+// prior_mu_app := initial mean (calc_summ_stats, update_params.cu:142-203).
+__global__ void k_init_prior_mu(SpDev sp, const int* __restrict__ nspix_ptr) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *nspix_ptr || k >= sp.cap) return;
+  int n = sp.count[k];
+  double c = n;
+  for (int ch = 0; ch < 3; ch++)
+    sp.prior_mu_app[3 * k + ch] =
+        n > 0 ? (float)(fx_unq(sp.acc[8 * k + ch], kFxAppShift) / c) : 0.f;
+}
+
+// ---------------------------------------------------------------------------
+// Sufficient statistics (sum_by_label, update_params.cu:89-130), R1.
+// Each thread owns a run of kRun pixels of one row, accumulates in registers while
+// the label stays the same and flushes one set of 64-bit atomics per label run;
+// position sums of a run are closed-form.
+constexpr int kRun = 16;
+
+__device__ __forceinline__ void flush_run(SpDev& sp, int k, int y, int x0, int x1,
+                                          long long sr, long long sg, long long sb) {
+  long long n = x1 - x0 + 1;
+  long long sx = (long long)(x0 + x1) * n / 2;
+  long long a = x0 - 1, b = x1;
+  long long sxx = b * (b + 1) * (2 * b + 1) / 6 - (a >= 0 ? a * (a + 1) * (2 * a + 1) / 6 : 0);
+  unsigned long long* acc = (unsigned long long*)(sp.acc + 8 * (size_t)k);
+  atomicAdd(&sp.count[k], (int)n);
+  atomicAdd(acc + 0, (unsigned long long)sr);
+  atomicAdd(acc + 1, (unsigned long long)sg);
+  atomicAdd(acc + 2, (unsigned long long)sb);
+  atomicAdd(acc + 3, (unsigned long long)sx);
+  atomicAdd(acc + 4, (unsigned long long)(n * y));
+  atomicAdd(acc + 5, (unsigned long long)sxx);
+  atomicAdd(acc + 6, (unsigned long long)(sx * y));
+  atomicAdd(acc + 7, (unsigned long long)(n * y * (long long)y));
+}
+
+__global__ void k_accumulate(const float* __restrict__ img, const int* __restrict__ seg, int H,
+                             int W, SpDev sp) {
+  const int cpr = (W + kRun - 1) / kRun;
+  int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= H * cpr) return;
+  int y = tid / cpr, xs = (tid % cpr) * kRun, xe = min(W, xs + kRun);
+  const int* srow = seg + (size_t)y * W;
+  const float* irow = img + (size_t)y * W * 3;
+  int cur = -1, x0 = xs;
+  long long sr = 0, sg = 0, sb = 0;
+  for (int x = xs; x < xe; x++) {
+    int k = srow[x];
+    if (k != cur) {
+      if (cur >= 0 && cur < sp.cap) flush_run(sp, cur, y, x0, x - 1, sr, sg, sb);
+      cur = k; x0 = x; sr = sg = sb = 0;
+    }
+    if (k >= 0) {
+      sr += fx_q(irow[3 * x], kFxAppShift);
+      sg += fx_q(irow[3 * x + 1], kFxAppShift);
+      sb += fx_q(irow[3 * x + 2], kFxAppShift);
+    }
+  }
+  if (cur >= 0 && cur < sp.cap) flush_run(sp, cur, y, x0, xe - 1, sr, sg, sb);
+}
+
+// ---------------------------------------------------------------------------
+// Posterior (calc_simple_update, update_params.cu:220-381, with
+// _add_sigma_smoothing :206-217) + clear_fields semantics for dead ids.
+__device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in_z, int count,
+                                             float pc, int sp_size, double* ox, double* oy,
+                                             double* oz) {
+  int nf = 50;
+  double total_count = 1. * (count + pc * nf);
+  *ox = (pc * sp_size + count * in_x) / (total_count + 3.0);
+  *oy = (count * in_y) / (total_count + 3.0);
+  *oz = (pc * sp_size + count * in_z) / (total_count + 3.0);
+}
+
+__global__ void k_posterior(SpDev sp, int sp_size, Scalars* sc) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap) return;
+  int count_int = sp.count[k];
+  bool live = sp.valid[k] && count_int > 0;
+  if (sp.valid[k] && count_int <= 0) sp.valid[k] = 0;
+  if (!live) {
+    for (int c = 0; c < 3; c++) { sp.mu_app[3 * k + c] = 0.f; sp.sigma_shape[3 * k + c] = 0.0; }
+    sp.mu_shape[2 * k] = 0.0; sp.mu_shape[2 * k + 1] = 0.0;
+    return;
+  }
+  float pc = sp.prior_count[k];
+  double count = count_int * 1.0;
+  double total_count = (double)count_int + pc * 50;
+  double px, py, pz;
+  if (sp.prop[k]) {
+    smooth_prior(sp.sample_sigma_shape[3 * k], sp.sample_sigma_shape[3 * k + 1],
+                 sp.sample_sigma_shape[3 * k + 2], (int)pc, pc, sp_size, &px, &py, &pz);
+  } else {
+    px = sp.prior_icov[3 * k]; py = sp.prior_icov[3 * k + 1]; pz = sp.prior_icov[3 * k + 2];
+  }
+  double pr_det = px * pz - py * py;
+  if (!(pr_det > 0)) atomicExch(&sc->status, STSPIX_ERR_DEGENERATE);
+  pr_det = sqrt(pr_det);
+  double psx = pc / pr_det * px, psy = pc / pr_det * py, psz = pc / pr_det * pz;
+  const long long* a = sp.acc + 8 * (size_t)k;
+  float mr = (float)(fx_unq(a[0], kFxAppShift) / count);
+  float mg = (float)(fx_unq(a[1], kFxAppShift) / count);
+  float mb = (float)(fx_unq(a[2], kFxAppShift) / count);
+  sp.mu_app[3 * k] = mr; sp.mu_app[3 * k + 1] = mg; sp.mu_app[3 * k + 2] = mb;
+  double mx = a[3] / count, my = a[4] / count;
+  sp.mu_shape[2 * k] = mx; sp.mu_shape[2 * k + 1] = my;
+  double sx = a[5] - count * mx * mx;
+  double sy = a[6] - count * mx * my;
+  double sz = a[7] - count * my * my;
+  sx = (pc * psx + sx) / (total_count + 3.0);
+  sy = (pc * psy + sy) / (total_count + 3.0);
+  sz = (pc * psz + sz) / (total_count + 3.0);
+  double det = sx * sz - sy * sy;
+  if (det <= 0) {
+    sx = sx + 0.00001;
+    sz = sz + 0.00001;
+    det = sx * sz - sy * sy;
+    if (det <= 0) det = 0.00001;
+  }
+  double ix = sz / det, iy = -sy / det, iz = sx / det;
+  double ld = log(det);
+  sp.sigma_shape[3 * k] = ix; sp.sigma_shape[3 * k + 1] = iy; sp.sigma_shape[3 * k + 2] = iz;
+  sp.logdet[k] = ld;
+  SweepRec r;
+  r.mu_r = mr; r.mu_g = mg; r.mu_b = mb; r.logdet = (float)ld;
+  r.mu_x = mx; r.mu_y = my;
+  r.isx = (float)ix; r.isy = (float)iy; r.isz = (float)iz;
+  r.count = count_int;
+  sp.rec[k] = r;
+}
+
+// store_sample_sigma_shape_k (update_params.cu:397-438).
+__global__ void k_store_sample(SpDev sp) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap || !sp.valid[k]) return;
+  const long long* a = sp.acc + 8 * (size_t)k;
+  double count = sp.count[k] * 1.0;
+  double mx = a[3] / count, my = a[4] / count;
+  sp.mu_shape[2 * k] = mx; sp.mu_shape[2 * k + 1] = my;
+  double sx, sy, sz;
+  if (count > 0) {
+    sx = a[5] / count - mx * mx;
+    sy = a[6] / count - mx * my;
+    sz = a[7] / count - my * my;
+  } else {
+    sx = sp.prior_sigma_shape[3 * k]; sy = sp.prior_sigma_shape[3 * k + 1];
+    sz = sp.prior_sigma_shape[3 * k + 2];
+  }
+  sp.sample_sigma_shape[3 * k] = sx;
+  sp.sample_sigma_shape[3 * k + 1] = sy;
+  sp.sample_sigma_shape[3 * k + 2] = sz;
+}
+
+// ---------------------------------------------------------------------------
+// Border masks (seg_utils.cu:164-195 and 218-257).
+__global__ void k_find_border(const int* __restrict__ seg, uint8_t* __restrict__ border, int H,
+                              int W) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= H * W) return;
+  int x = idx % W, y = idx / W;
+  if (y < 1 || x < 1 || y >= H - 1 || x >= W - 1) { border[idx] = 1; return; }
+  int C = seg[idx];
+  border[idx] = (C != seg[idx - W] || C != seg[idx + W] || C != seg[idx + 1] ||
+                 C != seg[idx - 1]) ? 1 : 0;
+}
+
+__global__ void k_find_border_end(const int* __restrict__ seg, uint8_t* __restrict__ border,
+                                  int H, int W, int nframes) {
+  long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long npix = (long long)H * W;
+  if (gi >= npix * nframes) return;
+  int idx = (int)(gi % npix);
+  const int* s = seg + (gi - idx);
+  int x = idx % W, y = idx / W;
+  int C = s[idx];
+  int N = -1, S = -1, E = -1, Wl = -1;
+  if (y > 0) N = s[idx - W];
+  if (x > 0) Wl = s[idx - 1];
+  if (y < H - 1) S = s[idx + W];
+  if (x < W - 1) E = s[idx + 1];
+  uint8_t b = 0;
+  if ((N >= 0 && C != N) || (S >= 0 && C != S) || (E >= 0 && C != E) || (Wl >= 0 && C != Wl)) {
+    if (N >= 0 && C > N) b = 1;
+    if (S >= 0 && C > S) b = 1;
+    if (E >= 0 && C > E) b = 1;
+    if (Wl >= 0 && C > Wl) b = 1;
+  }
+  border[gi] = b;
+}
+
+// GetImageOverlaid (pyapi.cu:221-246).
+__global__ void k_overlay(float* __restrict__ out, const float* __restrict__ img,
+                          const float* __restrict__ color, const uint8_t* __restrict__ border,
+                          long long n) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  if (border[t]) {
+    out[3 * t] = color[0]; out[3 * t + 1] = color[1]; out[3 * t + 2] = color[2];
+  } else {
+    for (int c = 0; c < 3; c++)
+      out[3 * t + c] = (float)fmax(fmin((double)img[3 * t + c], 1.), 0.0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Boundary sweep (update_seg_subset, update_seg.cu:30-190; calc_joint :194-259;
+// simple-point table seg_utils.h:15-79).
+// Simple-point table (data, identical to the reference's bass_lut): bit i of the
+// index is set when 3x3 neighbour i (NW,N,NE,W,E,SW,S,SE) carries the candidate
+// label or lies outside the image.
+__constant__ unsigned char c_simple_lut[256] = {
+    0, 0, 1, 1, 0, 0, 1, 1, 1, 1, 0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 0, 0,
+    0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0,
+    1, 1, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 1, 0, 1, 1, 0, 0, 0, 0,
+    0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+    1, 0, 0, 0, 1, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 1,
+    0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 1, 1, 0, 0, 1, 1, 0, 0};
+
+__device__ __forceinline__ bool simple_point(const int nb[8], int label, int* diff) {
+  int num = 0, d = 0;
+#pragma unroll
+  for (int i = 7; i >= 0; i--) {
+    num <<= 1;
+    bool b = (label == nb[i]) || (nb[i] == -1);
+    if (b) num++; else d++;
+  }
+  *diff = d;
+  return c_simple_lut[num] != 0;
+}
+
+__device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int y,
+                                      const SweepRec& r, int k, float s2, float neigh_neq,
+                                      float beta, float* best, int* best_label) {
+  float res = -1000;
+  const float x0 = pix[0] - r.mu_r;
+  const float x1 = pix[1] - r.mu_g;
+  const float x2 = pix[2] - r.mu_b;
+  const int d0 = (int)(x - r.mu_x);
+  const int d1 = (int)(y - r.mu_y);
+  res = res - (x0 * x0 + x1 * x1 + x2 * x2) / s2;
+  res = res - (float)(d0 * d0) * r.isx - (float)(d1 * d1) * r.isz - (float)(2 * d0 * d1) * r.isy;
+  res = res - r.logdet;
+  res = res - beta * neigh_neq;
+  res = res - (float)(100 * (r.count <= 10));
+  if (res > *best) { *best = res; *best_label = k; }
+}
+
+// One pixel of one parity class; reads labels live (other classes may already be
+// updated), border from the sweep start.
+__device__ __forceinline__ void update_pixel(const float* __restrict__ img, int* seg,
+                                             const uint8_t* __restrict__ border,
+                                             const SweepRec* __restrict__ rec, int cap, int x,
+                                             int y, int H, int W, float s2, float potts) {
+  int idx = y * W + x;
+  if (!border[idx]) return;
+  int C = seg[idx];
+  if (C < 0 || C >= cap) return;
+  int N = -1, S = -1, E = -1, Wl = -1, NE = -1, NW = -1, SE = -1, SW = -1;
+  if (x > 0) Wl = seg[idx - 1];
+  if (y > 0) N = seg[idx - W];
+  if (x < W - 1) E = seg[idx + 1];
+  if (y < H - 1) S = seg[idx + W];
+  if (y > 0 && x < W - 1) NE = seg[idx - W + 1];
+  if (y > 0 && x > 0) NW = seg[idx - W - 1];
+  if (x < W - 1 && y < H - 1) SE = seg[idx + W + 1];
+  if (x > 0 && y < H - 1) SW = seg[idx + W - 1];
+  const int nb[8] = {NW, N, NE, Wl, E, SW, S, SE};
+  int dN, dW, dS, dE;
+  bool vN = simple_point(nb, N, &dN);
+  bool vW = simple_point(nb, Wl, &dW);
+  bool vS = simple_point(nb, S, &dS);
+  bool vE = simple_point(nb, E, &dE);
+  if (!vN || !vW || !vS || !vE) return;
+  if (N >= cap || S >= cap || Wl >= cap || E >= cap) return;  // labels are < cap by construction
+  const float* pix = img + 3 * (size_t)idx;
+  float best = -9999.f;
+  int bl = C;
+  if (N >= 0) joint(pix, x, y, rec[N], N, s2, (float)dN, potts, &best, &bl);
+  if (S != N && S >= 0) joint(pix, x, y, rec[S], S, s2, (float)dS, potts, &best, &bl);
+  if (Wl != S && Wl != N && Wl >= 0) joint(pix, x, y, rec[Wl], Wl, s2, (float)dW, potts, &best, &bl);
+  if (E != Wl && E != S && E != N && E >= 0) joint(pix, x, y, rec[E], E, s2, (float)dE, potts, &best, &bl);
+  if (rec[C].count <= 2 && bl == C) {
+    if (N >= 0) bl = N;
+    else if (E >= 0) bl = E;
+    else if (S >= 0) bl = S;
+    else if (Wl >= 0) bl = Wl;
+  }
+  seg[idx] = bl;
+}
+
+__global__ void k_update_phase(const float* __restrict__ img, int* seg,
+                               const uint8_t* __restrict__ border, const SweepRec* __restrict__ rec,
+                               int cap, int H, int W, int xmod, int ymod, float s2, float potts) {
+  int hw = (W - xmod + 1) / 2;
+  int hh = (H - ymod + 1) / 2;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hw * hh) return;
+  int x = 2 * (i % hw) + xmod, y = 2 * (i / hw) + ymod;
+  update_pixel(img, seg, border, rec, cap, x, y, H, W, s2, potts);
+}
+
+// ---------------------------------------------------------------------------
+// Parameter read-out (read_params, sparams_io.cu:190-286) and prior update
+// (update_prior_kernel, sparams_io.cu:584-640) into the caller's SoA params.
+__global__ void k_read_params(SpDev sp, const int* __restrict__ n_ptr, stspix_params out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = *n_ptr;
+  if (i >= n || i >= out.capacity || i >= sp.cap) return;
+  bool upd = sp.count[i] > 0;
+  for (int c = 0; c < 3; c++) {
+    float m = sp.mu_app[3 * i + c];
+    out.mu_app[3 * i + c] = m;
+    out.prior_mu_app[3 * i + c] = upd ? m : sp.prior_mu_app[3 * i + c];
+    double s = sp.sigma_shape[3 * i + c];
+    out.sigma_shape[3 * i + c] = s;
+    out.prior_sigma_shape[3 * i + c] = upd ? s : sp.prior_sigma_shape[3 * i + c];
+    out.sample_sigma_shape[3 * i + c] = sp.sample_sigma_shape[3 * i + c];
+  }
+  for (int c = 0; c < 2; c++) {
+    double m = sp.mu_shape[2 * i + c];
+    out.mu_shape[2 * i + c] = m;
+    out.prior_mu_shape[2 * i + c] = upd ? m : sp.prior_mu_shape[2 * i + c];
+  }
+  out.logdet_sigma_shape[i] = (float)sp.logdet[i];
+  out.counts[i] = sp.count[i];
+  out.invalid_counts[i] = sp.icount[i];
+  out.sm_counts[i] = sp.sm_count[i];
+  out.prior_counts[i] = sp.prior_count[i];
+  out.ids[i] = i;
+}
+
+__global__ void k_dump_state(SpDev sp, stspix_state_dump d) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap || k >= d.capacity) return;
+  if (d.count) d.count[k] = sp.count[k];
+  if (d.valid) d.valid[k] = sp.valid[k];
+  if (d.prior_count) d.prior_count[k] = sp.prior_count[k];
+  for (int c = 0; c < 3; c++) {
+    if (d.mu_app) d.mu_app[3 * k + c] = sp.mu_app[3 * k + c];
+    if (d.sigma_shape) d.sigma_shape[3 * k + c] = sp.sigma_shape[3 * k + c];
+  }
+  for (int c = 0; c < 2; c++)
+    if (d.mu_shape) d.mu_shape[2 * k + c] = sp.mu_shape[2 * k + c];
+  if (d.logdet) d.logdet[k] = sp.logdet[k];
+  if (d.sums)
+    for (int c = 0; c < 8; c++) d.sums[8 * (size_t)k + c] = sp.acc[8 * (size_t)k + c];
+}
+
+}  // namespace stspix

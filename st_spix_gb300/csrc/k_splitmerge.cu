@@ -1,0 +1,458 @@
+// GB300 kernels of the split / merge proposals and their Hastings tests
+// (gauenk/st_spix st_spix/csrc/bist/split_merge.cu, split_merge_orig.cu,
+// split_merge_prop.cu), plus the bounded cooperative relaxation loops that replace
+// the reference's host-driven BFS (one launch + one device-to-host copy per step).
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "engine.h"
+#include "kernels.h"
+
+namespace stspix {
+
+constexpr int kTile = 32;
+constexpr int kHalo = kTile + 2;
+constexpr int kInf = 0x3fffffff;
+
+// ---------------------------------------------------------------------------
+// Split seeds (init_split, split_merge.cu:803-844) for both directions.
+__global__ void k_split_seed(SpDev sp, const int* __restrict__ seg, int H, int W, int direction,
+                             const Scalars* __restrict__ sc, int* __restrict__ d1,
+                             int* __restrict__ d2) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap || !sc->tmp0 /*split_on*/ || !sp.valid[k]) return;
+  for (int s = 0; s < 2; s++) {
+    int dir = s == 0 ? direction : -direction;
+    int x, y;
+    if (dir == 1 || dir == -1) {
+      x = int(sp.mu_shape[2 * k]) + dir;
+      y = int(sp.mu_shape[2 * k + 1]);
+    } else {
+      x = int(sp.mu_shape[2 * k]);
+      y = int(sp.mu_shape[2 * k + 1]) + dir;
+    }
+    long long ind = (long long)y * W + x;
+    if (ind < 0 || ind > (long long)W * H - 1) continue;
+    if (seg[ind] != k) continue;
+    (s == 0 ? d1 : d2)[ind] = 1;
+  }
+}
+
+__global__ void k_split_begin(Scalars* sc) {
+  // split runs unless max_spix > nspix_buffer / 2 (split_merge_orig.cu:215)
+  sc->tmp0 = sc->max_spix > sc->nbuf_logical / 2 ? 0 : 1;
+  sc->tmp1 = sc->max_spix + 1;  // offset of the second half
+}
+
+// ---------------------------------------------------------------------------
+// Relaxation to a fixed point inside 32x32 tiles with a one-pixel halo, repeated
+// over the grid until no tile changes (cooperative launch, bounded barrier).
+// mode 0: BFS distances of two seed fields (4-connected, same label, +1 per step;
+//         -1 = unreached) -- the fixed point equals the reference's layered BFS
+//         (calc_split_candidate, split_merge.cu:758-800).
+// mode 1: connected-component roots (8-connected, same label, min pixel index) --
+//         the fixed point of find_spix_min (split_disconnected.cu:458-498).
+template <int MODE>
+__device__ __forceinline__ void relax_coop(const int* __restrict__ seg, int* f1, int* f2, int H,
+                                           int W, Scalars* sc, int* round_flags,
+                                           int max_rounds) {
+  __shared__ int sl[kHalo * kHalo];
+  __shared__ int s1[kHalo * kHalo];
+  __shared__ int s2[MODE == 0 ? kHalo * kHalo : 1];
+  __shared__ int any;
+  const int tiles_x = (W + kTile - 1) / kTile, tiles_y = (H + kTile - 1) / kTile;
+  const int ntiles = tiles_x * tiles_y;
+  for (int round = 0; round < max_rounds; round++) {
+    int my_changed = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int tx0 = (t % tiles_x) * kTile, ty0 = (t / tiles_x) * kTile;
+      for (int i = threadIdx.x; i < kHalo * kHalo; i += blockDim.x) {
+        int gx = tx0 + i % kHalo - 1, gy = ty0 + i / kHalo - 1;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+          int g = gy * W + gx;
+          sl[i] = seg[g];
+          // f1/f2 are written by other blocks of this launch: read past L1.
+          if (MODE == 0) {
+            int a = __ldcg(f1 + g), b = __ldcg(f2 + g);
+            s1[i] = a < 0 ? kInf : a;
+            s2[i] = b < 0 ? kInf : b;
+          } else {
+            int a = __ldcg(f1 + g);
+            s1[i] = a < 0 ? kInf : a;
+          }
+        } else {
+          sl[i] = INT32_MIN;
+          s1[i] = kInf;
+          if (MODE == 0) s2[i] = kInf;
+        }
+      }
+      int local_iter = 0;
+      while (true) {
+        __syncthreads();
+        if (threadIdx.x == 0) any = 0;
+        __syncthreads();
+        int ch = 0;
+        for (int i = threadIdx.x; i < kTile * kTile; i += blockDim.x) {
+          int lx = i % kTile + 1, ly = i / kTile + 1;
+          if (tx0 + lx - 1 >= W || ty0 + ly - 1 >= H) continue;
+          int p = ly * kHalo + lx;
+          int L = sl[p];
+          if (MODE == 0) {
+            int a = s1[p], b = s2[p];
+            const int q4[4] = {p - kHalo, p - 1, p + kHalo, p + 1};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              int q = q4[j];
+              if (sl[q] != L) continue;
+              int qa = s1[q], qb = s2[q];
+              if (qa < kInf && qa + 1 < a) a = qa + 1;
+              if (qb < kInf && qb + 1 < b) b = qb + 1;
+            }
+            if (a < s1[p]) { s1[p] = a; ch = 1; }
+            if (b < s2[p]) { s2[p] = b; ch = 1; }
+          } else {
+            if (L < 0) continue;
+            int a = s1[p];
+#pragma unroll
+            for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+              for (int dx = -1; dx <= 1; dx++) {
+                int q = p + dy * kHalo + dx;
+                if (sl[q] == L && s1[q] < a) a = s1[q];
+              }
+            if (a < s1[p]) { s1[p] = a; ch = 1; }
+          }
+        }
+        if (ch) any = 1;
+        __syncthreads();
+        if (!any || ++local_iter > 4 * kTile * kTile) break;
+      }
+      // write back changed interior values
+      for (int i = threadIdx.x; i < kTile * kTile; i += blockDim.x) {
+        int lx = i % kTile + 1, ly = i / kTile + 1;
+        int gx = tx0 + lx - 1, gy = ty0 + ly - 1;
+        if (gx >= W || gy >= H) continue;
+        int p = ly * kHalo + lx, g = gy * W + gx;
+        if (MODE == 0) {
+          int a = s1[p] >= kInf ? -1 : s1[p];
+          int b = s2[p] >= kInf ? -1 : s2[p];
+          if (a != __ldcg(f1 + g)) { __stcg(f1 + g, a); my_changed = 1; }
+          if (b != __ldcg(f2 + g)) { __stcg(f2 + g, b); my_changed = 1; }
+        } else {
+          int a = s1[p] >= kInf ? -1 : s1[p];
+          if (a != __ldcg(f1 + g)) { __stcg(f1 + g, a); my_changed = 1; }
+        }
+      }
+      __syncthreads();
+    }
+    if (my_changed) atomicOr(&round_flags[round], 1);
+    if (!grid_barrier(sc)) return;
+    if (*(volatile int*)&round_flags[round] == 0) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&sc->status, STSPIX_ERR_ITER_LIMIT);
+}
+
+__global__ void __launch_bounds__(256) k_relax_bfs(const int* __restrict__ seg, int* f1, int* f2,
+                                                   int H, int W, Scalars* sc, int* round_flags,
+                                                   int max_rounds) {
+  relax_coop<0>(seg, f1, f2, H, W, sc, round_flags, max_rounds);
+}
+__global__ void __launch_bounds__(256) k_relax_cc(const int* __restrict__ seg, int* f1, int* f2,
+                                                  int H, int W, Scalars* sc, int* round_flags,
+                                                  int max_rounds) {
+  relax_coop<1>(seg, f1, f2, H, W, sc, round_flags, max_rounds);
+}
+
+// calc_seg_split (split_merge.cu:847-859): second half when d1 > d2.
+__global__ void k_split_partition(const int* __restrict__ seg, const int* __restrict__ d1,
+                                  const int* __restrict__ d2, int npix,
+                                  const Scalars* __restrict__ sc, int* __restrict__ sm) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npix) return;
+  int v = seg[t];
+  if (d1[t] > d2[t]) v += sc->tmp1;
+  sm[t] = v;
+}
+
+// sum_by_label over split/merge labels (split_merge.cu:862-891,
+// split_merge_prop.cu:1942-2018): count, colour sums, square sums, invalid count.
+__global__ void k_sm_accumulate(const float* __restrict__ img, const int* __restrict__ lab,
+                                const int* __restrict__ shifted, int H, int W, int cap,
+                                SmDev sm) {
+  constexpr int R = 16;
+  const int cpr = (W + R - 1) / R;
+  int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= H * cpr) return;
+  int y = tid / cpr, xs = (tid % cpr) * R, xe = min(W, xs + R);
+  const int* lrow = lab + (size_t)y * W;
+  const float* irow = img + (size_t)y * W * 3;
+  const int* shrow = shifted ? shifted + (size_t)y * W : nullptr;
+  int cur = -1, n = 0, ninv = 0;
+  long long s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+  auto flush = [&]() {
+    if (cur < 0 || cur >= cap) return;
+    atomicAdd(&sm.count[cur], n);
+    if (shrow) atomicAdd(&sm.ninvalid[cur], ninv);
+    for (int c = 0; c < 3; c++) {
+      atomicAdd((unsigned long long*)&sm.s[3 * (size_t)cur + c], (unsigned long long)s[c]);
+      atomicAdd((unsigned long long*)&sm.sq[3 * (size_t)cur + c], (unsigned long long)q[c]);
+    }
+  };
+  for (int x = xs; x < xe; x++) {
+    int k = lrow[x];
+    if (k != cur) {
+      flush();
+      cur = k; n = 0; ninv = 0;
+      s[0] = s[1] = s[2] = q[0] = q[1] = q[2] = 0;
+    }
+    if (k >= 0) {
+      n++;
+      for (int c = 0; c < 3; c++) {
+        float v = irow[3 * x + c];
+        s[c] += fx_q(v, kFxAppShift);
+        q[c] += fx_q(v * v, kFxSqShift);
+      }
+      if (shrow && shrow[x] < 0) ninv++;
+    }
+  }
+  flush();
+}
+
+// Hastings terms (split_merge_orig.cu:536-549, 845-877) in FP64; the lgamma(a_n)
+// terms of numerator and denominator are identical and cancel.
+__device__ __forceinline__ double marginal_channel(double n, double b0, double bn) {
+  const double a_n = 1e4 + n / 2;
+  return a_n * (log(b0) - log(bn)) + 0.5 * log(1.0 / n) -
+         (0.5 * n * log(3.14159265358979323846) + n * log(2.0));
+}
+__device__ __forceinline__ double total_marginal(double n, double b0, const long long* s,
+                                                 int s_stride, const long long* sq, bool clamp) {
+  double t = 0;
+  for (int c = 0; c < 3; c++) {
+    double S = fx_unq(s[c * s_stride], kFxAppShift), Q = fx_unq(sq[c], kFxSqShift);
+    double bn = b0 + 0.5 * (Q - S * S / n);
+    if (clamp && bn < 0) bn = 0.1;
+    t += marginal_channel(n, b0, bn);
+  }
+  return t;
+}
+__device__ __forceinline__ bool near_tie(double h) { return fabs(h + 2.0) < 1e-6; }
+
+// update_split_flag (split_merge_orig.cu:900-986) / update_split_flag_p
+// (split_merge_prop.cu:3026-3149): decision only; ids by scan afterwards (R2).
+__global__ void k_split_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, float split_alpha,
+                               int prop_mode, uint8_t* __restrict__ accept) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap) return;
+  accept[k] = 0;
+  if (!sc->tmp0 || !sp.valid[k]) return;
+  const int off = sc->tmp1;
+  int s = k + off;
+  if (s >= sc->nbuf_logical || s >= sp.cap + 2) return;
+  double count_f = sp.count[k], count_k = sm.count[k], count_s = sm.count[s];
+  if (count_f < 1 || count_k < 1 || count_s < 1) return;
+  if (count_f != count_k + count_s) return;
+  long long sq_f[3];
+  for (int c = 0; c < 3; c++) sq_f[c] = sm.sq[3 * (size_t)k + c] + sm.sq[3 * (size_t)s + c];
+  double mk = total_marginal(count_k, b0, &sm.s[3 * (size_t)k], 1, &sm.sq[3 * (size_t)k], false);
+  double ms = total_marginal(count_s, b0, &sm.s[3 * (size_t)s], 1, &sm.sq[3 * (size_t)s], false);
+  double mf = total_marginal(count_f, b0, sp.acc + 8 * (size_t)k, 1, sq_f, false);
+  double h = mk + ms - mf + split_alpha;
+  uint8_t fl = 1;
+  if (prop_mode) {
+    bool is_prop = sp.prop[k];
+    int ninv_k = sm.ninvalid[k], ninv_s = sm.ninvalid[s];
+    bool prop_k = (ninv_k <= ninv_s);
+    float iperc_k = (float)(ninv_k / (1.0 * count_k));
+    float iperc_s = (float)(ninv_k / (1.0 * count_s));  // reference uses ninvalid_k here
+    float iperc = prop_k ? iperc_k : iperc_s;
+    iperc = is_prop ? iperc : 1.0f;
+    h = h - 2 * (1.0 - iperc);
+    if (prop_k || !is_prop) fl |= 8;   // select
+    if (prop_k) fl |= 16;              // keep prior count on k
+  }
+  if (near_tie(h)) atomicAdd(&sc->near_ties, 1);
+  if (h > -2) accept[k] = fl;
+}
+
+// Split commit: new id = max_spix + 1 + rank (R2), prior counts.
+__global__ void k_split_commit(SpDev sp, SmDev sm, Scalars* sc, const uint8_t* __restrict__ accept,
+                               const int* __restrict__ excl, int prop_mode) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap) return;
+  uint8_t fl = accept[k];
+  if (!fl) return;
+  int snew = sc->max_spix + 1 + excl[k];
+  sm.newid[k] = snew;
+  if (snew >= sp.cap) { atomicExch(&sc->status, STSPIX_ERR_CAPACITY); sm.newid[k] = -1; return; }
+  if (!prop_mode) {
+    float pcn = (float)fmax(sp.prior_count[k] / 2.0, 8.0);
+    sp.prior_count[k] = pcn;
+    sp.prior_count[snew] = pcn;
+  } else {
+    float pc = sp.prior_count[k];
+    float half = (float)fmax(pc / 2.0, 36.0);
+    if (fl & 16) {
+      sp.prior_count[k] = pc;
+      sp.prior_count[snew] = (float)(pc / 2.);
+    } else {
+      sp.prior_count[k] = half;
+      sp.prior_count[snew] = half;
+      double pcs = half;
+      sp.prior_icov[3 * k] = pcs; sp.prior_icov[3 * k + 1] = 0; sp.prior_icov[3 * k + 2] = pcs;
+    }
+    sp.prop[snew] = 0;
+    sp.icount[k] = (float)(sp.icount[k] / 2.0);
+    double pcs = sp.prior_count[snew];
+    sp.prior_icov[3 * snew] = pcs; sp.prior_icov[3 * snew + 1] = 0; sp.prior_icov[3 * snew + 2] = pcs;
+  }
+  sp.valid[snew] = 1;
+}
+
+// split_sp (split_merge.cu:1002-1031) / split_sp_p (split_merge_prop.cu:2317-2350).
+__global__ void k_split_apply(int* __restrict__ seg, const int* __restrict__ smseg, int npix,
+                              SpDev sp, SmDev sm, const Scalars* __restrict__ sc,
+                              const uint8_t* __restrict__ accept, int prop_mode) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npix) return;
+  int k = seg[t];
+  if (k < 0 || k >= sp.cap) return;
+  uint8_t fl = accept[k];
+  if (!fl) return;
+  int s = sm.newid[k];
+  if (s < 0) return;
+  int k2 = k + sc->tmp1;
+  if (!prop_mode || (fl & 8)) {
+    if (smseg[t] == k2) seg[t] = s;
+  } else {
+    if (smseg[t] == k) seg[t] = s;
+  }
+}
+
+__global__ void k_split_end(Scalars* sc, const int* __restrict__ nsplits) {
+  int n = *nsplits;
+  sc->nsplits += n;
+  sc->max_spix += n;
+}
+
+// ---------------------------------------------------------------------------
+// Merge candidates (calc_merge_candidate, split_merge.cu:719-755;
+// calc_merge_candidate_p, split_merge_prop.cu:1808-1845).
+__global__ void k_merge_candidates(const int* __restrict__ seg, const uint8_t* __restrict__ border,
+                                   int H, int W, int direction, int prop_mode,
+                                   const uint8_t* __restrict__ prop, int cap,
+                                   int* __restrict__ pair) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= H * W || !border[idx]) return;
+  int x = idx % W, y = idx / W;
+  int C = seg[idx];
+  if (C < 0 || C >= cap) return;
+  int Wl = -1;
+  if (!prop_mode) {
+    if (direction == 1) { if (y >= 0 && y < H - 1) Wl = seg[idx + W]; }
+    else { if (x > 0 && x < W) Wl = seg[idx - 1]; }
+    if (Wl >= cap) Wl = -1;
+    if (Wl >= 0 && C != Wl) atomicMax(&pair[C], Wl);
+  } else {
+    if (direction == 1) { if (y > 1 && y < H - 2) Wl = seg[idx + W]; }
+    else { if (x > 1 && x < W - 2) Wl = seg[idx - 1]; }
+    if (Wl >= cap) Wl = -1;
+    bool pC = prop[C];
+    bool pW = (Wl >= 0) ? prop[Wl] : false;
+    if (Wl >= 0 && C != Wl && pC != pW) atomicMax(&pair[C], Wl);
+  }
+}
+
+// Single-superpixel marginal, present only when k has its own candidate
+// (calc_merge_stats_step0 computes b_n only then; split_merge_orig.cu:456-520).
+__global__ void k_merge_single(SpDev sp, SmDev sm, double b0) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap) return;
+  sm.flag[k] = 0;
+  if (!sp.valid[k] || sm.pair[k] < 0) return;
+  sm.msingle[k] = total_marginal(sp.count[k], b0, sp.acc + 8 * (size_t)k, 1,
+                                 &sm.sq[3 * (size_t)k], true);
+  sm.flag[k] = 16;
+}
+
+// calc_merge_stats_step2 + update_merge_flag (split_merge_orig.cu:555-656), R3.
+__global__ void k_merge_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, double log_alpha,
+                               float merge_alpha) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap || !sp.valid[k]) return;
+  int f = sm.pair[k];
+  if (f < 0 || !sp.valid[f]) return;
+  double count_k = sp.count[k];
+  double count_f = sp.count[k] + sp.count[f];
+  if (count_k < 1 || count_f < 1) return;
+  long long s_f[3], sq_f[3];
+  for (int c = 0; c < 3; c++) {
+    s_f[c] = sp.acc[8 * (size_t)k + c] + sp.acc[8 * (size_t)f + c];
+    sq_f[c] = sm.sq[3 * (size_t)k + c] + sm.sq[3 * (size_t)f + c];
+  }
+  double h;
+  if (!(sm.flag[f] & 16)) {
+    h = -INFINITY;
+  } else {
+    double m_merged = total_marginal(count_f, b0, s_f, 1, sq_f, true);
+    h = m_merged - (log_alpha + sm.msingle[k] + sm.msingle[f]) + merge_alpha;
+  }
+  if (near_tie(h)) atomicAdd(&sc->near_ties, 1);
+  if (h > -2) {
+    sm.flag[k] |= 1;  // only thread k writes flag[k] here; readers use bit 16 only
+    atomicMin(&sm.claim[f], k);
+  }
+}
+
+// merge flag := accepted and claimant of its target; snapshot valid; target := pair.
+__global__ void k_merge_flag(SpDev sp, SmDev sm, uint8_t* __restrict__ valid0) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap) return;
+  valid0[k] = sp.valid[k];
+  int f = sm.pair[k];
+  sm.target[k] = f;
+  uint8_t fl = sm.flag[k];
+  if ((fl & 1) && f >= 0 && sm.claim[f] == k) fl |= 2;
+  sm.flag[k] = fl;
+}
+
+// remove_sp (split_merge.cu:1035-1080) / remove_sp_p (split_merge_prop.cu:2353-2449).
+__global__ void k_merge_remove(SpDev sp, SmDev sm, Scalars* sc, const uint8_t* __restrict__ valid0,
+                               int prop_mode) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sp.cap) return;
+  int s = sm.pair[k];
+  if (s < 0) return;
+  bool is_cycle = sm.pair[s] == k;
+  if (!valid0[k] || !valid0[s]) return;
+  bool mk = sm.flag[k] & 2, ms = sm.flag[s] & 2;
+  if (!prop_mode) {
+    if (mk && (!ms || (is_cycle && k < s))) {
+      sm.flag[k] |= 4;
+      sp.valid[k] = 0;
+      sp.prior_count[s] = sp.prior_count[k] + sp.prior_count[s];
+      atomicAdd(&sc->nmerges, 1);
+    }
+  } else {
+    bool cond_c = is_cycle && sp.prop[k];
+    if (mk && (!ms || cond_c)) {
+      int r = k, t = s;
+      if (sp.prop[k]) { sm.target[s] = k; r = s; t = k; }
+      sm.flag[r] |= 4;  // each superpixel has at most one remover (single writer)
+      sp.valid[r] = 0;
+      sp.prior_count[t] = sp.prior_count[r] + sp.prior_count[t];
+      atomicAdd(&sc->nmerges, 1);
+    }
+  }
+}
+
+// merge_sp (split_merge.cu:984-1000).
+__global__ void k_merge_apply(int* __restrict__ seg, int npix, int cap, SmDev sm) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npix) return;
+  int k = seg[t];
+  if (k < 0 || k >= cap) return;
+  if (sm.flag[k] & 4) seg[t] = sm.target[k];
+}
+
+}  // namespace stspix

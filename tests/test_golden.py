@@ -1,0 +1,59 @@
+"""Golden fixtures (tests/golden/*.npz, made by tests/golden/make_golden.py): the
+oracle must reproduce them (CPU) and the GPU engine must match them (GPU)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return dict(np.load(os.path.join(HERE, name)))
+
+
+def test_oracle_reproduces_bass_golden():
+    g = load("bass_64x96.npz")
+    st, lab, p, n = O.run_bass(g["img"], O.default_config(niters=int(g["niters"])))
+    assert st == 0 and n == int(g["nspix"])
+    np.testing.assert_array_equal(lab, g["labels"])
+    for k, v in p.items():
+        np.testing.assert_array_equal(v, g[k], err_msg=k)
+
+
+def test_oracle_reproduces_video_golden():
+    g = load("bist_video_48x64x3.npz")
+    st, out, used = O.bist_forward(g["vid"], g["flows"], O.default_config(niters=int(g["niters"])),
+                                   True)
+    assert st == 0
+    np.testing.assert_array_equal(out, g["labels"])
+    np.testing.assert_array_equal(used, g["niters_used"])
+
+
+@pytest.mark.gpu
+def test_gpu_matches_bass_golden():
+    import torch
+    from st_spix_gb300 import bist_cuda
+    g = load("bass_64x96.npz")
+    lab, p = bist_cuda.run_bass(torch.from_numpy(g["img"]).cuda(), niters=int(g["niters"]))
+    assert p.n == int(g["nspix"])
+    np.testing.assert_array_equal(lab.cpu().numpy(), g["labels"])
+    for k, v in p.as_dict().items():
+        v = v.cpu().numpy().reshape(-1)
+        if v.dtype == np.float64:
+            np.testing.assert_allclose(v, g[k], rtol=1e-12, atol=0, err_msg=k)
+        else:
+            np.testing.assert_array_equal(v, g[k], err_msg=k)
+
+
+@pytest.mark.gpu
+def test_gpu_matches_video_golden():
+    import torch
+    from st_spix_gb300 import bist_cuda
+    g = load("bist_video_48x64x3.npz")
+    out = bist_cuda.bist_forward(torch.from_numpy(g["vid"]).cuda(),
+                                 torch.from_numpy(g["flows"]).cuda(), int(g["niters"]), 15, 0.5,
+                                 0.009 ** 2, float(np.log(0.5)), 0.0, True, False)
+    np.testing.assert_array_equal(out.cpu().numpy(), g["labels"])
