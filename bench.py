@@ -1,0 +1,427 @@
+"""Benchmark of the streaming-BASS (BIST) hot path on one node.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step"): the 30-frame 480x854 synthetic streaming video of the
+streaming-propagation configuration (Voronoi frames with 400 seeds, per-region
+affine motion, noise sigma 0.03, ground-truth forward flow), run through
+bist_forward in video mode: frame 0 is plain BASS, frames 1..29 are flow
+propagation + hole fill + 20 boundary iterations with split/merge every 10,
+superpixel size 20.  Each rank runs its own stream (seed = rank): replicas, no
+collective on the data path.  Prints ONE JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="bist_stream_480x854_T30", H=480, W=854, T=30, nseeds=400, sigma=0.03,
+                sp_size=20, niters=20, prop_niters=20, sm_period=10, potts=0.5,
+                sigma2_app=0.009 ** 2, alpha=math.log(0.5), split_alpha=0.0)
+SWEEP_BYTES_PER_PX = 20  # label read 4 + image read 12 + label write 4 per sweep
+METRIC = "streamed frames/sec"
+
+
+def gen_video(seed: int, T: int = None):
+    from st_spix_gb300 import synth
+    w = WORKLOAD
+    vid, flows, _ = synth.voronoi_video(w["H"], w["W"], T or w["T"], w["nseeds"], w["sigma"],
+                                        seed=seed)
+    return vid, flows
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the oracle (CPU restatement of the reference path), one stream per
+# worker process, a bounded number of frames per stream.
+_worker_data = {}
+
+
+def _cpu_worker(args):
+    seed, nframes = args
+    import numpy as np
+    from oracle import oracle as O
+    key = (seed, nframes)
+    if key not in _worker_data:
+        _worker_data[key] = gen_video(seed, T=nframes)
+    vid, flows = _worker_data[key]
+    w = WORKLOAD
+    cfg = O.default_config(niters=w["niters"], sp_size=w["sp_size"], prop_niters=w["prop_niters"],
+                           sm_period=w["sm_period"], potts=w["potts"],
+                           sigma2_app=w["sigma2_app"], alpha_hastings=w["alpha"])
+    t = time.perf_counter()
+    st, out, _ = O.bist_forward(vid, flows, cfg, True)
+    dt = time.perf_counter() - t
+    assert st == 0
+    return nframes, dt, int(np.unique(out[-1]).size)
+
+
+class CpuBaseline:
+    """Pool of spawned workers (one per host core) running the oracle."""
+
+    def __init__(self, frames_per_stream: int = 3):
+        import multiprocessing as mp
+        from oracle import oracle as O
+        O.build()
+        self.cores = os.cpu_count() or 1
+        self.frames = frames_per_stream
+        self.pool = mp.get_context("spawn").Pool(self.cores)
+        # generate each worker's stream once
+        self.pool.map(_cpu_worker_warm, [(s, self.frames) for s in range(self.cores)])
+
+    def step(self):
+        t = time.perf_counter()
+        res = self.pool.map(_cpu_worker, [(s, self.frames) for s in range(self.cores)])
+        wall = time.perf_counter() - t
+        frames = sum(r[0] for r in res)
+        return frames, wall
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+    def describe(self):
+        w = WORKLOAD
+        return (f"{self.cores} concurrent streams x first {self.frames} frames "
+                f"(1 BASS + {self.frames - 1} propagated) of the {w['H']}x{w['W']} workload, "
+                f"oracle (CPU restatement), one process per core")
+
+
+def _cpu_worker_warm(args):
+    seed, nframes = args
+    key = (seed, nframes)
+    if key not in _worker_data:
+        _worker_data[key] = gen_video(seed, T=nframes)
+    from oracle import oracle as O
+    O.lib()
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def sample_clocks(gpu_index: int, stop: threading.Event, out: list):
+    q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={q}",
+                              "--format=csv,noheader,nounits", "-lms", "200"],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+        return
+    try:
+        while not stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            out.append(line.strip())
+    finally:
+        p.terminate()
+        try:
+            p.wait(timeout=2)
+        except Exception:
+            p.kill()
+
+
+def summarize_clocks(lines: list) -> dict:
+    sm, mx, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in lines:
+        f = [x.strip() for x in ln.split(",")]
+        if len(f) < 8:
+            continue
+        try:
+            sm.append(float(f[0]))
+            mx = float(f[1])
+        except ValueError:
+            continue
+        for n, v in zip(names, f[4:8]):
+            if v.lower().startswith("active"):
+                reasons.add(n)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_traffic(workload: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary
+    (profiles/<kernel>_<workload>.md, line 'traffic_bytes_per_launch: N')."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if workload in fn and fn.endswith(".md"):
+            for ln in open(os.path.join(d, fn)):
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    try:
+                        return float(ln.split(":", 1)[1])
+                    except ValueError:
+                        return None
+    return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference path's CPU implementation (the oracle port; the
+    reference itself has no CPU path) on all host cores, same metric and config."""
+    if rank != 0:
+        return
+    base = CpuBaseline(frames_per_stream=3)
+    try:
+        for _ in range(args.warmup):
+            base.step()
+        frames, wall = 0, 0.0
+        for _ in range(args.steps):
+            f, w = base.step()
+            frames += f
+            wall += w
+        v = frames / wall
+        w = WORKLOAD
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * wall / max(args.steps, 1), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64+int64",
+                "data": "synthetic",
+                "config": {"workload": w["name"], "H": w["H"], "W": w["W"], "T": w["T"],
+                           "sp_size": w["sp_size"], "niters": w["niters"],
+                           "sm_period": w["sm_period"]},
+                "cpu_baseline": {"value": v, "unit": "frames/s", "cores": base.cores,
+                                 "kind": "port", "sample": base.describe()},
+                "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+    finally:
+        base.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--streams", type=int, default=8,
+                    help="concurrent video streams per GPU (host thread + CUDA stream each)")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    args.warmup = max(args.warmup, 3)
+
+    import numpy as np
+    import torch
+    from st_spix_gb300 import bist_cuda
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    w = WORKLOAD
+    S = max(1, args.streams)
+    kw = dict(sm_period=w["sm_period"], prop_niters=w["prop_niters"])
+
+    def call(v, f):
+        return bist_cuda.bist_forward(v, f, w["niters"], w["sp_size"], w["potts"],
+                                      w["sigma2_app"], w["alpha"], w["split_alpha"], True, False,
+                                      **kw)
+
+    # one video per stream (seed = rank * S + i), resident on the device
+    host = [gen_video(seed=rank * S + i) for i in range(S)]
+    dvid = [torch.from_numpy(v).to(dev) for v, _ in host]
+    dflo = [torch.from_numpy(f).to(dev) for _, f in host]
+    streams = [torch.cuda.Stream(dev) for _ in range(S)]
+    ctxs = [None] * S
+    frame_ms = [[] for _ in range(S)]
+    launches = [0] * S
+
+    def run_all(fn, nsteps):
+        """Run fn(i, step) for every stream i on its own host thread and CUDA stream."""
+        gate = threading.Barrier(S)
+        errs = []
+
+        def body(i):
+            try:
+                torch.cuda.set_device(dev)
+                with torch.cuda.stream(streams[i]):
+                    gate.wait()
+                    for st in range(nsteps):
+                        fn(i, st)
+                    streams[i].synchronize()
+            except Exception as e:  # surfaced below
+                errs.append(repr(e))
+        th = [threading.Thread(target=body, args=(i,)) for i in range(S)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        if errs:
+            raise RuntimeError("; ".join(errs))
+
+    def warm(i, st):
+        ctxs[i] = bist_cuda._ctx(dev)
+        call(dvid[i], dflo[i])
+
+    run_all(warm, args.warmup)
+    torch.cuda.synchronize()
+
+    # ---- timed region (device-resident inputs) ---------------------------------
+    clk_lines, stop = [], threading.Event()
+    th = threading.Thread(target=sample_clocks, args=(local, stop, clk_lines), daemon=True)
+    th.start()
+    l0 = [c.launches() for c in ctxs]
+
+    def timed(i, st):
+        call(dvid[i], dflo[i])
+        frame_ms[i].extend(ctxs[i].frame_times())
+
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run_all(timed, args.steps)
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    barrier()
+    total_launches = sum(c.launches() - a for c, a in zip(ctxs, l0))
+    stop.set()
+    th.join(timeout=5)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    frames_total = world * S * w["T"] * args.steps
+    value = frames_total / elapsed
+
+    # ---- per-family device time, one stream alone, CUDA events on its stream ----
+    with torch.cuda.stream(streams[0]):
+        ctx0 = bist_cuda._ctx(dev)  # the main thread's own context
+        call(dvid[0], dflo[0])      # warm it
+        ctx0.profile(True)
+        for _ in range(args.steps):
+            call(dvid[0], dflo[0])
+        streams[0].synchronize()
+        prof = ctx0.profile_get()
+        ctx0.profile(False)
+
+    # ---- e2e through the public API with host buffers --------------------------
+    h_vid = [torch.from_numpy(v).pin_memory() for v, _ in host]
+    h_flo = [torch.from_numpy(f).pin_memory() for _, f in host]
+    h_out = [torch.empty((w["T"], w["H"], w["W"]), dtype=torch.int32).pin_memory()
+             for _ in range(S)]
+
+    def e2e(i, st):
+        dv = h_vid[i].to(dev, non_blocking=True)
+        df = h_flo[i].to(dev, non_blocking=True)
+        o = call(dv, df)
+        h_out[i].copy_(o, non_blocking=True)
+        streams[i].synchronize()
+
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run_all(e2e, args.steps)
+    e2e_elapsed = time.perf_counter() - t0
+    barrier()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_elapsed], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_elapsed = float(t.item())
+    e2e_value = frames_total / e2e_elapsed
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel family --------------------------------
+    npix = w["H"] * w["W"]
+    fam = max(prof, key=lambda k: prof[k][1])
+    nsweep = prof["sweep"][0]       # one fused launch per sweep
+    sweep_ms = prof["sweep"][1]
+    peak, peak_kind = read_peaks()
+    achieved = (SWEEP_BYTES_PER_PX * npix * nsweep) / (sweep_ms / 1000.0) / 1e9 if sweep_ms else 0
+    traffic = read_traffic(w["name"])
+    passes_per_step = w["niters"] + (w["T"] - 1) * w["prop_niters"]
+    mpix_pass = world * S * args.steps * passes_per_step * npix / elapsed / 1e6
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        base = CpuBaseline(frames_per_stream=3)
+        try:
+            f, wall = base.step()
+            cpu = {"value": f / wall, "unit": "frames/s", "cores": base.cores, "kind": "port",
+                   "sample": base.describe()}
+        finally:
+            base.close()
+
+    fms = sorted(x for lst in frame_ms for x in lst)
+    pct = lambda q: fms[min(len(fms) - 1, int(q * len(fms)))] if fms else None
+    h_bytes = sum(v.nbytes + f.nbytes for v, f in host)
+    line = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32/f64+int64", "data": "synthetic",
+        "config": {"workload": w["name"], "H": w["H"], "W": w["W"], "T": w["T"],
+                   "sp_size": w["sp_size"], "niters": w["niters"],
+                   "prop_niters": w["prop_niters"], "sm_period": w["sm_period"],
+                   "streams_per_gpu": S, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2: %d MB of frames+flow read per step" %
+                         (h_bytes // 2 ** 20)},
+        "p50_frame_ms": pct(0.50), "p99_frame_ms": pct(0.99),
+        "mpix_per_s_per_pass": mpix_pass,
+        "roofline": {"bound": "hbm", "kernel": "k_sweep_fused (border + 4 parity phases)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": SWEEP_BYTES_PER_PX * npix,
+                     "dominant_family": fam,
+                     "family_ms": {k: round(v[1], 3) for k, v in prof.items()},
+                     "family_launches": {k: v[0] for k, v in prof.items()}},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "frames/s",
+                "h2d_bytes_per_step": int(h_bytes),
+                "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in h_out))},
+        "gpu_launches": int(total_launches),
+        "clocks": summarize_clocks(clk_lines),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -112,6 +112,24 @@ long long   stspix_kernel_launches(const stspix_ctx* ctx);
 /* Copy of the log of the last frame processed by this context (host). */
 int         stspix_get_frame_log(const stspix_ctx* ctx, stspix_frame_log* out);
 
+/* ---- measurement --------------------------------------------------------------
+ * Kernel-family profiling with CUDA events recorded on the launching stream
+ * around every launch of the family (off by default; enabling resets totals).
+ * Per-frame GPU durations of the last stspix_bist_forward call are always kept. */
+#define STSPIX_FAM_SWEEP     0   /* boundary sweep (border + 4 parity phases)      */
+#define STSPIX_FAM_STATS     1   /* sufficient statistics (sum_by_label)           */
+#define STSPIX_FAM_POSTERIOR 2   /* posterior / parameter kernels                  */
+#define STSPIX_FAM_SPLIT     3   /* split proposal + BFS + Hastings                */
+#define STSPIX_FAM_MERGE     4   /* merge proposal + Hastings (+ relabel)          */
+#define STSPIX_FAM_PROP      5   /* flow pooling, shift, fill, components          */
+#define STSPIX_FAM_OTHER     6   /* init, compaction, read-out                     */
+#define STSPIX_NFAM          7
+int stspix_profile_enable(stspix_ctx* ctx, int enable);
+int stspix_profile_get(const stspix_ctx* ctx, int family, long long* launches,
+                       double* total_ms);
+/* Per-frame durations (ms) of the last bist_forward call; returns the count. */
+int stspix_frame_times(const stspix_ctx* ctx, double* ms_out, int capacity);
+
 /* ---- drop-in surface ------------------------------------------------------ */
 
 /* bist_forward: vid f32 [T,H,W,3] contiguous; flows f32 [>=T-1,H,W,2]

@@ -22,8 +22,8 @@
 //   R6 connected components keep, per label, the largest 8-connected region, ties to
 //      the region whose first pixel (raster order) comes first (split_disconnected.cu:248).
 //   R7 values the reference reads uninitialised are zero: sm_helper.ninvalid
-//      (split_merge_prop.cu:2000, never cleared) and ss_comps for ids >= nspix_prev
-//      (relabel.cu:236, never written).
+//      (accumulated at split_merge_prop.cu:2005, never cleared) and ss_comps for ids
+//      >= nspix_prev (read at relabel.cu:143, written only at :273 for ids < nspix_prev).
 //   R8 floating point: IEEE binary32/64, no contraction into FMA (build with
 //      -ffp-contract=off); expression trees and float/double conversions follow the
 //      reference's source expressions.  The Hastings ratio (split/merge) is evaluated
@@ -480,43 +480,36 @@ void update_seg(Frame& f) {
 // -------------------------------------------------------------------------
 // Split / merge helpers.
 
-// Per-channel marginal of the reference's Hastings terms
-// (split_merge_orig.cu:536-549 and 845-877): numerator - denominator with
-//   numerator   = a_n log b_0 + lgamma(a_n) + 0.5 log(1/n)
-//   denominator = a_n log b_n + 0.5 n log(pi) + n log 2 + lgamma(a_n)
-// where a_n = a_0 + n/2.  The lgamma(a_n) terms cancel exactly and are dropped.
-inline double marginal_channel(double n, double b0, double bn) {
-  const double a_n = 1e4 + n / 2;
-  return a_n * (log(b0) - log(bn)) + 0.5 * log(1.0 / n) -
-         (0.5 * n * log(M_PI) + n * log(2.0));
-}
-
-// b_n = b_0 + 0.5 * (sum v^2 - (sum v)^2 / n)   (split_merge_orig.cu:480-501)
-inline double bn_of(double b0, double n, int64_t s, int64_t sq) {
-  double S = unfx(s, kFxAppShift), Q = unfx(sq, kFxSqShift);
-  return b0 + 0.5 * (Q - S * S / n);
-}
-
-double total_marginal(double n, double b0, const int64_t* s, const int64_t* sq,
-                      bool clamp_negative, bool* ok) {
-  double t = 0;
-  for (int c = 0; c < 3; c++) {
-    double bn = bn_of(b0, n, s[c], sq[c]);
-    if (clamp_negative && bn < 0) bn = 0.1;
-    t += marginal_channel(n, b0, bn);
-  }
-  if (ok) *ok = true;
-  return t;
-}
-
-// Split/merge constants (split_merge_orig.cu:97-106, 240-251).
-struct SmConst { double b0; double log_alpha; };
+// Split/merge constants (split_merge_orig.cu:97-106, 240-251): b_0 = 2 sqrt(s2) a_0
+// with a_0 = 1e4; log alpha; lc = 0.5 log(pi) + log 2.
+struct SmConst { double b0; double log_alpha; double log_b0; double lc; };
 SmConst sm_const(const stspix_config& c) {
   float i_std = (float)(sqrt(c.sigma2_app) * 2);
   float a0 = 1e4f;
   float b0 = i_std * a0;
   float alpha = (float)exp((double)c.alpha_hastings);
-  return SmConst{(double)b0, log((double)alpha)};
+  return SmConst{(double)b0, log((double)alpha), log((double)b0), 0.5 * log(M_PI) + log(2.0)};
+}
+
+// Marginal of one superpixel summed over the three colour channels: the
+// reference's numerator - denominator (split_merge_orig.cu:536-549, 845-877)
+//   numerator   = a_n log b_0 + lgamma(a_n) + 0.5 log(1/n)
+//   denominator = a_n log b_n + 0.5 n log(pi) + n log 2 + lgamma(a_n)
+// with a_n = a_0 + n/2 and b_n = b_0 + 0.5 (sum v^2 - (sum v)^2 / n)
+// (:480-501).  The lgamma(a_n) terms are identical and cancel; log b_0 - log b_n
+// is evaluated as -log1p((b_n - b_0) / b_0).  `clamp` is the merge path's
+// b_n < 0 -> 0.1 rule.
+double total_marginal(double n, const SmConst& K, const int64_t* s, const int64_t* sq,
+                      bool clamp) {
+  const double a_n = 1e4 + n / 2;
+  double t = 0;
+  for (int c = 0; c < 3; c++) {
+    double S = unfx(s[c], kFxAppShift), Q = unfx(sq[c], kFxSqShift);
+    double d = 0.5 * (Q - S * S / n);
+    double lr = (clamp && K.b0 + d < 0) ? log(0.1) - K.log_b0 : log1p(d / K.b0);
+    t += -a_n * lr;
+  }
+  return t + 3 * (-0.5 * log(n) - n * K.lc);
 }
 
 // sum_by_label (split_merge.cu:862-891 / split_merge_prop.cu:1942-2018) over `lab`.
@@ -623,9 +616,9 @@ void run_split(Frame& f, int direction, const int* shifted, bool prop_mode) {
       sq_f[c] = a.sq[3 * (size_t)k + c] + a.sq[3 * (size_t)s + c];
       s_f[c] = sp.acc[8 * (size_t)k + c];
     }
-    double mk = total_marginal(count_k, K.b0, &a.s[3 * (size_t)k], &a.sq[3 * (size_t)k], false, nullptr);
-    double ms = total_marginal(count_s, K.b0, &a.s[3 * (size_t)s], &a.sq[3 * (size_t)s], false, nullptr);
-    double mf = total_marginal(count_f, K.b0, s_f, sq_f, false, nullptr);
+    double mk = total_marginal(count_k, K, &a.s[3 * (size_t)k], &a.sq[3 * (size_t)k], false);
+    double ms = total_marginal(count_s, K, &a.s[3 * (size_t)s], &a.sq[3 * (size_t)s], false);
+    double mf = total_marginal(count_f, K, s_f, sq_f, false);
     double h = mk + ms - mf + f.cfg.split_alpha;
     bool prop_k = true;
     if (prop_mode) {
@@ -724,7 +717,7 @@ void run_merge(Frame& f, int direction, bool prop_mode) {
   std::vector<uint8_t> has_single(nbuf, 0);
   for (int k = 0; k < nbuf; k++) {
     if (!sp.valid[k] || pair[k] < 0) continue;
-    msingle[k] = total_marginal(sp.count[k], K.b0, &sp.acc[8 * (size_t)k], &a.sq[3 * (size_t)k], true, nullptr);
+    msingle[k] = total_marginal(sp.count[k], K, &sp.acc[8 * (size_t)k], &a.sq[3 * (size_t)k], true);
     has_single[k] = 1;
   }
   std::vector<int> claim(nbuf, INT32_MAX);
@@ -741,7 +734,7 @@ void run_merge(Frame& f, int direction, bool prop_mode) {
       s_f[c] = sp.acc[8 * (size_t)k + c] + sp.acc[8 * (size_t)fk + c];
       sq_f[c] = a.sq[3 * (size_t)k + c] + a.sq[3 * (size_t)fk + c];
     }
-    double m_merged = total_marginal(count_f, K.b0, s_f, sq_f, true, nullptr);
+    double m_merged = total_marginal(count_f, K, s_f, sq_f, true);
     double h;
     if (!has_single[fk]) {
       h = -INFINITY;  // f's own b_n never computed: log(0) -> ratio -inf

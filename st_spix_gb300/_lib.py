@@ -56,7 +56,10 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_version", "stspix_kernel_launches", "stspix_get_frame_log",
            "stspix_bist_forward", "stspix_get_marked_video", "stspix_run_bass",
            "stspix_shift_and_fill", "stspix_run_prop", "stspix_init_seg",
-           "stspix_find_border", "stspix_bass_partial"]
+           "stspix_find_border", "stspix_bass_partial", "stspix_profile_enable",
+           "stspix_profile_get", "stspix_frame_times"]
+
+FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
 
 def library_path() -> str:
@@ -96,6 +99,9 @@ def load(build_if_missing: bool = True):
             "stspix_find_border": (I, [P, P, P, P, I, I, I]),
             "stspix_bass_partial": (I, [P, P, P, I, I, C.POINTER(Config), I, I, P,
                                         C.POINTER(DumpC), C.POINTER(I), C.POINTER(I)]),
+            "stspix_profile_enable": (I, [P, I]),
+            "stspix_profile_get": (I, [P, I, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+            "stspix_frame_times": (I, [P, C.POINTER(C.c_double), I]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -137,6 +143,23 @@ class Context:
         lg = FrameLog()
         self.check(self.lib.stspix_get_frame_log(self.handle, C.byref(lg)))
         return lg
+
+    def profile(self, enable: bool = True):
+        self.check(self.lib.stspix_profile_enable(self.handle, int(bool(enable))))
+
+    def profile_get(self) -> dict:
+        out = {}
+        for i, name in enumerate(FAMILIES):
+            n, ms = C.c_longlong(0), C.c_double(0)
+            self.check(self.lib.stspix_profile_get(self.handle, i, C.byref(n), C.byref(ms)))
+            out[name] = (int(n.value), float(ms.value))
+        return out
+
+    def frame_times(self) -> list:
+        n = self.lib.stspix_frame_times(self.handle, None, 0)
+        buf = (C.c_double * max(n, 1))()
+        self.lib.stspix_frame_times(self.handle, buf, n)
+        return [buf[i] for i in range(n)]
 
     def close(self):
         if getattr(self, "handle", None):

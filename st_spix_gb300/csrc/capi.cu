@@ -62,7 +62,7 @@ struct stspix_ctx {
   // pixel buffers
   uint8_t* border = nullptr;
   int *d1 = nullptr, *d2 = nullptr, *smseg = nullptr, *hits = nullptr;
-  int *shifted = nullptr, *filled = nullptr;
+  int *shifted = nullptr, *filled = nullptr, *seg_alt = nullptr;
   unsigned long long* best = nullptr;
   // superpixel buffers
   SpDev sp{}, tmp{};
@@ -85,6 +85,16 @@ struct stspix_ctx {
   std::vector<Buf> pix_bufs, sp_bufs, pp_bufs;
   int pp_cap = 0;
   int coop_relax0 = 0, coop_relax1 = 0, coop_fill = 0;
+  // profiling (CUDA events on the launching stream)
+  int prof_on = 0;
+  int cur_fam = STSPIX_FAM_OTHER;
+  std::vector<cudaEvent_t> ev_free;
+  struct Pending { int fam; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  long long fam_launches[STSPIX_NFAM] = {0};
+  double fam_ms[STSPIX_NFAM] = {0};
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> frame_ev;
+  std::vector<double> frame_ms;
 };
 
 namespace {
@@ -110,20 +120,57 @@ int fail(stspix_ctx* c, int code, const char* fmt, ...) {
                   "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
   } while (0)
 
+cudaEvent_t ev_get(stspix_ctx* ctx) {
+  if (!ctx->ev_free.empty()) {
+    cudaEvent_t e = ctx->ev_free.back();
+    ctx->ev_free.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+inline cudaEvent_t prof_begin(stspix_ctx* ctx, cudaStream_t st) {
+  if (!ctx->prof_on) return nullptr;
+  cudaEvent_t e = ev_get(ctx);
+  cudaEventRecord(e, st);
+  return e;
+}
+inline void prof_end(stspix_ctx* ctx, cudaStream_t st, cudaEvent_t a) {
+  if (!a) return;
+  cudaEvent_t b = ev_get(ctx);
+  cudaEventRecord(b, st);
+  ctx->pending.push_back({ctx->cur_fam, a, b});
+}
+// Called after the stream has been synchronised.
+void prof_harvest(stspix_ctx* ctx) {
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      ctx->fam_ms[p.fam] += ms;
+      ctx->fam_launches[p.fam] += 1;
+    }
+    ctx->ev_free.push_back(p.a);
+    ctx->ev_free.push_back(p.b);
+  }
+  ctx->pending.clear();
+}
+
+#define LAUNCHG(kernel, grid, block, ...)                                      \
+  do {                                                                         \
+    cudaEvent_t pe_ = prof_begin(ctx, st);                                     \
+    kernel<<<grid, block, 0, st>>>(__VA_ARGS__);                               \
+    ctx->launches++;                                                           \
+    prof_end(ctx, st, pe_);                                                    \
+  } while (0)
+
 #define LAUNCH(kernel, n, ...)                                                 \
   do {                                                                         \
     long long n_ = (n);                                                        \
-    if (n_ > 0) {                                                              \
-      kernel<<<blocks_for(n_), kThreads, 0, st>>>(__VA_ARGS__);                \
-      ctx->launches++;                                                         \
-    }                                                                          \
+    if (n_ > 0) LAUNCHG(kernel, blocks_for(n_), kThreads, __VA_ARGS__);        \
   } while (0)
 
-#define LAUNCH1(kernel, ...)                                                   \
-  do {                                                                         \
-    kernel<<<1, 1, 0, st>>>(__VA_ARGS__);                                      \
-    ctx->launches++;                                                           \
-  } while (0)
+#define LAUNCH1(kernel, ...) LAUNCHG(kernel, 1, 1, __VA_ARGS__)
 
 template <typename T>
 int alloc(stspix_ctx* ctx, std::vector<Buf>& list, T** p, size_t n) {
@@ -186,6 +233,7 @@ int ensure(stspix_ctx* ctx, int npix, int sp_cap) {
     int n = npix;
     AL(L, ctx->border, n); AL(L, ctx->d1, n); AL(L, ctx->d2, n); AL(L, ctx->smseg, n);
     AL(L, ctx->hits, n); AL(L, ctx->shifted, n); AL(L, ctx->filled, n); AL(L, ctx->best, n);
+    AL(L, ctx->seg_alt, n);
     ctx->npix_cap = npix;
   }
   if (sp_cap > ctx->sp_cap) {
@@ -220,15 +268,17 @@ void hex_geometry(int sp_size, int W, int H, double* hh, double* ww, int* nx, in
   *ny = (int)floor(double(H) / (1.5 * Hh)) + 2;
 }
 
-struct SmK {
-  double b0, log_alpha;
-};
-SmK sm_constants(const stspix_config& c) {
+SmConsts sm_constants(const stspix_config& c) {
   float i_std = (float)(sqrt(c.sigma2_app) * 2);
   float a0 = 1e4f;
   float b0 = i_std * a0;
   float alpha = (float)exp((double)c.alpha_hastings);
-  return SmK{(double)b0, log((double)alpha)};
+  SmConsts K;
+  K.b0 = (double)b0;
+  K.log_alpha = log((double)alpha);
+  K.log_01_b0 = log(0.1) - log((double)b0);
+  K.lc = 0.5 * log(M_PI) + log(2.0);
+  return K;
 }
 
 // Parameter ping-pong buffers of bist_forward: grown to `cap` entries keeping the
@@ -267,8 +317,10 @@ int ensure_pp(stspix_ctx* ctx, cudaStream_t st, int cap, int keep_idx, int keep)
 int coop_launch(stspix_ctx* ctx, cudaStream_t st, const void* fn, int want_blocks, int max_blocks,
                 void** args) {
   int g = std::max(1, std::min(want_blocks, max_blocks));
+  cudaEvent_t pe = prof_begin(ctx, st);
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(g), dim3(kThreads), args, 0, st);
   ctx->launches++;
+  prof_end(ctx, st, pe);
   if (e != cudaSuccess)
     return fail(ctx, STSPIX_ERR_CUDA, "cooperative launch failed: %s", cudaGetErrorString(e));
   return STSPIX_OK;
@@ -281,7 +333,7 @@ struct Frame {
   int* seg;  // working labels (caller's output buffer)
   int H, W, npix;
   stspix_config cfg;
-  SmK K;
+  SmConsts K;
   const int* shifted;  // prop frames: shifted labels (for invalid counts)
   int prop_mode;
   int n_prev;
@@ -292,23 +344,36 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const Frame& f) {
   SpDev& sp = ctx->sp;
   CK(cudaMemsetAsync(sp.count, 0, sizeof(int) * (size_t)sp.cap, st));
   CK(cudaMemsetAsync(sp.acc, 0, sizeof(long long) * 8 * (size_t)sp.cap, st));
-  LAUNCH(k_accumulate, (long long)f.H * ((f.W + 15) / 16), f.img, f.seg, f.H, f.W, sp);
+  ctx->cur_fam = STSPIX_FAM_STATS;
+  {
+    long long nthr = (long long)f.H * ((f.W + 7) / 8);  // one 8-pixel run per thread
+    LAUNCHG(k_accumulate, (unsigned)((nthr + 127) / 128), 128, f.img, f.seg, f.H, f.W, sp);
+  }
+  ctx->cur_fam = STSPIX_FAM_POSTERIOR;
   LAUNCH(k_posterior, sp.cap, sp, f.cfg.sp_size, ctx->sc);
   return STSPIX_OK;
 }
 
-int update_seg(stspix_ctx* ctx, cudaStream_t st, const Frame& f) {
+// update_seg (update_seg.cu:281-311): niters_seg fused sweeps ping-ponging between
+// the frame's labels and a scratch buffer; the trailing border mask is only built
+// when the next iteration's merge reads it.
+int update_seg(stspix_ctx* ctx, cudaStream_t st, const Frame& f, bool need_border) {
   const int H = f.H, W = f.W;
+  ctx->cur_fam = STSPIX_FAM_SWEEP;
+  int* a = f.seg;
+  int* b = ctx->seg_alt;
+  dim3 grid((W + 31) / 32, (H + 31) / 32);
   for (int it = 0; it < f.cfg.niters_seg; it++) {
-    LAUNCH(k_find_border, f.npix, f.seg, ctx->border, H, W);
-    for (int xm = 0; xm < 2; xm++)
-      for (int ym = 0; ym < 2; ym++) {
-        long long n = (long long)((W - xm + 1) / 2) * ((H - ym + 1) / 2);
-        LAUNCH(k_update_phase, n, f.img, f.seg, ctx->border, ctx->sp.rec, ctx->sp.cap, H, W, xm,
-               ym, f.cfg.sigma2_app, f.cfg.potts);
-      }
+    LAUNCHG(k_sweep_fused, grid, 256, f.img, a, b, ctx->sp.rec, ctx->sp.cap, H, W,
+            f.cfg.sigma2_app, f.cfg.potts);
+    std::swap(a, b);
   }
-  LAUNCH(k_find_border, f.npix, f.seg, ctx->border, H, W);
+  if (a != f.seg)
+    CK(cudaMemcpyAsync(f.seg, a, sizeof(int) * (size_t)f.npix, cudaMemcpyDeviceToDevice, st));
+  if (need_border) {
+    ctx->cur_fam = STSPIX_FAM_MERGE;
+    LAUNCH(k_find_border, f.npix, f.seg, ctx->border, H, W);
+  }
   return STSPIX_OK;
 }
 
@@ -329,6 +394,7 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int direction) {
   SmDev& sm = ctx->sm;
   const int cap = sp.cap;
   const size_t c2 = (size_t)cap + 2;
+  ctx->cur_fam = STSPIX_FAM_SPLIT;
   LAUNCH1(k_split_begin, ctx->sc);
   CK(cudaMemsetAsync(ctx->d1, 0xff, sizeof(int) * (size_t)f.npix, st));
   CK(cudaMemsetAsync(ctx->d2, 0xff, sizeof(int) * (size_t)f.npix, st));
@@ -342,10 +408,9 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int direction) {
   CK(cudaMemsetAsync(sm.sq, 0, sizeof(long long) * 3 * c2, st));
   LAUNCH(k_sm_accumulate, (long long)f.H * ((f.W + 15) / 16), f.img, ctx->smseg,
          f.prop_mode ? f.shifted : nullptr, f.H, f.W, cap + 2, sm);
-  LAUNCH(k_split_decide, cap, sp, sm, ctx->sc, f.K.b0, f.cfg.split_alpha, f.prop_mode,
+  LAUNCH(k_split_decide, cap, sp, sm, ctx->sc, f.K, f.cfg.split_alpha, f.prop_mode,
          ctx->accept);
-  k_scan_flags<<<1, 1024, 0, st>>>(ctx->accept, nullptr, cap, ctx->excl, &ctx->sc->tmp2);
-  ctx->launches++;
+  LAUNCHG(k_scan_flags, 1, 1024, ctx->accept, nullptr, cap, ctx->excl, &ctx->sc->tmp2);
   LAUNCH(k_split_commit, cap, sp, sm, ctx->sc, ctx->accept, ctx->excl, f.prop_mode);
   LAUNCH(k_split_apply, f.npix, f.seg, ctx->smseg, f.npix, sp, sm, ctx->sc, ctx->accept,
          f.prop_mode);
@@ -356,18 +421,17 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int direction) {
 int run_relabel(stspix_ctx* ctx, cudaStream_t st, const Frame& f) {
   SpDev& sp = ctx->sp;
   const int cap = sp.cap;
+  ctx->cur_fam = STSPIX_FAM_MERGE;
   CK(cudaMemsetAsync(ctx->living, 0, (size_t)cap + 2, st));
   LAUNCH(k_living, f.npix, f.seg, f.npix, ctx->sc, ctx->living);
   LAUNCH(k_relabel_init, cap, cap, ctx->rbest, ctx->ss);
   const int chunk = 256;
   dim3 g(blocks_for(cap), (unsigned)std::max(1, (f.n_prev + chunk - 1) / chunk));
-  k_relabel_compare<<<g, kThreads, 0, st>>>(sp, f.prev_prior_mu_app, f.n_prev, ctx->sc,
-                                            ctx->living, ctx->rbest, ctx->ss, chunk);
-  ctx->launches++;
+  LAUNCHG(k_relabel_compare, g, kThreads, sp, f.prev_prior_mu_app, f.n_prev, ctx->sc,
+          ctx->living, ctx->rbest, ctx->ss, chunk);
   LAUNCH(k_relabel_mark, cap, cap, ctx->sc, ctx->living, ctx->rbest, ctx->ss,
          f.cfg.thresh_relabel, f.cfg.thresh_new, ctx->rid, ctx->mint);
-  k_scan_flags<<<1, 1024, 0, st>>>(ctx->mint, nullptr, cap, ctx->excl, &ctx->sc->tmp2);
-  ctx->launches++;
+  LAUNCHG(k_scan_flags, 1, 1024, ctx->mint, nullptr, cap, ctx->excl, &ctx->sc->tmp2);
   CK(cudaMemsetAsync(ctx->src_of, 0xff, sizeof(int) * ((size_t)cap + 2), st));
   LAUNCH(k_relabel_ids, cap, cap, ctx->sc, ctx->mint, ctx->excl, ctx->rid, ctx->src_of);
   LAUNCH(k_relabel_params, cap, sp, ctx->rid, ctx->src_of, f.n_prev);
@@ -382,6 +446,7 @@ int run_merge(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int direction) {
   SmDev& sm = ctx->sm;
   const int cap = sp.cap;
   const size_t c2 = (size_t)cap + 2;
+  ctx->cur_fam = STSPIX_FAM_MERGE;
   CK(cudaMemsetAsync(sm.pair, 0xff, sizeof(int) * c2, st));
   CK(cudaMemsetAsync(sm.claim, 0x7f, sizeof(int) * c2, st));
   LAUNCH(k_merge_candidates, f.npix, f.seg, ctx->border, f.H, f.W, direction, f.prop_mode,
@@ -391,8 +456,8 @@ int run_merge(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int direction) {
   CK(cudaMemsetAsync(sm.sq, 0, sizeof(long long) * 3 * c2, st));
   LAUNCH(k_sm_accumulate, (long long)f.H * ((f.W + 15) / 16), f.img, f.seg, nullptr, f.H, f.W,
          cap, sm);
-  LAUNCH(k_merge_single, cap, sp, sm, f.K.b0);
-  LAUNCH(k_merge_decide, cap, sp, sm, ctx->sc, f.K.b0, f.K.log_alpha, f.cfg.merge_alpha);
+  LAUNCH(k_merge_single, cap, sp, sm, f.K);
+  LAUNCH(k_merge_decide, cap, sp, sm, ctx->sc, f.K, f.cfg.merge_alpha);
   LAUNCH(k_merge_flag, cap, sp, sm, ctx->valid0);
   LAUNCH(k_merge_remove, cap, sp, sm, ctx->sc, ctx->valid0, f.prop_mode);
   LAUNCH(k_merge_apply, f.npix, f.seg, f.npix, cap, sm);
@@ -431,13 +496,16 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int niters, int 
         if ((r = update_params(ctx, st, f))) return r;
       }
     }
-    if ((r = update_seg(ctx, st, f))) return r;
+    const int nx = idx + 1;
+    const bool merge_next = nx < niters && nx > f.cfg.sm_start && nx % P == P / 2;
+    if ((r = update_seg(ctx, st, f, merge_next || stop_after >= 0))) return r;
   }
   if (stop_after >= 0) {
     if (extra_update && (r = update_params(ctx, st, f))) return r;
     return STSPIX_OK;
   }
   if ((r = update_params(ctx, st, f))) return r;
+  ctx->cur_fam = STSPIX_FAM_POSTERIOR;
   LAUNCH(k_store_sample, ctx->sp.cap, ctx->sp);
   return STSPIX_OK;
 }
@@ -445,11 +513,11 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int niters, int 
 // compactify_new_superpixels (compact_spix.cu:41-89) for ids >= lo, moving params.
 int compact(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int lo) {
   const int cap = ctx->sp.cap;
+  ctx->cur_fam = STSPIX_FAM_OTHER;
   CK(cudaMemsetAsync(ctx->flags, 0, (size_t)cap + 2, st));
   LAUNCH1(k_calc_n, ctx->sc, lo, cap);
   LAUNCH(k_mark_present, f.npix, f.seg, f.npix, lo, &ctx->sc->max_spix, 0, ctx->flags);
-  k_scan_flags<<<1, 1024, 0, st>>>(ctx->flags, &ctx->sc->tmp2, 0, ctx->excl, &ctx->sc->tmp1);
-  ctx->launches++;
+  LAUNCHG(k_scan_flags, 1, 1024, ctx->flags, &ctx->sc->tmp2, 0, ctx->excl, &ctx->sc->tmp1);
   LAUNCH(k_compact_gather, cap, ctx->sp, ctx->tmp, lo, &ctx->sc->max_spix, ctx->flags, ctx->excl);
   LAUNCH(k_compact_scatter, cap, ctx->sp, ctx->tmp, lo, &ctx->sc->tmp1);
   LAUNCH(k_remap, f.npix, f.seg, f.npix, lo, ctx->excl);
@@ -470,19 +538,20 @@ int bass_frame(stspix_ctx* ctx, cudaStream_t st, const float* img, int H, int W,
   int r;
   if ((r = ensure(ctx, npix, std::max(nbuf, 64)))) return r;
   Frame f{img, seg, H, W, npix, cfg, sm_constants(cfg), nullptr, 0, 0, nullptr};
+  ctx->cur_fam = STSPIX_FAM_OTHER;
   LAUNCH1(k_frame_begin, ctx->sc, 0, nbuf);
   LAUNCH(k_init_hex, npix, seg, H, W, Hh, w, nx, ny);
   // compact the hex ids (extract_unique_ids + compactify, bass.cu:251-252)
   CK(cudaMemsetAsync(ctx->flags, 0, (size_t)ctx->sp.cap + 2, st));
   LAUNCH(k_mark_present, npix, seg, npix, 0, nullptr, nraw - 1, ctx->flags);
-  k_scan_flags<<<1, 1024, 0, st>>>(ctx->flags, nullptr, nraw, ctx->excl, &ctx->sc->nspix);
-  ctx->launches++;
+  LAUNCHG(k_scan_flags, 1, 1024, ctx->flags, nullptr, nraw, ctx->excl, &ctx->sc->nspix);
   LAUNCH(k_remap, npix, seg, npix, 0, ctx->excl);
   LAUNCH1(k_bass_after_compact, ctx->sc);
   LAUNCH(k_init_bass_params, ctx->sp.cap, ctx->sp, &ctx->sc->nspix, npix, cfg.sp_size);
   CK(cudaMemsetAsync(ctx->sp.count, 0, sizeof(int) * (size_t)ctx->sp.cap, st));
   CK(cudaMemsetAsync(ctx->sp.acc, 0, sizeof(long long) * 8 * (size_t)ctx->sp.cap, st));
-  LAUNCH(k_accumulate, (long long)H * ((W + 15) / 16), img, seg, H, W, ctx->sp);
+  LAUNCHG(k_accumulate, (unsigned)(((long long)H * ((W + 7) / 8) + 127) / 128), 128, img, seg, H,
+          W, ctx->sp);
   LAUNCH(k_init_prior_mu, ctx->sp.cap, ctx->sp, &ctx->sc->nspix);
   LAUNCH(k_find_border, npix, seg, ctx->border, H, W);
   if ((r = bass_loop(ctx, st, f, cfg.niters, stop_after, extra_update))) return r;
@@ -498,6 +567,7 @@ int shift_fill(stspix_ctx* ctx, cudaStream_t st, const int* prev, const stspix_p
   const int npix = H * W;
   int r;
   if ((r = ensure(ctx, npix, std::max(10 * n_prev + 2, 64)))) return r;
+  ctx->cur_fam = STSPIX_FAM_PROP;
   CK(cudaMemsetAsync(ctx->cnt_pool, 0, sizeof(int) * (size_t)n_prev, st));
   CK(cudaMemsetAsync(ctx->fs, 0, sizeof(long long) * 2 * (size_t)n_prev, st));
   LAUNCH(k_flow_pool, (long long)H * ((W + 15) / 16), prev, flow, H, W, n_prev, ctx->cnt_pool,
@@ -545,6 +615,7 @@ int prop_frame(stspix_ctx* ctx, cudaStream_t st, const float* img, int H, int W,
   int r;
   if ((r = ensure(ctx, npix, std::max(10 * n_prev + 2, 64)))) return r;
   Frame f{img, seg, H, W, npix, cfg, sm_constants(cfg), shifted, 1, n_prev, prev.prior_mu_app};
+  ctx->cur_fam = STSPIX_FAM_OTHER;
   LAUNCH1(k_frame_begin, ctx->sc, n_prev - 1, 10 * n_prev);
   LAUNCH(k_write_params, ctx->sp.cap, ctx->sp, prev, n_prev, cfg.sp_size);
   LAUNCH(k_mark_active, npix, seg, npix, ctx->sp);
@@ -559,6 +630,7 @@ int sync_scalars(stspix_ctx* ctx, cudaStream_t st) {
   CK(cudaMemcpyAsync(ctx->sc_host, ctx->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
+  prof_harvest(ctx);
   const Scalars& s = *ctx->sc_host;
   ctx->log.nsplits = s.nsplits;
   ctx->log.nmerges = s.nmerges;
@@ -616,11 +688,14 @@ int stspix_create(stspix_ctx** out, int device) {
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
   int nb = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k_relax_bfs, kThreads, 0);
-  ctx->coop_relax0 = nb * ctx->num_sms;
+  // Cooperative grids use at most one block per SM: with up to
+  // (resident blocks per SM) streams launching cooperative kernels at once, all of
+  // their blocks can still be resident together (other kernels always drain).
+  ctx->coop_relax0 = std::min(nb, 1) * ctx->num_sms;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k_relax_cc, kThreads, 0);
-  ctx->coop_relax1 = nb * ctx->num_sms;
+  ctx->coop_relax1 = std::min(nb, 1) * ctx->num_sms;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k_fill_coop, kThreads, 0);
-  ctx->coop_fill = nb * ctx->num_sms;
+  ctx->coop_fill = std::min(nb, 1) * ctx->num_sms;
   if (!coop || ctx->coop_relax0 <= 0 || ctx->coop_fill <= 0) {
     delete ctx;
     return STSPIX_ERR_CUDA;
@@ -646,6 +721,9 @@ int stspix_destroy(stspix_ctx* ctx) {
   free_list(ctx->pix_bufs);
   free_list(ctx->sp_bufs);
   free_list(ctx->pp_bufs);
+  prof_harvest(ctx);
+  for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.first); ctx->ev_free.push_back(e.second); }
+  for (auto e : ctx->ev_free) cudaEventDestroy(e);
   cudaFree(ctx->round_flags);
   cudaFree(ctx->iter_counts);
   cudaFree(ctx->sc);
@@ -797,9 +875,14 @@ int stspix_bist_forward(stspix_ctx* ctx, void* stream, const float* vid, const f
   int cur = 0;    // ping-pong index of the current frame's params
   int n_prev = 0;
   int status = STSPIX_OK;
+  for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.first); ctx->ev_free.push_back(e.second); }
+  ctx->frame_ev.clear();
+  ctx->frame_ms.clear();
   for (int fi = 0; fi < T; fi++) {
     const float* img = vid + (size_t)fi * npix * 3;
     int* seg = spix_out + (size_t)fi * npix;
+    cudaEvent_t fe0 = ev_get(ctx), fe1 = ev_get(ctx);
+    cudaEventRecord(fe0, st);
     if (fi == 0 || !video_mode) {
       // params are only needed by the next frame in video mode
       if ((r = bass_frame(ctx, st, img, H, W, *cfg, seg, nullptr, -1, 0))) return r;
@@ -839,13 +922,43 @@ int stspix_bist_forward(stspix_ctx* ctx, void* stream, const float* vid, const f
       cur = nxt;
       ctx->log.niters = niters;
     }
+    cudaEventRecord(fe1, st);
+    ctx->frame_ev.push_back({fe0, fe1});
   }
   if (!video_mode) {
     if ((r = sync_scalars(ctx, st))) return r;
     if (ctx->sc_host->status) status = ctx->sc_host->status;
   }
+  CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
+  prof_harvest(ctx);
+  for (auto& e : ctx->frame_ev) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e.first, e.second);
+    ctx->frame_ms.push_back(ms);
+  }
   return status ? fail(ctx, status, "device status %d", status) : STSPIX_OK;
+}
+
+int stspix_profile_enable(stspix_ctx* ctx, int enable) {
+  if (!ctx) return STSPIX_ERR_ARG;
+  ctx->prof_on = enable ? 1 : 0;
+  for (int i = 0; i < STSPIX_NFAM; i++) { ctx->fam_launches[i] = 0; ctx->fam_ms[i] = 0; }
+  return STSPIX_OK;
+}
+
+int stspix_profile_get(const stspix_ctx* ctx, int family, long long* launches, double* total_ms) {
+  if (!ctx || family < 0 || family >= STSPIX_NFAM) return STSPIX_ERR_ARG;
+  if (launches) *launches = ctx->fam_launches[family];
+  if (total_ms) *total_ms = ctx->fam_ms[family];
+  return STSPIX_OK;
+}
+
+int stspix_frame_times(const stspix_ctx* ctx, double* ms_out, int capacity) {
+  if (!ctx) return -1;
+  int n = (int)ctx->frame_ms.size();
+  for (int i = 0; i < n && i < capacity && ms_out; i++) ms_out[i] = ctx->frame_ms[i];
+  return n;
 }
 
 int stspix_get_marked_video(stspix_ctx* ctx, void* stream, const float* vid, const int32_t* spix,

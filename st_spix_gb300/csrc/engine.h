@@ -28,14 +28,24 @@ constexpr int kMaxCoopRounds = 1 << 14;   // cap of the relaxation loops
 constexpr int kFillBreakIter = 1000;      // fill_missing.cu: break_iter
 constexpr long long kBarrierSpinLimit = 1LL << 24;
 
-// Packed record read by the boundary sweep: exactly the fields calc_joint reads
-// (update_seg.cu:194-259), already converted to the types it uses.
+// Packed record read by the boundary sweep: the fields calc_joint reads
+// (update_seg.cu:194-259), already converted to the types it uses.  The reference
+// truncates d0 = (int)(x - mu_x) in double; since x - mu_x is exact in double for
+// |x - mu_x| < 2^13, trunc(x - mu_x) = k - (k >= 1 && frac) with k = x - floor(mu_x),
+// so the record carries floor(mu) and a has-fraction flag and the sweep needs no FP64.
 struct __align__(16) SweepRec {
   float mu_r, mu_g, mu_b, logdet;  // mean colour, (float) log det Sigma
-  double mu_x, mu_y;               // mean position (double: d0 is truncated from it)
-  float isx, isy, isz;             // (float) inverse shape covariance
+  int mxi, myi;                    // floor(mu_x), floor(mu_y)
+  int frac;                        // bit0: mu_x not integral, bit1: mu_y not integral
   int count;                       // pixel count
+  float isx, isy, isz, pad;        // (float) inverse shape covariance
 };
+
+// Per-superpixel kernels spread consecutive ids over blocks (live ids are the low
+// ones, and the FP64 work per id is heavy on this part): id = block + grid * j.
+__device__ __forceinline__ int spread_id(int j) { return blockIdx.x + gridDim.x * j; }
+#define FOR_SP(k, n)                                                              \
+  for (int j_ = threadIdx.x, k = spread_id(j_); k < (n); j_ += blockDim.x, k = spread_id(j_))
 
 // Per-superpixel working state, structure of arrays, `cap` entries each.
 struct SpDev {
@@ -71,6 +81,13 @@ struct SmDev {
   int* newid;
   uint8_t* flag;     // bit0 accept/want, bit1 merge, bit2 remove, bit3 select, bit4 has_single
   double* msingle;
+};
+
+// Split/merge constants computed once on the host (split_merge_orig.cu:97-106):
+// b_0 = 2 sqrt(sigma2_app) a_0 (a_0 = 1e4), log alpha, log(0.1) - log b_0 and
+// lc = 0.5 log(pi) + log 2.
+struct SmConsts {
+  double b0, log_alpha, log_01_b0, lc;
 };
 
 // Frame-level device scalars.

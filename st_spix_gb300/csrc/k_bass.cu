@@ -175,7 +175,7 @@ __global__ void k_init_prior_mu(SpDev sp, const int* __restrict__ nspix_ptr) {
 // Each thread owns a run of kRun pixels of one row, accumulates in registers while
 // the label stays the same and flushes one set of 64-bit atomics per label run;
 // position sums of a run are closed-form.
-constexpr int kRun = 16;
+constexpr int kRun = 8;
 
 __device__ __forceinline__ void flush_run(SpDev& sp, int k, int y, int x0, int x1,
                                           long long sr, long long sg, long long sb) {
@@ -233,9 +233,7 @@ __device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in
   *oz = (pc * sp_size + count * in_z) / (total_count + 3.0);
 }
 
-__global__ void k_posterior(SpDev sp, int sp_size, Scalars* sc) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= sp.cap) return;
+__device__ __forceinline__ void posterior_one(SpDev& sp, int sp_size, Scalars* sc, int k) {
   int count_int = sp.count[k];
   bool live = sp.valid[k] && count_int > 0;
   if (sp.valid[k] && count_int <= 0) sp.valid[k] = 0;
@@ -284,16 +282,22 @@ __global__ void k_posterior(SpDev sp, int sp_size, Scalars* sc) {
   sp.logdet[k] = ld;
   SweepRec r;
   r.mu_r = mr; r.mu_g = mg; r.mu_b = mb; r.logdet = (float)ld;
-  r.mu_x = mx; r.mu_y = my;
-  r.isx = (float)ix; r.isy = (float)iy; r.isz = (float)iz;
+  double fx = floor(mx), fy = floor(my);
+  r.mxi = (int)fx; r.myi = (int)fy;
+  r.frac = (mx != fx ? 1 : 0) | (my != fy ? 2 : 0);
+  r.isx = (float)ix; r.isy = (float)iy; r.isz = (float)iz; r.pad = 0.f;
   r.count = count_int;
   sp.rec[k] = r;
 }
 
+__global__ void k_posterior(SpDev sp, int sp_size, Scalars* sc) {
+  FOR_SP(k, sp.cap) posterior_one(sp, sp_size, sc, k);
+}
+
 // store_sample_sigma_shape_k (update_params.cu:397-438).
 __global__ void k_store_sample(SpDev sp) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= sp.cap || !sp.valid[k]) return;
+  FOR_SP(k, sp.cap) {
+  if (!sp.valid[k]) continue;
   const long long* a = sp.acc + 8 * (size_t)k;
   double count = sp.count[k] * 1.0;
   double mx = a[3] / count, my = a[4] / count;
@@ -310,6 +314,7 @@ __global__ void k_store_sample(SpDev sp) {
   sp.sample_sigma_shape[3 * k] = sx;
   sp.sample_sigma_shape[3 * k + 1] = sy;
   sp.sample_sigma_shape[3 * k + 2] = sz;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -381,7 +386,7 @@ __constant__ unsigned char c_simple_lut[256] = {
     1, 0, 0, 0, 1, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 1,
     0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 1, 1, 0, 0, 1, 1, 0, 0};
 
-__device__ __forceinline__ bool simple_point(const int nb[8], int label, int* diff) {
+__device__ __forceinline__ int nbr_code(const int nb[8], int label, int* diff) {
   int num = 0, d = 0;
 #pragma unroll
   for (int i = 7; i >= 0; i--) {
@@ -390,7 +395,17 @@ __device__ __forceinline__ bool simple_point(const int nb[8], int label, int* di
     if (b) num++; else d++;
   }
   *diff = d;
-  return c_simple_lut[num] != 0;
+  return num;
+}
+__device__ __forceinline__ bool simple_point(const int nb[8], int label, int* diff) {
+  return c_simple_lut[nbr_code(nb, label, diff)] != 0;
+}
+// Same test against the table packed as 8 words in shared memory (divergent
+// constant-memory reads serialise across a warp).
+__device__ __forceinline__ bool simple_point_s(const unsigned* lut_bits, const int nb[8],
+                                               int label, int* diff) {
+  int num = nbr_code(nb, label, diff);
+  return (lut_bits[num >> 5] >> (num & 31)) & 1u;
 }
 
 __device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int y,
@@ -400,8 +415,9 @@ __device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int 
   const float x0 = pix[0] - r.mu_r;
   const float x1 = pix[1] - r.mu_g;
   const float x2 = pix[2] - r.mu_b;
-  const int d0 = (int)(x - r.mu_x);
-  const int d1 = (int)(y - r.mu_y);
+  int d0 = x - r.mxi, d1 = y - r.myi;   // == (int)(x - mu_x), see SweepRec
+  if ((r.frac & 1) && d0 >= 1) d0 -= 1;
+  if ((r.frac & 2) && d1 >= 1) d1 -= 1;
   res = res - (x0 * x0 + x1 * x1 + x2 * x2) / s2;
   res = res - (float)(d0 * d0) * r.isx - (float)(d1 * d1) * r.isz - (float)(2 * d0 * d1) * r.isy;
   res = res - r.logdet;
@@ -462,6 +478,118 @@ __global__ void k_update_phase(const float* __restrict__ img, int* seg,
   if (i >= hw * hh) return;
   int x = 2 * (i % hw) + xmod, y = 2 * (i / hw) + ymod;
   update_pixel(img, seg, border, rec, cap, x, y, H, W, s2, potts);
+}
+
+// ---------------------------------------------------------------------------
+// Fused sweep: border pass + the four parity phases of one sweep in one launch.
+// A block owns a 32x32 tile and stages labels of the tile plus a 4-pixel halo
+// (phase k is evaluated on the tile grown by 3-k pixels, so every label a tile
+// pixel depends on is produced inside the block exactly as the four separate
+// launches produce it), the image and the border mask of the tile plus 3 pixels.
+// Labels are read from seg_in (labels at the sweep start) and the tile is
+// written to seg_out, so neighbouring blocks never see each other's updates.
+constexpr int kST = 32;               // tile side
+constexpr int kSH = 4;                // label halo
+constexpr int kSL = kST + 2 * kSH;    // 40: staged label side
+constexpr int kSI = kST + 2 * (kSH - 1);  // 38: staged image / border side
+
+__global__ void __launch_bounds__(256) k_sweep_fused(const float* __restrict__ img,
+                                                     const int* __restrict__ seg_in,
+                                                     int* __restrict__ seg_out,
+                                                     const SweepRec* __restrict__ rec, int cap,
+                                                     int H, int W, float s2, float potts) {
+  __shared__ int L[kSL * kSL];
+  __shared__ float I[kSI * kSI * 3];
+  __shared__ uint8_t B[kSI * kSI];
+  __shared__ unsigned lut_bits[8];
+  if (threadIdx.x < 8) {
+    unsigned w = 0;
+    for (int b = 0; b < 32; b++) w |= (unsigned)(c_simple_lut[threadIdx.x * 32 + b] != 0) << b;
+    lut_bits[threadIdx.x] = w;
+  }
+  const int tx0 = blockIdx.x * kST, ty0 = blockIdx.y * kST;
+  const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;        // label region origin
+  const int ix0 = tx0 - (kSH - 1), iy0 = ty0 - (kSH - 1);  // image region origin
+  for (int i = threadIdx.x; i < kSL * kSL; i += blockDim.x) {
+    int gx = rx0 + i % kSL, gy = ry0 + i / kSL;
+    L[i] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? seg_in[gy * W + gx] : -1;
+  }
+  for (int i = threadIdx.x; i < kSI * kSI; i += blockDim.x) {
+    int gx = ix0 + i % kSI, gy = iy0 + i / kSI;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      const float* p = img + 3 * ((size_t)gy * W + gx);
+      I[3 * i] = p[0]; I[3 * i + 1] = p[1]; I[3 * i + 2] = p[2];
+    }
+  }
+  __syncthreads();
+  // border mask at the sweep start (find_border_pixels, seg_utils.cu:164-195)
+  for (int i = threadIdx.x; i < kSI * kSI; i += blockDim.x) {
+    int lx = i % kSI, ly = i / kSI;
+    int gx = ix0 + lx, gy = iy0 + ly;
+    uint8_t b = 0;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      if (gy < 1 || gx < 1 || gy >= H - 1 || gx >= W - 1) {
+        b = 1;
+      } else {
+        int p = (ly + 1) * kSL + (lx + 1);
+        int C = L[p];
+        b = (C != L[p - kSL] || C != L[p + kSL] || C != L[p + 1] || C != L[p - 1]) ? 1 : 0;
+      }
+    }
+    B[i] = b;
+  }
+  __syncthreads();
+  for (int ph = 0; ph < 4; ph++) {
+    const int xm = ph >> 1, ym = ph & 1;
+    const int grow = 3 - ph;  // region = tile grown by `grow` pixels
+    const int side = kST + 2 * grow;
+    const int half = side / 2;  // side is even; one pixel of each parity per 2x2
+    for (int i = threadIdx.x; i < half * half; i += blockDim.x) {
+      // region origin (tile origin - grow) has the parity of `grow`
+      int ox = tx0 - grow, oy = ty0 - grow;
+      int gx = ox + 2 * (i % half) + ((xm - ox) & 1);
+      int gy = oy + 2 * (i / half) + ((ym - oy) & 1);
+      if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+      int lx = gx - rx0, ly = gy - ry0;     // in label coordinates
+      int p = ly * kSL + lx;
+      int bi = (gy - iy0) * kSI + (gx - ix0);
+      if (!B[bi]) continue;
+      int C = L[p];
+      if (C < 0 || C >= cap) continue;
+      const int N = L[p - kSL], S = L[p + kSL], Wl = L[p - 1], E = L[p + 1];
+      const int NW = L[p - kSL - 1], NE = L[p - kSL + 1], SW = L[p + kSL - 1],
+                SE = L[p + kSL + 1];
+      const int nb[8] = {NW, N, NE, Wl, E, SW, S, SE};
+      int dN, dW, dS, dE;
+      bool vN = simple_point_s(lut_bits, nb, N, &dN);
+      bool vW = simple_point_s(lut_bits, nb, Wl, &dW);
+      bool vS = simple_point_s(lut_bits, nb, S, &dS);
+      bool vE = simple_point_s(lut_bits, nb, E, &dE);
+      if (!vN || !vW || !vS || !vE) continue;
+      if (N >= cap || S >= cap || Wl >= cap || E >= cap) continue;
+      const float* pix = &I[3 * bi];
+      float best = -9999.f;
+      int bl = C;
+      if (N >= 0) joint(pix, gx, gy, rec[N], N, s2, (float)dN, potts, &best, &bl);
+      if (S != N && S >= 0) joint(pix, gx, gy, rec[S], S, s2, (float)dS, potts, &best, &bl);
+      if (Wl != S && Wl != N && Wl >= 0)
+        joint(pix, gx, gy, rec[Wl], Wl, s2, (float)dW, potts, &best, &bl);
+      if (E != Wl && E != S && E != N && E >= 0)
+        joint(pix, gx, gy, rec[E], E, s2, (float)dE, potts, &best, &bl);
+      if (rec[C].count <= 2 && bl == C) {
+        if (N >= 0) bl = N;
+        else if (E >= 0) bl = E;
+        else if (S >= 0) bl = S;
+        else if (Wl >= 0) bl = Wl;
+      }
+      L[p] = bl;
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < kST * kST; i += blockDim.x) {
+    int gx = tx0 + i % kST, gy = ty0 + i / kST;
+    if (gx < W && gy < H) seg_out[gy * W + gx] = L[(gy - ry0) * kSL + (gx - rx0)];
+  }
 }
 
 // ---------------------------------------------------------------------------

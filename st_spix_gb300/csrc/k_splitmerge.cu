@@ -218,32 +218,31 @@ __global__ void k_sm_accumulate(const float* __restrict__ img, const int* __rest
   flush();
 }
 
-// Hastings terms (split_merge_orig.cu:536-549, 845-877) in FP64; the lgamma(a_n)
-// terms of numerator and denominator are identical and cancel.
-__device__ __forceinline__ double marginal_channel(double n, double b0, double bn) {
+// Marginal of one superpixel over the three colour channels, FP64: the
+// reference's numerator - denominator (split_merge_orig.cu:536-549, 845-877) with
+// the identical lgamma(a_n) terms cancelled and log b_0 - log b_n evaluated as
+// -log1p((b_n - b_0) / b_0); b_n = b_0 + 0.5 (sum v^2 - (sum v)^2 / n)
+// (:480-501).  `clamp` is the merge path's b_n < 0 -> 0.1 rule.
+__device__ __forceinline__ double total_marginal(double n, const SmConsts& K, const long long* s,
+                                                 const long long* sq, bool clamp) {
   const double a_n = 1e4 + n / 2;
-  return a_n * (log(b0) - log(bn)) + 0.5 * log(1.0 / n) -
-         (0.5 * n * log(3.14159265358979323846) + n * log(2.0));
-}
-__device__ __forceinline__ double total_marginal(double n, double b0, const long long* s,
-                                                 int s_stride, const long long* sq, bool clamp) {
   double t = 0;
   for (int c = 0; c < 3; c++) {
-    double S = fx_unq(s[c * s_stride], kFxAppShift), Q = fx_unq(sq[c], kFxSqShift);
-    double bn = b0 + 0.5 * (Q - S * S / n);
-    if (clamp && bn < 0) bn = 0.1;
-    t += marginal_channel(n, b0, bn);
+    double S = fx_unq(s[c], kFxAppShift), Q = fx_unq(sq[c], kFxSqShift);
+    double d = 0.5 * (Q - S * S / n);
+    double lr = (clamp && K.b0 + d < 0) ? K.log_01_b0 : log1p(d / K.b0);
+    t += -a_n * lr;
   }
-  return t;
+  return t + 3 * (-0.5 * log(n) - n * K.lc);
 }
 __device__ __forceinline__ bool near_tie(double h) { return fabs(h + 2.0) < 1e-6; }
 
 // update_split_flag (split_merge_orig.cu:900-986) / update_split_flag_p
 // (split_merge_prop.cu:3026-3149): decision only; ids by scan afterwards (R2).
-__global__ void k_split_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, float split_alpha,
-                               int prop_mode, uint8_t* __restrict__ accept) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= sp.cap) return;
+__device__ __forceinline__ void split_decide_one(SpDev& sp, SmDev& sm, Scalars* sc,
+                                                 const SmConsts& K, float split_alpha,
+                                                 int prop_mode, uint8_t* __restrict__ accept,
+                                                 int k) {
   accept[k] = 0;
   if (!sc->tmp0 || !sp.valid[k]) return;
   const int off = sc->tmp1;
@@ -254,9 +253,9 @@ __global__ void k_split_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, float
   if (count_f != count_k + count_s) return;
   long long sq_f[3];
   for (int c = 0; c < 3; c++) sq_f[c] = sm.sq[3 * (size_t)k + c] + sm.sq[3 * (size_t)s + c];
-  double mk = total_marginal(count_k, b0, &sm.s[3 * (size_t)k], 1, &sm.sq[3 * (size_t)k], false);
-  double ms = total_marginal(count_s, b0, &sm.s[3 * (size_t)s], 1, &sm.sq[3 * (size_t)s], false);
-  double mf = total_marginal(count_f, b0, sp.acc + 8 * (size_t)k, 1, sq_f, false);
+  double mk = total_marginal(count_k, K, &sm.s[3 * (size_t)k], &sm.sq[3 * (size_t)k], false);
+  double ms = total_marginal(count_s, K, &sm.s[3 * (size_t)s], &sm.sq[3 * (size_t)s], false);
+  double mf = total_marginal(count_f, K, sp.acc + 8 * (size_t)k, sq_f, false);
   double h = mk + ms - mf + split_alpha;
   uint8_t fl = 1;
   if (prop_mode) {
@@ -273,6 +272,11 @@ __global__ void k_split_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, float
   }
   if (near_tie(h)) atomicAdd(&sc->near_ties, 1);
   if (h > -2) accept[k] = fl;
+}
+
+__global__ void k_split_decide(SpDev sp, SmDev sm, Scalars* sc, SmConsts K, float split_alpha,
+                               int prop_mode, uint8_t* __restrict__ accept) {
+  FOR_SP(k, sp.cap) split_decide_one(sp, sm, sc, K, split_alpha, prop_mode, accept, k);
 }
 
 // Split commit: new id = max_spix + 1 + rank (R2), prior counts.
@@ -365,21 +369,20 @@ __global__ void k_merge_candidates(const int* __restrict__ seg, const uint8_t* _
 
 // Single-superpixel marginal, present only when k has its own candidate
 // (calc_merge_stats_step0 computes b_n only then; split_merge_orig.cu:456-520).
-__global__ void k_merge_single(SpDev sp, SmDev sm, double b0) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= sp.cap) return;
-  sm.flag[k] = 0;
-  if (!sp.valid[k] || sm.pair[k] < 0) return;
-  sm.msingle[k] = total_marginal(sp.count[k], b0, sp.acc + 8 * (size_t)k, 1,
-                                 &sm.sq[3 * (size_t)k], true);
-  sm.flag[k] = 16;
+__global__ void k_merge_single(SpDev sp, SmDev sm, SmConsts K) {
+  FOR_SP(k, sp.cap) {
+    sm.flag[k] = 0;
+    if (!sp.valid[k] || sm.pair[k] < 0) continue;
+    sm.msingle[k] = total_marginal(sp.count[k], K, sp.acc + 8 * (size_t)k,
+                                   &sm.sq[3 * (size_t)k], true);
+    sm.flag[k] = 16;
+  }
 }
 
 // calc_merge_stats_step2 + update_merge_flag (split_merge_orig.cu:555-656), R3.
-__global__ void k_merge_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, double log_alpha,
-                               float merge_alpha) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= sp.cap || !sp.valid[k]) return;
+__device__ __forceinline__ void merge_decide_one(SpDev& sp, SmDev& sm, Scalars* sc,
+                                                 const SmConsts& K, float merge_alpha, int k) {
+  if (!sp.valid[k]) return;
   int f = sm.pair[k];
   if (f < 0 || !sp.valid[f]) return;
   double count_k = sp.count[k];
@@ -394,14 +397,18 @@ __global__ void k_merge_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, doubl
   if (!(sm.flag[f] & 16)) {
     h = -INFINITY;
   } else {
-    double m_merged = total_marginal(count_f, b0, s_f, 1, sq_f, true);
-    h = m_merged - (log_alpha + sm.msingle[k] + sm.msingle[f]) + merge_alpha;
+    double m_merged = total_marginal(count_f, K, s_f, sq_f, true);
+    h = m_merged - (K.log_alpha + sm.msingle[k] + sm.msingle[f]) + merge_alpha;
   }
   if (near_tie(h)) atomicAdd(&sc->near_ties, 1);
   if (h > -2) {
     sm.flag[k] |= 1;  // only thread k writes flag[k] here; readers use bit 16 only
     atomicMin(&sm.claim[f], k);
   }
+}
+
+__global__ void k_merge_decide(SpDev sp, SmDev sm, Scalars* sc, SmConsts K, float merge_alpha) {
+  FOR_SP(k, sp.cap) merge_decide_one(sp, sm, sc, K, merge_alpha, k);
 }
 
 // merge flag := accepted and claimant of its target; snapshot valid; target := pair.

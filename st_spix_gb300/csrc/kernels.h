@@ -26,6 +26,8 @@ __global__ void k_overlay(float* out, const float* img, const float* color,
 __global__ void k_update_phase(const float* img, int* seg, const uint8_t* border,
                                const SweepRec* rec, int cap, int H, int W, int xmod, int ymod,
                                float s2, float potts);
+__global__ void k_sweep_fused(const float* img, const int* seg_in, int* seg_out,
+                              const SweepRec* rec, int cap, int H, int W, float s2, float potts);
 __global__ void k_read_params(SpDev sp, const int* n_ptr, stspix_params out);
 __global__ void k_dump_state(SpDev sp, stspix_state_dump d);
 
@@ -41,7 +43,7 @@ __global__ void k_split_partition(const int* seg, const int* d1, const int* d2, 
                                   const Scalars* sc, int* sm);
 __global__ void k_sm_accumulate(const float* img, const int* lab, const int* shifted, int H,
                                 int W, int cap, SmDev sm);
-__global__ void k_split_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, float split_alpha,
+__global__ void k_split_decide(SpDev sp, SmDev sm, Scalars* sc, SmConsts K, float split_alpha,
                                int prop_mode, uint8_t* accept);
 __global__ void k_split_commit(SpDev sp, SmDev sm, Scalars* sc, const uint8_t* accept,
                                const int* excl, int prop_mode);
@@ -51,9 +53,8 @@ __global__ void k_split_end(Scalars* sc, const int* nsplits);
 __global__ void k_merge_candidates(const int* seg, const uint8_t* border, int H, int W,
                                    int direction, int prop_mode, const uint8_t* prop, int cap,
                                    int* pair);
-__global__ void k_merge_single(SpDev sp, SmDev sm, double b0);
-__global__ void k_merge_decide(SpDev sp, SmDev sm, Scalars* sc, double b0, double log_alpha,
-                               float merge_alpha);
+__global__ void k_merge_single(SpDev sp, SmDev sm, SmConsts K);
+__global__ void k_merge_decide(SpDev sp, SmDev sm, Scalars* sc, SmConsts K, float merge_alpha);
 __global__ void k_merge_flag(SpDev sp, SmDev sm, uint8_t* valid0);
 __global__ void k_merge_remove(SpDev sp, SmDev sm, Scalars* sc, const uint8_t* valid0,
                                int prop_mode);

@@ -198,3 +198,41 @@ def test_input_checks():
     nc = torch.zeros((1, 8, 8, 2), device="cuda").transpose(1, 2)
     with pytest.raises(RuntimeError):
         bist_cuda.bist_forward(g, nc, 4, 15, 0.5, 1e-4, -0.69, 0.0, False, False)
+
+
+def test_concurrent_streams_match_sequential():
+    """Four host threads, each with its own CUDA stream and engine context, process
+    four different videos at once; every result equals the single-stream run."""
+    import threading
+    vids = [small_video(T=3, seed=s) for s in range(4)]
+    seq = []
+    for v, f in vids:
+        seq.append(bist_cuda.bist_forward(cuda(v), cuda(f), 10, 15, 0.5, 0.009 ** 2,
+                                          float(np.log(0.5)), 0.0, True, False).cpu().numpy())
+    out = [None] * 4
+    err = []
+    gate = threading.Barrier(4)
+
+    def run(i):
+        try:
+            s = torch.cuda.Stream()
+            v, f = vids[i]
+            with torch.cuda.stream(s):
+                gv, gf = cuda(v), cuda(f)
+                gate.wait()
+                for _ in range(3):
+                    o = bist_cuda.bist_forward(gv, gf, 10, 15, 0.5, 0.009 ** 2,
+                                               float(np.log(0.5)), 0.0, True, False)
+                s.synchronize()
+                out[i] = o.cpu().numpy()
+        except Exception as e:  # pragma: no cover - reported below
+            err.append(repr(e))
+
+    th = [threading.Thread(target=run, args=(i,)) for i in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not err, err
+    for i in range(4):
+        np.testing.assert_array_equal(out[i], seq[i])
