@@ -288,7 +288,7 @@ def main():
             raise RuntimeError("; ".join(errs))
 
     def warm(i, st):
-        ctxs[i] = bist_cuda._ctx(dev)
+        ctxs[i] = bist_cuda._ctx(dev)  # the context of stream i (one per CUDA stream)
         call(dvid[i], dflo[i])
 
     run_all(warm, args.warmup)
@@ -324,8 +324,7 @@ def main():
 
     # ---- per-family device time, one stream alone, CUDA events on its stream ----
     with torch.cuda.stream(streams[0]):
-        ctx0 = bist_cuda._ctx(dev)  # the main thread's own context
-        call(dvid[0], dflo[0])      # warm it
+        ctx0 = bist_cuda._ctx(dev)  # stream 0's context
         ctx0.profile(True)
         for _ in range(args.steps):
             call(dvid[0], dflo[0])

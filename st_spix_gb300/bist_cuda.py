@@ -23,17 +23,20 @@ import torch
 
 from . import _lib
 
-_tls = threading.local()
+_ctx_lock = threading.Lock()
+_contexts = {}
 
 
 def _ctx(device: torch.device) -> _lib.Context:
+    """The engine context (device workspace) of torch's current stream on `device`:
+    one per CUDA stream, so concurrent streams never share a workspace."""
     idx = device.index if device.index is not None else torch.cuda.current_device()
-    cache = getattr(_tls, "ctx", None)
-    if cache is None:
-        cache = _tls.ctx = {}
-    if idx not in cache:
-        cache[idx] = _lib.Context(idx)
-    return cache[idx]
+    key = (idx, torch.cuda.current_stream(idx).cuda_stream)
+    with _ctx_lock:
+        c = _contexts.get(key)
+        if c is None:
+            c = _contexts[key] = _lib.Context(idx)
+        return c
 
 
 def _check_input(x: torch.Tensor, name: str):

@@ -498,15 +498,18 @@ __global__ void __launch_bounds__(256) k_sweep_fused(const float* __restrict__ i
                                                      int* __restrict__ seg_out,
                                                      const SweepRec* __restrict__ rec, int cap,
                                                      int H, int W, float s2, float potts) {
+  constexpr int kMaxList = (kST / 2 + kSH - 1) * (kST / 2 + kSH - 1);  // 19 x 19
   __shared__ int L[kSL * kSL];
   __shared__ float I[kSI * kSI * 3];
-  __shared__ uint8_t B[kSI * kSI];
+  __shared__ short list[4][kMaxList];   // border pixels of each parity phase
+  __shared__ int cnt[4];
   __shared__ unsigned lut_bits[8];
   if (threadIdx.x < 8) {
     unsigned w = 0;
     for (int b = 0; b < 32; b++) w |= (unsigned)(c_simple_lut[threadIdx.x * 32 + b] != 0) << b;
     lut_bits[threadIdx.x] = w;
   }
+  if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
   const int tx0 = blockIdx.x * kST, ty0 = blockIdx.y * kST;
   const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;        // label region origin
   const int ix0 = tx0 - (kSH - 1), iy0 = ty0 - (kSH - 1);  // image region origin
@@ -522,38 +525,37 @@ __global__ void __launch_bounds__(256) k_sweep_fused(const float* __restrict__ i
     }
   }
   __syncthreads();
-  // border mask at the sweep start (find_border_pixels, seg_utils.cu:164-195)
+  // Border mask at the sweep start (find_border_pixels, seg_utils.cu:164-195); the
+  // border pixels of parity class k inside the tile grown by 3-k pixels are listed
+  // for phase k, so each phase scores only its border pixels, densely.
   for (int i = threadIdx.x; i < kSI * kSI; i += blockDim.x) {
     int lx = i % kSI, ly = i / kSI;
     int gx = ix0 + lx, gy = iy0 + ly;
-    uint8_t b = 0;
-    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-      if (gy < 1 || gx < 1 || gy >= H - 1 || gx >= W - 1) {
-        b = 1;
-      } else {
-        int p = (ly + 1) * kSL + (lx + 1);
-        int C = L[p];
-        b = (C != L[p - kSL] || C != L[p + kSL] || C != L[p + 1] || C != L[p - 1]) ? 1 : 0;
-      }
+    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+    bool b;
+    if (gy < 1 || gx < 1 || gy >= H - 1 || gx >= W - 1) {
+      b = true;
+    } else {
+      int p = (ly + 1) * kSL + (lx + 1);
+      int C = L[p];
+      b = (C != L[p - kSL] || C != L[p + kSL] || C != L[p + 1] || C != L[p - 1]);
     }
-    B[i] = b;
+    if (!b) continue;
+    int ph = ((gx & 1) << 1) | (gy & 1);
+    int grow = 3 - ph;
+    if (gx < tx0 - grow || gx >= tx0 + kST + grow || gy < ty0 - grow || gy >= ty0 + kST + grow)
+      continue;
+    int slot = atomicAdd(&cnt[ph], 1);
+    list[ph][slot] = (short)i;
   }
   __syncthreads();
   for (int ph = 0; ph < 4; ph++) {
-    const int xm = ph >> 1, ym = ph & 1;
-    const int grow = 3 - ph;  // region = tile grown by `grow` pixels
-    const int side = kST + 2 * grow;
-    const int half = side / 2;  // side is even; one pixel of each parity per 2x2
-    for (int i = threadIdx.x; i < half * half; i += blockDim.x) {
-      // region origin (tile origin - grow) has the parity of `grow`
-      int ox = tx0 - grow, oy = ty0 - grow;
-      int gx = ox + 2 * (i % half) + ((xm - ox) & 1);
-      int gy = oy + 2 * (i / half) + ((ym - oy) & 1);
-      if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
-      int lx = gx - rx0, ly = gy - ry0;     // in label coordinates
-      int p = ly * kSL + lx;
-      int bi = (gy - iy0) * kSI + (gx - ix0);
-      if (!B[bi]) continue;
+    const int n = cnt[ph];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      int bi = list[ph][j];
+      int lxi = bi % kSI, lyi = bi / kSI;
+      int gx = ix0 + lxi, gy = iy0 + lyi;
+      int p = (lyi + 1) * kSL + (lxi + 1);
       int C = L[p];
       if (C < 0 || C >= cap) continue;
       const int N = L[p - kSL], S = L[p + kSL], Wl = L[p - 1], E = L[p + 1];
