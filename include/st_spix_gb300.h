@@ -38,6 +38,7 @@ extern "C" {
 #define STSPIX_ERR_CAPACITY       6   /* superpixel ids exceeded the parameter buffer           */
 #define STSPIX_ERR_BARRIER        7   /* a grid barrier timed out (kernel returned early)       */
 #define STSPIX_ERR_DEGENERATE     8   /* non-positive prior covariance determinant              */
+#define STSPIX_ERR_TOO_LARGE      9   /* input larger than a fixed-size scratch array           */
 
 /* ---- configuration ------------------------------------------------------
  * Defaults (stspix_default_config) are the reference's values:
@@ -148,6 +149,19 @@ int stspix_get_marked_video(stspix_ctx* ctx, void* stream,
                             const float* vid, const int32_t* spix,
                             const float* color, int T, int H, int W, int nftrs,
                             float* marked_out);
+
+/* get_marked_video without any allocation.  No counterpart in the reference: it is
+ * for callers that must not allocate device memory while they run (a process that
+ * reserves its GPU memory up front, code inside someone else's stream capture, a
+ * real-time loop).  The border-mask scratch lives in a 16 MiB array compiled into
+ * the library (held on every GPU that loads it until exit); T*H*W above 2^24 pixels
+ * returns STSPIX_ERR_TOO_LARGE.  No context is needed; it runs on `stream` on the
+ * current device.  All calls share that one array, so calls that overlap on the GPU
+ * race and must be serialised by the caller.  The first call on a device looks up
+ * the array's address; make it before any stream capture.                      */
+int stspix_get_marked_video_noalloc(void* stream, const float* vid, const int32_t* spix,
+                                    const float* color, int T, int H, int W, int nftrs,
+                                    float* marked_out);
 
 /* ---- reference C++ entry points --------------------------------------------- */
 

@@ -57,7 +57,7 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_bist_forward", "stspix_get_marked_video", "stspix_run_bass",
            "stspix_shift_and_fill", "stspix_run_prop", "stspix_init_seg",
            "stspix_find_border", "stspix_bass_partial", "stspix_profile_enable",
-           "stspix_profile_get", "stspix_frame_times"]
+           "stspix_profile_get", "stspix_frame_times", "stspix_get_marked_video_noalloc"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -102,6 +102,7 @@ def load(build_if_missing: bool = True):
             "stspix_profile_enable": (I, [P, I]),
             "stspix_profile_get": (I, [P, I, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
             "stspix_frame_times": (I, [P, C.POINTER(C.c_double), I]),
+            "stspix_get_marked_video_noalloc": (I, [P, P, P, P, I, I, I, I, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
