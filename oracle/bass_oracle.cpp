@@ -1371,4 +1371,112 @@ void oracle_invalidate_disconnected(int32_t* seg, int H, int W, int nspix) {
 
 void oracle_get_frame_log(stspix_frame_log* out) { *out = g_last_log; }
 
+// Stage functions on caller-supplied state, used to pin the restatement against the
+// reference's own kernels (oracle/ref_harness.cpp) on identical inputs.
+
+// update_params (update_params.cu:12-31) given labels and priors.
+int oracle_update_params_given(const float* img, const int32_t* labels, int H, int W, int nbuf,
+                               int sp_size, float sigma2_app, const int* valid, const int* prop,
+                               const float* prior_count, const double* prior_icov,
+                               const double* sample_sigma, int* count_out, float* mu_app_out,
+                               double* mu_shape_out, double* sigma_shape_out,
+                               double* logdet_out, int* valid_out) {
+  Frame f;
+  f.H = H; f.W = W; f.npix = H * W; f.img = img;
+  oracle_default_config(&f.cfg);
+  f.cfg.sp_size = sp_size; f.cfg.sigma2_app = sigma2_app;
+  f.seg.assign(labels, labels + (size_t)H * W);
+  f.sp.init(nbuf);
+  for (int k = 0; k < nbuf; k++) {
+    f.sp.valid[k] = valid[k] ? 1 : 0;
+    f.sp.prop[k] = prop[k] ? 1 : 0;
+    f.sp.prior_count[k] = prior_count[k];
+    for (int c = 0; c < 3; c++) {
+      f.sp.prior_icov[3 * k + c] = prior_icov[3 * k + c];
+      f.sp.sample_sigma_shape[3 * k + c] = sample_sigma[3 * k + c];
+    }
+  }
+  update_params(f);
+  for (int k = 0; k < nbuf; k++) {
+    count_out[k] = f.sp.count[k];
+    valid_out[k] = f.sp.valid[k];
+    logdet_out[k] = f.sp.logdet[k];
+    for (int c = 0; c < 3; c++) {
+      mu_app_out[3 * k + c] = f.sp.mu_app[3 * k + c];
+      sigma_shape_out[3 * k + c] = f.sp.sigma_shape[3 * k + c];
+    }
+    for (int c = 0; c < 2; c++) mu_shape_out[2 * k + c] = f.sp.mu_shape[2 * k + c];
+  }
+  return f.status;
+}
+
+// update_seg (update_seg.cu:281-311) given parameters; labels updated in place.
+int oracle_update_seg_given(const float* img, int32_t* labels, int H, int W, int nbuf,
+                            int niters_seg, float sigma2_app, float potts, const int* count,
+                            const float* mu_app, const double* mu_shape,
+                            const double* sigma_shape, const double* logdet) {
+  Frame f;
+  f.H = H; f.W = W; f.npix = H * W; f.img = img;
+  oracle_default_config(&f.cfg);
+  f.cfg.niters_seg = niters_seg; f.cfg.sigma2_app = sigma2_app; f.cfg.potts = potts;
+  f.seg.assign(labels, labels + (size_t)H * W);
+  f.border.assign(f.npix, 0);
+  f.sp.init(nbuf);
+  for (int k = 0; k < nbuf; k++) {
+    f.sp.count[k] = count[k];
+    f.sp.logdet[k] = logdet[k];
+    for (int c = 0; c < 3; c++) {
+      f.sp.mu_app[3 * k + c] = mu_app[3 * k + c];
+      f.sp.sigma_shape[3 * k + c] = sigma_shape[3 * k + c];
+    }
+    for (int c = 0; c < 2; c++) f.sp.mu_shape[2 * k + c] = mu_shape[2 * k + c];
+  }
+  update_seg(f);
+  std::copy(f.seg.begin(), f.seg.end(), labels);
+  return 0;
+}
+
+// Split seeds for one direction + BFS distances (split_merge.cu:758-844).
+int oracle_split_bfs(const int32_t* labels, int H, int W, int nbuf, const int* valid,
+                     const double* mu_shape, int direction, int32_t* dist_out) {
+  Frame f;
+  f.H = H; f.W = W; f.npix = H * W;
+  f.seg.assign(labels, labels + (size_t)H * W);
+  f.sp.init(nbuf);
+  for (int k = 0; k < nbuf; k++) {
+    f.sp.valid[k] = valid[k] ? 1 : 0;
+    f.sp.mu_shape[2 * k] = mu_shape[2 * k];
+    f.sp.mu_shape[2 * k + 1] = mu_shape[2 * k + 1];
+  }
+  std::vector<int> d(f.npix, -1);
+  seed_split(f, d, direction);
+  bfs_dist(f, d);
+  std::copy(d.begin(), d.end(), dist_out);
+  return 0;
+}
+
+// Region roots of 8-connected equal-label regions (min pixel index), -1 for holes.
+void oracle_cc_roots(const int32_t* seg, int H, int W, int32_t* roots) {
+  const int npix = H * W;
+  std::vector<int> parent(npix);
+  std::iota(parent.begin(), parent.end(), 0);
+  auto find = [&](int a) {
+    while (parent[a] != a) { parent[a] = parent[parent[a]]; a = parent[a]; }
+    return a;
+  };
+  for (int idx = 0; idx < npix; idx++) {
+    int y = idx / W, x = idx % W;
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) {
+        int yy = y + dy, xx = x + dx;
+        if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+        int q = yy * W + xx;
+        if (seg[q] != seg[idx]) continue;
+        int a = find(idx), b = find(q);
+        if (a != b) { if (a < b) parent[b] = a; else parent[a] = b; }
+      }
+  }
+  for (int i = 0; i < npix; i++) roots[i] = find(i);
+}
+
 }  // extern "C"

@@ -100,6 +100,13 @@ def lib():
                                                  C.POINTER(C.c_int)]
             _lib.oracle_invalidate_disconnected.argtypes = [P, C.c_int, C.c_int, C.c_int]
             _lib.oracle_get_frame_log.argtypes = [C.POINTER(FrameLog)]
+            F = C.c_float
+            _lib.oracle_update_params_given.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                        F, P, P, P, P, P, P, P, P, P, P, P]
+            _lib.oracle_update_seg_given.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                     F, F, P, P, P, P, P]
+            _lib.oracle_split_bfs.argtypes = [P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P]
+            _lib.oracle_cc_roots.argtypes = [P, C.c_int, C.c_int, P]
             _lib.oracle_default_config.argtypes = [C.POINTER(Config)]
     return _lib
 
@@ -253,3 +260,53 @@ def last_log() -> FrameLog:
     lg = FrameLog()
     lib().oracle_get_frame_log(C.byref(lg))
     return lg
+
+
+# Stage functions on caller-supplied state (pinned against the reference's kernels).
+def update_params_given(img, labels, nbuf, sp_size, sigma2_app, valid, prop, prior_count,
+                        prior_icov, sample_sigma):
+    img = np.ascontiguousarray(img, np.float32)
+    labels = np.ascontiguousarray(labels, np.int32)
+    args = [np.ascontiguousarray(valid, np.int32), np.ascontiguousarray(prop, np.int32),
+            np.ascontiguousarray(prior_count, np.float32),
+            np.ascontiguousarray(prior_icov, np.float64),
+            np.ascontiguousarray(sample_sigma, np.float64)]
+    out = dict(count=np.zeros(nbuf, np.int32), mu_app=np.zeros(3 * nbuf, np.float32),
+               mu_shape=np.zeros(2 * nbuf, np.float64),
+               sigma_shape=np.zeros(3 * nbuf, np.float64), logdet=np.zeros(nbuf, np.float64),
+               valid=np.zeros(nbuf, np.int32))
+    H, W = labels.shape
+    lib().oracle_update_params_given(_p(img), _p(labels), H, W, nbuf, sp_size, sigma2_app,
+                                     *[_p(a) for a in args], _p(out["count"]), _p(out["mu_app"]),
+                                     _p(out["mu_shape"]), _p(out["sigma_shape"]),
+                                     _p(out["logdet"]), _p(out["valid"]))
+    return out
+
+
+def update_seg_given(img, labels, nbuf, niters_seg, sigma2_app, potts, count, mu_app, mu_shape,
+                     sigma_shape, logdet):
+    img = np.ascontiguousarray(img, np.float32)
+    lab = np.array(labels, np.int32, copy=True)
+    a = [np.ascontiguousarray(count, np.int32), np.ascontiguousarray(mu_app, np.float32),
+         np.ascontiguousarray(mu_shape, np.float64), np.ascontiguousarray(sigma_shape, np.float64),
+         np.ascontiguousarray(logdet, np.float64)]
+    H, W = lab.shape
+    lib().oracle_update_seg_given(_p(img), _p(lab), H, W, nbuf, niters_seg, sigma2_app, potts,
+                                  *[_p(x) for x in a])
+    return lab
+
+
+def split_bfs(labels, nbuf, valid, mu_shape, direction):
+    labels = np.ascontiguousarray(labels, np.int32)
+    out = np.zeros(labels.shape, np.int32)
+    H, W = labels.shape
+    lib().oracle_split_bfs(_p(labels), H, W, nbuf, _p(np.ascontiguousarray(valid, np.int32)),
+                           _p(np.ascontiguousarray(mu_shape, np.float64)), direction, _p(out))
+    return out
+
+
+def cc_roots(seg):
+    seg = np.ascontiguousarray(seg, np.int32)
+    out = np.zeros(seg.shape, np.int32)
+    lib().oracle_cc_roots(_p(seg), seg.shape[0], seg.shape[1], _p(out))
+    return out

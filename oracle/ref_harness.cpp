@@ -1,0 +1,324 @@
+// ORACLE -- test infrastructure only.  Runs the reference's OWN CUDA kernels (the
+// cubins oracle/ref_build.py compiles from gauenk/st_spix st_spix/csrc/bist/*.cu,
+// unmodified, into oracle/_ref/) through the CUDA driver API, sequenced the way the
+// reference's host functions sequence them, on inputs supplied by the tests.  It is
+// how the CPU oracle is pinned against the reference itself on the GPU host.
+//
+// Host code here is this project's; it mirrors the reference's host loops:
+//   update_seg            update_seg.cu:281-311
+//   update_params         update_params.cu:12-31
+//   init_seg              init_seg.cu:20-46
+//   split BFS             split_merge_orig.cu:262-356 (init_split + calc_split_candidate)
+//   fill_missing          fill_missing.cu:35-130
+//   find_spix_min loop    split_disconnected.cu:107-150
+// The reference's spix_params layout comes from oracle/_ref/spix_layout.h (generated
+// from its structs.h).
+#include <cuda.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "_ref/spix_layout.h"
+
+namespace {
+
+CUcontext g_ctx = nullptr;
+CUmodule g_mod[8] = {};
+std::string g_err;
+
+struct Fn { const char* module; const char* name; CUfunction f; };
+// Mangled names of the reference kernels (C++ signatures in the reference sources).
+Fn g_fn[] = {
+    {"seg_utils", "_Z18find_border_pixelsPKiPbiii", nullptr},
+    {"seg_utils", "_Z22find_border_pixels_endPKiPbiii", nullptr},
+    {"update_seg", "_Z17update_seg_subsetPfPiPbP11spix_paramsffiiiiiii", nullptr},
+    {"update_params", "_Z12clear_fieldsP11spix_paramsP11spix_helperii", nullptr},
+    {"update_params", "_Z12sum_by_labelPKfPKiP11spix_paramsP11spix_helperiiii", nullptr},
+    {"update_params", "_Z18calc_simple_updateP11spix_paramsP11spix_helperfii", nullptr},
+    {"init_seg", "_Z13InitHexCenterPdddiiii", nullptr},
+    {"init_seg", "_Z10InitHexSegPiPdiii", nullptr},
+    {"split_merge", "_Z20calc_split_candidatePiS_PbiS_iiii", nullptr},
+    {"split_merge", "_Z10init_splitPKbPiP11spix_paramsiiiiiPKiS1_i", nullptr},
+    {"fill_missing", "_Z21update_missing_seg_nnPiPdPbiiiiiib", nullptr},
+    {"fill_missing", "_Z25find_border_along_missingPKiPbiiiPi", nullptr},
+    {"split_disconnected", "_Z13find_spix_minPiS_S_S_iii", nullptr},
+};
+enum { F_BORDER, F_BORDER_END, F_UPDATE_SUBSET, F_CLEAR, F_SUM, F_SIMPLE_UPDATE, F_HEX_CENTER,
+       F_HEX_SEG, F_SPLIT_CAND, F_INIT_SPLIT, F_FILL_NN, F_FILL_BORDER, F_SPIX_MIN };
+const char* kModules[] = {"seg_utils", "update_seg", "update_params", "init_seg", "split_merge",
+                          "fill_missing", "split_disconnected"};
+constexpr int kHelperSize = 96;  // sizeof(spix_helper): float3, double3, longlong2, longlong3
+
+#define CU(call)                                                      \
+  do {                                                                \
+    CUresult r_ = (call);                                             \
+    if (r_ != CUDA_SUCCESS) {                                         \
+      const char* s_ = nullptr;                                       \
+      cuGetErrorString(r_, &s_);                                      \
+      g_err = std::string(#call) + ": " + (s_ ? s_ : "?");            \
+      return -1;                                                      \
+    }                                                                 \
+  } while (0)
+
+int launch(int fn, unsigned grid, unsigned block, void** args) {
+  CU(cuLaunchKernel(g_fn[fn].f, grid, 1, 1, block, 1, 1, 0, nullptr, args, nullptr));
+  return 0;
+}
+unsigned nblk(long long n) { return (unsigned)((n + 511) / 512); }  // THREADS_PER_BLOCK 512
+
+struct Dev {
+  CUdeviceptr p = 0;
+  ~Dev() { if (p) cuMemFree(p); }
+};
+int alloc(Dev& d, size_t bytes) {
+  CU(cuMemAlloc(&d.p, bytes ? bytes : 1));
+  return 0;
+}
+
+// Build the reference's AoS spix_params array from SoA fields (nullptr = zero).
+std::vector<unsigned char> pack_params(int n, const int* count, const float* mu_app,
+                                       const double* mu_shape, const double* sigma_shape,
+                                       const double* logdet, const float* prior_count,
+                                       const int* valid, const int* prop,
+                                       const double* prior_icov, const double* sample_sigma) {
+  std::vector<unsigned char> b((size_t)n * REF_SP_SIZE, 0);
+  for (int k = 0; k < n; k++) {
+    unsigned char* e = b.data() + (size_t)k * REF_SP_SIZE;
+    if (mu_app) memcpy(e + REF_OFF_mu_app, mu_app + 3 * k, 12);
+    if (mu_shape) memcpy(e + REF_OFF_mu_shape, mu_shape + 2 * k, 16);
+    if (sigma_shape) memcpy(e + REF_OFF_sigma_shape, sigma_shape + 3 * k, 24);
+    if (logdet) memcpy(e + REF_OFF_logdet_sigma_shape, logdet + k, 8);
+    if (count) memcpy(e + REF_OFF_count, count + k, 4);
+    if (prior_count) memcpy(e + REF_OFF_prior_count, prior_count + k, 4);
+    if (valid) memcpy(e + REF_OFF_valid, valid + k, 4);
+    if (prop) { bool v = prop[k] != 0; memcpy(e + REF_OFF_prop, &v, 1); }
+    if (prior_icov) memcpy(e + REF_OFF_prior_icov, prior_icov + 3 * k, 24);
+    if (sample_sigma) memcpy(e + REF_OFF_sample_sigma_shape, sample_sigma + 3 * k, 24);
+  }
+  return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* refh_error() { return g_err.c_str(); }
+
+int refh_init(const char* dir) {
+  if (g_ctx) return 0;
+  CU(cuInit(0));
+  CUdevice dev;
+  CU(cuDeviceGet(&dev, 0));
+  CU(cuDevicePrimaryCtxRetain(&g_ctx, dev));
+  CU(cuCtxSetCurrent(g_ctx));
+  for (int m = 0; m < 7; m++) {
+    std::string path = std::string(dir) + "/" + kModules[m] + ".cubin";
+    CU(cuModuleLoad(&g_mod[m], path.c_str()));
+  }
+  for (auto& fn : g_fn) {
+    int m = 0;
+    while (strcmp(kModules[m], fn.module) != 0) m++;
+    CU(cuModuleGetFunction(&fn.f, g_mod[m], fn.name));
+  }
+  return 0;
+}
+
+// find_border_pixels (mode 0) / find_border_pixels_end (mode 1).
+int refh_find_border(const int32_t* labels, uint8_t* border, int H, int W, int mode) {
+  CU(cuCtxSetCurrent(g_ctx));
+  int npix = H * W;
+  Dev s, b;
+  if (alloc(s, 4 * (size_t)npix) || alloc(b, npix)) return -1;
+  CU(cuMemcpyHtoD(s.p, labels, 4 * (size_t)npix));
+  CU(cuMemsetD8(b.p, 0, npix));
+  void* args[] = {&s.p, &b.p, &npix, &W, &H};
+  if (launch(mode ? F_BORDER_END : F_BORDER, nblk(npix), 512, args)) return -1;
+  CU(cuCtxSynchronize());
+  CU(cuMemcpyDtoH(border, b.p, npix));
+  return 0;
+}
+
+// init_seg (init_seg.cu:20-46): host geometry as there, reference kernels.
+int refh_init_seg(int H, int W, int sp_size, int32_t* labels) {
+  CU(cuCtxSetCurrent(g_ctx));
+  double Hh = sqrt(double(pow(sp_size, 2)) / (1.5 * sqrt(3.0)));
+  double w = sqrt(3.0) * Hh;
+  int nx = (int)floor(double(W) / w) + 2;
+  int ny = (int)floor(double(H) / (1.5 * Hh)) + 2;
+  int nspix = nx * ny, npix = H * W;
+  Dev c, s;
+  if (alloc(c, 16 * (size_t)nspix) || alloc(s, 4 * (size_t)npix)) return -1;
+  void* a1[] = {&c.p, &Hh, &w, &nspix, &nx, &W, &H};
+  if (launch(F_HEX_CENTER, nblk(nspix), 512, a1)) return -1;
+  void* a2[] = {&s.p, &c.p, &nspix, &npix, &W};
+  if (launch(F_HEX_SEG, nblk(npix), 512, a2)) return -1;
+  CU(cuCtxSynchronize());
+  CU(cuMemcpyDtoH(labels, s.p, 4 * (size_t)npix));
+  return nspix;
+}
+
+// update_params (update_params.cu:12-31) on given labels and priors.
+int refh_update_params(const float* img, const int32_t* labels, int H, int W, int nbuf,
+                       int sp_size, float sigma2_app, const int* valid, const int* prop,
+                       const float* prior_count, const double* prior_icov,
+                       const double* sample_sigma, int* count_out, float* mu_app_out,
+                       double* mu_shape_out, double* sigma_shape_out, double* logdet_out,
+                       int* valid_out) {
+  CU(cuCtxSetCurrent(g_ctx));
+  int npix = H * W, nbatch = 1, nftrs = 3;
+  auto host = pack_params(nbuf, nullptr, nullptr, nullptr, nullptr, nullptr, prior_count, valid,
+                          prop, prior_icov, sample_sigma);
+  Dev im, sg, sp, hp;
+  if (alloc(im, 12 * (size_t)npix) || alloc(sg, 4 * (size_t)npix) ||
+      alloc(sp, host.size()) || alloc(hp, (size_t)kHelperSize * nbuf))
+    return -1;
+  CU(cuMemcpyHtoD(im.p, img, 12 * (size_t)npix));
+  CU(cuMemcpyHtoD(sg.p, labels, 4 * (size_t)npix));
+  CU(cuMemcpyHtoD(sp.p, host.data(), host.size()));
+  void* a1[] = {&sp.p, &hp.p, &nbuf, &nftrs};
+  if (launch(F_CLEAR, nblk(nbuf), 512, a1)) return -1;
+  CU(cuMemsetD8(hp.p, 0, (size_t)kHelperSize * nbuf));
+  void* a2[] = {&im.p, &sg.p, &sp.p, &hp.p, &npix, &nbatch, &W, &nftrs};
+  if (launch(F_SUM, nblk(npix), 512, a2)) return -1;
+  void* a3[] = {&sp.p, &hp.p, &sigma2_app, &sp_size, &nbuf};
+  if (launch(F_SIMPLE_UPDATE, nblk(nbuf), 512, a3)) return -1;
+  CU(cuCtxSynchronize());
+  CU(cuMemcpyDtoH(host.data(), sp.p, host.size()));
+  for (int k = 0; k < nbuf; k++) {
+    const unsigned char* e = host.data() + (size_t)k * REF_SP_SIZE;
+    memcpy(count_out + k, e + REF_OFF_count, 4);
+    memcpy(mu_app_out + 3 * k, e + REF_OFF_mu_app, 12);
+    memcpy(mu_shape_out + 2 * k, e + REF_OFF_mu_shape, 16);
+    memcpy(sigma_shape_out + 3 * k, e + REF_OFF_sigma_shape, 24);
+    memcpy(logdet_out + k, e + REF_OFF_logdet_sigma_shape, 8);
+    memcpy(valid_out + k, e + REF_OFF_valid, 4);
+  }
+  return 0;
+}
+
+// update_seg (update_seg.cu:281-311) on given parameters; labels updated in place.
+int refh_update_seg(const float* img, int32_t* labels, int H, int W, int nbuf, int niters_seg,
+                    float sigma2_app, float potts, const int* count, const float* mu_app,
+                    const double* mu_shape, const double* sigma_shape, const double* logdet) {
+  CU(cuCtxSetCurrent(g_ctx));
+  int npix = H * W, nbatch = 1, nftrs = 3;
+  auto host = pack_params(nbuf, count, mu_app, mu_shape, sigma_shape, logdet, nullptr, nullptr,
+                          nullptr, nullptr, nullptr);
+  Dev im, sg, sp, bd;
+  if (alloc(im, 12 * (size_t)npix) || alloc(sg, 4 * (size_t)npix) ||
+      alloc(sp, host.size()) || alloc(bd, npix))
+    return -1;
+  CU(cuMemcpyHtoD(im.p, img, 12 * (size_t)npix));
+  CU(cuMemcpyHtoD(sg.p, labels, 4 * (size_t)npix));
+  CU(cuMemcpyHtoD(sp.p, host.data(), host.size()));
+  for (int it = 0; it < niters_seg; it++) {
+    CU(cuMemsetD8(bd.p, 0, npix));
+    void* ab[] = {&sg.p, &bd.p, &npix, &W, &H};
+    if (launch(F_BORDER, nblk(npix), 512, ab)) return -1;
+    for (int xm = 0; xm < 2; xm++)
+      for (int ym = 0; ym < 2; ym++) {
+        void* au[] = {&im.p, &sg.p, &bd.p, &sp.p, &sigma2_app, &potts, &npix, &nbatch, &W, &H,
+                      &nftrs, &xm, &ym};
+        if (launch(F_UPDATE_SUBSET, nblk(npix), 512, au)) return -1;
+      }
+  }
+  CU(cuCtxSynchronize());
+  CU(cuMemcpyDtoH(labels, sg.p, 4 * (size_t)npix));
+  return 0;
+}
+
+// init_split + calc_split_candidate loop (split_merge_orig.cu:262-356): distance
+// field of the seeds for `direction`.
+int refh_split_bfs(const int32_t* labels, int H, int W, int nbuf, const int* valid,
+                   const double* mu_shape, int direction, int max_spix, int32_t* dist_out) {
+  CU(cuCtxSetCurrent(g_ctx));
+  int npix = H * W, nbatch = 1;
+  auto host = pack_params(nbuf, nullptr, nullptr, mu_shape, nullptr, nullptr, nullptr, valid,
+                          nullptr, nullptr, nullptr);
+  Dev sg, sp, ds, bd, mx, done;
+  if (alloc(sg, 4 * (size_t)npix) || alloc(sp, host.size()) || alloc(ds, 4 * (size_t)npix) ||
+      alloc(bd, npix) || alloc(mx, 4) || alloc(done, 4))
+    return -1;
+  CU(cuMemcpyHtoD(sg.p, labels, 4 * (size_t)npix));
+  CU(cuMemcpyHtoD(sp.p, host.data(), host.size()));
+  CU(cuMemsetD8(ds.p, 0xff, 4 * (size_t)npix));
+  CU(cuMemsetD8(bd.p, 0, npix));
+  void* ai[] = {&bd.p, &ds.p, &sp.p, &nbuf, &nbatch, &W, &H, &direction, &sg.p, &mx.p, &max_spix};
+  if (launch(F_INIT_SPLIT, nblk(nbuf), 512, ai)) return -1;
+  int distance = 1, flag = 1, steps = 0;
+  while (flag) {
+    CU(cuMemsetD32(done.p, 0, 1));
+    void* ac[] = {&ds.p, &sg.p, &bd.p, &distance, &done.p, &npix, &nbatch, &W, &H};
+    if (launch(F_SPLIT_CAND, nblk(npix), 512, ac)) return -1;
+    distance++;
+    CU(cuMemcpyDtoH(&flag, done.p, 4));
+    if (++steps > 5005) { g_err = "BFS did not finish"; return -1; }
+  }
+  CU(cuMemcpyDtoH(dist_out, ds.p, 4 * (size_t)npix));
+  return steps;
+}
+
+// fill_missing (fill_missing.cu:35-130); returns iterations, or -2 on no progress.
+int refh_fill(int32_t* seg, const double* centers, int ncenters, int H, int W, int break_iter) {
+  CU(cuCtxSetCurrent(g_ctx));
+  int npix = H * W, nbatch = 1;
+  Dev sg, ct, bd, nn;
+  if (alloc(sg, 4 * (size_t)npix) || alloc(ct, 16 * (size_t)ncenters) || alloc(bd, npix) ||
+      alloc(nn, 4))
+    return -1;
+  CU(cuMemcpyHtoD(sg.p, seg, 4 * (size_t)npix));
+  CU(cuMemcpyHtoD(ct.p, centers, 16 * (size_t)ncenters));
+  int iter = 0, prev_neg = (int)1410065408, num_neg = 1, status = 0;
+  bool print_values = false;
+  while (num_neg > 0) {
+    if (break_iter > 0 && iter >= break_iter) break;
+    CU(cuMemsetD32(nn.p, 0, 1));
+    CU(cuMemsetD8(bd.p, 0, npix));
+    void* ab[] = {&sg.p, &bd.p, &nbatch, &H, &W, &nn.p};
+    if (launch(F_FILL_BORDER, nblk(npix), 512, ab)) return -1;
+    CU(cuMemcpyDtoH(&num_neg, nn.p, 4));
+    for (int xm = 0; xm < 2; xm++)
+      for (int ym = 0; ym < 2; ym++) {
+        void* af[] = {&sg.p, &ct.p, &bd.p, &nbatch, &H, &W, &npix, &xm, &ym, &print_values};
+        if (launch(F_FILL_NN, nblk(npix), 512, af)) return -1;
+      }
+    iter++;
+    if (num_neg == prev_neg) { status = -2; break; }
+    prev_neg = num_neg;
+  }
+  CU(cuCtxSynchronize());
+  CU(cuMemcpyDtoH(seg, sg.p, 4 * (size_t)npix));
+  return status ? status : iter;
+}
+
+// find_spix_min iterated to a fixed point (split_disconnected.cu:107-150): region
+// roots (minimum pixel index of each 8-connected equal-label region).
+int refh_cc_roots(const int32_t* seg, int H, int W, int32_t* roots) {
+  CU(cuCtxSetCurrent(g_ctx));
+  int npix = H * W;
+  std::vector<int32_t> init(npix);
+  for (int i = 0; i < npix; i++) init[i] = i;
+  Dev sg, cur, prev, ch;
+  if (alloc(sg, 4 * (size_t)npix) || alloc(cur, 4 * (size_t)npix) ||
+      alloc(prev, 4 * (size_t)npix) || alloc(ch, 4))
+    return -1;
+  CU(cuMemcpyHtoD(sg.p, seg, 4 * (size_t)npix));
+  CU(cuMemcpyHtoD(cur.p, init.data(), 4 * (size_t)npix));
+  int changes = 1, steps = 0;
+  while (changes) {
+    CU(cuMemcpyDtoD(prev.p, cur.p, 4 * (size_t)npix));
+    CU(cuMemsetD32(ch.p, 0, 1));
+    void* a[] = {&sg.p, &cur.p, &prev.p, &ch.p, &H, &W, &npix};
+    if (launch(F_SPIX_MIN, nblk(npix), 512, a)) return -1;
+    CU(cuMemcpyDtoH(&changes, ch.p, 4));
+    if (++steps > 100000) { g_err = "components did not converge"; return -1; }
+  }
+  CU(cuMemcpyDtoH(roots, cur.p, 4 * (size_t)npix));
+  return steps;
+}
+
+}  // extern "C"
