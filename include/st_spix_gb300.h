@@ -219,6 +219,55 @@ int stspix_bass_partial(stspix_ctx* ctx, void* stream, const float* img, int H, 
                         int32_t* labels_out, stspix_state_dump* dump,
                         int* nbuf_out, int* max_spix_out);
 
+/* ---- batched and serving forms -----------------------------------------------
+ * No single reference counterpart: the reference processes one frame per call
+ * (pyapi.cu:46 main_loop).  stspix_process_batch runs many frames, of uneven
+ * sizes, in one pass: every kernel of the per-frame path is launched once for all
+ * frames of the batch, so a frame's result is the same alone and in any batch.
+ * A frame is either independent (run_bass on it, video == NULL) or the next frame
+ * of a video stream whose labels, superpixel parameters and superpixel count stay
+ * resident on the device between calls (shift_and_fill + run_prop, as
+ * bist_forward does for frames after the first).                                 */
+typedef struct stspix_video stspix_video;
+
+/* Resident state of one video stream of frames of H x W pixels. */
+int stspix_video_create(stspix_ctx* ctx, stspix_video** out, int H, int W);
+int stspix_video_destroy(stspix_video* video);
+/* Forget the stream's history: its next frame starts a new video. */
+int stspix_video_reset(stspix_video* video);
+/* Superpixels of the stream's last frame (0 before its first frame). */
+int stspix_video_nspix(const stspix_video* video);
+/* Frames processed since creation or the last reset. */
+long long stspix_video_frames(const stspix_video* video);
+
+typedef struct stspix_frame {
+  const float* img;       /* f32 [H,W,3] device                                         */
+  const float* flow;      /* f32 [H,W,2] device, (dx,dy) from the video's previous
+                             frame to this one; ignored on a video's first frame        */
+  int H, W;
+  int sp_size;            /* superpixel size of this frame; 0: cfg->sp_size             */
+  int32_t* labels_out;    /* i32 [H,W] device                                           */
+  stspix_video* video;    /* NULL: independent frame; else the video it continues       */
+  /* set by stspix_process_batch (host): */
+  int nspix;              /* superpixels of the frame                                   */
+  int niters;             /* outer iterations run                                       */
+  int status;             /* per-frame status (STSPIX_OK, NOPROGRESS, ...)              */
+  stspix_frame_log log;
+} stspix_frame;
+
+/* Process `nframes` frames (at most one per video) as one batch on `stream`;
+ * synchronises the stream.  Returns the first non-zero per-frame status, or an
+ * error of the call itself.                                                      */
+int stspix_process_batch(stspix_ctx* ctx, void* stream, stspix_frame* frames, int nframes,
+                         const stspix_config* cfg);
+
+/* Device bytes held per video stream (resident state) and per batch slot (the
+ * working buffers of one frame in flight), for admission under a memory budget. */
+int stspix_footprint(int H, int W, int sp_size, long long* video_bytes,
+                     long long* slot_bytes);
+/* GPU time (ms) of the last stspix_process_batch call, from CUDA events. */
+double stspix_last_batch_ms(const stspix_ctx* ctx);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,13 +51,24 @@ class FrameLog(C.Structure):
                 ("niters", C.c_int), ("nspix", C.c_int)]
 
 
+class FrameC(C.Structure):
+    """stspix_frame (device pointers; the last four fields are outputs)."""
+    _fields_ = [("img", C.c_void_p), ("flow", C.c_void_p), ("H", C.c_int), ("W", C.c_int),
+                ("sp_size", C.c_int), ("labels_out", C.c_void_p), ("video", C.c_void_p),
+                ("nspix", C.c_int), ("niters", C.c_int), ("status", C.c_int),
+                ("log", FrameLog)]
+
+
 # Every symbol declared in include/st_spix_gb300.h.
 EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_last_error",
            "stspix_version", "stspix_kernel_launches", "stspix_get_frame_log",
            "stspix_bist_forward", "stspix_get_marked_video", "stspix_run_bass",
            "stspix_shift_and_fill", "stspix_run_prop", "stspix_init_seg",
            "stspix_find_border", "stspix_bass_partial", "stspix_profile_enable",
-           "stspix_profile_get", "stspix_frame_times", "stspix_get_marked_video_noalloc"]
+           "stspix_profile_get", "stspix_frame_times", "stspix_get_marked_video_noalloc",
+           "stspix_video_create", "stspix_video_destroy", "stspix_video_reset",
+           "stspix_video_nspix", "stspix_video_frames", "stspix_process_batch",
+           "stspix_footprint", "stspix_last_batch_ms"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -103,6 +114,15 @@ def load(build_if_missing: bool = True):
             "stspix_profile_get": (I, [P, I, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
             "stspix_frame_times": (I, [P, C.POINTER(C.c_double), I]),
             "stspix_get_marked_video_noalloc": (I, [P, P, P, P, I, I, I, I, P]),
+            "stspix_video_create": (I, [P, C.POINTER(C.c_void_p), I, I]),
+            "stspix_video_destroy": (I, [P]),
+            "stspix_video_reset": (I, [P]),
+            "stspix_video_nspix": (I, [P]),
+            "stspix_video_frames": (C.c_longlong, [P]),
+            "stspix_process_batch": (I, [P, P, C.POINTER(FrameC), I, C.POINTER(Config)]),
+            "stspix_footprint": (I, [I, I, I, C.POINTER(C.c_longlong),
+                                     C.POINTER(C.c_longlong)]),
+            "stspix_last_batch_ms": (C.c_double, [P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -162,6 +182,9 @@ class Context:
         self.lib.stspix_frame_times(self.handle, buf, n)
         return [buf[i] for i in range(n)]
 
+    def last_batch_ms(self) -> float:
+        return float(self.lib.stspix_last_batch_ms(self.handle))
+
     def close(self):
         if getattr(self, "handle", None):
             self.lib.stspix_destroy(self.handle)
@@ -182,3 +205,12 @@ def default_config(**kw) -> Config:
             raise KeyError(k)
         setattr(c, k, v)
     return c
+
+
+def footprint(H: int, W: int, sp_size: int) -> tuple:
+    """(bytes resident per video stream, bytes per batch slot) on the device."""
+    vb, sb = C.c_longlong(0), C.c_longlong(0)
+    st = load().stspix_footprint(int(H), int(W), int(sp_size), C.byref(vb), C.byref(sb))
+    if st != 0:
+        raise StspixError(st, "stspix_footprint: bad size")
+    return int(vb.value), int(sb.value)

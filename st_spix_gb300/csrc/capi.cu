@@ -1,14 +1,22 @@
 // Host orchestration and C ABI of the GB300 streaming-BASS engine.
 //
-// One context owns a device workspace sized for the largest frame seen so far.
-// A frame is a fixed sequence of kernel launches on the caller's stream with no
-// host synchronisation inside the BASS loop: data-dependent loops (split BFS, hole
-// filling, connected components) run as bounded cooperative kernels, and the
-// values the reference reads back to the host every step (done flags, max_spix,
-// counts) stay on the device.  Propagated frames read one small struct back per
-// frame (hole count and superpixel count: the iteration ladder and buffer sizing).
+// Every frame, alone or in a batch, goes through one batch runner.  A batch is a
+// set of slots (one frame each, uneven sizes allowed) described by device slot
+// tables; each phase of the per-frame path is ONE launch over all slots of the
+// batch (grid y = slot), so launch count and fixed costs are paid once per batch,
+// not once per frame, and a frame's arithmetic is the same alone and in a batch.
+// The outer BASS loop runs the slots sorted by iteration count, so at outer
+// iteration idx the slots still iterating are a prefix of the table.
+//
+// No host synchronisation inside the BASS loop: data-dependent loops (split BFS,
+// hole filling, connected components) run as bounded cooperative kernels and the
+// values the reference reads back every step stay on the device.  A batch with
+// propagated frames and the 4/8/12 iteration ladder reads the hole counts back
+// once (the ladder picks each frame's iteration count from them).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -22,33 +30,66 @@
 
 namespace stspix {
 
-__global__ void k_frame_begin(Scalars* sc, int max_spix, int nbuf_logical) {
-  sc->max_spix = max_spix;
-  sc->nbuf_logical = nbuf_logical;
-  sc->status = STSPIX_OK;
-  sc->nsplits = sc->nmerges = sc->nrevived = sc->nminted = sc->near_ties = 0;
-  sc->fill_iters = 0;
-  sc->ninvalid = 0;
-  sc->tmp0 = sc->tmp1 = sc->tmp2 = 0;
-}
-__global__ void k_bass_after_compact(Scalars* sc) {
-  sc->max_spix = sc->nspix - 1;
-}
-__global__ void k_calc_n(Scalars* sc, int lo, int cap) {
-  sc->tmp2 = min(sc->max_spix + 1, cap) - lo;  // ids beyond cap were never created
-}
-__global__ void k_finish_compact(Scalars* sc, int lo, const int* total) {
-  sc->nspix = lo + *total;
-}
+constexpr int kMaxRounds = 4096;  // relaxation rounds per cooperative launch
 
 struct Buf {
   void* p = nullptr;
   size_t bytes = 0;
 };
 
+// Working buffers of one batch position.
+struct SlotWork {
+  std::vector<Buf> pix, sp;
+  int npix_cap = 0, sp_cap = 0;
+  Slot s{};
+};
+
+// One frame of a batch as the host sees it.
+struct FrameDesc {
+  const float* img = nullptr;
+  const float* flow = nullptr;
+  int H = 0, W = 0, sp_size = 0;
+  int* seg = nullptr;              // output labels (propagated: filled labels on entry
+                                   // when the shift stage is skipped)
+  int mode = 0;                    // 0 BASS, 1 propagated
+  const int* prev = nullptr;       // previous labels (shift stage)
+  int n_prev = 0;
+  stspix_params pprev{}, pout{};
+  int* shifted = nullptr;          // shifted labels (null: slot workspace)
+  int* resident = nullptr;         // keep the finished labels here
+  int niters = -1;                 // -1: decided by the runner
+  int slot = 0;                    // batch position (workspace index)
+};
+
+enum { kStageShift = 1, kStageSeg = 2 };
+
+// Launch geometry of a slot table.
+struct List {
+  Slot* d = nullptr;               // device table
+  int B = 0;
+  int max_npix = 0, max_cap = 0, max_nprev = 0, max_tx = 0, max_ty = 0;
+  long long max_acc = 0, max_sm = 0;
+  int tiles = 0;
+  long long pix = 0, q = 0;
+  bool any_prop = false;
+  std::vector<int> tiles_upto;     // tiles of the first i slots
+};
+
 }  // namespace stspix
 
 using namespace stspix;
+
+struct stspix_video {
+  stspix_ctx* ctx = nullptr;
+  int H = 0, W = 0;
+  int n = 0;                 // superpixels of the last frame
+  int cur = 0;               // params of the last frame: pp[cur]
+  long long frames = 0;
+  int* labels = nullptr;     // last frame's labels
+  stspix_params pp[2]{};
+  int pp_cap = 0;
+  std::vector<Buf> lbufs, pbufs;
+};
 
 struct stspix_ctx {
   int device = 0;
@@ -56,35 +97,21 @@ struct stspix_ctx {
   std::string err;
   long long launches = 0;
   stspix_frame_log log{};
-  // sizing
-  int npix_cap = 0;
-  int sp_cap = 0;
-  // pixel buffers
-  uint8_t* border = nullptr;
-  int *d1 = nullptr, *d2 = nullptr, *smseg = nullptr, *hits = nullptr;
-  int *shifted = nullptr, *filled = nullptr, *seg_alt = nullptr;
-  unsigned long long* best = nullptr;
-  // superpixel buffers
-  SpDev sp{}, tmp{};
-  SmDev sm{};
-  uint8_t *flags = nullptr, *accept = nullptr, *valid0 = nullptr, *living = nullptr,
-          *mint = nullptr;
-  int *excl = nullptr, *rid = nullptr, *src_of = nullptr, *cnt_pool = nullptr, *cs = nullptr,
-      *cf = nullptr;
-  long long* fs = nullptr;
-  float *fds = nullptr, *ss = nullptr;
-  double* centers = nullptr;
-  unsigned long long *rbest = nullptr, *ccbest = nullptr;
-  // param ping-pong for bist_forward
-  stspix_params pp[2]{};
-  // control
-  int* round_flags = nullptr;
-  int* iter_counts = nullptr;
-  Scalars* sc = nullptr;
-  Scalars* sc_host = nullptr;  // pinned
-  std::vector<Buf> pix_bufs, sp_bufs, pp_bufs;
-  int pp_cap = 0;
+  std::vector<SlotWork> work;
+  // per-slot control (bcap slots)
+  int bcap = 0;
+  Scalars* sc = nullptr;        // device [bcap]
+  Scalars* sc_host = nullptr;   // pinned [bcap]
+  Scalars* ctl = nullptr;       // grid barrier of the cooperative launches
+  int* round_flags = nullptr;   // [kMaxRounds * (bcap + 1)]
+  int* fill_counts = nullptr;   // [kFillBreakIter * bcap]
+  int* fill_done = nullptr;     // [bcap]
+  Slot* d_slots = nullptr;      // device [3 * bcap]: all, BASS, propagated
+  Slot* h_slots = nullptr;      // pinned staging of the same
+  std::vector<Buf> ctl_bufs;
   int coop_relax0 = 0, coop_relax1 = 0, coop_fill = 0;
+  // bist_forward's stream state
+  stspix_video* fwd = nullptr;
   // profiling (CUDA events on the launching stream)
   int prof_on = 0;
   int cur_fam = STSPIX_FAM_OTHER;
@@ -93,14 +120,17 @@ struct stspix_ctx {
   std::vector<Pending> pending;
   long long fam_launches[STSPIX_NFAM] = {0};
   double fam_ms[STSPIX_NFAM] = {0};
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> frame_ev;
+  struct FrameEv { cudaEvent_t a, b; int n; };  // n frames between a and b
+  std::vector<FrameEv> frame_ev;
   std::vector<double> frame_ms;
+  cudaEvent_t batch_ev[2] = {nullptr, nullptr};
+  double batch_ms = 0;
 };
 
 namespace {
 
 const int kThreads = 256;
-inline unsigned blocks_for(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+inline unsigned blocks_for(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
 
 int fail(stspix_ctx* c, int code, const char* fmt, ...) {
   char buf[512];
@@ -170,12 +200,24 @@ void prof_harvest(stspix_ctx* ctx) {
     if (n_ > 0) LAUNCHG(kernel, blocks_for(n_), kThreads, __VA_ARGS__);        \
   } while (0)
 
-#define LAUNCH1(kernel, ...) LAUNCHG(kernel, 1, 1, __VA_ARGS__)
+// One launch over `nb` slots of table L, `n` work items per slot (max over slots).
+#define LAUNCHB(kernel, n, L, nb, ...)                                         \
+  do {                                                                         \
+    long long n_ = (n);                                                        \
+    if (n_ > 0 && (nb) > 0)                                                    \
+      LAUNCHG(kernel, dim3(blocks_for(n_), (unsigned)(nb)), kThreads, (L).d, ##__VA_ARGS__); \
+  } while (0)
+
+// One thread per slot.
+#define LAUNCHS(kernel, L, nb, ...)                                            \
+  do {                                                                         \
+    if ((nb) > 0) LAUNCHG(kernel, blocks_for(nb), kThreads, (L).d, (nb), ##__VA_ARGS__); \
+  } while (0)
 
 template <typename T>
 int alloc(stspix_ctx* ctx, std::vector<Buf>& list, T** p, size_t n) {
   void* q = nullptr;
-  size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  size_t bytes = (std::max<size_t>(n, 1) * sizeof(T) + 15) & ~size_t(15);
   cudaError_t e = cudaMalloc(&q, bytes);
   if (e != cudaSuccess)
     return fail(ctx, STSPIX_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
@@ -195,9 +237,8 @@ void free_list(std::vector<Buf>& list) {
     if (r_) return r_;                                        \
   } while (0)
 
-int alloc_spdev(stspix_ctx* ctx, SpDev& s, int cap) {
+int alloc_spdev(stspix_ctx* ctx, std::vector<Buf>& L, SpDev& s, int cap) {
   s.cap = cap;
-  auto& L = ctx->sp_bufs;
   AL(L, s.count, cap); AL(L, s.valid, cap); AL(L, s.prop, cap);
   AL(L, s.prior_count, cap); AL(L, s.icount, cap); AL(L, s.sm_count, cap);
   AL(L, s.mu_app, 3 * (size_t)cap); AL(L, s.mu_shape, 2 * (size_t)cap);
@@ -209,8 +250,7 @@ int alloc_spdev(stspix_ctx* ctx, SpDev& s, int cap) {
   return STSPIX_OK;
 }
 
-int alloc_params(stspix_ctx* ctx, stspix_params& p, int cap) {
-  auto& L = ctx->pp_bufs;
+int alloc_params(stspix_ctx* ctx, std::vector<Buf>& L, stspix_params& p, int cap) {
   p.capacity = cap;
   AL(L, p.mu_app, 3 * (size_t)cap); AL(L, p.prior_mu_app, 3 * (size_t)cap);
   AL(L, p.mu_shape, 2 * (size_t)cap); AL(L, p.sigma_shape, 3 * (size_t)cap);
@@ -221,42 +261,72 @@ int alloc_params(stspix_ctx* ctx, stspix_params& p, int cap) {
   return STSPIX_OK;
 }
 
-// Make sure pixel buffers hold npix and superpixel buffers hold sp_cap entries.
-// Growing synchronises the device and does not preserve contents (callers grow
-// only between frames); the bist_forward parameter buffers live in pp_bufs and are
-// grown by ensure_pp, which keeps the previous frame's parameters.
-int ensure(stspix_ctx* ctx, int npix, int sp_cap) {
-  if (npix > ctx->npix_cap) {
+// Bytes of the buffers above (for admission under a memory budget).
+constexpr long long kPixBytes = 1 + 5 * 4 + 8 + 4;            // border, d1 d2 smseg hits shifted, best, seg_alt
+constexpr long long kSpDevBytes = 4 + 1 + 1 + 4 + 4 + 4 + 12 + 16 + 24 + 8 + 12 + 16 + 24 + 24 + 24 +
+                                  64 + (long long)sizeof(SweepRec);
+constexpr long long kSmBytes = 4 + 24 + 24 + 4 + 4 + 4 + 4 + 4 + 1 + 8;
+constexpr long long kAuxBytes = 5 * 1 + 6 * 4 + 16 + 8 + 4 + 16 + 8 + 8;
+constexpr long long kParamBytes = 12 + 12 + 16 + 24 + 4 + 16 + 24 + 24 + 4 + 4 + 4 + 4 + 4;
+
+// Make sure slot position i holds npix pixels and sp_cap superpixels.  Growing
+// synchronises the device and does not preserve contents.
+int ensure_slot(stspix_ctx* ctx, int i, int npix, int sp_cap) {
+  if ((int)ctx->work.size() <= i) ctx->work.resize(i + 1);
+  SlotWork& w = ctx->work[i];
+  Slot& s = w.s;
+  if (npix > w.npix_cap) {
     CK(cudaDeviceSynchronize());
-    free_list(ctx->pix_bufs);
-    auto& L = ctx->pix_bufs;
+    free_list(w.pix);
+    auto& L = w.pix;
     int n = npix;
-    AL(L, ctx->border, n); AL(L, ctx->d1, n); AL(L, ctx->d2, n); AL(L, ctx->smseg, n);
-    AL(L, ctx->hits, n); AL(L, ctx->shifted, n); AL(L, ctx->filled, n); AL(L, ctx->best, n);
-    AL(L, ctx->seg_alt, n);
-    ctx->npix_cap = npix;
+    AL(L, s.border, n); AL(L, s.d1, n); AL(L, s.d2, n); AL(L, s.smseg, n);
+    AL(L, s.hits, n); AL(L, s.shifted, n); AL(L, s.best, n); AL(L, s.seg_alt, n);
+    w.npix_cap = npix;
   }
-  if (sp_cap > ctx->sp_cap) {
+  if (sp_cap > w.sp_cap) {
     CK(cudaDeviceSynchronize());
-    free_list(ctx->sp_bufs);
+    free_list(w.sp);
+    auto& L = w.sp;
     int cap = sp_cap;
     int r;
-    if ((r = alloc_spdev(ctx, ctx->sp, cap))) return r;
-    if ((r = alloc_spdev(ctx, ctx->tmp, cap))) return r;
-    auto& L = ctx->sp_bufs;
+    if ((r = alloc_spdev(ctx, L, s.sp, cap))) return r;
+    if ((r = alloc_spdev(ctx, L, s.tmp, cap))) return r;
     size_t c2 = (size_t)cap + 2;
-    AL(L, ctx->sm.count, c2); AL(L, ctx->sm.s, 3 * c2); AL(L, ctx->sm.sq, 3 * c2);
-    AL(L, ctx->sm.ninvalid, c2); AL(L, ctx->sm.pair, c2); AL(L, ctx->sm.claim, c2);
-    AL(L, ctx->sm.target, c2); AL(L, ctx->sm.newid, c2); AL(L, ctx->sm.flag, c2);
-    AL(L, ctx->sm.msingle, c2);
-    AL(L, ctx->flags, c2); AL(L, ctx->accept, c2); AL(L, ctx->valid0, c2);
-    AL(L, ctx->living, c2); AL(L, ctx->mint, c2);
-    AL(L, ctx->excl, c2); AL(L, ctx->rid, c2); AL(L, ctx->src_of, c2);
-    AL(L, ctx->cnt_pool, c2); AL(L, ctx->cs, c2); AL(L, ctx->cf, c2);
-    AL(L, ctx->fs, 2 * c2); AL(L, ctx->fds, 2 * c2); AL(L, ctx->ss, c2);
-    AL(L, ctx->centers, 2 * c2); AL(L, ctx->rbest, c2); AL(L, ctx->ccbest, c2);
-    ctx->sp_cap = cap;
+    SmDev& sm = s.sm;
+    AL(L, sm.count, c2); AL(L, sm.s, 3 * c2); AL(L, sm.sq, 3 * c2);
+    AL(L, sm.ninvalid, c2); AL(L, sm.pair, c2); AL(L, sm.claim, c2);
+    AL(L, sm.target, c2); AL(L, sm.newid, c2); AL(L, sm.flag, c2);
+    AL(L, sm.msingle, c2);
+    AL(L, s.flags, c2); AL(L, s.accept, c2); AL(L, s.valid0, c2);
+    AL(L, s.living, c2); AL(L, s.mint, c2);
+    AL(L, s.excl, c2); AL(L, s.rid, c2); AL(L, s.src_of, c2);
+    AL(L, s.cnt_pool, c2); AL(L, s.cs, c2); AL(L, s.cf, c2);
+    AL(L, s.fs, 2 * c2); AL(L, s.fds, 2 * c2); AL(L, s.ss, c2);
+    AL(L, s.centers, 2 * c2); AL(L, s.rbest, c2); AL(L, s.ccbest, c2);
+    w.sp_cap = cap;
   }
+  return STSPIX_OK;
+}
+
+// Per-slot control arrays for batches of up to B slots.
+int ensure_bcap(stspix_ctx* ctx, int B) {
+  if (B <= ctx->bcap) return STSPIX_OK;
+  CK(cudaDeviceSynchronize());
+  free_list(ctx->ctl_bufs);
+  if (ctx->sc_host) { cudaFreeHost(ctx->sc_host); ctx->sc_host = nullptr; }
+  if (ctx->h_slots) { cudaFreeHost(ctx->h_slots); ctx->h_slots = nullptr; }
+  int nb = std::max(B, 2 * ctx->bcap);
+  auto& L = ctx->ctl_bufs;
+  AL(L, ctx->sc, nb);
+  AL(L, ctx->round_flags, (size_t)kMaxRounds * (nb + 1));
+  AL(L, ctx->fill_counts, (size_t)kFillBreakIter * nb);
+  AL(L, ctx->fill_done, nb);
+  AL(L, ctx->d_slots, 3 * (size_t)nb);
+  CK(cudaMallocHost(&ctx->sc_host, sizeof(Scalars) * nb));
+  CK(cudaMallocHost(&ctx->h_slots, sizeof(Slot) * 3 * nb));
+  CK(cudaMemset(ctx->sc, 0, sizeof(Scalars) * nb));
+  ctx->bcap = nb;
   return STSPIX_OK;
 }
 
@@ -281,42 +351,80 @@ SmConsts sm_constants(const stspix_config& c) {
   return K;
 }
 
-// Parameter ping-pong buffers of bist_forward: grown to `cap` entries keeping the
-// first `keep` entries of buffer `keep_idx`.
-int ensure_pp(stspix_ctx* ctx, cudaStream_t st, int cap, int keep_idx, int keep) {
-  if (cap <= ctx->pp_cap) return STSPIX_OK;
-  std::vector<Buf> old = ctx->pp_bufs;
-  stspix_params oldp = ctx->pp[keep_idx];
-  ctx->pp_bufs.clear();
-  int r;
-  for (int i = 0; i < 2; i++)
-    if ((r = alloc_params(ctx, ctx->pp[i], cap))) return r;
-  if (keep > 0) {
-    stspix_params& np = ctx->pp[keep_idx];
-    size_t k = (size_t)keep;
-    CK(cudaMemcpyAsync(np.mu_app, oldp.mu_app, 12 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.prior_mu_app, oldp.prior_mu_app, 12 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.mu_shape, oldp.mu_shape, 16 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.sigma_shape, oldp.sigma_shape, 24 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.logdet_sigma_shape, oldp.logdet_sigma_shape, 4 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.prior_mu_shape, oldp.prior_mu_shape, 16 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.prior_sigma_shape, oldp.prior_sigma_shape, 24 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.sample_sigma_shape, oldp.sample_sigma_shape, 24 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.counts, oldp.counts, 4 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.sm_counts, oldp.sm_counts, 4 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.prior_counts, oldp.prior_counts, 4 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.ids, oldp.ids, 4 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(np.invalid_counts, oldp.invalid_counts, 4 * k, cudaMemcpyDeviceToDevice, st));
-    CK(cudaStreamSynchronize(st));
+int slot_cap(const FrameDesc& f) {
+  if (f.mode) return std::max(10 * f.n_prev + 2, 64);
+  double Hh, w;
+  int nx, ny;
+  hex_geometry(f.sp_size, f.W, f.H, &Hh, &w, &nx, &ny);
+  return std::max(30 * nx * ny, 64);
+}
+
+// Fill the slot record of frame f (workspace pointers + frame fields).
+Slot make_slot(stspix_ctx* ctx, const FrameDesc& f, int cap) {
+  Slot s = ctx->work[f.slot].s;
+  s.img = f.img;
+  s.seg = f.seg;
+  s.H = f.H; s.W = f.W; s.npix = f.H * f.W;
+  s.cap = cap;
+  s.sp.cap = cap;
+  s.tmp.cap = cap;
+  s.mode = f.mode;
+  s.sp_size = f.sp_size;
+  s.lo = f.mode ? f.n_prev : 0;
+  hex_geometry(f.sp_size, f.W, f.H, &s.hex_h, &s.hex_w, &s.hex_nx, &s.hex_ny);
+  s.nraw = s.hex_nx * s.hex_ny;
+  s.prev_labels = f.prev;
+  s.flow = f.flow;
+  s.n_prev = f.n_prev;
+  s.pprev = f.pprev;
+  s.pout = f.pout;
+  if (f.shifted) s.shifted = f.shifted;
+  s.resident_labels = f.resident;
+  s.sc = ctx->sc + f.slot;
+  return s;
+}
+
+// Build a slot table at `off` (0 all, 1 BASS, 2 propagated) of the staging area and
+// its launch geometry.
+List make_list(stspix_ctx* ctx, int off, const std::vector<Slot>& slots) {
+  List L;
+  L.d = ctx->d_slots + (size_t)off * ctx->bcap;
+  Slot* h = ctx->h_slots + (size_t)off * ctx->bcap;
+  L.B = (int)slots.size();
+  for (int i = 0; i < L.B; i++) {
+    Slot s = slots[i];
+    s.tile_base = L.tiles;
+    s.pix_base = L.pix;
+    s.q_base = L.q;
+    h[i] = s;
+    L.tiles_upto.push_back(L.tiles);
+    const int tx = (s.W + 31) / 32, ty = (s.H + 31) / 32;
+    L.tiles += tx * ty;
+    L.pix += s.npix;
+    L.q += (long long)((s.W + 1) / 2) * ((s.H + 1) / 2);
+    L.max_npix = std::max(L.max_npix, s.npix);
+    L.max_cap = std::max(L.max_cap, s.cap);
+    L.max_nprev = std::max(L.max_nprev, s.n_prev);
+    L.max_tx = std::max(L.max_tx, tx);
+    L.max_ty = std::max(L.max_ty, ty);
+    L.max_acc = std::max(L.max_acc, (long long)s.H * ((s.W + 7) / 8));
+    L.max_sm = std::max(L.max_sm, (long long)s.H * ((s.W + 15) / 16));
+    if (s.mode) L.any_prop = true;
   }
-  free_list(old);
-  ctx->pp_cap = cap;
+  L.tiles_upto.push_back(L.tiles);
+  return L;
+}
+
+int upload(stspix_ctx* ctx, cudaStream_t st, const List& L, int off) {
+  if (L.B <= 0) return STSPIX_OK;
+  CK(cudaMemcpyAsync(L.d, ctx->h_slots + (size_t)off * ctx->bcap, sizeof(Slot) * L.B,
+                     cudaMemcpyHostToDevice, st));
   return STSPIX_OK;
 }
 
-int coop_launch(stspix_ctx* ctx, cudaStream_t st, const void* fn, int want_blocks, int max_blocks,
-                void** args) {
-  int g = std::max(1, std::min(want_blocks, max_blocks));
+int coop_launch(stspix_ctx* ctx, cudaStream_t st, const void* fn, long long want_blocks,
+                int max_blocks, void** args) {
+  int g = (int)std::max(1LL, std::min<long long>(want_blocks, max_blocks));
   cudaEvent_t pe = prof_begin(ctx, st);
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(g), dim3(kThreads), args, 0, st);
   ctx->launches++;
@@ -327,318 +435,341 @@ int coop_launch(stspix_ctx* ctx, cudaStream_t st, const void* fn, int want_block
 }
 
 // ---------------------------------------------------------------------------
-// Stages.
-struct Frame {
-  const float* img;
-  int* seg;  // working labels (caller's output buffer)
-  int H, W, npix;
-  stspix_config cfg;
-  SmConsts K;
-  const int* shifted;  // prop frames: shifted labels (for invalid counts)
-  int prop_mode;
-  int n_prev;
-  const float* prev_prior_mu_app;
-};
+// Stages over the first nb slots of a table.
 
-int update_params(stspix_ctx* ctx, cudaStream_t st, const Frame& f) {
-  SpDev& sp = ctx->sp;
-  CK(cudaMemsetAsync(sp.count, 0, sizeof(int) * (size_t)sp.cap, st));
-  CK(cudaMemsetAsync(sp.acc, 0, sizeof(long long) * 8 * (size_t)sp.cap, st));
+// update_params (update_params.cu:12-52): statistics + posterior.
+int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb) {
   ctx->cur_fam = STSPIX_FAM_STATS;
-  {
-    long long nthr = (long long)f.H * ((f.W + 7) / 8);  // one 8-pixel run per thread
-    LAUNCHG(k_accumulate, (unsigned)((nthr + 127) / 128), 128, f.img, f.seg, f.H, f.W, sp);
-  }
+  LAUNCHB(kb_clear_stats, L.max_cap, L, nb);
+  LAUNCHG(kb_accumulate, dim3((unsigned)((L.max_acc + 127) / 128), (unsigned)nb), 128, L.d);
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
-  LAUNCH(k_posterior, sp.cap, sp, f.cfg.sp_size, ctx->sc);
+  LAUNCHB(kb_posterior, L.max_cap, L, nb);
   return STSPIX_OK;
 }
 
 // update_seg (update_seg.cu:281-311): niters_seg fused sweeps ping-ponging between
-// the frame's labels and a scratch buffer; the trailing border mask is only built
-// when the next iteration's merge reads it.
-int update_seg(stspix_ctx* ctx, cudaStream_t st, const Frame& f, bool need_border) {
-  const int H = f.H, W = f.W;
+// the labels and a scratch buffer; the border mask is only built when the next
+// iteration's merge reads it.
+int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
+               const stspix_config& cfg, bool need_border) {
   ctx->cur_fam = STSPIX_FAM_SWEEP;
-  int* a = f.seg;
-  int* b = ctx->seg_alt;
-  dim3 grid((W + 31) / 32, (H + 31) / 32);
-  for (int it = 0; it < f.cfg.niters_seg; it++) {
-    LAUNCHG(k_sweep_fused, grid, 256, f.img, a, b, ctx->sp.rec, ctx->sp.cap, H, W,
-            f.cfg.sigma2_app, f.cfg.potts);
-    std::swap(a, b);
-  }
-  if (a != f.seg)
-    CK(cudaMemcpyAsync(f.seg, a, sizeof(int) * (size_t)f.npix, cudaMemcpyDeviceToDevice, st));
+  dim3 grid((unsigned)L.max_tx, (unsigned)L.max_ty, (unsigned)nb);
+  for (int it = 0; it < cfg.niters_seg; it++)
+    LAUNCHG(kb_sweep, grid, 256, L.d, it & 1, cfg.sigma2_app, cfg.potts);
+  if (cfg.niters_seg & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;
-    LAUNCH(k_find_border, f.npix, f.seg, ctx->border, H, W);
+    LAUNCHB(kb_find_border, L.max_npix, L, nb);
   }
   return STSPIX_OK;
 }
 
-int run_relax(stspix_ctx* ctx, cudaStream_t st, int mode, const int* seg, int* f1, int* f2,
-              int H, int W) {
-  CK(cudaMemsetAsync(ctx->round_flags, 0, sizeof(int) * 4096, st));
-  int ntiles = ((W + 31) / 32) * ((H + 31) / 32);
-  int max_rounds = 4096;
-  void* args[] = {(void*)&seg, (void*)&f1, (void*)&f2, (void*)&H, (void*)&W, (void*)&ctx->sc,
+int run_relax(stspix_ctx* ctx, cudaStream_t st, int mode, const List& L, int nb) {
+  if (nb <= 0) return STSPIX_OK;
+  int total = L.tiles_upto[nb];  // tiles of the first nb slots
+  CK(cudaMemsetAsync(ctx->round_flags, 0, sizeof(int) * (size_t)(nb + 1), st));
+  int max_rounds = kMaxRounds;
+  Slot* d = L.d;
+  void* args[] = {(void*)&d, (void*)&nb, (void*)&total, (void*)&ctx->ctl,
                   (void*)&ctx->round_flags, (void*)&max_rounds};
   if (mode == 0)
-    return coop_launch(ctx, st, (const void*)k_relax_bfs, ntiles, ctx->coop_relax0, args);
-  return coop_launch(ctx, st, (const void*)k_relax_cc, ntiles, ctx->coop_relax1, args);
+    return coop_launch(ctx, st, (const void*)kb_relax_bfs, total, ctx->coop_relax0, args);
+  return coop_launch(ctx, st, (const void*)kb_relax_cc, total, ctx->coop_relax1, args);
 }
 
-int run_split(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int direction) {
-  SpDev& sp = ctx->sp;
-  SmDev& sm = ctx->sm;
-  const int cap = sp.cap;
-  const size_t c2 = (size_t)cap + 2;
+int run_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
+  CK(cudaMemsetAsync(ctx->fill_counts, 0, sizeof(int) * (size_t)L.B, st));
+  CK(cudaMemsetAsync(ctx->fill_done, 0, sizeof(int) * (size_t)L.B, st));
+  int B = L.B;
+  long long pix = L.pix, q = L.q;
+  int break_iter = kFillBreakIter;
+  Slot* d = L.d;
+  void* args[] = {(void*)&d, (void*)&B, (void*)&pix, (void*)&q, (void*)&ctx->ctl,
+                  (void*)&ctx->fill_counts, (void*)&ctx->fill_done, (void*)&break_iter};
+  return coop_launch(ctx, st, (const void*)kb_fill, blocks_for(pix), ctx->coop_fill, args);
+}
+
+int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmConsts& K,
+              const stspix_config& cfg, int dir_b, int dir_p) {
   ctx->cur_fam = STSPIX_FAM_SPLIT;
-  LAUNCH1(k_split_begin, ctx->sc);
-  CK(cudaMemsetAsync(ctx->d1, 0xff, sizeof(int) * (size_t)f.npix, st));
-  CK(cudaMemsetAsync(ctx->d2, 0xff, sizeof(int) * (size_t)f.npix, st));
-  LAUNCH(k_split_seed, cap, sp, f.seg, f.H, f.W, direction, ctx->sc, ctx->d1, ctx->d2);
-  int r = run_relax(ctx, st, 0, f.seg, ctx->d1, ctx->d2, f.H, f.W);
+  LAUNCHS(kb_split_begin, L, nb);
+  LAUNCHB(kb_split_clear, L.max_npix, L, nb);
+  LAUNCHB(kb_split_seed, L.max_cap, L, nb, dir_b, dir_p);
+  int r = run_relax(ctx, st, 0, L, nb);
   if (r) return r;
-  LAUNCH(k_split_partition, f.npix, f.seg, ctx->d1, ctx->d2, f.npix, ctx->sc, ctx->smseg);
-  CK(cudaMemsetAsync(sm.count, 0, sizeof(int) * c2, st));
-  CK(cudaMemsetAsync(sm.ninvalid, 0, sizeof(int) * c2, st));
-  CK(cudaMemsetAsync(sm.s, 0, sizeof(long long) * 3 * c2, st));
-  CK(cudaMemsetAsync(sm.sq, 0, sizeof(long long) * 3 * c2, st));
-  LAUNCH(k_sm_accumulate, (long long)f.H * ((f.W + 15) / 16), f.img, ctx->smseg,
-         f.prop_mode ? f.shifted : nullptr, f.H, f.W, cap + 2, sm);
-  LAUNCH(k_split_decide, cap, sp, sm, ctx->sc, f.K, f.cfg.split_alpha, f.prop_mode,
-         ctx->accept);
-  LAUNCHG(k_scan_flags, 1, 1024, ctx->accept, nullptr, cap, ctx->excl, &ctx->sc->tmp2);
-  LAUNCH(k_split_commit, cap, sp, sm, ctx->sc, ctx->accept, ctx->excl, f.prop_mode);
-  LAUNCH(k_split_apply, f.npix, f.seg, ctx->smseg, f.npix, sp, sm, ctx->sc, ctx->accept,
-         f.prop_mode);
-  LAUNCH1(k_split_end, ctx->sc, &ctx->sc->tmp2);
+  LAUNCHB(kb_split_partition, L.max_npix, L, nb);
+  LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
+  LAUNCHG(kb_sm_accumulate, dim3(blocks_for(L.max_sm), (unsigned)nb), kThreads, L.d, 1);
+  LAUNCHB(kb_split_decide, L.max_cap, L, nb, K, cfg.split_alpha);
+  LAUNCHG(kb_scan, (unsigned)nb, 1024, L.d, 1);
+  LAUNCHB(kb_split_commit, L.max_cap, L, nb);
+  LAUNCHB(kb_split_apply, L.max_npix, L, nb);
+  LAUNCHS(kb_split_end, L, nb);
   return STSPIX_OK;
 }
 
-int run_relabel(stspix_ctx* ctx, cudaStream_t st, const Frame& f) {
-  SpDev& sp = ctx->sp;
-  const int cap = sp.cap;
+// relabel (relabel.cu:126-409) on the propagated slots among the first nb.
+int run_relabel(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
+                const stspix_config& cfg) {
   ctx->cur_fam = STSPIX_FAM_MERGE;
-  CK(cudaMemsetAsync(ctx->living, 0, (size_t)cap + 2, st));
-  LAUNCH(k_living, f.npix, f.seg, f.npix, ctx->sc, ctx->living);
-  LAUNCH(k_relabel_init, cap, cap, ctx->rbest, ctx->ss);
+  LAUNCHB(kb_relabel_init, L.max_cap + 2, L, nb);
+  LAUNCHB(kb_living, L.max_npix, L, nb);
   const int chunk = 256;
-  dim3 g(blocks_for(cap), (unsigned)std::max(1, (f.n_prev + chunk - 1) / chunk));
-  LAUNCHG(k_relabel_compare, g, kThreads, sp, f.prev_prior_mu_app, f.n_prev, ctx->sc,
-          ctx->living, ctx->rbest, ctx->ss, chunk);
-  LAUNCH(k_relabel_mark, cap, cap, ctx->sc, ctx->living, ctx->rbest, ctx->ss,
-         f.cfg.thresh_relabel, f.cfg.thresh_new, ctx->rid, ctx->mint);
-  LAUNCHG(k_scan_flags, 1, 1024, ctx->mint, nullptr, cap, ctx->excl, &ctx->sc->tmp2);
-  CK(cudaMemsetAsync(ctx->src_of, 0xff, sizeof(int) * ((size_t)cap + 2), st));
-  LAUNCH(k_relabel_ids, cap, cap, ctx->sc, ctx->mint, ctx->excl, ctx->rid, ctx->src_of);
-  LAUNCH(k_relabel_params, cap, sp, ctx->rid, ctx->src_of, f.n_prev);
-  LAUNCH(k_relabel_apply, f.npix, f.seg, f.npix, cap, ctx->rid);
-  LAUNCH(k_count_revived, cap, ctx->rid, ctx->mint, cap, ctx->sc);
-  LAUNCH1(k_relabel_end, ctx->sc, &ctx->sc->tmp2, ctx->rid, cap);
+  dim3 g(blocks_for(L.max_cap), (unsigned)std::max(1, (L.max_nprev + chunk - 1) / chunk),
+         (unsigned)nb);
+  LAUNCHG(kb_relabel_compare, g, kThreads, L.d, chunk);
+  LAUNCHB(kb_relabel_mark, L.max_cap, L, nb, cfg.thresh_relabel, cfg.thresh_new);
+  LAUNCHG(kb_scan, (unsigned)nb, 1024, L.d, 2);
+  LAUNCHB(kb_relabel_ids, L.max_cap, L, nb);
+  LAUNCHB(kb_relabel_params, L.max_cap, L, nb);
+  LAUNCHB(kb_relabel_apply, L.max_npix, L, nb);
+  LAUNCHB(kb_count_revived, L.max_cap, L, nb);
+  LAUNCHS(kb_relabel_end, L, nb);
   return STSPIX_OK;
 }
 
-int run_merge(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int direction) {
-  SpDev& sp = ctx->sp;
-  SmDev& sm = ctx->sm;
-  const int cap = sp.cap;
-  const size_t c2 = (size_t)cap + 2;
+int run_merge(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmConsts& K,
+              const stspix_config& cfg, int dir_b, int dir_p) {
   ctx->cur_fam = STSPIX_FAM_MERGE;
-  CK(cudaMemsetAsync(sm.pair, 0xff, sizeof(int) * c2, st));
-  CK(cudaMemsetAsync(sm.claim, 0x7f, sizeof(int) * c2, st));
-  LAUNCH(k_merge_candidates, f.npix, f.seg, ctx->border, f.H, f.W, direction, f.prop_mode,
-         sp.prop, cap, sm.pair);
-  CK(cudaMemsetAsync(sm.count, 0, sizeof(int) * c2, st));
-  CK(cudaMemsetAsync(sm.s, 0, sizeof(long long) * 3 * c2, st));
-  CK(cudaMemsetAsync(sm.sq, 0, sizeof(long long) * 3 * c2, st));
-  LAUNCH(k_sm_accumulate, (long long)f.H * ((f.W + 15) / 16), f.img, f.seg, nullptr, f.H, f.W,
-         cap, sm);
-  LAUNCH(k_merge_single, cap, sp, sm, f.K);
-  LAUNCH(k_merge_decide, cap, sp, sm, ctx->sc, f.K, f.cfg.merge_alpha);
-  LAUNCH(k_merge_flag, cap, sp, sm, ctx->valid0);
-  LAUNCH(k_merge_remove, cap, sp, sm, ctx->sc, ctx->valid0, f.prop_mode);
-  LAUNCH(k_merge_apply, f.npix, f.seg, f.npix, cap, sm);
+  LAUNCHB(kb_merge_clear, L.max_cap + 2, L, nb);
+  LAUNCHB(kb_merge_candidates, L.max_npix, L, nb, dir_b, dir_p);
+  LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
+  LAUNCHG(kb_sm_accumulate, dim3(blocks_for(L.max_sm), (unsigned)nb), kThreads, L.d, 0);
+  LAUNCHB(kb_merge_single, L.max_cap, L, nb, K);
+  LAUNCHB(kb_merge_decide, L.max_cap, L, nb, K, cfg.merge_alpha);
+  LAUNCHB(kb_merge_flag, L.max_cap, L, nb);
+  LAUNCHB(kb_merge_remove, L.max_cap, L, nb);
+  LAUNCHB(kb_merge_apply, L.max_npix, L, nb);
   return STSPIX_OK;
 }
 
-// bass (bass.cu:46-181) / prop_bass_v3 (prop.cu:326-468) outer loop.
-int bass_loop(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int niters, int stop_after,
-              int extra_update) {
+// bass (bass.cu:46-181) / prop_bass_v3 (prop.cu:326-468) outer loop over a table
+// sorted by iteration count (nit[i] descending).  stop_after >= 0 (one slot only):
+// stop before that iteration (bass_partial).
+int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector<int>& nit,
+              const stspix_config& cfg, const SmConsts& K, int stop_after, int extra_update) {
   int r;
-  int count = 1;
-  const int P = f.cfg.sm_period > 0 ? f.cfg.sm_period : 4;
-  for (int idx = 0; idx < niters; idx++) {
+  int count_b = 1, count_p = 1;
+  const int P = cfg.sm_period > 0 ? cfg.sm_period : 4;
+  const int maxn = L.B ? nit[0] : 0;
+  int nb = L.B;
+  for (int idx = 0; idx < maxn; idx++) {
+    while (nb > 0 && nit[nb - 1] <= idx) nb--;
     if (stop_after >= 0 && idx == stop_after) {
-      if (extra_update && (r = update_params(ctx, st, f))) return r;
+      if (extra_update && (r = update_params(ctx, st, L, nb))) return r;
       return STSPIX_OK;
     }
-    if ((r = update_params(ctx, st, f))) return r;
-    if (idx > f.cfg.sm_start) {
+    if ((r = update_params(ctx, st, L, nb))) return r;
+    if (idx > cfg.sm_start) {
       if (idx % P == 0) {
-        count += 1;
-        int direction = count % 2 + 1;
-        if ((r = run_split(ctx, st, f, direction))) return r;
-        if ((r = update_params(ctx, st, f))) return r;
+        count_b += 1;
+        count_p += 1;
+        if ((r = run_split(ctx, st, L, nb, K, cfg, count_b % 2 + 1, count_p % 2 + 1))) return r;
+        if ((r = update_params(ctx, st, L, nb))) return r;
       }
       if (idx % P == P / 2) {
-        int direction;
-        if (f.prop_mode) {
-          count += 1;
-          direction = count % 2;
-          if ((r = run_relabel(ctx, st, f))) return r;
-        } else {
-          direction = count % 2;
-        }
-        if ((r = run_merge(ctx, st, f, direction))) return r;
-        if ((r = update_params(ctx, st, f))) return r;
+        count_p += 1;  // propagated frames step the direction again before merging
+        if (L.any_prop && (r = run_relabel(ctx, st, L, nb, cfg))) return r;
+        if ((r = run_merge(ctx, st, L, nb, K, cfg, count_b % 2, count_p % 2))) return r;
+        if ((r = update_params(ctx, st, L, nb))) return r;
       }
     }
     const int nx = idx + 1;
-    const bool merge_next = nx < niters && nx > f.cfg.sm_start && nx % P == P / 2;
-    if ((r = update_seg(ctx, st, f, merge_next || stop_after >= 0))) return r;
+    const bool merge_next = nx < maxn && nx > cfg.sm_start && nx % P == P / 2;
+    if ((r = update_seg(ctx, st, L, nb, cfg, merge_next || stop_after >= 0))) return r;
   }
   if (stop_after >= 0) {
-    if (extra_update && (r = update_params(ctx, st, f))) return r;
+    if (extra_update && (r = update_params(ctx, st, L, L.B))) return r;
     return STSPIX_OK;
   }
-  if ((r = update_params(ctx, st, f))) return r;
+  // final update_params + store_sample; slots that finished earlier were untouched
+  // since, so running theirs here is the same as running it right after their loop
+  if ((r = update_params(ctx, st, L, L.B))) return r;
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
-  LAUNCH(k_store_sample, ctx->sp.cap, ctx->sp);
+  LAUNCHB(kb_store_sample, L.max_cap, L, L.B);
   return STSPIX_OK;
 }
 
 // compactify_new_superpixels (compact_spix.cu:41-89) for ids >= lo, moving params.
-int compact(stspix_ctx* ctx, cudaStream_t st, const Frame& f, int lo) {
-  const int cap = ctx->sp.cap;
+int compact(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   ctx->cur_fam = STSPIX_FAM_OTHER;
-  CK(cudaMemsetAsync(ctx->flags, 0, (size_t)cap + 2, st));
-  LAUNCH1(k_calc_n, ctx->sc, lo, cap);
-  LAUNCH(k_mark_present, f.npix, f.seg, f.npix, lo, &ctx->sc->max_spix, 0, ctx->flags);
-  LAUNCHG(k_scan_flags, 1, 1024, ctx->flags, &ctx->sc->tmp2, 0, ctx->excl, &ctx->sc->tmp1);
-  LAUNCH(k_compact_gather, cap, ctx->sp, ctx->tmp, lo, &ctx->sc->max_spix, ctx->flags, ctx->excl);
-  LAUNCH(k_compact_scatter, cap, ctx->sp, ctx->tmp, lo, &ctx->sc->tmp1);
-  LAUNCH(k_remap, f.npix, f.seg, f.npix, lo, ctx->excl);
-  LAUNCH1(k_finish_compact, ctx->sc, lo, &ctx->sc->tmp1);
+  LAUNCHB(kb_clear_flags, L.max_cap + 2, L, L.B);
+  LAUNCHS(kb_scalars, L, L.B, (int)kOpCompactN);
+  LAUNCHB(kb_mark_present, L.max_npix, L, L.B, 1);
+  LAUNCHG(kb_scan, (unsigned)L.B, 1024, L.d, 3);
+  LAUNCHB(kb_compact_gather, L.max_cap, L, L.B);
+  LAUNCHB(kb_compact_scatter, L.max_cap, L, L.B);
+  LAUNCHB(kb_remap, L.max_npix, L, L.B, 1);
+  LAUNCHS(kb_scalars, L, L.B, (int)kOpCompactEnd);
   return STSPIX_OK;
 }
 
-// run_bass (bass.cu:221-345) on device buffers; params_out may be null.
-int bass_frame(stspix_ctx* ctx, cudaStream_t st, const float* img, int H, int W,
-               const stspix_config& cfg, int* seg, const stspix_params* params_out,
-               int stop_after, int extra_update) {
-  const int npix = H * W;
-  double Hh, w;
-  int nx, ny;
-  hex_geometry(cfg.sp_size, W, H, &Hh, &w, &nx, &ny);
-  const int nraw = nx * ny;
-  const int nbuf = 30 * nraw;
-  int r;
-  if ((r = ensure(ctx, npix, std::max(nbuf, 64)))) return r;
-  Frame f{img, seg, H, W, npix, cfg, sm_constants(cfg), nullptr, 0, 0, nullptr};
+// run_bass set-up (bass.cu:221-262) on the BASS slots.
+int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
+  if (L.B <= 0) return STSPIX_OK;
   ctx->cur_fam = STSPIX_FAM_OTHER;
-  LAUNCH1(k_frame_begin, ctx->sc, 0, nbuf);
-  LAUNCH(k_init_hex, npix, seg, H, W, Hh, w, nx, ny);
+  LAUNCHB(kb_init_hex, L.max_npix, L, L.B);
   // compact the hex ids (extract_unique_ids + compactify, bass.cu:251-252)
-  CK(cudaMemsetAsync(ctx->flags, 0, (size_t)ctx->sp.cap + 2, st));
-  LAUNCH(k_mark_present, npix, seg, npix, 0, nullptr, nraw - 1, ctx->flags);
-  LAUNCHG(k_scan_flags, 1, 1024, ctx->flags, nullptr, nraw, ctx->excl, &ctx->sc->nspix);
-  LAUNCH(k_remap, npix, seg, npix, 0, ctx->excl);
-  LAUNCH1(k_bass_after_compact, ctx->sc);
-  LAUNCH(k_init_bass_params, ctx->sp.cap, ctx->sp, &ctx->sc->nspix, npix, cfg.sp_size);
-  CK(cudaMemsetAsync(ctx->sp.count, 0, sizeof(int) * (size_t)ctx->sp.cap, st));
-  CK(cudaMemsetAsync(ctx->sp.acc, 0, sizeof(long long) * 8 * (size_t)ctx->sp.cap, st));
-  LAUNCHG(k_accumulate, (unsigned)(((long long)H * ((W + 7) / 8) + 127) / 128), 128, img, seg, H,
-          W, ctx->sp);
-  LAUNCH(k_init_prior_mu, ctx->sp.cap, ctx->sp, &ctx->sc->nspix);
-  LAUNCH(k_find_border, npix, seg, ctx->border, H, W);
-  if ((r = bass_loop(ctx, st, f, cfg.niters, stop_after, extra_update))) return r;
-  if (stop_after >= 0) return STSPIX_OK;
-  if ((r = compact(ctx, st, f, 0))) return r;
-  if (params_out) LAUNCH(k_read_params, ctx->sp.cap, ctx->sp, &ctx->sc->nspix, *params_out);
+  LAUNCHB(kb_clear_flags, L.max_cap + 2, L, L.B);
+  LAUNCHB(kb_mark_present, L.max_npix, L, L.B, 0);
+  LAUNCHG(kb_scan, (unsigned)L.B, 1024, L.d, 0);
+  LAUNCHB(kb_remap, L.max_npix, L, L.B, 0);
+  LAUNCHS(kb_scalars, L, L.B, (int)kOpAfterHex);
+  LAUNCHB(kb_init_bass_params, L.max_cap, L, L.B);
+  LAUNCHB(kb_clear_stats, L.max_cap, L, L.B);
+  LAUNCHG(kb_accumulate, dim3((unsigned)((L.max_acc + 127) / 128), (unsigned)L.B), 128, L.d);
+  LAUNCHB(kb_init_prior_mu, L.max_cap, L, L.B);
+  LAUNCHB(kb_find_border, L.max_npix, L, L.B);
   return STSPIX_OK;
 }
 
-// shift_and_fill (shift_and_fill.cu:108-339).
-int shift_fill(stspix_ctx* ctx, cudaStream_t st, const int* prev, const stspix_params& pp,
-               int n_prev, const float* flow, int H, int W, int* filled, int* shifted) {
-  const int npix = H * W;
+// shift_and_fill (shift_and_fill.cu:108-339) on the propagated slots.
+int shift_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
+  if (L.B <= 0) return STSPIX_OK;
   int r;
-  if ((r = ensure(ctx, npix, std::max(10 * n_prev + 2, 64)))) return r;
   ctx->cur_fam = STSPIX_FAM_PROP;
-  CK(cudaMemsetAsync(ctx->cnt_pool, 0, sizeof(int) * (size_t)n_prev, st));
-  CK(cudaMemsetAsync(ctx->fs, 0, sizeof(long long) * 2 * (size_t)n_prev, st));
-  LAUNCH(k_flow_pool, (long long)H * ((W + 15) / 16), prev, flow, H, W, n_prev, ctx->cnt_pool,
-         ctx->fs);
-  LAUNCH(k_flow_mean, n_prev, n_prev, ctx->cnt_pool, ctx->fs, pp.mu_shape, ctx->fds,
-         ctx->centers);
-  CK(cudaMemsetAsync(ctx->hits, 0, sizeof(int) * (size_t)npix, st));
-  CK(cudaMemsetAsync(ctx->best, 0xff, sizeof(unsigned long long) * (size_t)npix, st));
-  LAUNCH(k_shift, npix, prev, H, W, n_prev, ctx->cnt_pool, ctx->fds, ctx->hits, ctx->best);
-  CK(cudaMemsetAsync(&ctx->sc->ninvalid, 0, sizeof(int), st));
-  LAUNCH(k_shift_decode, npix, ctx->hits, ctx->best, npix, shifted, filled, ctx->sc);
-  CK(cudaMemsetAsync(ctx->cs, 0, sizeof(int) * (size_t)n_prev, st));
-  LAUNCH(k_count_labels, npix, filled, npix, n_prev, ctx->cs);
+  LAUNCHB(kb_prop_clear, std::max<long long>(L.max_npix, L.max_nprev), L, L.B);
+  LAUNCHG(kb_flow_pool, dim3(blocks_for(L.max_sm), (unsigned)L.B), kThreads, L.d);
+  LAUNCHB(kb_flow_mean, L.max_nprev, L, L.B);
+  LAUNCHB(kb_shift, L.max_npix, L, L.B);
+  LAUNCHB(kb_shift_decode, L.max_npix, L, L.B);
+  LAUNCHB(kb_count_labels, L.max_npix, L, L.B, 0);
   // fill, invalidate disconnected, fill
-  for (int pass = 0; pass < 2; pass++) {
-    CK(cudaMemsetAsync(ctx->iter_counts, 0, sizeof(int) * (kFillBreakIter + 2), st));
-    int break_iter = kFillBreakIter;
-    void* args[] = {(void*)&filled, (void*)&ctx->centers, (void*)&H, (void*)&W,
-                    (void*)&ctx->border, (void*)&ctx->sc, (void*)&ctx->iter_counts,
-                    (void*)&break_iter};
-    if ((r = coop_launch(ctx, st, (const void*)k_fill_coop, (int)blocks_for(npix),
-                         ctx->coop_fill, args)))
-      return r;
-    if (pass == 0) {
-      LAUNCH(k_cc_init, npix, filled, npix, ctx->d1);
-      if ((r = run_relax(ctx, st, 1, filled, ctx->d1, nullptr, H, W))) return r;
-      CK(cudaMemsetAsync(ctx->d2, 0, sizeof(int) * (size_t)npix, st));
-      LAUNCH(k_cc_size, npix, ctx->d1, npix, ctx->d2);
-      CK(cudaMemsetAsync(ctx->ccbest, 0, sizeof(unsigned long long) * (size_t)n_prev, st));
-      LAUNCH(k_cc_best, npix, filled, ctx->d1, ctx->d2, npix, n_prev, ctx->ccbest);
-      LAUNCH(k_cc_invalidate, npix, filled, ctx->d1, npix, n_prev, ctx->ccbest);
-    }
-  }
-  CK(cudaMemsetAsync(ctx->cf, 0, sizeof(int) * (size_t)n_prev, st));
-  LAUNCH(k_count_labels, npix, filled, npix, n_prev, ctx->cf);
-  LAUNCH(k_shift_params, n_prev, n_prev, ctx->cnt_pool, ctx->cs, ctx->cf, pp);
+  if ((r = run_fill(ctx, st, L))) return r;
+  LAUNCHB(kb_cc_init, L.max_npix, L, L.B);
+  if ((r = run_relax(ctx, st, 1, L, L.B))) return r;
+  LAUNCHB(kb_cc_size, L.max_npix, L, L.B);
+  LAUNCHB(kb_cc_best, L.max_npix, L, L.B);
+  LAUNCHB(kb_cc_invalidate, L.max_npix, L, L.B);
+  if ((r = run_fill(ctx, st, L))) return r;
+  LAUNCHB(kb_count_labels, L.max_npix, L, L.B, 1);
+  LAUNCHB(kb_shift_params, L.max_nprev, L, L.B);
   return STSPIX_OK;
 }
 
-// run_prop (prop.cu:677-865); seg already holds the filled labels.
-int prop_frame(stspix_ctx* ctx, cudaStream_t st, const float* img, int H, int W,
-               const stspix_config& cfg, int niters, int* seg, const int* shifted,
-               const stspix_params& prev, int n_prev, const stspix_params* params_out) {
-  const int npix = H * W;
-  int r;
-  if ((r = ensure(ctx, npix, std::max(10 * n_prev + 2, 64)))) return r;
-  Frame f{img, seg, H, W, npix, cfg, sm_constants(cfg), shifted, 1, n_prev, prev.prior_mu_app};
+// run_prop set-up (prop.cu:677-720): write_params + mark_active.
+int prop_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
+  if (L.B <= 0) return STSPIX_OK;
   ctx->cur_fam = STSPIX_FAM_OTHER;
-  LAUNCH1(k_frame_begin, ctx->sc, n_prev - 1, 10 * n_prev);
-  LAUNCH(k_write_params, ctx->sp.cap, ctx->sp, prev, n_prev, cfg.sp_size);
-  LAUNCH(k_mark_active, npix, seg, npix, ctx->sp);
-  LAUNCH1(k_prop_begin, ctx->sc, n_prev);
-  if ((r = bass_loop(ctx, st, f, niters, -1, 0))) return r;
-  if ((r = compact(ctx, st, f, n_prev))) return r;
-  if (params_out) LAUNCH(k_read_params, ctx->sp.cap, ctx->sp, &ctx->sc->nspix, *params_out);
+  LAUNCHB(kb_write_params, L.max_cap, L, L.B);
+  LAUNCHB(kb_mark_active, L.max_npix, L, L.B);
   return STSPIX_OK;
 }
 
-int sync_scalars(stspix_ctx* ctx, cudaStream_t st) {
-  CK(cudaMemcpyAsync(ctx->sc_host, ctx->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+int read_scalars(stspix_ctx* ctx, cudaStream_t st, int B) {
+  CK(cudaMemcpyAsync(ctx->sc_host, ctx->sc, sizeof(Scalars) * (size_t)B, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->sc_host + B, ctx->ctl, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
   prof_harvest(ctx);
-  const Scalars& s = *ctx->sc_host;
-  ctx->log.nsplits = s.nsplits;
-  ctx->log.nmerges = s.nmerges;
-  ctx->log.nrevived = s.nrevived;
-  ctx->log.nminted = s.nminted;
-  ctx->log.near_ties = s.near_ties;
-  ctx->log.fill_iters = s.fill_iters;
-  ctx->log.nspix = s.nspix;
+  return STSPIX_OK;
+}
+
+void fill_log(stspix_frame_log& log, const Scalars& s, int niters) {
+  log.nsplits = s.nsplits;
+  log.nmerges = s.nmerges;
+  log.nrevived = s.nrevived;
+  log.nminted = s.nminted;
+  log.near_ties = s.near_ties;
+  log.fill_iters = s.fill_iters;
+  log.nspix = s.nspix;
+  log.niters = niters;
+}
+
+struct BatchOut {
+  std::vector<int> nspix, niters, status;
+  std::vector<stspix_frame_log> log;
+};
+
+// The batch runner.  stages: kStageShift and/or kStageSeg.  Frames are processed
+// in workspace positions f.slot (distinct).  Returns a call-level error; per-frame
+// statuses land in out.
+int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
+              const stspix_config& cfg, int stages, BatchOut& out, int stop_after = -1,
+              int extra_update = 0) {
+  const int B = (int)fr.size();
+  int r;
+  if ((r = ensure_bcap(ctx, B + 1))) return r;
+  std::vector<int> caps(B);
+  for (int i = 0; i < B; i++) {
+    caps[i] = slot_cap(fr[i]);
+    if ((r = ensure_slot(ctx, fr[i].slot, fr[i].H * fr[i].W, caps[i]))) return r;
+  }
+  std::vector<Slot> all, bass, prop;
+  for (int i = 0; i < B; i++) {
+    Slot s = make_slot(ctx, fr[i], caps[i]);
+    all.push_back(s);
+    (fr[i].mode ? prop : bass).push_back(s);
+  }
+  List La = make_list(ctx, 0, all);
+  List Lb = make_list(ctx, 1, bass);
+  List Lp = make_list(ctx, 2, prop);
+  if ((r = upload(ctx, st, La, 0)) || (r = upload(ctx, st, Lb, 1)) || (r = upload(ctx, st, Lp, 2)))
+    return r;
+  CK(cudaMemsetAsync(ctx->ctl, 0, sizeof(Scalars), st));
+  ctx->cur_fam = STSPIX_FAM_OTHER;
+  LAUNCHS(kb_scalars, La, B, (int)kOpBegin);
+  if ((stages & kStageShift) && (r = shift_fill(ctx, st, Lp))) return r;
+  out.nspix.assign(B, 0);
+  out.niters.assign(B, 0);
+  out.status.assign(B, 0);
+  out.log.assign(B, stspix_frame_log{});
+  if (!(stages & kStageSeg)) {
+    if ((r = read_scalars(ctx, st, B))) return r;
+    for (int i = 0; i < B; i++) {
+      out.status[i] = ctx->sc_host[i].status ? ctx->sc_host[i].status : ctx->sc_host[B].status;
+      fill_log(out.log[i], ctx->sc_host[i], 0);
+    }
+    return STSPIX_OK;
+  }
+  // iteration counts: BASS frames cfg.niters; propagated frames the explicit count,
+  // cfg.prop_niters, or the 4/8/12 ladder on the hole fraction (pyapi.cu:143-146)
+  std::vector<int> nit(B, -1);
+  bool need_ladder = false;
+  for (int i = 0; i < B; i++) {
+    if (!fr[i].mode) nit[i] = cfg.niters;
+    else if (fr[i].niters >= 0) nit[i] = fr[i].niters;
+    else if (cfg.prop_niters > 0) nit[i] = cfg.prop_niters;
+    else need_ladder = true;
+  }
+  if ((r = bass_init(ctx, st, Lb))) return r;
+  if (need_ladder) {
+    if ((r = read_scalars(ctx, st, B))) return r;
+    for (int i = 0; i < B; i++) {
+      if (nit[i] >= 0) continue;
+      const int npix = fr[i].H * fr[i].W;
+      float iperc = ctx->sc_host[i].ninvalid / (1.0 * npix);
+      nit[i] = iperc > 0.20 ? 12 : (iperc < 0.01 ? 4 : 8);
+    }
+  }
+  if ((r = prop_init(ctx, st, Lp))) return r;
+  // the loop table: slots sorted by iteration count, descending (stable)
+  std::vector<int> order(B);
+  for (int i = 0; i < B; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nit[a] > nit[b]; });
+  std::vector<Slot> sorted;
+  std::vector<int> nit_sorted;
+  for (int i : order) { sorted.push_back(all[i]); nit_sorted.push_back(nit[i]); }
+  List Ls = La;
+  if (!std::is_sorted(order.begin(), order.end())) {
+    Ls = make_list(ctx, 0, sorted);
+    if ((r = upload(ctx, st, Ls, 0))) return r;
+  }
+  const SmConsts K = sm_constants(cfg);
+  if ((r = bass_loop(ctx, st, Ls, nit_sorted, cfg, K, stop_after, extra_update))) return r;
+  if (stop_after < 0) {
+    if ((r = compact(ctx, st, Ls))) return r;
+    LAUNCHB(kb_read_params, Ls.max_cap, Ls, Ls.B);
+    LAUNCHB(kb_save_prev, Ls.max_npix, Ls, Ls.B);
+  }
+  if ((r = read_scalars(ctx, st, B))) return r;
+  for (int i = 0; i < B; i++) {
+    const Scalars& s = ctx->sc_host[i];
+    out.nspix[i] = s.nspix;
+    out.niters[i] = nit[i];
+    out.status[i] = s.status ? s.status : ctx->sc_host[B].status;
+    fill_log(out.log[i], s, nit[i]);
+  }
   return STSPIX_OK;
 }
 
@@ -659,6 +790,81 @@ int check_size(stspix_ctx* ctx, int H, int W) {
   return STSPIX_OK;
 }
 
+int first_status(stspix_ctx* ctx, const BatchOut& o) {
+  for (size_t i = 0; i < o.status.size(); i++)
+    if (o.status[i]) return fail(ctx, o.status[i], "device status %d (frame %zu)", o.status[i], i);
+  return STSPIX_OK;
+}
+
+// Video stream state: label buffer and parameter ping-pong grown to `cap`,
+// keeping the current parameters.
+int video_ensure(stspix_ctx* ctx, cudaStream_t st, stspix_video* v, int cap) {
+  if (!v->labels) AL(v->lbufs, v->labels, (size_t)v->H * v->W);
+  if (cap <= v->pp_cap) return STSPIX_OK;
+  std::vector<Buf> old = v->pbufs;
+  stspix_params oldp = v->pp[v->cur];
+  v->pbufs.clear();
+  int r;
+  for (int i = 0; i < 2; i++)
+    if ((r = alloc_params(ctx, v->pbufs, v->pp[i], cap))) return r;
+  if (v->n > 0) {
+    stspix_params& np = v->pp[v->cur];
+    size_t k = (size_t)v->n;
+    CK(cudaMemcpyAsync(np.mu_app, oldp.mu_app, 12 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.prior_mu_app, oldp.prior_mu_app, 12 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.mu_shape, oldp.mu_shape, 16 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.sigma_shape, oldp.sigma_shape, 24 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.logdet_sigma_shape, oldp.logdet_sigma_shape, 4 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.prior_mu_shape, oldp.prior_mu_shape, 16 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.prior_sigma_shape, oldp.prior_sigma_shape, 24 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.sample_sigma_shape, oldp.sample_sigma_shape, 24 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.counts, oldp.counts, 4 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.sm_counts, oldp.sm_counts, 4 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.prior_counts, oldp.prior_counts, 4 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.ids, oldp.ids, 4 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(np.invalid_counts, oldp.invalid_counts, 4 * k, cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  free_list(old);
+  v->pp_cap = cap;
+  return STSPIX_OK;
+}
+
+// A frame of video v: BASS on its first frame, else shift + propagated BASS.
+int video_frame(stspix_ctx* ctx, cudaStream_t st, stspix_video* v, const float* img,
+                const float* flow, int sp_size, int* labels_out, int slot, FrameDesc& f) {
+  f.img = img;
+  f.H = v->H; f.W = v->W;
+  f.sp_size = sp_size;
+  f.seg = labels_out;
+  f.slot = slot;
+  f.resident = nullptr;
+  int r;
+  if (v->n <= 0) {
+    f.mode = 0;
+    int cap = slot_cap(f);
+    if ((r = video_ensure(ctx, st, v, cap))) return r;
+    f.pout = v->pp[v->cur];
+  } else {
+    f.mode = 1;
+    f.flow = flow;
+    f.prev = v->labels;
+    f.n_prev = v->n;
+    int cap = slot_cap(f);
+    if ((r = video_ensure(ctx, st, v, cap))) return r;
+    f.pprev = v->pp[v->cur];
+    f.pout = v->pp[1 - v->cur];
+  }
+  f.resident = v->labels;
+  return STSPIX_OK;
+}
+
+void video_commit(stspix_video* v, int mode, int nspix) {
+  if (mode) v->cur = 1 - v->cur;
+  v->n = nspix;
+  v->frames++;
+}
+
 }  // namespace
 
 // =========================================================================
@@ -673,7 +879,7 @@ void stspix_default_config(stspix_config* c) {
   c->thresh_relabel = 1e-5f; c->thresh_new = 1e-2f;
 }
 
-int stspix_version(void) { return 1; }
+int stspix_version(void) { return 2; }
 
 int stspix_create(stspix_ctx** out, int device) {
   if (!out) return STSPIX_ERR_ARG;
@@ -687,28 +893,26 @@ int stspix_create(stspix_ctx** out, int device) {
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k_relax_bfs, kThreads, 0);
   // Cooperative grids use at most one block per SM: with up to
   // (resident blocks per SM) streams launching cooperative kernels at once, all of
   // their blocks can still be resident together (other kernels always drain).
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)kb_relax_bfs, kThreads, 0);
   ctx->coop_relax0 = std::min(nb, 1) * ctx->num_sms;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k_relax_cc, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)kb_relax_cc, kThreads, 0);
   ctx->coop_relax1 = std::min(nb, 1) * ctx->num_sms;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)k_fill_coop, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)kb_fill, kThreads, 0);
   ctx->coop_fill = std::min(nb, 1) * ctx->num_sms;
-  if (!coop || ctx->coop_relax0 <= 0 || ctx->coop_fill <= 0) {
+  if (!coop || ctx->coop_relax0 <= 0 || ctx->coop_relax1 <= 0 || ctx->coop_fill <= 0) {
     delete ctx;
     return STSPIX_ERR_CUDA;
   }
-  std::vector<Buf> ctl;
-  if (cudaMalloc(&ctx->round_flags, sizeof(int) * 4096) != cudaSuccess ||
-      cudaMalloc(&ctx->iter_counts, sizeof(int) * (kFillBreakIter + 2)) != cudaSuccess ||
-      cudaMalloc(&ctx->sc, sizeof(Scalars)) != cudaSuccess ||
-      cudaMallocHost(&ctx->sc_host, sizeof(Scalars)) != cudaSuccess) {
+  if (cudaMalloc(&ctx->ctl, sizeof(Scalars)) != cudaSuccess ||
+      ensure_bcap(ctx, 4) != STSPIX_OK) {
     delete ctx;
     return STSPIX_ERR_NOMEM;
   }
-  cudaMemset(ctx->sc, 0, sizeof(Scalars));
+  cudaEventCreate(&ctx->batch_ev[0]);
+  cudaEventCreate(&ctx->batch_ev[1]);
   cudaDeviceSynchronize();
   *out = ctx;
   return STSPIX_OK;
@@ -718,16 +922,16 @@ int stspix_destroy(stspix_ctx* ctx) {
   if (!ctx) return STSPIX_OK;
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
-  free_list(ctx->pix_bufs);
-  free_list(ctx->sp_bufs);
-  free_list(ctx->pp_bufs);
+  if (ctx->fwd) stspix_video_destroy(ctx->fwd);
+  for (auto& w : ctx->work) { free_list(w.pix); free_list(w.sp); }
+  free_list(ctx->ctl_bufs);
   prof_harvest(ctx);
-  for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.first); ctx->ev_free.push_back(e.second); }
+  for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.a); ctx->ev_free.push_back(e.b); }
   for (auto e : ctx->ev_free) cudaEventDestroy(e);
-  cudaFree(ctx->round_flags);
-  cudaFree(ctx->iter_counts);
-  cudaFree(ctx->sc);
-  cudaFreeHost(ctx->sc_host);
+  for (auto e : ctx->batch_ev) if (e) cudaEventDestroy(e);
+  cudaFree(ctx->ctl);
+  if (ctx->sc_host) cudaFreeHost(ctx->sc_host);
+  if (ctx->h_slots) cudaFreeHost(ctx->h_slots);
   delete ctx;
   return STSPIX_OK;
 }
@@ -777,19 +981,18 @@ int stspix_run_bass(stspix_ctx* ctx, void* stream, const float* img, int H, int 
   if ((r = check_cfg(ctx, cfg)) || (r = check_size(ctx, H, W))) return r;
   cudaSetDevice(ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
-  if ((r = bass_frame(ctx, st, img, H, W, *cfg, labels_out, nullptr, -1, 0))) return r;
-  if ((r = sync_scalars(ctx, st))) return r;
-  int n = ctx->sc_host->nspix;
-  if (params_out) {
-    if (params_out->capacity < n)
-      return fail(ctx, STSPIX_ERR_CAPACITY, "params capacity %d < %d superpixels",
-                  params_out->capacity, n);
-    LAUNCH(k_read_params, ctx->sp.cap, ctx->sp, &ctx->sc->nspix, *params_out);
-    CK(cudaStreamSynchronize(st));
-  }
-  ctx->log.niters = cfg->niters;
-  if (nspix_out) *nspix_out = n;
-  return ctx->sc_host->status ? fail(ctx, ctx->sc_host->status, "device status %d", ctx->sc_host->status) : STSPIX_OK;
+  std::vector<FrameDesc> fr(1);
+  FrameDesc& f = fr[0];
+  f.img = img; f.H = H; f.W = W; f.sp_size = cfg->sp_size; f.seg = labels_out; f.mode = 0;
+  if (params_out) f.pout = *params_out;
+  BatchOut o;
+  if ((r = run_batch(ctx, st, fr, *cfg, kStageSeg, o))) return r;
+  ctx->log = o.log[0];
+  if (nspix_out) *nspix_out = o.nspix[0];
+  if (params_out && params_out->capacity < o.nspix[0])
+    return fail(ctx, STSPIX_ERR_CAPACITY, "params capacity %d < %d superpixels",
+                params_out->capacity, o.nspix[0]);
+  return first_status(ctx, o);
 }
 
 int stspix_bass_partial(stspix_ctx* ctx, void* stream, const float* img, int H, int W,
@@ -801,17 +1004,24 @@ int stspix_bass_partial(stspix_ctx* ctx, void* stream, const float* img, int H, 
   if ((r = check_cfg(ctx, cfg)) || (r = check_size(ctx, H, W))) return r;
   cudaSetDevice(ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
-  if ((r = bass_frame(ctx, st, img, H, W, *cfg, labels_out, nullptr, iters < 0 ? 0 : iters,
-                      extra_update)))
+  std::vector<FrameDesc> fr(1);
+  FrameDesc& f = fr[0];
+  f.img = img; f.H = H; f.W = W; f.sp_size = cfg->sp_size; f.seg = labels_out; f.mode = 0;
+  BatchOut o;
+  if ((r = run_batch(ctx, st, fr, *cfg, kStageSeg, o, iters < 0 ? 0 : iters, extra_update)))
     return r;
-  if (dump) LAUNCH(k_dump_state, ctx->sp.cap, ctx->sp, *dump);
-  if ((r = sync_scalars(ctx, st))) return r;
-  double Hh, w;
-  int nx, ny;
-  hex_geometry(cfg->sp_size, W, H, &Hh, &w, &nx, &ny);
-  if (nbuf_out) *nbuf_out = 30 * nx * ny;
-  if (max_spix_out) *max_spix_out = ctx->sc_host->max_spix;
-  return ctx->sc_host->status;
+  if (dump) {
+    LAUNCH(k_dump_state, ctx->work[0].s.sp.cap, ctx->work[0].s.sp, *dump);
+    CK(cudaStreamSynchronize(st));
+  }
+  if (nbuf_out) {
+    double Hh, w;
+    int nx, ny;
+    hex_geometry(cfg->sp_size, W, H, &Hh, &w, &nx, &ny);
+    *nbuf_out = 30 * nx * ny;
+  }
+  if (max_spix_out) *max_spix_out = ctx->sc_host[0].max_spix;
+  return ctx->sc_host[0].status;
 }
 
 int stspix_shift_and_fill(stspix_ctx* ctx, void* stream, const int32_t* labels_prev,
@@ -823,12 +1033,16 @@ int stspix_shift_and_fill(stspix_ctx* ctx, void* stream, const int32_t* labels_p
   if ((r = check_size(ctx, H, W))) return r;
   cudaSetDevice(ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
-  LAUNCH1(k_frame_begin, ctx->sc, 0, 0);
-  if ((r = shift_fill(ctx, st, labels_prev, *params_prev, n_prev, flow, H, W, filled_out,
-                      shifted_out)))
-    return r;
-  if ((r = sync_scalars(ctx, st))) return r;
-  return ctx->sc_host->status ? fail(ctx, ctx->sc_host->status, "device status %d", ctx->sc_host->status) : STSPIX_OK;
+  std::vector<FrameDesc> fr(1);
+  FrameDesc& f = fr[0];
+  f.H = H; f.W = W; f.sp_size = 15; f.seg = filled_out; f.mode = 1; f.prev = labels_prev;
+  f.n_prev = n_prev; f.flow = flow; f.pprev = *params_prev; f.shifted = shifted_out;
+  stspix_config cfg;
+  stspix_default_config(&cfg);
+  BatchOut o;
+  if ((r = run_batch(ctx, st, fr, cfg, kStageShift, o))) return r;
+  ctx->log = o.log[0];
+  return first_status(ctx, o);
 }
 
 int stspix_run_prop(stspix_ctx* ctx, void* stream, const float* img, int H, int W,
@@ -842,24 +1056,25 @@ int stspix_run_prop(stspix_ctx* ctx, void* stream, const float* img, int H, int 
   cudaSetDevice(ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
   CK(cudaMemcpyAsync(labels_out, filled, sizeof(int) * (size_t)H * W, cudaMemcpyDeviceToDevice, st));
-  if ((r = prop_frame(ctx, st, img, H, W, *cfg, niters, labels_out, shifted, *params_prev,
-                      n_prev, nullptr)))
-    return r;
-  if ((r = sync_scalars(ctx, st))) return r;
-  int n = ctx->sc_host->nspix;
-  if (params_out) {
-    if (params_out->capacity < n)
-      return fail(ctx, STSPIX_ERR_CAPACITY, "params capacity %d < %d superpixels",
-                  params_out->capacity, n);
-    LAUNCH(k_read_params, ctx->sp.cap, ctx->sp, &ctx->sc->nspix, *params_out);
-    CK(cudaStreamSynchronize(st));
-  }
-  ctx->log.niters = niters;
-  if (nspix_out) *nspix_out = n;
-  return ctx->sc_host->status ? fail(ctx, ctx->sc_host->status, "device status %d", ctx->sc_host->status) : STSPIX_OK;
+  std::vector<FrameDesc> fr(1);
+  FrameDesc& f = fr[0];
+  f.img = img; f.H = H; f.W = W; f.sp_size = cfg->sp_size; f.seg = labels_out; f.mode = 1;
+  f.n_prev = n_prev; f.pprev = *params_prev; f.shifted = const_cast<int*>(shifted);
+  f.niters = niters < 0 ? 0 : niters;
+  if (params_out) f.pout = *params_out;
+  BatchOut o;
+  if ((r = run_batch(ctx, st, fr, *cfg, kStageSeg, o))) return r;
+  ctx->log = o.log[0];
+  if (nspix_out) *nspix_out = o.nspix[0];
+  if (params_out && params_out->capacity < o.nspix[0])
+    return fail(ctx, STSPIX_ERR_CAPACITY, "params capacity %d < %d superpixels",
+                params_out->capacity, o.nspix[0]);
+  return first_status(ctx, o);
 }
 
-// main_loop (pyapi.cu:46-195).
+// main_loop (pyapi.cu:46-195).  Video mode: frame by frame through one resident
+// stream state (each frame needs the previous one).  Image mode: the frames are
+// independent and run as batches.
 int stspix_bist_forward(stspix_ctx* ctx, void* stream, const float* vid, const float* flows,
                         int T, int H, int W, int nftrs, const stspix_config* cfg, int video_mode,
                         int rgb2lab, int32_t* spix_out) {
@@ -872,73 +1087,172 @@ int stspix_bist_forward(stspix_ctx* ctx, void* stream, const float* vid, const f
   cudaSetDevice(ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
   const size_t npix = (size_t)H * W;
-  int cur = 0;    // ping-pong index of the current frame's params
-  int n_prev = 0;
   int status = STSPIX_OK;
-  for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.first); ctx->ev_free.push_back(e.second); }
+  for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.a); ctx->ev_free.push_back(e.b); }
   ctx->frame_ev.clear();
   ctx->frame_ms.clear();
-  for (int fi = 0; fi < T; fi++) {
-    const float* img = vid + (size_t)fi * npix * 3;
-    int* seg = spix_out + (size_t)fi * npix;
-    cudaEvent_t fe0 = ev_get(ctx), fe1 = ev_get(ctx);
-    cudaEventRecord(fe0, st);
-    if (fi == 0 || !video_mode) {
-      // params are only needed by the next frame in video mode
-      if ((r = bass_frame(ctx, st, img, H, W, *cfg, seg, nullptr, -1, 0))) return r;
-      if (video_mode) {
-        if ((r = ensure_pp(ctx, st, ctx->sp_cap, cur, 0))) return r;
-        LAUNCH(k_read_params, ctx->sp.cap, ctx->sp, &ctx->sc->nspix, ctx->pp[cur]);
-        if ((r = sync_scalars(ctx, st))) return r;
-        n_prev = ctx->sc_host->nspix;
-        if (ctx->sc_host->status) status = ctx->sc_host->status;
-      }
-      ctx->log.niters = cfg->niters;
-    } else {
-      const float* flow = flows + (size_t)(fi - 1) * npix * 2;
-      const int* prev = spix_out + (size_t)(fi - 1) * npix;
-      stspix_params pprev = ctx->pp[cur];
-      LAUNCH1(k_frame_begin, ctx->sc, 0, 0);
-      if ((r = shift_fill(ctx, st, prev, pprev, n_prev, flow, H, W, seg, ctx->shifted))) return r;
-      if ((r = sync_scalars(ctx, st))) return r;
-      if (ctx->sc_host->status) status = ctx->sc_host->status;
-      int niters;
-      if (cfg->prop_niters > 0) {
-        niters = cfg->prop_niters;
-      } else {
-        float iperc = ctx->sc_host->ninvalid / (1.0 * npix);
-        niters = iperc > 0.20 ? 12 : (iperc < 0.01 ? 4 : 8);
-      }
-      int nxt = 1 - cur;
-      if ((r = ensure(ctx, (int)npix, 10 * n_prev + 2))) return r;
-      if ((r = ensure_pp(ctx, st, ctx->sp_cap, cur, n_prev))) return r;
-      pprev = ctx->pp[cur];
-      if ((r = prop_frame(ctx, st, img, H, W, *cfg, niters, seg, ctx->shifted, pprev, n_prev,
-                          &ctx->pp[nxt])))
-        return r;
-      if ((r = sync_scalars(ctx, st))) return r;
-      if (ctx->sc_host->status) status = ctx->sc_host->status;
-      n_prev = ctx->sc_host->nspix;
-      cur = nxt;
-      ctx->log.niters = niters;
+  if (video_mode) {
+    if (ctx->fwd && (ctx->fwd->H != H || ctx->fwd->W != W)) {
+      stspix_video_destroy(ctx->fwd);
+      ctx->fwd = nullptr;
     }
-    cudaEventRecord(fe1, st);
-    ctx->frame_ev.push_back({fe0, fe1});
-  }
-  if (!video_mode) {
-    if ((r = sync_scalars(ctx, st))) return r;
-    if (ctx->sc_host->status) status = ctx->sc_host->status;
+    if (!ctx->fwd && (r = stspix_video_create(ctx, &ctx->fwd, H, W))) return r;
+    stspix_video_reset(ctx->fwd);
+    for (int fi = 0; fi < T; fi++) {
+      cudaEvent_t fe0 = ev_get(ctx), fe1 = ev_get(ctx);
+      cudaEventRecord(fe0, st);
+      std::vector<FrameDesc> fr(1);
+      const float* flow = fi > 0 ? flows + (size_t)(fi - 1) * npix * 2 : nullptr;
+      if ((r = video_frame(ctx, st, ctx->fwd, vid + (size_t)fi * npix * 3, flow, cfg->sp_size,
+                           spix_out + (size_t)fi * npix, 0, fr[0])))
+        return r;
+      BatchOut o;
+      if ((r = run_batch(ctx, st, fr, *cfg, kStageShift | kStageSeg, o))) return r;
+      video_commit(ctx->fwd, fr[0].mode, o.nspix[0]);
+      if (o.status[0] && !status) status = o.status[0];
+      ctx->log = o.log[0];
+      cudaEventRecord(fe1, st);
+      ctx->frame_ev.push_back({fe0, fe1, 1});
+    }
+  } else {
+    // independent frames: batches sized to keep the workspaces near 4 GiB
+    long long vb = 0, sb = 0;
+    stspix_footprint(H, W, cfg->sp_size, &vb, &sb);
+    int per = (int)std::max(1LL, std::min<long long>(64, (4LL << 30) / std::max(sb, 1LL)));
+    for (int f0 = 0; f0 < T; f0 += per) {
+      int nb = std::min(per, T - f0);
+      cudaEvent_t fe0 = ev_get(ctx), fe1 = ev_get(ctx);
+      cudaEventRecord(fe0, st);
+      std::vector<FrameDesc> fr(nb);
+      for (int i = 0; i < nb; i++) {
+        FrameDesc& f = fr[i];
+        f.img = vid + (size_t)(f0 + i) * npix * 3;
+        f.H = H; f.W = W; f.sp_size = cfg->sp_size;
+        f.seg = spix_out + (size_t)(f0 + i) * npix;
+        f.mode = 0;
+        f.slot = i;
+      }
+      BatchOut o;
+      if ((r = run_batch(ctx, st, fr, *cfg, kStageSeg, o))) return r;
+      for (int i = 0; i < nb; i++)
+        if (o.status[i] && !status) status = o.status[i];
+      ctx->log = o.log[nb - 1];
+      cudaEventRecord(fe1, st);
+      ctx->frame_ev.push_back({fe0, fe1, nb});
+    }
   }
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
   prof_harvest(ctx);
+  // per-frame times; the frames of one image-mode batch share its time equally
   for (auto& e : ctx->frame_ev) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, e.first, e.second);
-    ctx->frame_ms.push_back(ms);
+    cudaEventElapsedTime(&ms, e.a, e.b);
+    for (int i = 0; i < e.n; i++) ctx->frame_ms.push_back(ms / e.n);
   }
   return status ? fail(ctx, status, "device status %d", status) : STSPIX_OK;
 }
+
+int stspix_video_create(stspix_ctx* ctx, stspix_video** out, int H, int W) {
+  if (!ctx || !out) return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  int r = check_size(ctx, H, W);
+  if (r) return r;
+  stspix_video* v = new (std::nothrow) stspix_video();
+  if (!v) return fail(ctx, STSPIX_ERR_NOMEM, "host allocation failed");
+  v->ctx = ctx;
+  v->H = H;
+  v->W = W;
+  cudaSetDevice(ctx->device);
+  if ((r = alloc(ctx, v->lbufs, &v->labels, (size_t)H * W))) { delete v; return r; }
+  *out = v;
+  return STSPIX_OK;
+}
+
+int stspix_video_destroy(stspix_video* v) {
+  if (!v) return STSPIX_OK;
+  cudaSetDevice(v->ctx->device);
+  cudaDeviceSynchronize();
+  free_list(v->lbufs);
+  free_list(v->pbufs);
+  delete v;
+  return STSPIX_OK;
+}
+
+int stspix_video_reset(stspix_video* v) {
+  if (!v) return STSPIX_ERR_ARG;
+  v->n = 0;
+  v->cur = 0;
+  v->frames = 0;
+  return STSPIX_OK;
+}
+
+int stspix_video_nspix(const stspix_video* v) { return v ? v->n : -1; }
+long long stspix_video_frames(const stspix_video* v) { return v ? v->frames : -1; }
+
+int stspix_process_batch(stspix_ctx* ctx, void* stream, stspix_frame* frames, int n,
+                         const stspix_config* cfg) {
+  if (!ctx || (!frames && n > 0) || n < 0) return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  int r;
+  if ((r = check_cfg(ctx, cfg))) return r;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<FrameDesc> fr(n);
+  for (int i = 0; i < n; i++) {
+    stspix_frame& F = frames[i];
+    if (!F.img || !F.labels_out) return fail(ctx, STSPIX_ERR_ARG, "frame %d: null pointer", i);
+    if (F.sp_size < 0) return fail(ctx, STSPIX_ERR_ARG, "frame %d: sp_size < 0", i);
+    const int sp = F.sp_size > 0 ? F.sp_size : cfg->sp_size;
+    if (F.video) {
+      if (F.video->ctx != ctx) return fail(ctx, STSPIX_ERR_ARG, "frame %d: video of another context", i);
+      if (F.H != F.video->H || F.W != F.video->W)
+        return fail(ctx, STSPIX_ERR_ARG, "frame %d: %dx%d frame for a %dx%d video", i, F.H, F.W,
+                    F.video->H, F.video->W);
+      for (int j = 0; j < i; j++)
+        if (frames[j].video == F.video)
+          return fail(ctx, STSPIX_ERR_ARG, "frames %d and %d continue the same video", j, i);
+      if (F.video->n > 0 && !F.flow) return fail(ctx, STSPIX_ERR_ARG, "frame %d: flow required", i);
+      if ((r = check_size(ctx, F.H, F.W))) return r;
+      if ((r = video_frame(ctx, st, F.video, F.img, F.flow, sp, F.labels_out, i, fr[i]))) return r;
+    } else {
+      if ((r = check_size(ctx, F.H, F.W))) return r;
+      FrameDesc& f = fr[i];
+      f.img = F.img; f.H = F.H; f.W = F.W; f.sp_size = sp; f.seg = F.labels_out; f.mode = 0;
+      f.slot = i;
+    }
+  }
+  cudaEventRecord(ctx->batch_ev[0], st);
+  BatchOut o;
+  if ((r = run_batch(ctx, st, fr, *cfg, kStageShift | kStageSeg, o))) return r;
+  cudaEventRecord(ctx->batch_ev[1], st);
+  CK(cudaEventSynchronize(ctx->batch_ev[1]));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->batch_ev[0], ctx->batch_ev[1]);
+  ctx->batch_ms = ms;
+  for (int i = 0; i < n; i++) {
+    if (frames[i].video) video_commit(frames[i].video, fr[i].mode, o.nspix[i]);
+    frames[i].nspix = o.nspix[i];
+    frames[i].niters = o.niters[i];
+    frames[i].status = o.status[i];
+    frames[i].log = o.log[i];
+  }
+  if (n > 0) ctx->log = o.log[n - 1];
+  return first_status(ctx, o);
+}
+
+int stspix_footprint(int H, int W, int sp_size, long long* video_bytes, long long* slot_bytes) {
+  if (H < 1 || W < 1 || sp_size < 1) return STSPIX_ERR_ARG;
+  double Hh, w;
+  int nx, ny;
+  hex_geometry(sp_size, W, H, &Hh, &w, &nx, &ny);
+  const long long npix = (long long)H * W;
+  const long long cap = std::max(30LL * nx * ny, 64LL);
+  if (video_bytes) *video_bytes = 4 * npix + 2 * kParamBytes * cap;
+  if (slot_bytes)
+    *slot_bytes = kPixBytes * npix + (2 * kSpDevBytes + kSmBytes + kAuxBytes) * (cap + 2);
+  return STSPIX_OK;
+}
+
+double stspix_last_batch_ms(const stspix_ctx* ctx) { return ctx ? ctx->batch_ms : -1.0; }
 
 int stspix_profile_enable(stspix_ctx* ctx, int enable) {
   if (!ctx) return STSPIX_ERR_ARG;

@@ -46,6 +46,10 @@ struct __align__(16) SweepRec {
 __device__ __forceinline__ int spread_id(int j) { return blockIdx.x + gridDim.x * j; }
 #define FOR_SP(k, n)                                                              \
   for (int j_ = threadIdx.x, k = spread_id(j_); k < (n); j_ += blockDim.x, k = spread_id(j_))
+// Same over a batched launch whose x dimension alone covers the ids.
+__device__ __forceinline__ int spread_id_x(int j) { return blockIdx.x + gridDim.x * j; }
+#define FOR_SPX(k, n)                                                             \
+  for (int j_ = threadIdx.x, k = spread_id_x(j_); k < (n); j_ += blockDim.x, k = spread_id_x(j_))
 
 // Per-superpixel working state, structure of arrays, `cap` entries each.
 struct SpDev {
@@ -102,6 +106,56 @@ struct Scalars {
   int tmp0, tmp1, tmp2;
   unsigned int bar_count, bar_gen;   // grid barrier
 };
+
+// One frame of a batch: its inputs, outputs, workspace and scalars.  Kernels take
+// the device array of slots and pick theirs from the launch's slot dimension, so one
+// launch processes every frame of the batch (frames of uneven size: blocks past a
+// frame's extent return).
+struct Slot {
+  // frame
+  const float* img;        // [npix*3]
+  int* seg;                // working labels (the caller's output)
+  int* seg_alt;            // ping-pong labels for the sweeps
+  int H, W, npix;
+  int cap;                 // superpixel capacity of this slot's buffers
+  int mode;                // 0 plain BASS, 1 propagated frame
+  int sp_size;             // superpixel size (hex grid, shape prior)
+  int lo;                  // compaction keeps ids < lo (0, or n_prev on propagated frames)
+  // hex geometry (BASS frames)
+  double hex_h, hex_w;
+  int hex_nx, hex_ny, nraw;
+  // propagation inputs
+  const int* prev_labels;  // previous frame's labels
+  const float* flow;       // [npix*2]
+  int n_prev;              // superpixels of the previous frame
+  stspix_params pprev;     // previous frame's params (updated in place by the shift)
+  stspix_params pout;      // this frame's params (capacity 0: not wanted)
+  int* resident_labels;    // where the finished labels are kept for the next frame
+  // pixel workspace
+  uint8_t* border;
+  int *d1, *d2, *smseg, *hits, *shifted;
+  unsigned long long* best;
+  // superpixel workspace
+  SpDev sp, tmp;
+  SmDev sm;
+  uint8_t *flags, *accept, *valid0, *living, *mint;
+  int *excl, *rid, *src_of, *cnt_pool, *cs, *cf;
+  long long* fs;
+  float *fds, *ss;
+  double* centers;
+  unsigned long long *rbest, *ccbest;
+  Scalars* sc;
+  // offsets of this slot's work items in the flattened lists of a launch
+  int tile_base;           // 32x32 relaxation tiles
+  long long pix_base;      // pixels
+  long long q_base;        // quarter-lattice sites (ceil(W/2) x ceil(H/2))
+};
+
+// kb_scalars operations.
+enum { kOpBegin = 0, kOpAfterHex = 1, kOpCompactN = 2, kOpCompactEnd = 3 };
+
+#define SLOT_Y const Slot& S = slots[blockIdx.y]
+#define SLOT_Z const Slot& S = slots[blockIdx.z]
 
 // ---------------------------------------------------------------------------
 // Device helpers shared by the kernels.

@@ -40,25 +40,61 @@ __global__ void k_init_hex(int* __restrict__ seg, int H, int W, double Hh, doubl
   seg[idx] = best;
 }
 
+__global__ void kb_init_hex(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= S.npix) return;
+  const int W = S.W, nx = S.hex_nx, ny = S.hex_ny;
+  const double Hh = S.hex_h, w = S.hex_w;
+  int x = idx % W, y = idx / W;
+  int r0 = (int)floor(y / (1.5 * Hh));
+  int c0 = (int)floor(x / w);
+  double D2 = 1.7976931348623157e308;
+  int best = 0;
+  for (int r = r0 - 2; r <= r0 + 2; r++) {
+    if (r < 0 || r >= ny) continue;
+    for (int c = c0 - 2; c <= c0 + 2; c++) {
+      if (c < 0 || c >= nx) continue;
+      double xx = double(c) * w;
+      double yy = double(r) * 1.5 * Hh;
+      if (r % 2 == 0) xx = xx + 0.5 * w;
+      double dx = (x - xx);
+      double dy = (y - yy);
+      double d2 = dx * dx + dy * dy;
+      if (d2 <= D2) { D2 = d2; best = r * nx + c; }
+    }
+  }
+  S.seg[idx] = best;
+}
+
 // ---------------------------------------------------------------------------
 // Compaction (compact_spix.cu:41-122, 196-290): flags of live ids in [lo, hi],
 // exclusive scan, remap.
-__global__ void k_mark_present(const int* __restrict__ seg, int npix, int lo,
-                               const int* __restrict__ hi_ptr, int hi_static,
-                               uint8_t* __restrict__ flags) {
+// mode 0: hex ids [0, nraw); mode 1: ids [lo, max_spix] of the finished frame.
+__global__ void kb_mark_present(const Slot* __restrict__ slots, int mode) {
+  SLOT_Y;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= npix) return;
-  int hi = hi_ptr ? *hi_ptr : hi_static;
-  int v = seg[i];
-  if (v >= lo && v <= hi) flags[v - lo] = 1;
+  if (i >= S.npix) return;
+  int lo = mode == 0 ? 0 : S.lo;
+  int hi = mode == 0 ? S.nraw - 1 : min(S.sc->max_spix, S.cap - 1);
+  int v = S.seg[i];
+  if (v >= lo && v <= hi) S.flags[v - lo] = 1;
 }
 
-// Single-block exclusive scan of n byte flags (n up to a few 10^5).
-__global__ void k_scan_flags(const uint8_t* __restrict__ flags, const int* __restrict__ n_ptr,
-                             int n_static, int* __restrict__ excl, int* __restrict__ total) {
+// One block per slot: exclusive scan of n byte flags (n up to a few 10^5).
+//   mode 0: hex-id presence (n = nraw)        -> total = live hex ids
+//   mode 1: split acceptance (n = cap)        -> total = accepted splits
+//   mode 2: relabel mint flags (n = cap)      -> total = minted ids
+//   mode 3: final presence (n = max_spix+1-lo) -> total = live new ids
+__global__ void kb_scan(const Slot* __restrict__ slots, int mode) {
+  const Slot& S = slots[blockIdx.x];
+  if (mode == 2 && !S.mode) return;  // mint flags exist on propagated slots only
   __shared__ int part[1024];
   const int T = blockDim.x;
-  int n = n_ptr ? *n_ptr : n_static;
+  const uint8_t* flags = (mode == 1) ? S.accept : (mode == 2) ? S.mint : S.flags;
+  int n = (mode == 0) ? S.nraw : (mode == 3) ? S.sc->tmp2 : S.cap;
+  int* excl = S.excl;
+  int* total = (mode == 0) ? &S.sc->nspix : (mode == 3) ? &S.sc->tmp1 : &S.sc->tmp2;
   if (n < 0) n = 0;
   int chunk = (n + T - 1) / T;
   int b = threadIdx.x * chunk, e = min(n, b + chunk);
@@ -77,19 +113,25 @@ __global__ void k_scan_flags(const uint8_t* __restrict__ flags, const int* __res
   if (threadIdx.x == T - 1) *total = part[T - 1];
 }
 
-__global__ void k_remap(int* __restrict__ seg, int npix, int lo, const int* __restrict__ excl) {
+__global__ void kb_remap(const Slot* __restrict__ slots, int mode) {
+  SLOT_Y;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= npix) return;
-  int v = seg[i];
-  if (v >= lo) seg[i] = lo + excl[v - lo];
+  if (i >= S.npix) return;
+  int lo = mode == 0 ? 0 : S.lo;
+  int v = S.seg[i];
+  if (v >= lo) S.seg[i] = lo + S.excl[v - lo];
 }
 
 // fill_new_params_from_old (compact_spix.cu:220-265): gather moved fields.
-__global__ void k_compact_gather(SpDev sp, SpDev tmp, int lo, const int* __restrict__ hi_ptr,
-                                 const uint8_t* __restrict__ flags,
-                                 const int* __restrict__ excl) {
+__global__ void kb_compact_gather(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const SpDev& tmp = S.tmp;
+  const uint8_t* flags = S.flags;
+  const int* excl = S.excl;
+  const int lo = S.lo;
   int v = lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (v > *hi_ptr || v >= sp.cap) return;
+  if (v > S.sc->max_spix || v >= sp.cap) return;
   if (!flags[v - lo]) return;
   int j = excl[v - lo];
   for (int c = 0; c < 3; c++) {
@@ -110,9 +152,13 @@ __global__ void k_compact_gather(SpDev sp, SpDev tmp, int lo, const int* __restr
 }
 
 // fill_old_params_from_new (compact_spix.cu:268-290).
-__global__ void k_compact_scatter(SpDev sp, SpDev tmp, int lo, const int* __restrict__ nnew) {
+__global__ void kb_compact_scatter(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const SpDev& tmp = S.tmp;
+  const int lo = S.lo;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= *nnew) return;
+  if (j >= S.sc->tmp1) return;
   int d = lo + j;
   if (d >= sp.cap) return;
   for (int c = 0; c < 3; c++) {
@@ -135,11 +181,15 @@ __global__ void k_compact_scatter(SpDev sp, SpDev tmp, int lo, const int* __rest
 // ---------------------------------------------------------------------------
 // init_sp_params_kernel + mark_active_contiguous (init_sparams.cu:45-166,
 // 195-286) for a BASS frame; *nspix live ids, count = npix / nspix.
-__global__ void k_init_bass_params(SpDev sp, const int* __restrict__ nspix_ptr, int npix,
-                                   int sp_size) {
+__global__ void kb_init_bass_params(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (S.mode) return;
+  const int sp_size = S.sp_size;
+  const SpDev& sp = S.sp;
+  const int npix = S.npix;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sp.cap) return;
-  int nspix = *nspix_ptr;
+  int nspix = S.sc->nspix;
   int count = (int)(npix / (1. * nspix));
   sp.prior_sigma_shape[3 * k] = 1.0 / sp_size;
   sp.prior_sigma_shape[3 * k + 1] = 0.;
@@ -160,9 +210,12 @@ __global__ void k_init_bass_params(SpDev sp, const int* __restrict__ nspix_ptr, 
 }
 
 // prior_mu_app := initial mean (calc_summ_stats, update_params.cu:142-203).
-__global__ void k_init_prior_mu(SpDev sp, const int* __restrict__ nspix_ptr) {
+__global__ void kb_init_prior_mu(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (S.mode) return;
+  const SpDev& sp = S.sp;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= *nspix_ptr || k >= sp.cap) return;
+  if (k >= S.sc->nspix || k >= sp.cap) return;
   int n = sp.count[k];
   double c = n;
   for (int ch = 0; ch < 3; ch++)
@@ -177,7 +230,7 @@ __global__ void k_init_prior_mu(SpDev sp, const int* __restrict__ nspix_ptr) {
 // position sums of a run are closed-form.
 constexpr int kRun = 8;
 
-__device__ __forceinline__ void flush_run(SpDev& sp, int k, int y, int x0, int x1,
+__device__ __forceinline__ void flush_run(const SpDev& sp, int k, int y, int x0, int x1,
                                           long long sr, long long sg, long long sb) {
   long long n = x1 - x0 + 1;
   long long sx = (long long)(x0 + x1) * n / 2;
@@ -195,8 +248,12 @@ __device__ __forceinline__ void flush_run(SpDev& sp, int k, int y, int x0, int x
   atomicAdd(acc + 7, (unsigned long long)(n * y * (long long)y));
 }
 
-__global__ void k_accumulate(const float* __restrict__ img, const int* __restrict__ seg, int H,
-                             int W, SpDev sp) {
+__global__ void kb_accumulate(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const float* __restrict__ img = S.img;
+  const int* __restrict__ seg = S.seg;
+  const int H = S.H, W = S.W;
+  const SpDev& sp = S.sp;
   const int cpr = (W + kRun - 1) / kRun;
   int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= H * cpr) return;
@@ -233,7 +290,7 @@ __device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in
   *oz = (pc * sp_size + count * in_z) / (total_count + 3.0);
 }
 
-__device__ __forceinline__ void posterior_one(SpDev& sp, int sp_size, Scalars* sc, int k) {
+__device__ __forceinline__ void posterior_one(const SpDev& sp, int sp_size, Scalars* sc, int k) {
   int count_int = sp.count[k];
   bool live = sp.valid[k] && count_int > 0;
   if (sp.valid[k] && count_int <= 0) sp.valid[k] = 0;
@@ -290,12 +347,27 @@ __device__ __forceinline__ void posterior_one(SpDev& sp, int sp_size, Scalars* s
   sp.rec[k] = r;
 }
 
-__global__ void k_posterior(SpDev sp, int sp_size, Scalars* sc) {
-  FOR_SP(k, sp.cap) posterior_one(sp, sp_size, sc, k);
+__global__ void kb_posterior(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  FOR_SP(k, S.sp.cap) posterior_one(S.sp, S.sp_size, S.sc, k);
+}
+
+// clear_fields + the helper memset (update_params.cu:54-88, :26): zero the counts
+// and the sums of every slot.
+__global__ void kb_clear_stats(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S.sp.cap) return;
+  S.sp.count[k] = 0;
+  long long* a = S.sp.acc + 8 * (size_t)k;
+#pragma unroll
+  for (int c = 0; c < 8; c++) a[c] = 0;
 }
 
 // store_sample_sigma_shape_k (update_params.cu:397-438).
-__global__ void k_store_sample(SpDev sp) {
+__global__ void kb_store_sample(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
   FOR_SP(k, sp.cap) {
   if (!sp.valid[k]) continue;
   const long long* a = sp.acc + 8 * (size_t)k;
@@ -328,6 +400,19 @@ __global__ void k_find_border(const int* __restrict__ seg, uint8_t* __restrict__
   int C = seg[idx];
   border[idx] = (C != seg[idx - W] || C != seg[idx + W] || C != seg[idx + 1] ||
                  C != seg[idx - 1]) ? 1 : 0;
+}
+
+__global__ void kb_find_border(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= S.npix) return;
+  const int W = S.W, H = S.H;
+  const int* seg = S.seg;
+  int x = idx % W, y = idx / W;
+  if (y < 1 || x < 1 || y >= H - 1 || x >= W - 1) { S.border[idx] = 1; return; }
+  int C = seg[idx];
+  S.border[idx] = (C != seg[idx - W] || C != seg[idx + W] || C != seg[idx + 1] ||
+                   C != seg[idx - 1]) ? 1 : 0;
 }
 
 __global__ void k_find_border_end(const int* __restrict__ seg, uint8_t* __restrict__ border,
@@ -426,60 +511,6 @@ __device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int 
   if (res > *best) { *best = res; *best_label = k; }
 }
 
-// One pixel of one parity class; reads labels live (other classes may already be
-// updated), border from the sweep start.
-__device__ __forceinline__ void update_pixel(const float* __restrict__ img, int* seg,
-                                             const uint8_t* __restrict__ border,
-                                             const SweepRec* __restrict__ rec, int cap, int x,
-                                             int y, int H, int W, float s2, float potts) {
-  int idx = y * W + x;
-  if (!border[idx]) return;
-  int C = seg[idx];
-  if (C < 0 || C >= cap) return;
-  int N = -1, S = -1, E = -1, Wl = -1, NE = -1, NW = -1, SE = -1, SW = -1;
-  if (x > 0) Wl = seg[idx - 1];
-  if (y > 0) N = seg[idx - W];
-  if (x < W - 1) E = seg[idx + 1];
-  if (y < H - 1) S = seg[idx + W];
-  if (y > 0 && x < W - 1) NE = seg[idx - W + 1];
-  if (y > 0 && x > 0) NW = seg[idx - W - 1];
-  if (x < W - 1 && y < H - 1) SE = seg[idx + W + 1];
-  if (x > 0 && y < H - 1) SW = seg[idx + W - 1];
-  const int nb[8] = {NW, N, NE, Wl, E, SW, S, SE};
-  int dN, dW, dS, dE;
-  bool vN = simple_point(nb, N, &dN);
-  bool vW = simple_point(nb, Wl, &dW);
-  bool vS = simple_point(nb, S, &dS);
-  bool vE = simple_point(nb, E, &dE);
-  if (!vN || !vW || !vS || !vE) return;
-  if (N >= cap || S >= cap || Wl >= cap || E >= cap) return;  // labels are < cap by construction
-  const float* pix = img + 3 * (size_t)idx;
-  float best = -9999.f;
-  int bl = C;
-  if (N >= 0) joint(pix, x, y, rec[N], N, s2, (float)dN, potts, &best, &bl);
-  if (S != N && S >= 0) joint(pix, x, y, rec[S], S, s2, (float)dS, potts, &best, &bl);
-  if (Wl != S && Wl != N && Wl >= 0) joint(pix, x, y, rec[Wl], Wl, s2, (float)dW, potts, &best, &bl);
-  if (E != Wl && E != S && E != N && E >= 0) joint(pix, x, y, rec[E], E, s2, (float)dE, potts, &best, &bl);
-  if (rec[C].count <= 2 && bl == C) {
-    if (N >= 0) bl = N;
-    else if (E >= 0) bl = E;
-    else if (S >= 0) bl = S;
-    else if (Wl >= 0) bl = Wl;
-  }
-  seg[idx] = bl;
-}
-
-__global__ void k_update_phase(const float* __restrict__ img, int* seg,
-                               const uint8_t* __restrict__ border, const SweepRec* __restrict__ rec,
-                               int cap, int H, int W, int xmod, int ymod, float s2, float potts) {
-  int hw = (W - xmod + 1) / 2;
-  int hh = (H - ymod + 1) / 2;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= hw * hh) return;
-  int x = 2 * (i % hw) + xmod, y = 2 * (i / hw) + ymod;
-  update_pixel(img, seg, border, rec, cap, x, y, H, W, s2, potts);
-}
-
 // ---------------------------------------------------------------------------
 // Fused sweep: border pass + the four parity phases of one sweep in one launch.
 // A block owns a 32x32 tile and stages labels of the tile plus a 4-pixel halo
@@ -493,11 +524,16 @@ constexpr int kSH = 4;                // label halo
 constexpr int kSL = kST + 2 * kSH;    // 40: staged label side
 constexpr int kSI = kST + 2 * (kSH - 1);  // 38: staged image / border side
 
-__global__ void __launch_bounds__(256) k_sweep_fused(const float* __restrict__ img,
-                                                     const int* __restrict__ seg_in,
-                                                     int* __restrict__ seg_out,
-                                                     const SweepRec* __restrict__ rec, int cap,
-                                                     int H, int W, float s2, float potts) {
+__global__ void __launch_bounds__(256) kb_sweep(const Slot* __restrict__ slots, int parity,
+                                                float s2, float potts) {
+  SLOT_Z;
+  const int H = S.H, W = S.W;
+  if ((int)blockIdx.x * kST >= W || (int)blockIdx.y * kST >= H) return;
+  const float* __restrict__ img = S.img;
+  const int* __restrict__ seg_in = parity ? S.seg_alt : S.seg;
+  int* __restrict__ seg_out = parity ? S.seg : S.seg_alt;
+  const SweepRec* __restrict__ rec = S.sp.rec;
+  const int cap = S.sp.cap;
   constexpr int kMaxList = (kST / 2 + kSH - 1) * (kST / 2 + kSH - 1);  // 19 x 19
   __shared__ int L[kSL * kSL];
   __shared__ float I[kSI * kSI * 3];
@@ -597,9 +633,12 @@ __global__ void __launch_bounds__(256) k_sweep_fused(const float* __restrict__ i
 // ---------------------------------------------------------------------------
 // Parameter read-out (read_params, sparams_io.cu:190-286) and prior update
 // (update_prior_kernel, sparams_io.cu:584-640) into the caller's SoA params.
-__global__ void k_read_params(SpDev sp, const int* __restrict__ n_ptr, stspix_params out) {
+__global__ void kb_read_params(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const stspix_params& out = S.pout;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int n = *n_ptr;
+  int n = S.sc->nspix;
   if (i >= n || i >= out.capacity || i >= sp.cap) return;
   bool upd = sp.count[i] > 0;
   for (int c = 0; c < 3; c++) {
@@ -622,6 +661,55 @@ __global__ void k_read_params(SpDev sp, const int* __restrict__ n_ptr, stspix_pa
   out.sm_counts[i] = sp.sm_count[i];
   out.prior_counts[i] = sp.prior_count[i];
   out.ids[i] = i;
+}
+
+// Per-slot scalar steps, one thread per slot.
+__global__ void kb_scalars(const Slot* __restrict__ slots, int B, int op) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  const Slot& S = slots[i];
+  Scalars* sc = S.sc;
+  switch (op) {
+    case kOpBegin:  // frame start: counters, buffer sizes of the reference
+      sc->status = STSPIX_OK;
+      sc->nsplits = sc->nmerges = sc->nrevived = sc->nminted = sc->near_ties = 0;
+      sc->fill_iters = 0;
+      sc->ninvalid = 0;
+      sc->tmp0 = sc->tmp1 = sc->tmp2 = 0;
+      sc->nspix = 0;
+      if (S.mode) { sc->max_spix = S.n_prev - 1; sc->nbuf_logical = 10 * S.n_prev; }
+      else { sc->max_spix = 0; sc->nbuf_logical = 30 * S.nraw; }
+      break;
+    case kOpAfterHex:  // max_spix after compacting the hex ids
+      if (!S.mode) sc->max_spix = sc->nspix - 1;
+      break;
+    case kOpCompactN:  // ids beyond cap were never created
+      sc->tmp2 = min(sc->max_spix + 1, S.cap) - S.lo;
+      break;
+    case kOpCompactEnd:
+      sc->nspix = S.lo + sc->tmp1;
+      break;
+  }
+}
+
+// flags := 0 (cap + 2 entries) before a presence scan.
+__global__ void kb_clear_flags(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < S.cap + 2) S.flags[k] = 0;
+}
+
+// Keep a copy of the finished labels where the slot's video stream resides.
+__global__ void kb_save_prev(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (S.resident_labels && i < S.npix) S.resident_labels[i] = S.seg[i];
+}
+
+__global__ void kb_copy_labels(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < S.npix) S.seg[i] = S.seg_alt[i];
 }
 
 __global__ void k_dump_state(SpDev sp, stspix_state_dump d) {

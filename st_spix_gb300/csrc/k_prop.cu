@@ -13,9 +13,33 @@ namespace stspix {
 // Mean flow per superpixel (sp_downsample_kernel / normz_downsample_kernel,
 // sp_pooling.cu:27-71), R1 fixed point.  Runs of equal labels in a row are
 // aggregated before the atomics.
-__global__ void k_flow_pool(const int* __restrict__ lab, const float* __restrict__ flow, int H,
-                            int W, int n, int* __restrict__ cnt,
-                            long long* __restrict__ fs) {
+// Clear the per-previous-superpixel sums and the warp targets of every slot.
+__global__ void kb_prop_clear(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < S.n_prev) {
+    S.cnt_pool[i] = 0;
+    S.cs[i] = 0;
+    S.cf[i] = 0;
+    S.fs[2 * i] = 0;
+    S.fs[2 * i + 1] = 0;
+    S.ccbest[i] = 0;
+  }
+  if (i < S.npix) {
+    S.hits[i] = 0;
+    S.best[i] = ~0ull;
+    S.d2[i] = 0;
+  }
+  if (i == 0) S.sc->ninvalid = 0;
+}
+
+__global__ void kb_flow_pool(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const int* __restrict__ lab = S.prev_labels;
+  const float* __restrict__ flow = S.flow;
+  const int H = S.H, W = S.W, n = S.n_prev;
+  int* __restrict__ cnt = S.cnt_pool;
+  long long* __restrict__ fs = S.fs;
   constexpr int R = 16;
   const int cpr = (W + R - 1) / R;
   int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -44,9 +68,14 @@ __global__ void k_flow_pool(const int* __restrict__ lab, const float* __restrict
 }
 
 // normz + centres = mu_shape + mean flow (shift_and_fill.cu:140-150).
-__global__ void k_flow_mean(int n, const int* __restrict__ cnt,
-                            const long long* __restrict__ fs, const double* __restrict__ mu_shape,
-                            float* __restrict__ fds, double* __restrict__ centers) {
+__global__ void kb_flow_mean(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const int n = S.n_prev;
+  const int* __restrict__ cnt = S.cnt_pool;
+  const long long* __restrict__ fs = S.fs;
+  const double* __restrict__ mu_shape = S.pprev.mu_shape;
+  float* __restrict__ fds = S.fds;
+  double* __restrict__ centers = S.centers;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   for (int c = 0; c < 2; c++) {
@@ -58,9 +87,14 @@ __global__ void k_flow_mean(int n, const int* __restrict__ cnt,
 
 // Forward warp by the rounded mean flow (shift_labels_kernel, shift_labels.cu:33-112),
 // collisions resolved by the smallest packed (size, id) (R4).
-__global__ void k_shift(const int* __restrict__ lab, int H, int W, int n,
-                        const int* __restrict__ cnt, const float* __restrict__ fds,
-                        int* __restrict__ hits, unsigned long long* __restrict__ best) {
+__global__ void kb_shift(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const int* __restrict__ lab = S.prev_labels;
+  const int H = S.H, W = S.W, n = S.n_prev;
+  const int* __restrict__ cnt = S.cnt_pool;
+  const float* __restrict__ fds = S.fds;
+  int* __restrict__ hits = S.hits;
+  unsigned long long* __restrict__ best = S.best;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= H * W) return;
   int k = lab[t];
@@ -77,12 +111,15 @@ __global__ void k_shift(const int* __restrict__ lab, int H, int W, int n,
 }
 
 // decode_kernel (shift_labels.cu:128-164) + copy to `filled` + hole count.
-__global__ void k_shift_decode(const int* __restrict__ hits,
-                               const unsigned long long* __restrict__ best, int npix,
-                               int* __restrict__ shifted, int* __restrict__ filled,
-                               Scalars* sc) {
+__global__ void kb_shift_decode(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const int* __restrict__ hits = S.hits;
+  const unsigned long long* __restrict__ best = S.best;
+  int* __restrict__ shifted = S.shifted;
+  int* __restrict__ filled = S.seg;
+  Scalars* sc = S.sc;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
+  if (t >= S.npix) return;
   int v = hits[t] > 0 ? (int)(unsigned int)best[t] : -1;
   shifted[t] = v;
   filled[t] = v;
@@ -92,62 +129,110 @@ __global__ void k_shift_decode(const int* __restrict__ hits,
 }
 
 // Per-label pixel counts (get_spix_sizes, seg_utils.cu:56-75).
-__global__ void k_count_labels(const int* __restrict__ lab, int npix, int n,
-                               int* __restrict__ cnt) {
+// which 0: counts after the shift (cs), 1: after the fill (cf).
+__global__ void kb_count_labels(const Slot* __restrict__ slots, int which) {
+  SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
-  int k = lab[t];
-  if (k >= 0 && k < n) atomicAdd(&cnt[k], 1);
+  if (t >= S.npix) return;
+  int k = S.seg[t];
+  if (k >= 0 && k < S.n_prev) atomicAdd(&(which ? S.cf : S.cs)[k], 1);
 }
 
 // ---------------------------------------------------------------------------
 // Hole filling (fill_missing.cu:35-130, update_missing_seg_nn :288-441,
 // find_border_along_missing :617-647) as one cooperative kernel: per iteration a
 // border/count pass and four parity phases, separated by bounded grid barriers.
-__global__ void __launch_bounds__(256) k_fill_coop(int* seg, const double* __restrict__ centers,
-                                                   int H, int W, uint8_t* border, Scalars* sc,
-                                                   int* iter_counts, int break_iter) {
-  const int npix = H * W;
-  const int nthr = gridDim.x * blockDim.x;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  __shared__ int red[8];
-  int prev_neg = 1410065408;  // (int)10000000000 as the reference truncates it
-  for (int iter = 0;; iter++) {
-    if (break_iter > 0 && iter >= break_iter) break;
-    int local = 0;
-    for (int idx = gt; idx < npix; idx += nthr) {
-      int x = idx % W, y = idx / W;
-      int N = -1, S = -1, E = -1, Wl = -1;
-      if (y > 0) N = __ldcg(seg + idx - W);
-      if (x > 0) Wl = __ldcg(seg + idx - 1);
-      if (y < H - 1) S = __ldcg(seg + idx + W);
-      if (x < W - 1) E = __ldcg(seg + idx + 1);
-      border[idx] = (N >= 0 || Wl >= 0 || S >= 0 || E >= 0) ? 1 : 0;
-      if (__ldcg(seg + idx) < 0) local++;
+// Work items of the hole fill: pixels (pass 1) and quarter-lattice sites (the four
+// parity phases) of all slots of the launch, flattened in slot order
+// (slots[i].pix_base / slots[i].q_base are the prefix sums).
+__device__ __forceinline__ int advance_slot(const Slot* __restrict__ slots, int B, int s,
+                                            long long g, bool quarter) {
+  while (s + 1 < B && (quarter ? slots[s + 1].q_base : slots[s + 1].pix_base) <= g) s++;
+  return s;
+}
+
+// Hole filling (fill_missing.cu:35-130, update_missing_seg_nn :288-441,
+// find_border_along_missing :617-647) of every slot as one cooperative kernel: per
+// iteration a border/count pass and four parity phases, separated by bounded grid
+// barriers.  counts[it * B + i] is slot i's hole count at iteration it (row it + 1 is
+// cleared by block 0 during iteration it; the caller clears row 0).  done[i] = it + 1
+// records that slot i finished after iteration it (no holes, or no progress); the
+// slot still runs the phases of that iteration, as the reference does.
+__global__ void __launch_bounds__(256) kb_fill(const Slot* __restrict__ slots, int B,
+                                               long long total_pix, long long total_q,
+                                               Scalars* ctl, int* counts, int* done,
+                                               int break_iter) {
+  const long long nthr = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  for (int iter = 0; iter < break_iter; iter++) {
+    if (blockIdx.x == 0 && iter + 1 < break_iter)
+      for (int i = threadIdx.x; i < B; i += blockDim.x) counts[(iter + 1) * B + i] = 0;
+    // pass 1: border of the holes and hole counts (warp-uniform loop)
+    int si = 0;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < total_pix; base += nthr) {
+      const long long g = base + threadIdx.x;
+      int key = -1;
+      if (g < total_pix) {
+        si = advance_slot(slots, B, si, g, false);
+        const int dn = __ldcg(&done[si]);
+        if (dn == 0 || dn > iter) {
+          const Slot& S = slots[si];
+          const int W = S.W, H = S.H;
+          const int idx = (int)(g - S.pix_base);
+          const int* seg = S.seg;
+          int x = idx % W, y = idx / W;
+          int N = -1, So = -1, E = -1, Wl = -1;
+          if (y > 0) N = __ldcg(seg + idx - W);
+          if (x > 0) Wl = __ldcg(seg + idx - 1);
+          if (y < H - 1) So = __ldcg(seg + idx + W);
+          if (x < W - 1) E = __ldcg(seg + idx + 1);
+          S.border[idx] = (N >= 0 || Wl >= 0 || So >= 0 || E >= 0) ? 1 : 0;
+          if (__ldcg(seg + idx) < 0) key = si;
+        }
+      }
+      const unsigned m = __match_any_sync(0xffffffffu, key);
+      if (key >= 0 && lane == __ffs(m) - 1) atomicAdd(&counts[iter * B + key], __popc(m));
     }
-    // block reduction of the hole count
-    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int s = 0;
-      for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += red[i];
-      if (s) atomicAdd(&iter_counts[iter], s);
-    }
-    if (!grid_barrier(sc)) return;
-    const int num_neg = *(volatile int*)&iter_counts[iter];
+    if (!grid_barrier(ctl)) return;
+    // per-slot bookkeeping by block 0 (read by all after the phase barriers)
+    if (blockIdx.x == 0)
+      for (int i = threadIdx.x; i < B; i += blockDim.x) {
+        const int dn = __ldcg(&done[i]);
+        if (dn != 0 && dn <= iter) continue;
+        const int num_neg = __ldcg(&counts[iter * B + i]);
+        const int prev_neg = iter > 0 ? __ldcg(&counts[(iter - 1) * B + i])
+                                      : 1410065408;  // (int)10000000000 as the reference truncates it
+        Scalars* sc = slots[i].sc;
+        sc->fill_iters += 1;
+        if (num_neg == prev_neg) {
+          atomicExch(&sc->status, STSPIX_ERR_NOPROGRESS);
+          done[i] = iter + 1;
+        } else if (num_neg <= 0) {
+          done[i] = iter + 1;
+        }
+      }
     for (int ph = 0; ph < 4; ph++) {
       const int xm = ph >> 1, ym = ph & 1;
-      const int hw = (W - xm + 1) / 2, hh = (H - ym + 1) / 2;
-      for (int i = gt; i < hw * hh; i += nthr) {
-        int x = 2 * (i % hw) + xm, y = 2 * (i / hw) + ym;
-        int idx = y * W + x;
-        if (!__ldcg(border + idx) || __ldcg(seg + idx) != -1) continue;
-        int N = -1, S = -1, E = -1, Wl = -1;
+      int qi = 0;
+      for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total_q; g += nthr) {
+        qi = advance_slot(slots, B, qi, g, true);
+        const int dn = __ldcg(&done[qi]);
+        if (dn != 0 && dn <= iter) continue;
+        const Slot& S = slots[qi];
+        const int W = S.W, H = S.H;
+        const int hw0 = (W + 1) >> 1;
+        const int i = (int)(g - S.q_base);
+        const int x = 2 * (i % hw0) + xm, y = 2 * (i / hw0) + ym;
+        if (x >= W || y >= H) continue;
+        int* seg = S.seg;
+        const int idx = y * W + x;
+        if (!__ldcg(S.border + idx) || __ldcg(seg + idx) != -1) continue;
+        int N = -1, So = -1, E = -1, Wl = -1;
         if (x > 0) Wl = __ldcg(seg + idx - 1);
         if (y > 0) N = __ldcg(seg + idx - W);
         if (x < W - 1) E = __ldcg(seg + idx + 1);
-        if (y < H - 1) S = __ldcg(seg + idx + W);
+        if (y < H - 1) So = __ldcg(seg + idx + W);
+        const double* centers = S.centers;
         float bx = -999999;
         int bl = -1;
         auto consider = [&](int lab) {
@@ -158,44 +243,50 @@ __global__ void __launch_bounds__(256) k_fill_coop(int* seg, const double* __res
           if (sim > bx) { bx = sim; bl = lab; }
         };
         if (N >= 0) consider(N);
-        if (S >= 0 && S != N) consider(S);
-        if (Wl >= 0 && Wl != S && Wl != N) consider(Wl);
-        if (E >= 0 && E != Wl && E != S && E != N) consider(E);
+        if (So >= 0 && So != N) consider(So);
+        if (Wl >= 0 && Wl != So && Wl != N) consider(Wl);
+        if (E >= 0 && E != Wl && E != So && E != N) consider(E);
         __stcg(seg + idx, bl);
       }
-      if (!grid_barrier(sc)) return;
+      if (!grid_barrier(ctl)) return;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&sc->fill_iters, 1);
-    if (num_neg == prev_neg) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&sc->status, STSPIX_ERR_NOPROGRESS);
-      return;
+    // every block sees the same done[] here: stop when all slots finished
+    int all = 1;
+    for (int i = threadIdx.x; i < B; i += blockDim.x) {
+      const int dn = *(volatile int*)&done[i];
+      if (dn == 0 || dn > iter + 1) all = 0;
     }
-    prev_neg = num_neg;
-    if (num_neg <= 0) return;
+    if (__syncthreads_and(all)) return;
   }
 }
 
 // ---------------------------------------------------------------------------
 // Disconnected regions (split_disconnected.cu:33-96): roots from the cooperative
 // relaxation (mode 1), sizes, largest region per label (R6), invalidate the rest.
-__global__ void k_cc_init(const int* __restrict__ seg, int npix, int* __restrict__ root) {
+__global__ void kb_cc_init(const Slot* __restrict__ slots) {
+  SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
-  root[t] = seg[t] >= 0 ? t : -1;
+  if (t >= S.npix) return;
+  S.d1[t] = S.seg[t] >= 0 ? t : -1;
 }
 
-__global__ void k_cc_size(const int* __restrict__ root, int npix, int* __restrict__ size) {
+__global__ void kb_cc_size(const Slot* __restrict__ slots) {
+  SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
-  int r = root[t];
-  if (r >= 0) atomicAdd(&size[r], 1);
+  if (t >= S.npix) return;
+  int r = S.d1[t];
+  if (r >= 0) atomicAdd(&S.d2[r], 1);
 }
 
-__global__ void k_cc_best(const int* __restrict__ seg, const int* __restrict__ root,
-                          const int* __restrict__ size, int npix, int nlab,
-                          unsigned long long* __restrict__ best) {
+__global__ void kb_cc_best(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const int* __restrict__ seg = S.seg;
+  const int* __restrict__ root = S.d1;
+  const int* __restrict__ size = S.d2;
+  const int nlab = S.n_prev;
+  unsigned long long* __restrict__ best = S.ccbest;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix || root[t] != t) return;
+  if (t >= S.npix || root[t] != t) return;
   int L = seg[t];
   if (L < 0 || L >= nlab) return;
   unsigned long long key = ((unsigned long long)(unsigned int)size[t] << 32) |
@@ -203,10 +294,14 @@ __global__ void k_cc_best(const int* __restrict__ seg, const int* __restrict__ r
   atomicMax(&best[L], key);
 }
 
-__global__ void k_cc_invalidate(int* __restrict__ seg, const int* __restrict__ root, int npix,
-                                int nlab, const unsigned long long* __restrict__ best) {
+__global__ void kb_cc_invalidate(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int* __restrict__ seg = S.seg;
+  const int* __restrict__ root = S.d1;
+  const int nlab = S.n_prev;
+  const unsigned long long* __restrict__ best = S.ccbest;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
+  if (t >= S.npix) return;
   int L = seg[t];
   if (L < 0 || L >= nlab) return;
   unsigned int win = 0xffffffffu - (unsigned int)(best[L] & 0xffffffffull);
@@ -214,9 +309,13 @@ __global__ void k_cc_invalidate(int* __restrict__ seg, const int* __restrict__ r
 }
 
 // invalid_counts / prior_counts update (shift_and_fill.cu:300-330).
-__global__ void k_shift_params(int n, const int* __restrict__ cnt_pool,
-                               const int* __restrict__ cs, const int* __restrict__ cf,
-                               stspix_params pp) {
+__global__ void kb_shift_params(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const int n = S.n_prev;
+  const int* __restrict__ cnt_pool = S.cnt_pool;
+  const int* __restrict__ cs = S.cs;
+  const int* __restrict__ cf = S.cf;
+  const stspix_params& pp = S.pprev;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n || k >= pp.capacity) return;
   int f = cf[k], s = cs[k];
@@ -228,7 +327,11 @@ __global__ void k_shift_params(int n, const int* __restrict__ cnt_pool,
 // ---------------------------------------------------------------------------
 // run_prop set-up: write_params (sparams_io.cu:353-501, prior_icov = invert_cov
 // :505-520) then mark_active (init_sparams.cu:195-286).
-__global__ void k_write_params(SpDev sp, const stspix_params pp, int n, int sp_size) {
+__global__ void kb_write_params(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const stspix_params& pp = S.pprev;
+  const int n = S.n_prev, sp_size = S.sp_size;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= sp.cap) return;
   if (i < n) {
@@ -271,42 +374,53 @@ __global__ void k_write_params(SpDev sp, const stspix_params pp, int n, int sp_s
   sp.prop[i] = 0;
 }
 
-__global__ void k_mark_active(const int* __restrict__ lab, int npix, SpDev sp) {
+__global__ void kb_mark_active(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
-  int v = lab[t];
+  if (t >= S.npix) return;
+  int v = S.seg[t];
   if (v >= 0 && v < sp.cap) { sp.valid[v] = 1; sp.prop[v] = 1; }
 }
 
-__global__ void k_prop_begin(Scalars* sc, int n) {
-  sc->max_spix = n - 1;
-  sc->nbuf_logical = 10 * n;
-}
+
 
 // ---------------------------------------------------------------------------
 // Relabel (relabel.cu:126-409), R5.
-__global__ void k_living(const int* __restrict__ seg, int npix, const Scalars* __restrict__ sc,
-                         uint8_t* __restrict__ living) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
-  int v = seg[t];
-  if (v >= 0 && v <= sc->max_spix) living[v] = 1;
+// Relabel runs on propagated slots only (mode 1); plain BASS slots return at once.
+__global__ void kb_relabel_init(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.mode) return;
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S.cap + 2) return;
+  S.living[s] = 0;
+  S.src_of[s] = -1;
+  if (s >= S.cap) return;
+  S.rbest[s] = ((unsigned long long)__float_as_uint(10000.f) << 32) | 0x7fffffffull;
+  S.ss[s] = 0.f;
 }
 
-__global__ void k_relabel_init(int cap, unsigned long long* __restrict__ best,
-                               float* __restrict__ ss) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= cap) return;
-  best[s] = ((unsigned long long)__float_as_uint(10000.f) << 32) | 0x7fffffffull;
-  ss[s] = 0.f;
+__global__ void kb_living(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.mode) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.npix) return;
+  int v = S.seg[t];
+  if (v >= 0 && v <= S.sc->max_spix) S.living[v] = 1;
 }
 
 // find_most_similar_spix (relabel.cu:201-276): grid (s, candidate chunk).
-__global__ void k_relabel_compare(const SpDev sp, const float* __restrict__ prev_prior_mu_app,
-                                  int n_prev, const Scalars* __restrict__ sc,
-                                  const uint8_t* __restrict__ living,
-                                  unsigned long long* __restrict__ best, float* __restrict__ ss,
-                                  int chunk) {
+__global__ void kb_relabel_compare(const Slot* __restrict__ slots, int chunk) {
+  SLOT_Z;
+  if (!S.mode) return;
+  const SpDev& sp = S.sp;
+  const float* __restrict__ prev_prior_mu_app = S.pprev.prior_mu_app;
+  const int n_prev = S.n_prev;
+  const Scalars* __restrict__ sc = S.sc;
+  const uint8_t* __restrict__ living = S.living;
+  unsigned long long* __restrict__ best = S.rbest;
+  float* __restrict__ ss = S.ss;
+  if ((int)blockIdx.y * chunk >= n_prev) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   const int nspix = sc->max_spix + 1;
   if (s >= nspix || s >= sp.cap || !living[s]) return;
@@ -330,12 +444,17 @@ __global__ void k_relabel_compare(const SpDev sp, const float* __restrict__ prev
 }
 
 // mark_for_relabel (relabel.cu:126-192): revive flags and mint flags.
-__global__ void k_relabel_mark(int cap, const Scalars* __restrict__ sc,
-                               const uint8_t* __restrict__ living,
-                               const unsigned long long* __restrict__ best,
-                               const float* __restrict__ ss, float thresh_replace,
-                               float thresh_new, int* __restrict__ rid,
-                               uint8_t* __restrict__ mint) {
+__global__ void kb_relabel_mark(const Slot* __restrict__ slots, float thresh_replace,
+                                float thresh_new) {
+  SLOT_Y;
+  if (!S.mode) return;
+  const int cap = S.cap;
+  const Scalars* __restrict__ sc = S.sc;
+  const uint8_t* __restrict__ living = S.living;
+  const unsigned long long* __restrict__ best = S.rbest;
+  const float* __restrict__ ss = S.ss;
+  int* __restrict__ rid = S.rid;
+  uint8_t* __restrict__ mint = S.mint;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= cap) return;
   mint[s] = 0;
@@ -350,9 +469,15 @@ __global__ void k_relabel_mark(int cap, const Scalars* __restrict__ sc,
   else if (ss[s] > thresh_new) mint[s] = 1;
 }
 
-__global__ void k_relabel_ids(int cap, Scalars* sc, const uint8_t* __restrict__ mint,
-                              const int* __restrict__ excl, int* __restrict__ rid,
-                              int* __restrict__ src_of) {
+__global__ void kb_relabel_ids(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.mode) return;
+  const int cap = S.cap;
+  Scalars* sc = S.sc;
+  const uint8_t* __restrict__ mint = S.mint;
+  const int* __restrict__ excl = S.excl;
+  int* __restrict__ rid = S.rid;
+  int* __restrict__ src_of = S.src_of;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= cap) return;
   if (mint[s]) rid[s] = sc->max_spix + 1 + excl[s];
@@ -363,9 +488,13 @@ __global__ void k_relabel_ids(int cap, Scalars* sc, const uint8_t* __restrict__ 
 
 // relabel_spix_kernel parameter copies (relabel.cu:86-120), from the largest
 // reviving superpixel.
-__global__ void k_relabel_params(SpDev sp, const int* __restrict__ rid,
-                                 const int* __restrict__ src_of,
-                                 int n_prev) {
+__global__ void kb_relabel_params(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.mode) return;
+  const SpDev& sp = S.sp;
+  const int* __restrict__ rid = S.rid;
+  const int* __restrict__ src_of = S.src_of;
+  const int n_prev = S.n_prev;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= sp.cap) return;
   int n = rid[s];
@@ -387,29 +516,36 @@ __global__ void k_relabel_params(SpDev sp, const int* __restrict__ rid,
   }
 }
 
-__global__ void k_relabel_apply(int* __restrict__ seg, int npix, int cap,
-                                const int* __restrict__ rid) {
+__global__ void kb_relabel_apply(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.mode) return;
+  int* __restrict__ seg = S.seg;
+  const int cap = S.cap;
+  const int* __restrict__ rid = S.rid;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
+  if (t >= S.npix) return;
   int v = seg[t];
   if (v < 0 || v >= cap) return;
   int n = rid[v];
   if (n >= 0 && n < cap) seg[t] = n;
 }
 
-__global__ void k_relabel_end(Scalars* sc, const int* __restrict__ nminted,
-                              const int* __restrict__ rid, int cap) {
-  // single thread: bump max_spix, count revived ids for the log
-  int m = *nminted;
+__global__ void kb_relabel_end(const Slot* __restrict__ slots, int B) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B || !slots[i].mode) return;
+  Scalars* sc = slots[i].sc;
+  // bump max_spix by the minted ids
+  int m = sc->tmp2;
   sc->nminted += m;
   sc->max_spix += m;
 }
 
-__global__ void k_count_revived(const int* __restrict__ rid, const uint8_t* __restrict__ mint,
-                                int cap, Scalars* sc) {
+__global__ void kb_count_revived(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.mode) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= cap) return;
-  if (rid[s] >= 0 && !mint[s]) atomicAdd(&sc->nrevived, 1);
+  if (s >= S.cap) return;
+  if (S.rid[s] >= 0 && !S.mint[s]) atomicAdd(&S.sc->nrevived, 1);
 }
 
 }  // namespace stspix

@@ -16,11 +16,16 @@ constexpr int kInf = 0x3fffffff;
 
 // ---------------------------------------------------------------------------
 // Split seeds (init_split, split_merge.cu:803-844) for both directions.
-__global__ void k_split_seed(SpDev sp, const int* __restrict__ seg, int H, int W, int direction,
-                             const Scalars* __restrict__ sc, int* __restrict__ d1,
-                             int* __restrict__ d2) {
+__global__ void kb_split_seed(const Slot* __restrict__ slots, int dir_bass, int dir_prop) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const int* __restrict__ seg = S.seg;
+  const int H = S.H, W = S.W;
+  const int direction = S.mode ? dir_prop : dir_bass;
+  int* __restrict__ d1 = S.d1;
+  int* __restrict__ d2 = S.d2;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= sp.cap || !sc->tmp0 /*split_on*/ || !sp.valid[k]) return;
+  if (k >= sp.cap || !S.sc->tmp0 /*split_on*/ || !sp.valid[k]) return;
   for (int s = 0; s < 2; s++) {
     int dir = s == 0 ? direction : -direction;
     int x, y;
@@ -38,7 +43,19 @@ __global__ void k_split_seed(SpDev sp, const int* __restrict__ seg, int H, int W
   }
 }
 
-__global__ void k_split_begin(Scalars* sc) {
+// d1 = d2 = -1 (unreached) before the split seeds.
+__global__ void kb_split_clear(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.npix) return;
+  S.d1[t] = -1;
+  S.d2[t] = -1;
+}
+
+__global__ void kb_split_begin(const Slot* __restrict__ slots, int B) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  Scalars* sc = slots[i].sc;
   // split runs unless max_spix > nspix_buffer / 2 (split_merge_orig.cu:215)
   sc->tmp0 = sc->max_spix > sc->nbuf_logical / 2 ? 0 : 1;
   sc->tmp1 = sc->max_spix + 1;  // offset of the second half
@@ -52,20 +69,51 @@ __global__ void k_split_begin(Scalars* sc) {
 //         (calc_split_candidate, split_merge.cu:758-800).
 // mode 1: connected-component roots (8-connected, same label, min pixel index) --
 //         the fixed point of find_spix_min (split_disconnected.cu:458-498).
+// Slot of flattened work item t (slots[i].base ascending, slots[0].base == 0).
+__device__ __forceinline__ int slot_of(const Slot* __restrict__ slots, int B, long long t) {
+  int lo = 0, hi = B - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (slots[mid].tile_base <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// The tiles of every slot of the launch form one list (slot i owns tiles
+// [tile_base_i, tile_base_i + tiles_i)); flags[r * (B + 1) + i] records that slot i
+// changed in round r, flags[r * (B + 1) + B] that any slot did.  A slot that did not
+// change in round r is at its fixed point (its tiles read final halos) and is
+// skipped from round r + 1 on.  Row r + 1 is cleared by block 0 during round r; the
+// caller clears row 0.
 template <int MODE>
-__device__ __forceinline__ void relax_coop(const int* __restrict__ seg, int* f1, int* f2, int H,
-                                           int W, Scalars* sc, int* round_flags,
+__device__ __forceinline__ void relax_coop(const Slot* __restrict__ slots, int B,
+                                           int total_tiles, Scalars* ctl, int* flags,
                                            int max_rounds) {
   __shared__ int sl[kHalo * kHalo];
   __shared__ int s1[kHalo * kHalo];
   __shared__ int s2[MODE == 0 ? kHalo * kHalo : 1];
   __shared__ int any;
-  const int tiles_x = (W + kTile - 1) / kTile, tiles_y = (H + kTile - 1) / kTile;
-  const int ntiles = tiles_x * tiles_y;
+  const int row = B + 1;
   for (int round = 0; round < max_rounds; round++) {
-    int my_changed = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-      const int tx0 = (t % tiles_x) * kTile, ty0 = (t / tiles_x) * kTile;
+    if (blockIdx.x == 0 && round + 1 < max_rounds)
+      for (int i = threadIdx.x; i < row; i += blockDim.x) flags[(round + 1) * row + i] = 0;
+    int cur_slot = -1, my_changed = 0;
+    for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+      const int si = slot_of(slots, B, t);
+      if (si != cur_slot) {
+        if (my_changed) { atomicOr(&flags[round * row + cur_slot], 1); atomicOr(&flags[round * row + B], 1); }
+        cur_slot = si;
+        my_changed = 0;
+      }
+      if (round > 0 && *(volatile int*)&flags[(round - 1) * row + si] == 0) continue;
+      const Slot& S = slots[si];
+      const int H = S.H, W = S.W;
+      const int* __restrict__ seg = S.seg;
+      int* f1 = S.d1;
+      int* f2 = S.d2;
+      const int tiles_x = (W + kTile - 1) / kTile;
+      const int tl = t - S.tile_base;
+      const int tx0 = (tl % tiles_x) * kTile, ty0 = (tl / tiles_x) * kTile;
       for (int i = threadIdx.x; i < kHalo * kHalo; i += blockDim.x) {
         int gx = tx0 + i % kHalo - 1, gy = ty0 + i / kHalo - 1;
         if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
@@ -145,40 +193,61 @@ __device__ __forceinline__ void relax_coop(const int* __restrict__ seg, int* f1,
       }
       __syncthreads();
     }
-    if (my_changed) atomicOr(&round_flags[round], 1);
-    if (!grid_barrier(sc)) return;
-    if (*(volatile int*)&round_flags[round] == 0) return;
+    if (my_changed) { atomicOr(&flags[round * row + cur_slot], 1); atomicOr(&flags[round * row + B], 1); }
+    if (!grid_barrier(ctl)) return;
+    if (*(volatile int*)&flags[round * row + B] == 0) return;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&sc->status, STSPIX_ERR_ITER_LIMIT);
+  // round cap reached: flag the slots still changing
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < B; i += blockDim.x)
+      if (flags[(max_rounds - 1) * row + i]) atomicExch(&slots[i].sc->status, STSPIX_ERR_ITER_LIMIT);
 }
 
-__global__ void __launch_bounds__(256) k_relax_bfs(const int* __restrict__ seg, int* f1, int* f2,
-                                                   int H, int W, Scalars* sc, int* round_flags,
-                                                   int max_rounds) {
-  relax_coop<0>(seg, f1, f2, H, W, sc, round_flags, max_rounds);
+__global__ void __launch_bounds__(256) kb_relax_bfs(const Slot* __restrict__ slots, int B,
+                                                    int total_tiles, Scalars* ctl, int* flags,
+                                                    int max_rounds) {
+  relax_coop<0>(slots, B, total_tiles, ctl, flags, max_rounds);
 }
-__global__ void __launch_bounds__(256) k_relax_cc(const int* __restrict__ seg, int* f1, int* f2,
-                                                  int H, int W, Scalars* sc, int* round_flags,
-                                                  int max_rounds) {
-  relax_coop<1>(seg, f1, f2, H, W, sc, round_flags, max_rounds);
+__global__ void __launch_bounds__(256) kb_relax_cc(const Slot* __restrict__ slots, int B,
+                                                   int total_tiles, Scalars* ctl, int* flags,
+                                                   int max_rounds) {
+  relax_coop<1>(slots, B, total_tiles, ctl, flags, max_rounds);
 }
 
 // calc_seg_split (split_merge.cu:847-859): second half when d1 > d2.
-__global__ void k_split_partition(const int* __restrict__ seg, const int* __restrict__ d1,
-                                  const int* __restrict__ d2, int npix,
-                                  const Scalars* __restrict__ sc, int* __restrict__ sm) {
+__global__ void kb_split_partition(const Slot* __restrict__ slots) {
+  SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
-  int v = seg[t];
-  if (d1[t] > d2[t]) v += sc->tmp1;
-  sm[t] = v;
+  if (t >= S.npix) return;
+  int v = S.seg[t];
+  if (S.d1[t] > S.d2[t]) v += S.sc->tmp1;
+  S.smseg[t] = v;
+}
+
+// Clear the split/merge sums (cap + 2 entries).
+__global__ void kb_sm_clear(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SmDev& sm = S.sm;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S.cap + 2) return;
+  sm.count[k] = 0;
+  sm.ninvalid[k] = 0;
+#pragma unroll
+  for (int c = 0; c < 3; c++) { sm.s[3 * (size_t)k + c] = 0; sm.sq[3 * (size_t)k + c] = 0; }
 }
 
 // sum_by_label over split/merge labels (split_merge.cu:862-891,
 // split_merge_prop.cu:1942-2018): count, colour sums, square sums, invalid count.
-__global__ void k_sm_accumulate(const float* __restrict__ img, const int* __restrict__ lab,
-                                const int* __restrict__ shifted, int H, int W, int cap,
-                                SmDev sm) {
+// split: labels = split labels, invalid counts against the shifted labels (prop
+// slots); merge: labels = current labels, ids < cap.
+__global__ void kb_sm_accumulate(const Slot* __restrict__ slots, int split) {
+  SLOT_Y;
+  const float* __restrict__ img = S.img;
+  const int* __restrict__ lab = split ? S.smseg : S.seg;
+  const int* __restrict__ shifted = (split && S.mode) ? S.shifted : nullptr;
+  const int H = S.H, W = S.W;
+  const int cap = split ? S.cap + 2 : S.cap;
+  const SmDev& sm = S.sm;
   constexpr int R = 16;
   const int cpr = (W + R - 1) / R;
   int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -239,7 +308,7 @@ __device__ __forceinline__ bool near_tie(double h) { return fabs(h + 2.0) < 1e-6
 
 // update_split_flag (split_merge_orig.cu:900-986) / update_split_flag_p
 // (split_merge_prop.cu:3026-3149): decision only; ids by scan afterwards (R2).
-__device__ __forceinline__ void split_decide_one(SpDev& sp, SmDev& sm, Scalars* sc,
+__device__ __forceinline__ void split_decide_one(const SpDev& sp, const SmDev& sm, Scalars* sc,
                                                  const SmConsts& K, float split_alpha,
                                                  int prop_mode, uint8_t* __restrict__ accept,
                                                  int k) {
@@ -274,14 +343,20 @@ __device__ __forceinline__ void split_decide_one(SpDev& sp, SmDev& sm, Scalars* 
   if (h > -2) accept[k] = fl;
 }
 
-__global__ void k_split_decide(SpDev sp, SmDev sm, Scalars* sc, SmConsts K, float split_alpha,
-                               int prop_mode, uint8_t* __restrict__ accept) {
-  FOR_SP(k, sp.cap) split_decide_one(sp, sm, sc, K, split_alpha, prop_mode, accept, k);
+__global__ void kb_split_decide(const Slot* __restrict__ slots, SmConsts K, float split_alpha) {
+  SLOT_Y;
+  FOR_SP(k, S.sp.cap) split_decide_one(S.sp, S.sm, S.sc, K, split_alpha, S.mode, S.accept, k);
 }
 
 // Split commit: new id = max_spix + 1 + rank (R2), prior counts.
-__global__ void k_split_commit(SpDev sp, SmDev sm, Scalars* sc, const uint8_t* __restrict__ accept,
-                               const int* __restrict__ excl, int prop_mode) {
+__global__ void kb_split_commit(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const SmDev& sm = S.sm;
+  Scalars* sc = S.sc;
+  const uint8_t* __restrict__ accept = S.accept;
+  const int* __restrict__ excl = S.excl;
+  const int prop_mode = S.mode;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sp.cap) return;
   uint8_t fl = accept[k];
@@ -314,11 +389,17 @@ __global__ void k_split_commit(SpDev sp, SmDev sm, Scalars* sc, const uint8_t* _
 }
 
 // split_sp (split_merge.cu:1002-1031) / split_sp_p (split_merge_prop.cu:2317-2350).
-__global__ void k_split_apply(int* __restrict__ seg, const int* __restrict__ smseg, int npix,
-                              SpDev sp, SmDev sm, const Scalars* __restrict__ sc,
-                              const uint8_t* __restrict__ accept, int prop_mode) {
+__global__ void kb_split_apply(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int* __restrict__ seg = S.seg;
+  const int* __restrict__ smseg = S.smseg;
+  const SpDev& sp = S.sp;
+  const SmDev& sm = S.sm;
+  const Scalars* __restrict__ sc = S.sc;
+  const uint8_t* __restrict__ accept = S.accept;
+  const int prop_mode = S.mode;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
+  if (t >= S.npix) return;
   int k = seg[t];
   if (k < 0 || k >= sp.cap) return;
   uint8_t fl = accept[k];
@@ -333,8 +414,11 @@ __global__ void k_split_apply(int* __restrict__ seg, const int* __restrict__ sms
   }
 }
 
-__global__ void k_split_end(Scalars* sc, const int* __restrict__ nsplits) {
-  int n = *nsplits;
+__global__ void kb_split_end(const Slot* __restrict__ slots, int B) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  Scalars* sc = slots[i].sc;
+  int n = sc->tmp2;
   sc->nsplits += n;
   sc->max_spix += n;
 }
@@ -342,10 +426,16 @@ __global__ void k_split_end(Scalars* sc, const int* __restrict__ nsplits) {
 // ---------------------------------------------------------------------------
 // Merge candidates (calc_merge_candidate, split_merge.cu:719-755;
 // calc_merge_candidate_p, split_merge_prop.cu:1808-1845).
-__global__ void k_merge_candidates(const int* __restrict__ seg, const uint8_t* __restrict__ border,
-                                   int H, int W, int direction, int prop_mode,
-                                   const uint8_t* __restrict__ prop, int cap,
-                                   int* __restrict__ pair) {
+__global__ void kb_merge_candidates(const Slot* __restrict__ slots, int dir_bass, int dir_prop) {
+  SLOT_Y;
+  const int* __restrict__ seg = S.seg;
+  const uint8_t* __restrict__ border = S.border;
+  const int H = S.H, W = S.W;
+  const int prop_mode = S.mode;
+  const int direction = prop_mode ? dir_prop : dir_bass;
+  const uint8_t* __restrict__ prop = S.sp.prop;
+  const int cap = S.cap;
+  int* __restrict__ pair = S.sm.pair;
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= H * W || !border[idx]) return;
   int x = idx % W, y = idx / W;
@@ -369,7 +459,10 @@ __global__ void k_merge_candidates(const int* __restrict__ seg, const uint8_t* _
 
 // Single-superpixel marginal, present only when k has its own candidate
 // (calc_merge_stats_step0 computes b_n only then; split_merge_orig.cu:456-520).
-__global__ void k_merge_single(SpDev sp, SmDev sm, SmConsts K) {
+__global__ void kb_merge_single(const Slot* __restrict__ slots, SmConsts K) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const SmDev& sm = S.sm;
   FOR_SP(k, sp.cap) {
     sm.flag[k] = 0;
     if (!sp.valid[k] || sm.pair[k] < 0) continue;
@@ -380,7 +473,7 @@ __global__ void k_merge_single(SpDev sp, SmDev sm, SmConsts K) {
 }
 
 // calc_merge_stats_step2 + update_merge_flag (split_merge_orig.cu:555-656), R3.
-__device__ __forceinline__ void merge_decide_one(SpDev& sp, SmDev& sm, Scalars* sc,
+__device__ __forceinline__ void merge_decide_one(const SpDev& sp, const SmDev& sm, Scalars* sc,
                                                  const SmConsts& K, float merge_alpha, int k) {
   if (!sp.valid[k]) return;
   int f = sm.pair[k];
@@ -407,12 +500,26 @@ __device__ __forceinline__ void merge_decide_one(SpDev& sp, SmDev& sm, Scalars* 
   }
 }
 
-__global__ void k_merge_decide(SpDev sp, SmDev sm, Scalars* sc, SmConsts K, float merge_alpha) {
-  FOR_SP(k, sp.cap) merge_decide_one(sp, sm, sc, K, merge_alpha, k);
+__global__ void kb_merge_decide(const Slot* __restrict__ slots, SmConsts K, float merge_alpha) {
+  SLOT_Y;
+  FOR_SP(k, S.sp.cap) merge_decide_one(S.sp, S.sm, S.sc, K, merge_alpha, k);
+}
+
+// Merge set-up: candidate pairs unset, claims at +inf (cap + 2 entries).
+__global__ void kb_merge_clear(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S.cap + 2) return;
+  S.sm.pair[k] = -1;
+  S.sm.claim[k] = 0x7f7f7f7f;
 }
 
 // merge flag := accepted and claimant of its target; snapshot valid; target := pair.
-__global__ void k_merge_flag(SpDev sp, SmDev sm, uint8_t* __restrict__ valid0) {
+__global__ void kb_merge_flag(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const SmDev& sm = S.sm;
+  uint8_t* __restrict__ valid0 = S.valid0;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sp.cap) return;
   valid0[k] = sp.valid[k];
@@ -424,8 +531,13 @@ __global__ void k_merge_flag(SpDev sp, SmDev sm, uint8_t* __restrict__ valid0) {
 }
 
 // remove_sp (split_merge.cu:1035-1080) / remove_sp_p (split_merge_prop.cu:2353-2449).
-__global__ void k_merge_remove(SpDev sp, SmDev sm, Scalars* sc, const uint8_t* __restrict__ valid0,
-                               int prop_mode) {
+__global__ void kb_merge_remove(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const SmDev& sm = S.sm;
+  Scalars* sc = S.sc;
+  const uint8_t* __restrict__ valid0 = S.valid0;
+  const int prop_mode = S.mode;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sp.cap) return;
   int s = sm.pair[k];
@@ -454,9 +566,13 @@ __global__ void k_merge_remove(SpDev sp, SmDev sm, Scalars* sc, const uint8_t* _
 }
 
 // merge_sp (split_merge.cu:984-1000).
-__global__ void k_merge_apply(int* __restrict__ seg, int npix, int cap, SmDev sm) {
+__global__ void kb_merge_apply(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int* __restrict__ seg = S.seg;
+  const int cap = S.cap;
+  const SmDev& sm = S.sm;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
+  if (t >= S.npix) return;
   int k = seg[t];
   if (k < 0 || k >= cap) return;
   if (sm.flag[k] & 4) seg[t] = sm.target[k];

@@ -1,0 +1,119 @@
+"""Batched form: frames of uneven size (and video streams with resident state) run
+as one batch give exactly the labels of the plain per-frame path, alone or in any
+mix, and the plain path keeps matching the oracle (tested elsewhere), so the batch
+matches the oracle too (checked directly here on a small mixed batch)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from st_spix_gb300 import synth
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from st_spix_gb300 import batch, bist_cuda  # noqa: E402
+
+
+def cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+CFG = dict(niters=12, sm_period=4)
+
+
+def uneven_frames(n, seed=0, lo=40, hi=130):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        H = int(rng.integers(lo, hi)) // 8 * 8
+        W = int(rng.integers(lo, hi)) // 8 * 8
+        img, _ = synth.voronoi_frame(H, W, int(rng.integers(10, 60)),
+                                     float(rng.uniform(0.02, 0.08)), seed * 100 + i)
+        out.append((img, int(rng.choice([9, 12, 16]))))
+    return out
+
+
+def test_batch_independent_frames_match_single():
+    frames = uneven_frames(7, seed=1)
+    singles = []
+    for img, sp in frames:
+        lab, params = bist_cuda.run_bass(cuda(img), sp_size=sp, **CFG)
+        singles.append((lab.cpu().numpy(), params.n))
+    fr = [batch.Frame(img=cuda(img), sp_size=sp) for img, sp in frames]
+    batch.process_batch(fr, **CFG)
+    for f, (lab, n) in zip(fr, singles):
+        assert f.status == 0
+        assert f.nspix == n
+        np.testing.assert_array_equal(f.labels.cpu().numpy(), lab)
+    # and in another order / subset
+    sub = [batch.Frame(img=fr[i].img, sp_size=fr[i].sp_size) for i in (5, 2, 6)]
+    batch.process_batch(sub, **CFG)
+    for f, i in zip(sub, (5, 2, 6)):
+        np.testing.assert_array_equal(f.labels.cpu().numpy(), singles[i][0])
+
+
+def test_batch_matches_oracle():
+    frames = uneven_frames(3, seed=2)
+    fr = [batch.Frame(img=cuda(img), sp_size=sp) for img, sp in frames]
+    batch.process_batch(fr, **CFG)
+    for f, (img, sp) in zip(fr, frames):
+        st, lab, p, n = O.run_bass(img, O.default_config(sp_size=sp, **CFG))
+        assert st == 0 and f.nspix == n
+        np.testing.assert_array_equal(f.labels.cpu().numpy(), lab)
+
+
+@pytest.mark.parametrize("prop_niters", [0, 6])
+def test_batch_videos_match_bist_forward(prop_niters):
+    """Three videos of different sizes advanced one frame per batch (plus an
+    independent frame in every batch) equal bist_forward on each video."""
+    kw = dict(niters=10, sm_period=4, prop_niters=prop_niters)
+    specs = [(56, 72, 0), (64, 96, 1), (48, 40, 2)]
+    T = 4
+    vids = []
+    for H, W, s in specs:
+        v, f, _ = synth.voronoi_video(H, W, T, 20, 0.03, seed=s, max_shift=3.0)
+        vids.append((cuda(v), cuda(f)))
+    ref = []
+    for v, f in vids:
+        ref.append(bist_cuda.bist_forward(v, f, kw["niters"], 15, 0.5, 0.009 ** 2,
+                                          float(np.log(0.5)), 0.0, True, False,
+                                          sm_period=4, prop_niters=prop_niters).cpu().numpy())
+    extra_img, _ = synth.voronoi_frame(64, 64, 15, 0.05, 9)
+    extra_ref, _ = bist_cuda.run_bass(cuda(extra_img), sp_size=12, **kw)
+    videos = [batch.Video(v.shape[1], v.shape[2]) for v, _ in vids]
+    for t in range(T):
+        fr = []
+        for (v, f), vs in zip(vids, videos):
+            fr.append(batch.Frame(img=v[t], flow=f[t - 1] if t > 0 else None, video=vs))
+        fr.insert(1, batch.Frame(img=cuda(extra_img), sp_size=12))
+        batch.process_batch(fr, **kw)
+        np.testing.assert_array_equal(fr[1].labels.cpu().numpy(), extra_ref.cpu().numpy())
+        del fr[1]
+        for k, f in enumerate(fr):
+            assert f.status == 0
+            np.testing.assert_array_equal(f.labels.cpu().numpy(), ref[k][t],
+                                          err_msg=f"video {k} frame {t}")
+            assert videos[k].nspix == f.nspix
+    for vs in videos:
+        assert vs.frames == T
+        vs.close()
+
+
+def test_image_mode_bist_forward_batches():
+    """Image mode runs its frames as batches: same labels as one frame at a time."""
+    v, f, _ = synth.voronoi_video(64, 80, 5, 20, 0.03, seed=4, max_shift=3.0)
+    vid = cuda(v)
+    out = bist_cuda.bist_forward(vid, cuda(f), 9, 12, 0.5, 0.009 ** 2, float(np.log(0.5)), 0.0,
+                                 False, False, sm_period=4)
+    for t in range(5):
+        lab, _ = bist_cuda.run_bass(vid[t].contiguous(), niters=9, sp_size=12, sm_period=4)
+        np.testing.assert_array_equal(out[t].cpu().numpy(), lab.cpu().numpy())
+
+
+def test_batch_rejects_same_video_twice():
+    v, f, _ = synth.voronoi_video(32, 32, 2, 8, 0.03, seed=5, max_shift=2.0)
+    vs = batch.Video(32, 32)
+    fr = [batch.Frame(img=cuda(v[0]), video=vs), batch.Frame(img=cuda(v[1]), video=vs)]
+    with pytest.raises(RuntimeError):
+        batch.process_batch(fr, niters=4)
+    vs.close()
