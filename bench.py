@@ -5,10 +5,14 @@
 Workload (one "step"): the 30-frame 480x854 synthetic streaming video of the
 streaming-propagation configuration (Voronoi frames with 400 seeds, per-region
 affine motion, noise sigma 0.03, ground-truth forward flow), run through
-bist_forward in video mode: frame 0 is plain BASS, frames 1..29 are flow
-propagation + hole fill + 20 boundary iterations with split/merge every 10,
-superpixel size 20.  Each rank runs its own stream (seed = rank): replicas, no
-collective on the data path.  Prints ONE JSON line on rank 0.
+frame 0 is plain BASS, frames 1..29 are flow propagation + hole fill + 20
+boundary iterations with split/merge every 10, superpixel size 20.  Each GPU runs
+--streams such videos (seeds rank*S..), advanced together: frame t of the streams
+of one host lane is one batch of the batched engine (st_spix_gb300.batch), with
+labels, parameters and previous frame resident on the device between batches.  A
+step is the whole video of every stream.  Ranks are replicas (no collective on
+the data path).  The plain per-frame path (bist_forward, one stream) is timed
+beside it.  Prints ONE JSON line on rank 0.
 """
 from __future__ import annotations
 
@@ -219,10 +223,14 @@ def run_reference(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--streams", type=int, default=8,
-                    help="concurrent video streams per GPU (host thread + CUDA stream each)")
+    ap.add_argument("--streams", type=int, default=16,
+                    help="video streams per GPU; frame t of every stream of a lane runs as "
+                         "one batch")
+    ap.add_argument("--lanes", type=int, default=2,
+                    help="host threads per GPU, each with its own CUDA stream, engine "
+                         "context and share of the streams")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -233,7 +241,7 @@ def main():
 
     import numpy as np
     import torch
-    from st_spix_gb300 import bist_cuda
+    from st_spix_gb300 import batch, bist_cuda
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -248,38 +256,59 @@ def main():
 
     w = WORKLOAD
     S = max(1, args.streams)
-    kw = dict(sm_period=w["sm_period"], prop_niters=w["prop_niters"])
+    NL = max(1, min(args.lanes, S))
+    T = w["T"]
+    cfg = dict(niters=w["niters"], sp_size=w["sp_size"], potts=w["potts"],
+               sigma2_app=w["sigma2_app"], alpha=w["alpha"], split_alpha=w["split_alpha"],
+               sm_period=w["sm_period"], prop_niters=w["prop_niters"])
 
-    def call(v, f):
-        return bist_cuda.bist_forward(v, f, w["niters"], w["sp_size"], w["potts"],
-                                      w["sigma2_app"], w["alpha"], w["split_alpha"], True, False,
-                                      **kw)
+    # one video per stream (seed = rank * S + i), generated on the device; the host
+    # copies feed the end-to-end leg
+    from st_spix_gb300 import synth
+    dvid, dflo = [], []
+    for i in range(S):
+        v, f = synth.voronoi_video_device(w["H"], w["W"], T, w["nseeds"], w["sigma"],
+                                          seed=rank * S + i, device=dev)
+        dvid.append(v)
+        dflo.append(f)
+    host = [(v.cpu().numpy(), f.cpu().numpy()) for v, f in zip(dvid, dflo)]
+    dout = [torch.empty((T, w["H"], w["W"]), dtype=torch.int32, device=dev) for _ in range(S)]
+    lanes = [list(range(j, S, NL)) for j in range(NL)]
+    cstreams = [torch.cuda.Stream(dev) for _ in range(NL)]
+    videos, ctxs = [], []
+    for j in range(NL):
+        with torch.cuda.stream(cstreams[j]):
+            videos.append([batch.Video(w["H"], w["W"], dev) for _ in lanes[j]])
+            ctxs.append(bist_cuda._ctx(dev))
+    batch_ms = [[] for _ in range(NL)]
 
-    # one video per stream (seed = rank * S + i), resident on the device
-    host = [gen_video(seed=rank * S + i) for i in range(S)]
-    dvid = [torch.from_numpy(v).to(dev) for v, _ in host]
-    dflo = [torch.from_numpy(f).to(dev) for _, f in host]
-    streams = [torch.cuda.Stream(dev) for _ in range(S)]
-    ctxs = [None] * S
-    frame_ms = [[] for _ in range(S)]
-    launches = [0] * S
+    def video_pass(j, vid, flo, out, record):
+        """All T frames of lane j's streams: frame t of every stream in one batch."""
+        for v in videos[j]:
+            v.reset()
+        for t in range(T):
+            fr = [batch.Frame(img=vid[i][t], flow=flo[i][t - 1] if t > 0 else None,
+                              video=videos[j][k], labels=out[i][t])
+                  for k, i in enumerate(lanes[j])]
+            batch.process_batch(fr, **cfg)
+            if record:
+                batch_ms[j].append(ctxs[j].last_batch_ms())
 
-    def run_all(fn, nsteps):
-        """Run fn(i, step) for every stream i on its own host thread and CUDA stream."""
-        gate = threading.Barrier(S)
+    def run_lanes(fn, nsteps):
+        gate = threading.Barrier(NL)
         errs = []
 
-        def body(i):
+        def body(j):
             try:
                 torch.cuda.set_device(dev)
-                with torch.cuda.stream(streams[i]):
+                with torch.cuda.stream(cstreams[j]):
                     gate.wait()
                     for st in range(nsteps):
-                        fn(i, st)
-                    streams[i].synchronize()
+                        fn(j, st)
+                    cstreams[j].synchronize()
             except Exception as e:  # surfaced below
                 errs.append(repr(e))
-        th = [threading.Thread(target=body, args=(i,)) for i in range(S)]
+        th = [threading.Thread(target=body, args=(j,)) for j in range(NL)]
         for t in th:
             t.start()
         for t in th:
@@ -287,27 +316,18 @@ def main():
         if errs:
             raise RuntimeError("; ".join(errs))
 
-    def warm(i, st):
-        ctxs[i] = bist_cuda._ctx(dev)  # the context of stream i (one per CUDA stream)
-        call(dvid[i], dflo[i])
-
-    run_all(warm, args.warmup)
+    run_lanes(lambda j, st: video_pass(j, dvid, dflo, dout, False), args.warmup)
     torch.cuda.synchronize()
 
-    # ---- timed region (device-resident inputs) ---------------------------------
+    # ---- timed region (device-resident inputs, larger than L2) -----------------
     clk_lines, stop = [], threading.Event()
     th = threading.Thread(target=sample_clocks, args=(local, stop, clk_lines), daemon=True)
     th.start()
     l0 = [c.launches() for c in ctxs]
-
-    def timed(i, st):
-        call(dvid[i], dflo[i])
-        frame_ms[i].extend(ctxs[i].frame_times())
-
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    run_all(timed, args.steps)
+    run_lanes(lambda j, st: video_pass(j, dvid, dflo, dout, True), args.steps)
     torch.cuda.synchronize()
     elapsed = time.perf_counter() - t0
     barrier()
@@ -319,36 +339,53 @@ def main():
         t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
-    frames_total = world * S * w["T"] * args.steps
+    frames_total = world * S * T * args.steps
     value = frames_total / elapsed
 
-    # ---- per-family device time, one stream alone, CUDA events on its stream ----
-    with torch.cuda.stream(streams[0]):
-        ctx0 = bist_cuda._ctx(dev)  # stream 0's context
-        ctx0.profile(True)
+    # ---- plain per-frame path: one stream, frame by frame (bist_forward) -------
+    def plain_call():
+        return bist_cuda.bist_forward(dvid[0], dflo[0], w["niters"], w["sp_size"], w["potts"],
+                                      w["sigma2_app"], w["alpha"], w["split_alpha"], True, False,
+                                      sm_period=w["sm_period"], prop_niters=w["prop_niters"])
+    pstream = torch.cuda.Stream(dev)
+    with torch.cuda.stream(pstream):
+        plain_call()
+        pstream.synchronize()
+        t0 = time.perf_counter()
         for _ in range(args.steps):
-            call(dvid[0], dflo[0])
-        streams[0].synchronize()
-        prof = ctx0.profile_get()
-        ctx0.profile(False)
+            plain_out = plain_call()
+        pstream.synchronize()
+        plain_fps = T * args.steps / (time.perf_counter() - t0)
+    agree = float((plain_out == dout[0]).float().mean().item())
+
+    # ---- per-family device time of lane 0's batches (CUDA events on its stream) --
+    with torch.cuda.stream(cstreams[0]):
+        ctxs[0].profile(True)
+        video_pass(0, dvid, dflo, dout, False)
+        cstreams[0].synchronize()
+        prof = ctxs[0].profile_get()
+        ctxs[0].profile(False)
 
     # ---- e2e through the public API with host buffers --------------------------
     h_vid = [torch.from_numpy(v).pin_memory() for v, _ in host]
     h_flo = [torch.from_numpy(f).pin_memory() for _, f in host]
-    h_out = [torch.empty((w["T"], w["H"], w["W"]), dtype=torch.int32).pin_memory()
-             for _ in range(S)]
+    h_out = [torch.empty((T, w["H"], w["W"]), dtype=torch.int32).pin_memory() for _ in range(S)]
+    e_vid = [torch.empty_like(v) for v in dvid]
+    e_flo = [torch.empty_like(f) for f in dflo]
 
-    def e2e(i, st):
-        dv = h_vid[i].to(dev, non_blocking=True)
-        df = h_flo[i].to(dev, non_blocking=True)
-        o = call(dv, df)
-        h_out[i].copy_(o, non_blocking=True)
-        streams[i].synchronize()
+    def e2e(j, st):
+        for i in lanes[j]:
+            e_vid[i].copy_(h_vid[i], non_blocking=True)
+            e_flo[i].copy_(h_flo[i], non_blocking=True)
+        video_pass(j, e_vid, e_flo, dout, False)
+        for i in lanes[j]:
+            h_out[i].copy_(dout[i], non_blocking=True)
+        cstreams[j].synchronize()
 
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    run_all(e2e, args.steps)
+    run_lanes(e2e, args.steps)
     e2e_elapsed = time.perf_counter() - t0
     barrier()
     if world > 1:
@@ -364,16 +401,18 @@ def main():
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the dominant kernel family --------------------------------
+    # ---- roofline of the dominant kernel ---------------------------------------
     npix = w["H"] * w["W"]
+    B0 = len(lanes[0])
     fam = max(prof, key=lambda k: prof[k][1])
-    nsweep = prof["sweep"][0]       # one fused launch per sweep
+    nsweep = prof["sweep"][0]       # one fused launch per sweep, over the lane's batch
     sweep_ms = prof["sweep"][1]
     peak, peak_kind = read_peaks()
-    achieved = (SWEEP_BYTES_PER_PX * npix * nsweep) / (sweep_ms / 1000.0) / 1e9 if sweep_ms else 0
+    per_launch = SWEEP_BYTES_PER_PX * npix * B0
+    achieved = per_launch * nsweep / (sweep_ms / 1000.0) / 1e9 if sweep_ms else 0
     traffic = read_traffic(w["name"])
-    passes_per_step = w["niters"] + (w["T"] - 1) * w["prop_niters"]
-    mpix_pass = world * S * args.steps * passes_per_step * npix / elapsed / 1e6
+    passes_per_video = w["niters"] + (T - 1) * w["prop_niters"]
+    mpix_pass = world * S * args.steps * passes_per_video * npix / elapsed / 1e6
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -385,8 +424,8 @@ def main():
         finally:
             base.close()
 
-    fms = sorted(x for lst in frame_ms for x in lst)
-    pct = lambda q: fms[min(len(fms) - 1, int(q * len(fms)))] if fms else None
+    bms = sorted(x for lst in batch_ms for x in lst)
+    pct = lambda q: bms[min(len(bms) - 1, int(q * len(bms)))] if bms else None
     h_bytes = sum(v.nbytes + f.nbytes for v, f in host)
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
@@ -396,16 +435,22 @@ def main():
         "config": {"workload": w["name"], "H": w["H"], "W": w["W"], "T": w["T"],
                    "sp_size": w["sp_size"], "niters": w["niters"],
                    "prop_niters": w["prop_niters"], "sm_period": w["sm_period"],
-                   "streams_per_gpu": S, "parallelism": f"replicas{world}",
+                   "streams_per_gpu": S, "lanes": NL, "batch_per_lane": B0,
+                   "step": "all %d frames of every stream; frame t of a lane's streams is "
+                           "one batch" % T,
+                   "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2: %d MB of frames+flow read per step" %
                          (h_bytes // 2 ** 20)},
         "p50_frame_ms": pct(0.50), "p99_frame_ms": pct(0.99),
+        "latency_note": "frame latency = GPU time of the batch the frame ran in",
+        "plain_per_frame_fps": plain_fps,
+        "plain_vs_batched_label_agreement": agree,
         "mpix_per_s_per_pass": mpix_pass,
-        "roofline": {"bound": "hbm", "kernel": "k_sweep_fused (border + 4 parity phases)",
+        "roofline": {"bound": "hbm", "kernel": "kb_sweep (border + 4 parity phases, batched)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": SWEEP_BYTES_PER_PX * npix,
+                     "algorithmic_bytes_per_launch": per_launch,
                      "dominant_family": fam,
                      "family_ms": {k: round(v[1], 3) for k, v in prof.items()},
                      "family_launches": {k: v[0] for k, v in prof.items()}},

@@ -128,6 +128,9 @@ int         stspix_get_frame_log(const stspix_ctx* ctx, stspix_frame_log* out);
 int stspix_profile_enable(stspix_ctx* ctx, int enable);
 int stspix_profile_get(const stspix_ctx* ctx, int family, long long* launches,
                        double* total_ms);
+/* Per-kernel totals of the profiled launches as text, one "name launches ms" line
+ * per kernel; returns the bytes needed (including the terminating zero).       */
+int stspix_profile_kernels(const stspix_ctx* ctx, char* buf, int capacity);
 /* Per-frame durations (ms) of the last bist_forward call; returns the count. */
 int stspix_frame_times(const stspix_ctx* ctx, double* ms_out, int capacity);
 

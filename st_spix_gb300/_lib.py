@@ -68,7 +68,7 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_profile_get", "stspix_frame_times", "stspix_get_marked_video_noalloc",
            "stspix_video_create", "stspix_video_destroy", "stspix_video_reset",
            "stspix_video_nspix", "stspix_video_frames", "stspix_process_batch",
-           "stspix_footprint", "stspix_last_batch_ms"]
+           "stspix_footprint", "stspix_last_batch_ms", "stspix_profile_kernels"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -123,6 +123,7 @@ def load(build_if_missing: bool = True):
             "stspix_footprint": (I, [I, I, I, C.POINTER(C.c_longlong),
                                      C.POINTER(C.c_longlong)]),
             "stspix_last_batch_ms": (C.c_double, [P]),
+            "stspix_profile_kernels": (I, [P, C.c_char_p, I]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -174,6 +175,17 @@ class Context:
             n, ms = C.c_longlong(0), C.c_double(0)
             self.check(self.lib.stspix_profile_get(self.handle, i, C.byref(n), C.byref(ms)))
             out[name] = (int(n.value), float(ms.value))
+        return out
+
+    def profile_kernels(self) -> dict:
+        """Per-kernel (launches, total ms) of the profiled launches."""
+        n = self.lib.stspix_profile_kernels(self.handle, None, 0)
+        buf = C.create_string_buffer(max(n, 1))
+        self.lib.stspix_profile_kernels(self.handle, buf, n)
+        out = {}
+        for ln in buf.value.decode().splitlines():
+            name, cnt, ms = ln.split()
+            out[name] = (int(cnt), float(ms))
         return out
 
     def frame_times(self) -> list:

@@ -8,11 +8,12 @@
 // The outer BASS loop runs the slots sorted by iteration count, so at outer
 // iteration idx the slots still iterating are a prefix of the table.
 //
-// No host synchronisation inside the BASS loop: data-dependent loops (split BFS,
-// hole filling, connected components) run as bounded cooperative kernels and the
-// values the reference reads back every step stay on the device.  A batch with
-// propagated frames and the 4/8/12 iteration ladder reads the hole counts back
-// once (the ladder picks each frame's iteration count from them).
+// No host synchronisation inside the BASS loop and no grid-wide barrier anywhere:
+// the reference's host-driven loops (split BFS, hole filling, connected components)
+// become a block-per-superpixel BFS, a block-per-frame fill over the hole list and
+// a union-find, and the values the reference reads back every step stay on the
+// device.  A batch with propagated frames and the 4/8/12 iteration ladder reads the
+// hole counts back once (the ladder picks each frame's iteration count from them).
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -23,14 +24,14 @@
 #include <string>
 #include <vector>
 
+#include <map>
+
 #include <cuda_runtime.h>
 
 #include "engine.h"
 #include "kernels.h"
 
 namespace stspix {
-
-constexpr int kMaxRounds = 4096;  // relaxation rounds per cooperative launch
 
 struct Buf {
   void* p = nullptr;
@@ -67,12 +68,9 @@ enum { kStageShift = 1, kStageSeg = 2 };
 struct List {
   Slot* d = nullptr;               // device table
   int B = 0;
-  int max_npix = 0, max_cap = 0, max_nprev = 0, max_tx = 0, max_ty = 0;
+  int max_npix = 0, max_cap = 0, max_nprev = 0, max_tx = 0, max_ty = 0, max_w = 0, max_h = 0;
   long long max_acc = 0, max_sm = 0;
-  int tiles = 0;
-  long long pix = 0, q = 0;
   bool any_prop = false;
-  std::vector<int> tiles_upto;     // tiles of the first i slots
 };
 
 }  // namespace stspix
@@ -102,24 +100,27 @@ struct stspix_ctx {
   int bcap = 0;
   Scalars* sc = nullptr;        // device [bcap]
   Scalars* sc_host = nullptr;   // pinned [bcap]
-  Scalars* ctl = nullptr;       // grid barrier of the cooperative launches
-  int* round_flags = nullptr;   // [kMaxRounds * (bcap + 1)]
-  int* fill_counts = nullptr;   // [kFillBreakIter * bcap]
-  int* fill_done = nullptr;     // [bcap]
   Slot* d_slots = nullptr;      // device [3 * bcap]: all, BASS, propagated
   Slot* h_slots = nullptr;      // pinned staging of the same
   std::vector<Buf> ctl_bufs;
-  int coop_relax0 = 0, coop_relax1 = 0, coop_fill = 0;
+  // hole-fill loop graphs (conditional WHILE node), per (slot table, batch size)
+  struct FillGraph { cudaGraph_t g; cudaGraphExec_t exec; };
+  std::map<std::pair<const Slot*, int>, FillGraph> fill_graphs;
+  cudaStream_t capture_stream = nullptr;
+  int* body_iters = nullptr;       // device: fill-loop iterations run (launch count)
+  int* body_iters_host = nullptr;  // pinned
+  long long body_iters_seen = 0;
   // bist_forward's stream state
   stspix_video* fwd = nullptr;
   // profiling (CUDA events on the launching stream)
   int prof_on = 0;
   int cur_fam = STSPIX_FAM_OTHER;
   std::vector<cudaEvent_t> ev_free;
-  struct Pending { int fam; cudaEvent_t a, b; };
+  struct Pending { int fam; const char* name; cudaEvent_t a, b; };
   std::vector<Pending> pending;
   long long fam_launches[STSPIX_NFAM] = {0};
   double fam_ms[STSPIX_NFAM] = {0};
+  std::map<std::string, std::pair<long long, double>> kern;  // per kernel: launches, ms
   struct FrameEv { cudaEvent_t a, b; int n; };  // n frames between a and b
   std::vector<FrameEv> frame_ev;
   std::vector<double> frame_ms;
@@ -130,6 +131,7 @@ struct stspix_ctx {
 namespace {
 
 const int kThreads = 256;
+const int kBfsBigSmem = 5 * 512 * 8 * 8;  // kb_split_bfs_big: 5 arrays of 512 rows x 8 words
 inline unsigned blocks_for(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
 
 int fail(stspix_ctx* c, int code, const char* fmt, ...) {
@@ -166,11 +168,11 @@ inline cudaEvent_t prof_begin(stspix_ctx* ctx, cudaStream_t st) {
   cudaEventRecord(e, st);
   return e;
 }
-inline void prof_end(stspix_ctx* ctx, cudaStream_t st, cudaEvent_t a) {
+inline void prof_end(stspix_ctx* ctx, cudaStream_t st, cudaEvent_t a, const char* name) {
   if (!a) return;
   cudaEvent_t b = ev_get(ctx);
   cudaEventRecord(b, st);
-  ctx->pending.push_back({ctx->cur_fam, a, b});
+  ctx->pending.push_back({ctx->cur_fam, name, a, b});
 }
 // Called after the stream has been synchronised.
 void prof_harvest(stspix_ctx* ctx) {
@@ -179,6 +181,9 @@ void prof_harvest(stspix_ctx* ctx) {
     if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
       ctx->fam_ms[p.fam] += ms;
       ctx->fam_launches[p.fam] += 1;
+      auto& k = ctx->kern[p.name];
+      k.first += 1;
+      k.second += ms;
     }
     ctx->ev_free.push_back(p.a);
     ctx->ev_free.push_back(p.b);
@@ -191,7 +196,7 @@ void prof_harvest(stspix_ctx* ctx) {
     cudaEvent_t pe_ = prof_begin(ctx, st);                                     \
     kernel<<<grid, block, 0, st>>>(__VA_ARGS__);                               \
     ctx->launches++;                                                           \
-    prof_end(ctx, st, pe_);                                                    \
+    prof_end(ctx, st, pe_, #kernel);                                           \
   } while (0)
 
 #define LAUNCH(kernel, n, ...)                                                 \
@@ -304,24 +309,31 @@ int ensure_slot(stspix_ctx* ctx, int i, int npix, int sp_cap) {
     AL(L, s.cnt_pool, c2); AL(L, s.cs, c2); AL(L, s.cf, c2);
     AL(L, s.fs, 2 * c2); AL(L, s.fds, 2 * c2); AL(L, s.ss, c2);
     AL(L, s.centers, 2 * c2); AL(L, s.rbest, c2); AL(L, s.ccbest, c2);
+    AL(L, s.bbox, 4 * c2);
     w.sp_cap = cap;
   }
   return STSPIX_OK;
+}
+
+void drop_fill_graphs(stspix_ctx* ctx) {
+  for (auto& kv : ctx->fill_graphs) {
+    cudaGraphExecDestroy(kv.second.exec);
+    cudaGraphDestroy(kv.second.g);
+  }
+  ctx->fill_graphs.clear();
 }
 
 // Per-slot control arrays for batches of up to B slots.
 int ensure_bcap(stspix_ctx* ctx, int B) {
   if (B <= ctx->bcap) return STSPIX_OK;
   CK(cudaDeviceSynchronize());
+  drop_fill_graphs(ctx);
   free_list(ctx->ctl_bufs);
   if (ctx->sc_host) { cudaFreeHost(ctx->sc_host); ctx->sc_host = nullptr; }
   if (ctx->h_slots) { cudaFreeHost(ctx->h_slots); ctx->h_slots = nullptr; }
   int nb = std::max(B, 2 * ctx->bcap);
   auto& L = ctx->ctl_bufs;
   AL(L, ctx->sc, nb);
-  AL(L, ctx->round_flags, (size_t)kMaxRounds * (nb + 1));
-  AL(L, ctx->fill_counts, (size_t)kFillBreakIter * nb);
-  AL(L, ctx->fill_done, nb);
   AL(L, ctx->d_slots, 3 * (size_t)nb);
   CK(cudaMallocHost(&ctx->sc_host, sizeof(Scalars) * nb));
   CK(cudaMallocHost(&ctx->h_slots, sizeof(Slot) * 3 * nb));
@@ -392,26 +404,20 @@ List make_list(stspix_ctx* ctx, int off, const std::vector<Slot>& slots) {
   Slot* h = ctx->h_slots + (size_t)off * ctx->bcap;
   L.B = (int)slots.size();
   for (int i = 0; i < L.B; i++) {
-    Slot s = slots[i];
-    s.tile_base = L.tiles;
-    s.pix_base = L.pix;
-    s.q_base = L.q;
+    const Slot& s = slots[i];
     h[i] = s;
-    L.tiles_upto.push_back(L.tiles);
-    const int tx = (s.W + 31) / 32, ty = (s.H + 31) / 32;
-    L.tiles += tx * ty;
-    L.pix += s.npix;
-    L.q += (long long)((s.W + 1) / 2) * ((s.H + 1) / 2);
+    const int tx = (s.W + kSweepTileW - 1) / kSweepTileW, ty = (s.H + kSweepTileH - 1) / kSweepTileH;
     L.max_npix = std::max(L.max_npix, s.npix);
     L.max_cap = std::max(L.max_cap, s.cap);
     L.max_nprev = std::max(L.max_nprev, s.n_prev);
     L.max_tx = std::max(L.max_tx, tx);
+    L.max_w = std::max(L.max_w, s.W);
+    L.max_h = std::max(L.max_h, s.H);
     L.max_ty = std::max(L.max_ty, ty);
     L.max_acc = std::max(L.max_acc, (long long)s.H * ((s.W + 7) / 8));
     L.max_sm = std::max(L.max_sm, (long long)s.H * ((s.W + 15) / 16));
     if (s.mode) L.any_prop = true;
   }
-  L.tiles_upto.push_back(L.tiles);
   return L;
 }
 
@@ -422,26 +428,20 @@ int upload(stspix_ctx* ctx, cudaStream_t st, const List& L, int off) {
   return STSPIX_OK;
 }
 
-int coop_launch(stspix_ctx* ctx, cudaStream_t st, const void* fn, long long want_blocks,
-                int max_blocks, void** args) {
-  int g = (int)std::max(1LL, std::min<long long>(want_blocks, max_blocks));
-  cudaEvent_t pe = prof_begin(ctx, st);
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(g), dim3(kThreads), args, 0, st);
-  ctx->launches++;
-  prof_end(ctx, st, pe);
-  if (e != cudaSuccess)
-    return fail(ctx, STSPIX_ERR_CUDA, "cooperative launch failed: %s", cudaGetErrorString(e));
-  return STSPIX_OK;
-}
-
 // ---------------------------------------------------------------------------
 // Stages over the first nb slots of a table.
+
+// kb_accumulate blocks per slot: 8 warps each, about 4 row segments per warp.
+unsigned acc_blocks(const List& L) {
+  const long long segs = (long long)L.max_h * ((L.max_w + 31) / 32);
+  return (unsigned)std::max(1LL, (segs + 31) / 32);
+}
 
 // update_params (update_params.cu:12-52): statistics + posterior.
 int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb) {
   ctx->cur_fam = STSPIX_FAM_STATS;
   LAUNCHB(kb_clear_stats, L.max_cap, L, nb);
-  LAUNCHG(kb_accumulate, dim3((unsigned)((L.max_acc + 127) / 128), (unsigned)nb), 128, L.d);
+  LAUNCHG(kb_accumulate, dim3(acc_blocks(L), (unsigned)nb), 256, L.d);
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
   LAUNCHB(kb_posterior, L.max_cap, L, nb);
   return STSPIX_OK;
@@ -464,39 +464,20 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   return STSPIX_OK;
 }
 
-int run_relax(stspix_ctx* ctx, cudaStream_t st, int mode, const List& L, int nb) {
-  if (nb <= 0) return STSPIX_OK;
-  int total = L.tiles_upto[nb];  // tiles of the first nb slots
-  CK(cudaMemsetAsync(ctx->round_flags, 0, sizeof(int) * (size_t)(nb + 1), st));
-  int max_rounds = kMaxRounds;
-  Slot* d = L.d;
-  void* args[] = {(void*)&d, (void*)&nb, (void*)&total, (void*)&ctx->ctl,
-                  (void*)&ctx->round_flags, (void*)&max_rounds};
-  if (mode == 0)
-    return coop_launch(ctx, st, (const void*)kb_relax_bfs, total, ctx->coop_relax0, args);
-  return coop_launch(ctx, st, (const void*)kb_relax_cc, total, ctx->coop_relax1, args);
-}
-
-int run_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
-  CK(cudaMemsetAsync(ctx->fill_counts, 0, sizeof(int) * (size_t)L.B, st));
-  CK(cudaMemsetAsync(ctx->fill_done, 0, sizeof(int) * (size_t)L.B, st));
-  int B = L.B;
-  long long pix = L.pix, q = L.q;
-  int break_iter = kFillBreakIter;
-  Slot* d = L.d;
-  void* args[] = {(void*)&d, (void*)&B, (void*)&pix, (void*)&q, (void*)&ctx->ctl,
-                  (void*)&ctx->fill_counts, (void*)&ctx->fill_done, (void*)&break_iter};
-  return coop_launch(ctx, st, (const void*)kb_fill, blocks_for(pix), ctx->coop_fill, args);
-}
-
 int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmConsts& K,
               const stspix_config& cfg, int dir_b, int dir_p) {
   ctx->cur_fam = STSPIX_FAM_SPLIT;
   LAUNCHS(kb_split_begin, L, nb);
   LAUNCHB(kb_split_clear, L.max_npix, L, nb);
   LAUNCHB(kb_split_seed, L.max_cap, L, nb, dir_b, dir_p);
-  int r = run_relax(ctx, st, 0, L, nb);
-  if (r) return r;
+  LAUNCHG(kb_bbox, dim3(blocks_for(L.max_sm), (unsigned)nb), kThreads, L.d);
+  LAUNCHG(kb_split_bfs, dim3(256, (unsigned)nb), 128, L.d);  // 1024 warps per slot
+  {
+    cudaEvent_t pe_ = prof_begin(ctx, st);
+    kb_split_bfs_big<<<dim3(8, (unsigned)nb), 256, kBfsBigSmem, st>>>(L.d);
+    ctx->launches++;
+    prof_end(ctx, st, pe_, "kb_split_bfs_big");
+  }
   LAUNCHB(kb_split_partition, L.max_npix, L, nb);
   LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
   LAUNCHG(kb_sm_accumulate, dim3(blocks_for(L.max_sm), (unsigned)nb), kThreads, L.d, 1);
@@ -617,9 +598,65 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHS(kb_scalars, L, L.B, (int)kOpAfterHex);
   LAUNCHB(kb_init_bass_params, L.max_cap, L, L.B);
   LAUNCHB(kb_clear_stats, L.max_cap, L, L.B);
-  LAUNCHG(kb_accumulate, dim3((unsigned)((L.max_acc + 127) / 128), (unsigned)L.B), 128, L.d);
+  LAUNCHG(kb_accumulate, dim3(acc_blocks(L), (unsigned)L.B), 256, L.d);
   LAUNCHB(kb_init_prior_mu, L.max_cap, L, L.B);
   LAUNCHB(kb_find_border, L.max_npix, L, L.B);
+  return STSPIX_OK;
+}
+
+// The hole-fill loop of the propagated slots of table L as a graph: a WHILE node
+// whose body is one iteration (kb_fill_border, kb_fill_phase x 4, kb_fill_compact,
+// kb_fill_step); kb_fill_step sets the condition.  Built once per (table, size).
+int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
+  auto key = std::make_pair((const Slot*)L.d, L.B);
+  auto it = ctx->fill_graphs.find(key);
+  if (it != ctx->fill_graphs.end()) { *out = it->second.exec; return STSPIX_OK; }
+  if (!ctx->capture_stream) CK(cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle cond;
+  CK(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = cond;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  cudaStream_t cs = ctx->capture_stream;
+  CK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  const unsigned G = (unsigned)std::max(8, std::min(128, 2048 / std::max(L.B, 1)));
+  const dim3 grid(G, (unsigned)L.B);
+  kb_fill_border<<<grid, kThreads, 0, cs>>>(L.d);
+  for (int ph = 0; ph < 4; ph++) kb_fill_phase<<<grid, kThreads, 0, cs>>>(L.d, ph);
+  kb_fill_compact<<<grid, kThreads, 0, cs>>>(L.d);
+  kb_fill_step<<<1, kThreads, 0, cs>>>(L.d, L.B, cond, kFillBreakIter, ctx->body_iters);
+  cudaGraph_t captured = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(cs, &captured);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(ctx, STSPIX_ERR_CUDA, "fill graph capture failed: %s", cudaGetErrorString(ce));
+  }
+  cudaGraphExec_t exec = nullptr;
+  ce = cudaGraphInstantiate(&exec, g, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(ctx, STSPIX_ERR_CUDA, "fill graph instantiation failed: %s", cudaGetErrorString(ce));
+  }
+  ctx->fill_graphs[key] = {g, exec};
+  *out = exec;
+  return STSPIX_OK;
+}
+
+int run_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
+  cudaGraphExec_t exec;
+  int r = fill_graph(ctx, L, &exec);
+  if (r) return r;
+  LAUNCHS(kb_fill_begin, L, L.B);
+  cudaEvent_t pe = prof_begin(ctx, st);
+  CK(cudaGraphLaunch(exec, st));
+  prof_end(ctx, st, pe, "kb_fill_graph");
   return STSPIX_OK;
 }
 
@@ -633,16 +670,18 @@ int shift_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHB(kb_flow_mean, L.max_nprev, L, L.B);
   LAUNCHB(kb_shift, L.max_npix, L, L.B);
   LAUNCHB(kb_shift_decode, L.max_npix, L, L.B);
-  LAUNCHB(kb_count_labels, L.max_npix, L, L.B, 0);
+  LAUNCHG(kb_count_labels, dim3(blocks_for(L.max_sm), (unsigned)L.B), kThreads, L.d, 0);
   // fill, invalidate disconnected, fill
   if ((r = run_fill(ctx, st, L))) return r;
   LAUNCHB(kb_cc_init, L.max_npix, L, L.B);
-  if ((r = run_relax(ctx, st, 1, L, L.B))) return r;
+  LAUNCHB(kb_cc_hook, L.max_npix, L, L.B);
+  LAUNCHB(kb_cc_compress, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_size, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_best, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_invalidate, L.max_npix, L, L.B);
+  LAUNCHB(kb_list_holes, L.max_npix, L, L.B);
   if ((r = run_fill(ctx, st, L))) return r;
-  LAUNCHB(kb_count_labels, L.max_npix, L, L.B, 1);
+  LAUNCHG(kb_count_labels, dim3(blocks_for(L.max_sm), (unsigned)L.B), kThreads, L.d, 1);
   LAUNCHB(kb_shift_params, L.max_nprev, L, L.B);
   return STSPIX_OK;
 }
@@ -658,8 +697,11 @@ int prop_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
 
 int read_scalars(stspix_ctx* ctx, cudaStream_t st, int B) {
   CK(cudaMemcpyAsync(ctx->sc_host, ctx->sc, sizeof(Scalars) * (size_t)B, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(ctx->sc_host + B, ctx->ctl, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->body_iters_host, ctx->body_iters, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  // kernels launched by the fill graphs: 7 per loop iteration
+  ctx->launches += 7 * ((long long)*ctx->body_iters_host - ctx->body_iters_seen);
+  ctx->body_iters_seen = *ctx->body_iters_host;
   CK(cudaGetLastError());
   prof_harvest(ctx);
   return STSPIX_OK;
@@ -689,7 +731,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
               int extra_update = 0) {
   const int B = (int)fr.size();
   int r;
-  if ((r = ensure_bcap(ctx, B + 1))) return r;
+  if ((r = ensure_bcap(ctx, B))) return r;
   std::vector<int> caps(B);
   for (int i = 0; i < B; i++) {
     caps[i] = slot_cap(fr[i]);
@@ -706,7 +748,6 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
   List Lp = make_list(ctx, 2, prop);
   if ((r = upload(ctx, st, La, 0)) || (r = upload(ctx, st, Lb, 1)) || (r = upload(ctx, st, Lp, 2)))
     return r;
-  CK(cudaMemsetAsync(ctx->ctl, 0, sizeof(Scalars), st));
   ctx->cur_fam = STSPIX_FAM_OTHER;
   LAUNCHS(kb_scalars, La, B, (int)kOpBegin);
   if ((stages & kStageShift) && (r = shift_fill(ctx, st, Lp))) return r;
@@ -717,7 +758,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
   if (!(stages & kStageSeg)) {
     if ((r = read_scalars(ctx, st, B))) return r;
     for (int i = 0; i < B; i++) {
-      out.status[i] = ctx->sc_host[i].status ? ctx->sc_host[i].status : ctx->sc_host[B].status;
+      out.status[i] = ctx->sc_host[i].status;
       fill_log(out.log[i], ctx->sc_host[i], 0);
     }
     return STSPIX_OK;
@@ -767,7 +808,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     const Scalars& s = ctx->sc_host[i];
     out.nspix[i] = s.nspix;
     out.niters[i] = nit[i];
-    out.status[i] = s.status ? s.status : ctx->sc_host[B].status;
+    out.status[i] = s.status;
     fill_log(out.log[i], s, nit[i]);
   }
   return STSPIX_OK;
@@ -890,27 +931,17 @@ int stspix_create(stspix_ctx** out, int device) {
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) { delete ctx; return STSPIX_ERR_CUDA; }
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
-  int coop = 0;
-  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
-  int nb = 0;
-  // Cooperative grids use at most one block per SM: with up to
-  // (resident blocks per SM) streams launching cooperative kernels at once, all of
-  // their blocks can still be resident together (other kernels always drain).
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)kb_relax_bfs, kThreads, 0);
-  ctx->coop_relax0 = std::min(nb, 1) * ctx->num_sms;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)kb_relax_cc, kThreads, 0);
-  ctx->coop_relax1 = std::min(nb, 1) * ctx->num_sms;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)kb_fill, kThreads, 0);
-  ctx->coop_fill = std::min(nb, 1) * ctx->num_sms;
-  if (!coop || ctx->coop_relax0 <= 0 || ctx->coop_relax1 <= 0 || ctx->coop_fill <= 0) {
+  if (cudaFuncSetAttribute((const void*)kb_split_bfs_big,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, kBfsBigSmem) != cudaSuccess) {
     delete ctx;
     return STSPIX_ERR_CUDA;
   }
-  if (cudaMalloc(&ctx->ctl, sizeof(Scalars)) != cudaSuccess ||
-      ensure_bcap(ctx, 4) != STSPIX_OK) {
+  if (ensure_bcap(ctx, 4) != STSPIX_OK || cudaMalloc(&ctx->body_iters, sizeof(int)) != cudaSuccess ||
+      cudaMallocHost(&ctx->body_iters_host, sizeof(int)) != cudaSuccess) {
     delete ctx;
     return STSPIX_ERR_NOMEM;
   }
+  cudaMemset(ctx->body_iters, 0, sizeof(int));
   cudaEventCreate(&ctx->batch_ev[0]);
   cudaEventCreate(&ctx->batch_ev[1]);
   cudaDeviceSynchronize();
@@ -924,12 +955,15 @@ int stspix_destroy(stspix_ctx* ctx) {
   cudaDeviceSynchronize();
   if (ctx->fwd) stspix_video_destroy(ctx->fwd);
   for (auto& w : ctx->work) { free_list(w.pix); free_list(w.sp); }
+  drop_fill_graphs(ctx);
+  if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
   free_list(ctx->ctl_bufs);
+  cudaFree(ctx->body_iters);
+  if (ctx->body_iters_host) cudaFreeHost(ctx->body_iters_host);
   prof_harvest(ctx);
   for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.a); ctx->ev_free.push_back(e.b); }
   for (auto e : ctx->ev_free) cudaEventDestroy(e);
   for (auto e : ctx->batch_ev) if (e) cudaEventDestroy(e);
-  cudaFree(ctx->ctl);
   if (ctx->sc_host) cudaFreeHost(ctx->sc_host);
   if (ctx->h_slots) cudaFreeHost(ctx->h_slots);
   delete ctx;
@@ -1258,7 +1292,25 @@ int stspix_profile_enable(stspix_ctx* ctx, int enable) {
   if (!ctx) return STSPIX_ERR_ARG;
   ctx->prof_on = enable ? 1 : 0;
   for (int i = 0; i < STSPIX_NFAM; i++) { ctx->fam_launches[i] = 0; ctx->fam_ms[i] = 0; }
+  ctx->kern.clear();
   return STSPIX_OK;
+}
+
+int stspix_profile_kernels(const stspix_ctx* ctx, char* buf, int capacity) {
+  if (!ctx) return -1;
+  std::string out;
+  char line[160];
+  for (auto& kv : ctx->kern) {
+    snprintf(line, sizeof line, "%s %lld %.6f\n", kv.first.c_str(), kv.second.first,
+             kv.second.second);
+    out += line;
+  }
+  if (buf && capacity > 0) {
+    size_t n = std::min(out.size(), (size_t)capacity - 1);
+    memcpy(buf, out.data(), n);
+    buf[n] = 0;
+  }
+  return (int)out.size() + 1;
 }
 
 int stspix_profile_get(const stspix_ctx* ctx, int family, long long* launches, double* total_ms) {

@@ -24,9 +24,8 @@ namespace stspix {
 constexpr int kFxAppShift = 28;
 constexpr int kFxSqShift = 20;
 constexpr int kFxFlowShift = 24;
-constexpr int kMaxCoopRounds = 1 << 14;   // cap of the relaxation loops
 constexpr int kFillBreakIter = 1000;      // fill_missing.cu: break_iter
-constexpr long long kBarrierSpinLimit = 1LL << 24;
+constexpr int kSweepTileW = 64, kSweepTileH = 32;  // boundary-sweep tile
 
 // Packed record read by the boundary sweep: the fields calc_joint reads
 // (update_seg.cu:194-259), already converted to the types it uses.  The reference
@@ -104,7 +103,10 @@ struct Scalars {
   int fill_iters;
   int ninvalid;       // -1 pixels after the shift
   int tmp0, tmp1, tmp2;
-  unsigned int bar_count, bar_gen;   // grid barrier
+  int nhole;          // length of the hole list of the fill
+  // hole-fill loop state: current / next list length, previous count, iteration,
+  // finished flag, which buffer holds the current list (0 smseg, 1 hits)
+  int fl_n, fl_next, fl_prev, fl_iter, fl_done, fl_cur;
 };
 
 // One frame of a batch: its inputs, outputs, workspace and scalars.  Kernels take
@@ -144,11 +146,8 @@ struct Slot {
   float *fds, *ss;
   double* centers;
   unsigned long long *rbest, *ccbest;
+  int* bbox;               // [4*(cap+2)]: x0, x1, y0, y1 per superpixel (split BFS)
   Scalars* sc;
-  // offsets of this slot's work items in the flattened lists of a launch
-  int tile_base;           // 32x32 relaxation tiles
-  long long pix_base;      // pixels
-  long long q_base;        // quarter-lattice sites (ceil(W/2) x ceil(H/2))
 };
 
 // kb_scalars operations.
@@ -164,39 +163,6 @@ __device__ __forceinline__ long long fx_q(float v, int shift) {
 }
 __device__ __forceinline__ double fx_unq(long long q, int shift) {
   return ldexp((double)q, -shift);
-}
-
-// Bounded grid barrier for cooperative launches: every block calls it; returns
-// false (and sets status) when the wait exceeded the spin limit.
-__device__ __forceinline__ bool grid_barrier(Scalars* sc) {
-  __syncthreads();
-  __shared__ int ok;
-  if (threadIdx.x == 0) {
-    volatile unsigned int* gen = &sc->bar_gen;
-    unsigned int my = *gen;
-    __threadfence();
-    unsigned int arrived = atomicAdd(&sc->bar_count, 1u);
-    ok = 1;
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&sc->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&sc->bar_gen, 1u);
-    } else {
-      long long spins = 0;
-      while (*gen == my) {
-        if (++spins > kBarrierSpinLimit) {
-          atomicExch(&sc->status, STSPIX_ERR_BARRIER);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    if (*(volatile int*)&sc->status == STSPIX_ERR_BARRIER) ok = 0;
-  }
-  __syncthreads();
-  return ok != 0;
 }
 
 }  // namespace stspix

@@ -224,14 +224,14 @@ __global__ void kb_init_prior_mu(const Slot* __restrict__ slots) {
 }
 
 // ---------------------------------------------------------------------------
-// Sufficient statistics (sum_by_label, update_params.cu:89-130), R1.
-// Each thread owns a run of kRun pixels of one row, accumulates in registers while
-// the label stays the same and flushes one set of 64-bit atomics per label run;
-// position sums of a run are closed-form.
-constexpr int kRun = 8;
-
-__device__ __forceinline__ void flush_run(const SpDev& sp, int k, int y, int x0, int x1,
-                                          long long sr, long long sg, long long sb) {
+// Sufficient statistics (sum_by_label, update_params.cu:89-130), R1, as a
+// warp-aggregated scatter: a warp reads a 32-pixel row segment (coalesced labels and
+// colours), finds the runs of equal labels across its lanes, sums each run's
+// fixed-point colours with a warp prefix scan, and the run's last lane adds the
+// run into the label's sums with one set of 64-bit atomics (position sums of a run
+// are closed-form).  Integer sums, so the order of the additions does not matter.
+__device__ __forceinline__ void add_run_sums(const SpDev& sp, int k, int y, int x0, int x1,
+                                             long long sr, long long sg, long long sb) {
   long long n = x1 - x0 + 1;
   long long sx = (long long)(x0 + x1) * n / 2;
   long long a = x0 - 1, b = x1;
@@ -248,33 +248,58 @@ __device__ __forceinline__ void flush_run(const SpDev& sp, int k, int y, int x0,
   atomicAdd(acc + 7, (unsigned long long)(n * y * (long long)y));
 }
 
-__global__ void kb_accumulate(const Slot* __restrict__ slots) {
-  SLOT_Y;
-  const float* __restrict__ img = S.img;
-  const int* __restrict__ seg = S.seg;
-  const int H = S.H, W = S.W;
-  const SpDev& sp = S.sp;
-  const int cpr = (W + kRun - 1) / kRun;
-  int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= H * cpr) return;
-  int y = tid / cpr, xs = (tid % cpr) * kRun, xe = min(W, xs + kRun);
-  const int* srow = seg + (size_t)y * W;
-  const float* irow = img + (size_t)y * W * 3;
-  int cur = -1, x0 = xs;
-  long long sr = 0, sg = 0, sb = 0;
-  for (int x = xs; x < xe; x++) {
-    int k = srow[x];
-    if (k != cur) {
-      if (cur >= 0 && cur < sp.cap) flush_run(sp, cur, y, x0, x - 1, sr, sg, sb);
-      cur = k; x0 = x; sr = sg = sb = 0;
-    }
-    if (k >= 0) {
-      sr += fx_q(irow[3 * x], kFxAppShift);
-      sg += fx_q(irow[3 * x + 1], kFxAppShift);
-      sb += fx_q(irow[3 * x + 2], kFxAppShift);
-    }
+__device__ __forceinline__ long long warp_incl_scan(long long v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
   }
-  if (cur >= 0 && cur < sp.cap) flush_run(sp, cur, y, x0, xe - 1, sr, sg, sb);
+  return v;
+}
+
+// grid: (x blocks of 8 warps, slot); each warp walks 32-pixel row segments.
+__global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const int H = S.H, W = S.W;
+  const int spr = (W + 31) >> 5;                 // segments per row
+  const int nseg = H * spr;
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const SpDev& sp = S.sp;
+  const int cap = sp.cap;
+  for (int sgi = wid; sgi < nseg; sgi += nw) {
+    const int y = sgi / spr, xb = (sgi - y * spr) << 5;
+    const int x = xb + lane;
+    int k = -1;
+    long long q0 = 0, q1 = 0, q2 = 0;
+    if (x < W) {
+      const size_t g = (size_t)y * W + x;
+      k = S.seg[g];
+      if (k >= 0) {
+        const float* p = S.img + 3 * g;
+        q0 = fx_q(p[0], kFxAppShift);
+        q1 = fx_q(p[1], kFxAppShift);
+        q2 = fx_q(p[2], kFxAppShift);
+      }
+    }
+    const int kprev = __shfl_up_sync(0xffffffffu, k, 1);
+    const int knext = __shfl_down_sync(0xffffffffu, k, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != k);
+    const bool tail = lane == 31 || knext != k;
+    const long long p0 = warp_incl_scan(q0, lane);
+    const long long p1 = warp_incl_scan(q1, lane);
+    const long long p2 = warp_incl_scan(q2, lane);
+    // run start of this lane: the highest head at or below it
+    const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+    const int src = start > 0 ? start - 1 : 0;
+    long long b0 = __shfl_sync(0xffffffffu, p0, src);
+    long long b1 = __shfl_sync(0xffffffffu, p1, src);
+    long long b2 = __shfl_sync(0xffffffffu, p2, src);
+    if (start == 0) b0 = b1 = b2 = 0;
+    if (tail && k >= 0 && k < cap)
+      add_run_sums(sp, k, y, xb + start, x, p0 - b0, p1 - b1, p2 - b2);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -471,28 +496,6 @@ __constant__ unsigned char c_simple_lut[256] = {
     1, 0, 0, 0, 1, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 1,
     0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 1, 1, 0, 0, 1, 1, 0, 0};
 
-__device__ __forceinline__ int nbr_code(const int nb[8], int label, int* diff) {
-  int num = 0, d = 0;
-#pragma unroll
-  for (int i = 7; i >= 0; i--) {
-    num <<= 1;
-    bool b = (label == nb[i]) || (nb[i] == -1);
-    if (b) num++; else d++;
-  }
-  *diff = d;
-  return num;
-}
-__device__ __forceinline__ bool simple_point(const int nb[8], int label, int* diff) {
-  return c_simple_lut[nbr_code(nb, label, diff)] != 0;
-}
-// Same test against the table packed as 8 words in shared memory (divergent
-// constant-memory reads serialise across a warp).
-__device__ __forceinline__ bool simple_point_s(const unsigned* lut_bits, const int nb[8],
-                                               int label, int* diff) {
-  int num = nbr_code(nb, label, diff);
-  return (lut_bits[num >> 5] >> (num & 31)) & 1u;
-}
-
 __device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int y,
                                       const SweepRec& r, int k, float s2, float neigh_neq,
                                       float beta, float* best, int* best_label) {
@@ -513,30 +516,33 @@ __device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int 
 
 // ---------------------------------------------------------------------------
 // Fused sweep: border pass + the four parity phases of one sweep in one launch.
-// A block owns a 32x32 tile and stages labels of the tile plus a 4-pixel halo
+// A block owns a 64x32 tile and stages labels of the tile plus a 4-pixel halo
 // (phase k is evaluated on the tile grown by 3-k pixels, so every label a tile
 // pixel depends on is produced inside the block exactly as the four separate
 // launches produce it), the image and the border mask of the tile plus 3 pixels.
 // Labels are read from seg_in (labels at the sweep start) and the tile is
 // written to seg_out, so neighbouring blocks never see each other's updates.
-constexpr int kST = 32;               // tile side
+constexpr int kTX = kSweepTileW;      // tile width (64)
+constexpr int kTY = kSweepTileH;      // tile height (32)
 constexpr int kSH = 4;                // label halo
-constexpr int kSL = kST + 2 * kSH;    // 40: staged label side
-constexpr int kSI = kST + 2 * (kSH - 1);  // 38: staged image / border side
+constexpr int kLX = kTX + 2 * kSH;    // 72 x 40: staged labels
+constexpr int kLY = kTY + 2 * kSH;
+constexpr int kIX = kTX + 2 * (kSH - 1);  // 70 x 38: staged image / border region
+constexpr int kIY = kTY + 2 * (kSH - 1);
 
 __global__ void __launch_bounds__(256) kb_sweep(const Slot* __restrict__ slots, int parity,
                                                 float s2, float potts) {
   SLOT_Z;
   const int H = S.H, W = S.W;
-  if ((int)blockIdx.x * kST >= W || (int)blockIdx.y * kST >= H) return;
+  if ((int)blockIdx.x * kTX >= W || (int)blockIdx.y * kTY >= H) return;
   const float* __restrict__ img = S.img;
   const int* __restrict__ seg_in = parity ? S.seg_alt : S.seg;
   int* __restrict__ seg_out = parity ? S.seg : S.seg_alt;
   const SweepRec* __restrict__ rec = S.sp.rec;
   const int cap = S.sp.cap;
-  constexpr int kMaxList = (kST / 2 + kSH - 1) * (kST / 2 + kSH - 1);  // 19 x 19
-  __shared__ int L[kSL * kSL];
-  __shared__ float I[kSI * kSI * 3];
+  constexpr int kMaxList = (kTX / 2 + kSH - 1) * (kTY / 2 + kSH - 1);  // 35 x 19
+  __shared__ int L[kLX * kLY];
+  __shared__ float I[kIX * kIY * 3];
   __shared__ short list[4][kMaxList];   // border pixels of each parity phase
   __shared__ int cnt[4];
   __shared__ unsigned lut_bits[8];
@@ -546,64 +552,124 @@ __global__ void __launch_bounds__(256) kb_sweep(const Slot* __restrict__ slots, 
     lut_bits[threadIdx.x] = w;
   }
   if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
-  const int tx0 = blockIdx.x * kST, ty0 = blockIdx.y * kST;
+  const int tx0 = blockIdx.x * kTX, ty0 = blockIdx.y * kTY;
   const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;        // label region origin
   const int ix0 = tx0 - (kSH - 1), iy0 = ty0 - (kSH - 1);  // image region origin
-  for (int i = threadIdx.x; i < kSL * kSL; i += blockDim.x) {
-    int gx = rx0 + i % kSL, gy = ry0 + i / kSL;
-    L[i] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? seg_in[gy * W + gx] : -1;
+  // Staging: every thread issues all of its loads before the first store, so the
+  // block waits for one memory round trip, not one per element.
+  {
+    constexpr int kNL = (kLX * kLY + 255) / 256;  // 12 labels per thread
+    int lv[kNL];
+#pragma unroll
+    for (int j = 0; j < kNL; j++) {
+      const int i = threadIdx.x + 256 * j;
+      const int gx = rx0 + i % kLX, gy = ry0 + i / kLX;
+      lv[j] = (i < kLX * kLY && gx >= 0 && gx < W && gy >= 0 && gy < H) ? seg_in[gy * W + gx]
+                                                                          : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < kNL; j++) {
+      const int i = threadIdx.x + 256 * j;
+      if (i < kLX * kLY) L[i] = lv[j];
+    }
   }
-  for (int i = threadIdx.x; i < kSI * kSI; i += blockDim.x) {
-    int gx = ix0 + i % kSI, gy = iy0 + i / kSI;
-    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-      const float* p = img + 3 * ((size_t)gy * W + gx);
-      I[3 * i] = p[0]; I[3 * i + 1] = p[1]; I[3 * i + 2] = p[2];
+  {
+    // the image region as rows of 3 * kIX floats (same layout as I), in two
+    // batches of 16 loads per thread
+    constexpr int kRow = 3 * kIX;
+    constexpr int kNF = kIY * kRow;
+    constexpr int kNI = 16;
+#pragma unroll
+    for (int b0 = 0; b0 < kNF; b0 += 256 * kNI) {
+      float iv[kNI];
+#pragma unroll
+      for (int j = 0; j < kNI; j++) {
+        const int f = b0 + threadIdx.x + 256 * j;
+        const int r = f / kRow, c = f % kRow;
+        const int gy = iy0 + r, gc = 3 * ix0 + c;
+        iv[j] = (f < kNF && gy >= 0 && gy < H && gc >= 0 && gc < 3 * W)
+                    ? img[(size_t)gy * 3 * W + gc] : 0.f;
+      }
+#pragma unroll
+      for (int j = 0; j < kNI; j++) {
+        const int f = b0 + threadIdx.x + 256 * j;
+        if (f < kNF) I[f] = iv[j];
+      }
     }
   }
   __syncthreads();
   // Border mask at the sweep start (find_border_pixels, seg_utils.cu:164-195); the
   // border pixels of parity class k inside the tile grown by 3-k pixels are listed
   // for phase k, so each phase scores only its border pixels, densely.
-  for (int i = threadIdx.x; i < kSI * kSI; i += blockDim.x) {
-    int lx = i % kSI, ly = i / kSI;
-    int gx = ix0 + lx, gy = iy0 + ly;
-    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
-    bool b;
-    if (gy < 1 || gx < 1 || gy >= H - 1 || gx >= W - 1) {
-      b = true;
-    } else {
-      int p = (ly + 1) * kSL + (lx + 1);
-      int C = L[p];
-      b = (C != L[p - kSL] || C != L[p + kSL] || C != L[p + 1] || C != L[p - 1]);
+  // (appends are warp-aggregated: one shared atomic per warp and phase)
+  const int lane = threadIdx.x & 31;
+  for (int base = 0; base < kIX * kIY; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    int ph = -1;
+    if (i < kIX * kIY) {
+      const int lx = i % kIX, ly = i / kIX;
+      const int gx = ix0 + lx, gy = iy0 + ly;
+      if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+        bool b;
+        if (gy < 1 || gx < 1 || gy >= H - 1 || gx >= W - 1) {
+          b = true;
+        } else {
+          const int p = (ly + 1) * kLX + (lx + 1);
+          const int C = L[p];
+          b = (C != L[p - kLX] || C != L[p + kLX] || C != L[p + 1] || C != L[p - 1]);
+        }
+        const int c = ((gx & 1) << 1) | (gy & 1);
+        const int grow = 3 - c;
+        if (b && gx >= tx0 - grow && gx < tx0 + kTX + grow && gy >= ty0 - grow &&
+            gy < ty0 + kTY + grow)
+          ph = c;
+      }
     }
-    if (!b) continue;
-    int ph = ((gx & 1) << 1) | (gy & 1);
-    int grow = 3 - ph;
-    if (gx < tx0 - grow || gx >= tx0 + kST + grow || gy < ty0 - grow || gy >= ty0 + kST + grow)
-      continue;
-    int slot = atomicAdd(&cnt[ph], 1);
-    list[ph][slot] = (short)i;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const unsigned m = __ballot_sync(0xffffffffu, ph == c);
+      if (!m) continue;
+      const int leader = __ffs(m) - 1;
+      int at = 0;
+      if (lane == leader) at = atomicAdd(&cnt[c], __popc(m));
+      at = __shfl_sync(0xffffffffu, at, leader);
+      if (ph == c) list[c][at + __popc(m & ((1u << lane) - 1))] = (short)i;
+    }
   }
   __syncthreads();
   for (int ph = 0; ph < 4; ph++) {
     const int n = cnt[ph];
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
       int bi = list[ph][j];
-      int lxi = bi % kSI, lyi = bi / kSI;
+      int lxi = bi % kIX, lyi = bi / kIX;
       int gx = ix0 + lxi, gy = iy0 + lyi;
-      int p = (lyi + 1) * kSL + (lxi + 1);
+      int p = (lyi + 1) * kLX + (lxi + 1);
       int C = L[p];
       if (C < 0 || C >= cap) continue;
-      const int N = L[p - kSL], S = L[p + kSL], Wl = L[p - 1], E = L[p + 1];
-      const int NW = L[p - kSL - 1], NE = L[p - kSL + 1], SW = L[p + kSL - 1],
-                SE = L[p + kSL + 1];
+      const int N = L[p - kLX], S = L[p + kLX], Wl = L[p - 1], E = L[p + 1];
+      const int NW = L[p - kLX - 1], NE = L[p - kLX + 1], SW = L[p + kLX - 1],
+                SE = L[p + kLX + 1];
+      // simple-point codes of the four candidates: bit i set when neighbour i
+      // (NW,N,NE,W,E,SW,S,SE) carries the candidate or lies outside the image;
+      // equal candidates share one code; differing neighbours = 8 - popcount
       const int nb[8] = {NW, N, NE, Wl, E, SW, S, SE};
-      int dN, dW, dS, dE;
-      bool vN = simple_point_s(lut_bits, nb, N, &dN);
-      bool vW = simple_point_s(lut_bits, nb, Wl, &dW);
-      bool vS = simple_point_s(lut_bits, nb, S, &dS);
-      bool vE = simple_point_s(lut_bits, nb, E, &dE);
-      if (!vN || !vW || !vS || !vE) continue;
+      unsigned m1 = 0;
+#pragma unroll
+      for (int q = 0; q < 8; q++) m1 |= (unsigned)(nb[q] == -1) << q;
+      auto code = [&](int v) {
+        unsigned c = m1;
+#pragma unroll
+        for (int q = 0; q < 8; q++) c |= (unsigned)(nb[q] == v) << q;
+        return c;
+      };
+      const unsigned cN = code(N);
+      const unsigned cW = (Wl == N) ? cN : code(Wl);
+      const unsigned cS = (S == N) ? cN : (S == Wl) ? cW : code(S);
+      const unsigned cE = (E == N) ? cN : (E == Wl) ? cW : (E == S) ? cS : code(E);
+      auto simple = [&](unsigned c) { return (lut_bits[c >> 5] >> (c & 31)) & 1u; };
+      if (!simple(cN) || !simple(cW) || !simple(cS) || !simple(cE)) continue;
+      const int dN = 8 - __popc(cN), dW = 8 - __popc(cW), dS = 8 - __popc(cS),
+                dE = 8 - __popc(cE);
       if (N >= cap || S >= cap || Wl >= cap || E >= cap) continue;
       const float* pix = &I[3 * bi];
       float best = -9999.f;
@@ -624,9 +690,9 @@ __global__ void __launch_bounds__(256) kb_sweep(const Slot* __restrict__ slots, 
     }
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < kST * kST; i += blockDim.x) {
-    int gx = tx0 + i % kST, gy = ty0 + i / kST;
-    if (gx < W && gy < H) seg_out[gy * W + gx] = L[(gy - ry0) * kSL + (gx - rx0)];
+  for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x) {
+    int gx = tx0 + i % kTX, gy = ty0 + i / kTX;
+    if (gx < W && gy < H) seg_out[gy * W + gx] = L[(gy - ry0) * kLX + (gx - rx0)];
   }
 }
 

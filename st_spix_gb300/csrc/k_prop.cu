@@ -30,7 +30,7 @@ __global__ void kb_prop_clear(const Slot* __restrict__ slots) {
     S.best[i] = ~0ull;
     S.d2[i] = 0;
   }
-  if (i == 0) S.sc->ninvalid = 0;
+  if (i == 0) { S.sc->ninvalid = 0; S.sc->nhole = 0; }
 }
 
 __global__ void kb_flow_pool(const Slot* __restrict__ slots) {
@@ -111,163 +111,273 @@ __global__ void kb_shift(const Slot* __restrict__ slots) {
 }
 
 // decode_kernel (shift_labels.cu:128-164) + copy to `filled` + hole count.
+// Append pixel t to the slot's hole list (smseg, count sc->nhole) when `hole`;
+// warp-aggregated.  The list order depends on scheduling; the fill's result does
+// not (a parity phase updates pixels that are never 4-neighbours of each other).
+// With count_invalid the holes are also counted into sc->ninvalid (the hole count
+// after the shift, which the iteration ladder reads).
+__device__ __forceinline__ void append_hole(const Slot& S, int t, bool hole, bool count_invalid) {
+  const unsigned act = __activemask();
+  const unsigned m = __ballot_sync(act, hole);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) {
+    base = atomicAdd(&S.sc->nhole, __popc(m));
+    if (count_invalid) atomicAdd(&S.sc->ninvalid, __popc(m));
+  }
+  base = __shfl_sync(act, base, leader);
+  if (hole) S.smseg[base + __popc(m & ((1u << lane) - 1))] = t;
+}
+
 __global__ void kb_shift_decode(const Slot* __restrict__ slots) {
   SLOT_Y;
   const int* __restrict__ hits = S.hits;
   const unsigned long long* __restrict__ best = S.best;
   int* __restrict__ shifted = S.shifted;
   int* __restrict__ filled = S.seg;
-  Scalars* sc = S.sc;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
   int v = hits[t] > 0 ? (int)(unsigned int)best[t] : -1;
   shifted[t] = v;
   filled[t] = v;
-  unsigned mask = __ballot_sync(__activemask(), v < 0);
-  if ((threadIdx.x & 31) == (__ffs(__activemask()) - 1) && mask)
-    atomicAdd(&sc->ninvalid, __popc(mask));
+  append_hole(S, t, v < 0, true);
 }
 
 // Per-label pixel counts (get_spix_sizes, seg_utils.cu:56-75).
-// which 0: counts after the shift (cs), 1: after the fill (cf).
+// which 0: counts after the shift (cs), 1: after the fill (cf).  One 16-pixel
+// row run per thread; runs of equal labels are counted before the atomic.
 __global__ void kb_count_labels(const Slot* __restrict__ slots, int which) {
   SLOT_Y;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int k = S.seg[t];
-  if (k >= 0 && k < S.n_prev) atomicAdd(&(which ? S.cf : S.cs)[k], 1);
-}
-
-// ---------------------------------------------------------------------------
-// Hole filling (fill_missing.cu:35-130, update_missing_seg_nn :288-441,
-// find_border_along_missing :617-647) as one cooperative kernel: per iteration a
-// border/count pass and four parity phases, separated by bounded grid barriers.
-// Work items of the hole fill: pixels (pass 1) and quarter-lattice sites (the four
-// parity phases) of all slots of the launch, flattened in slot order
-// (slots[i].pix_base / slots[i].q_base are the prefix sums).
-__device__ __forceinline__ int advance_slot(const Slot* __restrict__ slots, int B, int s,
-                                            long long g, bool quarter) {
-  while (s + 1 < B && (quarter ? slots[s + 1].q_base : slots[s + 1].pix_base) <= g) s++;
-  return s;
-}
-
-// Hole filling (fill_missing.cu:35-130, update_missing_seg_nn :288-441,
-// find_border_along_missing :617-647) of every slot as one cooperative kernel: per
-// iteration a border/count pass and four parity phases, separated by bounded grid
-// barriers.  counts[it * B + i] is slot i's hole count at iteration it (row it + 1 is
-// cleared by block 0 during iteration it; the caller clears row 0).  done[i] = it + 1
-// records that slot i finished after iteration it (no holes, or no progress); the
-// slot still runs the phases of that iteration, as the reference does.
-__global__ void __launch_bounds__(256) kb_fill(const Slot* __restrict__ slots, int B,
-                                               long long total_pix, long long total_q,
-                                               Scalars* ctl, int* counts, int* done,
-                                               int break_iter) {
-  const long long nthr = (long long)gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
-  for (int iter = 0; iter < break_iter; iter++) {
-    if (blockIdx.x == 0 && iter + 1 < break_iter)
-      for (int i = threadIdx.x; i < B; i += blockDim.x) counts[(iter + 1) * B + i] = 0;
-    // pass 1: border of the holes and hole counts (warp-uniform loop)
-    int si = 0;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < total_pix; base += nthr) {
-      const long long g = base + threadIdx.x;
-      int key = -1;
-      if (g < total_pix) {
-        si = advance_slot(slots, B, si, g, false);
-        const int dn = __ldcg(&done[si]);
-        if (dn == 0 || dn > iter) {
-          const Slot& S = slots[si];
-          const int W = S.W, H = S.H;
-          const int idx = (int)(g - S.pix_base);
-          const int* seg = S.seg;
-          int x = idx % W, y = idx / W;
-          int N = -1, So = -1, E = -1, Wl = -1;
-          if (y > 0) N = __ldcg(seg + idx - W);
-          if (x > 0) Wl = __ldcg(seg + idx - 1);
-          if (y < H - 1) So = __ldcg(seg + idx + W);
-          if (x < W - 1) E = __ldcg(seg + idx + 1);
-          S.border[idx] = (N >= 0 || Wl >= 0 || So >= 0 || E >= 0) ? 1 : 0;
-          if (__ldcg(seg + idx) < 0) key = si;
-        }
-      }
-      const unsigned m = __match_any_sync(0xffffffffu, key);
-      if (key >= 0 && lane == __ffs(m) - 1) atomicAdd(&counts[iter * B + key], __popc(m));
+  constexpr int R = 16;
+  const int W = S.W, n = S.n_prev;
+  const int cpr = (W + R - 1) / R;
+  int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= S.H * cpr) return;
+  int y = tid / cpr, xs = (tid % cpr) * R, xe = min(W, xs + R);
+  const int* lrow = S.seg + (size_t)y * W;
+  int* cnt = which ? S.cf : S.cs;
+  int cur = -1, c = 0;
+  for (int x = xs; x <= xe; x++) {
+    int k = x < xe ? lrow[x] : -2;
+    if (k != cur) {
+      if (cur >= 0 && cur < n) atomicAdd(&cnt[cur], c);
+      cur = k;
+      c = 0;
     }
-    if (!grid_barrier(ctl)) return;
-    // per-slot bookkeeping by block 0 (read by all after the phase barriers)
-    if (blockIdx.x == 0)
-      for (int i = threadIdx.x; i < B; i += blockDim.x) {
-        const int dn = __ldcg(&done[i]);
-        if (dn != 0 && dn <= iter) continue;
-        const int num_neg = __ldcg(&counts[iter * B + i]);
-        const int prev_neg = iter > 0 ? __ldcg(&counts[(iter - 1) * B + i])
-                                      : 1410065408;  // (int)10000000000 as the reference truncates it
-        Scalars* sc = slots[i].sc;
-        sc->fill_iters += 1;
-        if (num_neg == prev_neg) {
-          atomicExch(&sc->status, STSPIX_ERR_NOPROGRESS);
-          done[i] = iter + 1;
-        } else if (num_neg <= 0) {
-          done[i] = iter + 1;
-        }
-      }
-    for (int ph = 0; ph < 4; ph++) {
-      const int xm = ph >> 1, ym = ph & 1;
-      int qi = 0;
-      for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total_q; g += nthr) {
-        qi = advance_slot(slots, B, qi, g, true);
-        const int dn = __ldcg(&done[qi]);
-        if (dn != 0 && dn <= iter) continue;
-        const Slot& S = slots[qi];
-        const int W = S.W, H = S.H;
-        const int hw0 = (W + 1) >> 1;
-        const int i = (int)(g - S.q_base);
-        const int x = 2 * (i % hw0) + xm, y = 2 * (i / hw0) + ym;
-        if (x >= W || y >= H) continue;
-        int* seg = S.seg;
-        const int idx = y * W + x;
-        if (!__ldcg(S.border + idx) || __ldcg(seg + idx) != -1) continue;
-        int N = -1, So = -1, E = -1, Wl = -1;
-        if (x > 0) Wl = __ldcg(seg + idx - 1);
-        if (y > 0) N = __ldcg(seg + idx - W);
-        if (x < W - 1) E = __ldcg(seg + idx + 1);
-        if (y < H - 1) So = __ldcg(seg + idx + W);
-        const double* centers = S.centers;
-        float bx = -999999;
-        int bl = -1;
-        auto consider = [&](int lab) {
-          const double* cp = centers + 2 * (size_t)lab;
-          float dx = (1.0f * x - cp[0]) / (1.0f * W);
-          float dy = (1.0f * y - cp[1]) / (1.0f * H);
-          float sim = -dx * dx - dy * dy;
-          if (sim > bx) { bx = sim; bl = lab; }
-        };
-        if (N >= 0) consider(N);
-        if (So >= 0 && So != N) consider(So);
-        if (Wl >= 0 && Wl != So && Wl != N) consider(Wl);
-        if (E >= 0 && E != Wl && E != So && E != N) consider(E);
-        __stcg(seg + idx, bl);
-      }
-      if (!grid_barrier(ctl)) return;
-    }
-    // every block sees the same done[] here: stop when all slots finished
-    int all = 1;
-    for (int i = threadIdx.x; i < B; i += blockDim.x) {
-      const int dn = *(volatile int*)&done[i];
-      if (dn == 0 || dn > iter + 1) all = 0;
-    }
-    if (__syncthreads_and(all)) return;
+    c++;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Disconnected regions (split_disconnected.cu:33-96): roots from the cooperative
-// relaxation (mode 1), sizes, largest region per label (R6), invalidate the rest.
+// Hole filling (fill_missing.cu:35-130, update_missing_seg_nn :288-441,
+// find_border_along_missing :617-647) over the list of hole pixels instead of the
+// frame.  One iteration = kb_fill_border, kb_fill_phase x 4, kb_fill_compact,
+// kb_fill_step; the host runs it as the body of a CUDA-graph WHILE node whose
+// condition kb_fill_step sets, so the loop needs neither host round trips nor grid
+// barriers.  Per iteration: the hole count (the list length), the border flag of
+// every hole (a 4-neighbour labelled at the start of the iteration), four parity
+// phases in which a bordered hole takes the label of the neighbour whose centre is
+// nearest, then the holes left are compacted into the other list buffer.  Stop
+// rules as the reference: a count equal to the previous one is an error (it exits),
+// no holes left ends the loop, both after the iteration's phases; break_iter caps it.
+__device__ __forceinline__ const int* fill_list(const Slot& S) {
+  return S.sc->fl_cur ? S.hits : S.smseg;
+}
+
+__global__ void kb_fill_begin(const Slot* __restrict__ slots, int B) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  Scalars* sc = slots[i].sc;
+  sc->fl_n = sc->nhole;
+  sc->fl_next = 0;
+  sc->fl_prev = 1410065408;  // (int)10000000000 as the reference truncates it
+  sc->fl_iter = 0;
+  sc->fl_done = 0;
+  sc->fl_cur = 0;
+}
+
+__global__ void kb_fill_border(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  const Scalars* sc = S.sc;
+  if (sc->fl_done) return;
+  const int n = sc->fl_n, W = S.W, H = S.H;
+  const int* la = fill_list(S);
+  const int* seg = S.seg;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int idx = la[j];
+    const int x = idx % W, y = idx / W;
+    const bool b = (y > 0 && seg[idx - W] >= 0) || (x > 0 && seg[idx - 1] >= 0) ||
+                   (y < H - 1 && seg[idx + W] >= 0) || (x < W - 1 && seg[idx + 1] >= 0);
+    S.border[j] = b ? 1 : 0;
+  }
+}
+
+__global__ void kb_fill_phase(const Slot* __restrict__ slots, int ph) {
+  SLOT_Y;
+  const Scalars* sc = S.sc;
+  if (sc->fl_done) return;
+  const int n = sc->fl_n, W = S.W, H = S.H;
+  const int xm = ph >> 1, ym = ph & 1;
+  const int* la = fill_list(S);
+  int* seg = S.seg;
+  const double* centers = S.centers;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int idx = la[j];
+    const int x = idx % W, y = idx / W;
+    if ((x & 1) != xm || (y & 1) != ym) continue;
+    if (!S.border[j] || seg[idx] != -1) continue;
+    int N = -1, So = -1, E = -1, Wl = -1;
+    if (x > 0) Wl = seg[idx - 1];
+    if (y > 0) N = seg[idx - W];
+    if (x < W - 1) E = seg[idx + 1];
+    if (y < H - 1) So = seg[idx + W];
+    float bx = -999999;
+    int bl = -1;
+    auto consider = [&](int lab) {
+      const double* cp = centers + 2 * (size_t)lab;
+      float dx = (1.0f * x - cp[0]) / (1.0f * W);
+      float dy = (1.0f * y - cp[1]) / (1.0f * H);
+      float sim = -dx * dx - dy * dy;
+      if (sim > bx) { bx = sim; bl = lab; }
+    };
+    if (N >= 0) consider(N);
+    if (So >= 0 && So != N) consider(So);
+    if (Wl >= 0 && Wl != So && Wl != N) consider(Wl);
+    if (E >= 0 && E != Wl && E != So && E != N) consider(E);
+    seg[idx] = bl;
+  }
+}
+
+// Holes still unfilled go to the other list buffer (warp-aggregated append; the
+// order does not matter, see append_hole).
+__global__ void kb_fill_compact(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  Scalars* sc = S.sc;
+  if (sc->fl_done) return;
+  const int n = sc->fl_n;
+  const int* la = fill_list(S);
+  int* lb = sc->fl_cur ? S.smseg : S.hits;
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int j = base + threadIdx.x;
+    int idx = -1;
+    if (j < n) idx = la[j];
+    const bool keep = j < n && S.seg[idx] < 0;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (!m) continue;
+    const int leader = __ffs(m) - 1;
+    int pos = 0;
+    if (lane == leader) pos = atomicAdd(&sc->fl_next, __popc(m));
+    pos = __shfl_sync(0xffffffffu, pos, leader);
+    if (keep) lb[pos + __popc(m & ((1u << lane) - 1))] = idx;
+  }
+}
+
+// End of an iteration, one thread per slot; thread 0 sets the loop condition
+// (any slot still filling).  *body_iters counts the iterations run.
+__global__ void kb_fill_step(const Slot* __restrict__ slots, int B,
+                             cudaGraphConditionalHandle cond, int break_iter, int* body_iters) {
+  int active = 0;
+  for (int i = threadIdx.x; i < B; i += blockDim.x) {
+    Scalars* sc = slots[i].sc;
+    if (sc->fl_done) continue;
+    const int num_neg = sc->fl_n;
+    sc->fill_iters += 1;
+    sc->fl_iter += 1;
+    if (num_neg == sc->fl_prev) {
+      sc->status = STSPIX_ERR_NOPROGRESS;
+      sc->fl_done = 1;
+    } else {
+      sc->fl_prev = num_neg;
+      if (num_neg <= 0 || sc->fl_iter >= break_iter) sc->fl_done = 1;
+    }
+    sc->fl_n = sc->fl_next;
+    sc->fl_next = 0;
+    sc->fl_cur ^= 1;
+    if (!sc->fl_done) active = 1;
+  }
+  active = __syncthreads_or(active);
+  if (threadIdx.x == 0) {
+    *body_iters += 1;
+    cudaGraphSetConditional(cond, active ? 1u : 0u);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Disconnected regions (split_disconnected.cu:33-96): component roots by
+// union-find, sizes, largest region per label (R6), invalidate the rest.
 __global__ void kb_cc_init(const Slot* __restrict__ slots) {
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
   S.d1[t] = S.seg[t] >= 0 ? t : -1;
+  if (t == 0) S.sc->nhole = 0;
+}
+
+// Connected components (8-connected, same label) by union-find with min-index
+// hooking: every tree's root is the smallest pixel index of its component, the
+// fixed point of find_spix_min (split_disconnected.cu:458-498).  Parents only
+// decrease, so the walks below end; they are capped all the same.
+constexpr int kUfLimit = 1 << 26;
+// Root of x with path halving (atomicMin keeps parents decreasing under races).
+__device__ __forceinline__ int uf_find(int* parent, int x) {
+  for (int i = 0; i < kUfLimit; i++) {
+    const int p = *(volatile int*)&parent[x];
+    if (p == x) return x;
+    const int g = *(volatile int*)&parent[p];
+    if (g == p) return p;
+    atomicMin(&parent[x], g);
+    x = g;
+  }
+  return -1;
+}
+__device__ __forceinline__ bool uf_unite(int* parent, int a, int b) {
+  for (int i = 0; i < kUfLimit; i++) {
+    a = uf_find(parent, a);
+    b = uf_find(parent, b);
+    if (a < 0 || b < 0) return false;
+    if (a == b) return true;
+    if (a < b) { int t = a; a = b; b = t; }
+    const int old = atomicMin(&parent[a], b);
+    if (old == a) return true;
+    a = old;
+  }
+  return false;
+}
+
+// Unions with the earlier 8-neighbours; a diagonal one is skipped when a 4-path
+// through W or N already joins it (W-NW and N-NW, N-NE are united at those pixels).
+__global__ void kb_cc_hook(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.npix) return;
+  const int W = S.W;
+  const int* seg = S.seg;
+  const int L = seg[t];
+  if (L < 0) return;
+  const int x = t % W, y = t / W;
+  bool ok = true;
+  const bool w = x > 0 && seg[t - 1] == L;
+  if (w) ok &= uf_unite(S.d1, t, t - 1);
+  if (y > 0) {
+    if (seg[t - W] == L) {
+      ok &= uf_unite(S.d1, t, t - W);
+    } else {
+      if (!w && x > 0 && seg[t - W - 1] == L) ok &= uf_unite(S.d1, t, t - W - 1);
+      if (x < W - 1 && seg[t - W + 1] == L) ok &= uf_unite(S.d1, t, t - W + 1);
+    }
+  }
+  if (!ok) atomicExch(&S.sc->status, STSPIX_ERR_ITER_LIMIT);
+}
+
+__global__ void kb_cc_compress(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.npix) return;
+  if (S.d1[t] >= 0) S.d1[t] = uf_find(S.d1, t);
 }
 
 __global__ void kb_cc_size(const Slot* __restrict__ slots) {
@@ -306,6 +416,14 @@ __global__ void kb_cc_invalidate(const Slot* __restrict__ slots) {
   if (L < 0 || L >= nlab) return;
   unsigned int win = 0xffffffffu - (unsigned int)(best[L] & 0xffffffffull);
   if ((unsigned int)root[t] != win) seg[t] = -1;
+}
+
+// Hole list of the second fill: every -1 pixel after the invalidation.
+__global__ void kb_list_holes(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.npix) return;
+  append_hole(S, t, S.seg[t] < 0, false);
 }
 
 // invalid_counts / prior_counts update (shift_and_fill.cu:300-330).

@@ -1,7 +1,7 @@
 // GB300 kernels of the split / merge proposals and their Hastings tests
 // (gauenk/st_spix st_spix/csrc/bist/split_merge.cu, split_merge_orig.cu,
-// split_merge_prop.cu), plus the bounded cooperative relaxation loops that replace
-// the reference's host-driven BFS (one launch + one device-to-host copy per step).
+// split_merge_prop.cu), plus a block-per-superpixel BFS that replaces the
+// reference's host-driven BFS (one launch + one device-to-host copy per step).
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -10,9 +10,6 @@
 
 namespace stspix {
 
-constexpr int kTile = 32;
-constexpr int kHalo = kTile + 2;
-constexpr int kInf = 0x3fffffff;
 
 // ---------------------------------------------------------------------------
 // Split seeds (init_split, split_merge.cu:803-844) for both directions.
@@ -25,7 +22,10 @@ __global__ void kb_split_seed(const Slot* __restrict__ slots, int dir_bass, int 
   int* __restrict__ d1 = S.d1;
   int* __restrict__ d2 = S.d2;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= sp.cap || !S.sc->tmp0 /*split_on*/ || !sp.valid[k]) return;
+  if (k >= sp.cap) return;
+  int* bb = S.bbox + 4 * (size_t)k;
+  bb[0] = INT32_MAX; bb[1] = -1; bb[2] = INT32_MAX; bb[3] = -1;
+  if (!S.sc->tmp0 /*split_on*/ || !sp.valid[k]) return;
   for (int s = 0; s < 2; s++) {
     int dir = s == 0 ? direction : -direction;
     int x, y;
@@ -59,159 +59,228 @@ __global__ void kb_split_begin(const Slot* __restrict__ slots, int B) {
   // split runs unless max_spix > nspix_buffer / 2 (split_merge_orig.cu:215)
   sc->tmp0 = sc->max_spix > sc->nbuf_logical / 2 ? 0 : 1;
   sc->tmp1 = sc->max_spix + 1;  // offset of the second half
+  sc->tmp2 = 0;                 // superpixels whose box is too large for one warp
 }
 
 // ---------------------------------------------------------------------------
-// Relaxation to a fixed point inside 32x32 tiles with a one-pixel halo, repeated
-// over the grid until no tile changes (cooperative launch, bounded barrier).
-// mode 0: BFS distances of two seed fields (4-connected, same label, +1 per step;
-//         -1 = unreached) -- the fixed point equals the reference's layered BFS
-//         (calc_split_candidate, split_merge.cu:758-800).
-// mode 1: connected-component roots (8-connected, same label, min pixel index) --
-//         the fixed point of find_spix_min (split_disconnected.cu:458-498).
-// Slot of flattened work item t (slots[i].base ascending, slots[0].base == 0).
-__device__ __forceinline__ int slot_of(const Slot* __restrict__ slots, int B, long long t) {
-  int lo = 0, hi = B - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (slots[mid].tile_base <= t) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
-// The tiles of every slot of the launch form one list (slot i owns tiles
-// [tile_base_i, tile_base_i + tiles_i)); flags[r * (B + 1) + i] records that slot i
-// changed in round r, flags[r * (B + 1) + B] that any slot did.  A slot that did not
-// change in round r is at its fixed point (its tiles read final halos) and is
-// skipped from round r + 1 on.  Row r + 1 is cleared by block 0 during round r; the
-// caller clears row 0.
-template <int MODE>
-__device__ __forceinline__ void relax_coop(const Slot* __restrict__ slots, int B,
-                                           int total_tiles, Scalars* ctl, int* flags,
-                                           int max_rounds) {
-  __shared__ int sl[kHalo * kHalo];
-  __shared__ int s1[kHalo * kHalo];
-  __shared__ int s2[MODE == 0 ? kHalo * kHalo : 1];
-  __shared__ int any;
-  const int row = B + 1;
-  for (int round = 0; round < max_rounds; round++) {
-    if (blockIdx.x == 0 && round + 1 < max_rounds)
-      for (int i = threadIdx.x; i < row; i += blockDim.x) flags[(round + 1) * row + i] = 0;
-    int cur_slot = -1, my_changed = 0;
-    for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-      const int si = slot_of(slots, B, t);
-      if (si != cur_slot) {
-        if (my_changed) { atomicOr(&flags[round * row + cur_slot], 1); atomicOr(&flags[round * row + B], 1); }
-        cur_slot = si;
-        my_changed = 0;
+// Bounding box of every superpixel (for the split BFS), one 16-pixel row run per
+// thread.
+__global__ void kb_bbox(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.sc->tmp0) return;
+  constexpr int R = 16;
+  const int W = S.W, cap = S.cap;
+  const int cpr = (W + R - 1) / R;
+  int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= S.H * cpr) return;
+  int y = tid / cpr, xs = (tid % cpr) * R, xe = min(W, xs + R);
+  const int* lrow = S.seg + (size_t)y * W;
+  int cur = -1, x0 = xs;
+  for (int x = xs; x <= xe; x++) {
+    int k = x < xe ? lrow[x] : -2;
+    if (k != cur) {
+      if (cur >= 0 && cur < cap) {
+        int* bb = S.bbox + 4 * (size_t)cur;
+        atomicMin(&bb[0], x0);
+        atomicMax(&bb[1], x - 1);
+        atomicMin(&bb[2], y);
+        atomicMax(&bb[3], y);
       }
-      if (round > 0 && *(volatile int*)&flags[(round - 1) * row + si] == 0) continue;
-      const Slot& S = slots[si];
-      const int H = S.H, W = S.W;
-      const int* __restrict__ seg = S.seg;
-      int* f1 = S.d1;
-      int* f2 = S.d2;
-      const int tiles_x = (W + kTile - 1) / kTile;
-      const int tl = t - S.tile_base;
-      const int tx0 = (tl % tiles_x) * kTile, ty0 = (tl / tiles_x) * kTile;
-      for (int i = threadIdx.x; i < kHalo * kHalo; i += blockDim.x) {
-        int gx = tx0 + i % kHalo - 1, gy = ty0 + i / kHalo - 1;
-        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-          int g = gy * W + gx;
-          sl[i] = seg[g];
-          // f1/f2 are written by other blocks of this launch: read past L1.
-          if (MODE == 0) {
-            int a = __ldcg(f1 + g), b = __ldcg(f2 + g);
-            s1[i] = a < 0 ? kInf : a;
-            s2[i] = b < 0 ? kInf : b;
-          } else {
-            int a = __ldcg(f1 + g);
-            s1[i] = a < 0 ? kInf : a;
-          }
-        } else {
-          sl[i] = INT32_MIN;
-          s1[i] = kInf;
-          if (MODE == 0) s2[i] = kInf;
-        }
-      }
-      int local_iter = 0;
-      while (true) {
-        __syncthreads();
-        if (threadIdx.x == 0) any = 0;
-        __syncthreads();
-        int ch = 0;
-        for (int i = threadIdx.x; i < kTile * kTile; i += blockDim.x) {
-          int lx = i % kTile + 1, ly = i / kTile + 1;
-          if (tx0 + lx - 1 >= W || ty0 + ly - 1 >= H) continue;
-          int p = ly * kHalo + lx;
-          int L = sl[p];
-          if (MODE == 0) {
-            int a = s1[p], b = s2[p];
-            const int q4[4] = {p - kHalo, p - 1, p + kHalo, p + 1};
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-              int q = q4[j];
-              if (sl[q] != L) continue;
-              int qa = s1[q], qb = s2[q];
-              if (qa < kInf && qa + 1 < a) a = qa + 1;
-              if (qb < kInf && qb + 1 < b) b = qb + 1;
-            }
-            if (a < s1[p]) { s1[p] = a; ch = 1; }
-            if (b < s2[p]) { s2[p] = b; ch = 1; }
-          } else {
-            if (L < 0) continue;
-            int a = s1[p];
-#pragma unroll
-            for (int dy = -1; dy <= 1; dy++)
-#pragma unroll
-              for (int dx = -1; dx <= 1; dx++) {
-                int q = p + dy * kHalo + dx;
-                if (sl[q] == L && s1[q] < a) a = s1[q];
-              }
-            if (a < s1[p]) { s1[p] = a; ch = 1; }
-          }
-        }
-        if (ch) any = 1;
-        __syncthreads();
-        if (!any || ++local_iter > 4 * kTile * kTile) break;
-      }
-      // write back changed interior values
-      for (int i = threadIdx.x; i < kTile * kTile; i += blockDim.x) {
-        int lx = i % kTile + 1, ly = i / kTile + 1;
-        int gx = tx0 + lx - 1, gy = ty0 + ly - 1;
-        if (gx >= W || gy >= H) continue;
-        int p = ly * kHalo + lx, g = gy * W + gx;
-        if (MODE == 0) {
-          int a = s1[p] >= kInf ? -1 : s1[p];
-          int b = s2[p] >= kInf ? -1 : s2[p];
-          if (a != __ldcg(f1 + g)) { __stcg(f1 + g, a); my_changed = 1; }
-          if (b != __ldcg(f2 + g)) { __stcg(f2 + g, b); my_changed = 1; }
-        } else {
-          int a = s1[p] >= kInf ? -1 : s1[p];
-          if (a != __ldcg(f1 + g)) { __stcg(f1 + g, a); my_changed = 1; }
-        }
-      }
-      __syncthreads();
+      cur = k;
+      x0 = x;
     }
-    if (my_changed) { atomicOr(&flags[round * row + cur_slot], 1); atomicOr(&flags[round * row + B], 1); }
-    if (!grid_barrier(ctl)) return;
-    if (*(volatile int*)&flags[round * row + B] == 0) return;
   }
-  // round cap reached: flag the slots still changing
-  if (blockIdx.x == 0)
-    for (int i = threadIdx.x; i < B; i += blockDim.x)
-      if (flags[(max_rounds - 1) * row + i]) atomicExch(&slots[i].sc->status, STSPIX_ERR_ITER_LIMIT);
 }
 
-__global__ void __launch_bounds__(256) kb_relax_bfs(const Slot* __restrict__ slots, int B,
-                                                    int total_tiles, Scalars* ctl, int* flags,
-                                                    int max_rounds) {
-  relax_coop<0>(slots, B, total_tiles, ctl, flags, max_rounds);
+// Split BFS (calc_split_candidate, split_merge.cu:758-800): distances from the two
+// seeds of every superpixel, 4-connected within its label, seed = 1, unreached =
+// -1 -- the reference's layered BFS, run per superpixel over its bounding box as a
+// bit-parallel BFS: the box is held as rows of 64-bit words (label mask M, frontier
+// F and visited V of each field), and one layer is
+//     N = (F << 1 | F >> 1 | F[row-1] | F[row+1]) & M & ~V
+// per word, so a layer costs O(rows x words) however the superpixel is shaped;
+// each newly reached pixel gets distance L + 1 written once.
+// kb_split_bfs runs one warp per superpixel (boxes up to 128 x 128 pixels) and
+// lists larger boxes for kb_split_bfs_big (one block each, boxes up to 512 x 512
+// pixels; beyond that the same layers run on the global distances).
+constexpr int kWarpRows = 128, kWarpWpr = 2;    // warp: 128 rows x 2 words
+constexpr int kBigRows = 512, kBigWpr = 8;      // block: 512 rows x 8 words
+
+template <int NT>
+__device__ __forceinline__ void group_sync() {
+  if (NT == 32) __syncwarp(); else __syncthreads();
 }
-__global__ void __launch_bounds__(256) kb_relax_cc(const Slot* __restrict__ slots, int B,
-                                                   int total_tiles, Scalars* ctl, int* flags,
-                                                   int max_rounds) {
-  relax_coop<1>(slots, B, total_tiles, ctl, flags, max_rounds);
+template <int NT>
+__device__ __forceinline__ int group_any(int v) {
+  if (NT == 32) { __syncwarp(); return __any_sync(0xffffffffu, v); }
+  return __syncthreads_or(v);
+}
+
+// t: thread index in the group of NT threads (NT a multiple of 32; whole warps).
+// Arrays hold bh * wpr words each.
+template <int NT, int ITEMS>
+__device__ void bfs_bits(int t, int k, int x0, int y0, int bw, int bh, int W,
+                         const int* __restrict__ seg, int* d1, int* d2,
+                         unsigned long long* M, unsigned long long* F1, unsigned long long* V1,
+                         unsigned long long* F2, unsigned long long* V2) {
+  const int wpr = (bw + 63) >> 6;
+  const int nwords = bh * wpr;
+  const int lane = t & 31;
+  // masks and seeds: one warp-wide ballot per 32-pixel chunk of a row
+  const int cpr = (bw + 31) >> 5;
+  unsigned* M32 = (unsigned*)M;
+  unsigned* F132 = (unsigned*)F1;
+  unsigned* F232 = (unsigned*)F2;
+  for (int c = t >> 5; c < bh * cpr; c += NT >> 5) {
+    const int r = c / cpr, cx = c % cpr;
+    const int xi = cx * 32 + lane;
+    bool m = false, s1 = false, s2 = false;
+    if (xi < bw) {
+      const int g = (y0 + r) * W + x0 + xi;
+      m = seg[g] == k;
+      if (m) { s1 = d1[g] == 1; s2 = d2[g] == 1; }
+    }
+    const unsigned bm = __ballot_sync(0xffffffffu, m);
+    const unsigned b1 = __ballot_sync(0xffffffffu, s1);
+    const unsigned b2 = __ballot_sync(0xffffffffu, s2);
+    if (lane == 0) {
+      const int w32 = r * wpr * 2 + cx;   // 32-bit half-word index (little endian)
+      M32[w32] = bm; F132[w32] = b1; F232[w32] = b2;
+    }
+  }
+  // zero the upper half of a row's last word when the row has an odd chunk count
+  if (cpr & 1)
+    for (int r = t; r < bh; r += NT) {
+      const int w32 = r * wpr * 2 + cpr;
+      M32[w32] = 0; F132[w32] = 0; F232[w32] = 0;
+    }
+  group_sync<NT>();
+  for (int i = t; i < nwords; i += NT) { V1[i] = F1[i]; V2[i] = F2[i]; }
+  group_sync<NT>();
+  const int area = bw * bh;
+  for (int L = 1; L <= area + 1; L++) {
+    unsigned long long n1[ITEMS], n2[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+      const int i = t + j * NT;
+      n1[j] = n2[j] = 0;
+      if (i < nwords) {
+        const int r = i / wpr, w = i - r * wpr;
+        const unsigned long long m = M[i];
+        if (m) {
+          unsigned long long f = F1[i];
+          unsigned long long a = (f << 1) | (f >> 1);
+          if (w > 0) a |= F1[i - 1] >> 63;
+          if (w < wpr - 1) a |= F1[i + 1] << 63;
+          if (r > 0) a |= F1[i - wpr];
+          if (r < bh - 1) a |= F1[i + wpr];
+          n1[j] = a & m & ~V1[i];
+          f = F2[i];
+          a = (f << 1) | (f >> 1);
+          if (w > 0) a |= F2[i - 1] >> 63;
+          if (w < wpr - 1) a |= F2[i + 1] << 63;
+          if (r > 0) a |= F2[i - wpr];
+          if (r < bh - 1) a |= F2[i + wpr];
+          n2[j] = a & m & ~V2[i];
+        }
+      }
+    }
+    group_sync<NT>();
+    int any = 0;
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+      const int i = t + j * NT;
+      if (i < nwords) {
+        F1[i] = n1[j];
+        F2[i] = n2[j];
+        if (n1[j] | n2[j]) {
+          any = 1;
+          V1[i] |= n1[j];
+          V2[i] |= n2[j];
+          const int r = i / wpr, w = i - r * wpr;
+          const int gb = (y0 + r) * W + x0 + 64 * w;
+          for (unsigned long long b = n1[j]; b; b &= b - 1) d1[gb + __ffsll((long long)b) - 1] = L + 1;
+          for (unsigned long long b = n2[j]; b; b &= b - 1) d2[gb + __ffsll((long long)b) - 1] = L + 1;
+        }
+      }
+    }
+    if (!group_any<NT>(any)) break;
+  }
+}
+
+struct BfsWarpSmem {
+  unsigned long long a[5][kWarpRows * kWarpWpr];
+};
+
+__global__ void __launch_bounds__(128) kb_split_bfs(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.sc->tmp0) return;
+  __shared__ BfsWarpSmem sm_all[4];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  BfsWarpSmem& sm = sm_all[warp];
+  const int n = min(S.cap, S.sc->max_spix + 1);
+  for (int k = blockIdx.x * 4 + warp; k < n; k += gridDim.x * 4) {
+    if (!S.sp.valid[k]) continue;
+    const int* bb = S.bbox + 4 * (size_t)k;
+    const int x0 = bb[0], x1 = bb[1], y0 = bb[2], y1 = bb[3];
+    if (x1 < x0 || y1 < y0) continue;
+    const int bw = x1 - x0 + 1, bh = y1 - y0 + 1;
+    if (bw > 64 * kWarpWpr || bh > kWarpRows) {
+      if (lane == 0) S.sm.newid[atomicAdd(&S.sc->tmp2, 1)] = k;
+      continue;
+    }
+    bfs_bits<32, kWarpRows * kWarpWpr / 32>(lane, k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2,
+                                            sm.a[0], sm.a[1], sm.a[2], sm.a[3], sm.a[4]);
+    __syncwarp();
+  }
+}
+
+// Block per large box; dynamic shared memory of 5 * kBigRows * kBigWpr words.
+__global__ void __launch_bounds__(256) kb_split_bfs_big(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  if (!S.sc->tmp0) return;
+  extern __shared__ unsigned long long big[];
+  const int nbig = S.sc->tmp2;
+  const int W = S.W;
+  const int* seg = S.seg;
+  int* d1 = S.d1;
+  int* d2 = S.d2;
+  constexpr int kA = kBigRows * kBigWpr;
+  for (int j = blockIdx.x; j < nbig; j += gridDim.x) {
+    const int k = S.sm.newid[j];
+    const int* bb = S.bbox + 4 * (size_t)k;
+    const int x0 = bb[0], y0 = bb[2];
+    const int bw = bb[1] - x0 + 1, bh = bb[3] - y0 + 1, area = bw * bh;
+    if (bw <= 64 * kBigWpr && bh <= kBigRows) {
+      bfs_bits<256, kA / 256>(threadIdx.x, k, x0, y0, bw, bh, W, seg, d1, d2, big, big + kA,
+                              big + 2 * kA, big + 3 * kA, big + 4 * kA);
+    } else {
+      for (int L = 1; L <= area + 1; L++) {
+        int ch = 0;
+        for (int i = threadIdx.x; i < area; i += blockDim.x) {
+          const int xi = i % bw, yi = i / bw;
+          const int g = (y0 + yi) * W + x0 + xi;
+          if (seg[g] != k) continue;
+          const int a = __ldcg(d1 + g), b = __ldcg(d2 + g);
+          if (a >= 0 && b >= 0) continue;
+          bool h1 = false, h2 = false;
+          auto look = [&](int q) {
+            if (seg[q] != k) return;
+            if (__ldcg(d1 + q) == L) h1 = true;
+            if (__ldcg(d2 + q) == L) h2 = true;
+          };
+          if (xi > 0) look(g - 1);
+          if (xi < bw - 1) look(g + 1);
+          if (yi > 0) look(g - W);
+          if (yi < bh - 1) look(g + W);
+          if (a < 0 && h1) { __stcg(d1 + g, L + 1); ch = 1; }
+          if (b < 0 && h2) { __stcg(d2 + g, L + 1); ch = 1; }
+        }
+        if (!__syncthreads_or(ch)) break;
+      }
+    }
+    __syncthreads();
+  }
 }
 
 // calc_seg_split (split_merge.cu:847-859): second half when d1 > d2.

@@ -1,9 +1,9 @@
 // Kernel declarations of the GB300 streaming-BASS engine.
 //
 // kb_* kernels are batched: they take the device array of slots (one frame each)
-// and pick their slot from the launch's y dimension (z for 3-D grids); the
-// cooperative kernels (kb_relax_*, kb_fill) walk the flattened work lists of all
-// slots.  k_* kernels serve the stand-alone utility entry points.
+// and pick their slot from the launch's y dimension (z for 3-D grids; x for the
+// one-block-per-slot kb_scan).  k_* kernels serve the stand-alone
+// utility entry points.
 #pragma once
 #include "engine.h"
 
@@ -41,10 +41,9 @@ __global__ void kb_save_prev(const Slot* slots);
 __global__ void kb_split_begin(const Slot* slots, int B);
 __global__ void kb_split_clear(const Slot* slots);
 __global__ void kb_split_seed(const Slot* slots, int dir_bass, int dir_prop);
-__global__ void kb_relax_bfs(const Slot* slots, int B, int total_tiles, Scalars* ctl, int* flags,
-                             int max_rounds);
-__global__ void kb_relax_cc(const Slot* slots, int B, int total_tiles, Scalars* ctl, int* flags,
-                            int max_rounds);
+__global__ void kb_bbox(const Slot* slots);
+__global__ void kb_split_bfs(const Slot* slots);
+__global__ void kb_split_bfs_big(const Slot* slots);
 __global__ void kb_split_partition(const Slot* slots);
 __global__ void kb_sm_clear(const Slot* slots);
 __global__ void kb_sm_accumulate(const Slot* slots, int split);
@@ -67,9 +66,16 @@ __global__ void kb_flow_mean(const Slot* slots);
 __global__ void kb_shift(const Slot* slots);
 __global__ void kb_shift_decode(const Slot* slots);
 __global__ void kb_count_labels(const Slot* slots, int which);
-__global__ void kb_fill(const Slot* slots, int B, long long total_pix, long long total_q,
-                        Scalars* ctl, int* counts, int* done, int break_iter);
+__global__ void kb_fill_begin(const Slot* slots, int B);
+__global__ void kb_fill_border(const Slot* slots);
+__global__ void kb_fill_phase(const Slot* slots, int ph);
+__global__ void kb_fill_compact(const Slot* slots);
+__global__ void kb_fill_step(const Slot* slots, int B, cudaGraphConditionalHandle cond,
+                             int break_iter, int* body_iters);
 __global__ void kb_cc_init(const Slot* slots);
+__global__ void kb_cc_hook(const Slot* slots);
+__global__ void kb_cc_compress(const Slot* slots);
+__global__ void kb_list_holes(const Slot* slots);
 __global__ void kb_cc_size(const Slot* slots);
 __global__ void kb_cc_best(const Slot* slots);
 __global__ void kb_cc_invalidate(const Slot* slots);

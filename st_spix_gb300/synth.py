@@ -77,6 +77,53 @@ def voronoi_video(H: int, W: int, T: int, nseeds: int, sigma: float, seed: int =
     return vid, flows, regs
 
 
+def voronoi_video_device(H: int, W: int, T: int, nseeds: int, sigma: float, seed: int = 0,
+                         max_shift: float = 4.0, max_rot_deg: float = 1.0, device="cuda"):
+    """voronoi_video's scene model generated on a torch device (for benchmarks that
+    need many large videos): the same seeds, colours and motions drawn from the
+    numpy generator of `seed`; region maps as the nearest moved seed (first index
+    on ties) and the noise from a torch generator seeded with `seed`.  Returns
+    (vid f32 [T,H,W,3], flows f32 [T-1,H,W,2]) on the device."""
+    import torch
+    rng = np.random.Generator(np.random.PCG64(seed))
+    seeds = rng.uniform([0, 0], [W, H], size=(nseeds, 2))
+    colors = rng.uniform(0, 1, size=(nseeds, 3)).astype(np.float32)
+    trans = rng.uniform(-max_shift, max_shift, size=(nseeds, 2))
+    rot = np.deg2rad(rng.uniform(-max_rot_deg, max_rot_deg, size=nseeds))
+    dev = torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(seed))
+    colors_t = torch.from_numpy(colors).to(dev)
+    trans_t = torch.from_numpy(trans).to(dev)
+    rot_t = torch.from_numpy(rot).to(dev)
+    ys, xs = torch.meshgrid(torch.arange(H, device=dev, dtype=torch.float64),
+                            torch.arange(W, device=dev, dtype=torch.float64), indexing="ij")
+    vid = torch.empty((T, H, W, 3), dtype=torch.float32, device=dev)
+    flows = torch.empty((max(T - 1, 0), H, W, 2), dtype=torch.float32, device=dev)
+    cur = torch.from_numpy(seeds).to(dev)
+    rows = max(1, (1 << 24) // max(1, W * nseeds))
+    for t in range(T):
+        reg = torch.empty((H, W), dtype=torch.long, device=dev)
+        for y0 in range(0, H, rows):
+            y1 = min(H, y0 + rows)
+            dx = xs[y0:y1, :, None] - cur[:, 0]
+            dy = ys[y0:y1, :, None] - cur[:, 1]
+            reg[y0:y1] = (dx * dx + dy * dy).argmin(-1)
+        noise = torch.randn((H, W, 3), generator=g, device=dev, dtype=torch.float32) * sigma
+        vid[t] = (colors_t[reg] + noise).clamp_(0, 1)
+        if t < T - 1:
+            c = cur[reg]
+            th = rot_t[reg]
+            dx, dy = xs - c[..., 0], ys - c[..., 1]
+            cs, sn = torch.cos(th), torch.sin(th)
+            nx = cs * dx - sn * dy + c[..., 0] + trans_t[reg, 0]
+            ny = sn * dx + cs * dy + c[..., 1] + trans_t[reg, 1]
+            flows[t, ..., 0] = (nx - xs).float()
+            flows[t, ..., 1] = (ny - ys).float()
+            cur = cur + trans_t
+    return vid, flows
+
+
 # Workloads (shapes and value distributions of the benchmark configurations).
 def config0(seed: int = 0):
     """240x320 RGB, 200 Voronoi seeds, noise sigma 0.05."""
