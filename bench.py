@@ -17,6 +17,7 @@ beside it.  Prints ONE JSON line on rank 0.
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import math
 import os
@@ -220,7 +221,90 @@ def run_reference(args, world, rank):
         base.close()
 
 
+SERVE = dict(name="serve_mixed_360p720p1080p_poisson30", mix=(0.4, 0.4, 0.2), T=30, fps=30.0,
+             budget_gb=120, pool=3)
+
+
+def run_serve(args, world, rank):
+    """--mode serve: the serving form on a mixed-resolution stream set (360p / 720p /
+    1080p at 0.4 / 0.4 / 0.2, each stream a video generated as the streaming
+    workload with its own Poisson 30 fps arrivals), admitted under a 120 GB budget
+    and served by continuous batching; the plain per-frame path (bist_forward, one
+    frame at a time) is timed on a sample of the same set."""
+    import numpy as np
+    import torch
+    from st_spix_gb300 import bist_cuda, serve, synth
+
+    torch.cuda.set_device(args.local)
+    dev = torch.device("cuda", args.local)
+    w, sv = WORKLOAD, SERVE
+    S = args.streams
+    res = synth.stream_resolution_mix(S, seed=rank)
+    cfg = dict(niters=w["niters"], sp_size=w["sp_size"], potts=w["potts"],
+               sigma2_app=w["sigma2_app"], alpha=w["alpha"], split_alpha=w["split_alpha"],
+               sm_period=w["sm_period"], prop_niters=w["prop_niters"])
+    # a small pool of device-resident videos per resolution, shared by the streams
+    pool = {}
+    for hw in sorted(set(res)):
+        pool[hw] = [synth.voronoi_video_device(hw[0], hw[1], sv["T"], w["nseeds"], w["sigma"],
+                                               seed=1000 * hw[0] + j, device=dev)
+                    for j in range(sv["pool"])]
+    # plain per-frame path on a sample (one stream per resolution, all frames)
+    plain_frames, plain_s = 0, 0.0
+    for hw in sorted(pool):
+        v, f = pool[hw][0]
+        bist_cuda.bist_forward(v[:2].contiguous(), f[:1].contiguous(), w["niters"],
+                               w["sp_size"], w["potts"], w["sigma2_app"], w["alpha"],
+                               w["split_alpha"], True, False, sm_period=w["sm_period"],
+                               prop_niters=w["prop_niters"])
+        torch.cuda.synchronize()
+        n_hw = sum(1 for r in res if r == hw)
+        t0 = time.perf_counter()
+        bist_cuda.bist_forward(v, f, w["niters"], w["sp_size"], w["potts"], w["sigma2_app"],
+                               w["alpha"], w["split_alpha"], True, False,
+                               sm_period=w["sm_period"], prop_niters=w["prop_niters"])
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        # weight by the share of streams at this resolution
+        plain_frames += n_hw * sv["T"]
+        plain_s += n_hw * dt
+    plain_fps = plain_frames / plain_s
+    budget = int(sv["budget_gb"] * 2 ** 30)
+    srv = serve.Server(budget, max_batch=args.max_batch, lanes=args.lanes, device=dev,
+                       seed=rank, **cfg)
+    for sid, hw in enumerate(res):
+        v, f = pool[hw][sid % sv["pool"]]
+        srv.add(serve.StreamRequest(sid, v, f, fps=sv["fps"]))
+    clk_lines, stop = [], threading.Event()
+    th = threading.Thread(target=sample_clocks, args=(args.local, stop, clk_lines), daemon=True)
+    th.start()
+    st = srv.run()
+    stop.set()
+    th.join(timeout=5)
+    if rank != 0:
+        return
+    hist = {f"{h}p": sum(1 for r in res if r[0] == h) for h in sorted(set(r[0] for r in res))}
+    line = {
+        "metric": "served frames/sec (mixed 360p/720p/1080p streams)", "value": st["frames_per_s"],
+        "unit": "frames/s", "n_gpus": world, "steps": 1, "warmup": 0,
+        "ms_per_step": 1000 * st["wall_s"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64+int64", "data": "synthetic",
+        "config": {"workload": sv["name"], "streams": S, "streams_by_height": hist,
+                   "frames_per_stream": sv["T"], "arrivals": "Poisson %.0f fps per stream" % sv["fps"],
+                   "offered_fps": S * sv["fps"], "budget_gb": sv["budget_gb"],
+                   "max_batch": args.max_batch, "lanes": args.lanes,
+                   "sp_size": w["sp_size"], "niters": w["niters"], "prop_niters": w["prop_niters"],
+                   "sm_period": w["sm_period"]},
+        "serving": st,
+        "plain_per_frame_fps": plain_fps,
+        "served_vs_plain": st["frames_per_s"] / plain_fps,
+        "clocks": summarize_clocks(clk_lines),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
+    faulthandler.enable(all_threads=True)
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -232,11 +316,18 @@ def main():
                     help="host threads per GPU, each with its own CUDA stream, engine "
                          "context and share of the streams")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="stream", choices=["stream", "serve"],
+                    help="stream: the 480x854 streaming workload (default); serve: the "
+                         "serving form on mixed-resolution Poisson streams")
+    ap.add_argument("--max-batch", type=int, default=8, help="serve: frames per batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_setup()
+    args.local = local
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.mode == "serve":
+        return run_serve(args, world, rank)
     args.warmup = max(args.warmup, 3)
 
     import numpy as np

@@ -233,7 +233,10 @@ int stspix_bass_partial(stspix_ctx* ctx, void* stream, const float* img, int H, 
  * bist_forward does for frames after the first).                                 */
 typedef struct stspix_video stspix_video;
 
-/* Resident state of one video stream of frames of H x W pixels. */
+/* Resident state of one video stream of frames of H x W pixels.  Any context on the
+ * same device may process its next frame; the caller keeps a video out of two
+ * batches that run at the same time (stspix_process_batch returns only when its
+ * batch has finished, so sequential calls from different contexts are safe).  */
 int stspix_video_create(stspix_ctx* ctx, stspix_video** out, int H, int W);
 int stspix_video_destroy(stspix_video* video);
 /* Forget the stream's history: its next frame starts a new video. */

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include <map>
+#include <mutex>
 
 #include <cuda_runtime.h>
 
@@ -100,7 +101,7 @@ struct stspix_ctx {
   int bcap = 0;
   Scalars* sc = nullptr;        // device [bcap]
   Scalars* sc_host = nullptr;   // pinned [bcap]
-  Slot* d_slots = nullptr;      // device [3 * bcap]: all, BASS, propagated
+  Slot* d_slots = nullptr;      // device [4 * bcap]: all, BASS, propagated, loop order
   Slot* h_slots = nullptr;      // pinned staging of the same
   std::vector<Buf> ctl_bufs;
   // hole-fill loop graphs (conditional WHILE node), per (slot table, batch size)
@@ -129,6 +130,12 @@ struct stspix_ctx {
 };
 
 namespace {
+
+// One lock for the rare operations that synchronise the whole device or change its
+// allocations (growing workspaces, freeing a video's state, destroying a context)
+// and for graph construction: contexts used from several host threads never run a
+// device-wide synchronisation or free while another thread captures a graph.
+std::mutex g_device_mu;
 
 const int kThreads = 256;
 const int kBfsBigSmem = 5 * 512 * 8 * 8;  // kb_split_bfs_big: 5 arrays of 512 rows x 8 words
@@ -280,6 +287,8 @@ int ensure_slot(stspix_ctx* ctx, int i, int npix, int sp_cap) {
   if ((int)ctx->work.size() <= i) ctx->work.resize(i + 1);
   SlotWork& w = ctx->work[i];
   Slot& s = w.s;
+  if (npix <= w.npix_cap && sp_cap <= w.sp_cap) return STSPIX_OK;
+  std::lock_guard<std::mutex> lk(g_device_mu);
   if (npix > w.npix_cap) {
     CK(cudaDeviceSynchronize());
     free_list(w.pix);
@@ -326,6 +335,7 @@ void drop_fill_graphs(stspix_ctx* ctx) {
 // Per-slot control arrays for batches of up to B slots.
 int ensure_bcap(stspix_ctx* ctx, int B) {
   if (B <= ctx->bcap) return STSPIX_OK;
+  std::lock_guard<std::mutex> lk(g_device_mu);
   CK(cudaDeviceSynchronize());
   drop_fill_graphs(ctx);
   free_list(ctx->ctl_bufs);
@@ -334,9 +344,9 @@ int ensure_bcap(stspix_ctx* ctx, int B) {
   int nb = std::max(B, 2 * ctx->bcap);
   auto& L = ctx->ctl_bufs;
   AL(L, ctx->sc, nb);
-  AL(L, ctx->d_slots, 3 * (size_t)nb);
+  AL(L, ctx->d_slots, 4 * (size_t)nb);
   CK(cudaMallocHost(&ctx->sc_host, sizeof(Scalars) * nb));
-  CK(cudaMallocHost(&ctx->h_slots, sizeof(Slot) * 3 * nb));
+  CK(cudaMallocHost(&ctx->h_slots, sizeof(Slot) * 4 * nb));
   CK(cudaMemset(ctx->sc, 0, sizeof(Scalars) * nb));
   ctx->bcap = nb;
   return STSPIX_OK;
@@ -396,8 +406,9 @@ Slot make_slot(stspix_ctx* ctx, const FrameDesc& f, int cap) {
   return s;
 }
 
-// Build a slot table at `off` (0 all, 1 BASS, 2 propagated) of the staging area and
-// its launch geometry.
+// Build a slot table at `off` (0 all, 1 BASS, 2 propagated, 3 loop order) of the
+// staging area and its launch geometry.  Each table has its own staging area, so no
+// host write touches the source of a copy still queued on the stream.
 List make_list(stspix_ctx* ctx, int off, const std::vector<Slot>& slots) {
   List L;
   L.d = ctx->d_slots + (size_t)off * ctx->bcap;
@@ -611,6 +622,7 @@ int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
   auto key = std::make_pair((const Slot*)L.d, L.B);
   auto it = ctx->fill_graphs.find(key);
   if (it != ctx->fill_graphs.end()) { *out = it->second.exec; return STSPIX_OK; }
+  std::lock_guard<std::mutex> lk(g_device_mu);
   if (!ctx->capture_stream) CK(cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking));
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
@@ -793,8 +805,8 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
   for (int i : order) { sorted.push_back(all[i]); nit_sorted.push_back(nit[i]); }
   List Ls = La;
   if (!std::is_sorted(order.begin(), order.end())) {
-    Ls = make_list(ctx, 0, sorted);
-    if ((r = upload(ctx, st, Ls, 0))) return r;
+    Ls = make_list(ctx, 3, sorted);
+    if ((r = upload(ctx, st, Ls, 3))) return r;
   }
   const SmConsts K = sm_constants(cfg);
   if ((r = bass_loop(ctx, st, Ls, nit_sorted, cfg, K, stop_after, extra_update))) return r;
@@ -840,6 +852,8 @@ int first_status(stspix_ctx* ctx, const BatchOut& o) {
 // Video stream state: label buffer and parameter ping-pong grown to `cap`,
 // keeping the current parameters.
 int video_ensure(stspix_ctx* ctx, cudaStream_t st, stspix_video* v, int cap) {
+  if (v->labels && cap <= v->pp_cap) return STSPIX_OK;
+  std::lock_guard<std::mutex> lk(g_device_mu);
   if (!v->labels) AL(v->lbufs, v->labels, (size_t)v->H * v->W);
   if (cap <= v->pp_cap) return STSPIX_OK;
   std::vector<Buf> old = v->pbufs;
@@ -936,7 +950,9 @@ int stspix_create(stspix_ctx** out, int device) {
     delete ctx;
     return STSPIX_ERR_CUDA;
   }
-  if (ensure_bcap(ctx, 4) != STSPIX_OK || cudaMalloc(&ctx->body_iters, sizeof(int)) != cudaSuccess ||
+  // slot tables for 256 frames per batch from the start: they never move for
+  // batches up to that size, so the graphs that point at them stay valid
+  if (ensure_bcap(ctx, 256) != STSPIX_OK || cudaMalloc(&ctx->body_iters, sizeof(int)) != cudaSuccess ||
       cudaMallocHost(&ctx->body_iters_host, sizeof(int)) != cudaSuccess) {
     delete ctx;
     return STSPIX_ERR_NOMEM;
@@ -951,9 +967,10 @@ int stspix_create(stspix_ctx** out, int device) {
 
 int stspix_destroy(stspix_ctx* ctx) {
   if (!ctx) return STSPIX_OK;
+  if (ctx->fwd) stspix_video_destroy(ctx->fwd);
+  std::lock_guard<std::mutex> lk(g_device_mu);
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
-  if (ctx->fwd) stspix_video_destroy(ctx->fwd);
   for (auto& w : ctx->work) { free_list(w.pix); free_list(w.sp); }
   drop_fill_graphs(ctx);
   if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
@@ -1196,6 +1213,7 @@ int stspix_video_create(stspix_ctx* ctx, stspix_video** out, int H, int W) {
   v->ctx = ctx;
   v->H = H;
   v->W = W;
+  std::lock_guard<std::mutex> lk(g_device_mu);
   cudaSetDevice(ctx->device);
   if ((r = alloc(ctx, v->lbufs, &v->labels, (size_t)H * W))) { delete v; return r; }
   *out = v;
@@ -1204,6 +1222,7 @@ int stspix_video_create(stspix_ctx* ctx, stspix_video** out, int H, int W) {
 
 int stspix_video_destroy(stspix_video* v) {
   if (!v) return STSPIX_OK;
+  std::lock_guard<std::mutex> lk(g_device_mu);
   cudaSetDevice(v->ctx->device);
   cudaDeviceSynchronize();
   free_list(v->lbufs);
@@ -1237,7 +1256,8 @@ int stspix_process_batch(stspix_ctx* ctx, void* stream, stspix_frame* frames, in
     if (F.sp_size < 0) return fail(ctx, STSPIX_ERR_ARG, "frame %d: sp_size < 0", i);
     const int sp = F.sp_size > 0 ? F.sp_size : cfg->sp_size;
     if (F.video) {
-      if (F.video->ctx != ctx) return fail(ctx, STSPIX_ERR_ARG, "frame %d: video of another context", i);
+      if (F.video->ctx->device != ctx->device)
+        return fail(ctx, STSPIX_ERR_ARG, "frame %d: video on another device", i);
       if (F.H != F.video->H || F.W != F.video->W)
         return fail(ctx, STSPIX_ERR_ARG, "frame %d: %dx%d frame for a %dx%d video", i, F.H, F.W,
                     F.video->H, F.video->W);
