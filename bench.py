@@ -303,6 +303,97 @@ def run_serve(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+BATCH = dict(name="batch64_uneven_240to1080", n=64, lo=240, hi=1080, seeds=(100, 800),
+             sigma=(0.02, 0.08), sp=(12, 16, 20, 25), niters=20, sm_period=10)
+
+
+def batch_frames(n: int, seed: int):
+    """The uneven batch: H, W uniform in [240, 1080] rounded down to multiples of 8,
+    a Voronoi frame with 100-800 seeds and noise sigma in [0.02, 0.08], superpixel
+    size drawn from {12, 16, 20, 25}."""
+    import numpy as np
+    from st_spix_gb300 import synth
+    b = BATCH
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(n):
+        H = int(rng.integers(b["lo"], b["hi"] + 1)) // 8 * 8
+        W = int(rng.integers(b["lo"], b["hi"] + 1)) // 8 * 8
+        ns = int(rng.integers(b["seeds"][0], b["seeds"][1] + 1))
+        sg = float(rng.uniform(*b["sigma"]))
+        sp = int(rng.choice(b["sp"]))
+        out.append((H, W, ns, sg, sp, 10_000 * seed + i))
+    return out
+
+
+def run_batch_mode(args, world, rank):
+    """--mode batch: 64 independent frames of uneven size as ONE batch (every kernel
+    of the path launched once for all frames), against the plain per-frame path
+    (run_bass one frame at a time) on the same frames; labels must be identical."""
+    import numpy as np
+    import torch
+    from st_spix_gb300 import batch, bist_cuda, synth
+
+    torch.cuda.set_device(args.local)
+    dev = torch.device("cuda", args.local)
+    b, w = BATCH, WORKLOAD
+    specs = batch_frames(b["n"], seed=rank)
+    imgs = []
+    for H, W, ns, sg, sp, sd in specs:
+        v, _ = synth.voronoi_video_device(H, W, 1, ns, sg, seed=sd, device=dev)
+        imgs.append((v[0].contiguous(), sp))
+    cfg = dict(niters=b["niters"], potts=w["potts"], sigma2_app=w["sigma2_app"],
+               alpha=w["alpha"], split_alpha=w["split_alpha"], sm_period=b["sm_period"])
+    npix = sum(im.shape[0] * im.shape[1] for im, _ in imgs)
+
+    def one_batch():
+        fr = [batch.Frame(img=im, sp_size=sp) for im, sp in imgs]
+        batch.process_batch(fr, **cfg)
+        return fr
+
+    for _ in range(args.warmup):
+        one_batch()
+    torch.cuda.synchronize()
+    clk_lines, stop = [], threading.Event()
+    th = threading.Thread(target=sample_clocks, args=(args.local, stop, clk_lines), daemon=True)
+    th.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fr = one_batch()
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    stop.set()
+    th.join(timeout=5)
+    gpu_ms = bist_cuda._ctx(dev).last_batch_ms()
+    # plain per-frame path on the same frames
+    t0 = time.perf_counter()
+    same = 0
+    for (im, sp), f in zip(imgs, fr):
+        lab, _ = bist_cuda.run_bass(im, sp_size=sp, **cfg)
+        same += int(torch.equal(lab, f.labels))
+    torch.cuda.synchronize()
+    plain = time.perf_counter() - t0
+    if rank != 0:
+        return
+    value = b["n"] * args.steps / elapsed
+    line = {
+        "metric": "batched frames/sec (64 uneven frames per batch)", "value": value,
+        "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64+int64", "data": "synthetic",
+        "config": {"workload": b["name"], "frames": b["n"], "mpix_per_batch": npix / 1e6,
+                   "niters": b["niters"], "sm_period": b["sm_period"],
+                   "sp_sizes": b["sp"], "step": "one batch of all frames"},
+        "batch_gpu_ms": gpu_ms,
+        "mpix_per_s": npix * args.steps / elapsed / 1e6,
+        "plain_per_frame_fps": b["n"] / plain,
+        "batched_vs_plain": value / (b["n"] / plain),
+        "frames_identical_to_plain": f"{same}/{b['n']}",
+        "clocks": summarize_clocks(clk_lines),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     faulthandler.enable(all_threads=True)
     ap = argparse.ArgumentParser()
@@ -316,9 +407,10 @@ def main():
                     help="host threads per GPU, each with its own CUDA stream, engine "
                          "context and share of the streams")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="stream", choices=["stream", "serve"],
+    ap.add_argument("--mode", default="stream", choices=["stream", "serve", "batch"],
                     help="stream: the 480x854 streaming workload (default); serve: the "
-                         "serving form on mixed-resolution Poisson streams")
+                         "serving form on mixed-resolution Poisson streams; batch: 64 "
+                         "independent frames of uneven size as one batch")
     ap.add_argument("--max-batch", type=int, default=8, help="serve: frames per batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -328,6 +420,8 @@ def main():
         return run_reference(args, world, rank)
     if args.mode == "serve":
         return run_serve(args, world, rank)
+    if args.mode == "batch":
+        return run_batch_mode(args, world, rank)
     args.warmup = max(args.warmup, 3)
 
     import numpy as np

@@ -69,9 +69,12 @@ enum { kStageShift = 1, kStageSeg = 2 };
 struct List {
   Slot* d = nullptr;               // device table
   int B = 0;
-  int max_npix = 0, max_cap = 0, max_nprev = 0, max_tx = 0, max_ty = 0, max_w = 0, max_h = 0;
+  int max_npix = 0, max_cap = 0, max_nprev = 0, max_w = 0, max_h = 0;
   long long max_acc = 0, max_sm = 0;
   bool any_prop = false;
+  std::vector<int> tiles_upto[2];  // sweep tiles (32- / 64-wide) of the first i slots
+  std::vector<long long> segs_upto;  // 32-pixel row segments of the first i slots
+  unsigned long long shape = 0;      // hash of the slot sizes (autotuner key)
 };
 
 }  // namespace stspix
@@ -107,7 +110,10 @@ struct stspix_ctx {
   // hole-fill loop graphs (conditional WHILE node), per (slot table, batch size)
   struct FillGraph { cudaGraph_t g; cudaGraphExec_t exec; };
   std::map<std::pair<const Slot*, int>, FillGraph> fill_graphs;
-  cudaStream_t capture_stream = nullptr;
+  // sweep tile autotuner
+  std::map<std::pair<unsigned long long, int>, int> sweep_choice;  // (shape, nb) -> variant
+  cudaEvent_t tune_ev[3] = {nullptr, nullptr, nullptr};
+  long long tunes = 0;
   int* body_iters = nullptr;       // device: fill-loop iterations run (launch count)
   int* body_iters_host = nullptr;  // pinned
   long long body_iters_seen = 0;
@@ -332,6 +338,99 @@ void drop_fill_graphs(stspix_ctx* ctx) {
   ctx->fill_graphs.clear();
 }
 
+// Load every kernel of the library once per process, before any of them is used.
+// With lazy module loading a kernel is otherwise loaded by its first launch, which
+// may fall inside another thread's stream capture or run concurrently with other
+// threads' launches; querying the attributes of each kernel loads it up front.
+std::once_flag g_preload_once;
+cudaError_t g_preload_err = cudaSuccess;
+
+void preload_kernels() {
+  std::call_once(g_preload_once, [] {
+    const void* fns[] = {
+      (const void*)k_init_hex,
+      (const void*)k_find_border,
+      (const void*)k_find_border_end,
+      (const void*)k_overlay,
+      (const void*)k_dump_state,
+      (const void*)kb_scalars,
+      (const void*)kb_init_hex,
+      (const void*)kb_clear_flags,
+      (const void*)kb_mark_present,
+      (const void*)kb_scan,
+      (const void*)kb_remap,
+      (const void*)kb_compact_gather,
+      (const void*)kb_compact_scatter,
+      (const void*)kb_init_bass_params,
+      (const void*)kb_init_prior_mu,
+      (const void*)kb_clear_stats,
+      (const void*)kb_accumulate,
+      (const void*)kb_posterior,
+      (const void*)kb_store_sample,
+      (const void*)kb_find_border,
+      (const void*)kb_sweep_t32,
+      (const void*)kb_sweep_t64,
+      (const void*)kb_copy_labels,
+      (const void*)kb_read_params,
+      (const void*)kb_save_prev,
+      (const void*)kb_split_begin,
+      (const void*)kb_split_clear,
+      (const void*)kb_split_seed,
+      (const void*)kb_bbox,
+      (const void*)kb_split_bfs,
+      (const void*)kb_split_bfs_big,
+      (const void*)kb_split_partition,
+      (const void*)kb_sm_clear,
+      (const void*)kb_sm_accumulate,
+      (const void*)kb_split_decide,
+      (const void*)kb_split_commit,
+      (const void*)kb_split_apply,
+      (const void*)kb_split_end,
+      (const void*)kb_merge_clear,
+      (const void*)kb_merge_candidates,
+      (const void*)kb_merge_single,
+      (const void*)kb_merge_decide,
+      (const void*)kb_merge_flag,
+      (const void*)kb_merge_remove,
+      (const void*)kb_merge_apply,
+      (const void*)kb_prop_clear,
+      (const void*)kb_flow_pool,
+      (const void*)kb_flow_mean,
+      (const void*)kb_shift,
+      (const void*)kb_shift_decode,
+      (const void*)kb_count_labels,
+      (const void*)kb_fill_begin,
+      (const void*)kb_fill_border,
+      (const void*)kb_fill_phase,
+      (const void*)kb_fill_compact,
+      (const void*)kb_fill_step,
+      (const void*)kb_cc_init,
+      (const void*)kb_cc_hook,
+      (const void*)kb_cc_compress,
+      (const void*)kb_list_holes,
+      (const void*)kb_cc_size,
+      (const void*)kb_cc_best,
+      (const void*)kb_cc_invalidate,
+      (const void*)kb_shift_params,
+      (const void*)kb_write_params,
+      (const void*)kb_mark_active,
+      (const void*)kb_relabel_init,
+      (const void*)kb_living,
+      (const void*)kb_relabel_compare,
+      (const void*)kb_relabel_mark,
+      (const void*)kb_relabel_ids,
+      (const void*)kb_relabel_params,
+      (const void*)kb_relabel_apply,
+      (const void*)kb_relabel_end,
+      (const void*)kb_count_revived};
+    for (const void* f : fns) {
+      cudaFuncAttributes a;
+      cudaError_t e = cudaFuncGetAttributes(&a, f);
+      if (e != cudaSuccess && g_preload_err == cudaSuccess) g_preload_err = e;
+    }
+  });
+}
+
 // Per-slot control arrays for batches of up to B slots.
 int ensure_bcap(stspix_ctx* ctx, int B) {
   if (B <= ctx->bcap) return STSPIX_OK;
@@ -412,19 +511,27 @@ Slot make_slot(stspix_ctx* ctx, const FrameDesc& f, int cap) {
 List make_list(stspix_ctx* ctx, int off, const std::vector<Slot>& slots) {
   List L;
   L.d = ctx->d_slots + (size_t)off * ctx->bcap;
+  for (int v = 0; v < 2; v++) L.tiles_upto[v].assign(1, 0);
+  L.segs_upto.assign(1, 0);
   Slot* h = ctx->h_slots + (size_t)off * ctx->bcap;
   L.B = (int)slots.size();
   for (int i = 0; i < L.B; i++) {
-    const Slot& s = slots[i];
+    Slot s = slots[i];
+    for (int v = 0; v < 2; v++) {
+      if (L.tiles_upto[v].empty()) L.tiles_upto[v].push_back(0);
+      s.tile_base[v] = L.tiles_upto[v].back();
+      const int tw = v ? 64 : 32;
+      L.tiles_upto[v].push_back(s.tile_base[v] + ((s.W + tw - 1) / tw) * ((s.H + 31) / 32));
+    }
+    if (L.segs_upto.empty()) L.segs_upto.push_back(0);
+    L.segs_upto.push_back(L.segs_upto.back() + (long long)s.H * ((s.W + 31) / 32));
+    L.shape = (L.shape ^ (unsigned long long)(s.H * 65536LL + s.W)) * 1099511628211ULL;
     h[i] = s;
-    const int tx = (s.W + kSweepTileW - 1) / kSweepTileW, ty = (s.H + kSweepTileH - 1) / kSweepTileH;
     L.max_npix = std::max(L.max_npix, s.npix);
     L.max_cap = std::max(L.max_cap, s.cap);
     L.max_nprev = std::max(L.max_nprev, s.n_prev);
-    L.max_tx = std::max(L.max_tx, tx);
     L.max_w = std::max(L.max_w, s.W);
     L.max_h = std::max(L.max_h, s.H);
-    L.max_ty = std::max(L.max_ty, ty);
     L.max_acc = std::max(L.max_acc, (long long)s.H * ((s.W + 7) / 8));
     L.max_sm = std::max(L.max_sm, (long long)s.H * ((s.W + 15) / 16));
     if (s.mode) L.any_prop = true;
@@ -442,17 +549,18 @@ int upload(stspix_ctx* ctx, cudaStream_t st, const List& L, int off) {
 // ---------------------------------------------------------------------------
 // Stages over the first nb slots of a table.
 
-// kb_accumulate blocks per slot: 8 warps each, about 4 row segments per warp.
-unsigned acc_blocks(const List& L) {
-  const long long segs = (long long)L.max_h * ((L.max_w + 31) / 32);
-  return (unsigned)std::max(1LL, (segs + 31) / 32);
+// kb_accumulate: a persistent grid of 8-warp blocks, about 2 segments per warp,
+// at most 8 blocks per SM.
+unsigned acc_blocks(const stspix_ctx* ctx, const List& L, int nb) {
+  const long long segs = L.segs_upto[nb];
+  return (unsigned)std::max(1LL, std::min<long long>((segs + 15) / 16, 8LL * ctx->num_sms));
 }
 
 // update_params (update_params.cu:12-52): statistics + posterior.
 int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb) {
   ctx->cur_fam = STSPIX_FAM_STATS;
   LAUNCHB(kb_clear_stats, L.max_cap, L, nb);
-  LAUNCHG(kb_accumulate, dim3(acc_blocks(L), (unsigned)nb), 256, L.d);
+  LAUNCHG(kb_accumulate, acc_blocks(ctx, L, nb), 256, L.d, nb);
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
   LAUNCHB(kb_posterior, L.max_cap, L, nb);
   return STSPIX_OK;
@@ -464,9 +572,38 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb) {
 int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
                const stspix_config& cfg, bool need_border) {
   ctx->cur_fam = STSPIX_FAM_SWEEP;
-  dim3 grid((unsigned)L.max_tx, (unsigned)L.max_ty, (unsigned)nb);
-  for (int it = 0; it < cfg.niters_seg; it++)
-    LAUNCHG(kb_sweep, grid, 256, L.d, it & 1, cfg.sigma2_app, cfg.potts);
+  auto sweep = [&](int v, int parity) {
+    const unsigned g = (unsigned)std::max(1, L.tiles_upto[v][nb]);
+    if (v) LAUNCHG(kb_sweep_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts);
+    else LAUNCHG(kb_sweep_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts);
+  };
+  // tile-shape autotuner: the first sweep of a batch shape runs both tile widths on
+  // the same input (a sweep reads only the labels at its start, so both write the
+  // same output) and the faster is kept for that shape
+  int it0 = 0;
+  const auto key = std::make_pair(L.shape, nb);
+  auto ch = ctx->sweep_choice.find(key);
+  int v;
+  if (ch != ctx->sweep_choice.end()) {
+    v = ch->second;
+  } else if (cfg.niters_seg > 0) {
+    float ms[2] = {0.f, 0.f};
+    CK(cudaEventRecord(ctx->tune_ev[0], st));
+    sweep(0, 0);
+    CK(cudaEventRecord(ctx->tune_ev[1], st));
+    sweep(1, 0);
+    CK(cudaEventRecord(ctx->tune_ev[2], st));
+    CK(cudaEventSynchronize(ctx->tune_ev[2]));
+    cudaEventElapsedTime(&ms[0], ctx->tune_ev[0], ctx->tune_ev[1]);
+    cudaEventElapsedTime(&ms[1], ctx->tune_ev[1], ctx->tune_ev[2]);
+    v = ms[1] <= ms[0] ? 1 : 0;
+    ctx->sweep_choice[key] = v;
+    ctx->tunes++;
+    it0 = 1;
+  } else {
+    v = 1;
+  }
+  for (int it = it0; it < cfg.niters_seg; it++) sweep(v, it & 1);
   if (cfg.niters_seg & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;
@@ -609,7 +746,7 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHS(kb_scalars, L, L.B, (int)kOpAfterHex);
   LAUNCHB(kb_init_bass_params, L.max_cap, L, L.B);
   LAUNCHB(kb_clear_stats, L.max_cap, L, L.B);
-  LAUNCHG(kb_accumulate, dim3(acc_blocks(L), (unsigned)L.B), 256, L.d);
+  LAUNCHG(kb_accumulate, acc_blocks(ctx, L, L.B), 256, L.d, L.B);
   LAUNCHB(kb_init_prior_mu, L.max_cap, L, L.B);
   LAUNCHB(kb_find_border, L.max_npix, L, L.B);
   return STSPIX_OK;
@@ -617,13 +754,13 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
 
 // The hole-fill loop of the propagated slots of table L as a graph: a WHILE node
 // whose body is one iteration (kb_fill_border, kb_fill_phase x 4, kb_fill_compact,
-// kb_fill_step); kb_fill_step sets the condition.  Built once per (table, size).
+// kb_fill_step, added as kernel nodes); kb_fill_step sets the condition.  Built once
+// per (table, size).
 int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
   auto key = std::make_pair((const Slot*)L.d, L.B);
   auto it = ctx->fill_graphs.find(key);
   if (it != ctx->fill_graphs.end()) { *out = it->second.exec; return STSPIX_OK; }
   std::lock_guard<std::mutex> lk(g_device_mu);
-  if (!ctx->capture_stream) CK(cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking));
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle cond;
@@ -636,19 +773,42 @@ int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
   cudaGraphNode_t node;
   CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
-  cudaStream_t cs = ctx->capture_stream;
-  CK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  // the body: border -> phase 0..3 -> compact -> step, as a chain of kernel nodes
   const unsigned G = (unsigned)std::max(8, std::min(128, 2048 / std::max(L.B, 1)));
   const dim3 grid(G, (unsigned)L.B);
-  kb_fill_border<<<grid, kThreads, 0, cs>>>(L.d);
-  for (int ph = 0; ph < 4; ph++) kb_fill_phase<<<grid, kThreads, 0, cs>>>(L.d, ph);
-  kb_fill_compact<<<grid, kThreads, 0, cs>>>(L.d);
-  kb_fill_step<<<1, kThreads, 0, cs>>>(L.d, L.B, cond, kFillBreakIter, ctx->body_iters);
-  cudaGraph_t captured = nullptr;
-  cudaError_t ce = cudaStreamEndCapture(cs, &captured);
+  Slot* table = L.d;
+  int B = L.B, break_iter = kFillBreakIter;
+  int ph_arg[4] = {0, 1, 2, 3};
+  cudaGraphNode_t prev = nullptr;
+  cudaError_t ce = cudaSuccess;
+  auto add = [&](const void* fn, dim3 gd, dim3 bd, void** args) {
+    if (ce != cudaSuccess) return;
+    cudaKernelNodeParams kp = {};
+    kp.func = const_cast<void*>(fn);
+    kp.gridDim = gd;
+    kp.blockDim = bd;
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    cudaGraphNode_t n;
+    ce = cudaGraphAddKernelNode(&n, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp);
+    prev = n;
+  };
+  void* a_border[] = {(void*)&table};
+  add((const void*)kb_fill_border, grid, dim3(kThreads), a_border);
+  void* a_ph[4][2];
+  for (int ph = 0; ph < 4; ph++) {
+    a_ph[ph][0] = (void*)&table;
+    a_ph[ph][1] = (void*)&ph_arg[ph];
+    add((const void*)kb_fill_phase, grid, dim3(kThreads), a_ph[ph]);
+  }
+  void* a_compact[] = {(void*)&table};
+  add((const void*)kb_fill_compact, grid, dim3(kThreads), a_compact);
+  void* a_step[] = {(void*)&table, (void*)&B, (void*)&cond, (void*)&break_iter,
+                    (void*)&ctx->body_iters};
+  add((const void*)kb_fill_step, dim3(1), dim3(kThreads), a_step);
   if (ce != cudaSuccess) {
     cudaGraphDestroy(g);
-    return fail(ctx, STSPIX_ERR_CUDA, "fill graph capture failed: %s", cudaGetErrorString(ce));
+    return fail(ctx, STSPIX_ERR_CUDA, "fill graph construction failed: %s", cudaGetErrorString(ce));
   }
   cudaGraphExec_t exec = nullptr;
   ce = cudaGraphInstantiate(&exec, g, 0);
@@ -944,6 +1104,11 @@ int stspix_create(stspix_ctx** out, int device) {
   ctx->device = device;
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) { delete ctx; return STSPIX_ERR_CUDA; }
+  {
+    std::lock_guard<std::mutex> lk(g_device_mu);
+    preload_kernels();
+  }
+  if (g_preload_err != cudaSuccess) { delete ctx; return STSPIX_ERR_CUDA; }
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (cudaFuncSetAttribute((const void*)kb_split_bfs_big,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, kBfsBigSmem) != cudaSuccess) {
@@ -960,6 +1125,7 @@ int stspix_create(stspix_ctx** out, int device) {
   cudaMemset(ctx->body_iters, 0, sizeof(int));
   cudaEventCreate(&ctx->batch_ev[0]);
   cudaEventCreate(&ctx->batch_ev[1]);
+  for (auto& e : ctx->tune_ev) cudaEventCreate(&e);
   cudaDeviceSynchronize();
   *out = ctx;
   return STSPIX_OK;
@@ -973,9 +1139,9 @@ int stspix_destroy(stspix_ctx* ctx) {
   cudaDeviceSynchronize();
   for (auto& w : ctx->work) { free_list(w.pix); free_list(w.sp); }
   drop_fill_graphs(ctx);
-  if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
   free_list(ctx->ctl_bufs);
   cudaFree(ctx->body_iters);
+  for (auto e : ctx->tune_ev) if (e) cudaEventDestroy(e);
   if (ctx->body_iters_host) cudaFreeHost(ctx->body_iters_host);
   prof_harvest(ctx);
   for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.a); ctx->ev_free.push_back(e.b); }

@@ -25,7 +25,6 @@ constexpr int kFxAppShift = 28;
 constexpr int kFxSqShift = 20;
 constexpr int kFxFlowShift = 24;
 constexpr int kFillBreakIter = 1000;      // fill_missing.cu: break_iter
-constexpr int kSweepTileW = 64, kSweepTileH = 32;  // boundary-sweep tile
 
 // Packed record read by the boundary sweep: the fields calc_joint reads
 // (update_seg.cu:194-259), already converted to the types it uses.  The reference
@@ -148,6 +147,7 @@ struct Slot {
   unsigned long long *rbest, *ccbest;
   int* bbox;               // [4*(cap+2)]: x0, x1, y0, y1 per superpixel (split BFS)
   Scalars* sc;
+  int tile_base[2];        // first sweep tile of this slot in the batch (32- / 64-wide)
 };
 
 // kb_scalars operations.

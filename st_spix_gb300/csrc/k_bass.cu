@@ -15,19 +15,41 @@ namespace stspix {
 // this pointy-top hex lattice lies within one hexagon radius, so a 5x5 window of
 // lattice sites around the pixel, scanned in ascending id order with the same
 // `<=` rule and the same double arithmetic, gives the identical label.
-__global__ void k_init_hex(int* __restrict__ seg, int H, int W, double Hh, double w, int nx,
-                           int ny) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= H * W) return;
-  int x = idx % W, y = idx / W;
-  int r0 = (int)floor(y / (1.5 * Hh));
-  int c0 = (int)floor(x / w);
+// Nearest hexagon centre of pixel (x, y) (InitHexSeg, init_seg.cu:63-75): the
+// reference scans every centre in FP64 and keeps the last one at the smallest
+// squared distance.  Only the 5x5 lattice neighbourhood of the pixel can hold the
+// nearest centre; an FP32 pass finds the smallest distance there, and only the
+// centres within an error margin of it are evaluated in FP64 with the reference's
+// rule, in the same scan order.  With |dx|, |dy| < 3 hexagon sizes s and centre
+// coordinates below x + y + 3s, the FP32 squared distance errs by less than
+// ~5e-6 s (x + y + 6s) + 1e-7 d2 px^2; the margin below exceeds twice that, so
+// every FP64 minimiser passes the filter and the label is the reference's.
+__device__ __forceinline__ int hex_label(int x, int y, double Hh, double w, int nx, int ny) {
+  const int r0 = (int)floor(y / (1.5 * Hh));
+  const int c0 = (int)floor(x / w);
+  const float wf = (float)w, hf = (float)(1.5 * Hh), half = (float)(0.5 * w);
+  const float xf = (float)x, yf = (float)y;
+  float mn = 3.0e38f;
+  for (int r = r0 - 2; r <= r0 + 2; r++) {
+    if (r < 0 || r >= ny) continue;
+    for (int c = c0 - 2; c <= c0 + 2; c++) {
+      if (c < 0 || c >= nx) continue;
+      const float dx = xf - ((float)c * wf + ((r % 2 == 0) ? half : 0.f));
+      const float dy = yf - (float)r * hf;
+      mn = fminf(mn, dx * dx + dy * dy);
+    }
+  }
+  const float sz = wf + hf;
+  const float lim = mn + 8.0f + 1e-5f * mn + 1e-5f * sz * (xf + yf + 8.0f * sz);
   double D2 = 1.7976931348623157e308;
   int best = 0;
   for (int r = r0 - 2; r <= r0 + 2; r++) {
     if (r < 0 || r >= ny) continue;
     for (int c = c0 - 2; c <= c0 + 2; c++) {
       if (c < 0 || c >= nx) continue;
+      const float dxf = xf - ((float)c * wf + ((r % 2 == 0) ? half : 0.f));
+      const float dyf = yf - (float)r * hf;
+      if (dxf * dxf + dyf * dyf > lim) continue;
       double xx = double(c) * w;
       double yy = double(r) * 1.5 * Hh;
       if (r % 2 == 0) xx = xx + 0.5 * w;
@@ -37,34 +59,21 @@ __global__ void k_init_hex(int* __restrict__ seg, int H, int W, double Hh, doubl
       if (d2 <= D2) { D2 = d2; best = r * nx + c; }
     }
   }
-  seg[idx] = best;
+  return best;
+}
+
+__global__ void k_init_hex(int* __restrict__ seg, int H, int W, double Hh, double w, int nx,
+                           int ny) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= H * W) return;
+  seg[idx] = hex_label(idx % W, idx / W, Hh, w, nx, ny);
 }
 
 __global__ void kb_init_hex(const Slot* __restrict__ slots) {
   SLOT_Y;
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= S.npix) return;
-  const int W = S.W, nx = S.hex_nx, ny = S.hex_ny;
-  const double Hh = S.hex_h, w = S.hex_w;
-  int x = idx % W, y = idx / W;
-  int r0 = (int)floor(y / (1.5 * Hh));
-  int c0 = (int)floor(x / w);
-  double D2 = 1.7976931348623157e308;
-  int best = 0;
-  for (int r = r0 - 2; r <= r0 + 2; r++) {
-    if (r < 0 || r >= ny) continue;
-    for (int c = c0 - 2; c <= c0 + 2; c++) {
-      if (c < 0 || c >= nx) continue;
-      double xx = double(c) * w;
-      double yy = double(r) * 1.5 * Hh;
-      if (r % 2 == 0) xx = xx + 0.5 * w;
-      double dx = (x - xx);
-      double dy = (y - yy);
-      double d2 = dx * dx + dy * dy;
-      if (d2 <= D2) { D2 = d2; best = r * nx + c; }
-    }
-  }
-  S.seg[idx] = best;
+  S.seg[idx] = hex_label(idx % S.W, idx / S.W, S.hex_h, S.hex_w, S.hex_nx, S.hex_ny);
 }
 
 // ---------------------------------------------------------------------------
@@ -257,15 +266,17 @@ __device__ __forceinline__ long long warp_incl_scan(long long v, int lane) {
   return v;
 }
 
-// grid: (x blocks of 8 warps, slot); each warp walks 32-pixel row segments.
-__global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ slots) {
-  SLOT_Y;
-  const int H = S.H, W = S.W;
-  const int spr = (W + 31) >> 5;                 // segments per row
-  const int nseg = H * spr;
+// Persistent grid: every warp walks the 32-pixel row segments of every slot in
+// turn (the first B slots), so frames of uneven size need no per-frame grid.
+__global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ slots, int B) {
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int si = 0; si < B; si++) {
+  const Slot& S = slots[si];
+  const int H = S.H, W = S.W;
+  const int spr = (W + 31) >> 5;                 // segments per row
+  const int nseg = H * spr;
   const SpDev& sp = S.sp;
   const int cap = sp.cap;
   for (int sgi = wid; sgi < nseg; sgi += nw) {
@@ -299,6 +310,7 @@ __global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ sl
     if (start == 0) b0 = b1 = b2 = 0;
     if (tail && k >= 0 && k < cap)
       add_run_sums(sp, k, y, xb + start, x, p0 - b0, p1 - b1, p2 - b2);
+  }
   }
 }
 
@@ -516,69 +528,78 @@ __device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int 
 
 // ---------------------------------------------------------------------------
 // Fused sweep: border pass + the four parity phases of one sweep in one launch.
-// A block owns a 64x32 tile and stages labels of the tile plus a 4-pixel halo
+// A block owns a TX x TY tile and stages labels of the tile plus a 4-pixel halo
 // (phase k is evaluated on the tile grown by 3-k pixels, so every label a tile
 // pixel depends on is produced inside the block exactly as the four separate
 // launches produce it), the image and the border mask of the tile plus 3 pixels.
 // Labels are read from seg_in (labels at the sweep start) and the tile is
 // written to seg_out, so neighbouring blocks never see each other's updates.
-constexpr int kTX = kSweepTileW;      // tile width (64)
-constexpr int kTY = kSweepTileH;      // tile height (32)
+//
+// The grid is the list of tiles of every frame of the batch (frame i owns tiles
+// [tile_base, tile_base + its tile count)); a block finds its frame by binary
+// search, so frames of uneven size cost what their tiles cost.
 constexpr int kSH = 4;                // label halo
-constexpr int kLX = kTX + 2 * kSH;    // 72 x 40: staged labels
-constexpr int kLY = kTY + 2 * kSH;
-constexpr int kIX = kTX + 2 * (kSH - 1);  // 70 x 38: staged image / border region
-constexpr int kIY = kTY + 2 * (kSH - 1);
 
-__global__ void __launch_bounds__(256) kb_sweep(const Slot* __restrict__ slots, int parity,
-                                                float s2, float potts) {
-  SLOT_Z;
+template <int TX, int TY>
+struct SweepTile {
+  static constexpr int kLX = TX + 2 * kSH, kLY = TY + 2 * kSH;      // staged labels
+  static constexpr int kIX = TX + 2 * (kSH - 1), kIY = TY + 2 * (kSH - 1);  // image / border
+  static constexpr int kMaxList = (TX / 2 + kSH - 1) * (TY / 2 + kSH - 1);
+  int L[kLX * kLY];
+  float I[kIX * kIY * 3];
+  short list[4][kMaxList];   // border pixels of each parity phase
+  int cnt[4];
+};
+
+template <int TX, int TY>
+__device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int parity, float s2,
+                                           float potts, SweepTile<TX, TY>& sm,
+                                           const unsigned* lut_bits) {
+  constexpr int kTX = TX, kTY = TY;
+  constexpr int kLX = SweepTile<TX, TY>::kLX, kLY = SweepTile<TX, TY>::kLY;
+  constexpr int kIX = SweepTile<TX, TY>::kIX, kIY = SweepTile<TX, TY>::kIY;
+  int* L = sm.L;
+  float* I = sm.I;
+  auto& list = sm.list;
+  int* cnt = sm.cnt;
+
   const int H = S.H, W = S.W;
-  if ((int)blockIdx.x * kTX >= W || (int)blockIdx.y * kTY >= H) return;
   const float* __restrict__ img = S.img;
   const int* __restrict__ seg_in = parity ? S.seg_alt : S.seg;
   int* __restrict__ seg_out = parity ? S.seg : S.seg_alt;
   const SweepRec* __restrict__ rec = S.sp.rec;
   const int cap = S.sp.cap;
-  constexpr int kMaxList = (kTX / 2 + kSH - 1) * (kTY / 2 + kSH - 1);  // 35 x 19
-  __shared__ int L[kLX * kLY];
-  __shared__ float I[kIX * kIY * 3];
-  __shared__ short list[4][kMaxList];   // border pixels of each parity phase
-  __shared__ int cnt[4];
-  __shared__ unsigned lut_bits[8];
-  if (threadIdx.x < 8) {
-    unsigned w = 0;
-    for (int b = 0; b < 32; b++) w |= (unsigned)(c_simple_lut[threadIdx.x * 32 + b] != 0) << b;
-    lut_bits[threadIdx.x] = w;
-  }
   if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
-  const int tx0 = blockIdx.x * kTX, ty0 = blockIdx.y * kTY;
+  const int tx0 = bx * kTX, ty0 = by * kTY;
   const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;        // label region origin
   const int ix0 = tx0 - (kSH - 1), iy0 = ty0 - (kSH - 1);  // image region origin
   // Staging: every thread issues all of its loads before the first store, so the
   // block waits for one memory round trip, not one per element.
   {
-    constexpr int kNL = (kLX * kLY + 255) / 256;  // 12 labels per thread
-    int lv[kNL];
+    constexpr int kNL = 8;  // labels per thread and batch
 #pragma unroll
-    for (int j = 0; j < kNL; j++) {
-      const int i = threadIdx.x + 256 * j;
-      const int gx = rx0 + i % kLX, gy = ry0 + i / kLX;
-      lv[j] = (i < kLX * kLY && gx >= 0 && gx < W && gy >= 0 && gy < H) ? seg_in[gy * W + gx]
-                                                                          : -1;
-    }
+    for (int b0 = 0; b0 < kLX * kLY; b0 += 256 * kNL) {
+      int lv[kNL];
 #pragma unroll
-    for (int j = 0; j < kNL; j++) {
-      const int i = threadIdx.x + 256 * j;
-      if (i < kLX * kLY) L[i] = lv[j];
+      for (int j = 0; j < kNL; j++) {
+        const int i = b0 + threadIdx.x + 256 * j;
+        const int gx = rx0 + i % kLX, gy = ry0 + i / kLX;
+        lv[j] = (i < kLX * kLY && gx >= 0 && gx < W && gy >= 0 && gy < H) ? seg_in[gy * W + gx]
+                                                                            : -1;
+      }
+#pragma unroll
+      for (int j = 0; j < kNL; j++) {
+        const int i = b0 + threadIdx.x + 256 * j;
+        if (i < kLX * kLY) L[i] = lv[j];
+      }
     }
   }
   {
-    // the image region as rows of 3 * kIX floats (same layout as I), in two
-    // batches of 16 loads per thread
+    // the image region as rows of 3 * kIX floats (same layout as I), in batches of
+    // 8 loads per thread
     constexpr int kRow = 3 * kIX;
     constexpr int kNF = kIY * kRow;
-    constexpr int kNI = 16;
+    constexpr int kNI = 8;
 #pragma unroll
     for (int b0 = 0; b0 < kNF; b0 += 256 * kNI) {
       float iv[kNI];
@@ -694,6 +715,39 @@ __global__ void __launch_bounds__(256) kb_sweep(const Slot* __restrict__ slots, 
     int gx = tx0 + i % kTX, gy = ty0 + i / kTX;
     if (gx < W && gy < H) seg_out[gy * W + gx] = L[(gy - ry0) * kLX + (gx - rx0)];
   }
+}
+
+template <int TX, int TY>
+__device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B, int parity,
+                                           float s2, float potts) {
+  __shared__ SweepTile<TX, TY> sm;
+  __shared__ unsigned lut_bits[8];
+  if (threadIdx.x < 8) {
+    unsigned w = 0;
+    for (int b = 0; b < 32; b++) w |= (unsigned)(c_simple_lut[threadIdx.x * 32 + b] != 0) << b;
+    lut_bits[threadIdx.x] = w;
+  }
+  const int v = TX == 32 ? 0 : 1;   // which tile_base of the slots
+  const int t = blockIdx.x;
+  int lo = 0, hi = B - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (slots[mid].tile_base[v] <= t) lo = mid; else hi = mid - 1;
+  }
+  const Slot& S = slots[lo];
+  const int tl = t - S.tile_base[v];
+  const int tiles_x = (S.W + TX - 1) / TX;
+  sweep_tile<TX, TY>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits);
+}
+
+// One block per tile of the batch (grid = the batch's total tile count).
+__global__ void __launch_bounds__(256) kb_sweep_t32(const Slot* __restrict__ slots, int B,
+                                                    int parity, float s2, float potts) {
+  sweep_flat<32, 32>(slots, B, parity, s2, potts);
+}
+__global__ void __launch_bounds__(256) kb_sweep_t64(const Slot* __restrict__ slots, int B,
+                                                    int parity, float s2, float potts) {
+  sweep_flat<64, 32>(slots, B, parity, s2, potts);
 }
 
 // ---------------------------------------------------------------------------
