@@ -280,7 +280,7 @@ int alloc_params(stspix_ctx* ctx, std::vector<Buf>& L, stspix_params& p, int cap
 }
 
 // Bytes of the buffers above (for admission under a memory budget).
-constexpr long long kPixBytes = 1 + 5 * 4 + 8 + 4;            // border, d1 d2 smseg hits shifted, best, seg_alt
+constexpr long long kPixBytes = 1 + 5 * 4 + 8 + 4 + 2;        // border, d1 d2 smseg hits shifted, best, seg_alt, chg x2
 constexpr long long kSpDevBytes = 4 + 1 + 1 + 4 + 4 + 4 + 12 + 16 + 24 + 8 + 12 + 16 + 24 + 24 + 24 +
                                   64 + (long long)sizeof(SweepRec);
 constexpr long long kSmBytes = 4 + 24 + 24 + 4 + 4 + 4 + 4 + 4 + 1 + 8;
@@ -302,6 +302,7 @@ int ensure_slot(stspix_ctx* ctx, int i, int npix, int sp_cap) {
     int n = npix;
     AL(L, s.border, n); AL(L, s.d1, n); AL(L, s.d2, n); AL(L, s.smseg, n);
     AL(L, s.hits, n); AL(L, s.shifted, n); AL(L, s.best, n); AL(L, s.seg_alt, n);
+    AL(L, s.chg[0], n); AL(L, s.chg[1], n);
     w.npix_cap = npix;
   }
   if (sp_cap > w.sp_cap) {
@@ -572,10 +573,12 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb) {
 int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
                const stspix_config& cfg, bool need_border) {
   ctx->cur_fam = STSPIX_FAM_SWEEP;
-  auto sweep = [&](int v, int parity) {
+  // the first sweep of the call scores every border pixel; the later ones only the
+  // active set next to the previous sweep's changes (same labels, see kb_sweep_t*)
+  auto sweep = [&](int v, int parity, int mode) {
     const unsigned g = (unsigned)std::max(1, L.tiles_upto[v][nb]);
-    if (v) LAUNCHG(kb_sweep_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts);
-    else LAUNCHG(kb_sweep_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts);
+    if (v) LAUNCHG(kb_sweep_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode);
+    else LAUNCHG(kb_sweep_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode);
   };
   // tile-shape autotuner: the first sweep of a batch shape runs both tile widths on
   // the same input (a sweep reads only the labels at its start, so both write the
@@ -589,9 +592,9 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   } else if (cfg.niters_seg > 0) {
     float ms[2] = {0.f, 0.f};
     CK(cudaEventRecord(ctx->tune_ev[0], st));
-    sweep(0, 0);
+    sweep(0, 0, 0);
     CK(cudaEventRecord(ctx->tune_ev[1], st));
-    sweep(1, 0);
+    sweep(1, 0, 0);
     CK(cudaEventRecord(ctx->tune_ev[2], st));
     CK(cudaEventSynchronize(ctx->tune_ev[2]));
     cudaEventElapsedTime(&ms[0], ctx->tune_ev[0], ctx->tune_ev[1]);
@@ -603,7 +606,7 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   } else {
     v = 1;
   }
-  for (int it = it0; it < cfg.niters_seg; it++) sweep(v, it & 1);
+  for (int it = it0; it < cfg.niters_seg; it++) sweep(v, it & 1, it > 0 ? 1 : 0);
   if (cfg.niters_seg & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;

@@ -134,6 +134,7 @@ struct Slot {
   int* resident_labels;    // where the finished labels are kept for the next frame
   // pixel workspace
   uint8_t* border;
+  uint8_t* chg[2];         // change flags of the last two sweeps (active-set sweeps)
   int *d1, *d2, *smseg, *hits, *shifted;
   unsigned long long* best;
   // superpixel workspace

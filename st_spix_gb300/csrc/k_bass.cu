@@ -549,12 +549,24 @@ struct SweepTile {
   float I[kIX * kIY * 3];
   short list[4][kMaxList];   // border pixels of each parity phase
   int cnt[4];
+  // active-set sweeps: change flags of the label region as row bitmasks (bit x of
+  // row y = label-region pixel (x, y)), dilated by 4 pixels
+  unsigned long long act[2][kLY];
+  int any;
 };
 
+// Active-set sweeps.  The parameters are fixed across the sweeps of one update_seg
+// call and a pixel's decision depends only on its 3x3 labels (after the earlier
+// phases of the sweep), its colour and the parameters, so a pixel of phase k can
+// only change if a label within Chebyshev distance k + 1 <= 4 changed during the
+// previous sweep or earlier in this one.  Sweeps after the first of a call (mode 1)
+// therefore list only the border pixels within 4 pixels of a change flagged by the
+// previous sweep (chg_in), and a tile whose whole label region saw no change keeps
+// its labels.  Every sweep writes its own change flags (chg_out).
 template <int TX, int TY>
 __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int parity, float s2,
                                            float potts, SweepTile<TX, TY>& sm,
-                                           const unsigned* lut_bits) {
+                                           const unsigned* lut_bits, int mode) {
   constexpr int kTX = TX, kTY = TY;
   constexpr int kLX = SweepTile<TX, TY>::kLX, kLY = SweepTile<TX, TY>::kLY;
   constexpr int kIX = SweepTile<TX, TY>::kIX, kIY = SweepTile<TX, TY>::kIY;
@@ -573,6 +585,64 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   const int tx0 = bx * kTX, ty0 = by * kTY;
   const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;        // label region origin
   const int ix0 = tx0 - (kSH - 1), iy0 = ty0 - (kSH - 1);  // image region origin
+  const uint8_t* __restrict__ chg_in = S.chg[parity ^ 1];
+  uint8_t* __restrict__ chg_out = S.chg[parity];
+  static_assert(kLX <= 128, "label region wider than two 64-bit words");
+  if (mode) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long* a0 = sm.act[0];
+    unsigned long long* a1 = sm.act[1];
+    if (threadIdx.x == 0) sm.any = 0;
+    for (int r = threadIdx.x; r < kLY; r += blockDim.x) { a0[r] = 0; a1[r] = 0; }
+    __syncthreads();
+    constexpr int kCh = (kLX + 31) / 32;
+    for (int c = warp; c < kLY * kCh; c += blockDim.x / 32) {
+      const int r = c / kCh, cx = c % kCh;
+      const int x = cx * 32 + lane;
+      const int gx = rx0 + x, gy = ry0 + r;
+      const bool f = x < kLX && gx >= 0 && gx < W && gy >= 0 && gy < H && chg_in[gy * W + gx];
+      const unsigned b = __ballot_sync(0xffffffffu, f);
+      if (lane == 0 && b) {
+        // chunk cx covers bits 32 cx .. 32 cx + 31 of the row: word cx / 2, half cx % 2
+        atomicOr(cx < 2 ? &a0[r] : &a1[r], (unsigned long long)b << (32 * (cx & 1)));
+        sm.any = 1;
+      }
+    }
+    __syncthreads();
+    if (!sm.any) {
+      // nothing within reach changed: the tile keeps its labels
+      for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x) {
+        const int gx = tx0 + i % kTX, gy = ty0 + i / kTX;
+        if (gx < W && gy < H) {
+          seg_out[gy * W + gx] = seg_in[gy * W + gx];
+          chg_out[gy * W + gx] = 0;
+        }
+      }
+      return;
+    }
+    // dilate by 4: horizontally within each row (two-word shifts), then vertically
+    unsigned long long h0 = 0, h1 = 0;
+    const int r = threadIdx.x;
+    if (r < kLY) {
+      const unsigned long long lo = a0[r], hi = a1[r];
+      h0 = lo; h1 = hi;
+#pragma unroll
+      for (int sft = 1; sft <= kSH; sft++) {
+        h0 |= (lo << sft) | (lo >> sft) | (hi << (64 - sft));
+        h1 |= (hi << sft) | (hi >> sft) | (lo >> (64 - sft));
+      }
+    }
+    __syncthreads();
+    if (r < kLY) { a0[r] = h0; a1[r] = h1; }
+    __syncthreads();
+    unsigned long long v0 = 0, v1 = 0;
+    if (r < kLY) {
+      for (int k = max(0, r - kSH); k <= min(kLY - 1, r + kSH); k++) { v0 |= a0[k]; v1 |= a1[k]; }
+    }
+    __syncthreads();
+    if (r < kLY) { a0[r] = v0; a1[r] = v1; }
+    // (the staging below ends with a barrier before the border pass reads act)
+  }
   // Staging: every thread issues all of its loads before the first store, so the
   // block waits for one memory round trip, not one per element.
   {
@@ -594,9 +664,10 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       }
     }
   }
-  {
+  if (!mode) {
     // the image region as rows of 3 * kIX floats (same layout as I), in batches of
-    // 8 loads per thread
+    // 8 loads per thread (active-set sweeps score few pixels and read their colours
+    // from global memory instead)
     constexpr int kRow = 3 * kIX;
     constexpr int kNF = kIY * kRow;
     constexpr int kNI = 8;
@@ -630,7 +701,12 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
     if (i < kIX * kIY) {
       const int lx = i % kIX, ly = i / kIX;
       const int gx = ix0 + lx, gy = iy0 + ly;
-      if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      bool act = gx >= 0 && gx < W && gy >= 0 && gy < H;
+      if (act && mode) {
+        const int ax = lx + 1, ay = ly + 1;   // label-region coordinates
+        act = ((ax < 64 ? sm.act[0][ay] >> ax : sm.act[1][ay] >> (ax - 64)) & 1ull) != 0;
+      }
+      if (act) {
         bool b;
         if (gy < 1 || gx < 1 || gy >= H - 1 || gx >= W - 1) {
           b = true;
@@ -692,7 +768,7 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       const int dN = 8 - __popc(cN), dW = 8 - __popc(cW), dS = 8 - __popc(cS),
                 dE = 8 - __popc(cE);
       if (N >= cap || S >= cap || Wl >= cap || E >= cap) continue;
-      const float* pix = &I[3 * bi];
+      const float* pix = mode ? img + 3 * ((size_t)gy * W + gx) : &I[3 * bi];
       float best = -9999.f;
       int bl = C;
       if (N >= 0) joint(pix, gx, gy, rec[N], N, s2, (float)dN, potts, &best, &bl);
@@ -713,13 +789,17 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   }
   for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x) {
     int gx = tx0 + i % kTX, gy = ty0 + i / kTX;
-    if (gx < W && gy < H) seg_out[gy * W + gx] = L[(gy - ry0) * kLX + (gx - rx0)];
+    if (gx < W && gy < H) {
+      const int v = L[(gy - ry0) * kLX + (gx - rx0)];
+      seg_out[gy * W + gx] = v;
+      chg_out[gy * W + gx] = v != seg_in[gy * W + gx];
+    }
   }
 }
 
 template <int TX, int TY>
 __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B, int parity,
-                                           float s2, float potts) {
+                                           float s2, float potts, int mode) {
   __shared__ SweepTile<TX, TY> sm;
   __shared__ unsigned lut_bits[8];
   if (threadIdx.x < 8) {
@@ -737,17 +817,20 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
   const Slot& S = slots[lo];
   const int tl = t - S.tile_base[v];
   const int tiles_x = (S.W + TX - 1) / TX;
-  sweep_tile<TX, TY>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits);
+  sweep_tile<TX, TY>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits, mode);
 }
 
 // One block per tile of the batch (grid = the batch's total tile count).
+// mode 0: every border pixel (first sweep of an update_seg call); 1: active set.
 __global__ void __launch_bounds__(256) kb_sweep_t32(const Slot* __restrict__ slots, int B,
-                                                    int parity, float s2, float potts) {
-  sweep_flat<32, 32>(slots, B, parity, s2, potts);
+                                                    int parity, float s2, float potts,
+                                                    int mode) {
+  sweep_flat<32, 32>(slots, B, parity, s2, potts, mode);
 }
 __global__ void __launch_bounds__(256) kb_sweep_t64(const Slot* __restrict__ slots, int B,
-                                                    int parity, float s2, float potts) {
-  sweep_flat<64, 32>(slots, B, parity, s2, potts);
+                                                    int parity, float s2, float potts,
+                                                    int mode) {
+  sweep_flat<64, 32>(slots, B, parity, s2, potts, mode);
 }
 
 // ---------------------------------------------------------------------------

@@ -33,8 +33,10 @@ __global__ void kb_posterior(const Slot* slots);
 __global__ void kb_store_sample(const Slot* slots);
 __global__ void kb_find_border(const Slot* slots);
 // boundary sweep, one block per 32x32 / 64x32 tile of the batch
-__global__ void kb_sweep_t32(const Slot* slots, int B, int parity, float s2, float potts);
-__global__ void kb_sweep_t64(const Slot* slots, int B, int parity, float s2, float potts);
+__global__ void kb_sweep_t32(const Slot* slots, int B, int parity, float s2, float potts,
+                             int mode);
+__global__ void kb_sweep_t64(const Slot* slots, int B, int parity, float s2, float potts,
+                             int mode);
 __global__ void kb_copy_labels(const Slot* slots);
 __global__ void kb_read_params(const Slot* slots);
 __global__ void kb_save_prev(const Slot* slots);
