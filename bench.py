@@ -394,6 +394,157 @@ def run_batch_mode(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+PRECISION = dict(name="precision_4k_2160x3840", H=2160, W=3840, nseeds=2000, sp=25, niters=20,
+                 sm_period=10, frames=3)
+
+
+def total_marginal_np(n, s, q, b0, log_01_b0):
+    """The split/merge marginal of one superpixel over three channels (the engine's
+    total_marginal, FP64), vectorised: n [m], s and q [m,3]."""
+    import numpy as np
+    a_n = 1e4 + n / 2.0
+    d = 0.5 * (q - s * s / n[:, None])
+    lr = np.where(b0 + d < 0, log_01_b0, np.log1p(d / b0))
+    return (-a_n[:, None] * lr).sum(1) + 3 * (-0.5 * np.log(n) - n * (0.5 * np.log(np.pi) + np.log(2.0)))
+
+
+def run_precision(args, world, rank):
+    """--mode precision: accumulator precision study on a 4K video (2160x3840, 2000
+    Voronoi seeds, superpixel size 25): the colour sums of the statistics as int64
+    fixed point (this engine), FP32 atomics (the reference's choice) and FP64 atomics
+    (the oracle).  Same labels: per-superpixel mean and colour-scatter errors against
+    FP64 and merge Hastings accept/reject flips over all adjacent pairs; full runs:
+    label agreement of FP32 / FP64 runs with the int64 run; per-kernel GB/s at 4K."""
+    import numpy as np
+    import torch
+    from st_spix_gb300 import batch, bist_cuda, synth, _lib
+
+    torch.cuda.set_device(args.local)
+    dev = torch.device("cuda", args.local)
+    pc, w = PRECISION, WORKLOAD
+    T = pc["frames"]
+    vid, flo = synth.voronoi_video_device(pc["H"], pc["W"], T, pc["nseeds"], w["sigma"],
+                                          seed=rank, device=dev)
+    base = dict(niters=pc["niters"], sp_size=pc["sp"], potts=w["potts"], sigma2_app=w["sigma2_app"],
+                alpha=w["alpha"], split_alpha=w["split_alpha"], sm_period=pc["sm_period"],
+                prop_niters=pc["niters"])
+    ctx = bist_cuda._ctx(dev)
+    labels, secs, logs = {}, {}, {}
+    for acc in (0, 1, 2):
+        v = batch.Video(pc["H"], pc["W"], dev)
+        outs = []
+        if acc == 0:
+            ctx.profile(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for t in range(T):
+            f = batch.Frame(img=vid[t], flow=flo[t - 1] if t else None, video=v)
+            batch.process_batch([f], accumulator=acc, **base)
+            outs.append(f.labels.clone())
+        torch.cuda.synchronize()
+        secs[acc] = time.perf_counter() - t0
+        if acc == 0:
+            kern = ctx.profile_kernels()
+            ctx.profile(False)
+        labels[acc] = outs
+        v.close()
+    npix = pc["H"] * pc["W"]
+    def matched(a, b):
+        """Fraction of pixels whose label in a maps to their label in b when every
+        label of a is matched to the label of b it overlaps most."""
+        a = a.reshape(-1).long()
+        b = b.reshape(-1).long()
+        nb = int(b.max().item()) + 2
+        key = (a + 1) * nb + (b + 1)
+        uk, cnt = torch.unique(key, return_counts=True)
+        ua = uk // nb
+        best = torch.zeros(int(ua.max().item()) + 1, dtype=cnt.dtype, device=cnt.device)
+        best.scatter_reduce_(0, ua, cnt, reduce="amax")
+        return float(best.sum().item()) / a.numel()
+    agree = {name: [float((labels[a][t] == labels[0][t]).float().mean().item()) for t in range(T)]
+             for name, a in (("fp32", 1), ("fp64", 2))}
+    agree_m = {name: [matched(labels[a][t], labels[0][t]) for t in range(T)]
+               for name, a in (("fp32", 1), ("fp64", 2))}
+    # same labels, three accumulators
+    cfg0 = _lib.default_config(sigma2_app=w["sigma2_app"])
+    b0 = float(np.float32(np.float32(np.sqrt(cfg0.sigma2_app) * 2) * np.float32(1e4)))
+    log_01_b0 = np.log(0.1) - np.log(b0)
+    log_alpha = float(np.log(np.float32(np.exp(w["alpha"]))))
+    per_frame = []
+    import ctypes as C
+    for t in range(T):
+        lab = labels[0][t]
+        n = int(lab.max().item()) + 1
+        st = {}
+        for acc in (0, 1, 2):
+            out = torch.empty(7 * n, dtype=torch.float64, device=dev)
+            ctx.check(ctx.lib.stspix_label_stats(ctx.handle, bist_cuda._stream(dev), vid[t].data_ptr(),
+                                                 lab.data_ptr(), pc["H"], pc["W"], n, acc,
+                                                 out.data_ptr()))
+            st[acc] = out.view(n, 7).cpu().numpy()
+        live = st[2][:, 0] > 0
+        cnt = st[2][live, 0]
+        res = {}
+        for name, a in (("int64", 0), ("fp32", 1)):
+            mu_a = st[a][live, 1:4] / cnt[:, None]
+            mu_r = st[2][live, 1:4] / cnt[:, None]
+            scat_a = st[a][live, 4:7] - st[a][live, 1:4] ** 2 / cnt[:, None]
+            scat_r = st[2][live, 4:7] - st[2][live, 1:4] ** 2 / cnt[:, None]
+            rel_mu = np.abs(mu_a - mu_r) / np.maximum(np.abs(mu_r), 1e-12)
+            rel_sc = np.abs(scat_a - scat_r) / np.maximum(np.abs(scat_r), 1e-12)
+            res[name] = {"mean_rel_err_max": float(rel_mu.max()),
+                         "mean_rel_err_median": float(np.median(rel_mu)),
+                         "scatter_rel_err_max": float(rel_sc.max()),
+                         "scatter_rel_err_median": float(np.median(rel_sc))}
+        # merge Hastings decisions over all adjacent pairs
+        L = lab.cpu().numpy()
+        pr = np.concatenate([np.stack([L[:, :-1].ravel(), L[:, 1:].ravel()], 1),
+                             np.stack([L[:-1, :].ravel(), L[1:, :].ravel()], 1)])
+        pr = pr[(pr[:, 0] != pr[:, 1]) & (pr[:, 0] >= 0) & (pr[:, 1] >= 0)]
+        pr = np.unique(np.sort(pr, 1), axis=0)
+        dec = {}
+        for a in (0, 1, 2):
+            S = st[a]
+            na, nb_ = S[pr[:, 0], 0], S[pr[:, 1], 0]
+            ma = total_marginal_np(na, S[pr[:, 0], 1:4], S[pr[:, 0], 4:7], b0, log_01_b0)
+            mb = total_marginal_np(nb_, S[pr[:, 1], 1:4], S[pr[:, 1], 4:7], b0, log_01_b0)
+            mf = total_marginal_np(na + nb_, S[pr[:, 0], 1:4] + S[pr[:, 1], 1:4],
+                                   S[pr[:, 0], 4:7] + S[pr[:, 1], 4:7], b0, log_01_b0)
+            h = mf - (log_alpha + ma + mb)
+            dec[a] = (h > -2, h)
+        for name, a in (("int64", 0), ("fp32", 1)):
+            res[name]["merge_flips_vs_fp64"] = int((dec[a][0] != dec[2][0]).sum())
+            res[name]["hastings_abs_err_max"] = float(np.abs(dec[a][1] - dec[2][1]).max())
+        res["pairs"] = int(len(pr))
+        res["superpixels"] = int(live.sum())
+        per_frame.append(res)
+    # per-kernel bandwidth of the int64 run at 4K (CUDA events)
+    bytes_per_px = {"kb_sweep_t32": 20, "kb_sweep_t64": 20, "kb_accumulate": 16}
+    gbs = {}
+    for k, (nl, ms) in kern.items():
+        if k in bytes_per_px and ms > 0:
+            gbs[k] = {"launches": nl, "avg_us": 1000 * ms / nl,
+                      "achieved_gbs": bytes_per_px[k] * npix * nl / (ms / 1000) / 1e9}
+    peak, peak_kind = read_peaks()
+    if rank != 0:
+        return
+    line = {
+        "metric": "accumulator precision study (4K)", "value": agree_m["fp32"][-1],
+        "unit": "matched label agreement of the FP32-accumulator run with the int64 run, last frame",
+        "n_gpus": world, "steps": 1, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64+int64", "data": "synthetic",
+        "config": {"workload": pc["name"], "H": pc["H"], "W": pc["W"], "frames": T,
+                   "nseeds": pc["nseeds"], "sp_size": pc["sp"], "niters": pc["niters"],
+                   "sm_period": pc["sm_period"],
+                   "sample": "first %d frames of the 60-frame configuration" % T},
+        "label_agreement_vs_int64": {"raw": agree, "matched": agree_m},
+        "same_labels": per_frame,
+        "seconds_per_run": secs,
+        "kernel_gbs_int64_run": gbs, "hbm_peak_gbs": peak, "peak_source": peak_kind,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     faulthandler.enable(all_threads=True)
     ap = argparse.ArgumentParser()
@@ -407,10 +558,11 @@ def main():
                     help="host threads per GPU, each with its own CUDA stream, engine "
                          "context and share of the streams")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="stream", choices=["stream", "serve", "batch"],
+    ap.add_argument("--mode", default="stream", choices=["stream", "serve", "batch", "precision"],
                     help="stream: the 480x854 streaming workload (default); serve: the "
                          "serving form on mixed-resolution Poisson streams; batch: 64 "
-                         "independent frames of uneven size as one batch")
+                         "independent frames of uneven size as one batch; precision: the "
+                         "accumulator precision study at 4K")
     ap.add_argument("--max-batch", type=int, default=8, help="serve: frames per batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -422,6 +574,8 @@ def main():
         return run_serve(args, world, rank)
     if args.mode == "batch":
         return run_batch_mode(args, world, rank)
+    if args.mode == "precision":
+        return run_precision(args, world, rank)
     args.warmup = max(args.warmup, 3)
 
     import numpy as np

@@ -62,6 +62,10 @@ typedef struct stspix_config {
   float sigma2_size;     /* kept for API parity (unused by the reference path)        */
   float thresh_relabel;  /* revive a dead id when appearance distance < this          */
   float thresh_new;      /* mint a new id when self distance > this                   */
+  int   accumulator;     /* colour sums of the statistics: 0 int64 fixed point
+                            (default, exact and order-independent), 1 FP32 atomics (as
+                            the reference; order-dependent), 2 FP64 atomics -- 1 and 2
+                            exist for the accumulator precision study               */
 } stspix_config;
 
 void stspix_default_config(stspix_config* cfg);
@@ -221,6 +225,14 @@ int stspix_bass_partial(stspix_ctx* ctx, void* stream, const float* img, int H, 
                         const stspix_config* cfg, int iters, int extra_update,
                         int32_t* labels_out, stspix_state_dump* dump,
                         int* nbuf_out, int* max_spix_out);
+
+/* Sufficient statistics of a labelling (precision study): per label id < nlabels,
+ * out[7*k .. 7*k+6] = count, sum r, sum g, sum b, sum r^2, sum g^2, sum b^2 of the
+ * pixels carrying k, accumulated as `accumulator` says (0 int64 fixed point: colours
+ * 2^-28, squares 2^-20; 1 FP32 atomics; 2 FP64 atomics), returned as doubles.
+ * Synchronises the stream.                                                     */
+int stspix_label_stats(stspix_ctx* ctx, void* stream, const float* img, const int32_t* labels,
+                       int H, int W, int nlabels, int accumulator, double* out);
 
 /* ---- batched and serving forms -----------------------------------------------
  * No single reference counterpart: the reference processes one frame per call

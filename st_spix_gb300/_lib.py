@@ -22,7 +22,8 @@ class Config(C.Structure):
                 ("sigma2_app", C.c_float), ("potts", C.c_float),
                 ("alpha_hastings", C.c_float), ("split_alpha", C.c_float),
                 ("merge_alpha", C.c_float), ("sigma2_size", C.c_float),
-                ("thresh_relabel", C.c_float), ("thresh_new", C.c_float)]
+                ("thresh_relabel", C.c_float), ("thresh_new", C.c_float),
+                ("accumulator", C.c_int)]
 
 
 class ParamsC(C.Structure):
@@ -68,7 +69,8 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_profile_get", "stspix_frame_times", "stspix_get_marked_video_noalloc",
            "stspix_video_create", "stspix_video_destroy", "stspix_video_reset",
            "stspix_video_nspix", "stspix_video_frames", "stspix_process_batch",
-           "stspix_footprint", "stspix_last_batch_ms", "stspix_profile_kernels"]
+           "stspix_footprint", "stspix_last_batch_ms", "stspix_profile_kernels",
+           "stspix_label_stats"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -124,6 +126,7 @@ def load(build_if_missing: bool = True):
                                      C.POINTER(C.c_longlong)]),
             "stspix_last_batch_ms": (C.c_double, [P]),
             "stspix_profile_kernels": (I, [P, C.c_char_p, I]),
+            "stspix_label_stats": (I, [P, P, P, P, I, I, I, I, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

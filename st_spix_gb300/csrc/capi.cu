@@ -114,6 +114,7 @@ struct stspix_ctx {
   std::map<std::pair<unsigned long long, int>, int> sweep_choice;  // (shape, nb) -> variant
   cudaEvent_t tune_ev[3] = {nullptr, nullptr, nullptr};
   long long tunes = 0;
+  int accumulator = 0;            // cfg.accumulator of the batch being run
   int* body_iters = nullptr;       // device: fill-loop iterations run (launch count)
   int* body_iters_host = nullptr;  // pinned
   long long body_iters_seen = 0;
@@ -423,7 +424,10 @@ void preload_kernels() {
       (const void*)kb_relabel_params,
       (const void*)kb_relabel_apply,
       (const void*)kb_relabel_end,
-      (const void*)kb_count_revived};
+      (const void*)kb_count_revived,
+      (const void*)kb_accumulate_fp, (const void*)kb_accumulate_fp_store,
+      (const void*)kb_accumulate_fp_clear, (const void*)k_label_stats,
+      (const void*)k_label_stats_out};
     for (const void* f : fns) {
       cudaFuncAttributes a;
       cudaError_t e = cudaFuncGetAttributes(&a, f);
@@ -558,10 +562,19 @@ unsigned acc_blocks(const stspix_ctx* ctx, const List& L, int nb) {
 }
 
 // update_params (update_params.cu:12-52): statistics + posterior.
+// The colour sums by FP32 / FP64 atomics instead of int64 fixed point (accumulator
+// precision study, cfg.accumulator 1 / 2).
+void accumulate_fp(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, int mode) {
+  LAUNCHB(kb_accumulate_fp_clear, L.max_cap, L, nb);
+  LAUNCHB(kb_accumulate_fp, L.max_npix, L, nb, mode);
+  LAUNCHB(kb_accumulate_fp_store, L.max_cap, L, nb, mode);
+}
+
 int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb) {
   ctx->cur_fam = STSPIX_FAM_STATS;
   LAUNCHB(kb_clear_stats, L.max_cap, L, nb);
   LAUNCHG(kb_accumulate, acc_blocks(ctx, L, nb), 256, L.d, nb);
+  if (ctx->accumulator) accumulate_fp(ctx, st, L, nb, ctx->accumulator);
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
   LAUNCHB(kb_posterior, L.max_cap, L, nb);
   return STSPIX_OK;
@@ -750,6 +763,7 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHB(kb_init_bass_params, L.max_cap, L, L.B);
   LAUNCHB(kb_clear_stats, L.max_cap, L, L.B);
   LAUNCHG(kb_accumulate, acc_blocks(ctx, L, L.B), 256, L.d, L.B);
+  if (ctx->accumulator) accumulate_fp(ctx, st, L, L.B, ctx->accumulator);
   LAUNCHB(kb_init_prior_mu, L.max_cap, L, L.B);
   LAUNCHB(kb_find_border, L.max_npix, L, L.B);
   return STSPIX_OK;
@@ -906,6 +920,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
               int extra_update = 0) {
   const int B = (int)fr.size();
   int r;
+  ctx->accumulator = cfg.accumulator;
   if ((r = ensure_bcap(ctx, B))) return r;
   std::vector<int> caps(B);
   for (int i = 0; i < B; i++) {
@@ -991,6 +1006,8 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
 
 int check_cfg(stspix_ctx* ctx, const stspix_config* cfg) {
   if (!cfg) return fail(ctx, STSPIX_ERR_ARG, "config is NULL");
+  if (cfg->accumulator < 0 || cfg->accumulator > 2)
+    return fail(ctx, STSPIX_ERR_ARG, "accumulator must be 0, 1 or 2");
   if (cfg->sp_size < 1) return fail(ctx, STSPIX_ERR_ARG, "sp_size must be >= 1");
   if (cfg->niters < 0 || cfg->niters_seg < 0)
     return fail(ctx, STSPIX_ERR_ARG, "iteration counts must be >= 0");
@@ -1095,6 +1112,7 @@ void stspix_default_config(stspix_config* c) {
   c->sigma2_app = 0.009f * 0.009f; c->potts = 0.5f; c->alpha_hastings = (float)log(0.5);
   c->split_alpha = 0.f; c->merge_alpha = 0.f; c->sigma2_size = 0.f;
   c->thresh_relabel = 1e-5f; c->thresh_new = 1e-2f;
+  c->accumulator = 0;
 }
 
 int stspix_version(void) { return 2; }
@@ -1476,6 +1494,35 @@ int stspix_footprint(int H, int W, int sp_size, long long* video_bytes, long lon
 }
 
 double stspix_last_batch_ms(const stspix_ctx* ctx) { return ctx ? ctx->batch_ms : -1.0; }
+
+int stspix_label_stats(stspix_ctx* ctx, void* stream, const float* img, const int32_t* labels,
+                       int H, int W, int nlabels, int accumulator, double* out) {
+  if (!ctx || !img || !labels || !out || nlabels < 1 || accumulator < 0 || accumulator > 2)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  int r;
+  if ((r = check_size(ctx, H, W))) return r;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n7 = 7 * (size_t)nlabels;
+  long long* iacc = nullptr;
+  float* facc = nullptr;
+  double* dacc = nullptr;
+  CK(cudaMallocAsync((void**)&iacc, sizeof(long long) * n7, st));
+  CK(cudaMallocAsync((void**)&facc, sizeof(float) * n7, st));
+  CK(cudaMallocAsync((void**)&dacc, sizeof(double) * n7, st));
+  CK(cudaMemsetAsync(iacc, 0, sizeof(long long) * n7, st));
+  CK(cudaMemsetAsync(facc, 0, sizeof(float) * n7, st));
+  CK(cudaMemsetAsync(dacc, 0, sizeof(double) * n7, st));
+  const long long npix = (long long)H * W;
+  LAUNCH(k_label_stats, npix, img, labels, npix, nlabels, accumulator, iacc, facc, dacc);
+  LAUNCH(k_label_stats_out, nlabels, nlabels, accumulator, iacc, facc, dacc, out);
+  CK(cudaFreeAsync(iacc, st));
+  CK(cudaFreeAsync(facc, st));
+  CK(cudaFreeAsync(dacc, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
 
 int stspix_profile_enable(stspix_ctx* ctx, int enable) {
   if (!ctx) return STSPIX_ERR_ARG;

@@ -314,6 +314,85 @@ __global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ sl
   }
 }
 
+// Accumulator precision study: colour sums by per-pixel FP32 (mode 1, as the
+// reference's sum_by_label, update_params.cu:115-117) or FP64 (mode 2) atomics into
+// a scratch array (the compaction buffer's sums), then written over the int64 colour
+// sums in 2^-28 units (exact for the magnitudes of colour sums), so the posterior sees
+// the precision of that accumulator.  Counts and positions stay exact.
+__global__ void kb_accumulate_fp(const Slot* __restrict__ slots, int mode) {
+  SLOT_Y;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.npix) return;
+  const int k = S.seg[t];
+  if (k < 0 || k >= S.sp.cap) return;
+  const float* p = S.img + 3 * (size_t)t;
+  if (mode == 1) {
+    float* f = (float*)S.tmp.acc;
+    for (int c = 0; c < 3; c++) atomicAdd(&f[3 * (size_t)k + c], p[c]);
+  } else {
+    double* d = (double*)S.tmp.acc;
+    for (int c = 0; c < 3; c++) atomicAdd(&d[3 * (size_t)k + c], (double)p[c]);
+  }
+}
+
+__global__ void kb_accumulate_fp_store(const Slot* __restrict__ slots, int mode) {
+  SLOT_Y;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S.sp.cap) return;
+  for (int c = 0; c < 3; c++) {
+    const double v = mode == 1 ? (double)((const float*)S.tmp.acc)[3 * (size_t)k + c]
+                               : ((const double*)S.tmp.acc)[3 * (size_t)k + c];
+    S.sp.acc[8 * (size_t)k + c] = __double2ll_rn(ldexp(v, kFxAppShift));
+  }
+}
+
+__global__ void kb_accumulate_fp_clear(const Slot* __restrict__ slots) {
+  SLOT_Y;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S.sp.cap) return;
+  double* d = (double*)S.tmp.acc;
+  for (int c = 0; c < 3; c++) d[3 * (size_t)k + c] = 0.0;
+}
+
+// Statistics of a labelling with a chosen accumulator (study entry point).
+__global__ void k_label_stats(const float* __restrict__ img, const int* __restrict__ lab,
+                              long long npix, int n, int mode, long long* iacc, float* facc,
+                              double* dacc) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npix) return;
+  const int k = lab[t];
+  if (k < 0 || k >= n) return;
+  const float* p = img + 3 * t;
+  atomicAdd((unsigned long long*)&iacc[7 * (size_t)k], 1ull);
+  for (int c = 0; c < 3; c++) {
+    const float v = p[c];
+    if (mode == 0) {
+      atomicAdd((unsigned long long*)&iacc[7 * (size_t)k + 1 + c], (unsigned long long)fx_q(v, kFxAppShift));
+      atomicAdd((unsigned long long*)&iacc[7 * (size_t)k + 4 + c], (unsigned long long)fx_q(v * v, kFxSqShift));
+    } else if (mode == 1) {
+      atomicAdd(&facc[7 * (size_t)k + 1 + c], v);
+      atomicAdd(&facc[7 * (size_t)k + 4 + c], v * v);
+    } else {
+      atomicAdd(&dacc[7 * (size_t)k + 1 + c], (double)v);
+      atomicAdd(&dacc[7 * (size_t)k + 4 + c], (double)v * (double)v);
+    }
+  }
+}
+
+__global__ void k_label_stats_out(int n, int mode, const long long* iacc, const float* facc,
+                                  const double* dacc, double* out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  out[7 * (size_t)k] = (double)iacc[7 * (size_t)k];
+  for (int c = 1; c < 7; c++) {
+    double v;
+    if (mode == 0) v = ldexp((double)iacc[7 * (size_t)k + c], c < 4 ? -kFxAppShift : -kFxSqShift);
+    else if (mode == 1) v = facc[7 * (size_t)k + c];
+    else v = dacc[7 * (size_t)k + c];
+    out[7 * (size_t)k + c] = v;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Posterior (calc_simple_update, update_params.cu:220-381, with
 // _add_sigma_smoothing :206-217) + clear_fields semantics for dead ids.

@@ -30,6 +30,13 @@ __global__ void kb_init_prior_mu(const Slot* slots);
 __global__ void kb_clear_stats(const Slot* slots);
 __global__ void kb_accumulate(const Slot* slots, int B);
 __global__ void kb_posterior(const Slot* slots);
+__global__ void kb_accumulate_fp(const Slot* slots, int mode);
+__global__ void kb_accumulate_fp_store(const Slot* slots, int mode);
+__global__ void kb_accumulate_fp_clear(const Slot* slots);
+__global__ void k_label_stats(const float* img, const int* lab, long long npix, int n, int mode,
+                              long long* iacc, float* facc, double* dacc);
+__global__ void k_label_stats_out(int n, int mode, const long long* iacc, const float* facc,
+                                  const double* dacc, double* out);
 __global__ void kb_store_sample(const Slot* slots);
 __global__ void kb_find_border(const Slot* slots);
 // boundary sweep, one block per 32x32 / 64x32 tile of the batch
