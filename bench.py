@@ -394,6 +394,51 @@ def run_batch_mode(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+IMAGE = dict(name="bass_image_240x320", H=240, W=320, nseeds=200, sigma=0.05, sp=15, niters=100,
+             sm_period=20)
+
+
+def run_image(args, world, rank):
+    """--mode image: plain BASS on one 240x320 Voronoi frame (200 seeds, noise 0.05,
+    superpixel size 15, 100 iterations, split/merge every 20), one frame per call
+    (run_bass), against the oracle on the same frame on one host core."""
+    import numpy as np
+    import torch
+    from oracle import oracle as O
+    from st_spix_gb300 import bist_cuda, synth
+
+    torch.cuda.set_device(args.local)
+    dev = torch.device("cuda", args.local)
+    im = IMAGE
+    img, _ = synth.voronoi_frame(im["H"], im["W"], im["nseeds"], im["sigma"], seed=rank)
+    g = torch.from_numpy(img).to(dev)
+    kw = dict(niters=im["niters"], sp_size=im["sp"], sm_period=im["sm_period"])
+    for _ in range(args.warmup):
+        lab, _ = bist_cuda.run_bass(g, **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lab, params = bist_cuda.run_bass(g, **kw)
+    torch.cuda.synchronize()
+    el = (time.perf_counter() - t0) / args.steps
+    O.build()
+    t0 = time.perf_counter()
+    st, olab, _, n = O.run_bass(img, O.default_config(**kw))
+    cpu = time.perf_counter() - t0
+    same = bool(np.array_equal(olab, lab.cpu().numpy()))
+    if rank != 0:
+        return
+    line = {"metric": "frames/sec (plain BASS, one 240x320 frame per call)", "value": 1.0 / el,
+            "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * el, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/f64+int64", "data": "synthetic",
+            "config": {"workload": im["name"], **{k: im[k] for k in ("H", "W", "nseeds", "sigma", "sp", "niters", "sm_period")}},
+            "nspix": int(params.n), "labels_identical_to_oracle": same,
+            "cpu_baseline": {"value": 1.0 / cpu, "unit": "frames/s", "cores": 1, "kind": "port",
+                             "sample": "the same frame, oracle (CPU restatement), one core"}}
+    print(json.dumps(line), flush=True)
+
+
 PRECISION = dict(name="precision_4k_2160x3840", H=2160, W=3840, nseeds=2000, sp=25, niters=20,
                  sm_period=10, frames=3)
 
@@ -558,11 +603,13 @@ def main():
                     help="host threads per GPU, each with its own CUDA stream, engine "
                          "context and share of the streams")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="stream", choices=["stream", "serve", "batch", "precision"],
+    ap.add_argument("--mode", default="stream",
+                    choices=["stream", "serve", "batch", "precision", "image"],
                     help="stream: the 480x854 streaming workload (default); serve: the "
                          "serving form on mixed-resolution Poisson streams; batch: 64 "
                          "independent frames of uneven size as one batch; precision: the "
-                         "accumulator precision study at 4K")
+                         "accumulator precision study at 4K; image: plain BASS on one "
+                         "240x320 frame")
     ap.add_argument("--max-batch", type=int, default=8, help="serve: frames per batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -576,6 +623,8 @@ def main():
         return run_batch_mode(args, world, rank)
     if args.mode == "precision":
         return run_precision(args, world, rank)
+    if args.mode == "image":
+        return run_image(args, world, rank)
     args.warmup = max(args.warmup, 3)
 
     import numpy as np

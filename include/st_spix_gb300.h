@@ -16,6 +16,8 @@
  *   stspix_run_prop            st_spix/csrc/bist/prop.cu:677  run_prop
  *   stspix_find_border         st_spix/csrc/bist/seg_utils.cu:156,211 CudaFindBorderPixels(_end)
  *   stspix_init_seg            st_spix/csrc/bist/init_seg.cu:20 init_seg
+ *   stspix_rgb2lab/_lab2rgb    st_spix/csrc/bist/rgb2lab.cu:39,46 rgb2lab / lab2rgb
+ *   stspix_rescale_u8          st_spix/csrc/bist/rgb2lab.cu:21 rescale_image
  *   stspix_bass_partial        st_spix/csrc/bist/bass.cu:46 bass() stopped after k iterations
  *                              (exposes update_params.cu:12 and update_seg.cu:281 state)
  */
@@ -225,6 +227,17 @@ int stspix_bass_partial(stspix_ctx* ctx, void* stream, const float* img, int H, 
                         const stspix_config* cfg, int iters, int extra_update,
                         int32_t* labels_out, stspix_state_dump* dump,
                         int* nbuf_out, int* max_spix_out);
+
+/* ---- colour front end (rgb2lab.cu; not called by bist_forward) ----------------
+ * rgb2lab: f32 [npix,3] (first channel read as blue, as the reference) -> CIELAB
+ * stored as (L/-100, a/100, b/100) (rgb2lab.cu:51-122); lab2rgb: the inverse
+ * (rgb2lab.cu:124-181); rescale_u8: u8 values -> f32 value/scale
+ * (rgb2lab.cu:184 rescale_image_kernel).  Pixels with a NaN channel are left
+ * unwritten, as in the reference.                                              */
+int stspix_rgb2lab(stspix_ctx* ctx, void* stream, const float* rgb, float* lab, long long npix);
+int stspix_lab2rgb(stspix_ctx* ctx, void* stream, const float* lab, float* rgb, long long npix);
+int stspix_rescale_u8(stspix_ctx* ctx, void* stream, const uint8_t* in, float* out,
+                      long long nvals, float scale);
 
 /* Sufficient statistics of a labelling (precision study): per label id < nlabels,
  * out[7*k .. 7*k+6] = count, sum r, sum g, sum b, sum r^2, sum g^2, sum b^2 of the

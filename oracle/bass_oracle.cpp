@@ -1220,6 +1220,7 @@ void oracle_default_config(stspix_config* c) {
   c->sigma2_app = 0.009f * 0.009f; c->potts = 0.5f; c->alpha_hastings = (float)log(0.5);
   c->split_alpha = 0.f; c->merge_alpha = 0.f; c->sigma2_size = 0.f;
   c->thresh_relabel = 1e-5f; c->thresh_new = 1e-2f;
+  c->accumulator = 0;
 }
 
 int oracle_hex_count(int H, int W, int sp_size) {
@@ -1477,6 +1478,64 @@ void oracle_cc_roots(const int32_t* seg, int H, int W, int32_t* roots) {
       }
   }
   for (int i = 0; i < npix; i++) roots[i] = find(i);
+}
+
+// rgb2lab / lab2rgb / rescale_image_kernel (rgb2lab.cu:51-198), restated on the host:
+// first channel read as blue, FP64 arithmetic with every power through the FP32 powf,
+// L stored / -100 and a, b / 100, NaN pixels left unwritten.
+void oracle_rgb2lab(const float* rgb, float* lab, long long npix) {
+  for (long long t = 0; t < npix; t++) {
+    double sB = rgb[3 * t], sG = rgb[3 * t + 1], sR = rgb[3 * t + 2];
+    if (sR != sR || sG != sG || sB != sB) continue;
+    auto lin = [](double c) {
+      return c <= 0.04045 ? c / 12.92 : (double)powf((float)((c + 0.055) / 1.055), 2.4f);
+    };
+    double r = lin(sR), g = lin(sG), b = lin(sB);
+    double X = r * 0.4124564 + g * 0.3575761 + b * 0.1804375;
+    double Y = r * 0.2126729 + g * 0.7151522 + b * 0.0721750;
+    double Z = r * 0.0193339 + g * 0.1191920 + b * 0.9503041;
+    auto f = [](double v) {
+      return v > 0.008856 ? (double)powf((float)v, (float)(1.0 / 3.0)) : (903.3 * v + 16.0) / 116.0;
+    };
+    double fx = f(X / 0.950456), fy = f(Y / 1.0), fz = f(Z / 1.088754);
+    float lval = (float)(116.0 * fy - 16.0), aval = (float)(500.0 * (fx - fy)),
+          bval = (float)(200.0 * (fy - fz));
+    lab[3 * t] = lval / (-100);
+    lab[3 * t + 1] = aval / 100;
+    lab[3 * t + 2] = bval / 100;
+  }
+}
+
+void oracle_lab2rgb(const float* lab, float* rgb, long long npix) {
+  for (long long t = 0; t < npix; t++) {
+    double L = lab[3 * t] * (-100), La = lab[3 * t + 1] * 100, Lb = lab[3 * t + 2] * 100;
+    if (L != L || La != La || Lb != Lb) continue;
+    double fy = (L + 16) / 116, fx = La / 500 + fy, fz = fy - Lb / 200;
+    auto inv = [](double v) {
+      double c = (double)powf((float)v, 3.0f);
+      return c > 0.008856 ? c : (v - 16.0 / 116.0) / 7.787;
+    };
+    double x = inv(fx), y = inv(fy), z = inv(fz);
+    double X = 0.950456 * x, Y = 1.000 * y, Z = 1.088754 * z;
+    double R = X * 3.2406 + Y * (-1.5372) + Z * (-0.4986);
+    double G = X * -0.9689 + Y * 1.8758 + Z * 0.0415;
+    double B = X * 0.0557 + Y * (-0.2040) + Z * 1.0570;
+    auto gam = [](double c) {
+      return c > 0.0031308 ? 1.055 * ((double)powf((float)c, (float)(1.0 / 2.4))) - 0.055 : 12.92 * c;
+    };
+    double r = gam(R), g = gam(G), b = gam(B);
+    float px = (float)std::fmin(1.0, b), py = (float)std::fmin(1.0, g), pz = (float)std::fmin(1.0, r);
+    px = (float)std::fmax(0.0, (double)px);
+    py = (float)std::fmax(0.0, (double)py);
+    pz = (float)std::fmax(0.0, (double)pz);
+    rgb[3 * t] = pz;
+    rgb[3 * t + 1] = py;
+    rgb[3 * t + 2] = px;
+  }
+}
+
+void oracle_rescale_u8(const uint8_t* in, float* out, long long nvals, float mval) {
+  for (long long t = 0; t < nvals; t++) out[t] = float(in[t] / mval);
 }
 
 }  // extern "C"

@@ -38,7 +38,8 @@ class Config(C.Structure):
                 ("sigma2_app", C.c_float), ("potts", C.c_float),
                 ("alpha_hastings", C.c_float), ("split_alpha", C.c_float),
                 ("merge_alpha", C.c_float), ("sigma2_size", C.c_float),
-                ("thresh_relabel", C.c_float), ("thresh_new", C.c_float)]
+                ("thresh_relabel", C.c_float), ("thresh_new", C.c_float),
+                ("accumulator", C.c_int)]
 
 
 class ParamsC(C.Structure):
@@ -309,4 +310,26 @@ def cc_roots(seg):
     seg = np.ascontiguousarray(seg, np.int32)
     out = np.zeros(seg.shape, np.int32)
     lib().oracle_cc_roots(_p(seg), seg.shape[0], seg.shape[1], _p(out))
+    return out
+
+
+def rgb2lab(rgb):
+    """rgb2lab.cu:51-122 restated (first channel read as blue; L/-100, a/100, b/100)."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    out = rgb.copy()
+    lib().oracle_rgb2lab(_p(rgb), _p(out), C.c_longlong(rgb.size // 3))
+    return out
+
+
+def lab2rgb(lab):
+    lab = np.ascontiguousarray(lab, np.float32)
+    out = lab.copy()
+    lib().oracle_lab2rgb(_p(lab), _p(out), C.c_longlong(lab.size // 3))
+    return out
+
+
+def rescale_u8(img, scale=255.0):
+    img = np.ascontiguousarray(img, np.uint8)
+    out = np.empty(img.shape, np.float32)
+    lib().oracle_rescale_u8(_p(img), _p(out), C.c_longlong(img.size), C.c_float(scale))
     return out

@@ -27,7 +27,7 @@ OUT = os.path.join(HERE, "_ref")
 REF = os.environ.get("STSPIX_REFERENCE", "/root/reference")
 BIST = os.path.join(REF, "st_spix", "csrc", "bist")
 UNITS = ["update_seg", "seg_utils", "update_params", "init_seg", "split_merge",
-         "fill_missing", "split_disconnected"]
+         "fill_missing", "split_disconnected", "rgb2lab"]
 FIELDS = ["mu_app", "prior_mu_app", "mu_shape", "sigma_shape", "prior_mu_shape",
           "prior_sigma_shape", "sample_sigma_shape", "prior_icov", "logdet_sigma_shape",
           "count", "icount", "prior_count", "valid", "prop"]

@@ -46,11 +46,15 @@ Fn g_fn[] = {
     {"fill_missing", "_Z21update_missing_seg_nnPiPdPbiiiiiib", nullptr},
     {"fill_missing", "_Z25find_border_along_missingPKiPbiiiPi", nullptr},
     {"split_disconnected", "_Z13find_spix_minPiS_S_S_iii", nullptr},
+    {"rgb2lab", "_Z10rgb_to_labPfS_i", nullptr},
+    {"rgb2lab", "_Z10lab_to_rgbPfS_i", nullptr},
+    {"rgb2lab", "_Z20rescale_image_kernelPhPfif", nullptr},
 };
 enum { F_BORDER, F_BORDER_END, F_UPDATE_SUBSET, F_CLEAR, F_SUM, F_SIMPLE_UPDATE, F_HEX_CENTER,
-       F_HEX_SEG, F_SPLIT_CAND, F_INIT_SPLIT, F_FILL_NN, F_FILL_BORDER, F_SPIX_MIN };
+       F_HEX_SEG, F_SPLIT_CAND, F_INIT_SPLIT, F_FILL_NN, F_FILL_BORDER, F_SPIX_MIN, F_RGB2LAB,
+       F_LAB2RGB, F_RESCALE };
 const char* kModules[] = {"seg_utils", "update_seg", "update_params", "init_seg", "split_merge",
-                          "fill_missing", "split_disconnected"};
+                          "fill_missing", "split_disconnected", "rgb2lab"};
 constexpr int kHelperSize = 96;  // sizeof(spix_helper): float3, double3, longlong2, longlong3
 
 #define CU(call)                                                      \
@@ -115,7 +119,9 @@ int refh_init(const char* dir) {
   CU(cuDeviceGet(&dev, 0));
   CU(cuDevicePrimaryCtxRetain(&g_ctx, dev));
   CU(cuCtxSetCurrent(g_ctx));
-  for (int m = 0; m < 7; m++) {
+  constexpr int kNumModules = (int)(sizeof(kModules) / sizeof(kModules[0]));
+  static_assert(kNumModules <= (int)(sizeof(g_mod) / sizeof(g_mod[0])), "module table too small");
+  for (int m = 0; m < kNumModules; m++) {
     std::string path = std::string(dir) + "/" + kModules[m] + ".cubin";
     CU(cuModuleLoad(&g_mod[m], path.c_str()));
   }
@@ -319,6 +325,37 @@ int refh_cc_roots(const int32_t* seg, int H, int W, int32_t* roots) {
   }
   CU(cuMemcpyDtoH(roots, cur.p, 4 * (size_t)npix));
   return steps;
+}
+
+// rgb_to_lab / lab_to_rgb (one batch); the input is copied, the output starts as a
+// copy of the input (the kernels leave NaN pixels unwritten).
+int refh_color(int which, const float* in, float* out, int npix) {
+  CU(cuCtxSetCurrent(g_ctx));
+  Dev a, b;
+  if (alloc(a, 12 * (size_t)npix) || alloc(b, 12 * (size_t)npix)) return -1;
+  CU(cuMemcpyHtoD(a.p, in, 12 * (size_t)npix));
+  CU(cuMemcpyHtoD(b.p, in, 12 * (size_t)npix));
+  // rgb_to_lab(img_rgb, img_lab, npix); lab_to_rgb(img_rgb, img_lab, npix)
+  void* args_fwd[] = {&a.p, &b.p, &npix};
+  void* args_inv[] = {&b.p, &a.p, &npix};
+  if (launch(which == 0 ? F_RGB2LAB : F_LAB2RGB, nblk(npix), 512,
+             which == 0 ? args_fwd : args_inv))
+    return -1;
+  CU(cuCtxSynchronize());
+  CU(cuMemcpyDtoH(out, b.p, 12 * (size_t)npix));
+  return 0;
+}
+
+int refh_rescale(const uint8_t* in, float* out, int npix, float mval) {
+  CU(cuCtxSetCurrent(g_ctx));
+  Dev a, b;
+  if (alloc(a, 3 * (size_t)npix) || alloc(b, 12 * (size_t)npix)) return -1;
+  CU(cuMemcpyHtoD(a.p, in, 3 * (size_t)npix));
+  void* args[] = {&a.p, &b.p, &npix, &mval};
+  if (launch(F_RESCALE, nblk(npix), 512, args)) return -1;
+  CU(cuCtxSynchronize());
+  CU(cuMemcpyDtoH(out, b.p, 12 * (size_t)npix));
+  return 0;
 }
 
 }  // extern "C"

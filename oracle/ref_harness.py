@@ -135,3 +135,26 @@ def cc_roots(seg):
     out = np.zeros(seg.shape, np.int32)
     _check(lib().refh_cc_roots(_p(seg), seg.shape[0], seg.shape[1], _p(out)))
     return out
+
+
+def rgb2lab(rgb):
+    """The reference's rgb_to_lab kernel on a copy of `rgb` (f32 [...,3])."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    out = np.empty_like(rgb)
+    _check(lib().refh_color(0, _p(rgb), _p(out), rgb.size // 3))
+    return out
+
+
+def lab2rgb(lab):
+    """The reference's lab_to_rgb kernel (writes the RGB image from a LAB image)."""
+    lab = np.ascontiguousarray(lab, np.float32)
+    out = np.empty_like(lab)
+    _check(lib().refh_color(1, _p(lab), _p(out), lab.size // 3))
+    return out
+
+
+def rescale_u8(img, mval=255.0):
+    img = np.ascontiguousarray(img, np.uint8)
+    out = np.empty(img.shape, np.float32)
+    _check(lib().refh_rescale(_p(img), _p(out), img.size // 3, C.c_float(mval)))
+    return out

@@ -214,3 +214,38 @@ def frame_log(device=None) -> _lib.FrameLog:
 def kernel_launches(device=None) -> int:
     dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
     return _ctx(dev).launches()
+
+
+# ---------------------------------------------------------------------------
+# Colour front end (rgb2lab.cu; the reference's frame pipeline, not bist_forward).
+def rgb2lab(img: torch.Tensor) -> torch.Tensor:
+    """f32 [...,3] (first channel read as blue, as the reference) -> CIELAB stored as
+    (L/-100, a/100, b/100), rgb2lab.cu:51-122."""
+    _check_input(img, "img")
+    out = img.clone()
+    ctx = _ctx(img.device)
+    ctx.check(ctx.lib.stspix_rgb2lab(ctx.handle, _stream(img.device), img.data_ptr(),
+                                     out.data_ptr(), img.numel() // 3))
+    return out
+
+
+def lab2rgb(lab: torch.Tensor) -> torch.Tensor:
+    """The inverse of rgb2lab (rgb2lab.cu:124-181), clamped to [0, 1]."""
+    _check_input(lab, "lab")
+    out = lab.clone()
+    ctx = _ctx(lab.device)
+    ctx.check(ctx.lib.stspix_lab2rgb(ctx.handle, _stream(lab.device), lab.data_ptr(),
+                                     out.data_ptr(), lab.numel() // 3))
+    return out
+
+
+def rescale_u8(img: torch.Tensor, scale: float = 255.0) -> torch.Tensor:
+    """u8 frames -> f32 value / scale (rgb2lab.cu:184 rescale_image_kernel)."""
+    _check_input(img, "img")
+    if img.dtype != torch.uint8:
+        raise RuntimeError("img must be uint8")
+    out = torch.empty(img.shape, dtype=torch.float32, device=img.device)
+    ctx = _ctx(img.device)
+    ctx.check(ctx.lib.stspix_rescale_u8(ctx.handle, _stream(img.device), img.data_ptr(),
+                                        out.data_ptr(), img.numel(), float(scale)))
+    return out

@@ -427,7 +427,8 @@ void preload_kernels() {
       (const void*)kb_count_revived,
       (const void*)kb_accumulate_fp, (const void*)kb_accumulate_fp_store,
       (const void*)kb_accumulate_fp_clear, (const void*)k_label_stats,
-      (const void*)k_label_stats_out};
+      (const void*)k_label_stats_out,
+      (const void*)k_rgb2lab, (const void*)k_lab2rgb, (const void*)k_rescale_u8};
     for (const void* f : fns) {
       cudaFuncAttributes a;
       cudaError_t e = cudaFuncGetAttributes(&a, f);
@@ -1494,6 +1495,37 @@ int stspix_footprint(int H, int W, int sp_size, long long* video_bytes, long lon
 }
 
 double stspix_last_batch_ms(const stspix_ctx* ctx) { return ctx ? ctx->batch_ms : -1.0; }
+
+int stspix_rgb2lab(stspix_ctx* ctx, void* stream, const float* rgb, float* lab,
+                   long long npix) {
+  if (!ctx || !rgb || !lab || npix < 0) return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  LAUNCH(k_rgb2lab, npix, rgb, lab, npix);
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_lab2rgb(stspix_ctx* ctx, void* stream, const float* lab, float* rgb,
+                   long long npix) {
+  if (!ctx || !rgb || !lab || npix < 0) return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  LAUNCH(k_lab2rgb, npix, lab, rgb, npix);
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_rescale_u8(stspix_ctx* ctx, void* stream, const uint8_t* in, float* out,
+                      long long nvals, float scale) {
+  if (!ctx || !in || !out || nvals < 0 || !(scale != 0.f))
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  LAUNCH(k_rescale_u8, nvals, in, out, nvals, scale);
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
 
 int stspix_label_stats(stspix_ctx* ctx, void* stream, const float* img, const int32_t* labels,
                        int H, int W, int nlabels, int accumulator, double* out) {

@@ -103,4 +103,9 @@ __global__ void kb_relabel_apply(const Slot* slots);
 __global__ void kb_relabel_end(const Slot* slots, int B);
 __global__ void kb_count_revived(const Slot* slots);
 
+// k_color.cu
+__global__ void k_rgb2lab(const float* rgb, float* lab, long long npix);
+__global__ void k_lab2rgb(const float* lab, float* rgb, long long npix);
+__global__ void k_rescale_u8(const uint8_t* in, float* out, long long nvals, float mval);
+
 }  // namespace stspix

@@ -15,7 +15,7 @@ HEADER = os.path.join(ROOT, "include", "st_spix_gb300.h")
 def declared_symbols():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(stspix_[a-z_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(stspix_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_header_lists_expected_entry_points():

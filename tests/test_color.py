@@ -1,0 +1,41 @@
+"""Colour front end (rgb2lab.cu): the engine against the oracle (host powf vs device
+powf: a few ulps), round trips, 8-bit ingest; known answers on the CPU."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_oracle_known_colours():
+    white = np.ones((1, 3), np.float32)
+    black = np.zeros((1, 3), np.float32)
+    lw = O.rgb2lab(white)[0]
+    lb = O.rgb2lab(black)[0]
+    # L stored divided by -100: white -> -1, black -> 0; neutral a, b ~ 0
+    assert abs(lw[0] + 1.0) < 1e-4 and abs(lw[1]) < 1e-3 and abs(lw[2]) < 1e-3
+    np.testing.assert_allclose(lb, 0.0, atol=1e-6)
+    # the first channel is read as blue: pure "R" in the first slot is blue-ish (b < 0)
+    blue_first = O.rgb2lab(np.array([[1, 0, 0]], np.float32))[0]
+    assert blue_first[2] < -0.5
+    np.testing.assert_allclose(O.lab2rgb(O.rgb2lab(white)), white, atol=2e-3)
+    np.testing.assert_array_equal(O.rescale_u8(np.array([[0, 128, 255]], np.uint8)),
+                                  np.array([[0, 128 / 255.0, 1.0]], np.float32))
+
+
+@pytest.mark.gpu
+def test_color_kernels_match_oracle():
+    torch = pytest.importorskip("torch")
+    from st_spix_gb300 import bist_cuda
+    rng = np.random.default_rng(0)
+    rgb = rng.uniform(0, 1, size=(64, 80, 3)).astype(np.float32)
+    rgb[0, 0] = [0.0, 0.04045, 1.0]          # branch edges
+    g = torch.from_numpy(rgb).cuda()
+    lab = bist_cuda.rgb2lab(g).cpu().numpy()
+    np.testing.assert_allclose(lab, O.rgb2lab(rgb), rtol=1e-5, atol=1e-6)
+    back = bist_cuda.lab2rgb(torch.from_numpy(lab).cuda()).cpu().numpy()
+    np.testing.assert_allclose(back, O.lab2rgb(lab), rtol=1e-5, atol=1e-6)
+    # rgb2lab reads (B, G, R), lab2rgb writes (R, G, B): a round trip reverses channels
+    np.testing.assert_allclose(back, rgb[..., ::-1], atol=2e-3)
+    u8 = rng.integers(0, 256, size=(32, 48, 3)).astype(np.uint8)
+    f = bist_cuda.rescale_u8(torch.from_numpy(u8).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(f, O.rescale_u8(u8))

@@ -113,3 +113,21 @@ def test_components_pinned():
     seg = (rng.random((40, 52)) < 0.45).astype(np.int32) + 2 * (rng.random((40, 52)) < 0.2)
     seg[5:9, 5:30] = -1
     np.testing.assert_array_equal(O.cc_roots(seg), R.cc_roots(seg))
+
+
+def test_color_pinned():
+    """The engine's colour kernels against the reference's (same device powf)."""
+    torch = pytest.importorskip("torch")
+    from st_spix_gb300 import bist_cuda
+    rng = np.random.default_rng(1)
+    rgb = rng.uniform(0, 1, size=(40, 56, 3)).astype(np.float32)
+    rgb[0, 0, 0] = np.nan                     # left unwritten by both
+    lab_ref = R.rgb2lab(rgb)
+    lab = bist_cuda.rgb2lab(torch.from_numpy(rgb).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(lab, lab_ref)
+    lab[0, 0] = lab_ref[0, 0] = 0.5
+    np.testing.assert_array_equal(bist_cuda.lab2rgb(torch.from_numpy(lab).cuda()).cpu().numpy(),
+                                  R.lab2rgb(lab_ref))
+    u8 = rng.integers(0, 256, size=(24, 30, 3)).astype(np.uint8)
+    np.testing.assert_array_equal(bist_cuda.rescale_u8(torch.from_numpy(u8).cuda()).cpu().numpy(),
+                                  R.rescale_u8(u8))
