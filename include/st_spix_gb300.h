@@ -271,6 +271,18 @@ int stspix_video_nspix(const stspix_video* video);
 /* Frames processed since creation or the last reset. */
 long long stspix_video_frames(const stspix_video* video);
 
+/* Snapshot / restore of a stream's resident state (labels, superpixel count and
+ * parameters of its last frame) to and from host memory, e.g. to move a stream to
+ * another context or process or to resume it later.  Layout: a 64-byte header
+ * (magic "SPXVIDEO", version 1, H, W, nspix, frames) then the labels (i32, H*W) and
+ * the 13 parameter arrays of stspix_params for nspix entries, in declaration order.
+ * stspix_video_save: returns the bytes needed in *bytes; writes when capacity is
+ * large enough.  stspix_video_load: the video must have the snapshot's H and W.
+ * Both synchronise the stream.                                                */
+int stspix_video_save(stspix_video* video, void* stream, void* host, long long capacity,
+                      long long* bytes);
+int stspix_video_load(stspix_video* video, void* stream, const void* host, long long bytes);
+
 typedef struct stspix_frame {
   const float* img;       /* f32 [H,W,3] device                                         */
   const float* flow;      /* f32 [H,W,2] device, (dx,dy) from the video's previous

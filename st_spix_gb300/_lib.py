@@ -70,7 +70,8 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_video_create", "stspix_video_destroy", "stspix_video_reset",
            "stspix_video_nspix", "stspix_video_frames", "stspix_process_batch",
            "stspix_footprint", "stspix_last_batch_ms", "stspix_profile_kernels",
-           "stspix_label_stats", "stspix_rgb2lab", "stspix_lab2rgb", "stspix_rescale_u8"]
+           "stspix_label_stats", "stspix_rgb2lab", "stspix_lab2rgb", "stspix_rescale_u8",
+           "stspix_video_save", "stspix_video_load"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -128,6 +129,8 @@ def load(build_if_missing: bool = True):
             "stspix_profile_kernels": (I, [P, C.c_char_p, I]),
             "stspix_label_stats": (I, [P, P, P, P, I, I, I, I, P]),
             "stspix_rgb2lab": (I, [P, P, P, P, C.c_longlong]),
+            "stspix_video_save": (I, [P, P, P, C.c_longlong, C.POINTER(C.c_longlong)]),
+            "stspix_video_load": (I, [P, P, P, C.c_longlong]),
             "stspix_lab2rgb": (I, [P, P, P, P, C.c_longlong]),
             "stspix_rescale_u8": (I, [P, P, P, P, C.c_longlong, C.c_float]),
         }

@@ -51,6 +51,21 @@ class Video:
         """Forget the history: the next frame starts a new video."""
         self.ctx.lib.stspix_video_reset(self.handle)
 
+    def save(self) -> bytes:
+        """Snapshot of the resident state (labels, superpixel count and parameters of
+        the last frame) as bytes (stspix_video_save)."""
+        n = C.c_longlong(0)
+        st = _stream(self.device)
+        self.ctx.check(self.ctx.lib.stspix_video_save(self.handle, st, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self.ctx.check(self.ctx.lib.stspix_video_save(self.handle, st, buf, n.value, C.byref(n)))
+        return buf.raw
+
+    def load(self, snapshot: bytes):
+        """Restore a snapshot taken by save(): the next frame continues that stream."""
+        self.ctx.check(self.ctx.lib.stspix_video_load(self.handle, _stream(self.device),
+                                                      snapshot, len(snapshot)))
+
     def close(self):
         if getattr(self, "handle", None):
             self.ctx.lib.stspix_video_destroy(self.handle)

@@ -1427,6 +1427,93 @@ int stspix_video_reset(stspix_video* v) {
   return STSPIX_OK;
 }
 
+namespace {
+// Parameter arrays of stspix_params in declaration order: element bytes x count per id.
+struct ParamField { size_t elem; int per; };
+const ParamField kParamFields[13] = {{4, 3}, {4, 3}, {8, 2}, {8, 3}, {4, 1}, {8, 2}, {8, 3},
+                                     {8, 3}, {4, 1}, {4, 1}, {4, 1}, {4, 1}, {4, 1}};
+void* param_ptr(const stspix_params& p, int i) {
+  void* f[13] = {p.mu_app, p.prior_mu_app, p.mu_shape, p.sigma_shape, p.logdet_sigma_shape,
+                 p.prior_mu_shape, p.prior_sigma_shape, p.sample_sigma_shape, p.counts,
+                 p.sm_counts, p.prior_counts, p.ids, p.invalid_counts};
+  return f[i];
+}
+struct SnapHeader {
+  char magic[8];
+  int version, H, W, n;
+  long long frames;
+  char pad[32];
+};
+static_assert(sizeof(SnapHeader) == 64, "snapshot header is 64 bytes");
+long long snap_bytes(int H, int W, int n) {
+  long long b = (long long)sizeof(SnapHeader) + 4LL * H * W;
+  for (const auto& f : kParamFields) b += (long long)f.elem * f.per * n;
+  return b;
+}
+}  // namespace
+
+int stspix_video_save(stspix_video* v, void* stream, void* host, long long capacity,
+                      long long* bytes) {
+  if (!v || !bytes) return STSPIX_ERR_ARG;
+  stspix_ctx* ctx = v->ctx;
+  const long long need = snap_bytes(v->H, v->W, v->n);
+  *bytes = need;
+  if (!host || capacity < need) return STSPIX_OK;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  SnapHeader h{};
+  memcpy(h.magic, "SPXVIDEO", 8);
+  h.version = 1; h.H = v->H; h.W = v->W; h.n = v->n; h.frames = v->frames;
+  char* out = (char*)host;
+  memcpy(out, &h, sizeof h);
+  out += sizeof h;
+  const size_t npix = (size_t)v->H * v->W;
+  if (v->labels) CK(cudaMemcpyAsync(out, v->labels, 4 * npix, cudaMemcpyDeviceToHost, st));
+  else memset(out, 0xff, 4 * npix);
+  out += 4 * npix;
+  for (int i = 0; i < 13; i++) {
+    const size_t b = kParamFields[i].elem * kParamFields[i].per * (size_t)v->n;
+    if (b) CK(cudaMemcpyAsync(out, param_ptr(v->pp[v->cur], i), b, cudaMemcpyDeviceToHost, st));
+    out += b;
+  }
+  CK(cudaStreamSynchronize(st));
+  return STSPIX_OK;
+}
+
+int stspix_video_load(stspix_video* v, void* stream, const void* host, long long bytes) {
+  if (!v || !host) return STSPIX_ERR_ARG;
+  stspix_ctx* ctx = v->ctx;
+  SnapHeader h;
+  if (bytes < (long long)sizeof h) return fail(ctx, STSPIX_ERR_ARG, "snapshot too short");
+  memcpy(&h, host, sizeof h);
+  if (memcmp(h.magic, "SPXVIDEO", 8) != 0 || h.version != 1)
+    return fail(ctx, STSPIX_ERR_ARG, "not a version-1 video snapshot");
+  if (h.H != v->H || h.W != v->W)
+    return fail(ctx, STSPIX_ERR_ARG, "snapshot of a %dx%d video for a %dx%d video", h.H, h.W,
+                v->H, v->W);
+  if (h.n < 0 || bytes < snap_bytes(h.H, h.W, h.n))
+    return fail(ctx, STSPIX_ERR_ARG, "snapshot truncated");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  v->n = 0;  // nothing to keep while growing
+  int r;
+  if ((r = video_ensure(ctx, st, v, std::max(10 * h.n + 2, 64)))) return r;
+  v->cur = 0;
+  const char* in = (const char*)host + sizeof h;
+  const size_t npix = (size_t)v->H * v->W;
+  CK(cudaMemcpyAsync(v->labels, in, 4 * npix, cudaMemcpyHostToDevice, st));
+  in += 4 * npix;
+  for (int i = 0; i < 13; i++) {
+    const size_t b = kParamFields[i].elem * kParamFields[i].per * (size_t)h.n;
+    if (b) CK(cudaMemcpyAsync(param_ptr(v->pp[0], i), in, b, cudaMemcpyHostToDevice, st));
+    in += b;
+  }
+  CK(cudaStreamSynchronize(st));
+  v->n = h.n;
+  v->frames = h.frames;
+  return STSPIX_OK;
+}
+
 int stspix_video_nspix(const stspix_video* v) { return v ? v->n : -1; }
 long long stspix_video_frames(const stspix_video* v) { return v ? v->frames : -1; }
 
