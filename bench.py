@@ -237,7 +237,7 @@ def run_serve(args, world, rank):
 
     torch.cuda.set_device(args.local)
     dev = torch.device("cuda", args.local)
-    w, sv = WORKLOAD, SERVE
+    w, sv = WORKLOAD, dict(SERVE, fps=args.fps, T=args.frames)
     S = args.streams
     res = synth.stream_resolution_mix(S, seed=rank)
     cfg = dict(niters=w["niters"], sp_size=w["sp_size"], potts=w["potts"],
@@ -271,7 +271,14 @@ def run_serve(args, world, rank):
     plain_fps = plain_frames / plain_s
     budget = int(sv["budget_gb"] * 2 ** 30)
     srv = serve.Server(budget, max_batch=args.max_batch, lanes=args.lanes, device=dev,
-                       seed=rank, **cfg)
+                       seed=rank, max_pixels=args.max_pixels, **cfg)
+    # warm-up run (untimed): two short streams per resolution, so that the lanes'
+    # engine contexts exist and the sweep tile classes are tuned
+    for j, hw in enumerate(sorted(pool) * 2):
+        v, f = pool[hw][0]
+        srv.add(serve.StreamRequest(-1 - j, v[:4], f[:3], fps=1000.0))
+    srv.run()
+    torch.cuda.synchronize()
     for sid, hw in enumerate(res):
         v, f = pool[hw][sid % sv["pool"]]
         srv.add(serve.StreamRequest(sid, v, f, fps=sv["fps"]))
@@ -292,7 +299,8 @@ def run_serve(args, world, rank):
         "config": {"workload": sv["name"], "streams": S, "streams_by_height": hist,
                    "frames_per_stream": sv["T"], "arrivals": "Poisson %.0f fps per stream" % sv["fps"],
                    "offered_fps": S * sv["fps"], "budget_gb": sv["budget_gb"],
-                   "max_batch": args.max_batch, "lanes": args.lanes,
+                   "max_batch": args.max_batch, "max_pixels": args.max_pixels,
+                   "lanes": args.lanes, "warmup": "2 streams x 4 frames per resolution, untimed",
                    "sp_size": w["sp_size"], "niters": w["niters"], "prop_niters": w["prop_niters"],
                    "sm_period": w["sm_period"]},
         "serving": st,
@@ -611,6 +619,10 @@ def main():
                          "accumulator precision study at 4K; image: plain BASS on one "
                          "240x320 frame")
     ap.add_argument("--max-batch", type=int, default=8, help="serve: frames per batch")
+    ap.add_argument("--max-pixels", type=int, default=0,
+                    help="serve: pixels per batch (0: no cap); bounds a batch's GPU time")
+    ap.add_argument("--fps", type=float, default=30.0, help="serve: mean frame rate per stream")
+    ap.add_argument("--frames", type=int, default=30, help="serve: frames per stream")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_setup()
@@ -655,10 +667,12 @@ def main():
     from st_spix_gb300 import synth
     dvid, dflo = [], []
     for i in range(S):
-        v, f = synth.voronoi_video_device(w["H"], w["W"], T, w["nseeds"], w["sigma"],
-                                          seed=rank * S + i, device=dev)
-        dvid.append(v)
-        dflo.append(f)
+        out = synth.voronoi_video_device(w["H"], w["W"], T, w["nseeds"], w["sigma"],
+                                         seed=rank * S + i, device=dev, regions=i == 0)
+        dvid.append(out[0])
+        dflo.append(out[1])
+        if i == 0:
+            regions0 = out[2]      # ground truth of stream 0 for the quality scores
     host = [(v.cpu().numpy(), f.cpu().numpy()) for v, f in zip(dvid, dflo)]
     dout = [torch.empty((T, w["H"], w["W"]), dtype=torch.int32, device=dev) for _ in range(S)]
     lanes = [list(range(j, S, NL)) for j in range(NL)]
@@ -745,6 +759,15 @@ def main():
         pstream.synchronize()
         plain_fps = T * args.steps / (time.perf_counter() - t0)
     agree = float((plain_out == dout[0]).float().mean().item())
+
+    # ---- quality scores of stream 0 against its generator's regions (GPU) --------
+    from st_spix_gb300 import metrics
+    metrics.evaluate(dvid[0][:2], dout[0][:2], regions0[:2])       # first-use warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    qual = metrics.computeSummary(dvid[0], regions0, dout[0])
+    torch.cuda.synchronize()
+    qual_ms = 1000 * (time.perf_counter() - t0)
 
     # ---- per-family device time of lane 0's batches (CUDA events on its stream) --
     with torch.cuda.stream(cstreams[0]):
@@ -848,6 +871,10 @@ def main():
                 "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in h_out))},
         "gpu_launches": int(total_launches),
         "clocks": summarize_clocks(clk_lines),
+        "quality": dict({k: qual[k] for k in ("tex", "szv", "ev", "ev3d", "pooling", "ue2d",
+                                              "sa2d", "ue3d", "sa3d", "spnum", "ave_nsp")},
+                        stream=0, ground_truth="generator regions (%d)" % w["nseeds"],
+                        evaluate_ms=qual_ms),
     }
     print(json.dumps(line), flush=True)
     if world > 1:

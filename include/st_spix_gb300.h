@@ -20,6 +20,10 @@
  *   stspix_rescale_u8          st_spix/csrc/bist/rgb2lab.cu:21 rescale_image
  *   stspix_bass_partial        st_spix/csrc/bist/bass.cu:46 bass() stopped after k iterations
  *                              (exposes update_params.cu:12 and update_seg.cu:281 state)
+ *   stspix_evaluate            st_spix/spix_utils/evaluate.py:94 computeSummary
+ *   stspix_count_spix          st_spix/spix_utils/evaluate.py:71 count_spix
+ *   stspix_size_variation      st_spix/spix_utils/evaluate.py:284 scoreMeanDurationAndSizeVariation
+ *   stspix_sp_pooling          st_spix/sp_pooling.py:10 pooling
  */
 #ifndef ST_SPIX_GB300_H
 #define ST_SPIX_GB300_H
@@ -246,6 +250,56 @@ int stspix_rescale_u8(stspix_ctx* ctx, void* stream, const uint8_t* in, float* o
  * Synchronises the stream.                                                     */
 int stspix_label_stats(stspix_ctx* ctx, void* stream, const float* img, const int32_t* labels,
                        int H, int W, int nlabels, int accumulator, double* out);
+
+/* ---- quality metrics -------------------------------------------------------------
+ * The superpixel quality scores of st_spix/spix_utils/evaluate.py, on the device.
+ * Labels are offset by their minimum first, as computeSummary does (evaluate.py:97).
+ *   tex, szv   scoreMeanDurationAndSizeVariation (evaluate.py:284): fraction of ids
+ *              alive per frame (mean over frames); mean over ids alive in more than
+ *              one frame of the unbiased std of their size (NaN if none)
+ *   ev         scoreExplainedVariance (evaluate.py:230): per-frame pooled colours
+ *   ev3d       scoreExplainedVariance3D (evaluate.py:254): ids pooled over the video
+ *   psnr       scoreSpixPoolingQuality (evaluate.py:214): 10 log10(1/mse) of the
+ *              per-frame pooled video, data range 1, mean over frames
+ *   ave_nsp    averge_unique_spix_v1 (evaluate.py:184); spnum = max - min + 1
+ *   ue2d, sa2d, ue3d, sa3d   scoreUEandSA (evaluate.py:372), given a ground truth
+ *              whose ids are 0..max, each present (else STSPIX_ERR_ARG); -1 without.
+ * Integer tables are exact; colour sums are FP64.                                   */
+typedef struct {
+  double tex, szv, ev, ev3d, psnr, ave_nsp;
+  double ue2d, sa2d, ue3d, sa3d;
+  int spnum;
+  int has_gt;
+} stspix_quality;
+
+/* vid f32 [T,H,W,3], spix i32 [T,H,W], gt i32 [T,H,W] or NULL (device pointers).
+ * Synchronises the stream.                                                          */
+int stspix_evaluate(stspix_ctx* ctx, void* stream, const float* vid, const int32_t* spix,
+                    const int32_t* gt, int T, int H, int W, stspix_quality* out);
+
+/* Minimum and maximum of n labels into out[0], out[1] (host). Synchronises.          */
+int stspix_label_range(stspix_ctx* ctx, void* stream, const int32_t* labels, long long n,
+                       int32_t* out);
+
+/* count_spix (evaluate.py:71): counts[t*nids + k] = pixels of frame t carrying id
+ * id_offset + k; every id must lie in [id_offset, id_offset + nids) (else
+ * STSPIX_ERR_ARG).  counts is a device array of T*nids int32.                        */
+int stspix_count_spix(stspix_ctx* ctx, void* stream, const int32_t* spix, int T, long long npix,
+                      int32_t id_offset, int nids, int32_t* counts);
+
+/* scoreMeanDurationAndSizeVariation (evaluate.py:284) on a device table of per-frame
+ * id sizes, int32 [T, S]: *tex, *szv as in stspix_quality, and (when ave_nsp is not
+ * NULL) averge_unique_spix_v1 (evaluate.py:184), the mean number of ids alive per
+ * frame. Synchronises.                                                               */
+int stspix_size_variation(stspix_ctx* ctx, void* stream, const int32_t* counts, int T, int S,
+                          double* tex, double* szv, double* ave_nsp);
+
+/* sp_pooling (st_spix/sp_pooling.py:10) for 3-channel frames: with ids 0..nids-1
+ * (every id of spix must be in range, else STSPIX_ERR_ARG), down f32 [T, nids, 3] =
+ * per-frame id mean colour (sum / (count + 1e-8); 0 for absent ids) and, when pooled
+ * is not NULL, pooled f32 [T,H,W,3] = the mean colour of each pixel's id.            */
+int stspix_sp_pooling(stspix_ctx* ctx, void* stream, const float* vid, const int32_t* spix,
+                      int T, int H, int W, int nids, float* pooled, float* down);
 
 /* ---- batched and serving forms -----------------------------------------------
  * No single reference counterpart: the reference processes one frame per call

@@ -60,6 +60,13 @@ class FrameC(C.Structure):
                 ("log", FrameLog)]
 
 
+class QualityC(C.Structure):
+    """stspix_quality (host)."""
+    _fields_ = [(n, C.c_double) for n in ("tex", "szv", "ev", "ev3d", "psnr", "ave_nsp",
+                                          "ue2d", "sa2d", "ue3d", "sa3d")] + \
+               [("spnum", C.c_int), ("has_gt", C.c_int)]
+
+
 # Every symbol declared in include/st_spix_gb300.h.
 EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_last_error",
            "stspix_version", "stspix_kernel_launches", "stspix_get_frame_log",
@@ -71,7 +78,8 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_video_nspix", "stspix_video_frames", "stspix_process_batch",
            "stspix_footprint", "stspix_last_batch_ms", "stspix_profile_kernels",
            "stspix_label_stats", "stspix_rgb2lab", "stspix_lab2rgb", "stspix_rescale_u8",
-           "stspix_video_save", "stspix_video_load"]
+           "stspix_video_save", "stspix_video_load", "stspix_evaluate", "stspix_label_range",
+           "stspix_count_spix", "stspix_size_variation", "stspix_sp_pooling"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -133,6 +141,12 @@ def load(build_if_missing: bool = True):
             "stspix_video_load": (I, [P, P, P, C.c_longlong]),
             "stspix_lab2rgb": (I, [P, P, P, P, C.c_longlong]),
             "stspix_rescale_u8": (I, [P, P, P, P, C.c_longlong, C.c_float]),
+            "stspix_evaluate": (I, [P, P, P, P, P, I, I, I, C.POINTER(QualityC)]),
+            "stspix_label_range": (I, [P, P, P, C.c_longlong, C.POINTER(C.c_int32)]),
+            "stspix_count_spix": (I, [P, P, P, I, C.c_longlong, C.c_int32, I, P]),
+            "stspix_size_variation": (I, [P, P, P, I, I, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+            "stspix_sp_pooling": (I, [P, P, P, P, I, I, I, I, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

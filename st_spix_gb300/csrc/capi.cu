@@ -15,6 +15,7 @@
 // device.  A batch with propagated frames and the 4/8/12 iteration ladder reads the
 // hole counts back once (the ladder picks each frame's iteration count from them).
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstddef>
@@ -74,7 +75,6 @@ struct List {
   bool any_prop = false;
   std::vector<int> tiles_upto[2];  // sweep tiles (32- / 64-wide) of the first i slots
   std::vector<long long> segs_upto;  // 32-pixel row segments of the first i slots
-  unsigned long long shape = 0;      // hash of the slot sizes (autotuner key)
 };
 
 }  // namespace stspix
@@ -531,7 +531,6 @@ List make_list(stspix_ctx* ctx, int off, const std::vector<Slot>& slots) {
     }
     if (L.segs_upto.empty()) L.segs_upto.push_back(0);
     L.segs_upto.push_back(L.segs_upto.back() + (long long)s.H * ((s.W + 31) / 32));
-    L.shape = (L.shape ^ (unsigned long long)(s.H * 65536LL + s.W)) * 1099511628211ULL;
     h[i] = s;
     L.max_npix = std::max(L.max_npix, s.npix);
     L.max_cap = std::max(L.max_cap, s.cap);
@@ -594,11 +593,15 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
     if (v) LAUNCHG(kb_sweep_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode);
     else LAUNCHG(kb_sweep_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode);
   };
-  // tile-shape autotuner: the first sweep of a batch shape runs both tile widths on
-  // the same input (a sweep reads only the labels at its start, so both write the
-  // same output) and the faster is kept for that shape
+  // tile-shape autotuner: the first sweep of a batch size class runs both tile widths
+  // on the same input (a sweep reads only the labels at its start, so both write the
+  // same output) and the faster is kept for that class.  The class is the number of
+  // 32x32 tiles of the sweeping slots in quarter octaves: the choice depends on how
+  // well the tiles fill the SMs, and mixed serving batches then tune a handful of
+  // times instead of once per combination of frame sizes.
   int it0 = 0;
-  const auto key = std::make_pair(L.shape, nb);
+  const int tl = std::max(1, L.tiles_upto[0][nb]);
+  const auto key = std::make_pair((unsigned long long)std::floor(4.0 * std::log2((double)tl)), 0);
   auto ch = ctx->sweep_choice.find(key);
   int v;
   if (ch != ctx->sweep_choice.end()) {
@@ -1640,6 +1643,309 @@ int stspix_label_stats(stspix_ctx* ctx, void* stream, const float* img, const in
   CK(cudaFreeAsync(dacc, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+// ---- quality metrics (evaluate.py) ------------------------------------------------
+namespace {
+// Scratch of one evaluation, carved from one allocation (256-byte aligned pieces).
+struct QualityScratch {
+  int* cnt;                    // [T*S]   per-frame id sizes
+  double* fsum;                // [T*S*3] per-frame id colour sums
+  double* vsum;                // [S*3]   video-wide id colour sums
+  double* msum;                // [T*3]   per-frame colour sums
+  double* pix2;                // [T]     sum (v - mean)^2
+  double* pix2s;               // [T]     the same at x255 scale
+  double* sse;                 // [T]     sum (v - pooled)^2
+  double* pool2;               // [T]     sum (pooled - mean)^2, per-frame pooling
+  double* pool3;               // [T]     the same, video pooling at x255
+  unsigned long long* live;    // [T]     ids alive per frame
+  long long* ntot;             // [S]     total size over the video
+  double* stdv;                // [S]     size std over the frames alive (-1: < 2)
+  int* J;                      // [T*S*G1] id x ground-truth overlaps
+  unsigned long long *ue, *sa, *gsize;   // [T*G1]
+  unsigned long long *ue3, *sa3;         // [G1]
+  size_t bytes;
+};
+
+QualityScratch quality_layout(char* base, long long T, long long S, long long G1, bool colour,
+                              bool gt) {
+  QualityScratch q{};
+  size_t off = 0;
+  auto take = [&](size_t n) -> char* {
+    char* p = base ? base + off : nullptr;
+    off += (n + 255) & ~size_t(255);
+    return p;
+  };
+  q.cnt = (int*)take(4 * T * S);
+  q.live = (unsigned long long*)take(8 * T);
+  q.ntot = (long long*)take(8 * S);
+  q.stdv = (double*)take(8 * S);
+  if (colour) {
+    q.fsum = (double*)take(24 * T * S);
+    q.vsum = (double*)take(24 * S);
+    q.msum = (double*)take(24 * T);
+    q.pix2 = (double*)take(8 * T);
+    q.pix2s = (double*)take(8 * T);
+    q.sse = (double*)take(8 * T);
+    q.pool2 = (double*)take(8 * T);
+    q.pool3 = (double*)take(8 * T);
+  }
+  if (gt) {
+    q.J = (int*)take(4 * T * S * G1);
+    q.ue = (unsigned long long*)take(8 * T * G1);
+    q.sa = (unsigned long long*)take(8 * T * G1);
+    q.gsize = (unsigned long long*)take(8 * T * G1);
+    q.ue3 = (unsigned long long*)take(8 * G1);
+    q.sa3 = (unsigned long long*)take(8 * G1);
+  }
+  q.bytes = off;
+  return q;
+}
+
+constexpr size_t kQualityMaxScratch = size_t(64) << 30;
+
+int label_range(stspix_ctx* ctx, cudaStream_t st, const int32_t* a, long long n, int out[2]) {
+  int* mm = nullptr;
+  CK(cudaMallocAsync((void**)&mm, 2 * sizeof(int), st));
+  LAUNCHG(k_q_range_init, 1, 32, mm);
+  const long long nb = std::min<long long>((n + kThreads - 1) / kThreads, 4LL * ctx->num_sms);
+  LAUNCHG(k_q_range, (unsigned)std::max(1LL, nb), kThreads, a, n, mm);
+  CK(cudaMemcpyAsync(out, mm, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaFreeAsync(mm, st));
+  CK(cudaStreamSynchronize(st));
+  return STSPIX_OK;
+}
+
+// tex / szv from the per-frame live counts and per-id stds (evaluate.py:287-327).
+void size_scores(const std::vector<unsigned long long>& live, const std::vector<double>& stdv,
+                 int T, long long S, double* tex, double* szv) {
+  double a = 0;
+  for (int t = 0; t < T; t++) a += (double)live[t] / (double)S;
+  *tex = a / T;
+  double s = 0;
+  long long n = 0;
+  for (long long k = 0; k < S; k++)
+    if (stdv[k] >= 0) { s += stdv[k]; n++; }
+  *szv = n ? s / n : std::nan("");
+}
+
+unsigned q_blocks(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
+}  // namespace
+
+int stspix_label_range(stspix_ctx* ctx, void* stream, const int32_t* labels, long long n,
+                       int32_t* out) {
+  if (!ctx || !labels || !out || n < 1) return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  int mm[2];
+  int r = label_range(ctx, st, labels, n, mm);
+  if (r) return r;
+  out[0] = mm[0];
+  out[1] = mm[1];
+  return STSPIX_OK;
+}
+
+int stspix_count_spix(stspix_ctx* ctx, void* stream, const int32_t* spix, int T, long long npix,
+                      int32_t id_offset, int nids, int32_t* counts) {
+  if (!ctx || !spix || !counts || T < 1 || npix < 1 || npix > INT_MAX || nids < 1 || T > 65535)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  int mm[2];
+  int r = label_range(ctx, st, spix, (long long)T * npix, mm);
+  if (r) return r;
+  if (mm[0] < id_offset || (long long)mm[1] >= (long long)id_offset + nids)
+    return fail(ctx, STSPIX_ERR_ARG, "ids %d..%d outside [%d, %lld)", mm[0], mm[1], id_offset,
+                (long long)id_offset + nids);
+  CK(cudaMemsetAsync(counts, 0, sizeof(int32_t) * (size_t)T * nids, st));
+  const long long segs = (long long)T * ((npix + 31) / 32);
+  const unsigned nb = (unsigned)std::max(1LL, std::min<long long>((segs + 7) / 8, 8LL * ctx->num_sms));
+  LAUNCHG(k_q_accum, nb, kThreads, nullptr, spix, nullptr, T, 1, (int)npix, id_offset, nids, 1,
+          counts, nullptr, nullptr, nullptr, nullptr);
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_size_variation(stspix_ctx* ctx, void* stream, const int32_t* counts, int T, int S,
+                          double* tex, double* szv, double* ave_nsp) {
+  if (!ctx || !counts || !tex || !szv || T < 1 || S < 1 || T > 65535)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  QualityScratch q = quality_layout(nullptr, T, S, 1, false, false);
+  char* base = nullptr;
+  CK(cudaMallocAsync((void**)&base, q.bytes, st));
+  q = quality_layout(base, T, S, 1, false, false);
+  CK(cudaMemsetAsync(base, 0, q.bytes, st));
+  LAUNCHG(k_q_id_time, q_blocks(S), kThreads, counts, T, S, q.ntot, q.stdv);
+  LAUNCHG(k_q_frame_ids, dim3(q_blocks(S), T), kThreads, counts, nullptr, nullptr, q.ntot,
+          nullptr, S, 1, q.live, nullptr, nullptr);
+  std::vector<unsigned long long> live(T);
+  std::vector<double> stdv(S);
+  CK(cudaMemcpyAsync(live.data(), q.live, 8 * (size_t)T, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(stdv.data(), q.stdv, 8 * (size_t)S, cudaMemcpyDeviceToHost, st));
+  CK(cudaFreeAsync(base, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  size_scores(live, stdv, T, S, tex, szv);
+  if (ave_nsp) {
+    double a = 0;
+    for (int t = 0; t < T; t++) a += (double)live[t];
+    *ave_nsp = a / T;
+  }
+  return STSPIX_OK;
+}
+
+int stspix_sp_pooling(stspix_ctx* ctx, void* stream, const float* vid, const int32_t* spix,
+                      int T, int H, int W, int nids, float* pooled, float* down) {
+  if (!ctx || !vid || !spix || !down || T < 1 || H < 1 || W < 1 || nids < 1 || T > 65535 ||
+      (long long)H * W > INT_MAX)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long npix = (long long)H * W, n = T * npix, TS = (long long)T * nids;
+  int mm[2];
+  int r = label_range(ctx, st, spix, n, mm);
+  if (r) return r;
+  if (mm[0] < 0 || mm[1] >= nids)
+    return fail(ctx, STSPIX_ERR_ARG, "ids %d..%d outside [0, %d)", mm[0], mm[1], nids);
+  // counts, per-frame id sums, and the video-wide id / per-frame sums that the
+  // accumulation pass also produces
+  const size_t cbytes = (4 * (size_t)TS + 255) & ~size_t(255);
+  const size_t bytes = cbytes + 24 * ((size_t)TS + nids + T);
+  char* base = nullptr;
+  CK(cudaMallocAsync((void**)&base, bytes, st));
+  CK(cudaMemsetAsync(base, 0, bytes, st));
+  int* cnt = (int*)base;
+  double* fsum = (double*)(base + cbytes);
+  double* vsum = fsum + 3 * (size_t)TS;
+  double* msum = vsum + 3 * (size_t)nids;
+  const long long segs = (long long)T * H * ((W + 31) / 32);
+  const unsigned nb = (unsigned)std::max(1LL, std::min<long long>((segs + 7) / 8, 8LL * ctx->num_sms));
+  LAUNCHG(k_q_accum, nb, kThreads, vid, spix, nullptr, T, H, W, 0, nids, 1, cnt, fsum, vsum, msum,
+          nullptr);
+  LAUNCHG(k_q_down, q_blocks(TS), kThreads, cnt, fsum, TS, down);
+  if (pooled)
+    LAUNCHG(k_q_pool_write, q_blocks(n), kThreads, spix, (int)npix, 0, nids, n, down, pooled);
+  CK(cudaFreeAsync(base, st));
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_evaluate(stspix_ctx* ctx, void* stream, const float* vid, const int32_t* spix,
+                    const int32_t* gt, int T, int H, int W, stspix_quality* out) {
+  if (!ctx || !vid || !spix || !out || T < 1 || H < 1 || W < 1 || T > 65535 ||
+      (long long)H * W > INT_MAX)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long npix = (long long)H * W, n = T * npix;
+  int sr[2], gr[2] = {0, 0};
+  int r = label_range(ctx, st, spix, n, sr);
+  if (r) return r;
+  if (gt && (r = label_range(ctx, st, gt, n, gr))) return r;
+  if (gt && gr[0] < 0) return fail(ctx, STSPIX_ERR_ARG, "negative ground-truth id %d", gr[0]);
+  const long long S = (long long)sr[1] - sr[0] + 1, G1 = gt ? (long long)gr[1] + 1 : 1;
+  if (S > INT_MAX || G1 > INT_MAX) return fail(ctx, STSPIX_ERR_TOO_LARGE, "id range too large");
+  QualityScratch q = quality_layout(nullptr, T, S, G1, true, gt != nullptr);
+  if (q.bytes > kQualityMaxScratch || (gt && (double)T * S * G1 > 2e9))
+    return fail(ctx, STSPIX_ERR_TOO_LARGE, "evaluation tables of %zu bytes (T=%d, ids=%lld, "
+                "ground-truth ids=%lld) exceed the limit", q.bytes, T, S, G1);
+  char* base = nullptr;
+  CK(cudaMallocAsync((void**)&base, q.bytes, st));
+  q = quality_layout(base, T, S, G1, true, gt != nullptr);
+  CK(cudaMemsetAsync(base, 0, q.bytes, st));
+  const long long segs = (long long)T * H * ((W + 31) / 32);
+  const unsigned nb = (unsigned)std::max(1LL, std::min<long long>((segs + 7) / 8, 8LL * ctx->num_sms));
+  LAUNCHG(k_q_accum, nb, kThreads, vid, spix, gt, T, H, W, sr[0], (int)S, (int)G1, q.cnt, q.fsum,
+          q.vsum, q.msum, q.J);
+  const unsigned rx = (unsigned)std::max(1LL, std::min<long long>(q_blocks(npix), 8LL * ctx->num_sms / T + 1));
+  LAUNCHG(k_q_resid, dim3(rx, T), kThreads, vid, spix, (int)npix, sr[0], (int)S, q.cnt, q.fsum,
+          q.msum, q.pix2, q.pix2s, q.sse);
+  LAUNCHG(k_q_id_time, q_blocks(S), kThreads, q.cnt, T, (int)S, q.ntot, q.stdv);
+  LAUNCHG(k_q_frame_ids, dim3(q_blocks(S), T), kThreads, q.cnt, q.fsum, q.vsum, q.ntot, q.msum,
+          (int)S, (int)npix, q.live, q.pool2, q.pool3);
+  if (gt) {
+    LAUNCHG(k_q_uesa_frame, dim3(q_blocks(S), T), kThreads, q.cnt, q.J, (int)S, (int)G1, q.ue,
+            q.sa, q.gsize);
+    LAUNCHG(k_q_uesa_id, q_blocks(S), kThreads, q.cnt, q.J, q.ntot, T, (int)S, (int)G1, q.ue3,
+            q.sa3);
+  }
+  // per-frame / per-id results to the host
+  std::vector<double> pix2(T), pix2s(T), sse(T), pool2(T), pool3(T), stdv(S);
+  std::vector<unsigned long long> live(T), ue, sa, gsize, ue3, sa3;
+  auto d2h = [&](void* dst, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+  };
+  CK(d2h(pix2.data(), q.pix2, 8 * (size_t)T));
+  CK(d2h(pix2s.data(), q.pix2s, 8 * (size_t)T));
+  CK(d2h(sse.data(), q.sse, 8 * (size_t)T));
+  CK(d2h(pool2.data(), q.pool2, 8 * (size_t)T));
+  CK(d2h(pool3.data(), q.pool3, 8 * (size_t)T));
+  CK(d2h(live.data(), q.live, 8 * (size_t)T));
+  CK(d2h(stdv.data(), q.stdv, 8 * (size_t)S));
+  if (gt) {
+    ue.resize(T * G1); sa.resize(T * G1); gsize.resize(T * G1); ue3.resize(G1); sa3.resize(G1);
+    CK(d2h(ue.data(), q.ue, 8 * (size_t)(T * G1)));
+    CK(d2h(sa.data(), q.sa, 8 * (size_t)(T * G1)));
+    CK(d2h(gsize.data(), q.gsize, 8 * (size_t)(T * G1)));
+    CK(d2h(ue3.data(), q.ue3, 8 * (size_t)G1));
+    CK(d2h(sa3.data(), q.sa3, 8 * (size_t)G1));
+  }
+  CK(cudaFreeAsync(base, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+
+  stspix_quality res{};
+  size_scores(live, stdv, T, S, &res.tex, &res.szv);
+  double ev = 0, ev3 = 0, ps = 0, nsp = 0;
+  for (int t = 0; t < T; t++) {
+    ev += pool2[t] / (pix2[t] + 1e-10);
+    ev3 += pool3[t] / (pix2s[t] + 1e-10);
+    const double mse = sse[t] / (3.0 * npix);
+    ps += mse > 0 ? 10.0 * std::log10(1.0 / mse) : INFINITY;
+    nsp += (double)live[t];
+  }
+  res.ev = ev / T;
+  res.ev3d = ev3 / T;
+  res.psnr = ps / T;
+  res.ave_nsp = nsp / T;
+  res.spnum = (int)S;
+  res.ue2d = res.sa2d = res.ue3d = res.sa3d = -1.0;
+  res.has_gt = gt ? 1 : 0;
+  if (gt) {
+    // evaluate.py:482-510; every ground-truth id 0..max must be present (the
+    // reference aligns its columns on that and asserts non-empty objects)
+    for (long long g = 0; g < G1; g++) {
+      unsigned long long tot = 0;
+      for (int t = 0; t < T; t++) tot += gsize[t * G1 + g];
+      if (!tot) return fail(ctx, STSPIX_ERR_ARG, "ground-truth id %lld of 0..%lld never occurs", g,
+                            G1 - 1);
+    }
+    double u2 = 0;
+    for (long long i = 0; i < T * G1; i++) u2 += (double)ue[i] / (double)npix;
+    res.ue2d = u2 / (double)(T * G1);
+    double s2 = 0, u3 = 0, s3 = 0;
+    for (long long g = 0; g < G1; g++) {
+      u3 += (double)ue3[g] / (double)(T * npix);
+      if (g == 0) continue;
+      double a = 0, tot = 0;
+      long long frames = 0;
+      for (int t = 0; t < T; t++) {
+        const unsigned long long z = gsize[t * G1 + g];
+        a += (double)sa[t * G1 + g] / (double)(z ? z : 1);
+        frames += z > 0;
+        tot += (double)z;
+      }
+      s2 += a / (double)frames;
+      s3 += (double)sa3[g] / tot;
+    }
+    res.ue3d = u3 / (double)G1;
+    res.sa2d = G1 > 1 ? s2 / (double)(G1 - 1) : std::nan("");
+    res.sa3d = G1 > 1 ? s3 / (double)(G1 - 1) : std::nan("");
+  }
+  *out = res;
   return STSPIX_OK;
 }
 

@@ -108,4 +108,26 @@ __global__ void k_rgb2lab(const float* rgb, float* lab, long long npix);
 __global__ void k_lab2rgb(const float* lab, float* rgb, long long npix);
 __global__ void k_rescale_u8(const uint8_t* in, float* out, long long nvals, float mval);
 
+// k_quality.cu
+constexpr int kQGtShared = 256;
+__global__ void k_q_range_init(int* mm);
+__global__ void k_q_range(const int32_t* a, long long n, int* mm);
+__global__ void k_q_accum(const float* vid, const int32_t* spix, const int32_t* gt, int T, int H,
+                          int W, int off, int S, int G1, int* cnt, double* fsum, double* vsum,
+                          double* msum, int* J);
+__global__ void k_q_resid(const float* vid, const int32_t* spix, int npix, int off, int S,
+                          const int* cnt, const double* fsum, const double* msum, double* pix2,
+                          double* pix2s, double* sse);
+__global__ void k_q_id_time(const int* cnt, int T, int S, long long* ntot, double* std_out);
+__global__ void k_q_frame_ids(const int* cnt, const double* fsum, const double* vsum,
+                              const long long* ntot, const double* msum, int S, int npix,
+                              unsigned long long* live, double* pool2, double* pool3);
+__global__ void k_q_uesa_frame(const int* cnt, const int* J, int S, int G1, unsigned long long* ue,
+                               unsigned long long* sa, unsigned long long* size);
+__global__ void k_q_uesa_id(const int* cnt, const int* J, const long long* ntot, int T, int S,
+                            int G1, unsigned long long* ue3, unsigned long long* sa3);
+__global__ void k_q_down(const int* cnt, const double* fsum, long long TS, float* down);
+__global__ void k_q_pool_write(const int32_t* spix, int npix, int off, int S, long long n,
+                               const float* down, float* pooled);
+
 }  // namespace stspix

@@ -38,6 +38,7 @@ class _StreamState:
     nbytes: int
     rel_arrivals: np.ndarray          # arrival times relative to admission (s)
     kind: object = None               # streams of one kind can reuse each other's state
+    npix: int = 0                     # pixels per frame (batch pixel cap)
     arrivals: Optional[np.ndarray] = None
     admitted_at: Optional[float] = None
     next: int = 0                     # next frame index to serve
@@ -60,12 +61,16 @@ class Scheduler:
     of its kind (still counted as used) until a new stream of that kind takes it
     over; when a stream needs fresh bytes that do not fit, spares of other kinds
     are evicted first (their kinds are appended to `evicted` for the caller to
-    free).  Not thread-safe; Server serialises calls with a lock."""
+    free).  A batch holds at most max_batch frames and, when max_pixels is set, at most
+    that many pixels (but always at least one frame): the cap bounds a batch's GPU
+    time and so the latency of the frames in it.  Not thread-safe; Server serialises
+    calls with a lock."""
 
-    def __init__(self, budget: int, reserve: int, max_batch: int):
+    def __init__(self, budget: int, reserve: int, max_batch: int, max_pixels: int = 0):
         if reserve > budget:
             raise ValueError(f"working buffers ({reserve} B) exceed the budget ({budget} B)")
         self.budget, self.reserve, self.max_batch = int(budget), int(reserve), int(max_batch)
+        self.max_pixels = int(max_pixels)
         self.used = self.reserve
         self.streams: Dict[int, _StreamState] = {}
         self.queue: List[int] = []        # offered, not yet admitted (FIFO)
@@ -76,14 +81,16 @@ class Scheduler:
         self.evicted: List[object] = []
         self.reused = 0
 
-    def offer(self, sid: int, nbytes: int, rel_arrivals, now: float = 0.0, kind=None) -> bool:
+    def offer(self, sid: int, nbytes: int, rel_arrivals, now: float = 0.0, kind=None,
+              npix: int = 0) -> bool:
         """Offer a stream; returns True if it was admitted at once."""
         if sid in self.streams:
             raise ValueError(f"stream {sid} offered twice")
         if self.reserve + nbytes > self.budget:
             raise ValueError(f"stream {sid} needs {nbytes} B: never fits the budget")
         self.streams[sid] = _StreamState(sid, int(nbytes), np.asarray(rel_arrivals, float),
-                                         kind if kind is not None else ("bytes", int(nbytes)))
+                                         kind if kind is not None else ("bytes", int(nbytes)),
+                                         int(npix))
         self.queue.append(sid)
         self.admit(now)
         return self.streams[sid].admitted_at is not None
@@ -113,7 +120,8 @@ class Scheduler:
 
     def next_batch(self, now: float) -> List[Tuple[int, int, float]]:
         """Frames that have arrived, one per idle stream, oldest first, at most
-        max_batch; they are marked in flight.  Items: (sid, frame, arrival)."""
+        max_batch (and max_pixels); they are marked in flight.  Items: (sid, frame,
+        arrival)."""
         ready = []
         for sid in self.active:
             st = self.streams[sid]
@@ -123,9 +131,14 @@ class Scheduler:
             if a <= now:
                 ready.append((a, sid))
         ready.sort()
-        items = []
-        for a, sid in ready[: self.max_batch]:
+        items, pix = [], 0
+        for a, sid in ready:
+            if len(items) >= self.max_batch:
+                break
             st = self.streams[sid]
+            if self.max_pixels and items and pix + st.npix > self.max_pixels:
+                break          # oldest first: a later, smaller frame does not jump the queue
+            pix += st.npix
             st.in_flight = True
             items.append((sid, st.next, float(a)))
         return items
@@ -204,7 +217,7 @@ class Server:
     """Continuous-batching server on one GPU (see the module docstring)."""
 
     def __init__(self, budget_bytes: int, max_batch: int = 8, lanes: int = 2, device=None,
-                 seed: int = 0, **cfg):
+                 seed: int = 0, max_pixels: int = 0, **cfg):
         import torch
         from . import batch, bist_cuda, _lib
         self._torch, self._batch, self._bist, self._lib = torch, batch, bist_cuda, _lib
@@ -212,20 +225,23 @@ class Server:
         self.device = torch.device("cuda", torch.cuda.current_device() if idx is None else idx)
         self.budget = int(budget_bytes)
         self.max_batch = int(max_batch)
+        self.max_pixels = int(max_pixels)
         self.lanes = int(lanes)
         self.cfg = cfg
         self.sp_default = int(cfg.get("sp_size", 15))
         self.rng = np.random.Generator(np.random.PCG64(seed))
-        self.requests: Dict[int, StreamRequest] = {}
+        self.requests: Dict[int, StreamRequest] = {}      # added, not yet served
+        self.served: Dict[int, StreamRequest] = {}
         self.labels: Dict[int, object] = {}
         self.videos: Dict[int, object] = {}
         self.batch_sizes: List[int] = []
         self.batch_ms: List[float] = []
         self._spare: Dict[Tuple[int, int], list] = {}
         self._spare_lock = threading.Lock()
+        self._streams = []    # one CUDA stream per lane, kept across runs (warm contexts)
 
     def add(self, req: StreamRequest):
-        if req.sid in self.requests:
+        if req.sid in self.requests or req.sid in self.served:
             raise ValueError(f"stream {req.sid} added twice")
         self.requests[req.sid] = req
 
@@ -235,14 +251,21 @@ class Server:
         return vb + 4 * H * W * (T if req.keep_labels else 1)
 
     def run(self) -> dict:
+        """Serve every stream added since the last run; returns its statistics.  The
+        lanes' CUDA streams (and so their engine contexts and tuned tile shapes) are
+        kept for later runs."""
         torch = self._torch
         reqs = list(self.requests.values())
         if not reqs:
             return {}
+        while len(self._streams) < self.lanes:
+            self._streams.append(torch.cuda.Stream(self.device))
+        self.batch_sizes, self.batch_ms = [], []
         # the largest frame's working buffers for every batch position of every lane
         slot_b = max(self._lib.footprint(r.vid.shape[1], r.vid.shape[2],
                                          r.sp_size or self.sp_default)[1] for r in reqs)
-        sched = Scheduler(self.budget, self.lanes * self.max_batch * slot_b, self.max_batch)
+        sched = Scheduler(self.budget, self.lanes * self.max_batch * slot_b, self.max_batch,
+                          self.max_pixels)
         lock = threading.Lock()
         wake = threading.Condition(lock)
         t0 = time.perf_counter()
@@ -250,15 +273,14 @@ class Server:
         for r in reqs:
             T, H, W = r.vid.shape[0], r.vid.shape[1], r.vid.shape[2]
             sched.offer(r.sid, self.stream_bytes(r), poisson_arrivals(T, r.fps, self.rng), 0.0,
-                        kind=(H, W, T if r.keep_labels else 1))
+                        kind=(H, W, T if r.keep_labels else 1), npix=H * W)
         dev = self.device
         errors = []
 
         def lane(j):
             try:
                 torch.cuda.set_device(dev)
-                cs = torch.cuda.Stream(dev)
-                with torch.cuda.stream(cs):
+                with torch.cuda.stream(self._streams[j]):
                     while True:
                         with lock:
                             if sched.done() or errors:
@@ -313,7 +335,10 @@ class Server:
         self._spare.clear()
         if errors:
             raise RuntimeError("; ".join(errors))
-        return self.stats(sched)
+        out = self.stats(sched)
+        self.served.update(self.requests)
+        self.requests = {}
+        return out
 
     # The state (video + label buffer) of a finished stream is kept and handed to the
     # next stream of the same kind (reset first), as the scheduler's accounting

@@ -78,12 +78,14 @@ def voronoi_video(H: int, W: int, T: int, nseeds: int, sigma: float, seed: int =
 
 
 def voronoi_video_device(H: int, W: int, T: int, nseeds: int, sigma: float, seed: int = 0,
-                         max_shift: float = 4.0, max_rot_deg: float = 1.0, device="cuda"):
+                         max_shift: float = 4.0, max_rot_deg: float = 1.0, device="cuda",
+                         regions: bool = False):
     """voronoi_video's scene model generated on a torch device (for benchmarks that
     need many large videos): the same seeds, colours and motions drawn from the
     numpy generator of `seed`; region maps as the nearest moved seed (first index
     on ties) and the noise from a torch generator seeded with `seed`.  Returns
-    (vid f32 [T,H,W,3], flows f32 [T-1,H,W,2]) on the device."""
+    (vid f32 [T,H,W,3], flows f32 [T-1,H,W,2]) on the device, and the region maps
+    i32 [T,H,W] as a third item when `regions`."""
     import torch
     rng = np.random.Generator(np.random.PCG64(seed))
     seeds = rng.uniform([0, 0], [W, H], size=(nseeds, 2))
@@ -100,6 +102,7 @@ def voronoi_video_device(H: int, W: int, T: int, nseeds: int, sigma: float, seed
                             torch.arange(W, device=dev, dtype=torch.float64), indexing="ij")
     vid = torch.empty((T, H, W, 3), dtype=torch.float32, device=dev)
     flows = torch.empty((max(T - 1, 0), H, W, 2), dtype=torch.float32, device=dev)
+    regs = torch.empty((T, H, W), dtype=torch.int32, device=dev) if regions else None
     cur = torch.from_numpy(seeds).to(dev)
     rows = max(1, (1 << 24) // max(1, W * nseeds))
     for t in range(T):
@@ -109,6 +112,8 @@ def voronoi_video_device(H: int, W: int, T: int, nseeds: int, sigma: float, seed
             dx = xs[y0:y1, :, None] - cur[:, 0]
             dy = ys[y0:y1, :, None] - cur[:, 1]
             reg[y0:y1] = (dx * dx + dy * dy).argmin(-1)
+        if regions:
+            regs[t] = reg
         noise = torch.randn((H, W, 3), generator=g, device=dev, dtype=torch.float32) * sigma
         vid[t] = (colors_t[reg] + noise).clamp_(0, 1)
         if t < T - 1:
@@ -121,7 +126,7 @@ def voronoi_video_device(H: int, W: int, T: int, nseeds: int, sigma: float, seed
             flows[t, ..., 0] = (nx - xs).float()
             flows[t, ..., 1] = (ny - ys).float()
             cur = cur + trans_t
-    return vid, flows
+    return (vid, flows, regs) if regions else (vid, flows)
 
 
 # Workloads (shapes and value distributions of the benchmark configurations).

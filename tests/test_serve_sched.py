@@ -92,3 +92,21 @@ def test_finished_state_is_reused_or_evicted():
     assert s.used == 100
     s.offer(4, 50, [0.0], kind="b")                 # takes over a spare: no fresh bytes
     assert s.reused == 1 and s.used == 100 and s.peak_used <= 100
+
+
+def test_pixel_cap_bounds_batches_oldest_first():
+    s = Scheduler(budget=1000, reserve=0, max_batch=8, max_pixels=1000)
+    s.offer(1, 1, [0.1], npix=600)
+    s.offer(2, 1, [0.2], npix=600)
+    s.offer(3, 1, [0.3], npix=300)
+    s.offer(4, 1, [0.4], npix=2000)        # larger than the cap: still served alone
+    items = s.next_batch(1.0)
+    assert [i[0] for i in items] == [1]     # 1 + 2 would exceed the cap; 3 may not jump 2
+    items = s.next_batch(1.0)
+    assert [i[0] for i in items] == [2, 3]
+    assert [i[0] for i in s.next_batch(1.0)] == [4]
+    # no cap: one batch of everything that arrived
+    s = Scheduler(budget=1000, reserve=0, max_batch=8)
+    for sid in range(3):
+        s.offer(sid, 1, [0.0], npix=10 ** 6)
+    assert len(s.next_batch(0.0)) == 3
