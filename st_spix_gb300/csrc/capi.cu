@@ -73,7 +73,7 @@ struct List {
   int max_npix = 0, max_cap = 0, max_nprev = 0, max_w = 0, max_h = 0;
   long long max_acc = 0, max_sm = 0;
   bool any_prop = false;
-  std::vector<int> tiles_upto[2];  // sweep tiles (32- / 64-wide) of the first i slots
+  std::vector<int> tiles_upto[3];  // sweep tiles (32-, 64-, 16-wide) of the first i slots
   std::vector<long long> segs_upto;  // 32-pixel row segments of the first i slots
 };
 
@@ -112,7 +112,7 @@ struct stspix_ctx {
   std::map<std::pair<const Slot*, int>, FillGraph> fill_graphs;
   // sweep tile autotuner
   std::map<std::pair<unsigned long long, int>, int> sweep_choice;  // (shape, nb) -> variant
-  cudaEvent_t tune_ev[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t tune_ev[kSweepVariants + 1] = {};
   long long tunes = 0;
   int accumulator = 0;            // cfg.accumulator of the batch being run
   int* body_iters = nullptr;       // device: fill-loop iterations run (launch count)
@@ -205,10 +205,27 @@ void prof_harvest(stspix_ctx* ctx) {
   ctx->pending.clear();
 }
 
+// Every kernel is launched with programmatic stream serialization (see pdl.h).
+template <typename... KArgs, typename... Args>
+void launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+              Args... args) {
+  cudaLaunchConfig_t c = {};
+  c.gridDim = grid;
+  c.blockDim = block;
+  c.dynamicSmemBytes = smem;
+  c.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  c.attrs = at;
+  c.numAttrs = 1;
+  cudaLaunchKernelEx(&c, k, args...);
+}
+
 #define LAUNCHG(kernel, grid, block, ...)                                      \
   do {                                                                         \
     cudaEvent_t pe_ = prof_begin(ctx, st);                                     \
-    kernel<<<grid, block, 0, st>>>(__VA_ARGS__);                               \
+    launch_k(kernel, dim3(grid), dim3(block), 0, st, __VA_ARGS__);             \
     ctx->launches++;                                                           \
     prof_end(ctx, st, pe_, #kernel);                                           \
   } while (0)
@@ -372,6 +389,7 @@ void preload_kernels() {
       (const void*)kb_find_border,
       (const void*)kb_sweep_t32,
       (const void*)kb_sweep_t64,
+      (const void*)kb_sweep_t16,
       (const void*)kb_copy_labels,
       (const void*)kb_read_params,
       (const void*)kb_save_prev,
@@ -517,16 +535,16 @@ Slot make_slot(stspix_ctx* ctx, const FrameDesc& f, int cap) {
 List make_list(stspix_ctx* ctx, int off, const std::vector<Slot>& slots) {
   List L;
   L.d = ctx->d_slots + (size_t)off * ctx->bcap;
-  for (int v = 0; v < 2; v++) L.tiles_upto[v].assign(1, 0);
+  for (int v = 0; v < kSweepVariants; v++) L.tiles_upto[v].assign(1, 0);
   L.segs_upto.assign(1, 0);
   Slot* h = ctx->h_slots + (size_t)off * ctx->bcap;
   L.B = (int)slots.size();
   for (int i = 0; i < L.B; i++) {
     Slot s = slots[i];
-    for (int v = 0; v < 2; v++) {
+    for (int v = 0; v < kSweepVariants; v++) {
       if (L.tiles_upto[v].empty()) L.tiles_upto[v].push_back(0);
       s.tile_base[v] = L.tiles_upto[v].back();
-      const int tw = v ? 64 : 32;
+      const int tw = kSweepTileW[v];
       L.tiles_upto[v].push_back(s.tile_base[v] + ((s.W + tw - 1) / tw) * ((s.H + 31) / 32));
     }
     if (L.segs_upto.empty()) L.segs_upto.push_back(0);
@@ -570,10 +588,15 @@ void accumulate_fp(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, int 
   LAUNCHB(kb_accumulate_fp_store, L.max_cap, L, nb, mode);
 }
 
-int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb) {
+// stats_ready: the last sweep of the preceding update_seg already cleared and added
+// the statistics of the first nb slots (see update_seg).
+int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
+                  bool stats_ready = false) {
   ctx->cur_fam = STSPIX_FAM_STATS;
-  LAUNCHB(kb_clear_stats, L.max_cap, L, nb);
-  LAUNCHG(kb_accumulate, acc_blocks(ctx, L, nb), 256, L.d, nb);
+  if (!stats_ready) {
+    LAUNCHB(kb_clear_stats, L.max_cap, L, nb);
+    LAUNCHG(kb_accumulate, acc_blocks(ctx, L, nb), 256, L.d, nb);
+  }
   if (ctx->accumulator) accumulate_fp(ctx, st, L, nb, ctx->accumulator);
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
   LAUNCHB(kb_posterior, L.max_cap, L, nb);
@@ -583,19 +606,30 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb) {
 // update_seg (update_seg.cu:281-311): niters_seg fused sweeps ping-ponging between
 // the labels and a scratch buffer; the border mask is only built when the next
 // iteration's merge reads it.
+// fuse_stats: the first sweep also clears the statistics and the last one adds those
+// of its final labels, so the next update_params skips its clear and accumulate
+// passes (needs two or more sweeps: no sweep reads the statistics in between).
 int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
-               const stspix_config& cfg, bool need_border) {
+               const stspix_config& cfg, bool need_border, bool fuse_stats) {
   ctx->cur_fam = STSPIX_FAM_SWEEP;
   // the first sweep of the call scores every border pixel; the later ones only the
   // active set next to the previous sweep's changes (same labels, see kb_sweep_t*)
-  auto sweep = [&](int v, int parity, int mode) {
+  auto sweep = [&](int v, int parity, int mode, int stats) {
     const unsigned g = (unsigned)std::max(1, L.tiles_upto[v][nb]);
-    if (v) LAUNCHG(kb_sweep_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode);
-    else LAUNCHG(kb_sweep_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode);
+    if (v == 1)
+      LAUNCHG(kb_sweep_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
+    else if (v == 2)
+      LAUNCHG(kb_sweep_t16, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
+    else
+      LAUNCHG(kb_sweep_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
   };
-  // tile-shape autotuner: the first sweep of a batch size class runs both tile widths
-  // on the same input (a sweep reads only the labels at its start, so both write the
-  // same output) and the faster is kept for that class.  The class is the number of
+  const bool fuse = fuse_stats && cfg.niters_seg >= 2;
+  auto stats_of = [&](int it) {
+    return !fuse ? 0 : it == 0 ? 1 : it == cfg.niters_seg - 1 ? 2 : 0;
+  };
+  // tile-shape autotuner: the first sweep of a batch size class runs every tile width
+  // on the same input (a sweep reads only the labels at its start, so all write the
+  // same output) and the fastest is kept for that class.  The class is the number of
   // 32x32 tiles of the sweeping slots in quarter octaves: the choice depends on how
   // well the tiles fill the SMs, and mixed serving batches then tune a handful of
   // times instead of once per combination of frame sizes.
@@ -607,23 +641,26 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   if (ch != ctx->sweep_choice.end()) {
     v = ch->second;
   } else if (cfg.niters_seg > 0) {
-    float ms[2] = {0.f, 0.f};
     CK(cudaEventRecord(ctx->tune_ev[0], st));
-    sweep(0, 0, 0);
-    CK(cudaEventRecord(ctx->tune_ev[1], st));
-    sweep(1, 0, 0);
-    CK(cudaEventRecord(ctx->tune_ev[2], st));
-    CK(cudaEventSynchronize(ctx->tune_ev[2]));
-    cudaEventElapsedTime(&ms[0], ctx->tune_ev[0], ctx->tune_ev[1]);
-    cudaEventElapsedTime(&ms[1], ctx->tune_ev[1], ctx->tune_ev[2]);
-    v = ms[1] <= ms[0] ? 1 : 0;
+    for (int c = 0; c < kSweepVariants; c++) {
+      sweep(c, 0, 0, stats_of(0));
+      CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
+    }
+    CK(cudaEventSynchronize(ctx->tune_ev[kSweepVariants]));
+    float best = 0.f;
+    v = 0;
+    for (int c = 0; c < kSweepVariants; c++) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ctx->tune_ev[c], ctx->tune_ev[c + 1]);
+      if (c == 0 || ms < best) { best = ms; v = c; }
+    }
     ctx->sweep_choice[key] = v;
     ctx->tunes++;
     it0 = 1;
   } else {
     v = 1;
   }
-  for (int it = it0; it < cfg.niters_seg; it++) sweep(v, it & 1, it > 0 ? 1 : 0);
+  for (int it = it0; it < cfg.niters_seg; it++) sweep(v, it & 1, it > 0 ? 1 : 0, stats_of(it));
   if (cfg.niters_seg & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;
@@ -642,7 +679,7 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
   LAUNCHG(kb_split_bfs, dim3(256, (unsigned)nb), 128, L.d);  // 1024 warps per slot
   {
     cudaEvent_t pe_ = prof_begin(ctx, st);
-    kb_split_bfs_big<<<dim3(8, (unsigned)nb), 256, kBfsBigSmem, st>>>(L.d);
+    launch_k(kb_split_bfs_big, dim3(8, (unsigned)nb), dim3(256), kBfsBigSmem, st, L.d);
     ctx->launches++;
     prof_end(ctx, st, pe_, "kb_split_bfs_big");
   }
@@ -702,13 +739,19 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector
   const int P = cfg.sm_period > 0 ? cfg.sm_period : 4;
   const int maxn = L.B ? nit[0] : 0;
   int nb = L.B;
+  // the statistics of the first nb slots were added by the last sweep of the
+  // previous iteration (fused statistics; integer sums, so identical to a separate
+  // pass); the int64 accumulator only
+  bool stats_ready = false;
+  const bool fuse = ctx->accumulator == 0;
   for (int idx = 0; idx < maxn; idx++) {
     while (nb > 0 && nit[nb - 1] <= idx) nb--;
     if (stop_after >= 0 && idx == stop_after) {
       if (extra_update && (r = update_params(ctx, st, L, nb))) return r;
       return STSPIX_OK;
     }
-    if ((r = update_params(ctx, st, L, nb))) return r;
+    if ((r = update_params(ctx, st, L, nb, stats_ready))) return r;
+    stats_ready = false;
     if (idx > cfg.sm_start) {
       if (idx % P == 0) {
         count_b += 1;
@@ -725,7 +768,9 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector
     }
     const int nx = idx + 1;
     const bool merge_next = nx < maxn && nx > cfg.sm_start && nx % P == P / 2;
-    if ((r = update_seg(ctx, st, L, nb, cfg, merge_next || stop_after >= 0))) return r;
+    const bool fuse_now = fuse && nx < maxn && !(stop_after >= 0 && nx == stop_after);
+    if ((r = update_seg(ctx, st, L, nb, cfg, merge_next || stop_after >= 0, fuse_now))) return r;
+    stats_ready = fuse_now && cfg.niters_seg >= 2;
   }
   if (stop_after >= 0) {
     if (extra_update && (r = update_params(ctx, st, L, L.B))) return r;

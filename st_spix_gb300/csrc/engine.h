@@ -14,6 +14,7 @@
 //   R7 reference reads of uninitialised memory are zero.
 //   R8 IEEE FP32/FP64 with no FMA contraction (-fmad=false); Hastings in FP64.
 #pragma once
+#include "pdl.h"
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -25,6 +26,8 @@ constexpr int kFxAppShift = 28;
 constexpr int kFxSqShift = 20;
 constexpr int kFxFlowShift = 24;
 constexpr int kFillBreakIter = 1000;      // fill_missing.cu: break_iter
+constexpr int kSweepVariants = 3;         // sweep tile shapes: 32x32, 64x32, 16x32
+constexpr int kSweepTileW[kSweepVariants] = {32, 64, 16};
 
 // Packed record read by the boundary sweep: the fields calc_joint reads
 // (update_seg.cu:194-259), already converted to the types it uses.  The reference
@@ -148,7 +151,7 @@ struct Slot {
   unsigned long long *rbest, *ccbest;
   int* bbox;               // [4*(cap+2)]: x0, x1, y0, y1 per superpixel (split BFS)
   Scalars* sc;
-  int tile_base[2];        // first sweep tile of this slot in the batch (32- / 64-wide)
+  int tile_base[3];        // first sweep tile of this slot in the batch (32-, 64-, 16-wide)
 };
 
 // kb_scalars operations.

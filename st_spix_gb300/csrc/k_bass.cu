@@ -64,12 +64,14 @@ __device__ __forceinline__ int hex_label(int x, int y, double Hh, double w, int 
 
 __global__ void k_init_hex(int* __restrict__ seg, int H, int W, double Hh, double w, int nx,
                            int ny) {
+  pdl_enter();
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= H * W) return;
   seg[idx] = hex_label(idx % W, idx / W, Hh, w, nx, ny);
 }
 
 __global__ void kb_init_hex(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= S.npix) return;
@@ -81,6 +83,7 @@ __global__ void kb_init_hex(const Slot* __restrict__ slots) {
 // exclusive scan, remap.
 // mode 0: hex ids [0, nraw); mode 1: ids [lo, max_spix] of the finished frame.
 __global__ void kb_mark_present(const Slot* __restrict__ slots, int mode) {
+  pdl_enter();
   SLOT_Y;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.npix) return;
@@ -96,6 +99,7 @@ __global__ void kb_mark_present(const Slot* __restrict__ slots, int mode) {
 //   mode 2: relabel mint flags (n = cap)      -> total = minted ids
 //   mode 3: final presence (n = max_spix+1-lo) -> total = live new ids
 __global__ void kb_scan(const Slot* __restrict__ slots, int mode) {
+  pdl_enter();
   const Slot& S = slots[blockIdx.x];
   if (mode == 2 && !S.mode) return;  // mint flags exist on propagated slots only
   __shared__ int part[1024];
@@ -123,6 +127,7 @@ __global__ void kb_scan(const Slot* __restrict__ slots, int mode) {
 }
 
 __global__ void kb_remap(const Slot* __restrict__ slots, int mode) {
+  pdl_enter();
   SLOT_Y;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.npix) return;
@@ -133,6 +138,7 @@ __global__ void kb_remap(const Slot* __restrict__ slots, int mode) {
 
 // fill_new_params_from_old (compact_spix.cu:220-265): gather moved fields.
 __global__ void kb_compact_gather(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const SpDev& tmp = S.tmp;
@@ -162,6 +168,7 @@ __global__ void kb_compact_gather(const Slot* __restrict__ slots) {
 
 // fill_old_params_from_new (compact_spix.cu:268-290).
 __global__ void kb_compact_scatter(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const SpDev& tmp = S.tmp;
@@ -191,6 +198,7 @@ __global__ void kb_compact_scatter(const Slot* __restrict__ slots) {
 // init_sp_params_kernel + mark_active_contiguous (init_sparams.cu:45-166,
 // 195-286) for a BASS frame; *nspix live ids, count = npix / nspix.
 __global__ void kb_init_bass_params(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (S.mode) return;
   const int sp_size = S.sp_size;
@@ -220,6 +228,7 @@ __global__ void kb_init_bass_params(const Slot* __restrict__ slots) {
 
 // prior_mu_app := initial mean (calc_summ_stats, update_params.cu:142-203).
 __global__ void kb_init_prior_mu(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (S.mode) return;
   const SpDev& sp = S.sp;
@@ -269,6 +278,7 @@ __device__ __forceinline__ long long warp_incl_scan(long long v, int lane) {
 // Persistent grid: every warp walks the 32-pixel row segments of every slot in
 // turn (the first B slots), so frames of uneven size need no per-frame grid.
 __global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ slots, int B) {
+  pdl_enter();
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -320,6 +330,7 @@ __global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ sl
 // sums in 2^-28 units (exact for the magnitudes of colour sums), so the posterior sees
 // the precision of that accumulator.  Counts and positions stay exact.
 __global__ void kb_accumulate_fp(const Slot* __restrict__ slots, int mode) {
+  pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
@@ -336,6 +347,7 @@ __global__ void kb_accumulate_fp(const Slot* __restrict__ slots, int mode) {
 }
 
 __global__ void kb_accumulate_fp_store(const Slot* __restrict__ slots, int mode) {
+  pdl_enter();
   SLOT_Y;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= S.sp.cap) return;
@@ -347,6 +359,7 @@ __global__ void kb_accumulate_fp_store(const Slot* __restrict__ slots, int mode)
 }
 
 __global__ void kb_accumulate_fp_clear(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= S.sp.cap) return;
@@ -358,6 +371,7 @@ __global__ void kb_accumulate_fp_clear(const Slot* __restrict__ slots) {
 __global__ void k_label_stats(const float* __restrict__ img, const int* __restrict__ lab,
                               long long npix, int n, int mode, long long* iacc, float* facc,
                               double* dacc) {
+  pdl_enter();
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= npix) return;
   const int k = lab[t];
@@ -381,6 +395,7 @@ __global__ void k_label_stats(const float* __restrict__ img, const int* __restri
 
 __global__ void k_label_stats_out(int n, int mode, const long long* iacc, const float* facc,
                                   const double* dacc, double* out) {
+  pdl_enter();
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   out[7 * (size_t)k] = (double)iacc[7 * (size_t)k];
@@ -407,29 +422,42 @@ __device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in
 }
 
 __device__ __forceinline__ void posterior_one(const SpDev& sp, int sp_size, Scalars* sc, int k) {
-  int count_int = sp.count[k];
-  bool live = sp.valid[k] && count_int > 0;
-  if (sp.valid[k] && count_int <= 0) sp.valid[k] = 0;
+  // loads in two round trips: the id's status, then (live ids only) every other
+  // input at once, both prior covariances included, instead of a chain of dependent
+  // loads behind each branch
+  const int count_int = sp.count[k];
+  const uint8_t valid = sp.valid[k];
+  const uint8_t prop = sp.prop[k];
+  const float pc = sp.prior_count[k];
+  bool live = valid && count_int > 0;
+  if (valid && count_int <= 0) sp.valid[k] = 0;
   if (!live) {
     for (int c = 0; c < 3; c++) { sp.mu_app[3 * k + c] = 0.f; sp.sigma_shape[3 * k + c] = 0.0; }
     sp.mu_shape[2 * k] = 0.0; sp.mu_shape[2 * k + 1] = 0.0;
     return;
   }
-  float pc = sp.prior_count[k];
+  const long long* ap = sp.acc + 8 * (size_t)k;
+  long long a[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) a[c] = ap[c];
+  double q[3], icv[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    q[c] = sp.sample_sigma_shape[3 * k + c];
+    icv[c] = sp.prior_icov[3 * k + c];
+  }
   double count = count_int * 1.0;
   double total_count = (double)count_int + pc * 50;
   double px, py, pz;
-  if (sp.prop[k]) {
-    smooth_prior(sp.sample_sigma_shape[3 * k], sp.sample_sigma_shape[3 * k + 1],
-                 sp.sample_sigma_shape[3 * k + 2], (int)pc, pc, sp_size, &px, &py, &pz);
+  if (prop) {
+    smooth_prior(q[0], q[1], q[2], (int)pc, pc, sp_size, &px, &py, &pz);
   } else {
-    px = sp.prior_icov[3 * k]; py = sp.prior_icov[3 * k + 1]; pz = sp.prior_icov[3 * k + 2];
+    px = icv[0]; py = icv[1]; pz = icv[2];
   }
   double pr_det = px * pz - py * py;
   if (!(pr_det > 0)) atomicExch(&sc->status, STSPIX_ERR_DEGENERATE);
   pr_det = sqrt(pr_det);
   double psx = pc / pr_det * px, psy = pc / pr_det * py, psz = pc / pr_det * pz;
-  const long long* a = sp.acc + 8 * (size_t)k;
   float mr = (float)(fx_unq(a[0], kFxAppShift) / count);
   float mg = (float)(fx_unq(a[1], kFxAppShift) / count);
   float mb = (float)(fx_unq(a[2], kFxAppShift) / count);
@@ -464,6 +492,7 @@ __device__ __forceinline__ void posterior_one(const SpDev& sp, int sp_size, Scal
 }
 
 __global__ void kb_posterior(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   FOR_SP(k, S.sp.cap) posterior_one(S.sp, S.sp_size, S.sc, k);
 }
@@ -471,6 +500,7 @@ __global__ void kb_posterior(const Slot* __restrict__ slots) {
 // clear_fields + the helper memset (update_params.cu:54-88, :26): zero the counts
 // and the sums of every slot.
 __global__ void kb_clear_stats(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= S.sp.cap) return;
@@ -482,6 +512,7 @@ __global__ void kb_clear_stats(const Slot* __restrict__ slots) {
 
 // store_sample_sigma_shape_k (update_params.cu:397-438).
 __global__ void kb_store_sample(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   FOR_SP(k, sp.cap) {
@@ -509,6 +540,7 @@ __global__ void kb_store_sample(const Slot* __restrict__ slots) {
 // Border masks (seg_utils.cu:164-195 and 218-257).
 __global__ void k_find_border(const int* __restrict__ seg, uint8_t* __restrict__ border, int H,
                               int W) {
+  pdl_enter();
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= H * W) return;
   int x = idx % W, y = idx / W;
@@ -519,6 +551,7 @@ __global__ void k_find_border(const int* __restrict__ seg, uint8_t* __restrict__
 }
 
 __global__ void kb_find_border(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= S.npix) return;
@@ -533,6 +566,7 @@ __global__ void kb_find_border(const Slot* __restrict__ slots) {
 
 __global__ void k_find_border_end(const int* __restrict__ seg, uint8_t* __restrict__ border,
                                   int H, int W, int nframes) {
+  pdl_enter();
   long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long npix = (long long)H * W;
   if (gi >= npix * nframes) return;
@@ -559,6 +593,7 @@ __global__ void k_find_border_end(const int* __restrict__ seg, uint8_t* __restri
 __global__ void k_overlay(float* __restrict__ out, const float* __restrict__ img,
                           const float* __restrict__ color, const uint8_t* __restrict__ border,
                           long long n) {
+  pdl_enter();
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   if (border[t]) {
@@ -624,15 +659,67 @@ struct SweepTile {
   static constexpr int kLX = TX + 2 * kSH, kLY = TY + 2 * kSH;      // staged labels
   static constexpr int kIX = TX + 2 * (kSH - 1), kIY = TY + 2 * (kSH - 1);  // image / border
   static constexpr int kMaxList = (TX / 2 + kSH - 1) * (TY / 2 + kSH - 1);
+  static_assert(kIX < 256 && kIY < 256, "list entries pack (ly << 8) | lx");
   int L[kLX * kLY];
-  float I[kIX * kIY * 3];
-  short list[4][kMaxList];   // border pixels of each parity phase
+  int L0[TX * TY];                    // the tile's labels at the sweep start
+  unsigned short list[4][kMaxList];   // border pixels of each parity phase, (ly << 8) | lx
   int cnt[4];
   // active-set sweeps: change flags of the label region as row bitmasks (bit x of
   // row y = label-region pixel (x, y)), dilated by 4 pixels
   unsigned long long act[2][kLY];
   int any;
 };
+
+// Statistics of a tile's final labels (the last sweep of an update_seg call adds
+// them, so the next update_params needs no separate pass): the same warp-run scatter
+// as kb_accumulate over the tile's rows (16-wide tiles: two rows per warp pass, a
+// row change starts a new run).  The sums are integers, so the totals equal
+// kb_accumulate's whatever the segmentation into runs.
+template <int TX, int TY>
+__device__ __noinline__ void tile_accumulate(const Slot& S, const int* __restrict__ L,
+                                                int kLX, int tx0, int ty0) {
+  constexpr int kSegs = (TX + 31) / 32;               // 32-pixel segments per row
+  constexpr int kRows = TX >= 32 ? 1 : 32 / TX;       // rows per warp pass
+  constexpr int kPasses = (TY / kRows) * kSegs;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int H = S.H, W = S.W;
+  const SpDev& sp = S.sp;
+  const int cap = sp.cap;
+  for (int ps = warp; ps < kPasses; ps += blockDim.x >> 5) {
+    int row, x;
+    if (TX >= 32) { row = ps / kSegs; x = (ps % kSegs) * 32 + lane; }
+    else { row = ps * kRows + lane / TX; x = lane % TX; }
+    const int gx = tx0 + x, gy = ty0 + row;
+    int k = -1;
+    long long q0 = 0, q1 = 0, q2 = 0;
+    if (gx < W && gy < H) {
+      k = L[(row + kSH) * kLX + (x + kSH)];
+      if (k >= 0) {
+        const float* p = S.img + 3 * ((size_t)gy * W + gx);
+        q0 = fx_q(p[0], kFxAppShift);
+        q1 = fx_q(p[1], kFxAppShift);
+        q2 = fx_q(p[2], kFxAppShift);
+      }
+    }
+    const int kprev = __shfl_up_sync(0xffffffffu, k, 1);
+    const int knext = __shfl_down_sync(0xffffffffu, k, 1);
+    const int rprev = __shfl_up_sync(0xffffffffu, row, 1);
+    const int rnext = __shfl_down_sync(0xffffffffu, row, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != k || rprev != row);
+    const bool tail = lane == 31 || knext != k || rnext != row;
+    const long long p0 = warp_incl_scan(q0, lane);
+    const long long p1 = warp_incl_scan(q1, lane);
+    const long long p2 = warp_incl_scan(q2, lane);
+    const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+    const int src = start > 0 ? start - 1 : 0;
+    long long b0 = __shfl_sync(0xffffffffu, p0, src);
+    long long b1 = __shfl_sync(0xffffffffu, p1, src);
+    long long b2 = __shfl_sync(0xffffffffu, p2, src);
+    if (start == 0) b0 = b1 = b2 = 0;
+    if (tail && k >= 0 && k < cap)
+      add_run_sums(sp, k, gy, gx - (lane - start), gx, p0 - b0, p1 - b1, p2 - b2);
+  }
+}
 
 // Active-set sweeps.  The parameters are fixed across the sweeps of one update_seg
 // call and a pixel's decision depends only on its 3x3 labels (after the earlier
@@ -645,12 +732,11 @@ struct SweepTile {
 template <int TX, int TY>
 __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int parity, float s2,
                                            float potts, SweepTile<TX, TY>& sm,
-                                           const unsigned* lut_bits, int mode) {
+                                           const unsigned* lut_bits, int mode, int stats) {
   constexpr int kTX = TX, kTY = TY;
   constexpr int kLX = SweepTile<TX, TY>::kLX, kLY = SweepTile<TX, TY>::kLY;
   constexpr int kIX = SweepTile<TX, TY>::kIX, kIY = SweepTile<TX, TY>::kIY;
   int* L = sm.L;
-  float* I = sm.I;
   auto& list = sm.list;
   int* cnt = sm.cnt;
 
@@ -667,8 +753,29 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   const uint8_t* __restrict__ chg_in = S.chg[parity ^ 1];
   uint8_t* __restrict__ chg_out = S.chg[parity];
   static_assert(kLX <= 128, "label region wider than two 64-bit words");
+  // The label region is loaded first, into registers: warp w takes rows w, w + 8, ...
+  // in 32-label chunks, every load issued before any is used, so the block waits for
+  // one memory round trip (overlapping the change-flag loads of active-set sweeps);
+  // the tile's part is kept in shared memory for the change flags at the end (no
+  // second read of the labels).
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kRW = (kLY + 7) / 8, kCK = (kLX + 31) / 32;
+  int lv[kRW][kCK];
+#pragma unroll
+  for (int a = 0; a < kRW; a++) {
+    const int r = warp + 8 * a, gy = ry0 + r;
+    const bool row_ok = r < kLY && gy >= 0 && gy < H;
+#pragma unroll
+    for (int c = 0; c < kCK; c++) {
+      const int x = lane + 32 * c, gx = rx0 + x;
+      lv[a][c] = (row_ok && x < kLX && gx >= 0 && gx < W) ? seg_in[gy * W + gx] : -1;
+    }
+  }
+  // tile pixels of the staging layout: (a, c) -> label-region (r, x)
+  auto in_tile = [&](int r, int x) {
+    return r >= kSH && r < kSH + kTY && x >= kSH && x < kSH + kTX && ry0 + r < H && rx0 + x < W;
+  };
   if (mode) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long* a0 = sm.act[0];
     unsigned long long* a1 = sm.act[1];
     if (threadIdx.x == 0) sm.any = 0;
@@ -690,12 +797,23 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
     __syncthreads();
     if (!sm.any) {
       // nothing within reach changed: the tile keeps its labels
-      for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x) {
-        const int gx = tx0 + i % kTX, gy = ty0 + i / kTX;
-        if (gx < W && gy < H) {
-          seg_out[gy * W + gx] = seg_in[gy * W + gx];
-          chg_out[gy * W + gx] = 0;
+#pragma unroll
+      for (int a = 0; a < kRW; a++) {
+        const int r = warp + 8 * a;
+#pragma unroll
+        for (int c = 0; c < kCK; c++) {
+          const int x = lane + 32 * c;
+          if (r < kLY && x < kLX && in_tile(r, x)) {
+            const size_t g = (size_t)(ry0 + r) * W + (rx0 + x);
+            seg_out[g] = lv[a][c];
+            chg_out[g] = 0;
+            if (stats == 2) L[r * kLX + x] = lv[a][c];
+          }
         }
+      }
+      if (stats == 2) {
+        __syncthreads();
+        tile_accumulate<TX, TY>(S, L, kLX, tx0, ty0);
       }
       return;
     }
@@ -720,51 +838,20 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
     }
     __syncthreads();
     if (r < kLY) { a0[r] = v0; a1[r] = v1; }
-    // (the staging below ends with a barrier before the border pass reads act)
+    // (the barrier after the label stores below orders these before the border pass)
   }
-  // Staging: every thread issues all of its loads before the first store, so the
-  // block waits for one memory round trip, not one per element.
-  {
-    constexpr int kNL = 8;  // labels per thread and batch
+  // labels to shared memory (colours are not staged: the scored border pixels read
+  // theirs from global memory)
 #pragma unroll
-    for (int b0 = 0; b0 < kLX * kLY; b0 += 256 * kNL) {
-      int lv[kNL];
+  for (int a = 0; a < kRW; a++) {
+    const int r = warp + 8 * a;
 #pragma unroll
-      for (int j = 0; j < kNL; j++) {
-        const int i = b0 + threadIdx.x + 256 * j;
-        const int gx = rx0 + i % kLX, gy = ry0 + i / kLX;
-        lv[j] = (i < kLX * kLY && gx >= 0 && gx < W && gy >= 0 && gy < H) ? seg_in[gy * W + gx]
-                                                                            : -1;
-      }
-#pragma unroll
-      for (int j = 0; j < kNL; j++) {
-        const int i = b0 + threadIdx.x + 256 * j;
-        if (i < kLX * kLY) L[i] = lv[j];
-      }
-    }
-  }
-  if (!mode) {
-    // the image region as rows of 3 * kIX floats (same layout as I), in batches of
-    // 8 loads per thread (active-set sweeps score few pixels and read their colours
-    // from global memory instead)
-    constexpr int kRow = 3 * kIX;
-    constexpr int kNF = kIY * kRow;
-    constexpr int kNI = 8;
-#pragma unroll
-    for (int b0 = 0; b0 < kNF; b0 += 256 * kNI) {
-      float iv[kNI];
-#pragma unroll
-      for (int j = 0; j < kNI; j++) {
-        const int f = b0 + threadIdx.x + 256 * j;
-        const int r = f / kRow, c = f % kRow;
-        const int gy = iy0 + r, gc = 3 * ix0 + c;
-        iv[j] = (f < kNF && gy >= 0 && gy < H && gc >= 0 && gc < 3 * W)
-                    ? img[(size_t)gy * 3 * W + gc] : 0.f;
-      }
-#pragma unroll
-      for (int j = 0; j < kNI; j++) {
-        const int f = b0 + threadIdx.x + 256 * j;
-        if (f < kNF) I[f] = iv[j];
+    for (int c = 0; c < kCK; c++) {
+      const int x = lane + 32 * c;
+      if (r < kLY && x < kLX) {
+        L[r * kLX + x] = lv[a][c];
+        if (r >= kSH && r < kSH + kTY && x >= kSH && x < kSH + kTX)
+          sm.L0[(r - kSH) * kTX + (x - kSH)] = lv[a][c];
       }
     }
   }
@@ -773,7 +860,6 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   // border pixels of parity class k inside the tile grown by 3-k pixels are listed
   // for phase k, so each phase scores only its border pixels, densely.
   // (appends are warp-aggregated: one shared atomic per warp and phase)
-  const int lane = threadIdx.x & 31;
   for (int base = 0; base < kIX * kIY; base += blockDim.x) {
     const int i = base + threadIdx.x;
     int ph = -1;
@@ -809,15 +895,17 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       int at = 0;
       if (lane == leader) at = atomicAdd(&cnt[c], __popc(m));
       at = __shfl_sync(0xffffffffu, at, leader);
-      if (ph == c) list[c][at + __popc(m & ((1u << lane) - 1))] = (short)i;
+      if (ph == c)
+        list[c][at + __popc(m & ((1u << lane) - 1))] =
+            (unsigned short)(((i / kIX) << 8) | (i % kIX));
     }
   }
   __syncthreads();
   for (int ph = 0; ph < 4; ph++) {
     const int n = cnt[ph];
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
-      int bi = list[ph][j];
-      int lxi = bi % kIX, lyi = bi / kIX;
+      const int bi = list[ph][j];
+      const int lxi = bi & 255, lyi = bi >> 8;
       int gx = ix0 + lxi, gy = iy0 + lyi;
       int p = (lyi + 1) * kLX + (lxi + 1);
       int C = L[p];
@@ -847,7 +935,7 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       const int dN = 8 - __popc(cN), dW = 8 - __popc(cW), dS = 8 - __popc(cS),
                 dE = 8 - __popc(cE);
       if (N >= cap || S >= cap || Wl >= cap || E >= cap) continue;
-      const float* pix = mode ? img + 3 * ((size_t)gy * W + gx) : &I[3 * bi];
+      const float* pix = img + 3 * ((size_t)gy * W + gx);
       float best = -9999.f;
       int bl = C;
       if (N >= 0) joint(pix, gx, gy, rec[N], N, s2, (float)dN, potts, &best, &bl);
@@ -866,19 +954,22 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
     }
     __syncthreads();
   }
+  // write back the tile, with change flags against the labels at the sweep start
   for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x) {
-    int gx = tx0 + i % kTX, gy = ty0 + i / kTX;
+    const int x = i % kTX, y = i / kTX;
+    const int gx = tx0 + x, gy = ty0 + y;
     if (gx < W && gy < H) {
-      const int v = L[(gy - ry0) * kLX + (gx - rx0)];
+      const int v = L[(y + kSH) * kLX + (x + kSH)];
       seg_out[gy * W + gx] = v;
-      chg_out[gy * W + gx] = v != seg_in[gy * W + gx];
+      chg_out[gy * W + gx] = v != sm.L0[i];
     }
   }
+  if (stats == 2) tile_accumulate<TX, TY>(S, L, kLX, tx0, ty0);
 }
 
 template <int TX, int TY>
 __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B, int parity,
-                                           float s2, float potts, int mode) {
+                                           float s2, float potts, int mode, int stats) {
   __shared__ SweepTile<TX, TY> sm;
   __shared__ unsigned lut_bits[8];
   if (threadIdx.x < 8) {
@@ -886,7 +977,7 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
     for (int b = 0; b < 32; b++) w |= (unsigned)(c_simple_lut[threadIdx.x * 32 + b] != 0) << b;
     lut_bits[threadIdx.x] = w;
   }
-  const int v = TX == 32 ? 0 : 1;   // which tile_base of the slots
+  const int v = TX == 32 ? 0 : TX == 64 ? 1 : 2;   // which tile_base of the slots
   const int t = blockIdx.x;
   int lo = 0, hi = B - 1;
   while (lo < hi) {
@@ -896,26 +987,51 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
   const Slot& S = slots[lo];
   const int tl = t - S.tile_base[v];
   const int tiles_x = (S.W + TX - 1) / TX;
-  sweep_tile<TX, TY>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits, mode);
+  if (stats == 1) {
+    // the clear_fields part of update_params (kb_clear_stats) for this tile's share of
+    // the ids; no sweep reads the counts or sums
+    const int ntiles = tiles_x * ((S.H + TY - 1) / TY);
+    const int cap = S.sp.cap, chunk = (cap + ntiles - 1) / ntiles;
+    const int k1 = min(cap, (tl + 1) * chunk);
+    for (int k = tl * chunk + threadIdx.x; k < k1; k += blockDim.x) {
+      S.sp.count[k] = 0;
+      long long* a = S.sp.acc + 8 * (size_t)k;
+#pragma unroll
+      for (int c = 0; c < 8; c++) a[c] = 0;
+    }
+  }
+  sweep_tile<TX, TY>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits, mode,
+                     stats);
 }
 
 // One block per tile of the batch (grid = the batch's total tile count).
 // mode 0: every border pixel (first sweep of an update_seg call); 1: active set.
+// stats 1: also clear the statistics (first sweep); 2: also add the statistics of the
+// final labels (last sweep); 0: neither.
 __global__ void __launch_bounds__(256) kb_sweep_t32(const Slot* __restrict__ slots, int B,
                                                     int parity, float s2, float potts,
-                                                    int mode) {
-  sweep_flat<32, 32>(slots, B, parity, s2, potts, mode);
+                                                    int mode, int stats) {
+  pdl_enter();
+  sweep_flat<32, 32>(slots, B, parity, s2, potts, mode, stats);
 }
-__global__ void __launch_bounds__(256) kb_sweep_t64(const Slot* __restrict__ slots, int B,
+__global__ void __launch_bounds__(256, 5) kb_sweep_t64(const Slot* __restrict__ slots, int B,
                                                     int parity, float s2, float potts,
-                                                    int mode) {
-  sweep_flat<64, 32>(slots, B, parity, s2, potts, mode);
+                                                    int mode, int stats) {
+  pdl_enter();
+  sweep_flat<64, 32>(slots, B, parity, s2, potts, mode, stats);
+}
+__global__ void __launch_bounds__(256) kb_sweep_t16(const Slot* __restrict__ slots, int B,
+                                                    int parity, float s2, float potts,
+                                                    int mode, int stats) {
+  pdl_enter();
+  sweep_flat<16, 32>(slots, B, parity, s2, potts, mode, stats);
 }
 
 // ---------------------------------------------------------------------------
 // Parameter read-out (read_params, sparams_io.cu:190-286) and prior update
 // (update_prior_kernel, sparams_io.cu:584-640) into the caller's SoA params.
 __global__ void kb_read_params(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const stspix_params& out = S.pout;
@@ -947,6 +1063,7 @@ __global__ void kb_read_params(const Slot* __restrict__ slots) {
 
 // Per-slot scalar steps, one thread per slot.
 __global__ void kb_scalars(const Slot* __restrict__ slots, int B, int op) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B) return;
   const Slot& S = slots[i];
@@ -976,6 +1093,7 @@ __global__ void kb_scalars(const Slot* __restrict__ slots, int B, int op) {
 
 // flags := 0 (cap + 2 entries) before a presence scan.
 __global__ void kb_clear_flags(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < S.cap + 2) S.flags[k] = 0;
@@ -983,18 +1101,21 @@ __global__ void kb_clear_flags(const Slot* __restrict__ slots) {
 
 // Keep a copy of the finished labels where the slot's video stream resides.
 __global__ void kb_save_prev(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (S.resident_labels && i < S.npix) S.resident_labels[i] = S.seg[i];
 }
 
 __global__ void kb_copy_labels(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < S.npix) S.seg[i] = S.seg_alt[i];
 }
 
 __global__ void k_dump_state(SpDev sp, stspix_state_dump d) {
+  pdl_enter();
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sp.cap || k >= d.capacity) return;
   if (d.count) d.count[k] = sp.count[k];

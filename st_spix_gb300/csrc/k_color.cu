@@ -13,9 +13,12 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pdl.h"
+
 namespace stspix {
 
 __global__ void k_rgb2lab(const float* __restrict__ rgb, float* __restrict__ lab, long long npix) {
+  pdl_enter();
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= npix) return;
   const double sB = (double)rgb[3 * t];
@@ -43,6 +46,7 @@ __global__ void k_rgb2lab(const float* __restrict__ rgb, float* __restrict__ lab
 }
 
 __global__ void k_lab2rgb(const float* __restrict__ lab, float* __restrict__ rgb, long long npix) {
+  pdl_enter();
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= npix) return;
   const double L = lab[3 * t] * (-100);
@@ -78,6 +82,7 @@ __global__ void k_lab2rgb(const float* __restrict__ lab, float* __restrict__ rgb
 // rescale_image_kernel (rgb2lab.cu:184-198): 8-bit frames to float, divided by mval.
 __global__ void k_rescale_u8(const uint8_t* __restrict__ in, float* __restrict__ out,
                              long long nvals, float mval) {
+  pdl_enter();
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nvals) return;
   out[t] = float(in[t] / mval);

@@ -15,6 +15,7 @@ namespace stspix {
 // aggregated before the atomics.
 // Clear the per-previous-superpixel sums and the warp targets of every slot.
 __global__ void kb_prop_clear(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < S.n_prev) {
@@ -34,6 +35,7 @@ __global__ void kb_prop_clear(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_flow_pool(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const int* __restrict__ lab = S.prev_labels;
   const float* __restrict__ flow = S.flow;
@@ -69,6 +71,7 @@ __global__ void kb_flow_pool(const Slot* __restrict__ slots) {
 
 // normz + centres = mu_shape + mean flow (shift_and_fill.cu:140-150).
 __global__ void kb_flow_mean(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const int n = S.n_prev;
   const int* __restrict__ cnt = S.cnt_pool;
@@ -88,6 +91,7 @@ __global__ void kb_flow_mean(const Slot* __restrict__ slots) {
 // Forward warp by the rounded mean flow (shift_labels_kernel, shift_labels.cu:33-112),
 // collisions resolved by the smallest packed (size, id) (R4).
 __global__ void kb_shift(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const int* __restrict__ lab = S.prev_labels;
   const int H = S.H, W = S.W, n = S.n_prev;
@@ -132,6 +136,7 @@ __device__ __forceinline__ void append_hole(const Slot& S, int t, bool hole, boo
 }
 
 __global__ void kb_shift_decode(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const int* __restrict__ hits = S.hits;
   const unsigned long long* __restrict__ best = S.best;
@@ -149,6 +154,7 @@ __global__ void kb_shift_decode(const Slot* __restrict__ slots) {
 // which 0: counts after the shift (cs), 1: after the fill (cf).  One 16-pixel
 // row run per thread; runs of equal labels are counted before the atomic.
 __global__ void kb_count_labels(const Slot* __restrict__ slots, int which) {
+  pdl_enter();
   SLOT_Y;
   constexpr int R = 16;
   const int W = S.W, n = S.n_prev;
@@ -187,6 +193,7 @@ __device__ __forceinline__ const int* fill_list(const Slot& S) {
 }
 
 __global__ void kb_fill_begin(const Slot* __restrict__ slots, int B) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B) return;
   Scalars* sc = slots[i].sc;
@@ -199,6 +206,7 @@ __global__ void kb_fill_begin(const Slot* __restrict__ slots, int B) {
 }
 
 __global__ void kb_fill_border(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const Scalars* sc = S.sc;
   if (sc->fl_done) return;
@@ -215,6 +223,7 @@ __global__ void kb_fill_border(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_fill_phase(const Slot* __restrict__ slots, int ph) {
+  pdl_enter();
   SLOT_Y;
   const Scalars* sc = S.sc;
   if (sc->fl_done) return;
@@ -253,6 +262,7 @@ __global__ void kb_fill_phase(const Slot* __restrict__ slots, int ph) {
 // Holes still unfilled go to the other list buffer (warp-aggregated append; the
 // order does not matter, see append_hole).
 __global__ void kb_fill_compact(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   Scalars* sc = S.sc;
   if (sc->fl_done) return;
@@ -280,6 +290,7 @@ __global__ void kb_fill_compact(const Slot* __restrict__ slots) {
 // (any slot still filling).  *body_iters counts the iterations run.
 __global__ void kb_fill_step(const Slot* __restrict__ slots, int B,
                              cudaGraphConditionalHandle cond, int break_iter, int* body_iters) {
+  pdl_enter();
   int active = 0;
   for (int i = threadIdx.x; i < B; i += blockDim.x) {
     Scalars* sc = slots[i].sc;
@@ -310,6 +321,7 @@ __global__ void kb_fill_step(const Slot* __restrict__ slots, int B,
 // Disconnected regions (split_disconnected.cu:33-96): component roots by
 // union-find, sizes, largest region per label (R6), invalidate the rest.
 __global__ void kb_cc_init(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
@@ -351,6 +363,7 @@ __device__ __forceinline__ bool uf_unite(int* parent, int a, int b) {
 // Unions with the earlier 8-neighbours; a diagonal one is skipped when a 4-path
 // through W or N already joins it (W-NW and N-NW, N-NE are united at those pixels).
 __global__ void kb_cc_hook(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
@@ -374,6 +387,7 @@ __global__ void kb_cc_hook(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_cc_compress(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
@@ -381,6 +395,7 @@ __global__ void kb_cc_compress(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_cc_size(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
@@ -389,6 +404,7 @@ __global__ void kb_cc_size(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_cc_best(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const int* __restrict__ seg = S.seg;
   const int* __restrict__ root = S.d1;
@@ -405,6 +421,7 @@ __global__ void kb_cc_best(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_cc_invalidate(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int* __restrict__ seg = S.seg;
   const int* __restrict__ root = S.d1;
@@ -420,6 +437,7 @@ __global__ void kb_cc_invalidate(const Slot* __restrict__ slots) {
 
 // Hole list of the second fill: every -1 pixel after the invalidation.
 __global__ void kb_list_holes(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
@@ -428,6 +446,7 @@ __global__ void kb_list_holes(const Slot* __restrict__ slots) {
 
 // invalid_counts / prior_counts update (shift_and_fill.cu:300-330).
 __global__ void kb_shift_params(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const int n = S.n_prev;
   const int* __restrict__ cnt_pool = S.cnt_pool;
@@ -446,6 +465,7 @@ __global__ void kb_shift_params(const Slot* __restrict__ slots) {
 // run_prop set-up: write_params (sparams_io.cu:353-501, prior_icov = invert_cov
 // :505-520) then mark_active (init_sparams.cu:195-286).
 __global__ void kb_write_params(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const stspix_params& pp = S.pprev;
@@ -493,6 +513,7 @@ __global__ void kb_write_params(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_mark_active(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -507,6 +528,7 @@ __global__ void kb_mark_active(const Slot* __restrict__ slots) {
 // Relabel (relabel.cu:126-409), R5.
 // Relabel runs on propagated slots only (mode 1); plain BASS slots return at once.
 __global__ void kb_relabel_init(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -519,6 +541,7 @@ __global__ void kb_relabel_init(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_living(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -529,6 +552,7 @@ __global__ void kb_living(const Slot* __restrict__ slots) {
 
 // find_most_similar_spix (relabel.cu:201-276): grid (s, candidate chunk).
 __global__ void kb_relabel_compare(const Slot* __restrict__ slots, int chunk) {
+  pdl_enter();
   SLOT_Z;
   if (!S.mode) return;
   const SpDev& sp = S.sp;
@@ -564,6 +588,7 @@ __global__ void kb_relabel_compare(const Slot* __restrict__ slots, int chunk) {
 // mark_for_relabel (relabel.cu:126-192): revive flags and mint flags.
 __global__ void kb_relabel_mark(const Slot* __restrict__ slots, float thresh_replace,
                                 float thresh_new) {
+  pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
   const int cap = S.cap;
@@ -588,6 +613,7 @@ __global__ void kb_relabel_mark(const Slot* __restrict__ slots, float thresh_rep
 }
 
 __global__ void kb_relabel_ids(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
   const int cap = S.cap;
@@ -607,6 +633,7 @@ __global__ void kb_relabel_ids(const Slot* __restrict__ slots) {
 // relabel_spix_kernel parameter copies (relabel.cu:86-120), from the largest
 // reviving superpixel.
 __global__ void kb_relabel_params(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
   const SpDev& sp = S.sp;
@@ -635,6 +662,7 @@ __global__ void kb_relabel_params(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_relabel_apply(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
   int* __restrict__ seg = S.seg;
@@ -649,6 +677,7 @@ __global__ void kb_relabel_apply(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_relabel_end(const Slot* __restrict__ slots, int B) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B || !slots[i].mode) return;
   Scalars* sc = slots[i].sc;
@@ -659,6 +688,7 @@ __global__ void kb_relabel_end(const Slot* __restrict__ slots, int B) {
 }
 
 __global__ void kb_count_revived(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;

@@ -25,11 +25,13 @@
 namespace stspix {
 
 __global__ void k_q_range_init(int* mm) {
+  pdl_enter();
   if (threadIdx.x == 0) { mm[0] = INT_MAX; mm[1] = INT_MIN; }
 }
 
 // min / max of n labels into mm[0], mm[1] (grid-stride, block reduction).
 __global__ void k_q_range(const int32_t* __restrict__ a, long long n, int* mm) {
+  pdl_enter();
   int lo = INT_MAX, hi = INT_MIN;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -73,6 +75,7 @@ __global__ void __launch_bounds__(256) k_q_accum(
     const int32_t* __restrict__ gt, int T, int H, int W, int off, int S, int G1,
     int* __restrict__ cnt, double* __restrict__ fsum, double* __restrict__ vsum,
     double* __restrict__ msum, int* __restrict__ J) {
+  pdl_enter();
   const int lane = threadIdx.x & 31;
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -152,6 +155,7 @@ __global__ void __launch_bounds__(256) k_q_resid(
     const float* __restrict__ vid, const int32_t* __restrict__ spix, int npix, int off, int S,
     const int* __restrict__ cnt, const double* __restrict__ fsum,
     const double* __restrict__ msum, double* pix2, double* pix2s, double* sse) {
+  pdl_enter();
   __shared__ double sh[32];
   const int t = blockIdx.y;
   const double m0 = msum[3 * t] / npix, m1 = msum[3 * t + 1] / npix, m2 = msum[3 * t + 2] / npix;
@@ -181,6 +185,7 @@ __global__ void __launch_bounds__(256) k_q_resid(
 // of its size over the frames it is alive in (-1 if alive in fewer than two).
 __global__ void k_q_id_time(const int* __restrict__ cnt, int T, int S, long long* ntot,
                             double* std_out) {
+  pdl_enter();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S) return;
   long long n = 0, s1 = 0;
@@ -206,6 +211,7 @@ __global__ void __launch_bounds__(256) k_q_frame_ids(
     const double* __restrict__ vsum, const long long* __restrict__ ntot,
     const double* __restrict__ msum, int S, int npix, unsigned long long* live, double* pool2,
     double* pool3) {
+  pdl_enter();
   __shared__ double sh[32];
   const int t = blockIdx.y;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -247,6 +253,7 @@ __global__ void __launch_bounds__(256) k_q_frame_ids(
 __global__ void __launch_bounds__(256) k_q_uesa_frame(
     const int* __restrict__ cnt, const int* __restrict__ J, int S, int G1,
     unsigned long long* ue, unsigned long long* sa, unsigned long long* size) {
+  pdl_enter();
   __shared__ unsigned long long sue[kQGtShared], ssa[kQGtShared], ssz[kQGtShared];
   const bool shared = G1 <= kQGtShared;
   if (shared)
@@ -292,6 +299,7 @@ __global__ void __launch_bounds__(256) k_q_uesa_frame(
 __global__ void __launch_bounds__(256) k_q_uesa_id(
     const int* __restrict__ cnt, const int* __restrict__ J, const long long* __restrict__ ntot,
     int T, int S, int G1, unsigned long long* ue3, unsigned long long* sa3) {
+  pdl_enter();
   __shared__ unsigned long long sue[kQGtShared], ssa[kQGtShared];
   const bool shared = G1 <= kQGtShared;
   if (shared)
@@ -330,6 +338,7 @@ __global__ void __launch_bounds__(256) k_q_uesa_id(
 // + 1e-8) for every id 0..S-1 of every frame, pooled[p] = down of the pixel's id.
 __global__ void k_q_down(const int* __restrict__ cnt, const double* __restrict__ fsum,
                          long long TS, float* __restrict__ down) {
+  pdl_enter();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= TS) return;
   const double n = (double)cnt[i] + 1e-8;
@@ -339,6 +348,7 @@ __global__ void k_q_down(const int* __restrict__ cnt, const double* __restrict__
 __global__ void k_q_pool_write(const int32_t* __restrict__ spix, int npix, int off, int S,
                                long long n, const float* __restrict__ down,
                                float* __restrict__ pooled) {
+  pdl_enter();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const long long t = i / npix;

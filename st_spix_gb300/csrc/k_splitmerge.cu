@@ -14,6 +14,7 @@ namespace stspix {
 // ---------------------------------------------------------------------------
 // Split seeds (init_split, split_merge.cu:803-844) for both directions.
 __global__ void kb_split_seed(const Slot* __restrict__ slots, int dir_bass, int dir_prop) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const int* __restrict__ seg = S.seg;
@@ -45,6 +46,7 @@ __global__ void kb_split_seed(const Slot* __restrict__ slots, int dir_bass, int 
 
 // d1 = d2 = -1 (unreached) before the split seeds.
 __global__ void kb_split_clear(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
@@ -53,6 +55,7 @@ __global__ void kb_split_clear(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_split_begin(const Slot* __restrict__ slots, int B) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B) return;
   Scalars* sc = slots[i].sc;
@@ -66,6 +69,7 @@ __global__ void kb_split_begin(const Slot* __restrict__ slots, int B) {
 // Bounding box of every superpixel (for the split BFS), one 16-pixel row run per
 // thread.
 __global__ void kb_bbox(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.sc->tmp0) return;
   constexpr int R = 16;
@@ -213,6 +217,7 @@ struct BfsWarpSmem {
 };
 
 __global__ void __launch_bounds__(128) kb_split_bfs(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.sc->tmp0) return;
   __shared__ BfsWarpSmem sm_all[4];
@@ -237,6 +242,7 @@ __global__ void __launch_bounds__(128) kb_split_bfs(const Slot* __restrict__ slo
 
 // Block per large box; dynamic shared memory of 5 * kBigRows * kBigWpr words.
 __global__ void __launch_bounds__(256) kb_split_bfs_big(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   if (!S.sc->tmp0) return;
   extern __shared__ unsigned long long big[];
@@ -285,6 +291,7 @@ __global__ void __launch_bounds__(256) kb_split_bfs_big(const Slot* __restrict__
 
 // calc_seg_split (split_merge.cu:847-859): second half when d1 > d2.
 __global__ void kb_split_partition(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
@@ -295,6 +302,7 @@ __global__ void kb_split_partition(const Slot* __restrict__ slots) {
 
 // Clear the split/merge sums (cap + 2 entries).
 __global__ void kb_sm_clear(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SmDev& sm = S.sm;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -310,6 +318,7 @@ __global__ void kb_sm_clear(const Slot* __restrict__ slots) {
 // split: labels = split labels, invalid counts against the shifted labels (prop
 // slots); merge: labels = current labels, ids < cap.
 __global__ void kb_sm_accumulate(const Slot* __restrict__ slots, int split) {
+  pdl_enter();
   SLOT_Y;
   const float* __restrict__ img = S.img;
   const int* __restrict__ lab = split ? S.smseg : S.seg;
@@ -413,12 +422,14 @@ __device__ __forceinline__ void split_decide_one(const SpDev& sp, const SmDev& s
 }
 
 __global__ void kb_split_decide(const Slot* __restrict__ slots, SmConsts K, float split_alpha) {
+  pdl_enter();
   SLOT_Y;
   FOR_SP(k, S.sp.cap) split_decide_one(S.sp, S.sm, S.sc, K, split_alpha, S.mode, S.accept, k);
 }
 
 // Split commit: new id = max_spix + 1 + rank (R2), prior counts.
 __global__ void kb_split_commit(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const SmDev& sm = S.sm;
@@ -459,6 +470,7 @@ __global__ void kb_split_commit(const Slot* __restrict__ slots) {
 
 // split_sp (split_merge.cu:1002-1031) / split_sp_p (split_merge_prop.cu:2317-2350).
 __global__ void kb_split_apply(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int* __restrict__ seg = S.seg;
   const int* __restrict__ smseg = S.smseg;
@@ -484,6 +496,7 @@ __global__ void kb_split_apply(const Slot* __restrict__ slots) {
 }
 
 __global__ void kb_split_end(const Slot* __restrict__ slots, int B) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B) return;
   Scalars* sc = slots[i].sc;
@@ -496,6 +509,7 @@ __global__ void kb_split_end(const Slot* __restrict__ slots, int B) {
 // Merge candidates (calc_merge_candidate, split_merge.cu:719-755;
 // calc_merge_candidate_p, split_merge_prop.cu:1808-1845).
 __global__ void kb_merge_candidates(const Slot* __restrict__ slots, int dir_bass, int dir_prop) {
+  pdl_enter();
   SLOT_Y;
   const int* __restrict__ seg = S.seg;
   const uint8_t* __restrict__ border = S.border;
@@ -529,6 +543,7 @@ __global__ void kb_merge_candidates(const Slot* __restrict__ slots, int dir_bass
 // Single-superpixel marginal, present only when k has its own candidate
 // (calc_merge_stats_step0 computes b_n only then; split_merge_orig.cu:456-520).
 __global__ void kb_merge_single(const Slot* __restrict__ slots, SmConsts K) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const SmDev& sm = S.sm;
@@ -570,12 +585,14 @@ __device__ __forceinline__ void merge_decide_one(const SpDev& sp, const SmDev& s
 }
 
 __global__ void kb_merge_decide(const Slot* __restrict__ slots, SmConsts K, float merge_alpha) {
+  pdl_enter();
   SLOT_Y;
   FOR_SP(k, S.sp.cap) merge_decide_one(S.sp, S.sm, S.sc, K, merge_alpha, k);
 }
 
 // Merge set-up: candidate pairs unset, claims at +inf (cap + 2 entries).
 __global__ void kb_merge_clear(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= S.cap + 2) return;
@@ -585,6 +602,7 @@ __global__ void kb_merge_clear(const Slot* __restrict__ slots) {
 
 // merge flag := accepted and claimant of its target; snapshot valid; target := pair.
 __global__ void kb_merge_flag(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const SmDev& sm = S.sm;
@@ -601,6 +619,7 @@ __global__ void kb_merge_flag(const Slot* __restrict__ slots) {
 
 // remove_sp (split_merge.cu:1035-1080) / remove_sp_p (split_merge_prop.cu:2353-2449).
 __global__ void kb_merge_remove(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const SmDev& sm = S.sm;
@@ -636,6 +655,7 @@ __global__ void kb_merge_remove(const Slot* __restrict__ slots) {
 
 // merge_sp (split_merge.cu:984-1000).
 __global__ void kb_merge_apply(const Slot* __restrict__ slots) {
+  pdl_enter();
   SLOT_Y;
   int* __restrict__ seg = S.seg;
   const int cap = S.cap;

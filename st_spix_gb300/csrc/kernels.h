@@ -39,11 +39,13 @@ __global__ void k_label_stats_out(int n, int mode, const long long* iacc, const 
                                   const double* dacc, double* out);
 __global__ void kb_store_sample(const Slot* slots);
 __global__ void kb_find_border(const Slot* slots);
-// boundary sweep, one block per 32x32 / 64x32 tile of the batch
+// boundary sweep, one block per 32x32 / 64x32 / 16x32 tile of the batch
 __global__ void kb_sweep_t32(const Slot* slots, int B, int parity, float s2, float potts,
-                             int mode);
+                             int mode, int stats);
 __global__ void kb_sweep_t64(const Slot* slots, int B, int parity, float s2, float potts,
-                             int mode);
+                             int mode, int stats);
+__global__ void kb_sweep_t16(const Slot* slots, int B, int parity, float s2, float potts,
+                             int mode, int stats);
 __global__ void kb_copy_labels(const Slot* slots);
 __global__ void kb_read_params(const Slot* slots);
 __global__ void kb_save_prev(const Slot* slots);
