@@ -24,6 +24,11 @@
  *   stspix_count_spix          st_spix/spix_utils/evaluate.py:71 count_spix
  *   stspix_size_variation      st_spix/spix_utils/evaluate.py:284 scoreMeanDurationAndSizeVariation
  *   stspix_sp_pooling          st_spix/sp_pooling.py:10 pooling
+ *   stspix_legacy_shift_labels st_spix/csrc/prop/shift_labels.cu:82 run_shift_labels
+ *   stspix_legacy_fill_missing st_spix/csrc/prop/fill_missing.cu:317 run_fill_missing
+ *   stspix_legacy_rgb_to_lab   st_spix/csrc/prop/rgb2lab.cu:167 run_rgb_to_lab
+ *   stspix_sp_video_pooling    st_spix/csrc/prop/sp_video_pooling.cu:62 sp_video_pooling
+ *   stspix_downsampled_video_to_pooled  st_spix/csrc/prop/sp_video_pooling.cu:211
  */
 #ifndef ST_SPIX_GB300_H
 #define ST_SPIX_GB300_H
@@ -300,6 +305,47 @@ int stspix_size_variation(stspix_ctx* ctx, void* stream, const int32_t* counts, 
  * is not NULL, pooled f32 [T,H,W,3] = the mean colour of each pixel's id.            */
 int stspix_sp_pooling(stspix_ctx* ctx, void* stream, const float* vid, const int32_t* spix,
                       int T, int H, int W, int nids, float* pooled, float* down);
+
+/* ---- legacy prop_cuda surface ------------------------------------------------------
+ * The ops of the older extension st_spix/csrc/prop (bound by pybind_prop.cpp, called by
+ * st_spix/prop and st_spix/models/bass.py) whose arithmetic is self-contained; its
+ * BASS drivers (bass, prop_bass, refine_missing) map onto stspix_run_bass /
+ * stspix_run_prop in the Python layer (st_spix_gb300.prop_cuda).
+ *
+ * shift_labels (prop/shift_labels.cu:82): every pixel of superpixel s moves by
+ * flow[2s], flow[2s+1] (integer dx, dy; nspix rows); shifted = the largest label
+ * arriving at a pixel (-1 if none), counts = arrivals.  Ids outside [0, nspix) stay. */
+int stspix_legacy_shift_labels(stspix_ctx* ctx, void* stream, const int32_t* spix,
+                               const int32_t* flow, int nspix, int H, int W, int32_t* shifted,
+                               int32_t* counts);
+
+/* fill_missing (prop/fill_missing.cu:317): fills the listed missing pixels (indices
+ * into the frame) in place by the nearest FP32 centre (centers [ncenters, 2] = x, y)
+ * among labelled 4-neighbours, parity phase by phase, until none is left, the count
+ * repeats or break_iter iterations (0: no cap) ran.  *iters and *remaining (host,
+ * may be NULL): iterations run and pixels still missing.  Synchronises per iteration.
+ * Labels >= ncenters are not candidates.                                               */
+int stspix_legacy_fill_missing(stspix_ctx* ctx, void* stream, int32_t* spix, const float* centers,
+                               int ncenters, const int32_t* missing, int nmissing, int H, int W,
+                               int break_iter, int* iters, int* remaining);
+
+/* rgb_to_lab (prop/rgb2lab.cu:167): as stspix_rgb2lab but the first channel is red.   */
+int stspix_legacy_rgb_to_lab(stspix_ctx* ctx, void* stream, const float* rgb, float* lab,
+                             long long npix);
+
+/* sp_video_pooling (prop/sp_video_pooling.cu:62): img f32 [B,T,H,W,F], seg i32
+ * [B,T,H,W] with ids < nspix -> down f32 [B,nspix,F] = per batch item mean feature of
+ * each id over all frames (sum / (count + 1e-10)), counts f32 [B,nspix] (may be NULL),
+ * pooled f32 [B,T,H,W,F] (may be NULL; 0 where the id is negative).                  */
+int stspix_sp_video_pooling(stspix_ctx* ctx, void* stream, const float* img, const int32_t* seg,
+                            int B, int T, int H, int W, int F, int nspix, float* pooled,
+                            float* down, float* counts);
+
+/* downsampled_video_to_pooled (prop/sp_video_pooling.cu:211): pooled[b,t,p] =
+ * down[b, seg[b,t,p]] (0 where the id is negative).                                  */
+int stspix_downsampled_video_to_pooled(stspix_ctx* ctx, void* stream, const float* down,
+                                       const int32_t* seg, int B, int T, int H, int W, int F,
+                                       int nspix, float* pooled);
 
 /* ---- batched and serving forms -----------------------------------------------
  * No single reference counterpart: the reference processes one frame per call

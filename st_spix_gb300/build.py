@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libstspix_gb300.so")
-SOURCES = ["k_bass.cu", "k_splitmerge.cu", "k_prop.cu", "k_color.cu", "k_quality.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["k_bass.cu", "k_splitmerge.cu", "k_prop.cu", "k_color.cu", "k_quality.cu", "k_legacy.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]

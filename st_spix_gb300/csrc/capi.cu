@@ -1636,7 +1636,7 @@ int stspix_rgb2lab(stspix_ctx* ctx, void* stream, const float* rgb, float* lab,
   if (!ctx || !rgb || !lab || npix < 0) return fail(ctx, STSPIX_ERR_ARG, "bad argument");
   cudaSetDevice(ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
-  LAUNCH(k_rgb2lab, npix, rgb, lab, npix);
+  LAUNCH(k_rgb2lab, npix, rgb, lab, npix, 1);
   CK(cudaGetLastError());
   return STSPIX_OK;
 }
@@ -1874,6 +1874,126 @@ int stspix_sp_pooling(stspix_ctx* ctx, void* stream, const float* vid, const int
   if (pooled)
     LAUNCHG(k_q_pool_write, q_blocks(n), kThreads, spix, (int)npix, 0, nids, n, down, pooled);
   CK(cudaFreeAsync(base, st));
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+// ---- legacy prop_cuda surface (st_spix/csrc/prop) -----------------------------------
+int stspix_legacy_shift_labels(stspix_ctx* ctx, void* stream, const int32_t* spix,
+                               const int32_t* flow, int nspix, int H, int W, int32_t* shifted,
+                               int32_t* counts) {
+  if (!ctx || !spix || !flow || !shifted || !counts || nspix < 0 || H < 1 || W < 1 ||
+      (long long)H * W > INT_MAX)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long n = (long long)H * W;
+  LAUNCH(k_fill_i32, n, shifted, n, -1);
+  CK(cudaMemsetAsync(counts, 0, sizeof(int32_t) * (size_t)n, st));
+  LAUNCH(k_lshift, n, spix, flow, nspix, H, W, shifted, counts);
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_legacy_fill_missing(stspix_ctx* ctx, void* stream, int32_t* spix, const float* centers,
+                               int ncenters, const int32_t* missing, int nmissing, int H, int W,
+                               int break_iter, int* iters, int* remaining) {
+  if (!ctx || !spix || (nmissing > 0 && (!missing || !centers)) || nmissing < 0 || ncenters < 0 ||
+      H < 1 || W < 1 || (long long)H * W > INT_MAX)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  if (iters) *iters = 0;
+  if (remaining) *remaining = 0;
+  if (nmissing == 0) return STSPIX_OK;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* border = nullptr;
+  int* num_neg = nullptr;
+  CK(cudaMallocAsync((void**)&border, (size_t)nmissing, st));
+  CK(cudaMallocAsync((void**)&num_neg, sizeof(int), st));
+  // fill_missing (prop/fill_missing.cu:26-90): count the listed pixels still missing
+  // (and mark the border), four parity phases; stop when a count is 0, repeats the
+  // previous one (starting from 1), or break_iter iterations ran.
+  int neg = 1, prev = 1, it = 0;
+  auto count_border = [&]() -> int {
+    CK(cudaMemsetAsync(num_neg, 0, sizeof(int), st));
+    LAUNCH(k_lfill_border, nmissing, spix, missing, nmissing, H, W, border, num_neg);
+    CK(cudaMemcpyAsync(&neg, num_neg, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return STSPIX_OK;
+  };
+  int r;
+  while (neg > 0) {
+    if (break_iter > 0 && it >= break_iter) break;
+    if ((r = count_border())) return r;
+    for (int xm = 0; xm < 2; xm++)
+      for (int ym = 0; ym < 2; ym++)
+        LAUNCH(k_lfill_phase, nmissing, spix, centers, ncenters, missing, border, nmissing, H, W,
+               xm, ym);
+    it++;
+    if (neg == prev) break;   // the legacy loop reports that the border won't shrink
+    prev = neg;
+  }
+  if ((r = count_border())) return r;
+  CK(cudaFreeAsync(border, st));
+  CK(cudaFreeAsync(num_neg, st));
+  CK(cudaGetLastError());
+  if (iters) *iters = it;
+  if (remaining) *remaining = neg;
+  return STSPIX_OK;
+}
+
+int stspix_legacy_rgb_to_lab(stspix_ctx* ctx, void* stream, const float* rgb, float* lab,
+                             long long npix) {
+  if (!ctx || !rgb || !lab || npix < 0) return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  LAUNCH(k_rgb2lab, npix, rgb, lab, npix, 0);
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_sp_video_pooling(stspix_ctx* ctx, void* stream, const float* img, const int32_t* seg,
+                            int B, int T, int H, int W, int F, int nspix, float* pooled,
+                            float* down, float* counts) {
+  if (!ctx || !img || !seg || !down || B < 1 || T < 1 || H < 1 || W < 1 || F < 1 || nspix < 1 ||
+      B > 65535 || T > 65535)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long npix = (long long)H * W, nbs = (long long)B * nspix;
+  double* sum = nullptr;
+  unsigned long long* cnt = nullptr;
+  CK(cudaMallocAsync((void**)&sum, sizeof(double) * (size_t)(nbs * F), st));
+  CK(cudaMallocAsync((void**)&cnt, sizeof(unsigned long long) * (size_t)nbs, st));
+  CK(cudaMemsetAsync(sum, 0, sizeof(double) * (size_t)(nbs * F), st));
+  CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (size_t)nbs, st));
+  const dim3 grid((unsigned)std::max(1LL, (npix + kThreads - 1) / kThreads), (unsigned)B,
+                  (unsigned)T);
+  LAUNCHG(k_vpool_accum, grid, kThreads, img, seg, T, npix, F, nspix, sum, cnt);
+  LAUNCH(k_vpool_mean, nbs, sum, cnt, nbs, F, down, counts);
+  if (pooled) {
+    CK(cudaMemsetAsync(pooled, 0, sizeof(float) * (size_t)(B * T * npix * F), st));
+    LAUNCHG(k_vpool_write, grid, kThreads, down, seg, T, npix, F, nspix, pooled);
+  }
+  CK(cudaFreeAsync(sum, st));
+  CK(cudaFreeAsync(cnt, st));
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_downsampled_video_to_pooled(stspix_ctx* ctx, void* stream, const float* down,
+                                       const int32_t* seg, int B, int T, int H, int W, int F,
+                                       int nspix, float* pooled) {
+  if (!ctx || !down || !seg || !pooled || B < 1 || T < 1 || H < 1 || W < 1 || F < 1 ||
+      nspix < 1 || B > 65535 || T > 65535)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long npix = (long long)H * W;
+  CK(cudaMemsetAsync(pooled, 0, sizeof(float) * (size_t)(B * T * npix * F), st));
+  const dim3 grid((unsigned)std::max(1LL, (npix + kThreads - 1) / kThreads), (unsigned)B,
+                  (unsigned)T);
+  LAUNCHG(k_vpool_write, grid, kThreads, down, seg, T, npix, F, nspix, pooled);
   CK(cudaGetLastError());
   return STSPIX_OK;
 }

@@ -17,13 +17,18 @@
 
 namespace stspix {
 
-__global__ void k_rgb2lab(const float* __restrict__ rgb, float* __restrict__ lab, long long npix) {
+// first_blue: the first channel is blue (bist/rgb2lab.cu:64-66); 0: red (the legacy
+// prop/rgb2lab.cu:42-44 reads the channels in RGB order, otherwise identical).
+__global__ void k_rgb2lab(const float* __restrict__ rgb, float* __restrict__ lab, long long npix,
+                          int first_blue) {
   pdl_enter();
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= npix) return;
-  const double sB = (double)rgb[3 * t];
+  const double c0 = (double)rgb[3 * t];
   const double sG = (double)rgb[3 * t + 1];
-  const double sR = (double)rgb[3 * t + 2];
+  const double c2 = (double)rgb[3 * t + 2];
+  const double sB = first_blue ? c0 : c2;
+  const double sR = first_blue ? c2 : c0;
   if (sR != sR || sG != sG || sB != sB) return;
   auto lin = [](double c) {
     return c <= 0.04045 ? c / 12.92 : (double)powf((float)((c + 0.055) / 1.055), (float)2.4);

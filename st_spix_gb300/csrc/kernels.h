@@ -106,7 +106,7 @@ __global__ void kb_relabel_end(const Slot* slots, int B);
 __global__ void kb_count_revived(const Slot* slots);
 
 // k_color.cu
-__global__ void k_rgb2lab(const float* rgb, float* lab, long long npix);
+__global__ void k_rgb2lab(const float* rgb, float* lab, long long npix, int first_blue);
 __global__ void k_lab2rgb(const float* lab, float* rgb, long long npix);
 __global__ void k_rescale_u8(const uint8_t* in, float* out, long long nvals, float mval);
 
@@ -129,6 +129,22 @@ __global__ void k_q_uesa_frame(const int* cnt, const int* J, int S, int G1, unsi
 __global__ void k_q_uesa_id(const int* cnt, const int* J, const long long* ntot, int T, int S,
                             int G1, unsigned long long* ue3, unsigned long long* sa3);
 __global__ void k_q_down(const int* cnt, const double* fsum, long long TS, float* down);
+
+// k_legacy.cu
+__global__ void k_fill_i32(int32_t* p, long long n, int32_t v);
+__global__ void k_lshift(const int32_t* spix, const int32_t* flow, int nspix, int H, int W,
+                         int32_t* shifted, int32_t* counts);
+__global__ void k_lfill_border(const int32_t* seg, const int32_t* missing, int nmissing, int H,
+                               int W, uint8_t* border, int* num_neg);
+__global__ void k_lfill_phase(int32_t* seg, const float* centers, int ncenters,
+                              const int32_t* missing, const uint8_t* border, int nmissing, int H,
+                              int W, int xm, int ym);
+__global__ void k_vpool_accum(const float* img, const int32_t* seg, int T, long long npix, int F,
+                              int nspix, double* sum, unsigned long long* cnt);
+__global__ void k_vpool_mean(const double* sum, const unsigned long long* cnt, long long nbs,
+                             int F, float* down, float* counts);
+__global__ void k_vpool_write(const float* down, const int32_t* seg, int T, long long npix, int F,
+                              int nspix, float* pooled);
 __global__ void k_q_pool_write(const int32_t* spix, int npix, int off, int S, long long n,
                                const float* down, float* pooled);
 
