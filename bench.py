@@ -412,6 +412,66 @@ IMAGE = dict(name="bass_image_240x320", H=240, W=320, nseeds=200, sigma=0.05, sp
              sm_period=20)
 
 
+LATENCY = dict(name="latency_stream_480p_720p_1080p", sizes=((480, 854), (720, 1280), (1080, 1920)),
+               frames=10, batches=(1, 8))
+
+
+def run_latency(args, world, rank):
+    """--mode latency: per-frame latency of the streaming workload's propagated frames
+    (400 seeds, sp 20, 20 iterations, split/merge every 10) with one frame per batch, and
+    the per-frame cost at 8 frames per batch, at 480x854, 720p and 1080p; every stream
+    runs its frames 0..frames-1 once untimed first."""
+    import torch
+    from st_spix_gb300 import batch, synth
+    torch.cuda.set_device(args.local)
+    dev = torch.device("cuda", args.local)
+    w, lt = WORKLOAD, LATENCY
+    cfg = dict(niters=w["niters"], sp_size=w["sp_size"], potts=w["potts"],
+               sigma2_app=w["sigma2_app"], alpha=w["alpha"], split_alpha=w["split_alpha"],
+               sm_period=w["sm_period"], prop_niters=w["prop_niters"])
+    T = lt["frames"]
+    res = {}
+    for H, W in lt["sizes"]:
+        for B in lt["batches"]:
+            vids = [synth.voronoi_video_device(H, W, T, w["nseeds"], w["sigma"], seed=i,
+                                               device=dev) for i in range(B)]
+            videos = [batch.Video(H, W, dev) for _ in range(B)]
+
+            def run(times):
+                for v in videos:
+                    v.reset()
+                for t in range(T):
+                    fr = [batch.Frame(img=vids[i][0][t], flow=vids[i][1][t - 1] if t else None,
+                                      video=videos[i]) for i in range(B)]
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    batch.process_batch(fr, **cfg)
+                    torch.cuda.synchronize()
+                    if t > 0:
+                        times.append(1000 * (time.perf_counter() - t0))
+            run([])
+            times = []
+            run(times)
+            for v in videos:
+                v.close()
+            times.sort()
+            res[f"{H}x{W}_batch{B}"] = {"batch_ms_p50": times[len(times) // 2],
+                                        "batch_ms_max": times[-1],
+                                        "ms_per_frame": sum(times) / len(times) / B}
+    if rank != 0:
+        return
+    line = {"metric": "per-frame latency (propagated frames)",
+            "value": res["720x1280_batch1"]["batch_ms_p50"], "unit": "ms",
+            "n_gpus": world, "steps": T - 1, "warmup": 1, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64+int64",
+            "data": "synthetic",
+            "config": {"workload": lt["name"], "frames": T, "sp_size": w["sp_size"],
+                       "niters": w["niters"], "sm_period": w["sm_period"],
+                       "value": "720p, one frame per batch, median wall ms"},
+            "by_size": res}
+    print(json.dumps(line), flush=True)
+
+
 def run_image(args, world, rank):
     """--mode image: plain BASS on one 240x320 Voronoi frame (200 seeds, noise 0.05,
     superpixel size 15, 100 iterations, split/merge every 20), one frame per call
@@ -618,12 +678,12 @@ def main():
                          "context and share of the streams")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="stream",
-                    choices=["stream", "serve", "batch", "precision", "image"],
+                    choices=["stream", "serve", "batch", "precision", "image", "latency"],
                     help="stream: the 480x854 streaming workload (default); serve: the "
                          "serving form on mixed-resolution Poisson streams; batch: 64 "
                          "independent frames of uneven size as one batch; precision: the "
                          "accumulator precision study at 4K; image: plain BASS on one "
-                         "240x320 frame")
+                         "240x320 frame; latency: per-frame latency at 480p/720p/1080p")
     ap.add_argument("--max-batch", type=int, default=8, help="serve: frames per batch")
     ap.add_argument("--max-pixels", type=int, default=0,
                     help="serve: pixels per batch (0: no cap); bounds a batch's GPU time")
@@ -645,6 +705,8 @@ def main():
         return run_precision(args, world, rank)
     if args.mode == "image":
         return run_image(args, world, rank)
+    if args.mode == "latency":
+        return run_latency(args, world, rank)
     args.warmup = max(args.warmup, 3)
 
     import numpy as np

@@ -599,7 +599,7 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   }
   if (ctx->accumulator) accumulate_fp(ctx, st, L, nb, ctx->accumulator);
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
-  LAUNCHB(kb_posterior, L.max_cap, L, nb);
+  LAUNCHG(kb_posterior, dim3((unsigned)((L.max_cap + 31) / 32), (unsigned)nb), 128, L.d);
   return STSPIX_OK;
 }
 

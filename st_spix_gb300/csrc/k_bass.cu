@@ -421,80 +421,102 @@ __device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in
   *oz = (pc * sp_size + count * in_z) / (total_count + 3.0);
 }
 
-__device__ __forceinline__ void posterior_one(const SpDev& sp, int sp_size, Scalars* sc, int k) {
-  // loads in two round trips: the id's status, then (live ids only) every other
-  // input at once, both prior covariances included, instead of a chain of dependent
-  // loads behind each branch
-  const int count_int = sp.count[k];
-  const uint8_t valid = sp.valid[k];
-  const uint8_t prop = sp.prop[k];
-  const float pc = sp.prior_count[k];
-  bool live = valid && count_int > 0;
-  if (valid && count_int <= 0) sp.valid[k] = 0;
-  if (!live) {
-    for (int c = 0; c < 3; c++) { sp.mu_app[3 * k + c] = 0.f; sp.sigma_shape[3 * k + c] = 0.0; }
-    sp.mu_shape[2 * k] = 0.0; sp.mu_shape[2 * k + 1] = 0.0;
-    return;
-  }
-  const long long* ap = sp.acc + 8 * (size_t)k;
-  long long a[8];
-#pragma unroll
-  for (int c = 0; c < 8; c++) a[c] = ap[c];
-  double q[3], icv[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    q[c] = sp.sample_sigma_shape[3 * k + c];
-    icv[c] = sp.prior_icov[3 * k + c];
-  }
-  double count = count_int * 1.0;
-  double total_count = (double)count_int + pc * 50;
-  double px, py, pz;
-  if (prop) {
-    smooth_prior(q[0], q[1], q[2], (int)pc, pc, sp_size, &px, &py, &pz);
-  } else {
-    px = icv[0]; py = icv[1]; pz = icv[2];
-  }
-  double pr_det = px * pz - py * py;
-  if (!(pr_det > 0)) atomicExch(&sc->status, STSPIX_ERR_DEGENERATE);
-  pr_det = sqrt(pr_det);
-  double psx = pc / pr_det * px, psy = pc / pr_det * py, psz = pc / pr_det * pz;
-  float mr = (float)(fx_unq(a[0], kFxAppShift) / count);
-  float mg = (float)(fx_unq(a[1], kFxAppShift) / count);
-  float mb = (float)(fx_unq(a[2], kFxAppShift) / count);
-  sp.mu_app[3 * k] = mr; sp.mu_app[3 * k + 1] = mg; sp.mu_app[3 * k + 2] = mb;
-  double mx = a[3] / count, my = a[4] / count;
-  sp.mu_shape[2 * k] = mx; sp.mu_shape[2 * k + 1] = my;
-  double sx = a[5] - count * mx * mx;
-  double sy = a[6] - count * mx * my;
-  double sz = a[7] - count * my * my;
-  sx = (pc * psx + sx) / (total_count + 3.0);
-  sy = (pc * psy + sy) / (total_count + 3.0);
-  sz = (pc * psz + sz) / (total_count + 3.0);
-  double det = sx * sz - sy * sy;
-  if (det <= 0) {
-    sx = sx + 0.00001;
-    sz = sz + 0.00001;
-    det = sx * sz - sy * sy;
-    if (det <= 0) det = 0.00001;
-  }
-  double ix = sz / det, iy = -sy / det, iz = sx / det;
-  double ld = log(det);
-  sp.sigma_shape[3 * k] = ix; sp.sigma_shape[3 * k + 1] = iy; sp.sigma_shape[3 * k + 2] = iz;
-  sp.logdet[k] = ld;
-  SweepRec r;
-  r.mu_r = mr; r.mu_g = mg; r.mu_b = mb; r.logdet = (float)ld;
-  double fx = floor(mx), fy = floor(my);
-  r.mxi = (int)fx; r.myi = (int)fy;
-  r.frac = (mx != fx ? 1 : 0) | (my != fy ? 2 : 0);
-  r.isx = (float)ix; r.isy = (float)iy; r.isz = (float)iz; r.pad = 0.f;
-  r.count = count_int;
-  sp.rec[k] = r;
-}
-
-__global__ void kb_posterior(const Slot* __restrict__ slots) {
+// One block = 32 consecutive ids, four warps splitting each id's FP64 chain (this part
+// issues FP64 slowly, so one warp per id set would serialise the whole chain on one
+// scheduler): warp 0 the colour means, warp 1 the prior shape term, warp 2 the shape
+// mean and scatter; then warps 0-2 one smoothed covariance entry each, then warps 0-2
+// one inverse entry each and warp 3 the log determinant.  Every value is the same
+// expression as a single-thread evaluation, exchanged through shared memory.
+__global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  FOR_SP(k, S.sp.cap) posterior_one(S.sp, S.sp_size, S.sc, k);
+  __shared__ double v_ps[3][32], v_raw[3][32], v_m[2][32], v_s[3][32], v_i[4][32];
+  __shared__ float v_app[3][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const SpDev& sp = S.sp;
+  const int k = blockIdx.x * 32 + lane;
+  const bool inr = k < sp.cap;
+  const int count_int = inr ? sp.count[k] : 0;
+  const uint8_t valid = inr ? sp.valid[k] : 0;
+  const bool live = valid && count_int > 0;
+  if (w == 0 && inr) {
+    if (valid && count_int <= 0) sp.valid[k] = 0;
+    if (!live) {
+      for (int c = 0; c < 3; c++) { sp.mu_app[3 * k + c] = 0.f; sp.sigma_shape[3 * k + c] = 0.0; }
+      sp.mu_shape[2 * k] = 0.0; sp.mu_shape[2 * k + 1] = 0.0;
+    }
+  }
+  if (!__syncthreads_or(live)) return;
+  const float pc = live ? sp.prior_count[k] : 0.f;
+  const double count = count_int * 1.0;
+  const double total_count = (double)count_int + pc * 50;
+  const long long* a = sp.acc + 8 * (size_t)k;
+  if (live) {
+    if (w == 0) {
+      // colour means (fixed-point sums, R1)
+      for (int c = 0; c < 3; c++) {
+        const float m = (float)(fx_unq(a[c], kFxAppShift) / count);
+        sp.mu_app[3 * k + c] = m;
+        v_app[c][lane] = m;
+      }
+    } else if (w == 1) {
+      // prior shape term (calc_simple_update with _add_sigma_smoothing)
+      double px, py, pz;
+      if (sp.prop[k]) {
+        smooth_prior(sp.sample_sigma_shape[3 * k], sp.sample_sigma_shape[3 * k + 1],
+                     sp.sample_sigma_shape[3 * k + 2], (int)pc, pc, S.sp_size, &px, &py, &pz);
+      } else {
+        px = sp.prior_icov[3 * k]; py = sp.prior_icov[3 * k + 1]; pz = sp.prior_icov[3 * k + 2];
+      }
+      double pr_det = px * pz - py * py;
+      if (!(pr_det > 0)) atomicExch(&S.sc->status, STSPIX_ERR_DEGENERATE);
+      pr_det = sqrt(pr_det);
+      v_ps[0][lane] = pc / pr_det * px;
+      v_ps[1][lane] = pc / pr_det * py;
+      v_ps[2][lane] = pc / pr_det * pz;
+    } else if (w == 2) {
+      // shape mean and scatter
+      const double mx = a[3] / count, my = a[4] / count;
+      sp.mu_shape[2 * k] = mx; sp.mu_shape[2 * k + 1] = my;
+      v_m[0][lane] = mx; v_m[1][lane] = my;
+      v_raw[0][lane] = a[5] - count * mx * mx;
+      v_raw[1][lane] = a[6] - count * mx * my;
+      v_raw[2][lane] = a[7] - count * my * my;
+    }
+  }
+  __syncthreads();
+  if (live && w < 3) v_s[w][lane] = (pc * v_ps[w][lane] + v_raw[w][lane]) / (total_count + 3.0);
+  __syncthreads();
+  if (live) {
+    double sx = v_s[0][lane], sy = v_s[1][lane], sz = v_s[2][lane];
+    double det = sx * sz - sy * sy;
+    if (det <= 0) {
+      sx = sx + 0.00001;
+      sz = sz + 0.00001;
+      det = sx * sz - sy * sy;
+      if (det <= 0) det = 0.00001;
+    }
+    if (w == 0) v_i[0][lane] = sz / det;
+    else if (w == 1) v_i[1][lane] = -sy / det;
+    else if (w == 2) v_i[2][lane] = sx / det;
+    else v_i[3][lane] = log(det);
+  }
+  __syncthreads();
+  if (live && w == 0) {
+    const double ix = v_i[0][lane], iy = v_i[1][lane], iz = v_i[2][lane], ld = v_i[3][lane];
+    const double mx = v_m[0][lane], my = v_m[1][lane];
+    sp.sigma_shape[3 * k] = ix; sp.sigma_shape[3 * k + 1] = iy; sp.sigma_shape[3 * k + 2] = iz;
+    sp.logdet[k] = ld;
+    SweepRec r;
+    r.mu_r = v_app[0][lane]; r.mu_g = v_app[1][lane]; r.mu_b = v_app[2][lane];
+    r.logdet = (float)ld;
+    const double fx = floor(mx), fy = floor(my);
+    r.mxi = (int)fx; r.myi = (int)fy;
+    r.frac = (mx != fx ? 1 : 0) | (my != fy ? 2 : 0);
+    r.isx = (float)ix; r.isy = (float)iy; r.isz = (float)iz; r.pad = 0.f;
+    r.count = count_int;
+    sp.rec[k] = r;
+  }
 }
 
 // clear_fields + the helper memset (update_params.cu:54-88, :26): zero the counts
