@@ -77,6 +77,8 @@ typedef struct stspix_config {
                             (default, exact and order-independent), 1 FP32 atomics (as
                             the reference; order-dependent), 2 FP64 atomics -- 1 and 2
                             exist for the accumulator precision study               */
+  int   sweep_schedule;  /* boundary sweeps per launch: 0 autotuned (default), 1 one,
+                            2 two whenever two remain; the labels are the same       */
 } stspix_config;
 
 void stspix_default_config(stspix_config* cfg);

@@ -1221,6 +1221,7 @@ void oracle_default_config(stspix_config* c) {
   c->split_alpha = 0.f; c->merge_alpha = 0.f; c->sigma2_size = 0.f;
   c->thresh_relabel = 1e-5f; c->thresh_new = 1e-2f;
   c->accumulator = 0;
+  c->sweep_schedule = 0;   // a launch schedule of the engine; the oracle sweeps one by one
 }
 
 int oracle_hex_count(int H, int W, int sp_size) {

@@ -115,7 +115,8 @@ struct stspix_ctx {
   cudaEvent_t tune_ev[kSweepVariants + 1] = {};
   long long tunes = 0;
   int accumulator = 0;            // cfg.accumulator of the batch being run
-  int* body_iters = nullptr;       // device: fill-loop iterations run (launch count)
+  int* body_iters = nullptr;       // device: [0] fill-loop iterations run (launch count),
+                                   // [1] the fill compaction's block counter
   int* body_iters_host = nullptr;  // pinned
   long long body_iters_seen = 0;
   // bist_forward's stream state
@@ -390,6 +391,8 @@ void preload_kernels() {
       (const void*)kb_sweep_t32,
       (const void*)kb_sweep_t64,
       (const void*)kb_sweep_t16,
+      (const void*)kb_sweep2_t32,
+      (const void*)kb_sweep2_t16,
       (const void*)kb_copy_labels,
       (const void*)kb_read_params,
       (const void*)kb_save_prev,
@@ -423,7 +426,6 @@ void preload_kernels() {
       (const void*)kb_fill_border,
       (const void*)kb_fill_phase,
       (const void*)kb_fill_compact,
-      (const void*)kb_fill_step,
       (const void*)kb_cc_init,
       (const void*)kb_cc_hook,
       (const void*)kb_cc_compress,
@@ -606,15 +608,19 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
 // update_seg (update_seg.cu:281-311): niters_seg fused sweeps ping-ponging between
 // the labels and a scratch buffer; the border mask is only built when the next
 // iteration's merge reads it.
-// fuse_stats: the first sweep also clears the statistics and the last one adds those
-// of its final labels, so the next update_params skips its clear and accumulate
-// passes (needs two or more sweeps: no sweep reads the statistics in between).
+// fuse_stats: the first sweep launch also clears the statistics and the last one adds
+// those of its final labels, so the next update_params skips its clear and accumulate
+// passes (needs two or more launches: no sweep reads the statistics in between).
+// *fused tells whether that happened.
 int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
-               const stspix_config& cfg, bool need_border, bool fuse_stats) {
+               const stspix_config& cfg, bool need_border, bool fuse_stats, bool* fused) {
   ctx->cur_fam = STSPIX_FAM_SWEEP;
+  const int nseg = cfg.niters_seg;
+  *fused = false;
   // the first sweep of the call scores every border pixel; the later ones only the
-  // active set next to the previous sweep's changes (same labels, see kb_sweep_t*)
-  auto sweep = [&](int v, int parity, int mode, int stats) {
+  // active set next to the previous sweep's changes (same labels, see kb_sweep_t*).
+  // Launch j reads the labels of parity j & 1 and writes the other buffer.
+  auto sweep1 = [&](int v, int parity, int mode, int stats) {
     const unsigned g = (unsigned)std::max(1, L.tiles_upto[v][nb]);
     if (v == 1)
       LAUNCHG(kb_sweep_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
@@ -623,45 +629,116 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
     else
       LAUNCHG(kb_sweep_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
   };
-  const bool fuse = fuse_stats && cfg.niters_seg >= 2;
-  auto stats_of = [&](int it) {
-    return !fuse ? 0 : it == 0 ? 1 : it == cfg.niters_seg - 1 ? 2 : 0;
+  auto sweep2 = [&](int v, int parity, int mode, int stats) {   // v: 0 (32 wide) or 2 (16)
+    const unsigned g = (unsigned)std::max(1, L.tiles_upto[v][nb]);
+    if (v == 2)
+      LAUNCHG(kb_sweep2_t16, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
+    else
+      LAUNCHG(kb_sweep2_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
   };
-  // tile-shape autotuner: the first sweep of a batch size class runs every tile width
-  // on the same input (a sweep reads only the labels at its start, so all write the
-  // same output) and the fastest is kept for that class.  The class is the number of
-  // 32x32 tiles of the sweeping slots in quarter octaves: the choice depends on how
-  // well the tiles fill the SMs, and mixed serving batches then tune a handful of
-  // times instead of once per combination of frame sizes.
-  int it0 = 0;
+  // Tile autotuner: the first update of a batch size class runs its first sweep with
+  // every single-sweep tile width and (with three or more sweeps) its second and
+  // third sweeps with every two-sweep width, each on the same input (a launch reads
+  // only the labels at its start, so all write the same output); the class keeps the
+  // fastest single width and, when the best two-sweep launch beats two single ones,
+  // two-sweep launches.  The class is the number of 32x32 tiles of the sweeping slots
+  // in quarter octaves: the choice depends on how well the tiles fill the SMs, and
+  // mixed serving batches then tune a handful of times.
   const int tl = std::max(1, L.tiles_upto[0][nb]);
   const auto key = std::make_pair((unsigned long long)std::floor(4.0 * std::log2((double)tl)), 0);
   auto ch = ctx->sweep_choice.find(key);
-  int v;
-  if (ch != ctx->sweep_choice.end()) {
-    v = ch->second;
-  } else if (cfg.niters_seg > 0) {
+  int done = 0, launch = 0;
+  int v1 = 1, v2 = -1;      // best single-sweep width, two-sweep width (-1: none)
+  // planned launches: the sweeps each covers
+  auto plan_launches = [&](int from, int v2_) {
+    int n = 0;
+    for (int it = from; it < nseg; it += (v2_ >= 0 && nseg - it >= 2) ? 2 : 1) n++;
+    return n;
+  };
+  if (cfg.sweep_schedule == 2) {
+    v1 = 0;
+    v2 = 0;
+  } else if (ch != ctx->sweep_choice.end()) {
+    v1 = ch->second & 0xff;
+    v2 = cfg.sweep_schedule == 1 ? -1 : (ch->second >> 8) - 1;
+  } else if (nseg > 0) {
+    // the whole call's launch count is known only after tuning; the clear rides on the
+    // first launch, the accumulation on the last (decided when it is issued)
+    const bool fuse_ok = fuse_stats && nseg >= 2;
     CK(cudaEventRecord(ctx->tune_ev[0], st));
     for (int c = 0; c < kSweepVariants; c++) {
-      sweep(c, 0, 0, stats_of(0));
+      sweep1(c, 0, 0, fuse_ok ? 1 : 0);
       CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
     }
     CK(cudaEventSynchronize(ctx->tune_ev[kSweepVariants]));
-    float best = 0.f;
-    v = 0;
+    float best1 = 0.f;
+    v1 = 0;
     for (int c = 0; c < kSweepVariants; c++) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, ctx->tune_ev[c], ctx->tune_ev[c + 1]);
-      if (c == 0 || ms < best) { best = ms; v = c; }
+      if (c == 0 || ms < best1) { best1 = ms; v1 = c; }
     }
-    ctx->sweep_choice[key] = v;
+    done = 1;
+    launch = 1;
+    if (nseg >= 3 && cfg.sweep_schedule == 0) {
+      // a two-sweep launch is an active-set sweep plus a full-listing one: with four or
+      // more sweeps the second sweep runs alone (timed, active set) and the pair covers
+      // the third and fourth, and the pair is compared with that sweep plus a full one
+      float ref = 2.f * best1;
+      if (nseg >= 4) {
+        CK(cudaEventRecord(ctx->tune_ev[0], st));
+        sweep1(v1, launch & 1, 1, 0);
+        CK(cudaEventRecord(ctx->tune_ev[1], st));
+        CK(cudaEventSynchronize(ctx->tune_ev[1]));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->tune_ev[0], ctx->tune_ev[1]);
+        ref = best1 + ms;
+        done = 2;
+        launch = 2;
+      }
+      // (both pair runs write the same labels; neither adds statistics, which would
+      // count them twice: when the pair ends the call the next update_params accumulates)
+      const int pv[2] = {0, 2};
+      float best2 = 0.f;
+      int b2 = 0;
+      CK(cudaEventRecord(ctx->tune_ev[0], st));
+      for (int c = 0; c < 2; c++) {
+        sweep2(pv[c], launch & 1, 1, 0);
+        CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
+      }
+      CK(cudaEventSynchronize(ctx->tune_ev[2]));
+      for (int c = 0; c < 2; c++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->tune_ev[c], ctx->tune_ev[c + 1]);
+        if (c == 0 || ms < best2) { best2 = ms; b2 = pv[c]; }
+      }
+      v2 = best2 < ref ? b2 : -1;
+      done += 2;
+      launch += 1;
+    }
+    if (cfg.sweep_schedule == 0) ctx->sweep_choice[key] = v1 | ((v2 + 1) << 8);
     ctx->tunes++;
-    it0 = 1;
-  } else {
-    v = 1;
+    if (done >= nseg) {
+      if (launch & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
+      if (need_border) {
+        ctx->cur_fam = STSPIX_FAM_MERGE;
+        LAUNCHB(kb_find_border, L.max_npix, L, nb);
+      }
+      return STSPIX_OK;
+    }
   }
-  for (int it = it0; it < cfg.niters_seg; it++) sweep(v, it & 1, it > 0 ? 1 : 0, stats_of(it));
-  if (cfg.niters_seg & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
+  const int total = launch + plan_launches(done, v2);
+  const bool fuse = fuse_stats && total >= 2;
+  while (done < nseg) {
+    const bool pair = v2 >= 0 && nseg - done >= 2;
+    const int stats = !fuse ? 0 : launch == 0 ? 1 : launch == total - 1 ? 2 : 0;
+    if (pair) sweep2(v2, launch & 1, done > 0 ? 1 : 0, stats);
+    else sweep1(v1, launch & 1, done > 0 ? 1 : 0, stats);
+    done += pair ? 2 : 1;
+    launch++;
+  }
+  *fused = fuse;
+  if (launch & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;
     LAUNCHB(kb_find_border, L.max_npix, L, nb);
@@ -769,8 +846,10 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector
     const int nx = idx + 1;
     const bool merge_next = nx < maxn && nx > cfg.sm_start && nx % P == P / 2;
     const bool fuse_now = fuse && nx < maxn && !(stop_after >= 0 && nx == stop_after);
-    if ((r = update_seg(ctx, st, L, nb, cfg, merge_next || stop_after >= 0, fuse_now))) return r;
-    stats_ready = fuse_now && cfg.niters_seg >= 2;
+    bool fused = false;
+    if ((r = update_seg(ctx, st, L, nb, cfg, merge_next || stop_after >= 0, fuse_now, &fused)))
+      return r;
+    stats_ready = fused;
   }
   if (stop_after >= 0) {
     if (extra_update && (r = update_params(ctx, st, L, L.B))) return r;
@@ -819,9 +898,9 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
 }
 
 // The hole-fill loop of the propagated slots of table L as a graph: a WHILE node
-// whose body is one iteration (kb_fill_border, kb_fill_phase x 4, kb_fill_compact,
-// kb_fill_step, added as kernel nodes); kb_fill_step sets the condition.  Built once
-// per (table, size).
+// whose body is one iteration (kb_fill_phase x 4, kb_fill_compact, added as kernel
+// nodes); kb_fill_compact's last block sets the condition.  Built once per (table,
+// size).
 int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
   auto key = std::make_pair((const Slot*)L.d, L.B);
   auto it = ctx->fill_graphs.find(key);
@@ -859,19 +938,16 @@ int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
     ce = cudaGraphAddKernelNode(&n, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp);
     prev = n;
   };
-  void* a_border[] = {(void*)&table};
-  add((const void*)kb_fill_border, grid, dim3(kThreads), a_border);
   void* a_ph[4][2];
   for (int ph = 0; ph < 4; ph++) {
     a_ph[ph][0] = (void*)&table;
     a_ph[ph][1] = (void*)&ph_arg[ph];
     add((const void*)kb_fill_phase, grid, dim3(kThreads), a_ph[ph]);
   }
-  void* a_compact[] = {(void*)&table};
+  unsigned* ctr = (unsigned*)(ctx->body_iters + 1);
+  void* a_compact[] = {(void*)&table, (void*)&B, (void*)&cond, (void*)&break_iter,
+                       (void*)&ctx->body_iters, (void*)&ctr};
   add((const void*)kb_fill_compact, grid, dim3(kThreads), a_compact);
-  void* a_step[] = {(void*)&table, (void*)&B, (void*)&cond, (void*)&break_iter,
-                    (void*)&ctx->body_iters};
-  add((const void*)kb_fill_step, dim3(1), dim3(kThreads), a_step);
   if (ce != cudaSuccess) {
     cudaGraphDestroy(g);
     return fail(ctx, STSPIX_ERR_CUDA, "fill graph construction failed: %s", cudaGetErrorString(ce));
@@ -892,6 +968,9 @@ int run_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   int r = fill_graph(ctx, L, &exec);
   if (r) return r;
   LAUNCHS(kb_fill_begin, L, L.B);
+  // the first iteration's border flags (later ones come with the compaction)
+  const unsigned G = (unsigned)std::max(8, std::min(128, 2048 / std::max(L.B, 1)));
+  LAUNCHG(kb_fill_border, dim3(G, (unsigned)L.B), kThreads, L.d);
   cudaEvent_t pe = prof_begin(ctx, st);
   CK(cudaGraphLaunch(exec, st));
   prof_end(ctx, st, pe, "kb_fill_graph");
@@ -937,8 +1016,8 @@ int read_scalars(stspix_ctx* ctx, cudaStream_t st, int B) {
   CK(cudaMemcpyAsync(ctx->sc_host, ctx->sc, sizeof(Scalars) * (size_t)B, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(ctx->body_iters_host, ctx->body_iters, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  // kernels launched by the fill graphs: 7 per loop iteration
-  ctx->launches += 7 * ((long long)*ctx->body_iters_host - ctx->body_iters_seen);
+  // kernels launched by the fill graphs: 5 per loop iteration
+  ctx->launches += 5 * ((long long)*ctx->body_iters_host - ctx->body_iters_seen);
   ctx->body_iters_seen = *ctx->body_iters_host;
   CK(cudaGetLastError());
   prof_harvest(ctx);
@@ -1057,6 +1136,8 @@ int check_cfg(stspix_ctx* ctx, const stspix_config* cfg) {
   if (!cfg) return fail(ctx, STSPIX_ERR_ARG, "config is NULL");
   if (cfg->accumulator < 0 || cfg->accumulator > 2)
     return fail(ctx, STSPIX_ERR_ARG, "accumulator must be 0, 1 or 2");
+  if (cfg->sweep_schedule < 0 || cfg->sweep_schedule > 2)
+    return fail(ctx, STSPIX_ERR_ARG, "sweep_schedule must be 0, 1 or 2");
   if (cfg->sp_size < 1) return fail(ctx, STSPIX_ERR_ARG, "sp_size must be >= 1");
   if (cfg->niters < 0 || cfg->niters_seg < 0)
     return fail(ctx, STSPIX_ERR_ARG, "iteration counts must be >= 0");
@@ -1162,6 +1243,7 @@ void stspix_default_config(stspix_config* c) {
   c->split_alpha = 0.f; c->merge_alpha = 0.f; c->sigma2_size = 0.f;
   c->thresh_relabel = 1e-5f; c->thresh_new = 1e-2f;
   c->accumulator = 0;
+  c->sweep_schedule = 0;
 }
 
 int stspix_version(void) { return 2; }
@@ -1187,12 +1269,12 @@ int stspix_create(stspix_ctx** out, int device) {
   }
   // slot tables for 256 frames per batch from the start: they never move for
   // batches up to that size, so the graphs that point at them stay valid
-  if (ensure_bcap(ctx, 256) != STSPIX_OK || cudaMalloc(&ctx->body_iters, sizeof(int)) != cudaSuccess ||
+  if (ensure_bcap(ctx, 256) != STSPIX_OK || cudaMalloc(&ctx->body_iters, 2 * sizeof(int)) != cudaSuccess ||
       cudaMallocHost(&ctx->body_iters_host, sizeof(int)) != cudaSuccess) {
     delete ctx;
     return STSPIX_ERR_NOMEM;
   }
-  cudaMemset(ctx->body_iters, 0, sizeof(int));
+  cudaMemset(ctx->body_iters, 0, 2 * sizeof(int));
   cudaEventCreate(&ctx->batch_ev[0]);
   cudaEventCreate(&ctx->batch_ev[1]);
   for (auto& e : ctx->tune_ev) cudaEventCreate(&e);

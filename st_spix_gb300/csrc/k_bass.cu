@@ -674,16 +674,21 @@ __device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int 
 // The grid is the list of tiles of every frame of the batch (frame i owns tiles
 // [tile_base, tile_base + its tile count)); a block finds its frame by binary
 // search, so frames of uneven size cost what their tiles cost.
-constexpr int kSH = 4;                // label halo
+constexpr int kReach = 4;             // a sweep's labels depend on labels this far away
 
-template <int TX, int TY>
+// NS sweeps per launch (1 or 2): the label halo is 4 NS pixels; sweep s of the launch
+// lists and scores the tile grown by G = 4 (NS - s) - 1 pixels (phase k on the tile
+// grown by G - k), so after sweep s the labels of the tile grown by 4 (NS - s - 1)
+// are exactly those of NS separate launches.
+template <int TX, int TY, int NS>
 struct SweepTile {
+  static constexpr int kSH = 4 * NS;                                 // label halo
+  static constexpr int kG0 = kSH - 1;                                // first sweep's growth
   static constexpr int kLX = TX + 2 * kSH, kLY = TY + 2 * kSH;      // staged labels
-  static constexpr int kIX = TX + 2 * (kSH - 1), kIY = TY + 2 * (kSH - 1);  // image / border
-  static constexpr int kMaxList = (TX / 2 + kSH - 1) * (TY / 2 + kSH - 1);
-  static_assert(kIX < 256 && kIY < 256, "list entries pack (ly << 8) | lx");
+  static constexpr int kMaxList = (TX / 2 + kG0) * (TY / 2 + kG0);
+  static_assert(TX + 2 * kG0 < 256 && TY + 2 * kG0 < 256, "list entries pack (ly << 8) | lx");
   int L[kLX * kLY];
-  int L0[TX * TY];                    // the tile's labels at the sweep start
+  int L0[TX * TY];                    // the tile's labels before the launch's last sweep
   unsigned short list[4][kMaxList];   // border pixels of each parity phase, (ly << 8) | lx
   int cnt[4];
   // active-set sweeps: change flags of the label region as row bitmasks (bit x of
@@ -699,7 +704,7 @@ struct SweepTile {
 // kb_accumulate's whatever the segmentation into runs.
 template <int TX, int TY>
 __device__ __noinline__ void tile_accumulate(const Slot& S, const int* __restrict__ L,
-                                                int kLX, int tx0, int ty0) {
+                                                int kLX, int kSH, int tx0, int ty0) {
   constexpr int kSegs = (TX + 31) / 32;               // 32-pixel segments per row
   constexpr int kRows = TX >= 32 ? 1 : 32 / TX;       // rows per warp pass
   constexpr int kPasses = (TY / kRows) * kSegs;
@@ -751,135 +756,28 @@ __device__ __noinline__ void tile_accumulate(const Slot& S, const int* __restric
 // therefore list only the border pixels within 4 pixels of a change flagged by the
 // previous sweep (chg_in), and a tile whose whole label region saw no change keeps
 // its labels.  Every sweep writes its own change flags (chg_out).
-template <int TX, int TY>
-__device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int parity, float s2,
-                                           float potts, SweepTile<TX, TY>& sm,
-                                           const unsigned* lut_bits, int mode, int stats) {
-  constexpr int kTX = TX, kTY = TY;
-  constexpr int kLX = SweepTile<TX, TY>::kLX, kLY = SweepTile<TX, TY>::kLY;
-  constexpr int kIX = SweepTile<TX, TY>::kIX, kIY = SweepTile<TX, TY>::kIY;
+// One sweep inside a launch: list the border pixels of each parity class on the tile
+// grown by G (phase k on the tile grown by G - k), then score them phase by phase in
+// shared memory.  OFF = label-region offset of the grown-by-G region; use_act: only
+// pixels flagged in sm.act (active-set sweeps).
+template <int TX, int TY, int NS, int G>
+__device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>& sm,
+                                           const unsigned* lut_bits, int tx0, int ty0,
+                                           float s2, float potts, bool use_act) {
+  constexpr int kLX = SweepTile<TX, TY, NS>::kLX;
+  constexpr int OFF = SweepTile<TX, TY, NS>::kSH - G;
+  constexpr int kIX = TX + 2 * G, kIY = TY + 2 * G;
   int* L = sm.L;
   auto& list = sm.list;
   int* cnt = sm.cnt;
-
   const int H = S.H, W = S.W;
   const float* __restrict__ img = S.img;
-  const int* __restrict__ seg_in = parity ? S.seg_alt : S.seg;
-  int* __restrict__ seg_out = parity ? S.seg : S.seg_alt;
   const SweepRec* __restrict__ rec = S.sp.rec;
   const int cap = S.sp.cap;
-  if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
-  const int tx0 = bx * kTX, ty0 = by * kTY;
-  const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;        // label region origin
-  const int ix0 = tx0 - (kSH - 1), iy0 = ty0 - (kSH - 1);  // image region origin
-  const uint8_t* __restrict__ chg_in = S.chg[parity ^ 1];
-  uint8_t* __restrict__ chg_out = S.chg[parity];
-  static_assert(kLX <= 128, "label region wider than two 64-bit words");
-  // The label region is loaded first, into registers: warp w takes rows w, w + 8, ...
-  // in 32-label chunks, every load issued before any is used, so the block waits for
-  // one memory round trip (overlapping the change-flag loads of active-set sweeps);
-  // the tile's part is kept in shared memory for the change flags at the end (no
-  // second read of the labels).
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int kRW = (kLY + 7) / 8, kCK = (kLX + 31) / 32;
-  int lv[kRW][kCK];
-#pragma unroll
-  for (int a = 0; a < kRW; a++) {
-    const int r = warp + 8 * a, gy = ry0 + r;
-    const bool row_ok = r < kLY && gy >= 0 && gy < H;
-#pragma unroll
-    for (int c = 0; c < kCK; c++) {
-      const int x = lane + 32 * c, gx = rx0 + x;
-      lv[a][c] = (row_ok && x < kLX && gx >= 0 && gx < W) ? seg_in[gy * W + gx] : -1;
-    }
-  }
-  // tile pixels of the staging layout: (a, c) -> label-region (r, x)
-  auto in_tile = [&](int r, int x) {
-    return r >= kSH && r < kSH + kTY && x >= kSH && x < kSH + kTX && ry0 + r < H && rx0 + x < W;
-  };
-  if (mode) {
-    unsigned long long* a0 = sm.act[0];
-    unsigned long long* a1 = sm.act[1];
-    if (threadIdx.x == 0) sm.any = 0;
-    for (int r = threadIdx.x; r < kLY; r += blockDim.x) { a0[r] = 0; a1[r] = 0; }
-    __syncthreads();
-    constexpr int kCh = (kLX + 31) / 32;
-    for (int c = warp; c < kLY * kCh; c += blockDim.x / 32) {
-      const int r = c / kCh, cx = c % kCh;
-      const int x = cx * 32 + lane;
-      const int gx = rx0 + x, gy = ry0 + r;
-      const bool f = x < kLX && gx >= 0 && gx < W && gy >= 0 && gy < H && chg_in[gy * W + gx];
-      const unsigned b = __ballot_sync(0xffffffffu, f);
-      if (lane == 0 && b) {
-        // chunk cx covers bits 32 cx .. 32 cx + 31 of the row: word cx / 2, half cx % 2
-        atomicOr(cx < 2 ? &a0[r] : &a1[r], (unsigned long long)b << (32 * (cx & 1)));
-        sm.any = 1;
-      }
-    }
-    __syncthreads();
-    if (!sm.any) {
-      // nothing within reach changed: the tile keeps its labels
-#pragma unroll
-      for (int a = 0; a < kRW; a++) {
-        const int r = warp + 8 * a;
-#pragma unroll
-        for (int c = 0; c < kCK; c++) {
-          const int x = lane + 32 * c;
-          if (r < kLY && x < kLX && in_tile(r, x)) {
-            const size_t g = (size_t)(ry0 + r) * W + (rx0 + x);
-            seg_out[g] = lv[a][c];
-            chg_out[g] = 0;
-            if (stats == 2) L[r * kLX + x] = lv[a][c];
-          }
-        }
-      }
-      if (stats == 2) {
-        __syncthreads();
-        tile_accumulate<TX, TY>(S, L, kLX, tx0, ty0);
-      }
-      return;
-    }
-    // dilate by 4: horizontally within each row (two-word shifts), then vertically
-    unsigned long long h0 = 0, h1 = 0;
-    const int r = threadIdx.x;
-    if (r < kLY) {
-      const unsigned long long lo = a0[r], hi = a1[r];
-      h0 = lo; h1 = hi;
-#pragma unroll
-      for (int sft = 1; sft <= kSH; sft++) {
-        h0 |= (lo << sft) | (lo >> sft) | (hi << (64 - sft));
-        h1 |= (hi << sft) | (hi >> sft) | (lo >> (64 - sft));
-      }
-    }
-    __syncthreads();
-    if (r < kLY) { a0[r] = h0; a1[r] = h1; }
-    __syncthreads();
-    unsigned long long v0 = 0, v1 = 0;
-    if (r < kLY) {
-      for (int k = max(0, r - kSH); k <= min(kLY - 1, r + kSH); k++) { v0 |= a0[k]; v1 |= a1[k]; }
-    }
-    __syncthreads();
-    if (r < kLY) { a0[r] = v0; a1[r] = v1; }
-    // (the barrier after the label stores below orders these before the border pass)
-  }
-  // labels to shared memory (colours are not staged: the scored border pixels read
-  // theirs from global memory)
-#pragma unroll
-  for (int a = 0; a < kRW; a++) {
-    const int r = warp + 8 * a;
-#pragma unroll
-    for (int c = 0; c < kCK; c++) {
-      const int x = lane + 32 * c;
-      if (r < kLY && x < kLX) {
-        L[r * kLX + x] = lv[a][c];
-        if (r >= kSH && r < kSH + kTY && x >= kSH && x < kSH + kTX)
-          sm.L0[(r - kSH) * kTX + (x - kSH)] = lv[a][c];
-      }
-    }
-  }
-  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int ix0 = tx0 - G, iy0 = ty0 - G;
   // Border mask at the sweep start (find_border_pixels, seg_utils.cu:164-195); the
-  // border pixels of parity class k inside the tile grown by 3-k pixels are listed
+  // border pixels of parity class k inside the tile grown by G-k pixels are listed
   // for phase k, so each phase scores only its border pixels, densely.
   // (appends are warp-aggregated: one shared atomic per warp and phase)
   for (int base = 0; base < kIX * kIY; base += blockDim.x) {
@@ -889,8 +787,8 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       const int lx = i % kIX, ly = i / kIX;
       const int gx = ix0 + lx, gy = iy0 + ly;
       bool act = gx >= 0 && gx < W && gy >= 0 && gy < H;
-      if (act && mode) {
-        const int ax = lx + 1, ay = ly + 1;   // label-region coordinates
+      if (act && use_act) {
+        const int ax = lx + OFF, ay = ly + OFF;   // label-region coordinates
         act = ((ax < 64 ? sm.act[0][ay] >> ax : sm.act[1][ay] >> (ax - 64)) & 1ull) != 0;
       }
       if (act) {
@@ -898,14 +796,14 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
         if (gy < 1 || gx < 1 || gy >= H - 1 || gx >= W - 1) {
           b = true;
         } else {
-          const int p = (ly + 1) * kLX + (lx + 1);
+          const int p = (ly + OFF) * kLX + (lx + OFF);
           const int C = L[p];
           b = (C != L[p - kLX] || C != L[p + kLX] || C != L[p + 1] || C != L[p - 1]);
         }
         const int c = ((gx & 1) << 1) | (gy & 1);
-        const int grow = 3 - c;
-        if (b && gx >= tx0 - grow && gx < tx0 + kTX + grow && gy >= ty0 - grow &&
-            gy < ty0 + kTY + grow)
+        const int grow = G - c;
+        if (b && gx >= tx0 - grow && gx < tx0 + TX + grow && gy >= ty0 - grow &&
+            gy < ty0 + TY + grow)
           ph = c;
       }
     }
@@ -929,7 +827,7 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       const int bi = list[ph][j];
       const int lxi = bi & 255, lyi = bi >> 8;
       int gx = ix0 + lxi, gy = iy0 + lyi;
-      int p = (lyi + 1) * kLX + (lxi + 1);
+      int p = (lyi + OFF) * kLX + (lxi + OFF);
       int C = L[p];
       if (C < 0 || C >= cap) continue;
       const int N = L[p - kLX], S = L[p + kLX], Wl = L[p - 1], E = L[p + 1];
@@ -976,7 +874,156 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
     }
     __syncthreads();
   }
-  // write back the tile, with change flags against the labels at the sweep start
+}
+
+// Active-set sweeps.  The parameters are fixed across the sweeps of one update_seg
+// call and a pixel's decision depends only on its 3x3 labels (after the earlier
+// phases of the sweep), its colour and the parameters, so a pixel of phase k can
+// only change if a label within Chebyshev distance k + 1 <= 4 changed during the
+// previous sweep or earlier in this one.  Sweeps after the first of a call (mode 1)
+// therefore list only the border pixels within 4 pixels of a change flagged by the
+// previous sweep (chg_in), and a tile whose whole label region saw no change keeps
+// its labels.  Every launch writes the change flags of its last sweep (chg_out); in
+// a two-sweep launch the second sweep lists every border pixel.
+template <int TX, int TY, int NS>
+__device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int parity, float s2,
+                                           float potts, SweepTile<TX, TY, NS>& sm,
+                                           const unsigned* lut_bits, int mode, int stats) {
+  constexpr int kTX = TX, kTY = TY;
+  constexpr int kSH = SweepTile<TX, TY, NS>::kSH;
+  constexpr int kLX = SweepTile<TX, TY, NS>::kLX, kLY = SweepTile<TX, TY, NS>::kLY;
+  int* L = sm.L;
+  int* cnt = sm.cnt;
+
+  const int H = S.H, W = S.W;
+  const int* __restrict__ seg_in = parity ? S.seg_alt : S.seg;
+  int* __restrict__ seg_out = parity ? S.seg : S.seg_alt;
+  if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
+  const int tx0 = bx * kTX, ty0 = by * kTY;
+  const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;        // label region origin
+  const uint8_t* __restrict__ chg_in = S.chg[parity ^ 1];
+  uint8_t* __restrict__ chg_out = S.chg[parity];
+  static_assert(kLX <= 128, "label region wider than two 64-bit words");
+  // The label region is loaded first, into registers: warp w takes rows w, w + 8, ...
+  // in 32-label chunks, every load issued before any is used, so the block waits for
+  // one memory round trip (overlapping the change-flag loads of active-set sweeps);
+  // the tile's part is kept in shared memory for the change flags at the end (no
+  // second read of the labels).
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kRW = (kLY + 7) / 8, kCK = (kLX + 31) / 32;
+  int lv[kRW][kCK];
+#pragma unroll
+  for (int a = 0; a < kRW; a++) {
+    const int r = warp + 8 * a, gy = ry0 + r;
+    const bool row_ok = r < kLY && gy >= 0 && gy < H;
+#pragma unroll
+    for (int c = 0; c < kCK; c++) {
+      const int x = lane + 32 * c, gx = rx0 + x;
+      lv[a][c] = (row_ok && x < kLX && gx >= 0 && gx < W) ? seg_in[gy * W + gx] : -1;
+    }
+  }
+  // tile pixels of the staging layout: (a, c) -> label-region (r, x)
+  auto in_tile = [&](int r, int x) {
+    return r >= kSH && r < kSH + kTY && x >= kSH && x < kSH + kTX && ry0 + r < H && rx0 + x < W;
+  };
+  if (mode) {
+    unsigned long long* a0 = sm.act[0];
+    unsigned long long* a1 = sm.act[1];
+    if (threadIdx.x == 0) sm.any = 0;
+    for (int r = threadIdx.x; r < kLY; r += blockDim.x) { a0[r] = 0; a1[r] = 0; }
+    __syncthreads();
+    constexpr int kCh = (kLX + 31) / 32;
+    for (int c = warp; c < kLY * kCh; c += blockDim.x / 32) {
+      const int r = c / kCh, cx = c % kCh;
+      const int x = cx * 32 + lane;
+      const int gx = rx0 + x, gy = ry0 + r;
+      const bool f = x < kLX && gx >= 0 && gx < W && gy >= 0 && gy < H && chg_in[gy * W + gx];
+      const unsigned b = __ballot_sync(0xffffffffu, f);
+      if (lane == 0 && b) {
+        // chunk cx covers bits 32 cx .. 32 cx + 31 of the row: word cx / 2, half cx % 2
+        atomicOr(cx < 2 ? &a0[r] : &a1[r], (unsigned long long)b << (32 * (cx & 1)));
+        sm.any = 1;
+      }
+    }
+    __syncthreads();
+    if (!sm.any) {
+      // nothing within reach changed: the tile keeps its labels (for every sweep of
+      // the launch: a later sweep can only move pixels within reach of an earlier
+      // change, and there is none in the label region)
+#pragma unroll
+      for (int a = 0; a < kRW; a++) {
+        const int r = warp + 8 * a;
+#pragma unroll
+        for (int c = 0; c < kCK; c++) {
+          const int x = lane + 32 * c;
+          if (r < kLY && x < kLX && in_tile(r, x)) {
+            const size_t g = (size_t)(ry0 + r) * W + (rx0 + x);
+            seg_out[g] = lv[a][c];
+            chg_out[g] = 0;
+            if (stats == 2) L[r * kLX + x] = lv[a][c];
+          }
+        }
+      }
+      if (stats == 2) {
+        __syncthreads();
+        tile_accumulate<TX, TY>(S, L, kLX, kSH, tx0, ty0);
+      }
+      return;
+    }
+    // dilate by the reach: horizontally within each row (two-word shifts), then
+    // vertically
+    unsigned long long h0 = 0, h1 = 0;
+    const int r = threadIdx.x;
+    if (r < kLY) {
+      const unsigned long long lo = a0[r], hi = a1[r];
+      h0 = lo; h1 = hi;
+#pragma unroll
+      for (int sft = 1; sft <= kReach; sft++) {
+        h0 |= (lo << sft) | (lo >> sft) | (hi << (64 - sft));
+        h1 |= (hi << sft) | (hi >> sft) | (lo >> (64 - sft));
+      }
+    }
+    __syncthreads();
+    if (r < kLY) { a0[r] = h0; a1[r] = h1; }
+    __syncthreads();
+    unsigned long long v0 = 0, v1 = 0;
+    if (r < kLY) {
+      for (int k = max(0, r - kReach); k <= min(kLY - 1, r + kReach); k++) {
+        v0 |= a0[k]; v1 |= a1[k];
+      }
+    }
+    __syncthreads();
+    if (r < kLY) { a0[r] = v0; a1[r] = v1; }
+    // (the barrier after the label stores below orders these before the border pass)
+  }
+  // labels to shared memory (colours are not staged: the scored border pixels read
+  // theirs from global memory)
+#pragma unroll
+  for (int a = 0; a < kRW; a++) {
+    const int r = warp + 8 * a;
+#pragma unroll
+    for (int c = 0; c < kCK; c++) {
+      const int x = lane + 32 * c;
+      if (r < kLY && x < kLX) {
+        L[r * kLX + x] = lv[a][c];
+        if (NS == 1 && r >= kSH && r < kSH + kTY && x >= kSH && x < kSH + kTX)
+          sm.L0[(r - kSH) * kTX + (x - kSH)] = lv[a][c];
+      }
+    }
+  }
+  __syncthreads();
+  if (NS == 1) {
+    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0);
+  } else {
+    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0);
+    // the tile's labels before the last sweep (its change flags), fresh lists
+    for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x)
+      sm.L0[i] = L[(i / kTX + kSH) * kLX + (i % kTX + kSH)];
+    if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    sweep_pass<TX, TY, NS, 3>(S, sm, lut_bits, tx0, ty0, s2, potts, false);
+  }
+  // write back the tile, with change flags of the last sweep
   for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x) {
     const int x = i % kTX, y = i / kTX;
     const int gx = tx0 + x, gy = ty0 + y;
@@ -986,13 +1033,13 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       chg_out[gy * W + gx] = v != sm.L0[i];
     }
   }
-  if (stats == 2) tile_accumulate<TX, TY>(S, L, kLX, tx0, ty0);
+  if (stats == 2) tile_accumulate<TX, TY>(S, L, kLX, kSH, tx0, ty0);
 }
 
-template <int TX, int TY>
+template <int TX, int TY, int NS>
 __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B, int parity,
                                            float s2, float potts, int mode, int stats) {
-  __shared__ SweepTile<TX, TY> sm;
+  __shared__ SweepTile<TX, TY, NS> sm;
   __shared__ unsigned lut_bits[8];
   if (threadIdx.x < 8) {
     unsigned w = 0;
@@ -1022,32 +1069,28 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
       for (int c = 0; c < 8; c++) a[c] = 0;
     }
   }
-  sweep_tile<TX, TY>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits, mode,
-                     stats);
+  sweep_tile<TX, TY, NS>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits, mode,
+                         stats);
 }
 
-// One block per tile of the batch (grid = the batch's total tile count).
+// One block per tile of the batch (grid = the batch's total tile count), one sweep
+// (kb_sweep_t*) or two consecutive sweeps (kb_sweep2_t*) per launch.
 // mode 0: every border pixel (first sweep of an update_seg call); 1: active set.
-// stats 1: also clear the statistics (first sweep); 2: also add the statistics of the
-// final labels (last sweep); 0: neither.
-__global__ void __launch_bounds__(256) kb_sweep_t32(const Slot* __restrict__ slots, int B,
-                                                    int parity, float s2, float potts,
-                                                    int mode, int stats) {
-  pdl_enter();
-  sweep_flat<32, 32>(slots, B, parity, s2, potts, mode, stats);
-}
-__global__ void __launch_bounds__(256, 5) kb_sweep_t64(const Slot* __restrict__ slots, int B,
-                                                    int parity, float s2, float potts,
-                                                    int mode, int stats) {
-  pdl_enter();
-  sweep_flat<64, 32>(slots, B, parity, s2, potts, mode, stats);
-}
-__global__ void __launch_bounds__(256) kb_sweep_t16(const Slot* __restrict__ slots, int B,
-                                                    int parity, float s2, float potts,
-                                                    int mode, int stats) {
-  pdl_enter();
-  sweep_flat<16, 32>(slots, B, parity, s2, potts, mode, stats);
-}
+// stats 1: also clear the statistics (first launch); 2: also add the statistics of the
+// final labels (last launch); 0: neither.
+#define STSPIX_SWEEP_KERNEL(name, TX, NS, MINB)                                          \
+  __global__ void __launch_bounds__(256, MINB) name(const Slot* __restrict__ slots, int B, \
+                                                    int parity, float s2, float potts,     \
+                                                    int mode, int stats) {                 \
+    pdl_enter();                                                                          \
+    sweep_flat<TX, 32, NS>(slots, B, parity, s2, potts, mode, stats);                     \
+  }
+STSPIX_SWEEP_KERNEL(kb_sweep_t32, 32, 1, 5)
+STSPIX_SWEEP_KERNEL(kb_sweep_t64, 64, 1, 5)
+STSPIX_SWEEP_KERNEL(kb_sweep_t16, 16, 1, 5)
+STSPIX_SWEEP_KERNEL(kb_sweep2_t32, 32, 2, 4)
+STSPIX_SWEEP_KERNEL(kb_sweep2_t16, 16, 2, 4)
+#undef STSPIX_SWEEP_KERNEL
 
 // ---------------------------------------------------------------------------
 // Parameter read-out (read_params, sparams_io.cu:190-286) and prior update

@@ -179,11 +179,12 @@ __global__ void kb_count_labels(const Slot* __restrict__ slots, int which) {
 // ---------------------------------------------------------------------------
 // Hole filling (fill_missing.cu:35-130, update_missing_seg_nn :288-441,
 // find_border_along_missing :617-647) over the list of hole pixels instead of the
-// frame.  One iteration = kb_fill_border, kb_fill_phase x 4, kb_fill_compact,
-// kb_fill_step; the host runs it as the body of a CUDA-graph WHILE node whose
-// condition kb_fill_step sets, so the loop needs neither host round trips nor grid
-// barriers.  Per iteration: the hole count (the list length), the border flag of
-// every hole (a 4-neighbour labelled at the start of the iteration), four parity
+// frame.  One iteration = kb_fill_phase x 4 and kb_fill_compact (the border flags of
+// the first iteration by kb_fill_border before the loop); the host runs it as the body
+// of a CUDA-graph WHILE node whose condition kb_fill_compact's last block sets, so the
+// loop needs neither host round trips nor grid barriers.  Per iteration: the hole
+// count (the list length), the border flag of every hole (a 4-neighbour labelled at
+// the start of the iteration), four parity
 // phases in which a bordered hole takes the label of the neighbour whose centre is
 // nearest, then the holes left are compacted into the other list buffer.  Stop
 // rules as the reference: a count equal to the previous one is an error (it exits),
@@ -260,59 +261,77 @@ __global__ void kb_fill_phase(const Slot* __restrict__ slots, int ph) {
 }
 
 // Holes still unfilled go to the other list buffer (warp-aggregated append; the
-// order does not matter, see append_hole).
-__global__ void kb_fill_compact(const Slot* __restrict__ slots) {
+// order does not matter, see append_hole), each with its border flag for the next
+// iteration (a labelled 4-neighbour now, i.e. at the start of the next iteration).
+// The last block to finish (a device counter, no waiting) closes the iteration for
+// every slot: count, stop rules, list swap, and the loop condition.  *body_iters
+// counts the iterations run; ctr is reset for the next iteration.
+__global__ void kb_fill_compact(const Slot* __restrict__ slots, int B,
+                                cudaGraphConditionalHandle cond, int break_iter, int* body_iters,
+                                unsigned* ctr) {
   pdl_enter();
   SLOT_Y;
   Scalars* sc = S.sc;
-  if (sc->fl_done) return;
-  const int n = sc->fl_n;
-  const int* la = fill_list(S);
-  int* lb = sc->fl_cur ? S.smseg : S.hits;
-  const int lane = threadIdx.x & 31;
-  const int stride = gridDim.x * blockDim.x;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const int j = base + threadIdx.x;
-    int idx = -1;
-    if (j < n) idx = la[j];
-    const bool keep = j < n && S.seg[idx] < 0;
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (!m) continue;
-    const int leader = __ffs(m) - 1;
-    int pos = 0;
-    if (lane == leader) pos = atomicAdd(&sc->fl_next, __popc(m));
-    pos = __shfl_sync(0xffffffffu, pos, leader);
-    if (keep) lb[pos + __popc(m & ((1u << lane) - 1))] = idx;
+  if (!sc->fl_done) {
+    const int n = sc->fl_n, W = S.W, H = S.H;
+    const int* la = fill_list(S);
+    int* lb = sc->fl_cur ? S.smseg : S.hits;
+    const int* seg = S.seg;
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+      const int j = base + threadIdx.x;
+      int idx = -1;
+      if (j < n) idx = la[j];
+      const bool keep = j < n && seg[idx] < 0;
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (!m) continue;
+      const int leader = __ffs(m) - 1;
+      int pos = 0;
+      if (lane == leader) pos = atomicAdd(&sc->fl_next, __popc(m));
+      pos = __shfl_sync(0xffffffffu, pos, leader);
+      if (keep) {
+        const int at = pos + __popc(m & ((1u << lane) - 1));
+        const int x = idx % W, y = idx / W;
+        const bool bd = (y > 0 && seg[idx - W] >= 0) || (x > 0 && seg[idx - 1] >= 0) ||
+                        (y < H - 1 && seg[idx + W] >= 0) || (x < W - 1 && seg[idx + 1] >= 0);
+        lb[at] = idx;
+        S.border[at] = bd ? 1 : 0;
+      }
+    }
   }
-}
-
-// End of an iteration, one thread per slot; thread 0 sets the loop condition
-// (any slot still filling).  *body_iters counts the iterations run.
-__global__ void kb_fill_step(const Slot* __restrict__ slots, int B,
-                             cudaGraphConditionalHandle cond, int break_iter, int* body_iters) {
-  pdl_enter();
+  __shared__ int is_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    is_last = atomicAdd(ctr, 1u) == gridDim.x * gridDim.y - 1;
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
   int active = 0;
   for (int i = threadIdx.x; i < B; i += blockDim.x) {
-    Scalars* sc = slots[i].sc;
-    if (sc->fl_done) continue;
-    const int num_neg = sc->fl_n;
-    sc->fill_iters += 1;
-    sc->fl_iter += 1;
-    if (num_neg == sc->fl_prev) {
-      sc->status = STSPIX_ERR_NOPROGRESS;
-      sc->fl_done = 1;
+    Scalars* si = slots[i].sc;
+    if (si->fl_done) continue;
+    const int num_neg = si->fl_n;
+    si->fill_iters += 1;
+    si->fl_iter += 1;
+    if (num_neg == si->fl_prev) {
+      si->status = STSPIX_ERR_NOPROGRESS;
+      si->fl_done = 1;
     } else {
-      sc->fl_prev = num_neg;
-      if (num_neg <= 0 || sc->fl_iter >= break_iter) sc->fl_done = 1;
+      si->fl_prev = num_neg;
+      if (num_neg <= 0 || si->fl_iter >= break_iter) si->fl_done = 1;
     }
-    sc->fl_n = sc->fl_next;
-    sc->fl_next = 0;
-    sc->fl_cur ^= 1;
-    if (!sc->fl_done) active = 1;
+    si->fl_n = si->fl_next;
+    si->fl_next = 0;
+    si->fl_cur ^= 1;
+    if (!si->fl_done) active = 1;
   }
   active = __syncthreads_or(active);
   if (threadIdx.x == 0) {
     *body_iters += 1;
+    *ctr = 0u;
     cudaGraphSetConditional(cond, active ? 1u : 0u);
   }
 }

@@ -46,6 +46,11 @@ __global__ void kb_sweep_t64(const Slot* slots, int B, int parity, float s2, flo
                              int mode, int stats);
 __global__ void kb_sweep_t16(const Slot* slots, int B, int parity, float s2, float potts,
                              int mode, int stats);
+// two consecutive sweeps per launch (8-pixel halo)
+__global__ void kb_sweep2_t32(const Slot* slots, int B, int parity, float s2, float potts,
+                              int mode, int stats);
+__global__ void kb_sweep2_t16(const Slot* slots, int B, int parity, float s2, float potts,
+                              int mode, int stats);
 __global__ void kb_copy_labels(const Slot* slots);
 __global__ void kb_read_params(const Slot* slots);
 __global__ void kb_save_prev(const Slot* slots);
@@ -82,9 +87,8 @@ __global__ void kb_count_labels(const Slot* slots, int which);
 __global__ void kb_fill_begin(const Slot* slots, int B);
 __global__ void kb_fill_border(const Slot* slots);
 __global__ void kb_fill_phase(const Slot* slots, int ph);
-__global__ void kb_fill_compact(const Slot* slots);
-__global__ void kb_fill_step(const Slot* slots, int B, cudaGraphConditionalHandle cond,
-                             int break_iter, int* body_iters);
+__global__ void kb_fill_compact(const Slot* slots, int B, cudaGraphConditionalHandle cond,
+                                int break_iter, int* body_iters, unsigned* ctr);
 __global__ void kb_cc_init(const Slot* slots);
 __global__ void kb_cc_hook(const Slot* slots);
 __global__ void kb_cc_compress(const Slot* slots);

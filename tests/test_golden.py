@@ -57,3 +57,26 @@ def test_gpu_matches_video_golden():
                                  torch.from_numpy(g["flows"]).cuda(), int(g["niters"]), 15, 0.5,
                                  0.009 ** 2, float(np.log(0.5)), 0.0, True, False)
     np.testing.assert_array_equal(out.cpu().numpy(), g["labels"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schedule", [0, 1, 2])
+@pytest.mark.parametrize("niters_seg", [3, 4, 5])
+def test_gpu_sweep_schedules_match_oracle(schedule, niters_seg):
+    """One sweep per launch, two sweeps per launch (8-pixel halo) and the autotuned mix
+    give the oracle's labels, with even and odd sweep counts (the final copy, the single
+    after pairs).  Each case runs on a new CUDA stream, i.e. a new engine context, so the
+    autotuner's first update (tuning launches) is exercised for every sweep count."""
+    import torch
+    from st_spix_gb300 import bist_cuda
+    g = load("bist_video_48x64x3.npz")
+    cfg = O.default_config(niters=int(g["niters"]), niters_seg=niters_seg)
+    st, ref, _ = O.bist_forward(g["vid"], g["flows"], cfg, True)
+    assert st == 0
+    with torch.cuda.stream(torch.cuda.Stream()):
+        out = bist_cuda.bist_forward(torch.from_numpy(g["vid"]).cuda(),
+                                     torch.from_numpy(g["flows"]).cuda(), int(g["niters"]), 15,
+                                     0.5, 0.009 ** 2, float(np.log(0.5)), 0.0, True, False,
+                                     niters_seg=niters_seg, sweep_schedule=schedule)
+        torch.cuda.current_stream().synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
