@@ -1085,9 +1085,9 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
     pdl_enter();                                                                          \
     sweep_flat<TX, 32, NS>(slots, B, parity, s2, potts, mode, stats);                     \
   }
-STSPIX_SWEEP_KERNEL(kb_sweep_t32, 32, 1, 5)
-STSPIX_SWEEP_KERNEL(kb_sweep_t64, 64, 1, 5)
-STSPIX_SWEEP_KERNEL(kb_sweep_t16, 16, 1, 5)
+STSPIX_SWEEP_KERNEL(kb_sweep_t32, 32, 1, 6)
+STSPIX_SWEEP_KERNEL(kb_sweep_t64, 64, 1, 6)
+STSPIX_SWEEP_KERNEL(kb_sweep_t16, 16, 1, 6)
 STSPIX_SWEEP_KERNEL(kb_sweep2_t32, 32, 2, 4)
 STSPIX_SWEEP_KERNEL(kb_sweep2_t16, 16, 2, 4)
 #undef STSPIX_SWEEP_KERNEL
