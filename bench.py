@@ -185,6 +185,24 @@ def read_traffic(workload: str):
     return None
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest x over the ranks of the process group (x itself with one rank):
+    the whole job's time is its slowest replica's."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seeds(rank: int, streams: int) -> list:
+    """Video seeds of a replica's streams: disjoint across ranks (replicas only; no
+    data is exchanged between GPUs)."""
+    return [rank * streams + i for i in range(streams)]
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -689,6 +707,9 @@ def main():
                     help="serve: pixels per batch (0: no cap); bounds a batch's GPU time")
     ap.add_argument("--fps", type=float, default=30.0, help="serve: mean frame rate per stream")
     ap.add_argument("--frames", type=int, default=30, help="serve: frames per stream")
+    ap.add_argument("--sweep-schedule", type=int, default=0, choices=[0, 1, 2],
+                    help="stream: boundary sweeps per launch (0 autotuned, 1 one, 2 two); "
+                         "the labels are the same")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.streams is None:
@@ -730,15 +751,16 @@ def main():
     T = w["T"]
     cfg = dict(niters=w["niters"], sp_size=w["sp_size"], potts=w["potts"],
                sigma2_app=w["sigma2_app"], alpha=w["alpha"], split_alpha=w["split_alpha"],
-               sm_period=w["sm_period"], prop_niters=w["prop_niters"])
+               sm_period=w["sm_period"], prop_niters=w["prop_niters"],
+               sweep_schedule=args.sweep_schedule)
 
     # one video per stream (seed = rank * S + i), generated on the device; the host
     # copies feed the end-to-end leg
     from st_spix_gb300 import synth
     dvid, dflo = [], []
-    for i in range(S):
+    for i, sd in enumerate(replica_seeds(rank, S)):
         out = synth.voronoi_video_device(w["H"], w["W"], T, w["nseeds"], w["sigma"],
-                                         seed=rank * S + i, device=dev, regions=i == 0)
+                                         seed=sd, device=dev, regions=i == 0)
         dvid.append(out[0])
         dflo.append(out[1])
         if i == 0:
@@ -806,11 +828,7 @@ def main():
     total_launches = sum(c.launches() - a for c, a in zip(ctxs, l0))
     stop.set()
     th.join(timeout=5)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(elapsed, world, dev)
     frames_total = world * S * T * args.steps
     value = frames_total / elapsed
 
@@ -869,11 +887,7 @@ def main():
     run_lanes(e2e, args.steps)
     e2e_elapsed = time.perf_counter() - t0
     barrier()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_elapsed], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_elapsed = float(t.item())
+    e2e_elapsed = max_over_ranks(e2e_elapsed, world, dev)
     e2e_value = frames_total / e2e_elapsed
 
     if rank != 0:
@@ -917,6 +931,7 @@ def main():
                    "sp_size": w["sp_size"], "niters": w["niters"],
                    "prop_niters": w["prop_niters"], "sm_period": w["sm_period"],
                    "streams_per_gpu": S, "lanes": NL, "batch_per_lane": B0,
+                   "sweep_schedule": args.sweep_schedule,
                    "step": "all %d frames of every stream; frame t of a lane's streams is "
                            "one batch" % T,
                    "parallelism": f"replicas{world}",
