@@ -127,6 +127,10 @@ const char* stspix_last_error(const stspix_ctx* ctx);
 int         stspix_version(void);
 /* Number of kernels this context has launched since creation. */
 long long   stspix_kernel_launches(const stspix_ctx* ctx);
+/* Number of batch steps this context ran as replays of a captured CUDA graph (a batch
+ * step whose frame sizes, capacities, iteration counts and configuration repeat is
+ * captured on its second occurrence and replayed from then on).                    */
+long long   stspix_graph_replays(const stspix_ctx* ctx);
 /* Copy of the log of the last frame processed by this context (host). */
 int         stspix_get_frame_log(const stspix_ctx* ctx, stspix_frame_log* out);
 

@@ -81,7 +81,8 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_video_save", "stspix_video_load", "stspix_evaluate", "stspix_label_range",
            "stspix_count_spix", "stspix_size_variation", "stspix_sp_pooling",
            "stspix_legacy_shift_labels", "stspix_legacy_fill_missing", "stspix_legacy_rgb_to_lab",
-           "stspix_sp_video_pooling", "stspix_downsampled_video_to_pooled"]
+           "stspix_sp_video_pooling", "stspix_downsampled_video_to_pooled",
+           "stspix_graph_replays"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -155,6 +156,7 @@ def load(build_if_missing: bool = True):
             "stspix_legacy_rgb_to_lab": (I, [P, P, P, P, C.c_longlong]),
             "stspix_sp_video_pooling": (I, [P, P, P, P, I, I, I, I, I, I, P, P, P]),
             "stspix_downsampled_video_to_pooled": (I, [P, P, P, P, I, I, I, I, I, I, P]),
+            "stspix_graph_replays": (C.c_longlong, [P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -191,6 +193,9 @@ class Context:
 
     def launches(self) -> int:
         return int(self.lib.stspix_kernel_launches(self.handle))
+
+    def graph_replays(self) -> int:
+        return int(self.lib.stspix_graph_replays(self.handle))
 
     def frame_log(self) -> FrameLog:
         lg = FrameLog()

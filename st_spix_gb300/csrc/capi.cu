@@ -135,6 +135,14 @@ struct stspix_ctx {
   std::vector<double> frame_ms;
   cudaEvent_t batch_ev[2] = {nullptr, nullptr};
   double batch_ms = 0;
+  // batch graphs: a batch step seen before (same signature) is captured once and
+  // replayed; launches = kernels one replay runs (for the launch counter)
+  bool capturing = false;
+  cudaStream_t cap_stream = nullptr;   // records graphs for callers on the legacy stream
+  struct BatchGraph { cudaGraph_t g; cudaGraphExec_t exec; long long launches; };
+  std::map<std::string, BatchGraph> batch_graphs;
+  std::map<std::string, int> batch_seen;
+  long long graph_replays = 0;
 };
 
 namespace {
@@ -207,8 +215,9 @@ void prof_harvest(stspix_ctx* ctx) {
 }
 
 // Every kernel is launched with programmatic stream serialization (see pdl.h).
+// (pdl 0: a plain stream dependency, as while a batch graph is captured)
 template <typename... KArgs, typename... Args>
-void launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+void launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, int pdl,
               Args... args) {
   cudaLaunchConfig_t c = {};
   c.gridDim = grid;
@@ -217,7 +226,7 @@ void launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStrea
   c.stream = st;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
+  at[0].val.programmaticStreamSerializationAllowed = pdl;
   c.attrs = at;
   c.numAttrs = 1;
   cudaLaunchKernelEx(&c, k, args...);
@@ -226,7 +235,7 @@ void launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStrea
 #define LAUNCHG(kernel, grid, block, ...)                                      \
   do {                                                                         \
     cudaEvent_t pe_ = prof_begin(ctx, st);                                     \
-    launch_k(kernel, dim3(grid), dim3(block), 0, st, __VA_ARGS__);             \
+    launch_k(kernel, dim3(grid), dim3(block), 0, st, ctx->capturing ? 0 : 1, __VA_ARGS__); \
     ctx->launches++;                                                           \
     prof_end(ctx, st, pe_, #kernel);                                           \
   } while (0)
@@ -350,12 +359,19 @@ int ensure_slot(stspix_ctx* ctx, int i, int npix, int sp_cap) {
   return STSPIX_OK;
 }
 
+// Graphs hold the slot-table and staging addresses: dropped when those move.
 void drop_fill_graphs(stspix_ctx* ctx) {
   for (auto& kv : ctx->fill_graphs) {
     cudaGraphExecDestroy(kv.second.exec);
     cudaGraphDestroy(kv.second.g);
   }
   ctx->fill_graphs.clear();
+  for (auto& kv : ctx->batch_graphs) {
+    cudaGraphExecDestroy(kv.second.exec);
+    cudaGraphDestroy(kv.second.g);
+  }
+  ctx->batch_graphs.clear();
+  ctx->batch_seen.clear();
 }
 
 // Load every kernel of the library once per process, before any of them is used.
@@ -499,7 +515,14 @@ SmConsts sm_constants(const stspix_config& c) {
 }
 
 int slot_cap(const FrameDesc& f) {
-  if (f.mode) return std::max(10 * f.n_prev + 2, 64);
+  // propagated frames: the reference's 10 x n_prev (+2) rounded up to a power of two,
+  // so consecutive frames of a stream keep one capacity (and one launch geometry); the
+  // logical buffer size (split rule) stays 10 x n_prev (Scalars::nbuf_logical)
+  if (f.mode) {
+    int c = 64;
+    while (c < 10 * f.n_prev + 2) c <<= 1;
+    return c;
+  }
   double Hh, w;
   int nx, ny;
   hex_geometry(f.sp_size, f.W, f.H, &Hh, &w, &nx, &ny);
@@ -554,7 +577,8 @@ List make_list(stspix_ctx* ctx, int off, const std::vector<Slot>& slots) {
     h[i] = s;
     L.max_npix = std::max(L.max_npix, s.npix);
     L.max_cap = std::max(L.max_cap, s.cap);
-    L.max_nprev = std::max(L.max_nprev, s.n_prev);
+    // a bound on n_prev that depends on the capacity only (grids over previous ids)
+    if (s.mode) L.max_nprev = std::max(L.max_nprev, (s.cap - 2) / 10);
     L.max_w = std::max(L.max_w, s.W);
     L.max_h = std::max(L.max_h, s.H);
     L.max_acc = std::max(L.max_acc, (long long)s.H * ((s.W + 7) / 8));
@@ -661,6 +685,9 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   } else if (ch != ctx->sweep_choice.end()) {
     v1 = ch->second & 0xff;
     v2 = cfg.sweep_schedule == 1 ? -1 : (ch->second >> 8) - 1;
+  } else if (ctx->capturing) {
+    v1 = 1;     // no timing inside a graph capture (a replayed batch was tuned before)
+    v2 = -1;
   } else if (nseg > 0) {
     // the whole call's launch count is known only after tuning; the clear rides on the
     // first launch, the accumulation on the last (decided when it is issued)
@@ -756,7 +783,8 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
   LAUNCHG(kb_split_bfs, dim3(256, (unsigned)nb), 128, L.d);  // 1024 warps per slot
   {
     cudaEvent_t pe_ = prof_begin(ctx, st);
-    launch_k(kb_split_bfs_big, dim3(8, (unsigned)nb), dim3(256), kBfsBigSmem, st, L.d);
+    launch_k(kb_split_bfs_big, dim3(8, (unsigned)nb), dim3(256), kBfsBigSmem, st,
+             ctx->capturing ? 0 : 1, L.d);
     ctx->launches++;
     prof_end(ctx, st, pe_, "kb_split_bfs_big");
   }
@@ -901,29 +929,16 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
 // whose body is one iteration (kb_fill_phase x 4, kb_fill_compact, added as kernel
 // nodes); kb_fill_compact's last block sets the condition.  Built once per (table,
 // size).
-int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
-  auto key = std::make_pair((const Slot*)L.d, L.B);
-  auto it = ctx->fill_graphs.find(key);
-  if (it != ctx->fill_graphs.end()) { *out = it->second.exec; return STSPIX_OK; }
-  std::lock_guard<std::mutex> lk(g_device_mu);
-  cudaGraph_t g = nullptr;
-  CK(cudaGraphCreate(&g, 0));
-  cudaGraphConditionalHandle cond;
-  CK(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
-  cudaGraphNodeParams np = {};
-  np.type = cudaGraphNodeTypeConditional;
-  np.conditional.handle = cond;
-  np.conditional.type = cudaGraphCondTypeWhile;
-  np.conditional.size = 1;
-  cudaGraphNode_t node;
-  CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
-  cudaGraph_t body = np.conditional.phGraph_out[0];
-  // the body: border -> phase 0..3 -> compact -> step, as a chain of kernel nodes
+// The loop body's kernel nodes (four parity phases, then the compaction, whose last
+// block sets `cond`) into graph `body`.
+cudaError_t add_fill_body(stspix_ctx* ctx, cudaGraph_t body, const List& L,
+                          cudaGraphConditionalHandle cond) {
   const unsigned G = (unsigned)std::max(8, std::min(128, 2048 / std::max(L.B, 1)));
   const dim3 grid(G, (unsigned)L.B);
   Slot* table = L.d;
   int B = L.B, break_iter = kFillBreakIter;
   int ph_arg[4] = {0, 1, 2, 3};
+  unsigned* ctr = (unsigned*)(ctx->body_iters + 1);
   cudaGraphNode_t prev = nullptr;
   cudaError_t ce = cudaSuccess;
   auto add = [&](const void* fn, dim3 gd, dim3 bd, void** args) {
@@ -944,10 +959,41 @@ int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
     a_ph[ph][1] = (void*)&ph_arg[ph];
     add((const void*)kb_fill_phase, grid, dim3(kThreads), a_ph[ph]);
   }
-  unsigned* ctr = (unsigned*)(ctx->body_iters + 1);
   void* a_compact[] = {(void*)&table, (void*)&B, (void*)&cond, (void*)&break_iter,
                        (void*)&ctx->body_iters, (void*)&ctr};
   add((const void*)kb_fill_compact, grid, dim3(kThreads), a_compact);
+  return ce;
+}
+
+// A conditional WHILE node (cond set to 1 at each launch of the enclosing graph) in
+// graph g after deps; its body graph is returned in *body.
+cudaError_t add_fill_loop(cudaGraph_t g, const cudaGraphNode_t* deps, const cudaGraphEdgeData* ed,
+                          size_t nd, cudaGraphConditionalHandle* cond, cudaGraphNode_t* node,
+                          cudaGraph_t* body) {
+  cudaError_t ce = cudaGraphConditionalHandleCreate(cond, g, 1, cudaGraphCondAssignDefault);
+  if (ce != cudaSuccess) return ce;
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = *cond;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  ce = cudaGraphAddNode(node, g, deps, ed, nd, &np);
+  if (ce == cudaSuccess) *body = np.conditional.phGraph_out[0];
+  return ce;
+}
+
+int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
+  auto key = std::make_pair((const Slot*)L.d, L.B);
+  auto it = ctx->fill_graphs.find(key);
+  if (it != ctx->fill_graphs.end()) { *out = it->second.exec; return STSPIX_OK; }
+  std::lock_guard<std::mutex> lk(g_device_mu);
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle cond;
+  cudaGraphNode_t node;
+  cudaGraph_t body;
+  cudaError_t ce = add_fill_loop(g, nullptr, nullptr, 0, &cond, &node, &body);
+  if (ce == cudaSuccess) ce = add_fill_body(ctx, body, L, cond);
   if (ce != cudaSuccess) {
     cudaGraphDestroy(g);
     return fail(ctx, STSPIX_ERR_CUDA, "fill graph construction failed: %s", cudaGetErrorString(ce));
@@ -964,13 +1010,30 @@ int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
 }
 
 int run_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
-  cudaGraphExec_t exec;
-  int r = fill_graph(ctx, L, &exec);
-  if (r) return r;
   LAUNCHS(kb_fill_begin, L, L.B);
   // the first iteration's border flags (later ones come with the compaction)
   const unsigned G = (unsigned)std::max(8, std::min(128, 2048 / std::max(L.B, 1)));
   LAUNCHG(kb_fill_border, dim3(G, (unsigned)L.B), kThreads, L.d);
+  if (ctx->capturing) {
+    // inside a batch capture: the loop node goes into the graph being captured
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* ed = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, &ed, &nd));
+    cudaGraphConditionalHandle cond;
+    cudaGraphNode_t node;
+    cudaGraph_t body;
+    CK(add_fill_loop(cg, deps, ed, nd, &cond, &node, &body));
+    CK(add_fill_body(ctx, body, L, cond));
+    CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                           cudaStreamSetCaptureDependencies));
+    return STSPIX_OK;
+  }
+  cudaGraphExec_t exec;
+  int r = fill_graph(ctx, L, &exec);
+  if (r) return r;
   cudaEvent_t pe = prof_begin(ctx, st);
   CK(cudaGraphLaunch(exec, st));
   prof_end(ctx, st, pe, "kb_fill_graph");
@@ -1040,9 +1103,46 @@ struct BatchOut {
   std::vector<stspix_frame_log> log;
 };
 
+// A batch's work from the table uploads to the parameter read-out, for the case with
+// known iteration counts and no partial stop (eager, or recorded into a graph).
+int batch_body(stspix_ctx* ctx, cudaStream_t st, int stages, const List& La, const List& Lb,
+               const List& Lp, const List& Ls, bool ls_own, const std::vector<int>& nit_sorted,
+               const stspix_config& cfg) {
+  int r;
+  if ((r = upload(ctx, st, La, 0)) || (r = upload(ctx, st, Lb, 1)) || (r = upload(ctx, st, Lp, 2)))
+    return r;
+  if (ls_own && (r = upload(ctx, st, Ls, 3))) return r;
+  ctx->cur_fam = STSPIX_FAM_OTHER;
+  LAUNCHS(kb_scalars, La, La.B, (int)kOpBegin);
+  if ((stages & kStageShift) && (r = shift_fill(ctx, st, Lp))) return r;
+  if ((r = bass_init(ctx, st, Lb))) return r;
+  if ((r = prop_init(ctx, st, Lp))) return r;
+  const SmConsts K = sm_constants(cfg);
+  if ((r = bass_loop(ctx, st, Ls, nit_sorted, cfg, K, -1, 0))) return r;
+  if ((r = compact(ctx, st, Ls))) return r;
+  LAUNCHB(kb_read_params, Ls.max_cap, Ls, Ls.B);
+  LAUNCHB(kb_save_prev, Ls.max_npix, Ls, Ls.B);
+  return STSPIX_OK;
+}
+
+// The key of a batch step's launch sequence: everything that sets a launch's grid or
+// arguments (the slot records themselves are uploaded by the graph's copy nodes).
+std::string batch_signature(const std::vector<FrameDesc>& fr, const std::vector<int>& caps,
+                            const std::vector<int>& nit, int stages, const stspix_config& cfg) {
+  std::string k((const char*)&cfg, sizeof cfg);
+  k.append((const char*)&stages, sizeof stages);
+  for (size_t i = 0; i < fr.size(); i++) {
+    const int v[7] = {fr[i].slot, fr[i].mode, fr[i].H, fr[i].W, fr[i].sp_size, caps[i], nit[i]};
+    k.append((const char*)v, sizeof v);
+  }
+  return k;
+}
+
 // The batch runner.  stages: kStageShift and/or kStageSeg.  Frames are processed
 // in workspace positions f.slot (distinct).  Returns a call-level error; per-frame
-// statuses land in out.
+// statuses land in out.  A batch step whose signature was seen before runs as a
+// CUDA graph: captured on the second occurrence (the first ran eagerly and tuned
+// the sweeps), replayed from then on.
 int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
               const stspix_config& cfg, int stages, BatchOut& out, int stop_after = -1,
               int extra_update = 0) {
@@ -1064,23 +1164,10 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
   List La = make_list(ctx, 0, all);
   List Lb = make_list(ctx, 1, bass);
   List Lp = make_list(ctx, 2, prop);
-  if ((r = upload(ctx, st, La, 0)) || (r = upload(ctx, st, Lb, 1)) || (r = upload(ctx, st, Lp, 2)))
-    return r;
-  ctx->cur_fam = STSPIX_FAM_OTHER;
-  LAUNCHS(kb_scalars, La, B, (int)kOpBegin);
-  if ((stages & kStageShift) && (r = shift_fill(ctx, st, Lp))) return r;
   out.nspix.assign(B, 0);
   out.niters.assign(B, 0);
   out.status.assign(B, 0);
   out.log.assign(B, stspix_frame_log{});
-  if (!(stages & kStageSeg)) {
-    if ((r = read_scalars(ctx, st, B))) return r;
-    for (int i = 0; i < B; i++) {
-      out.status[i] = ctx->sc_host[i].status;
-      fill_log(out.log[i], ctx->sc_host[i], 0);
-    }
-    return STSPIX_OK;
-  }
   // iteration counts: BASS frames cfg.niters; propagated frames the explicit count,
   // cfg.prop_niters, or the 4/8/12 ladder on the hole fraction (pyapi.cu:143-146)
   std::vector<int> nit(B, -1);
@@ -1090,6 +1177,93 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     else if (fr[i].niters >= 0) nit[i] = fr[i].niters;
     else if (cfg.prop_niters > 0) nit[i] = cfg.prop_niters;
     else need_ladder = true;
+  }
+  auto finish = [&]() -> int {
+    int rr;
+    if ((rr = read_scalars(ctx, st, B))) return rr;
+    for (int i = 0; i < B; i++) {
+      const Scalars& sc = ctx->sc_host[i];
+      out.nspix[i] = sc.nspix;
+      out.niters[i] = nit[i];
+      out.status[i] = sc.status;
+      fill_log(out.log[i], sc, nit[i]);
+    }
+    return STSPIX_OK;
+  };
+  // the loop table: slots sorted by iteration count, descending (stable)
+  auto sort_table = [&](std::vector<int>& nit_sorted, bool* own) {
+    std::vector<int> order(B);
+    for (int i = 0; i < B; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nit[a] > nit[b]; });
+    std::vector<Slot> sorted;
+    for (int i : order) { sorted.push_back(all[i]); nit_sorted.push_back(nit[i]); }
+    *own = !std::is_sorted(order.begin(), order.end());
+    return *own ? make_list(ctx, 3, sorted) : La;
+  };
+  if ((stages & kStageSeg) && !need_ladder && stop_after < 0 && !ctx->prof_on) {
+    std::vector<int> nit_sorted;
+    bool own = false;
+    const List Ls = sort_table(nit_sorted, &own);
+    const std::string key = batch_signature(fr, caps, nit, stages, cfg);
+    auto g = ctx->batch_graphs.find(key);
+    cudaStreamCaptureStatus outer = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &outer));   // a caller's own capture records the eager step
+    if (outer != cudaStreamCaptureStatusNone) g = ctx->batch_graphs.end();
+    else if (g == ctx->batch_graphs.end() && ctx->batch_seen[key]++ > 0 && ctx->batch_graphs.size() < 64) {
+      // second occurrence: record the step into a graph (the legacy default stream
+      // cannot be captured: record on the context's own stream then; nothing runs
+      // during a capture, and the graph is launched on the caller's stream)
+      std::lock_guard<std::mutex> lk(g_device_mu);
+      cudaStream_t cst = st;
+      if (st == nullptr || st == cudaStreamLegacy) {
+        if (!ctx->cap_stream) CK(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+        cst = ctx->cap_stream;
+      }
+      const long long l0 = ctx->launches;
+      cudaError_t ce = cudaStreamBeginCapture(cst, cudaStreamCaptureModeThreadLocal);
+      cudaGraph_t graph = nullptr;
+      if (ce == cudaSuccess) {
+        ctx->capturing = true;
+        r = batch_body(ctx, cst, stages, La, Lb, Lp, Ls, own, nit_sorted, cfg);
+        ctx->capturing = false;
+        ce = cudaStreamEndCapture(cst, &graph);
+      }
+      cudaGraphExec_t exec = nullptr;
+      cudaError_t ie = cudaErrorUnknown;
+      if (!r && ce == cudaSuccess) ie = cudaGraphInstantiate(&exec, graph, 0);
+      const long long nl = ctx->launches - l0;
+      ctx->launches = l0;
+      if (!r && ce == cudaSuccess && ie == cudaSuccess) {
+        g = ctx->batch_graphs.emplace(key, stspix_ctx::BatchGraph{graph, exec, nl}).first;
+      } else {
+        // nothing recorded ran: clear the capture error and run this step eagerly;
+        // the signature is not captured again
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        ctx->batch_seen[key] = -(1 << 30);
+      }
+    }
+    if (g != ctx->batch_graphs.end()) {
+      CK(cudaGraphLaunch(g->second.exec, st));
+      ctx->launches += g->second.launches;
+      ctx->graph_replays++;
+    } else if ((r = batch_body(ctx, st, stages, La, Lb, Lp, Ls, own, nit_sorted, cfg))) {
+      return r;
+    }
+    return finish();
+  }
+  if ((r = upload(ctx, st, La, 0)) || (r = upload(ctx, st, Lb, 1)) || (r = upload(ctx, st, Lp, 2)))
+    return r;
+  ctx->cur_fam = STSPIX_FAM_OTHER;
+  LAUNCHS(kb_scalars, La, B, (int)kOpBegin);
+  if ((stages & kStageShift) && (r = shift_fill(ctx, st, Lp))) return r;
+  if (!(stages & kStageSeg)) {
+    if ((r = read_scalars(ctx, st, B))) return r;
+    for (int i = 0; i < B; i++) {
+      out.status[i] = ctx->sc_host[i].status;
+      fill_log(out.log[i], ctx->sc_host[i], 0);
+    }
+    return STSPIX_OK;
   }
   if ((r = bass_init(ctx, st, Lb))) return r;
   if (need_ladder) {
@@ -1102,18 +1276,10 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     }
   }
   if ((r = prop_init(ctx, st, Lp))) return r;
-  // the loop table: slots sorted by iteration count, descending (stable)
-  std::vector<int> order(B);
-  for (int i = 0; i < B; i++) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nit[a] > nit[b]; });
-  std::vector<Slot> sorted;
   std::vector<int> nit_sorted;
-  for (int i : order) { sorted.push_back(all[i]); nit_sorted.push_back(nit[i]); }
-  List Ls = La;
-  if (!std::is_sorted(order.begin(), order.end())) {
-    Ls = make_list(ctx, 3, sorted);
-    if ((r = upload(ctx, st, Ls, 3))) return r;
-  }
+  bool own = false;
+  const List Ls = sort_table(nit_sorted, &own);
+  if (own && (r = upload(ctx, st, Ls, 3))) return r;
   const SmConsts K = sm_constants(cfg);
   if ((r = bass_loop(ctx, st, Ls, nit_sorted, cfg, K, stop_after, extra_update))) return r;
   if (stop_after < 0) {
@@ -1121,15 +1287,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     LAUNCHB(kb_read_params, Ls.max_cap, Ls, Ls.B);
     LAUNCHB(kb_save_prev, Ls.max_npix, Ls, Ls.B);
   }
-  if ((r = read_scalars(ctx, st, B))) return r;
-  for (int i = 0; i < B; i++) {
-    const Scalars& s = ctx->sc_host[i];
-    out.nspix[i] = s.nspix;
-    out.niters[i] = nit[i];
-    out.status[i] = s.status;
-    fill_log(out.log[i], s, nit[i]);
-  }
-  return STSPIX_OK;
+  return finish();
 }
 
 int check_cfg(stspix_ctx* ctx, const stspix_config* cfg) {
@@ -1299,6 +1457,7 @@ int stspix_destroy(stspix_ctx* ctx) {
   for (auto& e : ctx->frame_ev) { ctx->ev_free.push_back(e.a); ctx->ev_free.push_back(e.b); }
   for (auto e : ctx->ev_free) cudaEventDestroy(e);
   for (auto e : ctx->batch_ev) if (e) cudaEventDestroy(e);
+  if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   if (ctx->sc_host) cudaFreeHost(ctx->sc_host);
   if (ctx->h_slots) cudaFreeHost(ctx->h_slots);
   delete ctx;
@@ -1712,6 +1871,8 @@ int stspix_footprint(int H, int W, int sp_size, long long* video_bytes, long lon
 }
 
 double stspix_last_batch_ms(const stspix_ctx* ctx) { return ctx ? ctx->batch_ms : -1.0; }
+
+long long stspix_graph_replays(const stspix_ctx* ctx) { return ctx ? ctx->graph_replays : -1; }
 
 int stspix_rgb2lab(stspix_ctx* ctx, void* stream, const float* rgb, float* lab,
                    long long npix) {

@@ -117,3 +117,28 @@ def test_batch_rejects_same_video_twice():
     with pytest.raises(RuntimeError):
         batch.process_batch(fr, niters=4)
     vs.close()
+
+
+def test_repeated_batch_steps_replay_a_graph_with_the_oracle_labels():
+    """A stream with fixed propagated iterations repeats its batch step: the step is
+    captured as a CUDA graph on its second occurrence and replayed after, with labels
+    equal to the oracle's for every frame."""
+    import torch
+    T = 6
+    kw = dict(niters=8, sm_period=4, prop_niters=6, sp_size=12)
+    v, f, _ = synth.voronoi_video(48, 64, T, 16, 0.03, seed=7, max_shift=2.0)
+    st, ref, _ = O.bist_forward(v, f, O.default_config(**kw), True)
+    assert st == 0
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx = bist_cuda._ctx(torch.device("cuda", 0))
+        r0 = ctx.graph_replays()
+        vs = batch.Video(48, 64)
+        vid, flo = cuda(v), cuda(f)
+        for t in range(T):
+            fr = [batch.Frame(img=vid[t], flow=flo[t - 1] if t else None, video=vs, sp_size=12)]
+            batch.process_batch(fr, **kw)
+            assert fr[0].status == 0
+            np.testing.assert_array_equal(fr[0].labels.cpu().numpy(), ref[t], err_msg=f"frame {t}")
+        vs.close()
+        assert ctx.graph_replays() > r0
