@@ -26,6 +26,7 @@
  *   stspix_sp_pooling          st_spix/sp_pooling.py:10 pooling
  *   stspix_legacy_shift_labels st_spix/csrc/prop/shift_labels.cu:82 run_shift_labels
  *   stspix_legacy_fill_missing st_spix/csrc/prop/fill_missing.cu:317 run_fill_missing
+ *   stspix_legacy_split        st_spix/csrc/prop/bass.cu:389 run_split_py
  *   stspix_legacy_rgb_to_lab   st_spix/csrc/prop/rgb2lab.cu:167 run_rgb_to_lab
  *   stspix_sp_video_pooling    st_spix/csrc/prop/sp_video_pooling.cu:62 sp_video_pooling
  *   stspix_downsampled_video_to_pooled  st_spix/csrc/prop/sp_video_pooling.cu:211
@@ -315,7 +316,7 @@ int stspix_sp_pooling(stspix_ctx* ctx, void* stream, const float* vid, const int
 /* ---- legacy prop_cuda surface ------------------------------------------------------
  * The ops of the older extension st_spix/csrc/prop (bound by pybind_prop.cpp, called by
  * st_spix/prop and st_spix/models/bass.py) whose arithmetic is self-contained; its
- * BASS drivers (bass, prop_bass, refine_missing) map onto stspix_run_bass /
+ * BASS drivers (bass, prop_bass, refine, refine_missing) map onto stspix_run_bass /
  * stspix_run_prop in the Python layer (st_spix_gb300.prop_cuda).
  *
  * shift_labels (prop/shift_labels.cu:82): every pixel of superpixel s moves by
@@ -334,6 +335,16 @@ int stspix_legacy_shift_labels(stspix_ctx* ctx, void* stream, const int32_t* spi
 int stspix_legacy_fill_missing(stspix_ctx* ctx, void* stream, int32_t* spix, const float* centers,
                                int ncenters, const int32_t* missing, int nmissing, int H, int W,
                                int break_iter, int* iters, int* remaining);
+
+/* split (prop/bass.cu:389 run_split_py): one split step of the propagated model on
+ * the labels spix [H,W] with the previous params (n_prev entries): update_params, a
+ * split in direction 2 (direction == 0) or 1 (any other value, the count-parity rule of
+ * prop/split_merge.cu:41-43), update_params, compaction of the new ids.  Output as
+ * stspix_run_prop.  Synchronises the stream.                                          */
+int stspix_legacy_split(stspix_ctx* ctx, void* stream, const float* img, int H, int W,
+                        const stspix_config* cfg, int direction, const int32_t* spix,
+                        const stspix_params* params_prev, int n_prev, int32_t* labels_out,
+                        stspix_params* params_out, int* nspix_out);
 
 /* rgb_to_lab (prop/rgb2lab.cu:167): as stspix_rgb2lab but the first channel is red.   */
 int stspix_legacy_rgb_to_lab(stspix_ctx* ctx, void* stream, const float* rgb, float* lab,

@@ -1109,9 +1109,12 @@ int shift_and_fill(const std::vector<int>& prev, Params& pp, const float* flow, 
 
 // prop.cu:677-865 run_prop (with sparams_io.cu:123-140,353-520 write_params,
 // init_sparams.cu:195-286 mark_active).
+// split_dir > 0: instead of the outer loop, the legacy prop_cuda split step
+// (prop/bass.cu:464-488 run_split_py: update_params, one split in that direction) on
+// the given labels, followed by the loop's closing update_params + store_sample.
 int run_prop(Frame& f, const float* img, int H, int W, const stspix_config& cfg, int niters,
              const std::vector<int>& filled, const std::vector<int>& shifted,
-             const Params& prev, Params* out) {
+             const Params& prev, Params* out, int split_dir = 0) {
   f.H = H; f.W = W; f.npix = H * W; f.img = img; f.cfg = cfg;
   f.status = STSPIX_OK;
   int fill_iters = f.log.fill_iters;
@@ -1158,7 +1161,14 @@ int run_prop(Frame& f, const float* img, int H, int W, const stspix_config& cfg,
   }
   for (int v : f.seg) if (v >= 0 && v < nbuf) { sp.valid[v] = 1; sp.prop[v] = 1; }
   f.max_spix = nspix_prev - 1;
-  bass_loop(f, niters, shifted.data(), true, &prev, nspix_prev, -1, 0);
+  if (split_dir > 0) {
+    update_params(f);
+    run_split(f, split_dir, shifted.data(), true);
+    update_params(f);
+    store_sample_sigma_shape(f);
+  } else {
+    bass_loop(f, niters, shifted.data(), true, &prev, nspix_prev, -1, 0);
+  }
   find_border_end(f.seg.data(), f.border.data(), H, W);
   int n = compactify(f.seg, nspix_prev, &f.sp);
   if (out) read_params(f.sp, n, *out);
@@ -1297,6 +1307,23 @@ int oracle_run_prop(const float* img, int H, int W, const stspix_config* cfg, in
   std::vector<int> fl(filled, filled + (size_t)H * W), sh(shifted, shifted + (size_t)H * W);
   Frame f;
   int n = run_prop(f, img, H, W, *cfg, niters, fl, sh, prev, &out);
+  std::copy(f.seg.begin(), f.seg.end(), labels_out);
+  params_to_c(out, params_out);
+  if (nspix_out) *nspix_out = n;
+  g_last_log = f.log;
+  return f.status;
+}
+
+// prop/bass.cu:389-506 run_split_py: legacy direction 0 splits in direction 2,
+// any other value in direction 1 (the count-parity rule of prop/split_merge.cu:41-43).
+int oracle_legacy_split(const float* img, int H, int W, const stspix_config* cfg, int direction,
+                        const int32_t* spix, const stspix_params* pprev, int n_prev,
+                        int32_t* labels_out, stspix_params* params_out, int* nspix_out) {
+  Params prev, out;
+  params_from_c(pprev, n_prev, prev);
+  std::vector<int> fl(spix, spix + (size_t)H * W);
+  Frame f;
+  int n = run_prop(f, img, H, W, *cfg, 0, fl, fl, prev, &out, direction == 0 ? 2 : 1);
   std::copy(f.seg.begin(), f.seg.end(), labels_out);
   params_to_c(out, params_out);
   if (nspix_out) *nspix_out = n;

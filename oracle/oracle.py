@@ -91,6 +91,9 @@ def lib():
             _lib.oracle_run_prop.argtypes = [P, C.c_int, C.c_int, C.POINTER(Config), C.c_int,
                                              P, P, C.POINTER(ParamsC), C.c_int, P,
                                              C.POINTER(ParamsC), C.POINTER(C.c_int)]
+            _lib.oracle_legacy_split.argtypes = [P, C.c_int, C.c_int, C.POINTER(Config),
+                                                 C.c_int, P, C.POINTER(ParamsC), C.c_int, P,
+                                                 C.POINTER(ParamsC), C.POINTER(C.c_int)]
             _lib.oracle_bist_forward.argtypes = [P, P, C.c_int, C.c_int, C.c_int,
                                                  C.POINTER(Config), C.c_int, P, P]
             _lib.oracle_get_marked_video.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, P]
@@ -213,6 +216,24 @@ def run_prop(img, cfg: Config, niters: int, filled, shifted, params_prev: dict, 
     shifted = np.ascontiguousarray(shifted, np.int32)
     st = lib().oracle_run_prop(_p(img), H, W, C.byref(cfg), niters, _p(filled), _p(shifted),
                                C.byref(pprev), n_prev, _p(lab), C.byref(ps), C.byref(n))
+    out = {name: arrs[name][: n.value * per] for name, _, per in PARAM_FIELDS}
+    return st, lab, out, n.value
+
+
+def legacy_split(img, cfg: Config, direction: int, spix, params_prev: dict, n_prev: int):
+    """prop/bass.cu:389 run_split_py restated on the propagated model: one split step
+    in `direction` on the labels spix with the previous params."""
+    img = np.ascontiguousarray(img, np.float32)
+    H, W = img.shape[:2]
+    cap = 10 * n_prev
+    pprev = params_struct({k: np.ascontiguousarray(v) for k, v in params_prev.items()}, n_prev)
+    arrs = alloc_params(cap)
+    ps = params_struct(arrs, cap)
+    lab = np.zeros((H, W), np.int32)
+    n = C.c_int(0)
+    spix = np.ascontiguousarray(spix, np.int32)
+    st = lib().oracle_legacy_split(_p(img), H, W, C.byref(cfg), int(direction), _p(spix),
+                                   C.byref(pprev), n_prev, _p(lab), C.byref(ps), C.byref(n))
     out = {name: arrs[name][: n.value * per] for name, _, per in PARAM_FIELDS}
     return st, lab, out, n.value
 

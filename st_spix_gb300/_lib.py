@@ -80,7 +80,8 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_label_stats", "stspix_rgb2lab", "stspix_lab2rgb", "stspix_rescale_u8",
            "stspix_video_save", "stspix_video_load", "stspix_evaluate", "stspix_label_range",
            "stspix_count_spix", "stspix_size_variation", "stspix_sp_pooling",
-           "stspix_legacy_shift_labels", "stspix_legacy_fill_missing", "stspix_legacy_rgb_to_lab",
+           "stspix_legacy_shift_labels", "stspix_legacy_fill_missing", "stspix_legacy_split",
+           "stspix_legacy_rgb_to_lab",
            "stspix_sp_video_pooling", "stspix_downsampled_video_to_pooled",
            "stspix_graph_replays"]
 
@@ -153,6 +154,9 @@ def load(build_if_missing: bool = True):
             "stspix_legacy_shift_labels": (I, [P, P, P, P, I, I, I, P, P]),
             "stspix_legacy_fill_missing": (I, [P, P, P, P, I, P, I, I, I, I, C.POINTER(I),
                                                C.POINTER(I)]),
+            "stspix_legacy_split": (I, [P, P, P, I, I, C.POINTER(Config), I, P,
+                                        C.POINTER(ParamsC), I, P, C.POINTER(ParamsC),
+                                        C.POINTER(I)]),
             "stspix_legacy_rgb_to_lab": (I, [P, P, P, P, C.c_longlong]),
             "stspix_sp_video_pooling": (I, [P, P, P, P, I, I, I, I, I, I, P, P, P]),
             "stspix_downsampled_video_to_pooled": (I, [P, P, P, P, I, I, I, I, I, I, P]),

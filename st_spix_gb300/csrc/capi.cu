@@ -891,6 +891,20 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector
   return STSPIX_OK;
 }
 
+// The legacy prop_cuda split (prop/bass.cu:464-488 run_split_py) on the propagated
+// model: update_params, one split step in direction dir, and the outer loop's closing
+// update_params + store_sample.
+int split_only(stspix_ctx* ctx, cudaStream_t st, const List& L, const stspix_config& cfg,
+               const SmConsts& K, int dir) {
+  int r;
+  if ((r = update_params(ctx, st, L, L.B))) return r;
+  if ((r = run_split(ctx, st, L, L.B, K, cfg, dir, dir))) return r;
+  if ((r = update_params(ctx, st, L, L.B))) return r;
+  ctx->cur_fam = STSPIX_FAM_POSTERIOR;
+  LAUNCHB(kb_store_sample, L.max_cap, L, L.B);
+  return STSPIX_OK;
+}
+
 // compactify_new_superpixels (compact_spix.cu:41-89) for ids >= lo, moving params.
 int compact(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   ctx->cur_fam = STSPIX_FAM_OTHER;
@@ -1145,7 +1159,7 @@ std::string batch_signature(const std::vector<FrameDesc>& fr, const std::vector<
 // the sweeps), replayed from then on.
 int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
               const stspix_config& cfg, int stages, BatchOut& out, int stop_after = -1,
-              int extra_update = 0) {
+              int extra_update = 0, int split_dir = 0) {
   const int B = (int)fr.size();
   int r;
   ctx->accumulator = cfg.accumulator;
@@ -1200,7 +1214,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     *own = !std::is_sorted(order.begin(), order.end());
     return *own ? make_list(ctx, 3, sorted) : La;
   };
-  if ((stages & kStageSeg) && !need_ladder && stop_after < 0 && !ctx->prof_on) {
+  if ((stages & kStageSeg) && !need_ladder && stop_after < 0 && !split_dir && !ctx->prof_on) {
     std::vector<int> nit_sorted;
     bool own = false;
     const List Ls = sort_table(nit_sorted, &own);
@@ -1281,7 +1295,11 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
   const List Ls = sort_table(nit_sorted, &own);
   if (own && (r = upload(ctx, st, Ls, 3))) return r;
   const SmConsts K = sm_constants(cfg);
-  if ((r = bass_loop(ctx, st, Ls, nit_sorted, cfg, K, stop_after, extra_update))) return r;
+  if (split_dir) {
+    if ((r = split_only(ctx, st, Ls, cfg, K, split_dir))) return r;
+  } else if ((r = bass_loop(ctx, st, Ls, nit_sorted, cfg, K, stop_after, extra_update))) {
+    return r;
+  }
   if (stop_after < 0) {
     if ((r = compact(ctx, st, Ls))) return r;
     LAUNCHB(kb_read_params, Ls.max_cap, Ls, Ls.B);
@@ -1592,6 +1610,35 @@ int stspix_run_prop(stspix_ctx* ctx, void* stream, const float* img, int H, int 
   if (params_out) f.pout = *params_out;
   BatchOut o;
   if ((r = run_batch(ctx, st, fr, *cfg, kStageSeg, o))) return r;
+  ctx->log = o.log[0];
+  if (nspix_out) *nspix_out = o.nspix[0];
+  if (params_out && params_out->capacity < o.nspix[0])
+    return fail(ctx, STSPIX_ERR_CAPACITY, "params capacity %d < %d superpixels",
+                params_out->capacity, o.nspix[0]);
+  return first_status(ctx, o);
+}
+
+// run_split_py (prop/bass.cu:389-506): legacy direction 0 splits in direction 2, any
+// other value in direction 1 (count parity, prop/split_merge.cu:41-43).
+int stspix_legacy_split(stspix_ctx* ctx, void* stream, const float* img, int H, int W,
+                        const stspix_config* cfg, int direction, const int32_t* spix,
+                        const stspix_params* params_prev, int n_prev, int32_t* labels_out,
+                        stspix_params* params_out, int* nspix_out) {
+  if (!ctx || !img || !spix || !params_prev || !labels_out || n_prev < 1)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  int r;
+  if ((r = check_cfg(ctx, cfg)) || (r = check_size(ctx, H, W))) return r;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(cudaMemcpyAsync(labels_out, spix, sizeof(int) * (size_t)H * W, cudaMemcpyDeviceToDevice, st));
+  std::vector<FrameDesc> fr(1);
+  FrameDesc& f = fr[0];
+  f.img = img; f.H = H; f.W = W; f.sp_size = cfg->sp_size; f.seg = labels_out; f.mode = 1;
+  f.n_prev = n_prev; f.pprev = *params_prev; f.shifted = const_cast<int*>(spix);
+  f.niters = 0;
+  if (params_out) f.pout = *params_out;
+  BatchOut o;
+  if ((r = run_batch(ctx, st, fr, *cfg, kStageSeg, o, -1, 0, direction == 0 ? 2 : 1))) return r;
   ctx->log = o.log[0];
   if (nspix_out) *nspix_out = o.nspix[0];
   if (params_out && params_out->capacity < o.nspix[0])

@@ -7,11 +7,14 @@ the legacy functions assert it).  Two kinds of entries:
   * exact restatements of the legacy kernels (C ABI stspix_legacy_* and the pooling
     entries): shift_labels, fill_missing, find_border, init_spix, rgb_to_lab,
     lab_to_rgb, sp_video_pooling, downsampled_video_to_pooled;
-  * the BASS drivers bass, prop_bass and refine_missing, which run this engine's
-    BASS (run_bass) and propagated BASS (run_prop) -- the algorithm of the newer
-    bist extension -- with the legacy arguments mapped onto its configuration.
-    refine_missing lets every pixel move (the legacy version moves only the missing
-    ones) and returns a zero log.
+  * the BASS drivers bass, prop_bass, refine, refine_missing and split, which run this
+    engine's BASS (run_bass) and propagated BASS (run_prop) -- the algorithm of the
+    newer bist extension -- with the legacy arguments mapped onto its configuration.
+    refine is propagated BASS with split/merge disabled; split is one split step of
+    the propagated model (stspix_legacy_split; the legacy kernel's development-only
+    acceptance score is not restated); refine_missing lets every pixel move (the
+    legacy version moves only the missing ones).  refine and refine_missing return a
+    zero log.
 
 SuperpixelParams carries the legacy 17 tensors.  The engine's appearance model has a
 fixed isotropic variance, so sigma_app / prior_sigma_app hold sigma2_app and
@@ -145,6 +148,40 @@ def refine_missing(img, spix, missing, prior_params, nspix, niters, niters_seg, 
                        0.0, potts, math.log(0.5))
     log = torch.zeros((int(niters), 1), dtype=torch.float64, device=img.device)
     return out, p, log
+
+
+def refine(img, spix, params, niters, niters_seg, sp_size, sigma2_app, potts):
+    """prop/refine.cu:99 run_refine: niters rounds of update_params + update_seg on the
+    labels spix [1,H,W] from params, no split or merge -> (spix, params, log f64
+    [niters,1]); propagated BASS with split/merge disabled."""
+    out, p = prop_bass(img, spix, params, niters, niters_seg, int(niters), sp_size, sigma2_app,
+                       0.0, potts, math.log(0.5))
+    log = torch.zeros((int(niters), 1), dtype=torch.float64, device=img.device)
+    return out, p, log
+
+
+def split(img, spix, params, direction, sp_size, sigma2_app, sigma2_size, alpha_hastings):
+    """prop/bass.cu:389 run_split_py: one split step of the propagated model on the
+    labels spix [1,H,W] with params, in direction 2 (direction == 0) or 1 -> (spix,
+    params)."""
+    frame = _frame(img)
+    _check_input(spix, "spix")
+    if spix.dim() != 3 or spix.shape[0] != 1:
+        raise RuntimeError("spix must be [1,H,W] (batch size 1)")
+    H, W = frame.shape[:2]
+    pe = _engine_params(params)
+    cfg = bist_cuda.make_config(sp_size=int(sp_size), sigma2_app=float(sigma2_app),
+                                sigma2_size=float(sigma2_size), alpha=float(alpha_hastings))
+    out = bist_cuda.SuperpixelParams(10 * pe.n, img.device)
+    lab = torch.zeros((1, H, W), dtype=torch.int32, device=img.device)
+    pprev, ps, n = pe.struct(), out.struct(), C.c_int(0)
+    ctx = _ctx(img.device)
+    ctx.check(ctx.lib.stspix_legacy_split(ctx.handle, _stream(img.device), frame.data_ptr(), H, W,
+                                          C.byref(cfg), int(direction), spix[0].contiguous().data_ptr(),
+                                          C.byref(pprev), pe.n, lab.data_ptr(), C.byref(ps),
+                                          C.byref(n)))
+    out.n = n.value
+    return lab, _legacy_params(out, float(sigma2_app))
 
 
 def init_spix(img, sp_size):

@@ -131,3 +131,78 @@ def test_bass_drivers_run_the_engine():
     out, _, log = prop_cuda.refine_missing(img1[None], spix, None, params, n, 5, 4, 10,
                                            0.009 ** 2, 0.5)
     assert out.shape == (1, 48, 64) and log.shape == (5, 1)
+
+
+def _split_case():
+    """A BASS labelling of a Voronoi frame with every three ids joined (superpixels
+    spanning several colour regions) and the BASS params of the first ids as the
+    previous params."""
+    from oracle import oracle as O
+    from st_spix_gb300 import synth
+    img, _ = synth.voronoi_frame(64, 80, 12, 0.03, seed=3)
+    st, lab0, op0, _ = O.run_bass(img, O.default_config(niters=8, sp_size=16))
+    assert st == 0
+    lab = (lab0 // 3).astype(np.int32)
+    n = int(lab.max()) + 1
+    per = {name: p for name, _, p in O.PARAM_FIELDS}
+    prev = {k: np.ascontiguousarray(v[: n * per[k]]) for k, v in op0.items()}
+    return img, lab, prev, n
+
+
+def test_oracle_split_divides_coarse_superpixels():
+    from oracle import oracle as O
+    img, lab, prev, n = _split_case()
+    outs = []
+    for d in (0, 1):
+        st, out, _, nout = O.legacy_split(img, O.default_config(sp_size=16), d, lab, prev, n)
+        assert st == 0 and nout > n
+        assert out.min() == 0 and out.max() == nout - 1
+        # a split only divides: every new superpixel lies inside one old one
+        for k in range(nout):
+            assert len(np.unique(lab[out == k])) == 1
+        outs.append(out)
+    assert (outs[0] != outs[1]).any()    # the two directions bisect differently
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("direction", [0, 1])
+def test_split_matches_the_oracle(direction):
+    import torch
+    from oracle import oracle as O
+    from st_spix_gb300 import bist_cuda, prop_cuda
+    img, lab, prev, n = _split_case()
+    gp = bist_cuda.SuperpixelParams(n, "cuda")
+    gp.n = n
+    for name, _, _ in bist_cuda.PARAM_FIELDS:
+        getattr(gp, "_" + name).copy_(torch.from_numpy(prev[name].reshape(-1)))
+    params = prop_cuda._legacy_params(gp, 0.009 ** 2)
+    out, p = prop_cuda.split(torch.from_numpy(img)[None].cuda(), torch.from_numpy(lab)[None].cuda(),
+                             params, direction, 16, 0.009 ** 2, 0.0, math.log(0.5))
+    st, ref, rp, rn = O.legacy_split(img, O.default_config(sp_size=16), direction, lab, prev, n)
+    assert st == 0 and rn > n
+    np.testing.assert_array_equal(out[0].cpu().numpy(), ref)
+    assert p.counts.shape[0] == rn
+    np.testing.assert_array_equal(p.counts.cpu().numpy(), rp["counts"])
+    np.testing.assert_allclose(p.mu_shape.cpu().numpy().reshape(-1), rp["mu_shape"],
+                               rtol=1e-12, atol=0)
+
+
+@pytest.mark.gpu
+def test_refine_is_propagated_bass_without_split_merge():
+    import torch
+    from oracle import oracle as O
+    from st_spix_gb300 import bist_cuda, prop_cuda
+    img, lab, prev, n = _split_case()
+    gp = bist_cuda.SuperpixelParams(n, "cuda")
+    gp.n = n
+    for name, _, _ in bist_cuda.PARAM_FIELDS:
+        getattr(gp, "_" + name).copy_(torch.from_numpy(prev[name].reshape(-1)))
+    params = prop_cuda._legacy_params(gp, 0.009 ** 2)
+    out, p, log = prop_cuda.refine(torch.from_numpy(img)[None].cuda(),
+                                   torch.from_numpy(lab)[None].cuda(), params, 6, 4, 16,
+                                   0.009 ** 2, 0.5)
+    st, ref, rp, rn = O.run_prop(img, O.default_config(sp_size=16, sm_start=6), 6, lab, lab,
+                                 prev, n)
+    assert st == 0 and rn <= n and log.shape == (6, 1)
+    np.testing.assert_array_equal(out[0].cpu().numpy(), ref)
+    np.testing.assert_array_equal(p.counts.cpu().numpy(), rp["counts"])
