@@ -689,11 +689,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--streams", type=int, default=None,
-                    help="video streams per GPU (default 16; serve: 256); stream mode: frame "
+                    help="video streams per GPU (default 24; serve: 256); stream mode: frame "
                          "t of every stream of a lane runs as one batch")
-    ap.add_argument("--lanes", type=int, default=2,
+    ap.add_argument("--lanes", type=int, default=None,
                     help="host threads per GPU, each with its own CUDA stream, engine "
-                         "context and share of the streams")
+                         "context and share of the streams (default 3; serve: 2)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="stream",
                     choices=["stream", "serve", "batch", "precision", "image", "latency"],
@@ -713,7 +713,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.streams is None:
-        args.streams = SERVE["streams"] if args.mode == "serve" else 16
+        args.streams = SERVE["streams"] if args.mode == "serve" else 24
+    if args.lanes is None:
+        args.lanes = 2 if args.mode == "serve" else 3
     world, rank, local = dist_setup()
     args.local = local
     if args.impl == "reference":

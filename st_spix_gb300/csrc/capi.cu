@@ -1222,6 +1222,10 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     auto g = ctx->batch_graphs.find(key);
     cudaStreamCaptureStatus outer = cudaStreamCaptureStatusNone;
     CK(cudaStreamIsCapturing(st, &outer));   // a caller's own capture records the eager step
+    // a server whose batch compositions rarely repeat keeps the table of seen
+    // signatures bounded: it restarts counting when it grows large
+    if (g == ctx->batch_graphs.end() && ctx->batch_seen.size() >= 4096 && !ctx->batch_seen.count(key))
+      ctx->batch_seen.clear();
     if (outer != cudaStreamCaptureStatusNone) g = ctx->batch_graphs.end();
     else if (g == ctx->batch_graphs.end() && ctx->batch_seen[key]++ > 0 && ctx->batch_graphs.size() < 64) {
       // second occurrence: record the step into a graph (the legacy default stream
