@@ -711,6 +711,9 @@ def main():
                     help="stream: boundary sweeps per launch (0 autotuned, 1 one, 2 two); "
                          "the labels are the same")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch-graphs", action="store_true",
+                    help="stream: launch every batch step's kernels one by one (ncu lists no "
+                         "kernel of a graph that holds conditional nodes)")
     args = ap.parse_args()
     if args.streams is None:
         args.streams = SERVE["streams"] if args.mode == "serve" else 24
@@ -776,6 +779,7 @@ def main():
         with torch.cuda.stream(cstreams[j]):
             videos.append([batch.Video(w["H"], w["W"], dev) for _ in lanes[j]])
             ctxs.append(bist_cuda._ctx(dev))
+            ctxs[-1].set_batch_graphs(not args.no_batch_graphs)
     batch_ms = [[] for _ in range(NL)]
 
     def video_pass(j, vid, flo, out, record):
@@ -934,6 +938,7 @@ def main():
                    "prop_niters": w["prop_niters"], "sm_period": w["sm_period"],
                    "streams_per_gpu": S, "lanes": NL, "batch_per_lane": B0,
                    "sweep_schedule": args.sweep_schedule,
+                   "batch_graphs": not args.no_batch_graphs,
                    "step": "all %d frames of every stream; frame t of a lane's streams is "
                            "one batch" % T,
                    "parallelism": f"replicas{world}",

@@ -132,6 +132,9 @@ long long   stspix_kernel_launches(const stspix_ctx* ctx);
  * step whose frame sizes, capacities, iteration counts and configuration repeat is
  * captured on its second occurrence and replayed from then on).                    */
 long long   stspix_graph_replays(const stspix_ctx* ctx);
+/* Enable (default) or disable the capture and replay of repeated batch steps; with
+ * them off every step launches its kernels one by one (same results).              */
+int         stspix_set_batch_graphs(stspix_ctx* ctx, int enable);
 /* Copy of the log of the last frame processed by this context (host). */
 int         stspix_get_frame_log(const stspix_ctx* ctx, stspix_frame_log* out);
 

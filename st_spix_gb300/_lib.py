@@ -83,7 +83,7 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_legacy_shift_labels", "stspix_legacy_fill_missing", "stspix_legacy_split",
            "stspix_legacy_rgb_to_lab",
            "stspix_sp_video_pooling", "stspix_downsampled_video_to_pooled",
-           "stspix_graph_replays"]
+           "stspix_graph_replays", "stspix_set_batch_graphs"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -161,6 +161,7 @@ def load(build_if_missing: bool = True):
             "stspix_sp_video_pooling": (I, [P, P, P, P, I, I, I, I, I, I, P, P, P]),
             "stspix_downsampled_video_to_pooled": (I, [P, P, P, P, I, I, I, I, I, I, P]),
             "stspix_graph_replays": (C.c_longlong, [P]),
+            "stspix_set_batch_graphs": (I, [P, I]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -200,6 +201,9 @@ class Context:
 
     def graph_replays(self) -> int:
         return int(self.lib.stspix_graph_replays(self.handle))
+
+    def set_batch_graphs(self, enable: bool) -> None:
+        self.check(self.lib.stspix_set_batch_graphs(self.handle, int(bool(enable))))
 
     def frame_log(self) -> FrameLog:
         lg = FrameLog()

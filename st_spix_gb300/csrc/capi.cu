@@ -139,6 +139,7 @@ struct stspix_ctx {
   // replayed; launches = kernels one replay runs (for the launch counter)
   bool capturing = false;
   cudaStream_t cap_stream = nullptr;   // records graphs for callers on the legacy stream
+  bool graphs_on = true;
   struct BatchGraph { cudaGraph_t g; cudaGraphExec_t exec; long long launches; };
   std::map<std::string, BatchGraph> batch_graphs;
   std::map<std::string, int> batch_seen;
@@ -1214,7 +1215,8 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     *own = !std::is_sorted(order.begin(), order.end());
     return *own ? make_list(ctx, 3, sorted) : La;
   };
-  if ((stages & kStageSeg) && !need_ladder && stop_after < 0 && !split_dir && !ctx->prof_on) {
+  if ((stages & kStageSeg) && !need_ladder && stop_after < 0 && !split_dir && !ctx->prof_on &&
+      ctx->graphs_on) {
     std::vector<int> nit_sorted;
     bool own = false;
     const List Ls = sort_table(nit_sorted, &own);
@@ -1924,6 +1926,12 @@ int stspix_footprint(int H, int W, int sp_size, long long* video_bytes, long lon
 double stspix_last_batch_ms(const stspix_ctx* ctx) { return ctx ? ctx->batch_ms : -1.0; }
 
 long long stspix_graph_replays(const stspix_ctx* ctx) { return ctx ? ctx->graph_replays : -1; }
+
+int stspix_set_batch_graphs(stspix_ctx* ctx, int enable) {
+  if (!ctx) return STSPIX_ERR_ARG;
+  ctx->graphs_on = enable != 0;
+  return STSPIX_OK;
+}
 
 int stspix_rgb2lab(stspix_ctx* ctx, void* stream, const float* rgb, float* lab,
                    long long npix) {

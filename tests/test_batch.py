@@ -142,3 +142,28 @@ def test_repeated_batch_steps_replay_a_graph_with_the_oracle_labels():
             np.testing.assert_array_equal(fr[0].labels.cpu().numpy(), ref[t], err_msg=f"frame {t}")
         vs.close()
         assert ctx.graph_replays() > r0
+
+
+def test_batch_graphs_off_launch_eagerly_with_the_same_labels():
+    T = 5
+    kw = dict(niters=8, sm_period=4, prop_niters=6, sp_size=12)
+    v, f, _ = synth.voronoi_video(48, 64, T, 16, 0.03, seed=8, max_shift=2.0)
+    st, ref, _ = O.bist_forward(v, f, O.default_config(**kw), True)
+    assert st == 0
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx = bist_cuda._ctx(torch.device("cuda", 0))
+        ctx.set_batch_graphs(False)
+        try:
+            r0 = ctx.graph_replays()
+            vs = batch.Video(48, 64)
+            vid, flo = cuda(v), cuda(f)
+            for t in range(T):
+                fr = [batch.Frame(img=vid[t], flow=flo[t - 1] if t else None, video=vs,
+                                  sp_size=12)]
+                batch.process_batch(fr, **kw)
+                np.testing.assert_array_equal(fr[0].labels.cpu().numpy(), ref[t])
+            vs.close()
+            assert ctx.graph_replays() == r0
+        finally:
+            ctx.set_batch_graphs(True)
