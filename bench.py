@@ -824,14 +824,29 @@ def main():
     th = threading.Thread(target=sample_clocks, args=(local, stop, clk_lines), daemon=True)
     th.start()
     l0 = [c.launches() for c in ctxs]
+    g0 = [c.graph_replays() for c in ctxs]
     barrier()
     torch.cuda.synchronize()
+    # device time: one start event, every lane's stream waits on it and records its own
+    # end event after its last batch; the step time is the latest end
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev_end = [torch.cuda.Event(enable_timing=True) for _ in range(NL)]
+    ev0.record()
+    for cs in cstreams:
+        cs.wait_event(ev0)
     t0 = time.perf_counter()
-    run_lanes(lambda j, st: video_pass(j, dvid, dflo, dout, True), args.steps)
+
+    def timed(j, st):
+        video_pass(j, dvid, dflo, dout, True)
+        if st == args.steps - 1:
+            ev_end[j].record(cstreams[j])
+    run_lanes(timed, args.steps)
     torch.cuda.synchronize()
-    elapsed = time.perf_counter() - t0
+    wall = time.perf_counter() - t0
+    elapsed = max(ev0.elapsed_time(e) for e in ev_end) / 1000.0
     barrier()
     total_launches = sum(c.launches() - a for c, a in zip(ctxs, l0))
+    replays = sum(c.graph_replays() - a for c, a in zip(ctxs, g0))
     stop.set()
     th.join(timeout=5)
     elapsed = max_over_ranks(elapsed, world, dev)
@@ -962,6 +977,10 @@ def main():
                 "h2d_bytes_per_step": int(h_bytes),
                 "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in h_out))},
         "gpu_launches": int(total_launches),
+        "graph_replays": int(replays),
+        "timing": "CUDA events (start on the default stream, every lane's stream waits on it; "
+                  "step time = latest lane end); host wall %.1f ms per step" %
+                  (1000 * wall / args.steps),
         "clocks": summarize_clocks(clk_lines),
         "quality": dict({k: qual[k] for k in ("tex", "szv", "ev", "ev3d", "pooling", "ue2d",
                                               "sa2d", "ue3d", "sa3d", "spnum", "ave_nsp")},

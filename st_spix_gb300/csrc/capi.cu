@@ -111,7 +111,7 @@ struct stspix_ctx {
   struct FillGraph { cudaGraph_t g; cudaGraphExec_t exec; };
   std::map<std::pair<const Slot*, int>, FillGraph> fill_graphs;
   // sweep tile autotuner
-  std::map<std::pair<unsigned long long, int>, int> sweep_choice;  // (shape, nb) -> variant
+  std::map<std::pair<unsigned long long, int>, int> sweep_choice;  // (tile class, single forced) -> widths
   cudaEvent_t tune_ev[kSweepVariants + 1] = {};
   long long tunes = 0;
   int accumulator = 0;            // cfg.accumulator of the batch being run
@@ -670,7 +670,9 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   // in quarter octaves: the choice depends on how well the tiles fill the SMs, and
   // mixed serving batches then tune a handful of times.
   const int tl = std::max(1, L.tiles_upto[0][nb]);
-  const auto key = std::make_pair((unsigned long long)std::floor(4.0 * std::log2((double)tl)), 0);
+  // (a forced single-sweep schedule keeps its own entries: its tuning skips the pairs)
+  const auto key = std::make_pair((unsigned long long)std::floor(4.0 * std::log2((double)tl)),
+                                  cfg.sweep_schedule == 1 ? 1 : 0);
   auto ch = ctx->sweep_choice.find(key);
   int done = 0, launch = 0;
   int v1 = 1, v2 = -1;      // best single-sweep width, two-sweep width (-1: none)
@@ -744,7 +746,7 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
       done += 2;
       launch += 1;
     }
-    if (cfg.sweep_schedule == 0) ctx->sweep_choice[key] = v1 | ((v2 + 1) << 8);
+    ctx->sweep_choice[key] = v1 | ((v2 + 1) << 8);
     ctx->tunes++;
     if (done >= nseg) {
       if (launch & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
