@@ -710,6 +710,9 @@ def main():
     ap.add_argument("--sweep-schedule", type=int, default=0, choices=[0, 1, 2],
                     help="stream: boundary sweeps per launch (0 autotuned, 1 one, 2 two); "
                          "the labels are the same")
+    ap.add_argument("--sweep-tile", type=int, default=0, choices=[0, 16, 32, 64],
+                    help="stream: single-sweep tile width (0 autotuned); profiler runs pin "
+                         "the width the autotuner picks without the profiler")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch-graphs", action="store_true",
                     help="stream: launch every batch step's kernels one by one (ncu lists no "
@@ -757,7 +760,7 @@ def main():
     cfg = dict(niters=w["niters"], sp_size=w["sp_size"], potts=w["potts"],
                sigma2_app=w["sigma2_app"], alpha=w["alpha"], split_alpha=w["split_alpha"],
                sm_period=w["sm_period"], prop_niters=w["prop_niters"],
-               sweep_schedule=args.sweep_schedule)
+               sweep_schedule=args.sweep_schedule, sweep_tile=args.sweep_tile)
 
     # one video per stream (seed = rank * S + i), generated on the device; the host
     # copies feed the end-to-end leg
@@ -884,6 +887,8 @@ def main():
         video_pass(0, dvid, dflo, dout, False)
         cstreams[0].synchronize()
         prof = ctxs[0].profile_get()
+        sweep_kernels = {k: v[0] for k, v in ctxs[0].profile_kernels().items()
+                         if k.startswith("kb_sweep")}
         ctxs[0].profile(False)
 
     # ---- e2e through the public API with host buffers --------------------------
@@ -952,7 +957,7 @@ def main():
                    "sp_size": w["sp_size"], "niters": w["niters"],
                    "prop_niters": w["prop_niters"], "sm_period": w["sm_period"],
                    "streams_per_gpu": S, "lanes": NL, "batch_per_lane": B0,
-                   "sweep_schedule": args.sweep_schedule,
+                   "sweep_schedule": args.sweep_schedule, "sweep_tile": args.sweep_tile,
                    "batch_graphs": not args.no_batch_graphs,
                    "step": "all %d frames of every stream; frame t of a lane's streams is "
                            "one batch" % T,
@@ -971,7 +976,8 @@ def main():
                      "algorithmic_bytes_per_launch": per_launch,
                      "dominant_family": fam,
                      "family_ms": {k: round(v[1], 3) for k, v in prof.items()},
-                     "family_launches": {k: v[0] for k, v in prof.items()}},
+                     "family_launches": {k: v[0] for k, v in prof.items()},
+                     "sweep_kernels_lane0": sweep_kernels},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "frames/s",
                 "h2d_bytes_per_step": int(h_bytes),

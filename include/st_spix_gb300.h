@@ -80,6 +80,8 @@ typedef struct stspix_config {
                             exist for the accumulator precision study               */
   int   sweep_schedule;  /* boundary sweeps per launch: 0 autotuned (default), 1 one,
                             2 two whenever two remain; the labels are the same       */
+  int   sweep_tile;      /* single-sweep tile width: 0 autotuned (default), or 16, 32,
+                            64 (no timing; schedule 0 then runs single sweeps)       */
 } stspix_config;
 
 void stspix_default_config(stspix_config* cfg);

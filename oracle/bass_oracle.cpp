@@ -1232,6 +1232,7 @@ void oracle_default_config(stspix_config* c) {
   c->thresh_relabel = 1e-5f; c->thresh_new = 1e-2f;
   c->accumulator = 0;
   c->sweep_schedule = 0;   // a launch schedule of the engine; the oracle sweeps one by one
+  c->sweep_tile = 0;
 }
 
 int oracle_hex_count(int H, int W, int sp_size) {

@@ -685,6 +685,10 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   if (cfg.sweep_schedule == 2) {
     v1 = 0;
     v2 = 0;
+  } else if (cfg.sweep_tile) {
+    for (int c = 0; c < kSweepVariants; c++)
+      if (kSweepTileW[c] == cfg.sweep_tile) v1 = c;
+    v2 = -1;
   } else if (ch != ctx->sweep_choice.end()) {
     v1 = ch->second & 0xff;
     v2 = cfg.sweep_schedule == 1 ? -1 : (ch->second >> 8) - 1;
@@ -694,20 +698,27 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   } else if (nseg > 0) {
     // the whole call's launch count is known only after tuning; the clear rides on the
     // first launch, the accumulation on the last (decided when it is issued)
+    // Every trial runs kTuneRounds times and keeps its fastest run: other streams of
+    // the device (concurrent lanes) only ever slow a run down.
     const bool fuse_ok = fuse_stats && nseg >= 2;
-    CK(cudaEventRecord(ctx->tune_ev[0], st));
-    for (int c = 0; c < kSweepVariants; c++) {
-      sweep1(c, 0, 0, fuse_ok ? 1 : 0);
-      CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
+    float t1[kSweepVariants];
+    for (int r = 0; r < kTuneRounds; r++) {
+      CK(cudaEventRecord(ctx->tune_ev[0], st));
+      for (int c = 0; c < kSweepVariants; c++) {
+        sweep1(c, 0, 0, fuse_ok ? 1 : 0);
+        CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
+      }
+      CK(cudaEventSynchronize(ctx->tune_ev[kSweepVariants]));
+      for (int c = 0; c < kSweepVariants; c++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->tune_ev[c], ctx->tune_ev[c + 1]);
+        t1[c] = r == 0 ? ms : std::min(t1[c], ms);
+      }
     }
-    CK(cudaEventSynchronize(ctx->tune_ev[kSweepVariants]));
-    float best1 = 0.f;
+    float best1 = t1[0];
     v1 = 0;
-    for (int c = 0; c < kSweepVariants; c++) {
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, ctx->tune_ev[c], ctx->tune_ev[c + 1]);
-      if (c == 0 || ms < best1) { best1 = ms; v1 = c; }
-    }
+    for (int c = 1; c < kSweepVariants; c++)
+      if (t1[c] < best1) { best1 = t1[c]; v1 = c; }
     done = 1;
     launch = 1;
     if (nseg >= 3 && cfg.sweep_schedule == 0) {
@@ -716,32 +727,39 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
       // the third and fourth, and the pair is compared with that sweep plus a full one
       float ref = 2.f * best1;
       if (nseg >= 4) {
-        CK(cudaEventRecord(ctx->tune_ev[0], st));
-        sweep1(v1, launch & 1, 1, 0);
-        CK(cudaEventRecord(ctx->tune_ev[1], st));
-        CK(cudaEventSynchronize(ctx->tune_ev[1]));
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->tune_ev[0], ctx->tune_ev[1]);
-        ref = best1 + ms;
+        float ms1 = 0.f;
+        for (int r = 0; r < kTuneRounds; r++) {
+          CK(cudaEventRecord(ctx->tune_ev[0], st));
+          sweep1(v1, launch & 1, 1, 0);
+          CK(cudaEventRecord(ctx->tune_ev[1], st));
+          CK(cudaEventSynchronize(ctx->tune_ev[1]));
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, ctx->tune_ev[0], ctx->tune_ev[1]);
+          ms1 = r == 0 ? ms : std::min(ms1, ms);
+        }
+        ref = best1 + ms1;
         done = 2;
         launch = 2;
       }
       // (both pair runs write the same labels; neither adds statistics, which would
       // count them twice: when the pair ends the call the next update_params accumulates)
       const int pv[2] = {0, 2};
-      float best2 = 0.f;
-      int b2 = 0;
-      CK(cudaEventRecord(ctx->tune_ev[0], st));
-      for (int c = 0; c < 2; c++) {
-        sweep2(pv[c], launch & 1, 1, 0);
-        CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
+      float t2[2];
+      for (int r = 0; r < kTuneRounds; r++) {
+        CK(cudaEventRecord(ctx->tune_ev[0], st));
+        for (int c = 0; c < 2; c++) {
+          sweep2(pv[c], launch & 1, 1, 0);
+          CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
+        }
+        CK(cudaEventSynchronize(ctx->tune_ev[2]));
+        for (int c = 0; c < 2; c++) {
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, ctx->tune_ev[c], ctx->tune_ev[c + 1]);
+          t2[c] = r == 0 ? ms : std::min(t2[c], ms);
+        }
       }
-      CK(cudaEventSynchronize(ctx->tune_ev[2]));
-      for (int c = 0; c < 2; c++) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->tune_ev[c], ctx->tune_ev[c + 1]);
-        if (c == 0 || ms < best2) { best2 = ms; b2 = pv[c]; }
-      }
+      const float best2 = std::min(t2[0], t2[1]);
+      const int b2 = t2[1] < t2[0] ? pv[1] : pv[0];
       v2 = best2 < ref ? b2 : -1;
       done += 2;
       launch += 1;
@@ -1322,6 +1340,8 @@ int check_cfg(stspix_ctx* ctx, const stspix_config* cfg) {
     return fail(ctx, STSPIX_ERR_ARG, "accumulator must be 0, 1 or 2");
   if (cfg->sweep_schedule < 0 || cfg->sweep_schedule > 2)
     return fail(ctx, STSPIX_ERR_ARG, "sweep_schedule must be 0, 1 or 2");
+  if (cfg->sweep_tile != 0 && cfg->sweep_tile != 16 && cfg->sweep_tile != 32 && cfg->sweep_tile != 64)
+    return fail(ctx, STSPIX_ERR_ARG, "sweep_tile must be 0, 16, 32 or 64");
   if (cfg->sp_size < 1) return fail(ctx, STSPIX_ERR_ARG, "sp_size must be >= 1");
   if (cfg->niters < 0 || cfg->niters_seg < 0)
     return fail(ctx, STSPIX_ERR_ARG, "iteration counts must be >= 0");
@@ -1428,6 +1448,7 @@ void stspix_default_config(stspix_config* c) {
   c->thresh_relabel = 1e-5f; c->thresh_new = 1e-2f;
   c->accumulator = 0;
   c->sweep_schedule = 0;
+  c->sweep_tile = 0;
 }
 
 int stspix_version(void) { return 2; }

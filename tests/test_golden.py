@@ -80,3 +80,22 @@ def test_gpu_sweep_schedules_match_oracle(schedule, niters_seg):
                                      niters_seg=niters_seg, sweep_schedule=schedule)
         torch.cuda.current_stream().synchronize()
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tile", [16, 32, 64])
+def test_gpu_forced_sweep_tile_matches_oracle(tile):
+    """A forced single-sweep tile width (no autotuning) gives the oracle's labels."""
+    import torch
+    from st_spix_gb300 import bist_cuda
+    g = load("bist_video_48x64x3.npz")
+    st, ref, _ = O.bist_forward(g["vid"], g["flows"], O.default_config(niters=int(g["niters"])),
+                                True)
+    assert st == 0
+    with torch.cuda.stream(torch.cuda.Stream()):
+        out = bist_cuda.bist_forward(torch.from_numpy(g["vid"]).cuda(),
+                                     torch.from_numpy(g["flows"]).cuda(), int(g["niters"]), 15,
+                                     0.5, 0.009 ** 2, float(np.log(0.5)), 0.0, True, False,
+                                     sweep_tile=tile)
+        torch.cuda.current_stream().synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
