@@ -785,15 +785,20 @@ def main():
             ctxs[-1].set_batch_graphs(not args.no_batch_graphs)
     batch_ms = [[] for _ in range(NL)]
 
-    def video_pass(j, vid, flo, out, record):
-        """All T frames of lane j's streams: frame t of every stream in one batch."""
+    def video_pass(j, vid, flo, out, record, before=None, after=None):
+        """All T frames of lane j's streams: frame t of every stream in one batch
+        (before(t) / after(t): hooks around batch t)."""
         for v in videos[j]:
             v.reset()
         for t in range(T):
+            if before:
+                before(t)
             fr = [batch.Frame(img=vid[i][t], flow=flo[i][t - 1] if t > 0 else None,
                               video=videos[j][k], labels=out[i][t])
                   for k, i in enumerate(lanes[j])]
             batch.process_batch(fr, **cfg)
+            if after:
+                after(t)
             if record:
                 batch_ms[j].append(ctxs[j].last_batch_ms())
 
@@ -898,13 +903,35 @@ def main():
     e_vid = [torch.empty_like(v) for v in dvid]
     e_flo = [torch.empty_like(f) for f in dflo]
 
+    # frames stream in: every frame's host->device copy is queued on the lane's copy-in
+    # stream ahead of the batches, batch t waits for frame t only, and frame t's labels
+    # go back on the copy-out stream while later batches run
+    in_streams = [torch.cuda.Stream(dev) for _ in range(NL)]
+    out_streams = [torch.cuda.Stream(dev) for _ in range(NL)]
+
     def e2e(j, st):
-        for i in lanes[j]:
-            e_vid[i].copy_(h_vid[i], non_blocking=True)
-            e_flo[i].copy_(h_flo[i], non_blocking=True)
-        video_pass(j, e_vid, e_flo, dout, False)
-        for i in lanes[j]:
-            h_out[i].copy_(dout[i], non_blocking=True)
+        ev_in = [torch.cuda.Event() for _ in range(T)]
+        with torch.cuda.stream(in_streams[j]):
+            in_streams[j].wait_stream(cstreams[j])     # the previous step's reads are done
+            for t in range(T):
+                for i in lanes[j]:
+                    e_vid[i][t].copy_(h_vid[i][t], non_blocking=True)
+                    if t < T - 1:
+                        e_flo[i][t].copy_(h_flo[i][t], non_blocking=True)
+                ev_in[t].record(in_streams[j])
+
+        def before(t):
+            cstreams[j].wait_event(ev_in[t])
+
+        def after(t):
+            ev = torch.cuda.Event()
+            ev.record(cstreams[j])
+            out_streams[j].wait_event(ev)
+            with torch.cuda.stream(out_streams[j]):
+                for i in lanes[j]:
+                    h_out[i][t].copy_(dout[i][t], non_blocking=True)
+        video_pass(j, e_vid, e_flo, dout, False, before, after)
+        out_streams[j].synchronize()
         cstreams[j].synchronize()
 
     barrier()
