@@ -844,11 +844,15 @@ def main():
         cs.wait_event(ev0)
     t0 = time.perf_counter()
 
+    lane_done = [0.0] * NL
+
     def timed(j, st):
         video_pass(j, dvid, dflo, dout, True)
         if st == args.steps - 1:
             ev_end[j].record(cstreams[j])
+            lane_done[j] = time.perf_counter() - t0
     run_lanes(timed, args.steps)
+    t_joined = time.perf_counter() - t0
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     elapsed = max(ev0.elapsed_time(e) for e in ev_end) / 1000.0
@@ -1012,8 +1016,9 @@ def main():
         "gpu_launches": int(total_launches),
         "graph_replays": int(replays),
         "timing": "CUDA events (start on the default stream, every lane's stream waits on it; "
-                  "step time = latest lane end); host wall %.1f ms per step" %
-                  (1000 * wall / args.steps),
+                  "step time = latest lane end); host wall %.1f ms per step (last lane "
+                  "done %.1f ms, threads joined %.1f ms after the start, %d steps)" %
+                  (1000 * wall / args.steps, 1000 * max(lane_done), 1000 * t_joined, args.steps),
         "clocks": summarize_clocks(clk_lines),
         "quality": dict({k: qual[k] for k in ("tex", "szv", "ev", "ev3d", "pooling", "ue2d",
                                               "sa2d", "ue3d", "sa3d", "spnum", "ave_nsp")},
