@@ -1015,6 +1015,7 @@ def main():
                 "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in h_out))},
         "gpu_launches": int(total_launches),
         "graph_replays": int(replays),
+        "sweep_choices": [c.sweep_choices() for c in ctxs],
         "timing": "CUDA events (start on the default stream, every lane's stream waits on it; "
                   "step time = latest lane end); host wall %.1f ms per step (last lane "
                   "done %.1f ms, threads joined %.1f ms after the start, %d steps)" %

@@ -80,8 +80,9 @@ typedef struct stspix_config {
                             exist for the accumulator precision study               */
   int   sweep_schedule;  /* boundary sweeps per launch: 0 autotuned (default), 1 one,
                             2 two whenever two remain; the labels are the same       */
-  int   sweep_tile;      /* single-sweep tile width: 0 autotuned (default), or 16, 32,
-                            64 (no timing; schedule 0 then runs single sweeps)       */
+  int   sweep_tile;      /* tile width: 0 autotuned (default), or 16, 32, 64 (no
+                            timing; schedules 0 and 1 then run single sweeps of that
+                            width, schedule 2 two-sweep launches of that width)      */
 } stspix_config;
 
 void stspix_default_config(stspix_config* cfg);
@@ -134,6 +135,11 @@ long long   stspix_kernel_launches(const stspix_ctx* ctx);
  * step whose frame sizes, capacities, iteration counts and configuration repeat is
  * captured on its second occurrence and replayed from then on).                    */
 long long   stspix_graph_replays(const stspix_ctx* ctx);
+/* The sweep autotuner's choices, entry idx (0..): *tiles_class = the batch's 32x32 tile
+ * count class (4 log2 tiles), *single_w = the single-sweep tile width, *pair_w = the
+ * two-sweep width (0: single sweeps only).  Returns 1 while idx is an entry, else 0.  */
+int         stspix_sweep_choice(const stspix_ctx* ctx, int idx, int* tiles_class, int* single_w,
+                                int* pair_w);
 /* Enable (default) or disable the capture and replay of repeated batch steps; with
  * them off every step launches its kernels one by one (same results).              */
 int         stspix_set_batch_graphs(stspix_ctx* ctx, int enable);

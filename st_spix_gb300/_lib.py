@@ -84,7 +84,7 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_legacy_shift_labels", "stspix_legacy_fill_missing", "stspix_legacy_split",
            "stspix_legacy_rgb_to_lab",
            "stspix_sp_video_pooling", "stspix_downsampled_video_to_pooled",
-           "stspix_graph_replays", "stspix_set_batch_graphs"]
+           "stspix_graph_replays", "stspix_set_batch_graphs", "stspix_sweep_choice"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
 
@@ -163,6 +163,7 @@ def load(build_if_missing: bool = True):
             "stspix_downsampled_video_to_pooled": (I, [P, P, P, P, I, I, I, I, I, I, P]),
             "stspix_graph_replays": (C.c_longlong, [P]),
             "stspix_set_batch_graphs": (I, [P, I]),
+            "stspix_sweep_choice": (I, [P, I, C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -202,6 +203,15 @@ class Context:
 
     def graph_replays(self) -> int:
         return int(self.lib.stspix_graph_replays(self.handle))
+
+    def sweep_choices(self) -> list:
+        """The autotuner's (tile-count class, single width, pair width or 0) entries."""
+        out, i = [], 0
+        a, b, c = C.c_int(0), C.c_int(0), C.c_int(0)
+        while self.lib.stspix_sweep_choice(self.handle, i, C.byref(a), C.byref(b), C.byref(c)):
+            out.append((a.value, b.value, c.value))
+            i += 1
+        return out
 
     def set_batch_graphs(self, enable: bool) -> None:
         self.check(self.lib.stspix_set_batch_graphs(self.handle, int(bool(enable))))

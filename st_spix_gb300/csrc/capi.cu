@@ -410,6 +410,7 @@ void preload_kernels() {
       (const void*)kb_sweep_t16,
       (const void*)kb_sweep2_t32,
       (const void*)kb_sweep2_t16,
+      (const void*)kb_sweep2_t64,
       (const void*)kb_copy_labels,
       (const void*)kb_read_params,
       (const void*)kb_save_prev,
@@ -654,10 +655,12 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
     else
       LAUNCHG(kb_sweep_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
   };
-  auto sweep2 = [&](int v, int parity, int mode, int stats) {   // v: 0 (32 wide) or 2 (16)
+  auto sweep2 = [&](int v, int parity, int mode, int stats) {   // v: 0 (32 wide), 1 (64), 2 (16)
     const unsigned g = (unsigned)std::max(1, L.tiles_upto[v][nb]);
     if (v == 2)
       LAUNCHG(kb_sweep2_t16, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
+    else if (v == 1)
+      LAUNCHG(kb_sweep2_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
     else
       LAUNCHG(kb_sweep2_t32, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
   };
@@ -682,12 +685,14 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
     for (int it = from; it < nseg; it += (v2_ >= 0 && nseg - it >= 2) ? 2 : 1) n++;
     return n;
   };
+  int forced = -1;     // the width stspix_config.sweep_tile pins
+  for (int c = 0; c < kSweepVariants; c++)
+    if (kSweepTileW[c] == cfg.sweep_tile) forced = c;
   if (cfg.sweep_schedule == 2) {
-    v1 = 0;
-    v2 = 0;
-  } else if (cfg.sweep_tile) {
-    for (int c = 0; c < kSweepVariants; c++)
-      if (kSweepTileW[c] == cfg.sweep_tile) v1 = c;
+    v1 = forced >= 0 ? forced : 0;
+    v2 = v1;
+  } else if (forced >= 0) {
+    v1 = forced;
     v2 = -1;
   } else if (ch != ctx->sweep_choice.end()) {
     v1 = ch->second & 0xff;
@@ -721,7 +726,11 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
       if (t1[c] < best1) { best1 = t1[c]; v1 = c; }
     done = 1;
     launch = 1;
-    if (nseg >= 3 && cfg.sweep_schedule == 0) {
+    // Large batches keep single sweeps: a two-sweep launch holds more registers (4
+    // blocks per SM against 6), which costs more than its timing alone shows once other
+    // lanes' kernels share the SMs (batches of 8 480x854 frames on three lanes: 1532-1535
+    // frames/s when one lane picked 64x32 pairs, 1624-1631 with single sweeps on all).
+    if (nseg >= 3 && cfg.sweep_schedule == 0 && tl < kPairMaxTiles) {
       // a two-sweep launch is an active-set sweep plus a full-listing one: with four or
       // more sweeps the second sweep runs alone (timed, active set) and the pair covers
       // the third and fourth, and the pair is compared with that sweep plus a full one
@@ -743,23 +752,24 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
       }
       // (both pair runs write the same labels; neither adds statistics, which would
       // count them twice: when the pair ends the call the next update_params accumulates)
-      const int pv[2] = {0, 2};
-      float t2[2];
+      float t2[kSweepVariants];
       for (int r = 0; r < kTuneRounds; r++) {
         CK(cudaEventRecord(ctx->tune_ev[0], st));
-        for (int c = 0; c < 2; c++) {
-          sweep2(pv[c], launch & 1, 1, 0);
+        for (int c = 0; c < kSweepVariants; c++) {
+          sweep2(c, launch & 1, 1, 0);
           CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
         }
-        CK(cudaEventSynchronize(ctx->tune_ev[2]));
-        for (int c = 0; c < 2; c++) {
+        CK(cudaEventSynchronize(ctx->tune_ev[kSweepVariants]));
+        for (int c = 0; c < kSweepVariants; c++) {
           float ms = 0.f;
           cudaEventElapsedTime(&ms, ctx->tune_ev[c], ctx->tune_ev[c + 1]);
           t2[c] = r == 0 ? ms : std::min(t2[c], ms);
         }
       }
-      const float best2 = std::min(t2[0], t2[1]);
-      const int b2 = t2[1] < t2[0] ? pv[1] : pv[0];
+      float best2 = t2[0];
+      int b2 = 0;
+      for (int c = 1; c < kSweepVariants; c++)
+        if (t2[c] < best2) { best2 = t2[c]; b2 = c; }
       v2 = best2 < ref ? b2 : -1;
       done += 2;
       launch += 1;
@@ -1949,6 +1959,20 @@ int stspix_footprint(int H, int W, int sp_size, long long* video_bytes, long lon
 double stspix_last_batch_ms(const stspix_ctx* ctx) { return ctx ? ctx->batch_ms : -1.0; }
 
 long long stspix_graph_replays(const stspix_ctx* ctx) { return ctx ? ctx->graph_replays : -1; }
+
+int stspix_sweep_choice(const stspix_ctx* ctx, int idx, int* tiles_class, int* single_w,
+                        int* pair_w) {
+  if (!ctx || idx < 0) return 0;
+  for (const auto& kv : ctx->sweep_choice) {
+    if (kv.first.second != 0 || idx-- > 0) continue;   // autotuned entries only
+    const int v1 = kv.second & 0xff, v2 = (kv.second >> 8) - 1;
+    if (tiles_class) *tiles_class = (int)kv.first.first;
+    if (single_w) *single_w = kSweepTileW[v1];
+    if (pair_w) *pair_w = v2 >= 0 ? kSweepTileW[v2] : 0;
+    return 1;
+  }
+  return 0;
+}
 
 int stspix_set_batch_graphs(stspix_ctx* ctx, int enable) {
   if (!ctx) return STSPIX_ERR_ARG;

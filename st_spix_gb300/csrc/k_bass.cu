@@ -1090,6 +1090,7 @@ STSPIX_SWEEP_KERNEL(kb_sweep_t64, 64, 1, 6)
 STSPIX_SWEEP_KERNEL(kb_sweep_t16, 16, 1, 6)
 STSPIX_SWEEP_KERNEL(kb_sweep2_t32, 32, 2, 4)
 STSPIX_SWEEP_KERNEL(kb_sweep2_t16, 16, 2, 4)
+STSPIX_SWEEP_KERNEL(kb_sweep2_t64, 64, 2, 4)
 #undef STSPIX_SWEEP_KERNEL
 
 // ---------------------------------------------------------------------------

@@ -51,6 +51,8 @@ __global__ void kb_sweep2_t32(const Slot* slots, int B, int parity, float s2, fl
                               int mode, int stats);
 __global__ void kb_sweep2_t16(const Slot* slots, int B, int parity, float s2, float potts,
                               int mode, int stats);
+__global__ void kb_sweep2_t64(const Slot* slots, int B, int parity, float s2, float potts,
+                              int mode, int stats);
 __global__ void kb_copy_labels(const Slot* slots);
 __global__ void kb_read_params(const Slot* slots);
 __global__ void kb_save_prev(const Slot* slots);

@@ -83,9 +83,11 @@ def test_gpu_sweep_schedules_match_oracle(schedule, niters_seg):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("schedule", [1, 2])
 @pytest.mark.parametrize("tile", [16, 32, 64])
-def test_gpu_forced_sweep_tile_matches_oracle(tile):
-    """A forced single-sweep tile width (no autotuning) gives the oracle's labels."""
+def test_gpu_forced_sweep_tile_matches_oracle(tile, schedule):
+    """A forced tile width (no autotuning), one or two sweeps per launch, gives the
+    oracle's labels."""
     import torch
     from st_spix_gb300 import bist_cuda
     g = load("bist_video_48x64x3.npz")
@@ -96,6 +98,6 @@ def test_gpu_forced_sweep_tile_matches_oracle(tile):
         out = bist_cuda.bist_forward(torch.from_numpy(g["vid"]).cuda(),
                                      torch.from_numpy(g["flows"]).cuda(), int(g["niters"]), 15,
                                      0.5, 0.009 ** 2, float(np.log(0.5)), 0.0, True, False,
-                                     sweep_tile=tile)
+                                     sweep_tile=tile, sweep_schedule=schedule)
         torch.cuda.current_stream().synchronize()
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
