@@ -644,13 +644,13 @@ __constant__ unsigned char c_simple_lut[256] = {
     1, 0, 0, 0, 1, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 1,
     0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 1, 1, 0, 0, 1, 1, 0, 0};
 
-__device__ __forceinline__ void joint(const float* __restrict__ pix, int x, int y,
+__device__ __forceinline__ void joint(float c0, float c1, float c2, int x, int y,
                                       const SweepRec& r, int k, float s2, float neigh_neq,
                                       float beta, float* best, int* best_label) {
   float res = -1000;
-  const float x0 = pix[0] - r.mu_r;
-  const float x1 = pix[1] - r.mu_g;
-  const float x2 = pix[2] - r.mu_b;
+  const float x0 = c0 - r.mu_r;
+  const float x1 = c1 - r.mu_g;
+  const float x2 = c2 - r.mu_b;
   int d0 = x - r.mxi, d1 = y - r.myi;   // == (int)(x - mu_x), see SweepRec
   if ((r.frac & 1) && d0 >= 1) d0 -= 1;
   if ((r.frac & 2) && d1 >= 1) d1 -= 1;
@@ -828,6 +828,9 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
       const int lxi = bi & 255, lyi = bi >> 8;
       int gx = ix0 + lxi, gy = iy0 + lyi;
       int p = (lyi + OFF) * kLX + (lxi + OFF);
+      // the pixel's colour is loaded first: its latency overlaps the simple-point tests
+      const float* pix = img + 3 * ((size_t)gy * W + gx);
+      const float c0 = __ldg(pix), c1 = __ldg(pix + 1), c2 = __ldg(pix + 2);
       int C = L[p];
       if (C < 0 || C >= cap) continue;
       const int N = L[p - kLX], S = L[p + kLX], Wl = L[p - 1], E = L[p + 1];
@@ -855,15 +858,14 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
       const int dN = 8 - __popc(cN), dW = 8 - __popc(cW), dS = 8 - __popc(cS),
                 dE = 8 - __popc(cE);
       if (N >= cap || S >= cap || Wl >= cap || E >= cap) continue;
-      const float* pix = img + 3 * ((size_t)gy * W + gx);
       float best = -9999.f;
       int bl = C;
-      if (N >= 0) joint(pix, gx, gy, rec[N], N, s2, (float)dN, potts, &best, &bl);
-      if (S != N && S >= 0) joint(pix, gx, gy, rec[S], S, s2, (float)dS, potts, &best, &bl);
+      if (N >= 0) joint(c0, c1, c2, gx, gy, rec[N], N, s2, (float)dN, potts, &best, &bl);
+      if (S != N && S >= 0) joint(c0, c1, c2, gx, gy, rec[S], S, s2, (float)dS, potts, &best, &bl);
       if (Wl != S && Wl != N && Wl >= 0)
-        joint(pix, gx, gy, rec[Wl], Wl, s2, (float)dW, potts, &best, &bl);
+        joint(c0, c1, c2, gx, gy, rec[Wl], Wl, s2, (float)dW, potts, &best, &bl);
       if (E != Wl && E != S && E != N && E >= 0)
-        joint(pix, gx, gy, rec[E], E, s2, (float)dE, potts, &best, &bl);
+        joint(c0, c1, c2, gx, gy, rec[E], E, s2, (float)dE, potts, &best, &bl);
       if (rec[C].count <= 2 && bl == C) {
         if (N >= 0) bl = N;
         else if (E >= 0) bl = E;
