@@ -293,7 +293,8 @@ def run_serve(args, world, rank):
     plain_fps = plain_frames / plain_s
     budget = int(sv["budget_gb"] * 2 ** 30)
     srv = serve.Server(budget, max_batch=args.max_batch, lanes=args.lanes, device=dev,
-                       seed=rank, max_pixels=args.max_pixels, **cfg)
+                       seed=rank, max_pixels=args.max_pixels,
+                       group_sizes=not args.no_group_sizes, **cfg)
     # warm-up run (untimed): two short streams per resolution, so that the lanes'
     # engine contexts exist and the sweep tile classes are tuned
     for j, hw in enumerate(sorted(pool) * 2):
@@ -322,6 +323,7 @@ def run_serve(args, world, rank):
                    "frames_per_stream": sv["T"], "arrivals": "Poisson %.0f fps per stream" % sv["fps"],
                    "offered_fps": S * sv["fps"], "budget_gb": sv["budget_gb"],
                    "max_batch": args.max_batch, "max_pixels": args.max_pixels,
+                   "group_sizes": not args.no_group_sizes,
                    "lanes": args.lanes, "warmup": "2 streams x 4 frames per resolution, untimed",
                    "sp_size": w["sp_size"], "niters": w["niters"], "prop_niters": w["prop_niters"],
                    "sm_period": w["sm_period"]},
@@ -693,7 +695,7 @@ def main():
                          "t of every stream of a lane runs as one batch")
     ap.add_argument("--lanes", type=int, default=None,
                     help="host threads per GPU, each with its own CUDA stream, engine "
-                         "context and share of the streams (default 3; serve: 2)")
+                         "context and share of the streams (default 3)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="stream",
                     choices=["stream", "serve", "batch", "precision", "image", "latency"],
@@ -713,6 +715,9 @@ def main():
     ap.add_argument("--sweep-tile", type=int, default=0, choices=[0, 16, 32, 64],
                     help="stream: single-sweep tile width (0 autotuned); profiler runs pin "
                          "the width the autotuner picks without the profiler")
+    ap.add_argument("--no-group-sizes", action="store_true",
+                    help="serve: batches take frames oldest first across sizes (default: the "
+                         "oldest frame's size first)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch-graphs", action="store_true",
                     help="stream: launch every batch step's kernels one by one (ncu lists no "
@@ -721,7 +726,7 @@ def main():
     if args.streams is None:
         args.streams = SERVE["streams"] if args.mode == "serve" else 24
     if args.lanes is None:
-        args.lanes = 2 if args.mode == "serve" else 3
+        args.lanes = 3
     world, rank, local = dist_setup()
     args.local = local
     if args.impl == "reference":

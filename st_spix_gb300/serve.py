@@ -66,11 +66,13 @@ class Scheduler:
     time and so the latency of the frames in it.  Not thread-safe; Server serialises
     calls with a lock."""
 
-    def __init__(self, budget: int, reserve: int, max_batch: int, max_pixels: int = 0):
+    def __init__(self, budget: int, reserve: int, max_batch: int, max_pixels: int = 0,
+                 group_sizes: bool = True):
         if reserve > budget:
             raise ValueError(f"working buffers ({reserve} B) exceed the budget ({budget} B)")
         self.budget, self.reserve, self.max_batch = int(budget), int(reserve), int(max_batch)
         self.max_pixels = int(max_pixels)
+        self.group_sizes = bool(group_sizes)
         self.used = self.reserve
         self.streams: Dict[int, _StreamState] = {}
         self.queue: List[int] = []        # offered, not yet admitted (FIFO)
@@ -119,9 +121,12 @@ class Scheduler:
         return out
 
     def next_batch(self, now: float) -> List[Tuple[int, int, float]]:
-        """Frames that have arrived, one per idle stream, oldest first, at most
-        max_batch (and max_pixels); they are marked in flight.  Items: (sid, frame,
-        arrival)."""
+        """Frames that have arrived, one per idle stream, at most max_batch (and
+        max_pixels); they are marked in flight.  Items: (sid, frame, arrival).  The
+        oldest frame goes first, then (group_sizes) the other frames of its size, then
+        the rest, each oldest first: batches of one frame size waste no grid blocks on
+        smaller frames and repeat their launch sequence (which the engine replays as a
+        CUDA graph)."""
         ready = []
         for sid in self.active:
             st = self.streams[sid]
@@ -131,6 +136,10 @@ class Scheduler:
             if a <= now:
                 ready.append((a, sid))
         ready.sort()
+        if self.group_sizes and ready:
+            n0 = self.streams[ready[0][1]].npix
+            ready = ([r for r in ready if self.streams[r[1]].npix == n0] +
+                     [r for r in ready if self.streams[r[1]].npix != n0])
         items, pix = [], 0
         for a, sid in ready:
             if len(items) >= self.max_batch:
@@ -217,7 +226,7 @@ class Server:
     """Continuous-batching server on one GPU (see the module docstring)."""
 
     def __init__(self, budget_bytes: int, max_batch: int = 8, lanes: int = 2, device=None,
-                 seed: int = 0, max_pixels: int = 0, **cfg):
+                 seed: int = 0, max_pixels: int = 0, group_sizes: bool = True, **cfg):
         import torch
         from . import batch, bist_cuda, _lib
         self._torch, self._batch, self._bist, self._lib = torch, batch, bist_cuda, _lib
@@ -226,6 +235,7 @@ class Server:
         self.budget = int(budget_bytes)
         self.max_batch = int(max_batch)
         self.max_pixels = int(max_pixels)
+        self.group_sizes = bool(group_sizes)
         self.lanes = int(lanes)
         self.cfg = cfg
         self.sp_default = int(cfg.get("sp_size", 15))
@@ -265,7 +275,7 @@ class Server:
         slot_b = max(self._lib.footprint(r.vid.shape[1], r.vid.shape[2],
                                          r.sp_size or self.sp_default)[1] for r in reqs)
         sched = Scheduler(self.budget, self.lanes * self.max_batch * slot_b, self.max_batch,
-                          self.max_pixels)
+                          self.max_pixels, self.group_sizes)
         lock = threading.Lock()
         wake = threading.Condition(lock)
         t0 = time.perf_counter()

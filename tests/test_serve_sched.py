@@ -110,3 +110,20 @@ def test_pixel_cap_bounds_batches_oldest_first():
     for sid in range(3):
         s.offer(sid, 1, [0.0], npix=10 ** 6)
     assert len(s.next_batch(0.0)) == 3
+
+
+def test_batches_group_frames_of_the_oldest_frames_size():
+    s = Scheduler(budget=1000, reserve=0, max_batch=3)
+    s.offer(1, 1, [0.1], npix=100)
+    s.offer(2, 1, [0.2], npix=400)
+    s.offer(3, 1, [0.3], npix=100)
+    s.offer(4, 1, [0.4], npix=400)
+    s.offer(5, 1, [0.5], npix=100)
+    # the oldest frame (100 px) first, then the other 100-px frames, oldest first
+    assert [i[0] for i in s.next_batch(1.0)] == [1, 3, 5]
+    assert [i[0] for i in s.next_batch(1.0)] == [2, 4]
+    # without grouping: oldest first across sizes
+    s = Scheduler(budget=1000, reserve=0, max_batch=3, group_sizes=False)
+    for sid, n in zip(range(1, 6), [100, 400, 100, 400, 100]):
+        s.offer(sid, 1, [0.1 * sid], npix=n)
+    assert [i[0] for i in s.next_batch(1.0)] == [1, 2, 3]
