@@ -140,7 +140,8 @@ struct stspix_ctx {
   bool capturing = false;
   cudaStream_t cap_stream = nullptr;   // records graphs for callers on the legacy stream
   bool graphs_on = true;
-  struct BatchGraph { cudaGraph_t g; cudaGraphExec_t exec; long long launches; };
+  struct BatchGraph { cudaGraph_t g; cudaGraphExec_t exec; long long launches, last; };
+  long long graph_tick = 0;
   std::map<std::string, BatchGraph> batch_graphs;
   std::map<std::string, int> batch_seen;
   long long graph_replays = 0;
@@ -1259,7 +1260,18 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     if (g == ctx->batch_graphs.end() && ctx->batch_seen.size() >= 4096 && !ctx->batch_seen.count(key))
       ctx->batch_seen.clear();
     if (outer != cudaStreamCaptureStatusNone) g = ctx->batch_graphs.end();
-    else if (g == ctx->batch_graphs.end() && ctx->batch_seen[key]++ > 0 && ctx->batch_graphs.size() < 64) {
+    else if (g == ctx->batch_graphs.end() && ++ctx->batch_seen[key] >= 2 &&
+             ((int)ctx->batch_graphs.size() < kMaxBatchGraphs || ctx->batch_seen[key] >= 4)) {
+      // a full cache takes only signatures seen four times, in place of the least
+      // recently replayed graph (a graph still in flight is freed when it completes)
+      if ((int)ctx->batch_graphs.size() >= kMaxBatchGraphs) {
+        auto lru = ctx->batch_graphs.begin();
+        for (auto it = ctx->batch_graphs.begin(); it != ctx->batch_graphs.end(); ++it)
+          if (it->second.last < lru->second.last) lru = it;
+        cudaGraphExecDestroy(lru->second.exec);
+        cudaGraphDestroy(lru->second.g);
+        ctx->batch_graphs.erase(lru);
+      }
       // second occurrence: record the step into a graph (the legacy default stream
       // cannot be captured: record on the context's own stream then; nothing runs
       // during a capture, and the graph is launched on the caller's stream)
@@ -1284,7 +1296,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
       const long long nl = ctx->launches - l0;
       ctx->launches = l0;
       if (!r && ce == cudaSuccess && ie == cudaSuccess) {
-        g = ctx->batch_graphs.emplace(key, stspix_ctx::BatchGraph{graph, exec, nl}).first;
+        g = ctx->batch_graphs.emplace(key, stspix_ctx::BatchGraph{graph, exec, nl, 0}).first;
       } else {
         // nothing recorded ran: clear the capture error and run this step eagerly;
         // the signature is not captured again
@@ -1295,6 +1307,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     }
     if (g != ctx->batch_graphs.end()) {
       CK(cudaGraphLaunch(g->second.exec, st));
+      g->second.last = ++ctx->graph_tick;
       ctx->launches += g->second.launches;
       ctx->graph_replays++;
     } else if ((r = batch_body(ctx, st, stages, La, Lb, Lp, Ls, own, nit_sorted, cfg))) {

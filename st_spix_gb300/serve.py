@@ -286,13 +286,17 @@ class Server:
                         kind=(H, W, T if r.keep_labels else 1), npix=H * W)
         dev = self.device
         errors = []
+        replays = [0] * self.lanes
 
         def lane(j):
             try:
                 torch.cuda.set_device(dev)
                 with torch.cuda.stream(self._streams[j]):
+                    ctx = self._bist._ctx(dev)
+                    r0 = ctx.graph_replays()
                     while True:
                         with lock:
+                            replays[j] = ctx.graph_replays() - r0
                             if sched.done() or errors:
                                 wake.notify_all()
                                 return
@@ -346,6 +350,7 @@ class Server:
         if errors:
             raise RuntimeError("; ".join(errors))
         out = self.stats(sched)
+        out["graph_replays"] = int(sum(replays))
         self.served.update(self.requests)
         self.requests = {}
         return out
