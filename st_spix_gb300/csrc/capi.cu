@@ -21,6 +21,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <string>
 #include <vector>
@@ -1149,19 +1150,25 @@ struct BatchOut {
   std::vector<stspix_frame_log> log;
 };
 
-// A batch's work from the table uploads to the parameter read-out, for the case with
-// known iteration counts and no partial stop (eager, or recorded into a graph).
-int batch_body(stspix_ctx* ctx, cudaStream_t st, int stages, const List& La, const List& Lb,
-               const List& Lp, const List& Ls, bool ls_own, const std::vector<int>& nit_sorted,
-               const stspix_config& cfg) {
+// A batch's work in two parts (eager, or each recorded into a graph): the head, from
+// the table uploads to the BASS initialisation (after it the host may read the hole
+// fractions for the 4/8/12 ladder), and the tail, from the propagated initialisation
+// to the parameter read-out, for known iteration counts and no partial stop.
+int batch_head(stspix_ctx* ctx, cudaStream_t st, int stages, const List& La, const List& Lb,
+               const List& Lp) {
   int r;
   if ((r = upload(ctx, st, La, 0)) || (r = upload(ctx, st, Lb, 1)) || (r = upload(ctx, st, Lp, 2)))
     return r;
-  if (ls_own && (r = upload(ctx, st, Ls, 3))) return r;
   ctx->cur_fam = STSPIX_FAM_OTHER;
   LAUNCHS(kb_scalars, La, La.B, (int)kOpBegin);
   if ((stages & kStageShift) && (r = shift_fill(ctx, st, Lp))) return r;
-  if ((r = bass_init(ctx, st, Lb))) return r;
+  return bass_init(ctx, st, Lb);
+}
+
+int batch_tail(stspix_ctx* ctx, cudaStream_t st, const List& Lp, const List& Ls, bool ls_own,
+               const std::vector<int>& nit_sorted, const stspix_config& cfg) {
+  int r;
+  if (ls_own && (r = upload(ctx, st, Ls, 3))) return r;
   if ((r = prop_init(ctx, st, Lp))) return r;
   const SmConsts K = sm_constants(cfg);
   if ((r = bass_loop(ctx, st, Ls, nit_sorted, cfg, K, -1, 0))) return r;
@@ -1169,6 +1176,76 @@ int batch_body(stspix_ctx* ctx, cudaStream_t st, int stages, const List& La, con
   LAUNCHB(kb_read_params, Ls.max_cap, Ls, Ls.B);
   LAUNCHB(kb_save_prev, Ls.max_npix, Ls, Ls.B);
   return STSPIX_OK;
+}
+
+// Runs body(stream) eagerly, or, from the second occurrence of key on, as a replay of
+// the CUDA graph recorded on that occurrence.  body only launches work (no host
+// synchronisation, no host decision on device results).
+int run_graphed(stspix_ctx* ctx, cudaStream_t st, const std::string& key,
+                const std::function<int(cudaStream_t)>& body) {
+  int r = STSPIX_OK;
+  auto g = ctx->batch_graphs.find(key);
+  cudaStreamCaptureStatus outer = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(st, &outer));   // a caller's own capture records the eager step
+  // a server whose batch compositions rarely repeat keeps the table of seen
+  // signatures bounded: it restarts counting when it grows large
+  if (g == ctx->batch_graphs.end() && ctx->batch_seen.size() >= 4096 && !ctx->batch_seen.count(key))
+    ctx->batch_seen.clear();
+  if (outer != cudaStreamCaptureStatusNone) {
+    g = ctx->batch_graphs.end();
+  } else if (g == ctx->batch_graphs.end() && ++ctx->batch_seen[key] >= 2 &&
+             ((int)ctx->batch_graphs.size() < kMaxBatchGraphs || ctx->batch_seen[key] >= 4)) {
+    // a full cache takes only signatures seen four times, in place of the least
+    // recently replayed graph (a graph still in flight is freed when it completes)
+    if ((int)ctx->batch_graphs.size() >= kMaxBatchGraphs) {
+      auto lru = ctx->batch_graphs.begin();
+      for (auto it = ctx->batch_graphs.begin(); it != ctx->batch_graphs.end(); ++it)
+        if (it->second.last < lru->second.last) lru = it;
+      cudaGraphExecDestroy(lru->second.exec);
+      cudaGraphDestroy(lru->second.g);
+      ctx->batch_graphs.erase(lru);
+    }
+    // record (the legacy default stream cannot be captured: record on the context's
+    // own stream then; nothing runs during a capture, and the graph is launched on
+    // the caller's stream)
+    std::lock_guard<std::mutex> lk(g_device_mu);
+    cudaStream_t cst = st;
+    if (st == nullptr || st == cudaStreamLegacy) {
+      if (!ctx->cap_stream) CK(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+      cst = ctx->cap_stream;
+    }
+    const long long l0 = ctx->launches;
+    cudaError_t ce = cudaStreamBeginCapture(cst, cudaStreamCaptureModeThreadLocal);
+    cudaGraph_t graph = nullptr;
+    if (ce == cudaSuccess) {
+      ctx->capturing = true;
+      r = body(cst);
+      ctx->capturing = false;
+      ce = cudaStreamEndCapture(cst, &graph);
+    }
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ie = cudaErrorUnknown;
+    if (!r && ce == cudaSuccess) ie = cudaGraphInstantiate(&exec, graph, 0);
+    const long long nl = ctx->launches - l0;
+    ctx->launches = l0;
+    if (!r && ce == cudaSuccess && ie == cudaSuccess) {
+      g = ctx->batch_graphs.emplace(key, stspix_ctx::BatchGraph{graph, exec, nl, 0}).first;
+    } else {
+      // nothing recorded ran: clear the capture error and run this step eagerly;
+      // the signature is not captured again
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      ctx->batch_seen[key] = -(1 << 30);
+    }
+  }
+  if (g != ctx->batch_graphs.end()) {
+    CK(cudaGraphLaunch(g->second.exec, st));
+    g->second.last = ++ctx->graph_tick;
+    ctx->launches += g->second.launches;
+    ctx->graph_replays++;
+    return STSPIX_OK;
+  }
+  return body(st);
 }
 
 // The key of a batch step's launch sequence: everything that sets a launch's grid or
@@ -1246,73 +1323,31 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     *own = !std::is_sorted(order.begin(), order.end());
     return *own ? make_list(ctx, 3, sorted) : La;
   };
-  if ((stages & kStageSeg) && !need_ladder && stop_after < 0 && !split_dir && !ctx->prof_on &&
-      ctx->graphs_on) {
+  // full steps (known or laddered iteration counts) run as head + tail, each replayed
+  // as a CUDA graph once its launch sequence repeats
+  if ((stages & kStageSeg) && stop_after < 0 && !split_dir && !ctx->prof_on && ctx->graphs_on) {
+    const std::string key = batch_signature(fr, caps, nit, stages, cfg);
+    if ((r = run_graphed(ctx, st, key + "h", [&](cudaStream_t s) {
+           return batch_head(ctx, s, stages, La, Lb, Lp);
+         })))
+      return r;
+    if (need_ladder) {
+      if ((r = read_scalars(ctx, st, B))) return r;
+      for (int i = 0; i < B; i++) {
+        if (nit[i] >= 0) continue;
+        const int npix = fr[i].H * fr[i].W;
+        float iperc = ctx->sc_host[i].ninvalid / (1.0 * npix);
+        nit[i] = iperc > 0.20 ? 12 : (iperc < 0.01 ? 4 : 8);
+      }
+    }
     std::vector<int> nit_sorted;
     bool own = false;
     const List Ls = sort_table(nit_sorted, &own);
-    const std::string key = batch_signature(fr, caps, nit, stages, cfg);
-    auto g = ctx->batch_graphs.find(key);
-    cudaStreamCaptureStatus outer = cudaStreamCaptureStatusNone;
-    CK(cudaStreamIsCapturing(st, &outer));   // a caller's own capture records the eager step
-    // a server whose batch compositions rarely repeat keeps the table of seen
-    // signatures bounded: it restarts counting when it grows large
-    if (g == ctx->batch_graphs.end() && ctx->batch_seen.size() >= 4096 && !ctx->batch_seen.count(key))
-      ctx->batch_seen.clear();
-    if (outer != cudaStreamCaptureStatusNone) g = ctx->batch_graphs.end();
-    else if (g == ctx->batch_graphs.end() && ++ctx->batch_seen[key] >= 2 &&
-             ((int)ctx->batch_graphs.size() < kMaxBatchGraphs || ctx->batch_seen[key] >= 4)) {
-      // a full cache takes only signatures seen four times, in place of the least
-      // recently replayed graph (a graph still in flight is freed when it completes)
-      if ((int)ctx->batch_graphs.size() >= kMaxBatchGraphs) {
-        auto lru = ctx->batch_graphs.begin();
-        for (auto it = ctx->batch_graphs.begin(); it != ctx->batch_graphs.end(); ++it)
-          if (it->second.last < lru->second.last) lru = it;
-        cudaGraphExecDestroy(lru->second.exec);
-        cudaGraphDestroy(lru->second.g);
-        ctx->batch_graphs.erase(lru);
-      }
-      // second occurrence: record the step into a graph (the legacy default stream
-      // cannot be captured: record on the context's own stream then; nothing runs
-      // during a capture, and the graph is launched on the caller's stream)
-      std::lock_guard<std::mutex> lk(g_device_mu);
-      cudaStream_t cst = st;
-      if (st == nullptr || st == cudaStreamLegacy) {
-        if (!ctx->cap_stream) CK(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
-        cst = ctx->cap_stream;
-      }
-      const long long l0 = ctx->launches;
-      cudaError_t ce = cudaStreamBeginCapture(cst, cudaStreamCaptureModeThreadLocal);
-      cudaGraph_t graph = nullptr;
-      if (ce == cudaSuccess) {
-        ctx->capturing = true;
-        r = batch_body(ctx, cst, stages, La, Lb, Lp, Ls, own, nit_sorted, cfg);
-        ctx->capturing = false;
-        ce = cudaStreamEndCapture(cst, &graph);
-      }
-      cudaGraphExec_t exec = nullptr;
-      cudaError_t ie = cudaErrorUnknown;
-      if (!r && ce == cudaSuccess) ie = cudaGraphInstantiate(&exec, graph, 0);
-      const long long nl = ctx->launches - l0;
-      ctx->launches = l0;
-      if (!r && ce == cudaSuccess && ie == cudaSuccess) {
-        g = ctx->batch_graphs.emplace(key, stspix_ctx::BatchGraph{graph, exec, nl, 0}).first;
-      } else {
-        // nothing recorded ran: clear the capture error and run this step eagerly;
-        // the signature is not captured again
-        if (graph) cudaGraphDestroy(graph);
-        cudaGetLastError();
-        ctx->batch_seen[key] = -(1 << 30);
-      }
-    }
-    if (g != ctx->batch_graphs.end()) {
-      CK(cudaGraphLaunch(g->second.exec, st));
-      g->second.last = ++ctx->graph_tick;
-      ctx->launches += g->second.launches;
-      ctx->graph_replays++;
-    } else if ((r = batch_body(ctx, st, stages, La, Lb, Lp, Ls, own, nit_sorted, cfg))) {
+    const std::string tkey = need_ladder ? batch_signature(fr, caps, nit, stages, cfg) : key;
+    if ((r = run_graphed(ctx, st, tkey + "t", [&](cudaStream_t s) {
+           return batch_tail(ctx, s, Lp, Ls, own, nit_sorted, cfg);
+         })))
       return r;
-    }
     return finish();
   }
   if ((r = upload(ctx, st, La, 0)) || (r = upload(ctx, st, Lb, 1)) || (r = upload(ctx, st, Lp, 2)))

@@ -167,3 +167,29 @@ def test_batch_graphs_off_launch_eagerly_with_the_same_labels():
             assert ctx.graph_replays() == r0
         finally:
             ctx.set_batch_graphs(True)
+
+
+def test_laddered_steps_replay_graphs_with_the_oracle_labels():
+    """Propagated frames with the 4/8/12 ladder run as a head and a tail: both replay as
+    CUDA graphs once their launch sequences repeat (the tail's key holds the ladder's
+    outcome), with the oracle's labels on every pass."""
+    T = 5
+    kw = dict(niters=8, sm_period=4, sp_size=12)
+    v, f, _ = synth.voronoi_video(48, 64, T, 16, 0.03, seed=9, max_shift=2.0)
+    st, ref, _ = O.bist_forward(v, f, O.default_config(**kw), True)
+    assert st == 0
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx = bist_cuda._ctx(torch.device("cuda", 0))
+        r0 = ctx.graph_replays()
+        vs = batch.Video(48, 64)
+        vid, flo = cuda(v), cuda(f)
+        for _ in range(3):
+            vs.reset()
+            for t in range(T):
+                fr = [batch.Frame(img=vid[t], flow=flo[t - 1] if t else None, video=vs,
+                                  sp_size=12)]
+                batch.process_batch(fr, **kw)
+                np.testing.assert_array_equal(fr[0].labels.cpu().numpy(), ref[t])
+        vs.close()
+        assert ctx.graph_replays() > r0
