@@ -726,6 +726,16 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
     v1 = 0;
     for (int c = 1; c < kSweepVariants; c++)
       if (t1[c] < best1) { best1 = t1[c]; v1 = c; }
+    // Large batches keep the widest tile (the least halo work per pixel: 1.41 staged
+    // labels per pixel against 1.56 for 32x32) unless another width is 5 % faster:
+    // with other lanes' kernels on the SMs the total work decides, and timings of
+    // 64x32 and 32x32 alone differ by less than their noise (batches of 8 480x854
+    // frames on three lanes: 1545 frames/s when one lane picked 32x32, 1635-1642
+    // with 64x32 on all).
+    if (tl >= kPairMaxTiles && t1[1] <= kWideMargin * best1) {
+      best1 = t1[1];
+      v1 = 1;
+    }
     done = 1;
     launch = 1;
     // Large batches keep single sweeps: a two-sweep launch holds more registers (4

@@ -29,6 +29,7 @@ constexpr int kFillBreakIter = 1000;      // fill_missing.cu: break_iter
 constexpr int kSweepVariants = 3;         // sweep tile shapes: 32x32, 64x32, 16x32
 constexpr int kTuneRounds = 3;            // timed runs per autotuner trial (fastest kept)
 constexpr int kMaxBatchGraphs = 64;       // captured batch steps kept per context
+constexpr float kWideMargin = 1.05f;      // large batches: 64x32 unless 5 % slower
 constexpr int kPairMaxTiles = 2048;       // two-sweep launches only below this many 32x32 tiles
 constexpr int kSweepTileW[kSweepVariants] = {32, 64, 16};
 
