@@ -436,6 +436,35 @@ LATENCY = dict(name="latency_stream_480p_720p_1080p", sizes=((480, 854), (720, 1
                frames=10, batches=(1, 8))
 
 
+def frame_latencies(H, W, B, T, cfg, dev, nseeds, sigma):
+    """Host wall ms of each propagated batch of B streams of H x W (frames 1..T-1), one
+    frame per stream per batch, after one untimed pass over the same frames."""
+    import torch
+    from st_spix_gb300 import batch, synth
+    vids = [synth.voronoi_video_device(H, W, T, nseeds, sigma, seed=i, device=dev)
+            for i in range(B)]
+    videos = [batch.Video(H, W, dev) for _ in range(B)]
+
+    def run(times):
+        for v in videos:
+            v.reset()
+        for t in range(T):
+            fr = [batch.Frame(img=vids[i][0][t], flow=vids[i][1][t - 1] if t else None,
+                              video=videos[i]) for i in range(B)]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            batch.process_batch(fr, **cfg)
+            torch.cuda.synchronize()
+            if t > 0:
+                times.append(1000 * (time.perf_counter() - t0))
+    run([])
+    times = []
+    run(times)
+    for v in videos:
+        v.close()
+    return sorted(times)
+
+
 def run_latency(args, world, rank):
     """--mode latency: per-frame latency of the streaming workload's propagated frames
     (400 seeds, sp 20, 20 iterations, split/merge every 10) with one frame per batch, and
@@ -453,28 +482,7 @@ def run_latency(args, world, rank):
     res = {}
     for H, W in lt["sizes"]:
         for B in lt["batches"]:
-            vids = [synth.voronoi_video_device(H, W, T, w["nseeds"], w["sigma"], seed=i,
-                                               device=dev) for i in range(B)]
-            videos = [batch.Video(H, W, dev) for _ in range(B)]
-
-            def run(times):
-                for v in videos:
-                    v.reset()
-                for t in range(T):
-                    fr = [batch.Frame(img=vids[i][0][t], flow=vids[i][1][t - 1] if t else None,
-                                      video=videos[i]) for i in range(B)]
-                    torch.cuda.synchronize()
-                    t0 = time.perf_counter()
-                    batch.process_batch(fr, **cfg)
-                    torch.cuda.synchronize()
-                    if t > 0:
-                        times.append(1000 * (time.perf_counter() - t0))
-            run([])
-            times = []
-            run(times)
-            for v in videos:
-                v.close()
-            times.sort()
+            times = frame_latencies(H, W, B, T, cfg, dev, w["nseeds"], w["sigma"])
             res[f"{H}x{W}_batch{B}"] = {"batch_ms_p50": times[len(times) // 2],
                                         "batch_ms_max": times[-1],
                                         "ms_per_frame": sum(times) / len(times) / B}
@@ -895,6 +903,13 @@ def main():
     torch.cuda.synchronize()
     qual_ms = 1000 * (time.perf_counter() - t0)
 
+    # ---- 720p frame latency: one stream alone, one frame per batch -------------------
+    lat = frame_latencies(720, 1280, 1, T, cfg, dev, w["nseeds"], w["sigma"])
+    lat720 = {"frames": len(lat), "p50_ms": lat[len(lat) // 2],
+              "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+              "note": "one 720p stream of the same video model alone, one frame per batch, host "
+                      "wall per propagated frame (frames 1..%d, after one untimed pass)" % (T - 1)}
+
     # ---- per-family device time of lane 0's batches (CUDA events on its stream) --
     with torch.cuda.stream(cstreams[0]):
         ctxs[0].profile(True)
@@ -1001,6 +1016,7 @@ def main():
                    "l2": "inputs larger than L2: %d MB of frames+flow read per step" %
                          (h_bytes // 2 ** 20)},
         "p50_frame_ms": pct(0.50), "p99_frame_ms": pct(0.99),
+        "latency_720p": lat720,
         "latency_note": "frame latency = GPU time of the batch the frame ran in",
         "plain_per_frame_fps": plain_fps,
         "plain_vs_batched_label_agreement": agree,
