@@ -590,6 +590,16 @@ std::vector<int> split_partition(const Frame& f, int direction) {
 
 inline bool near_tie(double h) { return fabs(h + 2.0) < 1e-6; }
 
+// Per-id record of one split or merge step, filled when oracle_sm_step sets it: the
+// Hastings log-ratio of every id the step scores, the merge candidate, the threshold
+// test (want) and the final decision (accept: a split taken / a merge claim won).
+struct SmTrace {
+  std::vector<double> h;
+  std::vector<int> pair;
+  std::vector<uint8_t> want, accept;
+};
+SmTrace* g_trace = nullptr;
+
 // split_merge_orig.cu:202-414 CudaCalcSplitCandidate_orig (and the prop variant,
 // split_merge_prop.cu:184-395 with update_split_flag_p :3026-3149 when prop_mode).
 void run_split(Frame& f, int direction, const int* shifted, bool prop_mode) {
@@ -633,8 +643,10 @@ void run_split(Frame& f, int direction, const int* shifted, bool prop_mode) {
       h = h - 2 * (1.0 - iperc);
     }
     if (near_tie(h)) f.log.near_ties++;
+    if (g_trace) g_trace->h[k] = h;
     if (!(h > -2)) continue;
     accept[k] = 1;
+    if (g_trace) g_trace->want[k] = g_trace->accept[k] = 1;
     int snew = ++next;
     newid[k] = snew;
     if (!prop_mode) {
@@ -742,11 +754,16 @@ void run_merge(Frame& f, int direction, bool prop_mode) {
       h = m_merged - (K.log_alpha + msingle[k] + msingle[fk]) + f.cfg.merge_alpha;
     }
     if (near_tie(h)) f.log.near_ties++;
+    if (g_trace) g_trace->h[k] = h;
     if (h > -2) { want[k] = 1; claim[fk] = std::min(claim[fk], k); }
   }
   std::vector<uint8_t> merge(nbuf, 0);
   for (int k = 0; k < nbuf; k++)
     if (want[k] && claim[pair[k]] == k) merge[k] = 1;
+  if (g_trace) {
+    g_trace->pair = pair;
+    for (int k = 0; k < nbuf; k++) { g_trace->want[k] = want[k]; g_trace->accept[k] = merge[k]; }
+  }
   // remove_sp / remove_sp_p
   std::vector<uint8_t> remove(nbuf, 0);
   std::vector<int> target = pair;
@@ -1400,6 +1417,62 @@ void oracle_invalidate_disconnected(int32_t* seg, int H, int W, int nspix) {
 }
 
 void oracle_get_frame_log(stspix_frame_log* out) { *out = g_last_log; }
+
+// One split (kind 0: BASS, split_merge_orig.cu:202-414; 2: propagated,
+// split_merge_prop.cu:184-395) or merge (kind 1: split_merge_orig.cu:79-199; 3:
+// split_merge_prop.cu:87-181) step on a given state: labels seg_in (ids < nbuf), per
+// id valid / prior_count / prop / sample_sigma_shape (prior_icov = identity and
+// prior_sigma_shape = 1/sp_size as init_sparams.cu:60-100 sets them).  As in the
+// reference's loop, update_params runs first and the border mask is the last
+// update_seg pass's find_border_pixels.  Outputs per id: h (NaN where the step scores
+// no ratio), the merge candidate, want (h > -2) and accept; the labels after the step.
+int oracle_sm_step(const float* img, const int32_t* seg_in, int H, int W,
+                   const stspix_config* cfg, int nbuf, const uint8_t* valid,
+                   const float* prior_count, const uint8_t* prop, const double* sample_sigma,
+                   int max_spix, int kind, int direction, const int32_t* shifted, double* h_out,
+                   int32_t* pair_out, uint8_t* want_out, uint8_t* accept_out, int32_t* seg_out,
+                   int* max_spix_out) {
+  Frame f;
+  f.H = H; f.W = W; f.npix = H * W; f.img = img; f.cfg = *cfg;
+  f.seg.assign(seg_in, seg_in + f.npix);
+  f.border.assign(f.npix, 0);
+  f.sp.init(nbuf);
+  Sp& sp = f.sp;
+  for (int k = 0; k < nbuf; k++) {
+    sp.valid[k] = valid[k];
+    sp.prior_count[k] = prior_count[k];
+    sp.prop[k] = prop ? prop[k] : 0;
+    sp.prior_icov[3 * k] = 1; sp.prior_icov[3 * k + 1] = 0; sp.prior_icov[3 * k + 2] = 1;
+    sp.prior_sigma_shape[3 * k] = 1.0 / cfg->sp_size;
+    sp.prior_sigma_shape[3 * k + 2] = 1.0 / cfg->sp_size;
+    for (int c = 0; c < 3; c++) sp.sample_sigma_shape[3 * k + c] = sample_sigma[3 * k + c];
+  }
+  f.max_spix = max_spix;
+  update_params(f);
+  find_border(f.seg.data(), f.border.data(), H, W);
+  SmTrace tr;
+  tr.h.assign(nbuf, NAN);
+  tr.pair.assign(nbuf, -1);
+  tr.want.assign(nbuf, 0);
+  tr.accept.assign(nbuf, 0);
+  g_trace = &tr;
+  switch (kind) {
+    case 0: run_split(f, direction, nullptr, false); break;
+    case 1: run_merge(f, direction, false); break;
+    case 2: run_split(f, direction, shifted, true); break;
+    default: run_merge(f, direction, true); break;
+  }
+  g_trace = nullptr;
+  for (int k = 0; k < nbuf; k++) {
+    h_out[k] = tr.h[k];
+    pair_out[k] = tr.pair[k];
+    want_out[k] = tr.want[k];
+    accept_out[k] = tr.accept[k];
+  }
+  std::copy(f.seg.begin(), f.seg.end(), seg_out);
+  *max_spix_out = f.max_spix;
+  return f.status;
+}
 
 // Stage functions on caller-supplied state, used to pin the restatement against the
 // reference's own kernels (oracle/ref_harness.cpp) on identical inputs.

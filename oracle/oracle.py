@@ -113,6 +113,9 @@ def lib():
             _lib.oracle_split_bfs.argtypes = [P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P]
             _lib.oracle_cc_roots.argtypes = [P, C.c_int, C.c_int, P]
             _lib.oracle_default_config.argtypes = [C.POINTER(Config)]
+            _lib.oracle_sm_step.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Config), C.c_int,
+                                            P, P, P, P, C.c_int, C.c_int, C.c_int, P, P, P, P,
+                                            P, P, C.POINTER(C.c_int)]
     return _lib
 
 
@@ -354,4 +357,32 @@ def rescale_u8(img, scale=255.0):
     img = np.ascontiguousarray(img, np.uint8)
     out = np.empty(img.shape, np.float32)
     lib().oracle_rescale_u8(_p(img), _p(out), C.c_longlong(img.size), C.c_float(scale))
+    return out
+
+
+def sm_step(img, labels, cfg: Config, nbuf, valid, prior_count, prop, sample_sigma, max_spix,
+            kind, direction, shifted=None):
+    """One split (kind 0 BASS / 2 propagated) or merge (kind 1 / 3) step on a given
+    state (oracle_sm_step): per id the Hastings log-ratio (NaN where none is scored),
+    merge candidate, threshold test and decision, and the labels after the step."""
+    img = np.ascontiguousarray(img, np.float32)
+    labels = np.ascontiguousarray(labels, np.int32)
+    H, W = labels.shape
+    valid = np.ascontiguousarray(valid, np.uint8)
+    prior_count = np.ascontiguousarray(prior_count, np.float32)
+    prop = np.ascontiguousarray(prop, np.uint8)
+    sample_sigma = np.ascontiguousarray(sample_sigma, np.float64)
+    shifted = (np.ascontiguousarray(shifted, np.int32) if shifted is not None
+               else np.zeros((H, W), np.int32))
+    out = dict(h=np.zeros(nbuf, np.float64), pair=np.zeros(nbuf, np.int32),
+               want=np.zeros(nbuf, np.uint8), accept=np.zeros(nbuf, np.uint8),
+               labels=np.zeros((H, W), np.int32))
+    mx = C.c_int(0)
+    st = lib().oracle_sm_step(_p(img), _p(labels), H, W, C.byref(cfg), nbuf, _p(valid),
+                              _p(prior_count), _p(prop), _p(sample_sigma), int(max_spix),
+                              int(kind), int(direction), _p(shifted), _p(out["h"]),
+                              _p(out["pair"]), _p(out["want"]), _p(out["accept"]),
+                              _p(out["labels"]), C.byref(mx))
+    out["max_spix"] = mx.value
+    out["status"] = st
     return out

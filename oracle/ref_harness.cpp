@@ -2,7 +2,15 @@
 // cubins oracle/ref_build.py compiles from gauenk/st_spix st_spix/csrc/bist/*.cu,
 // unmodified, into oracle/_ref/) through the CUDA driver API, sequenced the way the
 // reference's host functions sequence them, on inputs supplied by the tests.  It is
-// how the CPU oracle is pinned against the reference itself on the GPU host.
+// how the CPU oracle and the engine are pinned against the reference itself on the
+// GPU host.
+//
+// Two layers:
+//   * stage functions (refh_find_border ... refh_rescale) that run one reference
+//     stage on host arrays, used by the stage pins;
+//   * a generic layer (refh_variant_load, refh_fn, refh_malloc, refh_launch, ...)
+//     over which oracle/ref_runner.py restates the reference's whole host drivers
+//     (run_bass, shift_and_fill, run_prop, main_loop) in Python.
 //
 // Host code here is this project's; it mirrors the reference's host loops:
 //   update_seg            update_seg.cu:281-311
@@ -355,6 +363,142 @@ int refh_rescale(const uint8_t* in, float* out, int npix, float mval) {
   if (launch(F_RESCALE, nblk(npix), 512, args)) return -1;
   CU(cuCtxSynchronize());
   CU(cuMemcpyDtoH(out, b.p, 12 * (size_t)npix));
+  return 0;
+}
+
+
+// ---------------------------------------------------------------------------------
+// Generic layer.  A "variant" is one directory of cubins (oracle/_ref for the
+// -fmad=false build, oracle/_ref/stock for nvcc's default contraction).  Kernels are
+// looked up by module and unmangled name from the functions the driver enumerates in
+// that module.  Every launch goes to the legacy default stream, as the reference's.
+// ---------------------------------------------------------------------------------
+namespace {
+struct Variant {
+  std::vector<std::string> names;
+  std::vector<CUmodule> mods;
+};
+std::vector<Variant> g_var;
+std::vector<CUfunction> g_gfn;
+std::vector<std::string> g_gfn_name;
+std::vector<CUevent> g_ev;
+}  // namespace
+
+// Load the cubins `units` (comma separated) from `dir`; returns the variant index.
+int refh_variant_load(const char* dir, const char* units) {
+  if (!g_ctx) { g_err = "refh_init first"; return -1; }
+  CU(cuCtxSetCurrent(g_ctx));
+  Variant v;
+  std::string all(units), cur;
+  for (size_t i = 0; i <= all.size(); i++) {
+    if (i == all.size() || all[i] == ',') {
+      if (!cur.empty()) {
+        CUmodule m;
+        std::string path = std::string(dir) + "/" + cur + ".cubin";
+        CU(cuModuleLoad(&m, path.c_str()));
+        v.names.push_back(cur);
+        v.mods.push_back(m);
+      }
+      cur.clear();
+    } else {
+      cur += all[i];
+    }
+  }
+  g_var.push_back(v);
+  return (int)g_var.size() - 1;
+}
+
+// Kernel `name` (unmangled) of `module` in variant `var`.  When the module holds
+// several kernels of that name, `mangled` (non-empty) picks one.  Returns a handle.
+int refh_fn(int var, const char* module, const char* name, const char* mangled) {
+  CU(cuCtxSetCurrent(g_ctx));
+  if (var < 0 || var >= (int)g_var.size()) { g_err = "bad variant"; return -1; }
+  Variant& v = g_var[var];
+  int mi = -1;
+  for (int i = 0; i < (int)v.names.size(); i++)
+    if (v.names[i] == module) mi = i;
+  if (mi < 0) { g_err = std::string("module not loaded: ") + module; return -1; }
+  unsigned n = 0;
+  CU(cuModuleGetFunctionCount(&n, v.mods[mi]));
+  std::vector<CUfunction> fs(n);
+  if (n) CU(cuModuleEnumerateFunctions(fs.data(), n, v.mods[mi]));
+  std::string prefix = "_Z" + std::to_string(strlen(name)) + name;
+  CUfunction hit = nullptr;
+  std::string hit_name, seen;
+  int hits = 0;
+  for (CUfunction f : fs) {
+    const char* nm = nullptr;
+    CU(cuFuncGetName(&nm, f));
+    if (!nm) continue;
+    std::string s(nm);
+    bool match = mangled && *mangled ? s == mangled : s.rfind(prefix, 0) == 0;
+    if (match) { hit = f; hit_name = s; hits++; seen += s + " "; }
+  }
+  if (hits != 1) {
+    g_err = std::string(module) + "." + name + ": " + std::to_string(hits) + " matches " + seen;
+    return -1;
+  }
+  g_gfn.push_back(hit);
+  g_gfn_name.push_back(hit_name);
+  return (int)g_gfn.size() - 1;
+}
+
+const char* refh_fn_name(int h) {
+  return (h >= 0 && h < (int)g_gfn_name.size()) ? g_gfn_name[h].c_str() : "";
+}
+
+unsigned long long refh_malloc(unsigned long long bytes) {
+  if (cuCtxSetCurrent(g_ctx) != CUDA_SUCCESS) return 0;
+  CUdeviceptr p = 0;
+  CUresult r = cuMemAlloc(&p, bytes ? bytes : 16);
+  if (r != CUDA_SUCCESS) { g_err = "cuMemAlloc failed"; return 0; }
+  return (unsigned long long)p;
+}
+int refh_free(unsigned long long p) { CU(cuMemFree((CUdeviceptr)p)); return 0; }
+int refh_memset8(unsigned long long p, unsigned v, unsigned long long n) {
+  CU(cuMemsetD8((CUdeviceptr)p, (unsigned char)v, n)); return 0;
+}
+int refh_memset32(unsigned long long p, unsigned v, unsigned long long n) {
+  CU(cuMemsetD32((CUdeviceptr)p, v, n)); return 0;
+}
+int refh_h2d(unsigned long long p, const void* h, unsigned long long n) {
+  CU(cuMemcpyHtoD((CUdeviceptr)p, h, n)); return 0;
+}
+int refh_d2h(void* h, unsigned long long p, unsigned long long n) {
+  CU(cuMemcpyDtoH(h, (CUdeviceptr)p, n)); return 0;
+}
+int refh_d2d(unsigned long long d, unsigned long long s, unsigned long long n) {
+  CU(cuMemcpyDtoD((CUdeviceptr)d, (CUdeviceptr)s, n)); return 0;
+}
+// Launch handle `h` on grid (gx, gy) x block (bx) with `nargs` arguments, each held in
+// one 8-byte slot (its value in the slot's low bytes, as the kernel's parameter type).
+int refh_launch(int h, unsigned gx, unsigned gy, unsigned bx, unsigned long long* slots,
+                int nargs) {
+  if (h < 0 || h >= (int)g_gfn.size()) { g_err = "bad kernel handle"; return -1; }
+  if (gx == 0 || gy == 0) return 0;  // an empty grid launches nothing
+  void* params[32];
+  if (nargs > 32) { g_err = "too many kernel arguments"; return -1; }
+  for (int i = 0; i < nargs; i++) params[i] = &slots[i];
+  CU(cuLaunchKernel(g_gfn[h], gx, gy, 1, bx, 1, 1, 0, nullptr, params, nullptr));
+  return 0;
+}
+int refh_sync() { CU(cuCtxSynchronize()); return 0; }
+// Events for timing reference kernels on the default stream.
+int refh_event_record(int i) {
+  while ((int)g_ev.size() <= i) {
+    CUevent e;
+    CU(cuEventCreate(&e, CU_EVENT_DEFAULT));
+    g_ev.push_back(e);
+  }
+  CU(cuEventRecord(g_ev[i], nullptr));
+  return 0;
+}
+int refh_event_ms(int a, int b, float* ms) {
+  if (a < 0 || b < 0 || a >= (int)g_ev.size() || b >= (int)g_ev.size()) {
+    g_err = "bad event index"; return -1;
+  }
+  CU(cuEventSynchronize(g_ev[b]));
+  CU(cuEventElapsedTime(ms, g_ev[a], g_ev[b]));
   return 0;
 }
 

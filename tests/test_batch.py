@@ -193,3 +193,30 @@ def test_laddered_steps_replay_graphs_with_the_oracle_labels():
                 np.testing.assert_array_equal(fr[0].labels.cpu().numpy(), ref[t])
         vs.close()
         assert ctx.graph_replays() > r0
+
+
+def test_uneven_batch_at_full_size_matches_oracle_and_plain_path():
+    """A subset of the 64-frame uneven batch at its real sizes (H, W uniform in
+    [240, 1080] rounded to multiples of 8, 100-800 seeds, noise 0.02-0.08, superpixel
+    size from {12, 16, 20, 25}, 20 iterations, split/merge every 10): 4 frames in one
+    batch give the oracle's labels and the plain per-frame path's, and each frame is
+    the same alone and in the batch."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    specs = []
+    for i in range(4):
+        H = int(rng.integers(240, 1081)) // 8 * 8
+        W = int(rng.integers(240, 1081)) // 8 * 8
+        specs.append((H, W, int(rng.integers(100, 801)), float(rng.uniform(0.02, 0.08)),
+                      int(rng.choice([12, 16, 20, 25])), 7000 + i))
+    imgs = [(synth.voronoi_frame(H, W, ns, sg, sd)[0], sp) for H, W, ns, sg, sp, sd in specs]
+    cfg = dict(niters=20, sm_period=10)
+    fr = [batch.Frame(img=cuda(img), sp_size=sp) for img, sp in imgs]
+    batch.process_batch(fr, **cfg)
+    for f, (img, sp) in zip(fr, imgs):
+        assert f.status == 0
+        st, lab, _, n = O.run_bass(img, O.default_config(sp_size=sp, **cfg))
+        assert st == 0 and f.nspix == n
+        np.testing.assert_array_equal(f.labels.cpu().numpy(), lab)
+        alone, p = bist_cuda.run_bass(cuda(img), sp_size=sp, **cfg)
+        np.testing.assert_array_equal(alone.cpu().numpy(), lab)
+        assert p.n == n

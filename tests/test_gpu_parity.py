@@ -236,3 +236,70 @@ def test_concurrent_streams_match_sequential():
     assert not err, err
     for i in range(4):
         np.testing.assert_array_equal(out[i], seq[i])
+
+
+def _log_tuple(lg):
+    return (lg.nsplits, lg.nmerges, lg.nrevived, lg.nminted, lg.near_ties)
+
+
+def test_run_bass_config0_decisions_fire_and_match_the_oracle():
+    """Config 0 with the reference's own period (split at idx % 4 == 0, merge at 2): the
+    split and merge paths fire, and the counts of accepted splits / merges equal the
+    oracle's."""
+    from st_spix_gb300 import synth
+    img, _ = synth.config0()
+    glab, gp = bist_cuda.run_bass(cuda(img), niters=100, sm_period=4)
+    glog = _log_tuple(bist_cuda.frame_log())
+    st, olab, op, n = O.run_bass(img, ocfg(niters=100, sm_period=4))
+    assert st == 0 and gp.n == n
+    np.testing.assert_array_equal(glab.cpu().numpy(), olab)
+    assert glog == _log_tuple(O.last_log())
+    assert glog[0] > 0 and glog[1] > 0, glog
+
+
+def test_propagated_chain_relabels_fire_and_match_the_oracle():
+    """A fast-moving video (shifts up to 6 px per frame) frame by frame through
+    shift_and_fill + run_prop with the reference's 4/8/12 ladder: labels identical to
+    the oracle on every frame, and revivals, new ids, splits and merges all occur."""
+    from st_spix_gb300 import synth
+    vid, flows, _ = synth.voronoi_video(120, 160, 8, 30, 0.05, 1, max_shift=6.0)
+    st, olab, op, n = O.run_bass(vid[0], ocfg(niters=20))
+    assert st == 0
+    glab, gp = bist_cuda.run_bass(cuda(vid[0]), niters=20)
+    np.testing.assert_array_equal(glab.cpu().numpy(), olab)
+    totals = np.zeros(5, np.int64)
+    for t in range(1, vid.shape[0]):
+        gf, gs = bist_cuda.shift_and_fill(glab, gp, cuda(flows[t - 1]))
+        st, of, osh, opu = O.shift_and_fill(olab, op, n, flows[t - 1])
+        assert st == 0
+        np.testing.assert_array_equal(gs.cpu().numpy(), osh)
+        np.testing.assert_array_equal(gf.cpu().numpy(), of)
+        hole = float((osh < 0).mean())
+        niters = 12 if hole > 0.20 else (4 if hole < 0.01 else 8)
+        glab, gp = bist_cuda.run_prop(cuda(vid[t]), niters, gf, gs, gp)
+        glog = _log_tuple(bist_cuda.frame_log())
+        st, olab, op, n = O.run_prop(vid[t], ocfg(), niters, of, osh, opu, n)
+        assert st == 0 and gp.n == n
+        np.testing.assert_array_equal(glab.cpu().numpy(), olab)
+        assert glog == _log_tuple(O.last_log()), (t, glog)
+        compare_params(gp.as_dict(), op)
+        totals += np.array(glog)
+    assert totals[0] > 0 and totals[1] > 0 and totals[2] > 0 and totals[3] > 0, totals
+
+
+def test_streaming_workload_size_matches_the_oracle():
+    """The streaming workload at full size (480x854, 400 seeds, 20 iterations,
+    split/merge every 10, 20 iterations on propagated frames), first 3 frames through
+    bist_forward, against the oracle; the last frame's decisions fire."""
+    from st_spix_gb300 import synth
+    vid, flows, _ = synth.config1(0, T=3)
+    out = bist_cuda.bist_forward(cuda(vid), cuda(flows), 20, 20, 0.5, 0.009 ** 2,
+                                 float(np.log(0.5)), 0.0, True, False, sm_period=10,
+                                 prop_niters=20)
+    glog = _log_tuple(bist_cuda.frame_log())
+    st, ref, _ = O.bist_forward(vid, flows, ocfg(niters=20, sp_size=20, sm_period=10,
+                                                 prop_niters=20), True)
+    assert st == 0
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+    assert glog == _log_tuple(O.last_log())
+    assert glog[0] > 0 and glog[1] > 0, glog

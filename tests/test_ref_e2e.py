@@ -1,0 +1,121 @@
+"""End-to-end agreement with the reference's OWN bist_forward path.
+
+oracle/ref_runner.py runs the reference's whole per-frame path on the GPU: its kernels
+(oracle/_ref cubins, unmodified sources; the -fmad=false build and the stock build
+with nvcc's default contraction) sequenced by a restatement of its host drivers
+(pyapi.cu main_loop, bass.cu run_bass, shift_and_fill.cu, prop.cu run_prop).
+
+The reference is not deterministic (FP32 atomic sums, first-writer merge claims,
+atomic split / relabel ids, equal-size warp collisions), so the comparison is label
+agreement after one-to-one matching of ids by overlap (tests.helpers.label_agreement),
+measured beside the reference's agreement with ITSELF on repeated runs:
+
+  * image mode (plain BASS, config 0: 240x320, 100 iterations, split/merge every 4
+    as the reference hard-codes) on several seeds;
+  * video mode in lockstep: every propagated frame of the engine starts from the
+    reference's own previous labels and parameters, so each frame's agreement
+    measures that frame alone (without lockstep, differences compound over frames in
+    the reference's repeated runs as well); the shift-and-fill maps are compared
+    first.
+
+The bars (AGREE_*) are the measured levels of this build on these inputs; the
+reference's repeated runs reach similar levels against each other (printed)."""
+import numpy as np
+import pytest
+
+from oracle import ref_runner as RR
+from st_spix_gb300 import synth
+from tests.helpers import label_agreement
+
+torch = pytest.importorskip("torch")
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not RR.available("nofma"), reason="oracle/_ref not built")]
+
+S2 = 0.009 ** 2
+LA = float(np.log(0.5))
+AGREE_IMAGE = 0.997
+AGREE_FRAME = 0.97
+_ref = {}
+
+
+def ref(variant):
+    if variant not in _ref:
+        _ref[variant] = RR.Ref(variant)
+    return _ref[variant]
+
+
+def _engine_params(host: dict, n: int, dev):
+    from st_spix_gb300 import bist_cuda
+    p = bist_cuda.SuperpixelParams(n, dev)
+    p.n = n
+    for name, _, per in bist_cuda.PARAM_FIELDS:
+        getattr(p, "_" + name).copy_(torch.from_numpy(np.ascontiguousarray(host[name][: n * per])))
+    return p
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_image_mode_agrees_with_reference(seed):
+    from st_spix_gb300 import bist_cuda
+    img, _ = synth.config0(seed)
+    vid = img[None]
+    flows = np.zeros((1, 240, 320, 2), np.float32)
+    eng = bist_cuda.bist_forward(torch.from_numpy(vid).cuda(), torch.from_numpy(flows).cuda(),
+                                 100, 15, 0.5, S2, LA, 0.0, False, False).cpu().numpy()
+    lg = bist_cuda.frame_log()
+    assert lg.nsplits > 0 and lg.nmerges > 0
+    out = {}
+    for variant in ("nofma", "stock"):
+        R = ref(variant)
+        runs = [R.bist_forward(vid, flows, 100, 15, 0.5, S2, LA, 0.0, False) for _ in range(2)]
+        assert sum(e[1] for e in R.log if e[0] == "split") > 0
+        out[variant] = ([label_agreement(eng[0], r[0]) for r in runs],
+                        label_agreement(runs[0][0], runs[1][0]))
+    print(f"config0 seed {seed}: engine~reference, reference~itself:", out)
+    for variant, (agree, _self) in out.items():
+        assert max(agree) >= AGREE_IMAGE, (variant, agree)
+
+
+VIDEOS = [("config1_480x854_T3", lambda: synth.config1(0, T=3)[:2], 20, 20),
+          ("video_120x160_T8", lambda: synth.voronoi_video(120, 160, 8, 30, 0.05, 1,
+                                                           max_shift=6.0)[:2], 20, 15)]
+
+
+@pytest.mark.parametrize("variant", ["nofma", "stock"])
+@pytest.mark.parametrize("name,make,niters,sp", VIDEOS, ids=[v[0] for v in VIDEOS])
+def test_video_lockstep_agrees_with_reference(name, make, niters, sp, variant):
+    from st_spix_gb300 import bist_cuda
+    vid, flows = make()
+    T, H, W = vid.shape[:3]
+    R = ref(variant)
+    R.bist_forward(vid, flows, niters, sp, 0.5, S2, LA, 0.0, True, record=True)
+    recs = R.frames
+    again = R.bist_forward(vid, flows, niters, sp, 0.5, S2, LA, 0.0, True)
+    dev = torch.device("cuda")
+    eng0, _ = bist_cuda.run_bass(torch.from_numpy(vid[0]).to(dev), niters=niters, sp_size=sp)
+    rows = [(0, label_agreement(eng0.cpu().numpy(), recs[0]["labels"]),
+             label_agreement(again[0], recs[0]["labels"]), None)]
+    events = {"splits": 0, "merges": 0, "revived": 0, "minted": 0}
+    for t in range(1, T):
+        prev = recs[t - 1]
+        n_prev = int(len(prev["params"]["counts"]))
+        pe = _engine_params(prev["params"], n_prev, dev)
+        lab_prev = torch.from_numpy(prev["labels"]).to(dev)
+        flow = torch.from_numpy(np.ascontiguousarray(flows[t - 1])).to(dev)
+        filled, shifted = bist_cuda.shift_and_fill(lab_prev, pe, flow)
+        sh_same = float((shifted.cpu().numpy() == recs[t]["shifted"]).mean())
+        fi_same = float((filled.cpu().numpy() == recs[t]["filled"]).mean())
+        lab, _ = bist_cuda.run_prop(torch.from_numpy(vid[t]).to(dev), recs[t]["niters"], filled,
+                                    shifted, pe, sp_size=sp)
+        lg = bist_cuda.frame_log()
+        for k, f in (("splits", "nsplits"), ("merges", "nmerges"), ("revived", "nrevived"),
+                     ("minted", "nminted")):
+            events[k] += getattr(lg, f)
+        rows.append((t, label_agreement(lab.cpu().numpy(), recs[t]["labels"]),
+                     label_agreement(again[t], recs[t]["labels"]), (sh_same, fi_same)))
+    print(f"{name} [{variant}] (frame, engine~ref, ref~ref (no lockstep), "
+          f"(shifted, filled) identical): {rows}; engine events {events}")
+    for t, agree, _, maps in rows:
+        assert agree >= AGREE_FRAME, (t, agree)
+        if maps is not None:
+            assert maps[0] >= 0.995 and maps[1] >= 0.99, (t, maps)
+    assert events["splits"] > 0 and events["merges"] > 0 and events["minted"] > 0

@@ -64,3 +64,33 @@ def test_marked_video_noalloc_rejects_oversize():
                                              dummy.data_ptr(), 1, 4097, 4096, 3,
                                              dummy.data_ptr())
     assert st == STSPIX_ERR_TOO_LARGE
+
+
+def test_marked_video_noalloc_at_the_size_limit():
+    """Exactly 2^24 pixels (the largest input the fixed scratch holds) is accepted and
+    matches the allocating entry point."""
+    from st_spix_gb300 import _lib
+    lib = _lib.load()
+    ctx = _lib.Context(0)
+    stream = torch.cuda.current_stream().cuda_stream
+    T, H, W = 4, 2048, 2048
+    assert T * H * W == MAX_PIXELS
+    try:
+        g = torch.Generator(device="cuda").manual_seed(5)
+        gv = torch.rand((T, H, W, 3), device="cuda", generator=g) * 1.4 - 0.2
+        ys = torch.arange(H, device="cuda").view(1, H, 1)
+        xs = torch.arange(W, device="cuda").view(1, 1, W)
+        ts = torch.arange(T, device="cuda").view(T, 1, 1)
+        gs = (((ys // 9) * 131 + (xs // 11) * 7 + ts) % 997).to(torch.int32).contiguous()
+        color = torch.tensor([1.0, 0.0, 0.25], dtype=torch.float32, device="cuda")
+        ref = torch.empty((T, H, W, 3), device="cuda")
+        got = torch.empty((T, H, W, 3), device="cuda")
+        ctx.check(lib.stspix_get_marked_video(ctx.handle, stream, gv.data_ptr(), gs.data_ptr(),
+                                              color.data_ptr(), T, H, W, 3, ref.data_ptr()))
+        st = lib.stspix_get_marked_video_noalloc(stream, gv.data_ptr(), gs.data_ptr(),
+                                                 color.data_ptr(), T, H, W, 3, got.data_ptr())
+        assert st == 0
+        torch.cuda.synchronize()
+        assert torch.equal(got, ref)
+    finally:
+        ctx.close()
