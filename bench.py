@@ -38,6 +38,12 @@ WORKLOAD = dict(name="bist_stream_480x854_T30", H=480, W=854, T=30, nseeds=400, 
 # (image 12 + labels 4) = 96 B/px, the BASS pass of the scope's measurement rules;
 # per sweep launch on average 24 B/px.
 SWEEP_BYTES_PER_PX = 24
+# DRAM bytes (read + write) per sweep launch from one ncu capture of the same workload
+# (a batch of 8 frames, mean of a full and an active-set sweep); a constant of that
+# capture, re-taken whenever the sweep kernel changes, not a live measurement.
+SWEEP_TRAFFIC_NCU = dict(bytes_per_launch=37055104,
+                         source="ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                "profiles/kb_sweep_bist_stream_480x854_T30.md")
 METRIC = "streamed frames/sec"
 
 
@@ -51,68 +57,111 @@ def gen_video(seed: int, T: int = None):
 
 # ---------------------------------------------------------------------------
 # CPU leg: the oracle (CPU restatement of the reference path), one stream per
-# worker process, a bounded number of frames per stream.
-_worker_data = {}
-
-
-def _cpu_worker(args):
-    seed, nframes = args
-    import numpy as np
-    from oracle import oracle as O
-    key = (seed, nframes)
-    if key not in _worker_data:
-        _worker_data[key] = gen_video(seed, T=nframes)
-    vid, flows = _worker_data[key]
+# worker process.  Each step runs the next `window` frames of every worker's stream
+# (frame 0 plain BASS, frames 1..T-1 propagated; a stream restarts after its last
+# frame), so consecutive steps walk the streaming workload's frame mix.
+def workload_config() -> dict:
+    """The `config` of both arms' bench lines: the streaming workload itself (the same
+    dict on the GPU arm and the reference arm; run details go under "run")."""
     w = WORKLOAD
-    cfg = O.default_config(niters=w["niters"], sp_size=w["sp_size"], prop_niters=w["prop_niters"],
-                           sm_period=w["sm_period"], potts=w["potts"],
-                           sigma2_app=w["sigma2_app"], alpha_hastings=w["alpha"])
-    t = time.perf_counter()
-    st, out, _ = O.bist_forward(vid, flows, cfg, True)
-    dt = time.perf_counter() - t
-    assert st == 0
-    return nframes, dt, int(np.unique(out[-1]).size)
+    return {"workload": w["name"], "H": w["H"], "W": w["W"], "T": w["T"],
+            "nseeds": w["nseeds"], "sigma": w["sigma"], "sp_size": w["sp_size"],
+            "niters": w["niters"], "prop_niters": w["prop_niters"], "sm_period": w["sm_period"],
+            "frame_mix": "per stream: frame 0 plain BASS, frames 1-%d propagated" % (w["T"] - 1),
+            "l2": "inputs larger than L2: a %dx%d frame and its flow take %.1f MB and a step "
+                  "reads every frame of every stream it runs" %
+                  (w["H"], w["W"], w["H"] * w["W"] * 20 / 1e6)}
+
+
+def _cpu_config():
+    from oracle import oracle as O
+    w = WORKLOAD
+    return O.default_config(niters=w["niters"], sp_size=w["sp_size"], prop_niters=w["prop_niters"],
+                            sm_period=w["sm_period"], potts=w["potts"],
+                            sigma2_app=w["sigma2_app"], alpha_hastings=w["alpha"])
+
+
+def _cpu_stream_loop(seed, conn):
+    """Worker process: owns one stream; each request runs its next `window` frames."""
+    from oracle import oracle as O
+    O.lib()
+    vid, flows = gen_video(seed)
+    cfg = _cpu_config()
+    w = WORKLOAD
+    t, prev = 0, None
+    conn.send(("ready", 0, 0.0))
+    while True:
+        msg = conn.recv()
+        if msg is None:
+            break
+        window = int(msg)
+        t0 = time.perf_counter()
+        for _ in range(window):
+            if t == 0:
+                rc, lab, params, n = O.run_bass(vid[0], cfg)
+            else:
+                lab_prev, params_prev, n_prev = prev
+                rc, filled, shifted, pp = O.shift_and_fill(lab_prev, params_prev, n_prev,
+                                                           flows[t - 1])
+                if rc == 0:
+                    rc, lab, params, n = O.run_prop(vid[t], cfg, w["prop_niters"], filled,
+                                                    shifted, pp, n_prev)
+            if rc != 0:
+                conn.send(("error", rc, 0.0))
+                return
+            prev = (lab, params, n)
+            t = (t + 1) % w["T"]
+        conn.send(("ok", window, time.perf_counter() - t0))
 
 
 class CpuBaseline:
-    """Pool of spawned workers (one per host core) running the oracle."""
+    """One spawned process per host core, each owning one stream of the workload and
+    running the oracle on the next `window` frames of it per step."""
 
-    def __init__(self, frames_per_stream: int = 3):
+    def __init__(self, window: int = 3):
         import multiprocessing as mp
         from oracle import oracle as O
         O.build()
         self.cores = os.cpu_count() or 1
-        self.frames = frames_per_stream
-        self.pool = mp.get_context("spawn").Pool(self.cores)
-        # generate each worker's stream once
-        self.pool.map(_cpu_worker_warm, [(s, self.frames) for s in range(self.cores)])
+        self.window = window
+        ctx = mp.get_context("spawn")
+        self.conns, self.procs = [], []
+        for s in range(self.cores):
+            a, b = ctx.Pipe()
+            pr = ctx.Process(target=_cpu_stream_loop, args=(s, b), daemon=True)
+            pr.start()
+            self.conns.append(a)
+            self.procs.append(pr)
+        for c in self.conns:
+            c.recv()
 
     def step(self):
         t = time.perf_counter()
-        res = self.pool.map(_cpu_worker, [(s, self.frames) for s in range(self.cores)])
-        wall = time.perf_counter() - t
-        frames = sum(r[0] for r in res)
-        return frames, wall
+        for c in self.conns:
+            c.send(self.window)
+        frames = 0
+        for c in self.conns:
+            kind, n, _ = c.recv()
+            if kind != "ok":
+                raise RuntimeError("CPU baseline worker failed with status %d" % n)
+            frames += n
+        return frames, time.perf_counter() - t
 
     def close(self):
-        self.pool.close()
-        self.pool.join()
+        for c in self.conns:
+            try:
+                c.send(None)
+            except (BrokenPipeError, OSError):
+                pass
+        for pr in self.procs:
+            pr.join(timeout=30)
 
     def describe(self):
         w = WORKLOAD
-        return (f"{self.cores} concurrent streams x first {self.frames} frames "
-                f"(1 BASS + {self.frames - 1} propagated) of the {w['H']}x{w['W']} workload, "
-                f"oracle (CPU restatement), one process per core")
-
-
-def _cpu_worker_warm(args):
-    seed, nframes = args
-    key = (seed, nframes)
-    if key not in _worker_data:
-        _worker_data[key] = gen_video(seed, T=nframes)
-    from oracle import oracle as O
-    O.lib()
-    return 0
+        return (f"{self.cores} concurrent streams of the {w['H']}x{w['W']}x{w['T']} workload, "
+                f"one process per core, each step the next {self.window} frames of every "
+                f"stream (frame 0 plain BASS, frames 1-{w['T'] - 1} propagated, a stream "
+                f"restarts after frame {w['T'] - 1}), oracle (CPU restatement)")
 
 
 # ---------------------------------------------------------------------------
@@ -168,21 +217,6 @@ def read_peaks():
         return 6800.0, "fallback"
 
 
-def read_traffic(workload: str):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary
-    (profiles/<kernel>_<workload>.md, line 'traffic_bytes_per_launch: N')."""
-    d = os.path.join(ROOT, "profiles")
-    if not os.path.isdir(d):
-        return None
-    for fn in sorted(os.listdir(d)):
-        if workload in fn and fn.endswith(".md"):
-            for ln in open(os.path.join(d, fn)):
-                if ln.startswith("traffic_bytes_per_launch:"):
-                    try:
-                        return float(ln.split(":", 1)[1])
-                    except ValueError:
-                        return None
-    return None
 
 
 def max_over_ranks(x: float, world: int, device=None) -> float:
@@ -215,7 +249,7 @@ def run_reference(args, world, rank):
     reference itself has no CPU path) on all host cores, same metric and config."""
     if rank != 0:
         return
-    base = CpuBaseline(frames_per_stream=3)
+    base = CpuBaseline(window=3)
     try:
         for _ in range(args.warmup):
             base.step()
@@ -231,9 +265,8 @@ def run_reference(args, world, rank):
                 "ms_per_step": 1000 * wall / max(args.steps, 1), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64+int64",
                 "data": "synthetic",
-                "config": {"workload": w["name"], "H": w["H"], "W": w["W"], "T": w["T"],
-                           "sp_size": w["sp_size"], "niters": w["niters"],
-                           "sm_period": w["sm_period"]},
+                "config": workload_config(),
+                "run": {"sample": base.describe(), "cores": base.cores},
                 "cpu_baseline": {"value": v, "unit": "frames/s", "cores": base.cores,
                                  "kind": "port", "sample": base.describe()},
                 "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
@@ -247,21 +280,19 @@ SERVE = dict(name="serve_mixed_360p720p1080p_poisson30", mix=(0.4, 0.4, 0.2), T=
              budget_gb=120, pool=3, streams=256)
 
 
-def run_serve(args, world, rank):
-    """--mode serve: the serving form on a mixed-resolution stream set (360p / 720p /
-    1080p at 0.4 / 0.4 / 0.2, each stream a video generated as the streaming
-    workload with its own Poisson 30 fps arrivals), admitted under a 120 GB budget
-    and served by continuous batching; the plain per-frame path (bist_forward, one
-    frame at a time) is timed on a sample of the same set."""
-    import numpy as np
+def serve_leg(args, dev, rank, streams, frames, fps, lanes=None, max_batch=None,
+              group_sizes=True, max_pixels=0):
+    """The serving form on a mixed-resolution stream set (360p / 720p / 1080p at 0.4 /
+    0.4 / 0.2, each stream a video generated as the streaming workload with its own
+    Poisson `fps` arrivals), admitted under a 120 GB budget and served by continuous
+    batching; the plain per-frame path (bist_forward, one frame at a time) is timed on
+    one stream per resolution of the same set and weighted by the set's mix.  Returns
+    the serving statistics, the plain figure and the clocks seen while serving."""
     import torch
     from st_spix_gb300 import bist_cuda, serve, synth
 
-    torch.cuda.set_device(args.local)
-    dev = torch.device("cuda", args.local)
-    w, sv = WORKLOAD, dict(SERVE, fps=args.fps, T=args.frames)
-    S = args.streams
-    res = synth.stream_resolution_mix(S, seed=rank)
+    w, sv = WORKLOAD, dict(SERVE, fps=fps, T=frames)
+    res = synth.stream_resolution_mix(streams, seed=rank)
     cfg = dict(niters=w["niters"], sp_size=w["sp_size"], potts=w["potts"],
                sigma2_app=w["sigma2_app"], alpha=w["alpha"], split_alpha=w["split_alpha"],
                sm_period=w["sm_period"], prop_niters=w["prop_niters"])
@@ -292,9 +323,9 @@ def run_serve(args, world, rank):
         plain_s += n_hw * dt
     plain_fps = plain_frames / plain_s
     budget = int(sv["budget_gb"] * 2 ** 30)
-    srv = serve.Server(budget, max_batch=args.max_batch, lanes=args.lanes, device=dev,
-                       seed=rank, max_pixels=args.max_pixels,
-                       group_sizes=not args.no_group_sizes, **cfg)
+    srv = serve.Server(budget, max_batch=max_batch or args.max_batch,
+                       lanes=lanes or args.lanes, device=dev, seed=rank,
+                       max_pixels=max_pixels, group_sizes=group_sizes, **cfg)
     # warm-up run (untimed): two short streams per resolution, so that the lanes'
     # engine contexts exist and the sweep tile classes are tuned
     for j, hw in enumerate(sorted(pool) * 2):
@@ -311,28 +342,60 @@ def run_serve(args, world, rank):
     st = srv.run()
     stop.set()
     th.join(timeout=5)
+    hist = {f"{h}p": sum(1 for r in res if r[0] == h) for h in sorted(set(r[0] for r in res))}
+    return {"serving": st, "plain_per_frame_fps": plain_fps,
+            "served_vs_plain": st["frames_per_s"] / plain_fps, "streams_by_height": hist,
+            "offered_fps": streams * sv["fps"], "clocks": summarize_clocks(clk_lines)}
+
+
+def run_serve(args, world, rank):
+    """--mode serve: the serving form (serve_leg) on SERVE's stream set."""
+    import torch
+
+    torch.cuda.set_device(args.local)
+    dev = torch.device("cuda", args.local)
+    w, sv = WORKLOAD, dict(SERVE, fps=args.fps, T=args.frames)
+    S = args.streams
+    leg = serve_leg(args, dev, rank, S, sv["T"], sv["fps"],
+                    group_sizes=not args.no_group_sizes, max_pixels=args.max_pixels)
+    st = leg["serving"]
     if rank != 0:
         return
-    hist = {f"{h}p": sum(1 for r in res if r[0] == h) for h in sorted(set(r[0] for r in res))}
     line = {
         "metric": "served frames/sec (mixed 360p/720p/1080p streams)", "value": st["frames_per_s"],
         "unit": "frames/s", "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": 1000 * st["wall_s"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/f64+int64", "data": "synthetic",
-        "config": {"workload": sv["name"], "streams": S, "streams_by_height": hist,
+        "config": {"workload": sv["name"], "streams": S,
+                   "streams_by_height": leg["streams_by_height"],
                    "frames_per_stream": sv["T"], "arrivals": "Poisson %.0f fps per stream" % sv["fps"],
-                   "offered_fps": S * sv["fps"], "budget_gb": sv["budget_gb"],
+                   "offered_fps": leg["offered_fps"], "budget_gb": sv["budget_gb"],
                    "max_batch": args.max_batch, "max_pixels": args.max_pixels,
                    "group_sizes": not args.no_group_sizes,
                    "lanes": args.lanes, "warmup": "2 streams x 4 frames per resolution, untimed",
                    "sp_size": w["sp_size"], "niters": w["niters"], "prop_niters": w["prop_niters"],
                    "sm_period": w["sm_period"]},
         "serving": st,
-        "plain_per_frame_fps": plain_fps,
-        "served_vs_plain": st["frames_per_s"] / plain_fps,
-        "clocks": summarize_clocks(clk_lines),
+        "plain_per_frame_fps": leg["plain_per_frame_fps"],
+        "served_vs_plain": leg["served_vs_plain"],
+        "clocks": leg["clocks"],
     }
     print(json.dumps(line), flush=True)
+
+
+def serving_summary(leg: dict, label: str) -> dict:
+    """The serving figures the default bench line carries for one load."""
+    st = leg["serving"]
+    bh = st.get("by_height", {})
+    return {"load": label, "streams_by_height": leg["streams_by_height"],
+            "offered_fps": leg["offered_fps"], "served_fps": st.get("frames_per_s"),
+            "frames": st.get("frames"), "plain_per_frame_fps": leg["plain_per_frame_fps"],
+            "served_vs_plain": leg["served_vs_plain"],
+            "p50_ms": st.get("p50_ms"), "p99_ms": st.get("p99_ms"),
+            "p50_720p_ms": bh.get("720p", {}).get("p50_ms"),
+            "p99_720p_ms": bh.get("720p", {}).get("p99_ms"),
+            "by_height": bh, "mean_batch": st.get("mean_batch"),
+            "clocks": leg["clocks"]}
 
 
 BATCH = dict(name="batch64_uneven_240to1080", n=64, lo=240, hi=1080, seeds=(100, 800),
@@ -727,6 +790,10 @@ def main():
                     help="serve: batches take frames oldest first across sizes (default: the "
                          "oldest frame's size first)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="stream: skip the serving figures (config-3 load and the sustained load)")
+    ap.add_argument("--serve-frames", type=int, default=10,
+                    help="stream: frames per stream of the config-3 serving leg (bounds its time)")
     ap.add_argument("--no-batch-graphs", action="store_true",
                     help="stream: launch every batch step's kernels one by one (ncu lists no "
                          "kernel of a graph that holds conditional nodes)")
@@ -967,6 +1034,22 @@ def main():
     e2e_elapsed = max_over_ranks(e2e_elapsed, world, dev)
     e2e_value = frames_total / e2e_elapsed
 
+    # ---- serving form on the mixed-resolution set: config-3 load (256 streams, Poisson
+    # 30 fps, frames per stream bounded) and the largest load it sustains (streams at
+    # 30 fps offering 85 % of the rate served under the config-3 backlog) -------------
+    serving = None
+    if not args.no_serve and world == 1:
+        full = serve_leg(args, dev, rank, SERVE["streams"], args.serve_frames, SERVE["fps"])
+        served = full["serving"].get("frames_per_s") or 0.0
+        n_sus = max(1, int(0.85 * served / SERVE["fps"]))
+        sus = serve_leg(args, dev, rank, n_sus, WORKLOAD["T"], SERVE["fps"])
+        serving = {"config3": serving_summary(full, "256 streams, Poisson 30 fps each, %d frames "
+                                               "per stream" % args.serve_frames),
+                   "sustained": serving_summary(sus, "%d streams, Poisson 30 fps each, %d frames "
+                                                "per stream (85%% of the config-3 served rate)"
+                                                % (n_sus, WORKLOAD["T"])),
+                   "target": "served / plain >= 5 and 720p p99 < 10 ms"}
+
     if rank != 0:
         if world > 1:
             import torch.distributed as dist
@@ -982,17 +1065,16 @@ def main():
     peak, peak_kind = read_peaks()
     per_launch = SWEEP_BYTES_PER_PX * npix * B0
     achieved = per_launch * nsweep / (sweep_ms / 1000.0) / 1e9 if sweep_ms else 0
-    traffic = read_traffic(w["name"])
     passes_per_video = w["niters"] + (T - 1) * w["prop_niters"]
     mpix_pass = world * S * args.steps * passes_per_video * npix / elapsed / 1e6
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        base = CpuBaseline(frames_per_stream=3)
+        base = CpuBaseline(window=3)
         try:
-            f, wall = base.step()
-            cpu = {"value": f / wall, "unit": "frames/s", "cores": base.cores, "kind": "port",
-                   "sample": base.describe()}
+            cpu_frames, cpu_wall = base.step()
+            cpu = {"value": cpu_frames / cpu_wall, "unit": "frames/s", "cores": base.cores,
+                   "kind": "port", "sample": base.describe()}
         finally:
             base.close()
 
@@ -1004,17 +1086,14 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32/f64+int64", "data": "synthetic",
-        "config": {"workload": w["name"], "H": w["H"], "W": w["W"], "T": w["T"],
-                   "sp_size": w["sp_size"], "niters": w["niters"],
-                   "prop_niters": w["prop_niters"], "sm_period": w["sm_period"],
-                   "streams_per_gpu": S, "lanes": NL, "batch_per_lane": B0,
+        "config": workload_config(),
+        "run": {"streams_per_gpu": S, "lanes": NL, "batch_per_lane": B0,
                    "sweep_schedule": args.sweep_schedule, "sweep_tile": args.sweep_tile,
                    "batch_graphs": not args.no_batch_graphs,
                    "step": "all %d frames of every stream; frame t of a lane's streams is "
                            "one batch" % T,
                    "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2: %d MB of frames+flow read per step" %
-                         (h_bytes // 2 ** 20)},
+                   "inputs_mb_per_step": h_bytes // 2 ** 20},
         "p50_frame_ms": pct(0.50), "p99_frame_ms": pct(0.99),
         "latency_720p": lat720,
         "latency_note": "frame latency = GPU time of the batch the frame ran in",
@@ -1023,7 +1102,8 @@ def main():
         "mpix_per_s_per_pass": mpix_pass,
         "roofline": {"bound": "hbm", "kernel": "kb_sweep (border + 4 parity phases, batched; statistics fused into the last sweep of each update)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "frac": achieved / peak if peak else None, "traffic": SWEEP_TRAFFIC_NCU["bytes_per_launch"],
+                     "traffic_source": SWEEP_TRAFFIC_NCU["source"],
                      "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": per_launch,
                      "dominant_family": fam,
@@ -1042,6 +1122,7 @@ def main():
                   "done %.1f ms, threads joined %.1f ms after the start, %d steps)" %
                   (1000 * wall / args.steps, 1000 * max(lane_done), 1000 * t_joined, args.steps),
         "clocks": summarize_clocks(clk_lines),
+        "serving": serving,
         "quality": dict({k: qual[k] for k in ("tex", "szv", "ev", "ev3d", "pooling", "ue2d",
                                               "sa2d", "ue3d", "sa3d", "spnum", "ave_nsp")},
                         stream=0, ground_truth="generator regions (%d)" % w["nseeds"],

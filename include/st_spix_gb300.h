@@ -180,7 +180,8 @@ int stspix_bist_forward(stspix_ctx* ctx, void* stream,
                         int32_t* spix_out);
 
 /* get_marked_video: border (find_border_pixels_end) painted with `color`
- * (3 floats, device), elsewhere the frame clipped to [0,1].                      */
+ * (3 floats, device), elsewhere the frame clipped to [0,1].  Frames have 3
+ * channels (nftrs != 3 returns STSPIX_ERR_ARG).                                  */
 int stspix_get_marked_video(stspix_ctx* ctx, void* stream,
                             const float* vid, const int32_t* spix,
                             const float* color, int T, int H, int W, int nftrs,
@@ -188,13 +189,15 @@ int stspix_get_marked_video(stspix_ctx* ctx, void* stream,
 
 /* get_marked_video without any allocation.  No counterpart in the reference: it is
  * for callers that must not allocate device memory while they run (a process that
- * reserves its GPU memory up front, code inside someone else's stream capture, a
+ * reserves its GPU memory up front, a plugin whose host owns every allocation, a
  * real-time loop).  The border-mask scratch lives in a 16 MiB array compiled into
  * the library (held on every GPU that loads it until exit); T*H*W above 2^24 pixels
- * returns STSPIX_ERR_TOO_LARGE.  No context is needed; it runs on `stream` on the
- * current device.  All calls share that one array, so calls that overlap on the GPU
- * race and must be serialised by the caller.  The first call on a device looks up
- * the array's address; make it before any stream capture.                      */
+ * returns STSPIX_ERR_TOO_LARGE.  Frames have 3 channels (else STSPIX_ERR_ARG).  No
+ * context is needed; it runs on `stream`, which must belong to the current device
+ * (else STSPIX_ERR_ARG).  All calls share that one array, so calls that overlap on
+ * the GPU race and must be serialised by the caller.  The first call on a device
+ * looks up the array's address and caches it for the process; make it before any
+ * stream capture, and do not use the entry point across a cudaDeviceReset.       */
 int stspix_get_marked_video_noalloc(void* stream, const float* vid, const int32_t* spix,
                                     const float* color, int T, int H, int W, int nftrs,
                                     float* marked_out);

@@ -1926,6 +1926,19 @@ int stspix_video_load(stspix_video* v, void* stream, const void* host, long long
                 v->H, v->W);
   if (h.n < 0 || bytes < snap_bytes(h.H, h.W, h.n))
     return fail(ctx, STSPIX_ERR_ARG, "snapshot truncated");
+  if (h.frames > 0) {
+    // later propagation and statistics kernels index the parameter arrays by these
+    // labels, so a corrupt or mismatched snapshot is refused before anything is copied
+    const int32_t* lab = (const int32_t*)((const char*)host + sizeof h);
+    const size_t np = (size_t)h.H * h.W;
+    for (size_t i = 0; i < np; i++) {
+      int32_t l;
+      memcpy(&l, lab + i, 4);
+      if (l < -1 || l >= h.n)
+        return fail(ctx, STSPIX_ERR_ARG, "snapshot label %d at pixel %zu outside [-1, %d)", l, i,
+                    h.n);
+    }
+  }
   cudaSetDevice(ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
   v->n = 0;  // nothing to keep while growing

@@ -1,9 +1,9 @@
 // Allocation-free variant of get_marked_video (stspix_get_marked_video_noalloc).
 //
 // Some callers cannot allocate device memory at call time: a process that reserves
-// all of its GPU memory up front and forbids later cudaMalloc, code running inside
-// a stream capture owned by another library, or a real-time loop where an
-// allocation (and the device synchronisation cudaFree implies) is not allowed.
+// all of its GPU memory up front and forbids later cudaMalloc, a plugin whose host
+// application owns every device allocation, or a real-time loop where an allocation
+// (and the device synchronisation cudaFree implies) is not allowed.
 // stspix_get_marked_video needs a one-byte-per-pixel border mask as scratch; this
 // variant keeps that scratch in a fixed array compiled into the library instead.
 //
@@ -16,7 +16,12 @@
 //    caller; each call rewrites every byte it reads, so nothing needs clearing;
 //  * the first call on a device looks up the array's device address (set-up, once
 //    per device, with that device current); make that first call before starting any
-//    stream capture.
+//    stream capture.  The address is cached per device for the life of the process,
+//    so the entry point must not be used across a cudaDeviceReset of that device;
+//  * frames have 3 channels (nftrs == 3), as for stspix_get_marked_video;
+//  * `stream` must belong to the current device (checked: STSPIX_ERR_ARG otherwise);
+//  * launch failures are read from the launch calls themselves, so an error left
+//    pending by unrelated earlier work is neither reported here nor cleared.
 #include <cstdint>
 #include <mutex>
 
@@ -60,8 +65,21 @@ extern "C" int stspix_get_marked_video_noalloc(void* stream, const float* vid,
     border = g_border_addr[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
+  int sdev = -1;
+  if (cudaStreamGetDevice(st, &sdev) != cudaSuccess) return STSPIX_ERR_ARG;
+  if (sdev != dev) return STSPIX_ERR_ARG;
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  stspix::k_find_border_end<<<blocks, 256, 0, st>>>(spix, (uint8_t*)border, H, W, T);
-  stspix::k_overlay<<<blocks, 256, 0, st>>>(marked_out, vid, color, (const uint8_t*)border, n);
-  return cudaGetLastError() == cudaSuccess ? STSPIX_OK : STSPIX_ERR_CUDA;
+  uint8_t* bmask = (uint8_t*)border;
+  const uint8_t* cmask = bmask;
+  int h = H, w = W, t = T;
+  long long nn = n;
+  void* a1[] = {(void*)&spix, (void*)&bmask, (void*)&h, (void*)&w, (void*)&t};
+  if (cudaLaunchKernel((const void*)stspix::k_find_border_end, dim3(blocks), dim3(256), a1, 0,
+                       st) != cudaSuccess)
+    return STSPIX_ERR_CUDA;
+  void* a2[] = {(void*)&marked_out, (void*)&vid, (void*)&color, (void*)&cmask, (void*)&nn};
+  if (cudaLaunchKernel((const void*)stspix::k_overlay, dim3(blocks), dim3(256), a2, 0, st) !=
+      cudaSuccess)
+    return STSPIX_ERR_CUDA;
+  return STSPIX_OK;
 }
