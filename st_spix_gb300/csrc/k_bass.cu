@@ -93,7 +93,8 @@ __global__ void kb_mark_present(const Slot* __restrict__ slots, int mode) {
   if (v >= lo && v <= hi) S.flags[v - lo] = 1;
 }
 
-// One block per slot: exclusive scan of n byte flags (n up to a few 10^5).
+// One block per slot: exclusive scan of n byte flags (n up to a few 10^5), each
+// counted as 0 or 1 (the split acceptance flags of propagated frames carry extra bits).
 //   mode 0: hex-id presence (n = nraw)        -> total = live hex ids
 //   mode 1: split acceptance (n = cap)        -> total = accepted splits
 //   mode 2: relabel mint flags (n = cap)      -> total = minted ids
@@ -112,7 +113,7 @@ __global__ void kb_scan(const Slot* __restrict__ slots, int mode) {
   int chunk = (n + T - 1) / T;
   int b = threadIdx.x * chunk, e = min(n, b + chunk);
   int s = 0;
-  for (int i = b; i < e; i++) s += flags[i];
+  for (int i = b; i < e; i++) s += flags[i] != 0;
   part[threadIdx.x] = s;
   __syncthreads();
   for (int off = 1; off < T; off <<= 1) {
@@ -122,7 +123,7 @@ __global__ void kb_scan(const Slot* __restrict__ slots, int mode) {
     __syncthreads();
   }
   int run = threadIdx.x ? part[threadIdx.x - 1] : 0;
-  for (int i = b; i < e; i++) { excl[i] = run; run += flags[i]; }
+  for (int i = b; i < e; i++) { excl[i] = run; run += flags[i] != 0; }
   if (threadIdx.x == T - 1) *total = part[T - 1];
 }
 
@@ -694,7 +695,6 @@ struct SweepTile {
   // active-set sweeps: change flags of the label region as row bitmasks (bit x of
   // row y = label-region pixel (x, y)), dilated by 4 pixels
   unsigned long long act[2][kLY];
-  int any;
 };
 
 // Statistics of a tile's final labels (the last sweep of an update_seg call adds
@@ -778,46 +778,59 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
   const int ix0 = tx0 - G, iy0 = ty0 - G;
   // Border mask at the sweep start (find_border_pixels, seg_utils.cu:164-195); the
   // border pixels of parity class k inside the tile grown by G-k pixels are listed
-  // for phase k, so each phase scores only its border pixels, densely.
-  // (appends are warp-aggregated: one shared atomic per warp and phase)
-  for (int base = 0; base < kIX * kIY; base += blockDim.x) {
-    const int i = base + threadIdx.x;
-    int ph = -1;
-    if (i < kIX * kIY) {
-      const int lx = i % kIX, ly = i / kIX;
-      const int gx = ix0 + lx, gy = iy0 + ly;
-      bool act = gx >= 0 && gx < W && gy >= 0 && gy < H;
-      if (act && use_act) {
-        const int ax = lx + OFF, ay = ly + OFF;   // label-region coordinates
-        act = ((ax < 64 ? sm.act[0][ay] >> ax : sm.act[1][ay] >> (ax - 64)) & 1ull) != 0;
+  // for phase k, so each phase scores only its border pixels, densely.  A warp takes
+  // one row of the grown region at a time in 32-pixel chunks: a row holds the two
+  // classes of its y parity, each appended with one shared atomic per chunk.  Rows
+  // whose (dilated) change mask is empty are skipped whole in active-set sweeps.
+  {
+    constexpr int kChunks = (kIX + 31) / 32;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int ly = warp; ly < kIY; ly += nwarps) {
+      const int gy = iy0 + ly;
+      if (gy < 0 || gy >= H) continue;
+      const int ay = ly + OFF;                   // label-region row
+      unsigned long long m0 = ~0ull, m1 = ~0ull;
+      if (use_act) {
+        m0 = sm.act[0][ay];
+        m1 = sm.act[1][ay];
+        if (!(m0 | m1)) continue;
       }
-      if (act) {
-        bool b;
-        if (gy < 1 || gx < 1 || gy >= H - 1 || gx >= W - 1) {
-          b = true;
-        } else {
-          const int p = (ly + OFF) * kLX + (lx + OFF);
-          const int C = L[p];
-          b = (C != L[p - kLX] || C != L[p + kLX] || C != L[p + 1] || C != L[p - 1]);
-        }
-        const int c = ((gx & 1) << 1) | (gy & 1);
-        const int grow = G - c;
-        if (b && gx >= tx0 - grow && gx < tx0 + TX + grow && gy >= ty0 - grow &&
-            gy < ty0 + TY + grow)
-          ph = c;
-      }
-    }
+      const int cy = gy & 1;
+      const bool edge_row = gy < 1 || gy >= H - 1;
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
-      const unsigned m = __ballot_sync(0xffffffffu, ph == c);
-      if (!m) continue;
-      const int leader = __ffs(m) - 1;
-      int at = 0;
-      if (lane == leader) at = atomicAdd(&cnt[c], __popc(m));
-      at = __shfl_sync(0xffffffffu, at, leader);
-      if (ph == c)
-        list[c][at + __popc(m & ((1u << lane) - 1))] =
-            (unsigned short)(((i / kIX) << 8) | (i % kIX));
+      for (int ch = 0; ch < kChunks; ch++) {
+        const int lx = ch * 32 + lane;
+        const int gx = ix0 + lx;
+        bool b = lx < kIX && gx >= 0 && gx < W;
+        if (b && use_act) {
+          const int ax = lx + OFF;
+          b = ((ax < 64 ? m0 >> ax : m1 >> (ax - 64)) & 1ull) != 0;
+        }
+        int c = 0;
+        if (b) {
+          if (!(edge_row || gx < 1 || gx >= W - 1)) {
+            const int p = ay * kLX + (lx + OFF);
+            const int C = L[p];
+            b = (C != L[p - kLX] || C != L[p + kLX] || C != L[p + 1] || C != L[p - 1]);
+          }
+          c = ((gx & 1) << 1) | cy;
+          const int grow = G - c;
+          b = b && gx >= tx0 - grow && gx < tx0 + TX + grow && gy >= ty0 - grow &&
+              gy < ty0 + TY + grow;
+        }
+#pragma unroll
+        for (int xo = 0; xo < 2; xo++) {
+          const int cc = (xo << 1) | cy;
+          const unsigned m = __ballot_sync(0xffffffffu, b && c == cc);
+          if (!m) continue;
+          const int leader = __ffs(m) - 1;
+          int at = 0;
+          if (lane == leader) at = atomicAdd(&cnt[cc], __popc(m));
+          at = __shfl_sync(0xffffffffu, at, leader);
+          if (b && c == cc) list[cc][at + __popc(m & lt)] = (unsigned short)((ly << 8) | lx);
+        }
+      }
     }
   }
   __syncthreads();
@@ -903,8 +916,11 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
   const int tx0 = bx * kTX, ty0 = by * kTY;
   const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;        // label region origin
-  const uint8_t* __restrict__ chg_in = S.chg[parity ^ 1];
-  uint8_t* __restrict__ chg_out = S.chg[parity];
+  // change flags: one bit per pixel, rows of P16 16-bit words (bit x & 15 of word
+  // x >> 4); a tile's x origin is a multiple of 16, so every word has one writer
+  const uint16_t* __restrict__ chg_in = (const uint16_t*)S.chg[parity ^ 1];
+  uint16_t* __restrict__ chg_out = (uint16_t*)S.chg[parity];
+  const int P16 = (W + 15) >> 4;
   static_assert(kLX <= 128, "label region wider than two 64-bit words");
   // The label region is loaded first, into registers: warp w takes rows w, w + 8, ...
   // in 32-label chunks, every load issued before any is used, so the block waits for
@@ -931,40 +947,64 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   if (mode) {
     unsigned long long* a0 = sm.act[0];
     unsigned long long* a1 = sm.act[1];
-    if (threadIdx.x == 0) sm.any = 0;
-    for (int r = threadIdx.x; r < kLY; r += blockDim.x) { a0[r] = 0; a1[r] = 0; }
-    __syncthreads();
-    constexpr int kCh = (kLX + 31) / 32;
-    for (int c = warp; c < kLY * kCh; c += blockDim.x / 32) {
-      const int r = c / kCh, cx = c % kCh;
-      const int x = cx * 32 + lane;
-      const int gx = rx0 + x, gy = ry0 + r;
-      const bool f = x < kLX && gx >= 0 && gx < W && gy >= 0 && gy < H && chg_in[gy * W + gx];
-      const unsigned b = __ballot_sync(0xffffffffu, f);
-      if (lane == 0 && b) {
-        // chunk cx covers bits 32 cx .. 32 cx + 31 of the row: word cx / 2, half cx % 2
-        atomicOr(cx < 2 ? &a0[r] : &a1[r], (unsigned long long)b << (32 * (cx & 1)));
-        sm.any = 1;
+    // each row of the label region: its change bits from the previous sweep's plane
+    // (kNW 16-bit words starting at word rx0 >> 4, shifted by the region's offset in
+    // the first word), then dilated by the reach horizontally
+    constexpr int kNW = (kLX + 15) / 16 + 1;
+    static_assert(kNW <= 8 && kLX <= 128, "a label-region row spans at most 8 words");
+    const int w0 = rx0 >> 4;                     // rx0 >= -8: arithmetic shift floors
+    const int off = rx0 - (w0 << 4);             // 16 - halo, in 1..15
+    unsigned long long h0 = 0, h1 = 0;
+    bool nz = false;
+    const int r = threadIdx.x;
+    if (r < kLY) {
+      const int gy = ry0 + r;
+      unsigned long long lo = 0, hi = 0;
+      if (gy >= 0 && gy < H) {
+        const uint16_t* row = chg_in + (size_t)gy * P16;
+#pragma unroll
+        for (int k = 0; k < kNW; k++) {
+          const int wi = w0 + k;
+          const unsigned long long v = (wi >= 0 && wi < P16) ? (unsigned long long)row[wi] : 0ull;
+          if (k < 4) lo |= v << (16 * k);
+          else hi |= v << (16 * (k - 4));
+        }
       }
+      unsigned long long f0 = (lo >> off) | (hi << (64 - off));
+      unsigned long long f1 = hi >> off;
+      if (kLX < 64) { f0 &= (1ull << (kLX & 63)) - 1ull; f1 = 0; }
+      else if (kLX < 128) { f1 &= (1ull << ((kLX - 64) & 63)) - 1ull; }
+      nz = (f0 | f1) != 0;
+      h0 = f0; h1 = f1;
+#pragma unroll
+      for (int sft = 1; sft <= kReach; sft++) {
+        h0 |= (f0 << sft) | (f0 >> sft) | (f1 << (64 - sft));
+        h1 |= (f1 << sft) | (f1 >> sft) | (f0 >> (64 - sft));
+      }
+      a0[r] = h0;
+      a1[r] = h1;
     }
-    __syncthreads();
-    if (!sm.any) {
+    if (!__syncthreads_or(nz)) {
       // nothing within reach changed: the tile keeps its labels (for every sweep of
       // the launch: a later sweep can only move pixels within reach of an earlier
       // change, and there is none in the label region)
 #pragma unroll
       for (int a = 0; a < kRW; a++) {
-        const int r = warp + 8 * a;
+        const int rr = warp + 8 * a;
 #pragma unroll
         for (int c = 0; c < kCK; c++) {
           const int x = lane + 32 * c;
-          if (r < kLY && x < kLX && in_tile(r, x)) {
-            const size_t g = (size_t)(ry0 + r) * W + (rx0 + x);
-            seg_out[g] = lv[a][c];
-            chg_out[g] = 0;
-            if (stats == 2) L[r * kLX + x] = lv[a][c];
+          if (rr < kLY && x < kLX && in_tile(rr, x)) {
+            seg_out[(size_t)(ry0 + rr) * W + (rx0 + x)] = lv[a][c];
+            if (stats == 2) L[rr * kLX + x] = lv[a][c];
           }
         }
+      }
+      // zero change words of the tile's rows
+      constexpr int kTW = kTX / 16;
+      for (int i = threadIdx.x; i < kTY * kTW; i += blockDim.x) {
+        const int gy = ty0 + i / kTW, wi = (tx0 >> 4) + i % kTW;
+        if (gy < H && wi < P16) chg_out[(size_t)gy * P16 + wi] = 0;
       }
       if (stats == 2) {
         __syncthreads();
@@ -972,22 +1012,7 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       }
       return;
     }
-    // dilate by the reach: horizontally within each row (two-word shifts), then
-    // vertically
-    unsigned long long h0 = 0, h1 = 0;
-    const int r = threadIdx.x;
-    if (r < kLY) {
-      const unsigned long long lo = a0[r], hi = a1[r];
-      h0 = lo; h1 = hi;
-#pragma unroll
-      for (int sft = 1; sft <= kReach; sft++) {
-        h0 |= (lo << sft) | (lo >> sft) | (hi << (64 - sft));
-        h1 |= (hi << sft) | (hi >> sft) | (lo >> (64 - sft));
-      }
-    }
-    __syncthreads();
-    if (r < kLY) { a0[r] = h0; a1[r] = h1; }
-    __syncthreads();
+    // vertical dilation
     unsigned long long v0 = 0, v1 = 0;
     if (r < kLY) {
       for (int k = max(0, r - kReach); k <= min(kLY - 1, r + kReach); k++) {
@@ -1025,15 +1050,21 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
     __syncthreads();
     sweep_pass<TX, TY, NS, 3>(S, sm, lut_bits, tx0, ty0, s2, potts, false);
   }
-  // write back the tile, with change flags of the last sweep
+  // write back the tile, with change flags of the last sweep: a warp covers 32
+  // consecutive pixels of a row (16-wide tiles: two rows), and the lanes that start a
+  // 16-pixel group store its 16 change bits as one word
   for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x) {
     const int x = i % kTX, y = i / kTX;
     const int gx = tx0 + x, gy = ty0 + y;
+    bool changed = false;
     if (gx < W && gy < H) {
       const int v = L[(y + kSH) * kLX + (x + kSH)];
       seg_out[gy * W + gx] = v;
-      chg_out[gy * W + gx] = v != sm.L0[i];
+      changed = v != sm.L0[i];
     }
+    const unsigned bits = __ballot_sync(0xffffffffu, changed);
+    if ((lane & 15) == 0 && gy < H && (gx >> 4) < P16)
+      chg_out[(size_t)gy * P16 + (gx >> 4)] = (uint16_t)(bits >> (lane & 16));
   }
   if (stats == 2) tile_accumulate<TX, TY>(S, L, kLX, kSH, tx0, ty0);
 }
