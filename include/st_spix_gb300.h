@@ -30,6 +30,11 @@
  *   stspix_legacy_rgb_to_lab   st_spix/csrc/prop/rgb2lab.cu:167 run_rgb_to_lab
  *   stspix_sp_video_pooling    st_spix/csrc/prop/sp_video_pooling.cu:62 sp_video_pooling
  *   stspix_downsampled_video_to_pooled  st_spix/csrc/prop/sp_video_pooling.cu:211
+ *   stspix_legacy_update_prior st_spix/csrc/prop/sparams_io.cu:795 run_update_prior
+ *   stspix_legacy_shift_tensor st_spix/csrc/prop/shift_tensor.cu:60 run_shift_tensor
+ *                              (+ shift_tensor_ordered.cu:53 run_shift_tensor_ordered)
+ *   stspix_legacy_shift_order  st_spix/csrc/prop/shift_order.cu:43 run_shift_order
+ *   stspix_legacy_split_disconnected  st_spix/csrc/prop/split_disconnected.cu:390
  */
 #ifndef ST_SPIX_GB300_H
 #define ST_SPIX_GB300_H
@@ -377,6 +382,47 @@ int stspix_sp_video_pooling(stspix_ctx* ctx, void* stream, const float* img, con
 int stspix_downsampled_video_to_pooled(stspix_ctx* ctx, void* stream, const float* down,
                                        const int32_t* seg, int B, int T, int H, int W, int F,
                                        int nspix, float* pooled);
+
+/* run_update_prior (prop/sparams_io.cu:795-834): every id present in spix [npix] that
+ * is >= prev_nspix (and < nids, the rows of the arrays) takes its estimates as priors:
+ * prior_mu_app = mu_app [nids,3] (f32), prior_mu_shape = mu_shape [nids,2] (f64),
+ * prior_sigma_shape = sigma_shape [nids,3] (f64; its 2x2 inverse when invert, with a
+ * negative determinant replaced by 1e-6).                                            */
+int stspix_legacy_update_prior(stspix_ctx* ctx, void* stream, const int32_t* spix,
+                               long long npix, int nids, const float* mu_app, float* prior_mu_app,
+                               const double* mu_shape, double* prior_mu_shape,
+                               const double* sigma_shape, double* prior_sigma_shape,
+                               int prev_nspix, int invert);
+
+/* shift_tensor (prop/shift_tensor.cu:60-139; selected == NULL) and shift_tensor_ordered
+ * (prop/shift_tensor_ordered.cu:53-137; selected i32 [B,H,W]): every pixel of in f32
+ * [B,H,W,F] moves by its superpixel's integer flow (flow i32 [B,nspix,2] = dx, dy; labels
+ * outside [0, nspix) stay); out [B,H,W,F] = sum of the features arriving at a pixel
+ * (ordered: only those of its selected id), counts i32 [B,H,W] = their number,
+ * contributors u8 [B,H,W,nspix] (may be NULL) = which ids arrive.  Sums are FP64, rounded
+ * once (the legacy kernels add FP32 atomics in arbitrary order).                    */
+int stspix_legacy_shift_tensor(stspix_ctx* ctx, void* stream, const float* in,
+                               const int32_t* spix, const int32_t* flow, int B, int H, int W,
+                               int F, int nspix, const int32_t* selected, float* out,
+                               int32_t* counts, uint8_t* contributors);
+
+/* shift_order (prop/shift_order.cu:43-119): selected i32 [B,H,W] = the first (smallest)
+ * id whose contributors flag is set at the pixel, -1 if none (the legacy loop's running
+ * minimum never updates after its first contributor).                               */
+int stspix_legacy_shift_order(stspix_ctx* ctx, void* stream, const uint8_t* contributors,
+                              int B, int H, int W, int nspix, int32_t* selected);
+
+/* split_disconnected (prop/split_disconnected.cu:31-255, :390): spix i32 [H,W] with
+ * labels in [0, nspix) is relabelled in place so that every connected region (equal
+ * labels, neighbours within Chebyshev distance 2) but the largest of its label gets
+ * the id nspix + split_starts[label] + its rank among the label's regions;
+ * split_starts i32 [nspix]; children i32 [nspix, *max_nsplits] lists the new ids of
+ * each label (-1 elsewhere).  *max_nsplits (host) = the total number of extra regions.
+ * When nspix * *max_nsplits exceeds children_cap, nothing is relabelled and
+ * STSPIX_ERR_CAPACITY is returned with *max_nsplits set.  Synchronises the stream.   */
+int stspix_legacy_split_disconnected(stspix_ctx* ctx, void* stream, int32_t* spix, int H, int W,
+                                     int nspix, int32_t* split_starts, int32_t* children,
+                                     long long children_cap, int* max_nsplits);
 
 /* ---- batched and serving forms -----------------------------------------------
  * No single reference counterpart: the reference processes one frame per call

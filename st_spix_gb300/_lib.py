@@ -84,9 +84,16 @@ EXPORTS = ["stspix_default_config", "stspix_create", "stspix_destroy", "stspix_l
            "stspix_legacy_shift_labels", "stspix_legacy_fill_missing", "stspix_legacy_split",
            "stspix_legacy_rgb_to_lab",
            "stspix_sp_video_pooling", "stspix_downsampled_video_to_pooled",
-           "stspix_graph_replays", "stspix_set_batch_graphs", "stspix_sweep_choice"]
+           "stspix_graph_replays", "stspix_set_batch_graphs", "stspix_sweep_choice",
+           "stspix_legacy_update_prior", "stspix_legacy_shift_tensor",
+           "stspix_legacy_shift_order", "stspix_legacy_split_disconnected"]
 
 FAMILIES = ["sweep", "stats", "posterior", "split", "merge", "prop", "other"]
+
+# status codes (include/st_spix_gb300.h)
+STSPIX_OK, STSPIX_ERR_ARG, STSPIX_ERR_CUDA, STSPIX_ERR_NOMEM = 0, 1, 2, 3
+STSPIX_ERR_NOPROGRESS, STSPIX_ERR_ITER_LIMIT, STSPIX_ERR_CAPACITY = 4, 5, 6
+STSPIX_ERR_BARRIER, STSPIX_ERR_DEGENERATE, STSPIX_ERR_TOO_LARGE = 7, 8, 9
 
 
 def library_path() -> str:
@@ -164,6 +171,12 @@ def load(build_if_missing: bool = True):
             "stspix_graph_replays": (C.c_longlong, [P]),
             "stspix_set_batch_graphs": (I, [P, I]),
             "stspix_sweep_choice": (I, [P, I, C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+            "stspix_legacy_update_prior": (I, [P, P, P, C.c_longlong, I, P, P, P, P, P, P, I,
+                                               I]),
+            "stspix_legacy_shift_tensor": (I, [P, P, P, P, P, I, I, I, I, I, P, P, P, P]),
+            "stspix_legacy_shift_order": (I, [P, P, P, I, I, I, I, P]),
+            "stspix_legacy_split_disconnected": (I, [P, P, P, I, I, I, P, P, C.c_longlong,
+                                                     C.POINTER(I)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

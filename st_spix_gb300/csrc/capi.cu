@@ -2418,6 +2418,128 @@ int stspix_downsampled_video_to_pooled(stspix_ctx* ctx, void* stream, const floa
   return STSPIX_OK;
 }
 
+int stspix_legacy_update_prior(stspix_ctx* ctx, void* stream, const int32_t* spix,
+                               long long npix, int nids, const float* mu_app, float* prior_mu_app,
+                               const double* mu_shape, double* prior_mu_shape,
+                               const double* sigma_shape, double* prior_sigma_shape,
+                               int prev_nspix, int invert) {
+  if (!ctx || !spix || !mu_app || !prior_mu_app || !mu_shape || !prior_mu_shape || !sigma_shape ||
+      !prior_sigma_shape || npix < 0 || nids < 0)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  if (nids == 0 || npix == 0) return STSPIX_OK;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* present = nullptr;
+  CK(cudaMallocAsync((void**)&present, (size_t)nids, st));
+  CK(cudaMemsetAsync(present, 0, (size_t)nids, st));
+  LAUNCH(k_lmark_ids, npix, spix, npix, nids, present);
+  LAUNCH(k_lupdate_prior, nids, present, nids, prev_nspix, invert, mu_app, prior_mu_app,
+         mu_shape, prior_mu_shape, sigma_shape, prior_sigma_shape);
+  CK(cudaFreeAsync(present, st));
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_legacy_shift_tensor(stspix_ctx* ctx, void* stream, const float* in,
+                               const int32_t* spix, const int32_t* flow, int B, int H, int W,
+                               int F, int nspix, const int32_t* selected, float* out,
+                               int32_t* counts, uint8_t* contributors) {
+  if (!ctx || !in || !spix || !flow || !out || !counts || B < 1 || H < 1 || W < 1 || F < 1 ||
+      nspix < 1 || B > 65535 || (long long)H * W > INT_MAX)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long npix = (long long)H * W, n = B * npix;
+  double* acc = nullptr;
+  CK(cudaMallocAsync((void**)&acc, sizeof(double) * (size_t)(n * F), st));
+  CK(cudaMemsetAsync(acc, 0, sizeof(double) * (size_t)(n * F), st));
+  CK(cudaMemsetAsync(counts, 0, sizeof(int32_t) * (size_t)n, st));
+  if (contributors) CK(cudaMemsetAsync(contributors, 0, (size_t)(n * nspix), st));
+  LAUNCHG(k_lshift_tensor, dim3(blocks_for(npix), (unsigned)B), kThreads, in, spix, flow, H, W, F,
+          nspix, selected, acc, counts, contributors);
+  LAUNCH(k_round_f32, n * F, acc, n * F, out);
+  CK(cudaFreeAsync(acc, st));
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_legacy_shift_order(stspix_ctx* ctx, void* stream, const uint8_t* contributors,
+                              int B, int H, int W, int nspix, int32_t* selected) {
+  if (!ctx || !contributors || !selected || B < 1 || H < 1 || W < 1 || nspix < 1)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long n = (long long)B * H * W;
+  LAUNCH(k_fill_i32, n, selected, n, -1);
+  LAUNCH(k_lshift_order, n, contributors, n, nspix, selected);
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
+int stspix_legacy_split_disconnected(stspix_ctx* ctx, void* stream, int32_t* spix, int H, int W,
+                                     int nspix, int32_t* split_starts, int32_t* children,
+                                     long long children_cap, int* max_nsplits) {
+  if (!ctx || !spix || !split_starts || !max_nsplits || H < 1 || W < 1 || nspix < 1 ||
+      (long long)H * W > INT_MAX / 2)
+    return fail(ctx, STSPIX_ERR_ARG, "bad argument");
+  int r, rng[2];
+  const int npix = H * W;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((r = label_range(ctx, st, spix, npix, rng))) return r;
+  if (rng[0] < 0 || rng[1] >= nspix)
+    return fail(ctx, STSPIX_ERR_ARG, "labels must lie in [0, %d) (got %d..%d)", nspix, rng[0],
+                rng[1]);
+  // scratch: parent/root, root flags, ranks, region of pixel, per-region label, size and
+  // offset (npix each at most), per-label counts, scalars
+  int32_t* buf = nullptr;
+  const size_t words = 7 * (size_t)npix + (size_t)nspix + 4;
+  CK(cudaMallocAsync((void**)&buf, sizeof(int32_t) * words, st));
+  int32_t* parent = buf;
+  int32_t* is_root = parent + npix;
+  int32_t* rank = is_root + npix;
+  int32_t* region_of = rank + npix;
+  int32_t* region_spix = region_of + npix;
+  int32_t* region_size = region_spix + npix;
+  int32_t* region_offset = region_size + npix;
+  int32_t* spix_counts = region_offset + npix;
+  int32_t* sc = spix_counts + nspix;  // [0] status, [1] regions, [2] max_nsplits
+  CK(cudaMemsetAsync(sc, 0, 4 * sizeof(int32_t), st));
+  CK(cudaMemsetAsync(region_size, 0, sizeof(int32_t) * (size_t)npix, st));
+  CK(cudaMemsetAsync(region_offset, 0xff, sizeof(int32_t) * (size_t)npix, st));
+  CK(cudaMemsetAsync(spix_counts, 0, sizeof(int32_t) * (size_t)nspix, st));
+  LAUNCH(k_lsd_init, npix, parent, npix);
+  LAUNCH(k_lsd_hook, npix, spix, H, W, parent, sc);
+  LAUNCH(k_lsd_roots, npix, parent, npix, is_root);
+  LAUNCHG(k_lscan, 1, 1024, is_root, npix, rank, sc + 1);
+  LAUNCH(k_lsd_regions, npix, spix, parent, rank, npix, nspix, region_of, region_spix,
+         region_size, spix_counts);
+  LAUNCHG(k_lsd_starts, 1, 32, spix_counts, nspix, split_starts, sc + 2);
+  int32_t host_sc[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(host_sc, sc, sizeof host_sc, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (host_sc[0]) {
+    cudaFreeAsync(buf, st);
+    return fail(ctx, STSPIX_ERR_ITER_LIMIT, "connected components did not converge");
+  }
+  const int nregions = host_sc[1], mx = host_sc[2];
+  *max_nsplits = mx;
+  if ((long long)nspix * mx > children_cap || (mx > 0 && !children)) {
+    cudaFreeAsync(buf, st);
+    return fail(ctx, STSPIX_ERR_CAPACITY, "children needs %lld entries (%d x %d), capacity %lld",
+                (long long)nspix * mx, nspix, mx, children_cap);
+  }
+  if (mx > 0) {
+    LAUNCH(k_fill_i32, (long long)nspix * mx, children, (long long)nspix * mx, -1);
+    LAUNCH(k_lsd_offsets, nspix, region_spix, region_size, nregions, nspix, region_offset);
+    LAUNCH(k_lsd_update, npix, spix, region_of, region_offset, split_starts, npix, nspix, mx,
+           children);
+  }
+  CK(cudaFreeAsync(buf, st));
+  CK(cudaGetLastError());
+  return STSPIX_OK;
+}
+
 int stspix_evaluate(stspix_ctx* ctx, void* stream, const float* vid, const int32_t* spix,
                     const int32_t* gt, int T, int H, int W, stspix_quality* out) {
   if (!ctx || !vid || !spix || !out || T < 1 || H < 1 || W < 1 || T > 65535 ||

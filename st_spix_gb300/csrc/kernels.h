@@ -153,5 +153,30 @@ __global__ void k_vpool_write(const float* down, const int32_t* seg, int T, long
                               int nspix, float* pooled);
 __global__ void k_q_pool_write(const int32_t* spix, int npix, int off, int S, long long n,
                                const float* down, float* pooled);
+__global__ void k_lmark_ids(const int32_t* spix, long long n, int nids, uint8_t* present);
+__global__ void k_lupdate_prior(const uint8_t* present, int nids, int prev_nspix, int invert,
+                                const float* mu_app, float* prior_mu_app, const double* mu_shape,
+                                double* prior_mu_shape, const double* sigma_shape,
+                                double* prior_sigma_shape);
+__global__ void k_lshift_tensor(const float* in, const int32_t* spix, const int32_t* flow, int H,
+                                int W, int F, int nspix, const int32_t* selected, double* acc,
+                                int32_t* counts, uint8_t* contributors);
+__global__ void k_round_f32(const double* acc, long long n, float* out);
+__global__ void k_lshift_order(const uint8_t* contributors, long long npix_all, int nspix,
+                               int32_t* selected);
+__global__ void k_lsd_init(int32_t* parent, int npix);
+__global__ void k_lsd_hook(const int32_t* spix, int H, int W, int32_t* parent, int* status);
+__global__ void k_lsd_roots(int32_t* parent, int npix, int32_t* is_root);
+__global__ void k_lscan(const int32_t* in, int n, int32_t* out, int32_t* total);
+__global__ void k_lsd_regions(const int32_t* spix, const int32_t* root, const int32_t* rank,
+                              int npix, int nspix, int32_t* region_of, int32_t* region_spix,
+                              int32_t* region_size, int32_t* spix_counts);
+__global__ void k_lsd_starts(const int32_t* spix_counts, int nspix, int32_t* split_starts,
+                             int32_t* max_nsplits);
+__global__ void k_lsd_offsets(const int32_t* region_spix, const int32_t* region_size,
+                              int nregions, int nspix, int32_t* region_offset);
+__global__ void k_lsd_update(int32_t* spix, const int32_t* region_of,
+                             const int32_t* region_offset, const int32_t* split_starts, int npix,
+                             int nspix, int max_nchild, int32_t* children);
 
 }  // namespace stspix

@@ -295,3 +295,108 @@ def downsampled_video_to_pooled(downsampled, seg):
                                                          B, T, H, W, F, nspix,
                                                          pooled.data_ptr()))
     return pooled
+
+
+def run_update_prior(spix, params, prev_nspix, invert):
+    """prop/sparams_io.cu:795 run_update_prior: for every id present in spix at or
+    above prev_nspix, params' priors (prior_mu_app, prior_mu_shape, prior_sigma_shape)
+    take the estimates (mu_app, mu_shape, sigma_shape; its inverse when invert), in
+    place."""
+    _check_input(spix, "spix")
+    for k in ("mu_app", "prior_mu_app", "mu_shape", "prior_mu_shape", "sigma_shape",
+              "prior_sigma_shape"):
+        _check_input(getattr(params, k), k)
+    nids = int(params.mu_app.shape[0])
+    if spix.numel() and int(spix.max().item()) >= nids:
+        raise RuntimeError("spix holds ids beyond the parameter rows")
+    if params.mu_app.dtype != torch.float32 or params.prior_mu_app.dtype != torch.float32 or \
+            params.mu_shape.dtype != torch.float64 or params.sigma_shape.dtype != torch.float64:
+        raise RuntimeError("mu_app / prior_mu_app must be float32, shape fields float64")
+    ctx = _ctx(spix.device)
+    ctx.check(ctx.lib.stspix_legacy_update_prior(
+        ctx.handle, _stream(spix.device), spix.data_ptr(), spix.numel(), nids,
+        params.mu_app.data_ptr(), params.prior_mu_app.data_ptr(), params.mu_shape.data_ptr(),
+        params.prior_mu_shape.data_ptr(), params.sigma_shape.data_ptr(),
+        params.prior_sigma_shape.data_ptr(), int(prev_nspix), int(bool(invert))))
+    params._engine = None      # the legacy tensors changed: rebuild on the next prop_bass
+
+
+def _shift_tensor(in_tensor, spix, flow, selected):
+    _check_input(in_tensor, "in_tensor")
+    _check_input(spix, "spix")
+    _check_input(flow, "flow")
+    if spix.dtype != torch.int32 or flow.dtype != torch.int32 or in_tensor.dtype != torch.float32:
+        raise RuntimeError("spix and flow must be int32, in_tensor float32")
+    B, H, W = spix.shape
+    F = int(in_tensor.shape[3])
+    nspix = int(spix.max().item()) + 1
+    if int(flow.shape[1]) != nspix:
+        raise RuntimeError("flow must have one row per superpixel (spix.max() + 1)")
+    out = torch.empty((B, H, W, F), dtype=torch.float32, device=spix.device)
+    counts = torch.empty((B, H, W), dtype=torch.int32, device=spix.device)
+    contrib = None
+    if selected is None:
+        contrib = torch.empty((B, H, W, nspix), dtype=torch.bool, device=spix.device)
+    ctx = _ctx(spix.device)
+    ctx.check(ctx.lib.stspix_legacy_shift_tensor(
+        ctx.handle, _stream(spix.device), in_tensor.data_ptr(), spix.data_ptr(), flow.data_ptr(),
+        B, H, W, F, nspix, selected.data_ptr() if selected is not None else None, out.data_ptr(),
+        counts.data_ptr(), contrib.data_ptr() if contrib is not None else None))
+    return out, counts, contrib
+
+
+def shift_tensor(in_tensor, spix, flow):
+    """prop/shift_tensor.cu:60 run_shift_tensor: in f32 [B,H,W,F], spix i32 [B,H,W], flow
+    i32 [B,nspix,2] -> (shifted features f32 [B,H,W,F] (sums of the arrivals), counts
+    i32 [B,H,W], contributors bool [B,H,W,nspix])."""
+    return _shift_tensor(in_tensor, spix, flow, None)
+
+
+def shift_tensor_ordered(in_tensor, spix, flow, select):
+    """prop/shift_tensor_ordered.cu:53: as shift_tensor, but a pixel takes only the
+    arrivals of its selected id (select i32 [B,H,W]) -> (shifted features, counts)."""
+    _check_input(select, "select")
+    out, counts, _ = _shift_tensor(in_tensor, spix, flow, select.to(torch.int32).contiguous())
+    return out, counts
+
+
+def shift_order(contributors, sizes):
+    """prop/shift_order.cu:43 run_shift_order: contributors bool [B,H,W,nspix], sizes i32
+    [B,nspix] -> selected i32 [B,H,W]: the first contributing id (-1 if none), which is
+    what the legacy loop returns whatever the sizes."""
+    _check_input(contributors, "contributors")
+    _check_input(sizes, "sizes")
+    B, H, W, nspix = contributors.shape
+    sel = torch.empty((B, H, W), dtype=torch.int32, device=contributors.device)
+    ctx = _ctx(contributors.device)
+    ctx.check(ctx.lib.stspix_legacy_shift_order(ctx.handle, _stream(contributors.device),
+                                                contributors.contiguous().data_ptr(), B, H, W,
+                                                nspix, sel.data_ptr()))
+    return sel
+
+
+def split_disconnected(spix, nspix):
+    """prop/split_disconnected.cu:390 split_disconnected: spix i32 [1,H,W] (relabelled in
+    place) -> (spix, children i32 [nspix, max_nsplits], split_starts i32 [nspix])."""
+    _check_input(spix, "spix")
+    if spix.dtype != torch.int32 or spix.shape[0] != 1:
+        raise RuntimeError("spix must be int32 [1,H,W]")
+    _, H, W = spix.shape
+    nspix = int(nspix)
+    starts = torch.empty((nspix,), dtype=torch.int32, device=spix.device)
+    ctx = _ctx(spix.device)
+    mx = C.c_int(0)
+    cap = nspix * 8
+    children = torch.empty((cap,), dtype=torch.int32, device=spix.device)
+    st = ctx.lib.stspix_legacy_split_disconnected(ctx.handle, _stream(spix.device),
+                                                  spix.data_ptr(), H, W, nspix, starts.data_ptr(),
+                                                  children.data_ptr(), cap, C.byref(mx))
+    if st == _lib.STSPIX_ERR_CAPACITY:
+        cap = nspix * mx.value
+        children = torch.empty((max(cap, 1),), dtype=torch.int32, device=spix.device)
+        st = ctx.lib.stspix_legacy_split_disconnected(ctx.handle, _stream(spix.device),
+                                                      spix.data_ptr(), H, W, nspix,
+                                                      starts.data_ptr(), children.data_ptr(),
+                                                      cap, C.byref(mx))
+    ctx.check(st)
+    return spix, children[: nspix * mx.value].view(nspix, mx.value), starts

@@ -206,3 +206,84 @@ def test_refine_is_propagated_bass_without_split_merge():
     assert st == 0 and rn <= n and log.shape == (6, 1)
     np.testing.assert_array_equal(out[0].cpu().numpy(), ref)
     np.testing.assert_array_equal(p.counts.cpu().numpy(), rp["counts"])
+
+
+# ---- run_update_prior, shift_tensor(_ordered), shift_order, split_disconnected -------
+def _blocky(H, W, seed, nlab=12):
+    rng = np.random.default_rng(seed)
+    ys, xs = np.mgrid[0:H, 0:W]
+    lab = ((ys // 7) * 5 + (xs // 9)) % nlab
+    lab[rng.integers(0, H, 30), rng.integers(0, W, 30)] = rng.integers(0, nlab, 30)
+    return lab.astype(np.int32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("invert", [False, True])
+def test_update_prior_matches_restatement(invert):
+    import torch
+    from st_spix_gb300 import prop_cuda
+    rng = np.random.default_rng(3)
+    n, prev = 40, 15
+    spix = _blocky(30, 41, 3, nlab=37)
+    p = prop_cuda.SuperpixelParams(*[None] * len(prop_cuda.KEYS))
+    host = dict(mu_app=rng.random((n, 3)).astype(np.float32),
+                prior_mu_app=rng.random((n, 3)).astype(np.float32),
+                mu_shape=rng.random((n, 2)) * 30, prior_mu_shape=rng.random((n, 2)) * 30,
+                sigma_shape=np.stack([rng.uniform(0.5, 2, n), rng.uniform(-0.3, 0.3, n),
+                                      rng.uniform(0.5, 2, n)], 1),
+                prior_sigma_shape=rng.random((n, 3)))
+    host["sigma_shape"][3] = (0.1, 1.0, 0.1)     # negative determinant
+    for k, v in host.items():
+        setattr(p, k, torch.from_numpy(np.ascontiguousarray(v)).cuda())
+    prop_cuda.run_update_prior(torch.from_numpy(spix[None]).cuda(), p, prev, invert)
+    pma, pms, pss = LG.update_prior(spix, host["mu_app"], host["prior_mu_app"], host["mu_shape"],
+                                   host["prior_mu_shape"], host["sigma_shape"],
+                                   host["prior_sigma_shape"], prev, invert)
+    np.testing.assert_array_equal(p.prior_mu_app.cpu().numpy(), pma)
+    np.testing.assert_array_equal(p.prior_mu_shape.cpu().numpy(), pms)
+    np.testing.assert_allclose(p.prior_sigma_shape.cpu().numpy(), pss, rtol=1e-15, atol=0)
+
+
+@pytest.mark.gpu
+def test_shift_tensor_and_order_match_restatement():
+    import torch
+    from st_spix_gb300 import prop_cuda
+    rng = np.random.default_rng(4)
+    H, W, F = 24, 31, 3
+    spix = _blocky(H, W, 4, nlab=9)
+    nspix = int(spix.max()) + 1
+    flow = rng.integers(-3, 4, size=(nspix, 2)).astype(np.int32)
+    x = rng.random((H, W, F)).astype(np.float32)
+    g = lambda a: torch.from_numpy(np.ascontiguousarray(a)[None]).cuda()
+    out, counts, contrib = prop_cuda.shift_tensor(g(x), g(spix), g(flow))
+    ro, rc, rcon = LG.shift_tensor(x, spix, flow)
+    np.testing.assert_array_equal(counts[0].cpu().numpy(), rc)
+    np.testing.assert_array_equal(contrib[0].cpu().numpy(), rcon)
+    np.testing.assert_array_equal(out[0].cpu().numpy(), ro)
+    sizes = np.bincount(spix.reshape(-1), minlength=nspix).astype(np.int32)
+    sel = prop_cuda.shift_order(contrib, g(sizes))
+    rsel = LG.shift_order(rcon, sizes)
+    np.testing.assert_array_equal(sel[0].cpu().numpy(), rsel)
+    out2, counts2 = prop_cuda.shift_tensor_ordered(g(x), g(spix), g(flow), sel)
+    ro2, rc2, _ = LG.shift_tensor(x, spix, flow, rsel)
+    np.testing.assert_array_equal(counts2[0].cpu().numpy(), rc2)
+    np.testing.assert_array_equal(out2[0].cpu().numpy(), ro2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [5, 6])
+def test_split_disconnected_matches_restatement(seed):
+    import torch
+    from st_spix_gb300 import prop_cuda
+    H, W = 40, 52
+    spix = _blocky(H, W, seed, nlab=14)
+    # cut some labels into pieces further than 2 pixels apart
+    spix[:, 20:24] = 13
+    nspix = int(spix.max()) + 1
+    ref_lab, ref_children, ref_starts = LG.split_disconnected(spix, nspix)
+    t = torch.from_numpy(spix[None].copy()).cuda()
+    lab, children, starts = prop_cuda.split_disconnected(t, nspix)
+    np.testing.assert_array_equal(lab[0].cpu().numpy(), ref_lab)
+    np.testing.assert_array_equal(starts.cpu().numpy(), ref_starts)
+    np.testing.assert_array_equal(children.cpu().numpy(), ref_children)
+    assert ref_children.shape[1] > 0

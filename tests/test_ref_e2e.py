@@ -34,7 +34,7 @@ pytestmark = [pytest.mark.gpu,
 S2 = 0.009 ** 2
 LA = float(np.log(0.5))
 AGREE_IMAGE = 0.997
-AGREE_FRAME = 0.97
+AGREE_FRAME = 0.98
 _ref = {}
 
 
