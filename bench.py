@@ -41,7 +41,7 @@ SWEEP_BYTES_PER_PX = 24
 # DRAM bytes (read + write) per sweep launch from one ncu capture of the same workload
 # (a batch of 8 frames, mean of a full and an active-set sweep); a constant of that
 # capture, re-taken whenever the sweep kernel changes, not a live measurement.
-SWEEP_TRAFFIC_NCU = dict(bytes_per_launch=37055104,
+SWEEP_TRAFFIC_NCU = dict(bytes_per_launch=35541120,
                          source="ncu dram__bytes_read.sum + dram__bytes_write.sum, "
                                 "profiles/kb_sweep_bist_stream_480x854_T30.md")
 METRIC = "streamed frames/sec"
@@ -1041,13 +1041,24 @@ def main():
     if not args.no_serve and world == 1:
         full = serve_leg(args, dev, rank, SERVE["streams"], args.serve_frames, SERVE["fps"])
         served = full["serving"].get("frames_per_s") or 0.0
-        n_sus = max(1, int(0.85 * served / SERVE["fps"]))
-        sus = serve_leg(args, dev, rank, n_sus, WORKLOAD["T"], SERVE["fps"])
+        # the largest load served as offered: start at 85 % of the config-3 served rate and
+        # shrink until the served rate is within 5 % of the offered one (3 tries at most)
+        n_sus, tries = max(1, int(0.85 * served / SERVE["fps"])), []
+        for _ in range(3):
+            sus = serve_leg(args, dev, rank, n_sus, WORKLOAD["T"], SERVE["fps"])
+            got = sus["serving"].get("frames_per_s") or 0.0
+            tries.append({"streams": n_sus, "offered_fps": sus["offered_fps"], "served_fps": got})
+            if got >= 0.95 * sus["offered_fps"] or n_sus == 1:
+                break
+            n_sus = max(1, int(0.9 * n_sus * got / sus["offered_fps"]))
+        light = serve_leg(args, dev, rank, 4, WORKLOAD["T"], SERVE["fps"])
         serving = {"config3": serving_summary(full, "256 streams, Poisson 30 fps each, %d frames "
                                                "per stream" % args.serve_frames),
-                   "sustained": serving_summary(sus, "%d streams, Poisson 30 fps each, %d frames "
-                                                "per stream (85%% of the config-3 served rate)"
-                                                % (n_sus, WORKLOAD["T"])),
+                   "sustained": dict(serving_summary(sus, "%d streams, Poisson 30 fps each, %d "
+                                                     "frames per stream" % (n_sus, WORKLOAD["T"])),
+                                     search=tries),
+                   "light": serving_summary(light, "4 streams, Poisson 30 fps each, %d frames per "
+                                            "stream" % WORKLOAD["T"]),
                    "target": "served / plain >= 5 and 720p p99 < 10 ms"}
 
     if rank != 0:
