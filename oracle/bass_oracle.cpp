@@ -30,9 +30,13 @@
 //      in FP64 with the lgamma(a_n) terms, which cancel exactly in the reference's
 //      formula, removed (split_merge_orig.cu:536-549, 845-877).
 //
-// Parity status: the reference has no CPU path, no tests and no golden vectors, and
-// its CUDA code cannot run here; this restatement is pinned only by the reference's
-// source (parity unpinned against reference outputs).
+// Parity status: the reference has no CPU path, no tests and no golden vectors.  Its
+// own kernels, compiled unmodified for the GPU by oracle/ref_build.py and launched by
+// oracle/ref_harness.cpp, pin this restatement: stage by stage (tests/test_ref_pin.py),
+// on shared split/merge decision states (tests/test_ref_decisions.py) and end to end
+// through the reference's restated host drivers (oracle/ref_runner.py,
+// tests/test_ref_e2e.py), with every remaining disagreement traced to a near-threshold
+// decision or one of the races R1-R5 (oracle/ref_trace.py, tests/test_ref_trace.py).
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -1426,12 +1430,56 @@ void oracle_get_frame_log(stspix_frame_log* out) { *out = g_last_log; }
 // reference's loop, update_params runs first and the border mask is the last
 // update_seg pass's find_border_pixels.  Outputs per id: h (NaN where the step scores
 // no ratio), the merge candidate, want (h > -2) and accept; the labels after the step.
+static int sm_step_impl(const float* img, const int32_t* seg_in, int H, int W,
+                        const stspix_config* cfg, int nbuf, const uint8_t* valid,
+                        const float* prior_count, const uint8_t* prop,
+                        const double* sample_sigma, int max_spix, int kind, int direction,
+                        const int32_t* shifted, const uint8_t* border_in,
+                        const int32_t* rid, int nspix_rel, int nspix_prev, double* h_out,
+                        int32_t* pair_out, uint8_t* want_out, uint8_t* accept_out,
+                        int32_t* seg_out, int* max_spix_out);
+
 int oracle_sm_step(const float* img, const int32_t* seg_in, int H, int W,
                    const stspix_config* cfg, int nbuf, const uint8_t* valid,
                    const float* prior_count, const uint8_t* prop, const double* sample_sigma,
                    int max_spix, int kind, int direction, const int32_t* shifted, double* h_out,
                    int32_t* pair_out, uint8_t* want_out, uint8_t* accept_out, int32_t* seg_out,
                    int* max_spix_out) {
+  return sm_step_impl(img, seg_in, H, W, cfg, nbuf, valid, prior_count, prop, sample_sigma,
+                      max_spix, kind, direction, shifted, nullptr, nullptr, 0, 0, h_out,
+                      pair_out, want_out, accept_out, seg_out, max_spix_out);
+}
+
+// The same step on the state a running loop holds (the divergence tracer,
+// oracle/ref_trace.py).  border (optional): the border mask the loop's last
+// update_seg pass left (find_border_pixels of the labels before that pass,
+// update_seg.cu:309-310) instead of the border of seg_in.  rid (optional): a merge
+// right after a propagated frame's relabel (prop.cu:326-468 runs update_params, then
+// relabel_spix, then the merge, with no update_params between): seg_in are the labels
+// update_params saw and rid[s] (s < nspix_rel) the id relabel_spix gave s (-1:
+// unchanged); the ids are changed as relabel() changes them (count copied to the new
+// id, the old id invalid, new ids >= nspix_prev not propagated) before the step, so
+// the step scores the stale per-id state the loop scores.
+int oracle_sm_step_ex(const float* img, const int32_t* seg_in, int H, int W,
+                      const stspix_config* cfg, int nbuf, const uint8_t* valid,
+                      const float* prior_count, const uint8_t* prop, const double* sample_sigma,
+                      int max_spix, int kind, int direction, const int32_t* shifted,
+                      const uint8_t* border, const int32_t* rid, int nspix_rel, int nspix_prev,
+                      double* h_out, int32_t* pair_out, uint8_t* want_out, uint8_t* accept_out,
+                      int32_t* seg_out, int* max_spix_out) {
+  return sm_step_impl(img, seg_in, H, W, cfg, nbuf, valid, prior_count, prop, sample_sigma,
+                      max_spix, kind, direction, shifted, border, rid, nspix_rel, nspix_prev,
+                      h_out, pair_out, want_out, accept_out, seg_out, max_spix_out);
+}
+
+static int sm_step_impl(const float* img, const int32_t* seg_in, int H, int W,
+                        const stspix_config* cfg, int nbuf, const uint8_t* valid,
+                        const float* prior_count, const uint8_t* prop,
+                        const double* sample_sigma, int max_spix, int kind, int direction,
+                        const int32_t* shifted, const uint8_t* border_in,
+                        const int32_t* rid, int nspix_rel, int nspix_prev, double* h_out,
+                        int32_t* pair_out, uint8_t* want_out, uint8_t* accept_out,
+                        int32_t* seg_out, int* max_spix_out) {
   Frame f;
   f.H = H; f.W = W; f.npix = H * W; f.img = img; f.cfg = *cfg;
   f.seg.assign(seg_in, seg_in + f.npix);
@@ -1449,7 +1497,23 @@ int oracle_sm_step(const float* img, const int32_t* seg_in, int H, int W,
   }
   f.max_spix = max_spix;
   update_params(f);
-  find_border(f.seg.data(), f.border.data(), H, W);
+  if (border_in) std::copy(border_in, border_in + f.npix, f.border.begin());
+  else find_border(f.seg.data(), f.border.data(), H, W);
+  if (rid) {
+    // relabel_spix_kernel (relabel.cu:86-120) as relabel() applies it
+    for (int s = 0; s < nspix_rel && s < nbuf; s++) {
+      const int n = rid[s];
+      if (n < 0 || n >= nbuf || n == s) continue;
+      sp.count[n] = sp.count[s];
+      sp.valid[s] = 0;
+      sp.valid[n] = 1;
+      if (n >= nspix_prev) sp.prop[n] = 0;
+    }
+    for (int& v : f.seg)
+      if (v >= 0 && v < nspix_rel && rid[v] >= 0 && rid[v] < nbuf) v = rid[v];
+    for (int s = 0; s < nspix_rel && s < nbuf; s++)
+      if (rid[s] > f.max_spix && rid[s] < nbuf) f.max_spix = rid[s];
+  }
   SmTrace tr;
   tr.h.assign(nbuf, NAN);
   tr.pair.assign(nbuf, -1);

@@ -116,6 +116,9 @@ def lib():
             _lib.oracle_sm_step.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Config), C.c_int,
                                             P, P, P, P, C.c_int, C.c_int, C.c_int, P, P, P, P,
                                             P, P, C.POINTER(C.c_int)]
+            _lib.oracle_sm_step_ex.argtypes = [
+                P, P, C.c_int, C.c_int, C.POINTER(Config), C.c_int, P, P, P, P, C.c_int,
+                C.c_int, C.c_int, P, P, P, C.c_int, C.c_int, P, P, P, P, P, C.POINTER(C.c_int)]
     return _lib
 
 
@@ -361,10 +364,14 @@ def rescale_u8(img, scale=255.0):
 
 
 def sm_step(img, labels, cfg: Config, nbuf, valid, prior_count, prop, sample_sigma, max_spix,
-            kind, direction, shifted=None):
+            kind, direction, shifted=None, relabel=None, border=None):
     """One split (kind 0 BASS / 2 propagated) or merge (kind 1 / 3) step on a given
     state (oracle_sm_step): per id the Hastings log-ratio (NaN where none is scored),
-    merge candidate, threshold test and decision, and the labels after the step."""
+    merge candidate, threshold test and decision, and the labels after the step.
+    relabel=(rid, nspix_prev): `labels` are those update_params saw and rid[s] the id a
+    propagated frame's relabel_spix gave s (-1: kept), applied before the step
+    (oracle_sm_step_ex).  The step keeps the relabelled labels.  border: the border
+    mask to use in place of the border of `labels` (the one a running loop holds)."""
     img = np.ascontiguousarray(img, np.float32)
     labels = np.ascontiguousarray(labels, np.int32)
     H, W = labels.shape
@@ -378,11 +385,19 @@ def sm_step(img, labels, cfg: Config, nbuf, valid, prior_count, prop, sample_sig
                want=np.zeros(nbuf, np.uint8), accept=np.zeros(nbuf, np.uint8),
                labels=np.zeros((H, W), np.int32))
     mx = C.c_int(0)
-    st = lib().oracle_sm_step(_p(img), _p(labels), H, W, C.byref(cfg), nbuf, _p(valid),
-                              _p(prior_count), _p(prop), _p(sample_sigma), int(max_spix),
-                              int(kind), int(direction), _p(shifted), _p(out["h"]),
-                              _p(out["pair"]), _p(out["want"]), _p(out["accept"]),
-                              _p(out["labels"]), C.byref(mx))
+    tail = (_p(out["h"]), _p(out["pair"]), _p(out["want"]), _p(out["accept"]),
+            _p(out["labels"]), C.byref(mx))
+    head = (_p(img), _p(labels), H, W, C.byref(cfg), nbuf, _p(valid), _p(prior_count), _p(prop),
+            _p(sample_sigma), int(max_spix), int(kind), int(direction), _p(shifted))
+    if relabel is None and border is None:
+        st = lib().oracle_sm_step(*head, *tail)
+    else:
+        rid, nspix_prev = relabel if relabel is not None else (None, 0)
+        rid = np.ascontiguousarray(rid, np.int32) if rid is not None else None
+        border = np.ascontiguousarray(border, np.uint8) if border is not None else None
+        st = lib().oracle_sm_step_ex(*head, _p(border) if border is not None else None,
+                                     _p(rid) if rid is not None else None,
+                                     len(rid) if rid is not None else 0, int(nspix_prev), *tail)
     out["max_spix"] = mx.value
     out["status"] = st
     return out

@@ -578,6 +578,10 @@ class Ref:
         max_spix = self.int_at(mx)
         flags = self.d2h(relabel, np.uint8, nspix)
         self.log.append(("relabel", int(flags.sum()), max_spix - max_spix_in))
+        if S.get("relabel_hook"):
+            rid = self.d2h(relabel_id, np.int32, nspix)
+            S["relabel_hook"](self.labels(seg, npix).reshape(H, W),
+                              np.where(flags > 0, rid, -1).astype(np.int32), nspix_prev)
         self.launch("relabel", "relabel_spix_kernel", nblk(npix),
                     [P(seg), P(sp), P(relabel), P(relabel_id), I(npix), I(nspix), I(nspix_prev)])
         dl = self.h2d(living.astype(np.int32))
@@ -992,6 +996,35 @@ class Ref:
         self._free_state(S, keep=("img", "seg"))
         self.free(S["border"])
         return seg, pr, nspix
+
+    def prop_frame(self, img_h: np.ndarray, labels_prev: np.ndarray, params_prev: dict,
+                   flow_h: np.ndarray, niters: int, sp_size: int, potts: float,
+                   sigma2_app: float, alpha: float, split_alpha: float) -> np.ndarray:
+        """One propagated frame of main_loop (pyapi.cu:120-170) from a given host state:
+        the previous frame's labels and SuperpixelParams fields (as recorded by
+        bist_forward(record=True)), the flow into this frame and the iteration count
+        the recorded run chose.  Returns the frame's int32 [H,W] labels.  Rerunning a
+        recorded frame this way measures how much the reference's races alone change
+        one frame."""
+        H, W = labels_prev.shape
+        npix = H * W
+        n = int(len(params_prev["counts"]))
+        pr = Params(self, n)
+        for name, dt, k in Params.FIELDS:
+            self.upload(getattr(pr, name), np.ascontiguousarray(params_prev[name][: n * k], dt))
+        spix = self.h2d(np.ascontiguousarray(labels_prev, np.int32))
+        flow = self.h2d(np.ascontiguousarray(flow_h, np.float32))
+        img = self.h2d(np.ascontiguousarray(img_h, np.float32))
+        filled, shifted = self.shift_and_fill(spix, pr, flow, H, W)
+        seg, pr2, _ = self.run_prop(img, H, W, niters, 4, 0, sp_size, sigma2_app, potts, alpha,
+                                    filled, shifted, pr, 1e-5, 1e-2, 0.0, split_alpha)
+        out = self.labels(seg, npix).reshape(H, W)
+        for b in (spix, flow, img, filled, shifted, seg):
+            self.free(b)
+        pr.free(self)
+        pr2.free(self)
+        self.sync()
+        return out
 
     def bist_forward(self, vid: np.ndarray, flows: np.ndarray, niters: int, sp_size: int,
                      potts: float, sigma2_app: float, alpha: float, split_alpha: float,

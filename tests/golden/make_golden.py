@@ -2,9 +2,10 @@
 
     python tests/golden/make_golden.py
 
-The reference (gauenk/st_spix bist_cuda) cannot be executed in this environment,
-so these vectors pin the oracle's restatement (and the GPU engine against it);
-they are not outputs of the reference itself.
+These vectors are outputs of the oracle's restatement, not of the reference: they
+pin the CPU tests and the GPU engine against the oracle.  The oracle itself is pinned
+to the reference's own kernels on the GPU (tests/test_ref_pin.py, test_ref_decisions.py,
+test_ref_e2e.py), which need a GPU and so cannot produce CPU fixtures.
 """
 import os
 import sys

@@ -49,3 +49,48 @@ def test_every_divergence_is_a_traced_tie(seed, variant):
         assert "sweep_arith" not in kinds, kinds.get("sweep_arith")
     if agree < 1.0:
         assert events, "labels differ without a traced tie"
+
+
+@pytest.mark.parametrize("variant", ["nofma", "stock"])
+def test_every_propagated_divergence_is_a_traced_tie(variant):
+    """Propagated frames (shift_and_fill + run_prop, split/merge of split_merge_prop.cu):
+    a fast-moving 120x160 video, every frame traced in lockstep from the reference's own
+    recorded previous state, against the engine's frame from the same state."""
+    from oracle import ref_trace
+    from st_spix_gb300 import bist_cuda
+    vid, flows, _ = synth.voronoi_video(120, 160, 8, 30, 0.05, 1, max_shift=6.0)
+    R = RR.Ref(variant)
+    R.bist_forward(vid, flows, 20, 15, 0.5, S2, LA, 0.0, True, record=True)
+    recs = R.frames
+    dev = torch.device("cuda")
+    tr = ref_trace.Tracer(variant)
+    rows = []
+    for t in range(1, vid.shape[0]):
+        prev = recs[t - 1]
+        n_prev = int(len(prev["params"]["counts"]))
+        pe = bist_cuda.SuperpixelParams(n_prev, dev)
+        pe.n = n_prev
+        for name, _, per in bist_cuda.PARAM_FIELDS:
+            getattr(pe, "_" + name).copy_(torch.from_numpy(
+                np.ascontiguousarray(prev["params"][name][: n_prev * per])))
+        flow = torch.from_numpy(np.ascontiguousarray(flows[t - 1])).to(dev)
+        filled, shifted = bist_cuda.shift_and_fill(torch.from_numpy(prev["labels"]).to(dev), pe,
+                                                   flow)
+        eng, _ = bist_cuda.run_prop(torch.from_numpy(vid[t]).to(dev), recs[t]["niters"], filled,
+                                    shifted, pe, sp_size=15)
+        lab_ref, events = tr.prop_frame_traced(vid[t], prev["labels"], prev["params"],
+                                               flows[t - 1], recs[t]["niters"], 15, S2, 0.5, LA,
+                                               0.0)
+        agree = label_agreement(eng.cpu().numpy(), lab_ref)
+        kinds = {}
+        for e in events:
+            kinds.setdefault(e[0], []).append(e[1])
+        rows.append((t, round(agree, 5), {k: (len(v), round(max(v), 4)) for k, v in kinds.items()}))
+        for k in ("split", "merge"):
+            for margin in kinds.get(k, []):
+                assert margin < NEAR, (t, k, margin)
+        if variant == "nofma":
+            assert "sweep_arith" not in kinds, (t, kinds.get("sweep_arith"))
+        if agree < 1.0:
+            assert events, (t, agree, "labels differ without a traced tie")
+    print(f"video_120x160_T8 [{variant}] (frame, engine~reference, traced events): {rows}")
