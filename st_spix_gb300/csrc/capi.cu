@@ -602,11 +602,10 @@ int upload(stspix_ctx* ctx, cudaStream_t st, const List& L, int off) {
 // ---------------------------------------------------------------------------
 // Stages over the first nb slots of a table.
 
-// kb_accumulate: a persistent grid of 8-warp blocks, about 2 segments per warp,
-// at most 8 blocks per SM.
+// kb_accumulate: one 8-warp block per 64 x 32 tile of the first nb slots.
 unsigned acc_blocks(const stspix_ctx* ctx, const List& L, int nb) {
-  const long long segs = L.segs_upto[nb];
-  return (unsigned)std::max(1LL, std::min<long long>((segs + 15) / 16, 8LL * ctx->num_sms));
+  (void)ctx;
+  return (unsigned)std::max(1LL, (long long)L.tiles_upto[1][nb]);
 }
 
 // update_params (update_params.cu:12-52): statistics + posterior.
@@ -636,10 +635,10 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
 // update_seg (update_seg.cu:281-311): niters_seg fused sweeps ping-ponging between
 // the labels and a scratch buffer; the border mask is only built when the next
 // iteration's merge reads it.
-// fuse_stats: the first sweep launch also clears the statistics and the last one adds
-// those of its final labels, so the next update_params skips its clear and accumulate
-// passes (needs two or more launches: no sweep reads the statistics in between).
-// *fused tells whether that happened.
+// fuse_stats: the first sweep launch also clears the statistics (no sweep reads them)
+// and the statistics of the final labels are added right after the last launch, so
+// the next update_params skips its clear and accumulate passes (needs two or more
+// launches).  *fused tells whether that happened.
 int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
                const stspix_config& cfg, bool need_border, bool fuse_stats, bool* fused) {
   ctx->cur_fam = STSPIX_FAM_SWEEP;
@@ -801,7 +800,7 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   const bool fuse = fuse_stats && total >= 2;
   while (done < nseg) {
     const bool pair = v2 >= 0 && nseg - done >= 2;
-    const int stats = !fuse ? 0 : launch == 0 ? 1 : launch == total - 1 ? 2 : 0;
+    const int stats = fuse && launch == 0 ? 1 : 0;
     if (pair) sweep2(v2, launch & 1, done > 0 ? 1 : 0, stats);
     else sweep1(v1, launch & 1, done > 0 ? 1 : 0, stats);
     done += pair ? 2 : 1;
@@ -809,6 +808,11 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   }
   *fused = fuse;
   if (launch & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
+  if (fuse) {
+    ctx->cur_fam = STSPIX_FAM_STATS;
+    LAUNCHG(kb_accumulate, acc_blocks(ctx, L, nb), 256, L.d, nb);
+    ctx->cur_fam = STSPIX_FAM_SWEEP;
+  }
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;
     LAUNCHB(kb_find_border, L.max_npix, L, nb);

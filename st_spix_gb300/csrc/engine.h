@@ -166,8 +166,17 @@ enum { kOpBegin = 0, kOpAfterHex = 1, kOpCompactN = 2, kOpCompactEnd = 3 };
 
 // ---------------------------------------------------------------------------
 // Device helpers shared by the kernels.
+// round(v * 2^shift) (round half to even, as llrintf(ldexpf(v, shift))) for
+// |v * 2^shift| < 2^41, without a float -> 64-bit integer conversion (those run on the
+// FP64 pipe, which GB300 has little of).  t = v * 2^shift is exact (a power of two);
+// h = trunc(t / 2^18) is an exact integer-valued float; l = t - h * 2^18 holds the bits
+// of t below 2^18 (same sign, |l| < 2^18) and is exact; h * 2^18 is an even integer, so
+// round(t) = h * 2^18 + round(l), ties included.
 __device__ __forceinline__ long long fx_q(float v, int shift) {
-  return __float2ll_rn(ldexpf(v, shift));
+  const float t = v * (float)(1u << shift);
+  const float h = truncf(t * 0x1p-18f);
+  const float l = t - h * 0x1p18f;
+  return (long long)__float2int_rz(h) * 262144LL + (long long)__float2int_rn(l);
 }
 __device__ __forceinline__ double fx_unq(long long q, int shift) {
   return ldexp((double)q, -shift);

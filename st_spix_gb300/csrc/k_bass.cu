@@ -243,86 +243,114 @@ __global__ void kb_init_prior_mu(const Slot* __restrict__ slots) {
 }
 
 // ---------------------------------------------------------------------------
-// Sufficient statistics (sum_by_label, update_params.cu:89-130), R1, as a
-// warp-aggregated scatter: a warp reads a 32-pixel row segment (coalesced labels and
-// colours), finds the runs of equal labels across its lanes, sums each run's
-// fixed-point colours with a warp prefix scan, and the run's last lane adds the
-// run into the label's sums with one set of 64-bit atomics (position sums of a run
-// are closed-form).  Integer sums, so the order of the additions does not matter.
-__device__ __forceinline__ void add_run_sums(const SpDev& sp, int k, int y, int x0, int x1,
-                                             long long sr, long long sg, long long sb) {
-  long long n = x1 - x0 + 1;
-  long long sx = (long long)(x0 + x1) * n / 2;
-  long long a = x0 - 1, b = x1;
-  long long sxx = b * (b + 1) * (2 * b + 1) / 6 - (a >= 0 ? a * (a + 1) * (2 * a + 1) / 6 : 0);
-  unsigned long long* acc = (unsigned long long*)(sp.acc + 8 * (size_t)k);
-  atomicAdd(&sp.count[k], (int)n);
-  atomicAdd(acc + 0, (unsigned long long)sr);
-  atomicAdd(acc + 1, (unsigned long long)sg);
-  atomicAdd(acc + 2, (unsigned long long)sb);
-  atomicAdd(acc + 3, (unsigned long long)sx);
-  atomicAdd(acc + 4, (unsigned long long)(n * y));
-  atomicAdd(acc + 5, (unsigned long long)sxx);
-  atomicAdd(acc + 6, (unsigned long long)(sx * y));
-  atomicAdd(acc + 7, (unsigned long long)(n * y * (long long)y));
+// Sufficient statistics (sum_by_label, update_params.cu:89-130), R1.  A warp owns a
+// 32 x 8 block of a frame: lane = column, and it holds the block's 8 labels and
+// fixed-point colours of its column in registers (every load issued before any is
+// used).  The warp then takes the block's labels one at a time (the first pending
+// label of the lowest lane that still has one): each lane sums its pixels of that
+// label, the warp adds the lanes' sums with full-warp reductions (colour sums in
+// 24-bit parts, positions relative to the block so they fit 32 bits) and one lane adds
+// the label's totals to its global sums with one set of 64-bit atomics.  A block holds
+// a few labels, so a few reductions and atomic sets serve 256 pixels (the row-segment
+// scatter this replaces, with a set of atomics per run of a 32-pixel row, took 50 us
+// per 8-frame 480x854 batch against 43 us here).  Integer sums: the totals do not
+// depend on the grouping or the order of the adds.
+__device__ __forceinline__ long long warp_sum64(long long v) {
+  // |v| < 2^54 per lane: v = hi * 2^24 + lo, lo in [0, 2^24)
+  const unsigned lo = (unsigned)(v & 0xFFFFFF);
+  const int hi = (int)(v >> 24);
+  return (long long)__reduce_add_sync(0xffffffffu, hi) * (1LL << 24) +
+         (long long)__reduce_add_sync(0xffffffffu, lo);
 }
 
-__device__ __forceinline__ long long warp_incl_scan(long long v, int lane) {
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const long long t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += t;
-  }
-  return v;
-}
-
-// Persistent grid: every warp walks the 32-pixel row segments of every slot in
-// turn (the first B slots), so frames of uneven size need no per-frame grid.
-__global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ slots, int B) {
-  pdl_enter();
+__device__ __forceinline__ void block_stats(const Slot& S, int bx, int by) {
   const int lane = threadIdx.x & 31;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int si = 0; si < B; si++) {
-  const Slot& S = slots[si];
   const int H = S.H, W = S.W;
-  const int spr = (W + 31) >> 5;                 // segments per row
-  const int nseg = H * spr;
   const SpDev& sp = S.sp;
   const int cap = sp.cap;
-  for (int sgi = wid; sgi < nseg; sgi += nw) {
-    const int y = sgi / spr, xb = (sgi - y * spr) << 5;
-    const int x = xb + lane;
-    int k = -1;
-    long long q0 = 0, q1 = 0, q2 = 0;
-    if (x < W) {
-      const size_t g = (size_t)y * W + x;
-      k = S.seg[g];
-      if (k >= 0) {
-        const float* p = S.img + 3 * g;
-        q0 = fx_q(p[0], kFxAppShift);
-        q1 = fx_q(p[1], kFxAppShift);
-        q2 = fx_q(p[2], kFxAppShift);
+  const int gx = bx + lane;
+  int lab[8];
+  float c[8][3];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int gy = by + i;
+    const bool in = gx < W && gy < H;
+    const size_t g = (size_t)gy * W + gx;
+    lab[i] = in ? S.seg[g] : -1;
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) c[i][ch] = in ? S.img[3 * g + ch] : 0.f;
+  }
+  long long q[8][3];
+  unsigned pend = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) q[i][ch] = fx_q(c[i][ch], kFxAppShift);
+    if (lab[i] >= 0 && lab[i] < cap) pend |= 1u << i;
+  }
+  for (;;) {
+    const unsigned any = __ballot_sync(0xffffffffu, pend != 0);
+    if (!any) break;
+    const int src = __ffs(any) - 1;
+    int first = -1;
+#pragma unroll
+    for (int i = 7; i >= 0; i--)
+      if ((pend >> i) & 1u) first = lab[i];
+    const int k = __shfl_sync(0xffffffffu, first, src);
+    unsigned m = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) m |= (unsigned)(lab[i] == k) << i;
+    pend &= ~m;              // every pixel of label k of this column is taken now
+    long long s0 = 0, s1 = 0, s2 = 0;
+    int sy = 0, syy = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      if ((m >> i) & 1u) {
+        s0 += q[i][0]; s1 += q[i][1]; s2 += q[i][2];
+        sy += i; syy += i * i;
       }
     }
-    const int kprev = __shfl_up_sync(0xffffffffu, k, 1);
-    const int knext = __shfl_down_sync(0xffffffffu, k, 1);
-    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != k);
-    const bool tail = lane == 31 || knext != k;
-    const long long p0 = warp_incl_scan(q0, lane);
-    const long long p1 = warp_incl_scan(q1, lane);
-    const long long p2 = warp_incl_scan(q2, lane);
-    // run start of this lane: the highest head at or below it
-    const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-    const int src = start > 0 ? start - 1 : 0;
-    long long b0 = __shfl_sync(0xffffffffu, p0, src);
-    long long b1 = __shfl_sync(0xffffffffu, p1, src);
-    long long b2 = __shfl_sync(0xffffffffu, p2, src);
-    if (start == 0) b0 = b1 = b2 = 0;
-    if (tail && k >= 0 && k < cap)
-      add_run_sums(sp, k, y, xb + start, x, p0 - b0, p1 - b1, p2 - b2);
+    const int n = __popc(m);
+    const int N = __reduce_add_sync(0xffffffffu, n);
+    const int SX = __reduce_add_sync(0xffffffffu, n * lane);
+    const int SXX = __reduce_add_sync(0xffffffffu, n * lane * lane);
+    const int SY = __reduce_add_sync(0xffffffffu, sy);
+    const int SYY = __reduce_add_sync(0xffffffffu, syy);
+    const int SXY = __reduce_add_sync(0xffffffffu, lane * sy);
+    const long long S0 = warp_sum64(s0), S1 = warp_sum64(s1), S2 = warp_sum64(s2);
+    if (lane == src) {
+      const long long ln = N, X = bx, Y = by;
+      unsigned long long* acc = (unsigned long long*)(sp.acc + 8 * (size_t)k);
+      atomicAdd(&sp.count[k], N);
+      atomicAdd(acc + 0, (unsigned long long)S0);
+      atomicAdd(acc + 1, (unsigned long long)S1);
+      atomicAdd(acc + 2, (unsigned long long)S2);
+      atomicAdd(acc + 3, (unsigned long long)(ln * X + SX));
+      atomicAdd(acc + 4, (unsigned long long)(ln * Y + SY));
+      atomicAdd(acc + 5, (unsigned long long)(ln * X * X + 2 * X * SX + SXX));
+      atomicAdd(acc + 6, (unsigned long long)(ln * X * Y + X * SY + Y * SX + SXY));
+      atomicAdd(acc + 7, (unsigned long long)(ln * Y * Y + 2 * Y * SY + SYY));
+    }
   }
+}
+
+// Grid: the 64 x 32 tiles of the first B slots (a block finds its slot by binary
+// search over the slots' first tiles); warp w takes the tile's 32 x 8 block
+// (w & 1, w >> 1).
+__global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ slots, int B) {
+  pdl_enter();
+  if (B <= 0) return;
+  const int t = blockIdx.x;
+  int lo = 0, hi = B - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (slots[mid].tile_base[1] <= t) lo = mid; else hi = mid - 1;
   }
+  const Slot& S = slots[lo];
+  const int tl = t - S.tile_base[1];
+  const int tiles_x = (S.W + 63) / 64;
+  const int warp = threadIdx.x >> 5;
+  block_stats(S, (tl % tiles_x) * 64 + (warp & 1) * 32, (tl / tiles_x) * 32 + (warp >> 1) * 8);
 }
 
 // Accumulator precision study: colour sums by per-pixel FP32 (mode 1, as the
@@ -688,65 +716,33 @@ struct SweepTile {
   static constexpr int kLX = TX + 2 * kSH, kLY = TY + 2 * kSH;      // staged labels
   static constexpr int kMaxList = (TX / 2 + kG0) * (TY / 2 + kG0);
   static_assert(TX + 2 * kG0 < 256 && TY + 2 * kG0 < 256, "list entries pack (ly << 8) | lx");
+  static_assert(kLX <= 128, "a label-region row is at most two 64-bit words");
   int L[kLX * kLY];
-  int L0[TX * TY];                    // the tile's labels before the launch's last sweep
   unsigned short list[4][kMaxList];   // border pixels of each parity phase, (ly << 8) | lx
   int cnt[4];
   // active-set sweeps: change flags of the label region as row bitmasks (bit x of
   // row y = label-region pixel (x, y)), dilated by 4 pixels
   unsigned long long act[2][kLY];
+  // label edges of the label region as row bitmasks: bit x of edE[.][y] is set when
+  // pixel (x, y) and its right neighbour differ, of edS[.][y] when (x, y) and the pixel
+  // below differ
+  unsigned long long edE[2][kLY];
+  unsigned long long edS[2][kLY];
+  // pixels of the tile whose label the launch's last sweep changed, as row bitmasks
+  // over label-region columns (the change flags the launch writes)
+  unsigned long long chg[TY][2];
 };
 
-// Statistics of a tile's final labels (the last sweep of an update_seg call adds
-// them, so the next update_params needs no separate pass): the same warp-run scatter
-// as kb_accumulate over the tile's rows (16-wide tiles: two rows per warp pass, a
-// row change starts a new run).  The sums are integers, so the totals equal
-// kb_accumulate's whatever the segmentation into runs.
-template <int TX, int TY>
-__device__ __noinline__ void tile_accumulate(const Slot& S, const int* __restrict__ L,
-                                                int kLX, int kSH, int tx0, int ty0) {
-  constexpr int kSegs = (TX + 31) / 32;               // 32-pixel segments per row
-  constexpr int kRows = TX >= 32 ? 1 : 32 / TX;       // rows per warp pass
-  constexpr int kPasses = (TY / kRows) * kSegs;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int H = S.H, W = S.W;
-  const SpDev& sp = S.sp;
-  const int cap = sp.cap;
-  for (int ps = warp; ps < kPasses; ps += blockDim.x >> 5) {
-    int row, x;
-    if (TX >= 32) { row = ps / kSegs; x = (ps % kSegs) * 32 + lane; }
-    else { row = ps * kRows + lane / TX; x = lane % TX; }
-    const int gx = tx0 + x, gy = ty0 + row;
-    int k = -1;
-    long long q0 = 0, q1 = 0, q2 = 0;
-    if (gx < W && gy < H) {
-      k = L[(row + kSH) * kLX + (x + kSH)];
-      if (k >= 0) {
-        const float* p = S.img + 3 * ((size_t)gy * W + gx);
-        q0 = fx_q(p[0], kFxAppShift);
-        q1 = fx_q(p[1], kFxAppShift);
-        q2 = fx_q(p[2], kFxAppShift);
-      }
-    }
-    const int kprev = __shfl_up_sync(0xffffffffu, k, 1);
-    const int knext = __shfl_down_sync(0xffffffffu, k, 1);
-    const int rprev = __shfl_up_sync(0xffffffffu, row, 1);
-    const int rnext = __shfl_down_sync(0xffffffffu, row, 1);
-    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || kprev != k || rprev != row);
-    const bool tail = lane == 31 || knext != k || rnext != row;
-    const long long p0 = warp_incl_scan(q0, lane);
-    const long long p1 = warp_incl_scan(q1, lane);
-    const long long p2 = warp_incl_scan(q2, lane);
-    const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-    const int src = start > 0 ? start - 1 : 0;
-    long long b0 = __shfl_sync(0xffffffffu, p0, src);
-    long long b1 = __shfl_sync(0xffffffffu, p1, src);
-    long long b2 = __shfl_sync(0xffffffffu, p2, src);
-    if (start == 0) b0 = b1 = b2 = 0;
-    if (tail && k >= 0 && k < cap)
-      add_run_sums(sp, k, gy, gx - (lane - start), gx, p0 - b0, p1 - b1, p2 - b2);
-  }
+// Bit masks over a label-region row (two 64-bit words, bit x of word x >> 6).
+__host__ __device__ constexpr unsigned long long bits_below(int n) {
+  return n <= 0 ? 0ull : n >= 64 ? ~0ull : ((1ull << n) - 1ull);
 }
+// bits [a, b) of word w
+__host__ __device__ constexpr unsigned long long range_word(int a, int b, int w) {
+  return bits_below(b - 64 * w) & ~bits_below(a - 64 * w);
+}
+constexpr unsigned long long kEvenBits = 0x5555555555555555ull;
+constexpr unsigned long long kOddBits = 0xAAAAAAAAAAAAAAAAull;
 
 // Active-set sweeps.  The parameters are fixed across the sweeps of one update_seg
 // call and a pixel's decision depends only on its 3x3 labels (after the earlier
@@ -763,10 +759,14 @@ __device__ __noinline__ void tile_accumulate(const Slot& S, const int* __restric
 template <int TX, int TY, int NS, int G>
 __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>& sm,
                                            const unsigned* lut_bits, int tx0, int ty0,
-                                           float s2, float potts, bool use_act) {
+                                           float s2, float potts, bool use_act, bool last) {
   constexpr int kLX = SweepTile<TX, TY, NS>::kLX;
-  constexpr int OFF = SweepTile<TX, TY, NS>::kSH - G;
+  constexpr int kLY = SweepTile<TX, TY, NS>::kLY;
+  constexpr int kSH = SweepTile<TX, TY, NS>::kSH;
+  constexpr int OFF = kSH - G;
   constexpr int kIX = TX + 2 * G, kIY = TY + 2 * G;
+  constexpr int kCK = (kLX + 31) / 32;
+  static_assert(OFF >= 1, "every listed pixel has its 4 neighbours in the label region");
   int* L = sm.L;
   auto& list = sm.list;
   int* cnt = sm.cnt;
@@ -775,61 +775,102 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
   const SweepRec* __restrict__ rec = S.sp.rec;
   const int cap = S.sp.cap;
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int ix0 = tx0 - G, iy0 = ty0 - G;
-  // Border mask at the sweep start (find_border_pixels, seg_utils.cu:164-195); the
-  // border pixels of parity class k inside the tile grown by G-k pixels are listed
-  // for phase k, so each phase scores only its border pixels, densely.  A warp takes
-  // one row of the grown region at a time in 32-pixel chunks: a row holds the two
-  // classes of its y parity, each appended with one shared atomic per chunk.  Rows
-  // whose (dilated) change mask is empty are skipped whole in active-set sweeps.
+  const int rx0 = tx0 - kSH, ry0 = ty0 - kSH;
+  // Border mask at the sweep start (find_border_pixels, seg_utils.cu:164-195) as row
+  // bitmasks: a pixel is a border pixel when one of its 4 neighbours carries another
+  // label (labels outside the image are staged as -1, so in-image pixels of the image's
+  // edge rows and columns count as border pixels as in the reference).  First the
+  // edges of the label region, one warp per row in 32-pixel chunks (rows with no
+  // change in reach are skipped in active-set sweeps).
+  for (int ay = OFF - 1 + warp; ay < OFF + kIY; ay += nwarps) {
+    if (use_act) {
+      const int an = min(ay + 1, kLY - 1);
+      if (!(sm.act[0][ay] | sm.act[1][ay] | sm.act[0][an] | sm.act[1][an])) continue;
+    }
+    unsigned e[kCK], d[kCK];
+#pragma unroll
+    for (int c = 0; c < kCK; c++) {
+      const int x = lane + 32 * c;
+      const bool in = x < kLX;
+      const int v = in ? L[ay * kLX + x] : -1;
+      const int r = (x + 1 < kLX) ? L[ay * kLX + x + 1] : v;
+      const int dn = (in && ay + 1 < kLY) ? L[(ay + 1) * kLX + x] : v;
+      e[c] = __ballot_sync(0xffffffffu, v != r);
+      d[c] = __ballot_sync(0xffffffffu, v != dn);
+    }
+    if (lane == 0) {
+      unsigned long long e0 = e[0], e1 = 0, d0 = d[0], d1 = 0;
+      if (kCK > 1) { e0 |= (unsigned long long)e[1 % kCK] << 32; d0 |= (unsigned long long)d[1 % kCK] << 32; }
+      if (kCK > 2) { e1 = e[2 % kCK]; d1 = d[2 % kCK]; }
+      if (kCK > 3) { e1 |= (unsigned long long)e[3 % kCK] << 32; d1 |= (unsigned long long)d[3 % kCK] << 32; }
+      sm.edE[0][ay] = e0; sm.edE[1][ay] = e1;
+      sm.edS[0][ay] = d0; sm.edS[1][ay] = d1;
+    }
+  }
+  __syncthreads();
+  // Then the border pixels of each parity class inside the tile grown by G minus the
+  // class (the class's phase), one warp per row: the row's border mask, restricted to
+  // the image, the active set and the two classes of the row's y parity, is counted
+  // per class (one shared atomic per class and row) and its set bits appended in
+  // ascending x order.
   {
-    constexpr int kChunks = (kIX + 31) / 32;
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
+    const unsigned long long img0 = range_word(-rx0, W - rx0, 0);
+    const unsigned long long img1 = range_word(-rx0, W - rx0, 1);
     for (int ly = warp; ly < kIY; ly += nwarps) {
       const int gy = iy0 + ly;
       if (gy < 0 || gy >= H) continue;
       const int ay = ly + OFF;                   // label-region row
-      unsigned long long m0 = ~0ull, m1 = ~0ull;
+      unsigned long long m0 = img0, m1 = img1;
       if (use_act) {
-        m0 = sm.act[0][ay];
-        m1 = sm.act[1][ay];
+        m0 &= sm.act[0][ay];
+        m1 &= sm.act[1][ay];
         if (!(m0 | m1)) continue;
       }
       const int cy = gy & 1;
-      const bool edge_row = gy < 1 || gy >= H - 1;
+      // the two classes of this row: (xo << 1) | cy, listed on the tile grown by
+      // G - class; x parity of a label-region column equals that of the image column
+      const int ga = G - cy, gb = G - (2 | cy);
+      const int ry = ay - kSH;                   // row relative to the tile
+      const bool ya = ry >= -ga && ry < TY + ga, yb = ry >= -gb && ry < TY + gb;
+      const unsigned long long k0 =
+          (ya ? range_word(kSH - ga, kSH + TX + ga, 0) & kEvenBits : 0ull) |
+          (yb ? range_word(kSH - gb, kSH + TX + gb, 0) & kOddBits : 0ull);
+      const unsigned long long k1 =
+          (ya ? range_word(kSH - ga, kSH + TX + ga, 1) & kEvenBits : 0ull) |
+          (yb ? range_word(kSH - gb, kSH + TX + gb, 1) & kOddBits : 0ull);
+      const unsigned long long e0 = sm.edE[0][ay], e1 = sm.edE[1][ay];
+      const unsigned long long b0 = e0 | (e0 << 1) | sm.edS[0][ay] | sm.edS[0][ay - 1];
+      const unsigned long long b1 =
+          e1 | (e1 << 1) | (e0 >> 63) | sm.edS[1][ay] | sm.edS[1][ay - 1];
+      m0 &= b0 & k0;
+      m1 &= b1 & k1;
+      if (!(m0 | m1)) continue;
+      const int na = __popcll(m0 & kEvenBits) + __popcll(m1 & kEvenBits);
+      const int nb = __popcll(m0 & kOddBits) + __popcll(m1 & kOddBits);
+      int base = 0;
+      if (lane < 2) {
+        const int n = lane ? nb : na;
+        if (n) base = atomicAdd(&cnt[(lane << 1) | cy], n);
+      }
+      int base_a = __shfl_sync(0xffffffffu, base, 0);
+      int base_b = __shfl_sync(0xffffffffu, base, 1);
+      const bool odd = lane & 1;
+      const unsigned mine = odd ? 0xAAAAAAAAu : 0x55555555u;
+      unsigned short* out = list[((int)odd << 1) | cy];
 #pragma unroll
-      for (int ch = 0; ch < kChunks; ch++) {
-        const int lx = ch * 32 + lane;
-        const int gx = ix0 + lx;
-        bool b = lx < kIX && gx >= 0 && gx < W;
-        if (b && use_act) {
-          const int ax = lx + OFF;
-          b = ((ax < 64 ? m0 >> ax : m1 >> (ax - 64)) & 1ull) != 0;
+      for (int c = 0; c < kCK; c++) {
+        const unsigned w = (unsigned)((c < 2 ? m0 : m1) >> (32 * (c & 1)));
+        if (!w) continue;
+        const int ax = 32 * c + lane;
+        if ((w >> lane) & 1u) {
+          const int pos = (odd ? base_b : base_a) + __popc(w & mine & lt);
+          out[pos] = (unsigned short)((ly << 8) | (ax - OFF));
         }
-        int c = 0;
-        if (b) {
-          if (!(edge_row || gx < 1 || gx >= W - 1)) {
-            const int p = ay * kLX + (lx + OFF);
-            const int C = L[p];
-            b = (C != L[p - kLX] || C != L[p + kLX] || C != L[p + 1] || C != L[p - 1]);
-          }
-          c = ((gx & 1) << 1) | cy;
-          const int grow = G - c;
-          b = b && gx >= tx0 - grow && gx < tx0 + TX + grow && gy >= ty0 - grow &&
-              gy < ty0 + TY + grow;
-        }
-#pragma unroll
-        for (int xo = 0; xo < 2; xo++) {
-          const int cc = (xo << 1) | cy;
-          const unsigned m = __ballot_sync(0xffffffffu, b && c == cc);
-          if (!m) continue;
-          const int leader = __ffs(m) - 1;
-          int at = 0;
-          if (lane == leader) at = atomicAdd(&cnt[cc], __popc(m));
-          at = __shfl_sync(0xffffffffu, at, leader);
-          if (b && c == cc) list[cc][at + __popc(m & lt)] = (unsigned short)((ly << 8) | lx);
-        }
+        base_a += __popc(w & 0x55555555u);
+        base_b += __popc(w & 0xAAAAAAAAu);
       }
     }
   }
@@ -885,10 +926,18 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
         else if (S >= 0) bl = S;
         else if (Wl >= 0) bl = Wl;
       }
-      L[p] = bl;
+      if (bl != C) {
+        L[p] = bl;
+        // a tile pixel changed by the launch's last sweep: its change flag (each pixel
+        // is scored once per sweep, so a changed pixel keeps its new label)
+        const int ty = lyi + OFF - kSH, ax = lxi + OFF;
+        if (last && ty >= 0 && ty < TY && ax >= kSH && ax < kSH + TX)
+          atomicOr(&sm.chg[ty][ax >> 6], 1ull << (ax & 63));
+      }
     }
     __syncthreads();
   }
+  (void)rx0; (void)ry0;
 }
 
 // Active-set sweeps.  The parameters are fixed across the sweeps of one update_seg
@@ -921,12 +970,9 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   const uint16_t* __restrict__ chg_in = (const uint16_t*)S.chg[parity ^ 1];
   uint16_t* __restrict__ chg_out = (uint16_t*)S.chg[parity];
   const int P16 = (W + 15) >> 4;
-  static_assert(kLX <= 128, "label region wider than two 64-bit words");
   // The label region is loaded first, into registers: warp w takes rows w, w + 8, ...
   // in 32-label chunks, every load issued before any is used, so the block waits for
-  // one memory round trip (overlapping the change-flag loads of active-set sweeps);
-  // the tile's part is kept in shared memory for the change flags at the end (no
-  // second read of the labels).
+  // one memory round trip (overlapping the change-flag loads of active-set sweeps).
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int kRW = (kLY + 7) / 8, kCK = (kLX + 31) / 32;
   int lv[kRW][kCK];
@@ -994,10 +1040,8 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
 #pragma unroll
         for (int c = 0; c < kCK; c++) {
           const int x = lane + 32 * c;
-          if (rr < kLY && x < kLX && in_tile(rr, x)) {
+          if (rr < kLY && x < kLX && in_tile(rr, x))
             seg_out[(size_t)(ry0 + rr) * W + (rx0 + x)] = lv[a][c];
-            if (stats == 2) L[rr * kLX + x] = lv[a][c];
-          }
         }
       }
       // zero change words of the tile's rows
@@ -1005,10 +1049,6 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       for (int i = threadIdx.x; i < kTY * kTW; i += blockDim.x) {
         const int gy = ty0 + i / kTW, wi = (tx0 >> 4) + i % kTW;
         if (gy < H && wi < P16) chg_out[(size_t)gy * P16 + wi] = 0;
-      }
-      if (stats == 2) {
-        __syncthreads();
-        tile_accumulate<TX, TY>(S, L, kLX, kSH, tx0, ty0);
       }
       return;
     }
@@ -1031,42 +1071,39 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
 #pragma unroll
     for (int c = 0; c < kCK; c++) {
       const int x = lane + 32 * c;
-      if (r < kLY && x < kLX) {
-        L[r * kLX + x] = lv[a][c];
-        if (NS == 1 && r >= kSH && r < kSH + kTY && x >= kSH && x < kSH + kTX)
-          sm.L0[(r - kSH) * kTX + (x - kSH)] = lv[a][c];
-      }
+      if (r < kLY && x < kLX) L[r * kLX + x] = lv[a][c];
     }
   }
   __syncthreads();
+  for (int i = threadIdx.x; i < 2 * kTY; i += blockDim.x) (&sm.chg[0][0])[i] = 0ull;
   if (NS == 1) {
-    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0);
+    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0, true);
   } else {
-    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0);
-    // the tile's labels before the last sweep (its change flags), fresh lists
-    for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x)
-      sm.L0[i] = L[(i / kTX + kSH) * kLX + (i % kTX + kSH)];
-    if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
-    __syncthreads();
-    sweep_pass<TX, TY, NS, 3>(S, sm, lut_bits, tx0, ty0, s2, potts, false);
+    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0, false);
+    if (threadIdx.x < 4) cnt[threadIdx.x] = 0;   // fresh lists (the phases' last barrier
+                                                 // ordered every read of the counts)
+    sweep_pass<TX, TY, NS, 3>(S, sm, lut_bits, tx0, ty0, s2, potts, false, true);
   }
-  // write back the tile, with change flags of the last sweep: a warp covers 32
-  // consecutive pixels of a row (16-wide tiles: two rows), and the lanes that start a
-  // 16-pixel group store its 16 change bits as one word
+  // write back the tile (a warp covers 32 consecutive pixels of a row; 16-wide tiles:
+  // two rows), then the change words of the last sweep: word i of a tile row holds
+  // tile columns 16 i .. 16 i + 15 = label-region columns kSH + 16 i ..
   for (int i = threadIdx.x; i < kTX * kTY; i += blockDim.x) {
     const int x = i % kTX, y = i / kTX;
     const int gx = tx0 + x, gy = ty0 + y;
-    bool changed = false;
-    if (gx < W && gy < H) {
-      const int v = L[(y + kSH) * kLX + (x + kSH)];
-      seg_out[gy * W + gx] = v;
-      changed = v != sm.L0[i];
-    }
-    const unsigned bits = __ballot_sync(0xffffffffu, changed);
-    if ((lane & 15) == 0 && gy < H && (gx >> 4) < P16)
-      chg_out[(size_t)gy * P16 + (gx >> 4)] = (uint16_t)(bits >> (lane & 16));
+    if (gx < W && gy < H) seg_out[(size_t)gy * W + gx] = L[(y + kSH) * kLX + (x + kSH)];
   }
-  if (stats == 2) tile_accumulate<TX, TY>(S, L, kLX, kSH, tx0, ty0);
+  constexpr int kTW = kTX / 16;
+  for (int i = threadIdx.x; i < kTY * kTW; i += blockDim.x) {
+    const int y = i / kTW, q = i % kTW;
+    const int gy = ty0 + y, wi = (tx0 >> 4) + q;
+    if (gy < H && wi < P16) {
+      const int b0 = kSH + 16 * q;
+      const unsigned long long lo = sm.chg[y][0], hi = sm.chg[y][1];
+      const unsigned long long v = b0 < 64 ? ((lo >> b0) | (b0 > 48 ? hi << (64 - b0) : 0ull))
+                                           : (hi >> (b0 - 64));
+      chg_out[(size_t)gy * P16 + wi] = (uint16_t)v;
+    }
+  }
 }
 
 template <int TX, int TY, int NS>
@@ -1109,8 +1146,7 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
 // One block per tile of the batch (grid = the batch's total tile count), one sweep
 // (kb_sweep_t*) or two consecutive sweeps (kb_sweep2_t*) per launch.
 // mode 0: every border pixel (first sweep of an update_seg call); 1: active set.
-// stats 1: also clear the statistics (first launch); 2: also add the statistics of the
-// final labels (last launch); 0: neither.
+// stats 1: also clear the statistics (first launch of a call); 0: not.
 #define STSPIX_SWEEP_KERNEL(name, TX, NS, MINB)                                          \
   __global__ void __launch_bounds__(256, MINB) name(const Slot* __restrict__ slots, int B, \
                                                     int parity, float s2, float potts,     \

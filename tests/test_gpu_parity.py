@@ -137,6 +137,24 @@ def test_run_bass_config0_100_iters():
     compare_params(gp.as_dict(), op)
 
 
+@pytest.mark.parametrize("lo,hi", [(-0.6, 1.4), (0.0, 1.0)])
+def test_run_bass_colours_outside_unit_range(lo, hi):
+    """Colours outside [0, 1] (e.g. CIELAB scaled as the colour front end writes it)
+    take the statistics' general fixed-point path; [0, 1] the 32-bit one.  Both must
+    give the oracle's labels and parameters bit for bit, also with a frame whose blocks
+    mix both kinds."""
+    img = small_frame(H=96, W=128, nseeds=30, seed=3)
+    img = (lo + (hi - lo) * img).astype(np.float32)
+    if lo < 0:
+        img[:, :64] = np.clip(img[:, :64], 0.0, 1.0)    # left half in range, right half not
+    glab, gp = bist_cuda.run_bass(cuda(img), niters=24, sm_period=4)
+    st, olab, op, n = O.run_bass(img, ocfg(niters=24, sm_period=4))
+    assert st == 0
+    assert gp.n == n
+    np.testing.assert_array_equal(glab.cpu().numpy(), olab)
+    compare_params(gp.as_dict(), op)
+
+
 def _oracle_params_for_gpu(op, n, dev="cuda"):
     p = bist_cuda.SuperpixelParams(n, dev)
     p.n = n
