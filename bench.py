@@ -33,10 +33,12 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(name="bist_stream_480x854_T30", H=480, W=854, T=30, nseeds=400, sigma=0.03,
                 sp_size=20, niters=20, prop_niters=20, sm_period=10, potts=0.5,
                 sigma2_app=0.009 ** 2, alpha=math.log(0.5), split_alpha=0.0)
-# Algorithmic bytes of one boundary sweep launch: label read 4 + image read 12 + label
-# write 4 = 20 B/px (a BASS pass = 4 sweeps + one statistics pass of 16 B/px = 96 B/px,
-# the scope's measurement rules; the statistics run as their own kernel).
-SWEEP_BYTES_PER_PX = 20
+# Algorithmic bytes of one BASS pass (the scope's measurement rules): 4 sweeps x (label
+# read 4 + image read 12 + label write 4) + the statistics of the new labels 16 = 96 B/px.
+# The 4 sweep launches of an update do the whole pass: they keep the statistics current
+# by moving those of every relabelled pixel (incremental statistics), so no separate
+# statistics pass runs between two updates: 24 B/px per sweep launch on average.
+SWEEP_BYTES_PER_PX = 24
 # DRAM bytes (read + write) per sweep launch from one ncu capture of the same workload
 # (a batch of 8 frames, mean of a full and an active-set sweep); a constant of that
 # capture, re-taken whenever the sweep kernel changes, not a live measurement.

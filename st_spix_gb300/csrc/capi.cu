@@ -635,10 +635,11 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
 // update_seg (update_seg.cu:281-311): niters_seg fused sweeps ping-ponging between
 // the labels and a scratch buffer; the border mask is only built when the next
 // iteration's merge reads it.
-// fuse_stats: the first sweep launch also clears the statistics (no sweep reads them)
-// and the statistics of the final labels are added right after the last launch, so
-// the next update_params skips its clear and accumulate passes (needs two or more
-// launches).  *fused tells whether that happened.
+// fuse_stats: every sweep launch moves the statistics of the pixels it relabels
+// (incremental statistics, see kb_sweep_t*), so the statistics stay those of the
+// current labels and the next update_params skips its clear and accumulate passes.
+// Not while tuning (the trial launches rerun the same sweep).  *fused tells whether
+// that happened.
 int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
                const stspix_config& cfg, bool need_border, bool fuse_stats, bool* fused) {
   ctx->cur_fam = STSPIX_FAM_SWEEP;
@@ -680,12 +681,6 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   auto ch = ctx->sweep_choice.find(key);
   int done = 0, launch = 0;
   int v1 = 1, v2 = -1;      // best single-sweep width, two-sweep width (-1: none)
-  // planned launches: the sweeps each covers
-  auto plan_launches = [&](int from, int v2_) {
-    int n = 0;
-    for (int it = from; it < nseg; it += (v2_ >= 0 && nseg - it >= 2) ? 2 : 1) n++;
-    return n;
-  };
   int forced = -1;     // the width stspix_config.sweep_tile pins
   for (int c = 0; c < kSweepVariants; c++)
     if (kSweepTileW[c] == cfg.sweep_tile) forced = c;
@@ -706,12 +701,11 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
     // first launch, the accumulation on the last (decided when it is issued)
     // Every trial runs kTuneRounds times and keeps its fastest run: other streams of
     // the device (concurrent lanes) only ever slow a run down.
-    const bool fuse_ok = fuse_stats && nseg >= 2;
     float t1[kSweepVariants];
     for (int r = 0; r < kTuneRounds; r++) {
       CK(cudaEventRecord(ctx->tune_ev[0], st));
       for (int c = 0; c < kSweepVariants; c++) {
-        sweep1(c, 0, 0, fuse_ok ? 1 : 0);
+        sweep1(c, 0, 0, 0);
         CK(cudaEventRecord(ctx->tune_ev[c + 1], st));
       }
       CK(cudaEventSynchronize(ctx->tune_ev[kSweepVariants]));
@@ -761,8 +755,8 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
         done = 2;
         launch = 2;
       }
-      // (both pair runs write the same labels; neither adds statistics, which would
-      // count them twice: when the pair ends the call the next update_params accumulates)
+      // (both pair runs write the same labels; neither moves statistics, which would
+      // count them twice: a tuned call ends with a full statistics pass)
       float t2[kSweepVariants];
       for (int r = 0; r < kTuneRounds; r++) {
         CK(cudaEventRecord(ctx->tune_ev[0], st));
@@ -796,23 +790,17 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
       return STSPIX_OK;
     }
   }
-  const int total = launch + plan_launches(done, v2);
-  const bool fuse = fuse_stats && total >= 2;
+  const bool fuse = fuse_stats && done == 0;   // no tuning trials in this call
   while (done < nseg) {
     const bool pair = v2 >= 0 && nseg - done >= 2;
-    const int stats = fuse && launch == 0 ? 1 : 0;
-    if (pair) sweep2(v2, launch & 1, done > 0 ? 1 : 0, stats);
-    else sweep1(v1, launch & 1, done > 0 ? 1 : 0, stats);
+    const int deltas = fuse ? 1 : 0;
+    if (pair) sweep2(v2, launch & 1, done > 0 ? 1 : 0, deltas);
+    else sweep1(v1, launch & 1, done > 0 ? 1 : 0, deltas);
     done += pair ? 2 : 1;
     launch++;
   }
   *fused = fuse;
   if (launch & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
-  if (fuse) {
-    ctx->cur_fam = STSPIX_FAM_STATS;
-    LAUNCHG(kb_accumulate, acc_blocks(ctx, L, nb), 256, L.d, nb);
-    ctx->cur_fam = STSPIX_FAM_SWEEP;
-  }
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;
     LAUNCHB(kb_find_border, L.max_npix, L, nb);
@@ -891,8 +879,8 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector
   const int P = cfg.sm_period > 0 ? cfg.sm_period : 4;
   const int maxn = L.B ? nit[0] : 0;
   int nb = L.B;
-  // the statistics of the first nb slots were added by the last sweep of the
-  // previous iteration (fused statistics; integer sums, so identical to a separate
+  // the statistics of the first nb slots were kept current by the previous
+  // iteration's sweeps (incremental statistics; integer sums, so identical to a full
   // pass); the int64 accumulator only
   bool stats_ready = false;
   const bool fuse = ctx->accumulator == 0;

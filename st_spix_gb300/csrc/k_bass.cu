@@ -709,6 +709,91 @@ constexpr int kReach = 4;             // a sweep's labels depend on labels this 
 // lists and scores the tile grown by G = 4 (NS - s) - 1 pixels (phase k on the tile
 // grown by G - k), so after sweep s the labels of the tile grown by 4 (NS - s - 1)
 // are exactly those of NS separate launches.
+// Incremental statistics.  Between two update_params of the BASS loop the labels
+// change only in the sweeps, so the statistics of the new labels are those of the old
+// ones plus, for every pixel a sweep relabels from C to bl, its contribution moved
+// from C to bl.  A sweep block collects the moves of its tile's own pixels in a small
+// table in shared memory (label -> count and sums, 32-bit fields: colours split into
+// 16-bit parts, positions relative to the tile) and adds each touched label's net
+// change to its 64-bit global sums once per launch.  Integer sums, so the result is
+// identical to clearing and summing every pixel again.
+constexpr int kDeltaTab = 64;         // labels a tile's moves can touch (a power of two)
+
+struct DeltaTab {
+  int key[kDeltaTab];                 // label, -1 free
+  int v[kDeltaTab][12];               // count, colour lo/hi x 3, sx, sy, sxx, sxy, syy
+};
+
+__device__ __forceinline__ int delta_slot(DeltaTab& tb, int k) {
+  const unsigned h = ((unsigned)k * 2654435761u) >> 26;
+#pragma unroll 1
+  for (int p = 0; p < kDeltaTab; p++) {
+    const int s = (int)((h + p) & (kDeltaTab - 1));
+    const int cur = ((volatile int*)tb.key)[s];
+    if (cur == k) return s;
+    if (cur == -1) {
+      const int old = atomicCAS(&tb.key[s], -1, k);
+      if (old == -1 || old == k) return s;
+    }
+  }
+  return -1;
+}
+
+// pixel (gx, gy), tile origin (tx0, ty0), moved from label C to label b.
+__device__ __forceinline__ void delta_move(DeltaTab& tb, const SpDev& sp, int C, int b, int gx,
+                                           int gy, int tx0, int ty0, float c0, float c1,
+                                           float c2) {
+  const bool unit = c0 >= 0.f && c0 <= 1.f && c1 >= 0.f && c1 <= 1.f && c2 >= 0.f && c2 <= 1.f;
+  const int sc = unit ? delta_slot(tb, C) : -1;
+  const int sb = unit ? delta_slot(tb, b) : -1;
+  if (sc >= 0 && sb >= 0) {
+    // colours in [0, 1]: the fixed-point value is one exact conversion, at most 2^28
+    const unsigned q0 = __float2uint_rn(c0 * 0x1p28f), q1 = __float2uint_rn(c1 * 0x1p28f),
+                   q2 = __float2uint_rn(c2 * 0x1p28f);
+    const int x = gx - tx0, y = gy - ty0;
+    const int d[12] = {1, (int)(q0 & 0xFFFF), (int)(q0 >> 16), (int)(q1 & 0xFFFF), (int)(q1 >> 16),
+                       (int)(q2 & 0xFFFF), (int)(q2 >> 16), x, y, x * x, x * y, y * y};
+#pragma unroll
+    for (int f = 0; f < 12; f++) {
+      atomicAdd(&tb.v[sb][f], d[f]);
+      atomicSub(&tb.v[sc][f], d[f]);
+    }
+    return;
+  }
+  // other colours, or a full table: the move goes to the global sums at once
+  const long long q[3] = {fx_q(c0, kFxAppShift), fx_q(c1, kFxAppShift), fx_q(c2, kFxAppShift)};
+  const long long X = gx, Y = gy;
+  const long long d[8] = {q[0], q[1], q[2], X, Y, X * X, X * Y, Y * Y};
+  unsigned long long* ab = (unsigned long long*)(sp.acc + 8 * (size_t)b);
+  unsigned long long* ac = (unsigned long long*)(sp.acc + 8 * (size_t)C);
+  atomicAdd(&sp.count[b], 1);
+  atomicSub(&sp.count[C], 1);
+#pragma unroll
+  for (int f = 0; f < 8; f++) {
+    atomicAdd(ab + f, (unsigned long long)d[f]);
+    atomicAdd(ac + f, (unsigned long long)(-d[f]));
+  }
+}
+
+// The table's net changes to the global sums (block-wide; after the last phase).
+__device__ __forceinline__ void delta_flush(DeltaTab& tb, const SpDev& sp, int tx0, int ty0) {
+  for (int i = threadIdx.x; i < kDeltaTab; i += blockDim.x) {
+    const int k = tb.key[i];
+    if (k < 0) continue;
+    const int* v = tb.v[i];
+    const long long n = v[0], X = tx0, Y = ty0;
+    const long long sx = v[7], sy = v[8];
+    const long long d[8] = {(long long)v[2] * 65536 + v[1], (long long)v[4] * 65536 + v[3],
+                            (long long)v[6] * 65536 + v[5], n * X + sx, n * Y + sy,
+                            n * X * X + 2 * X * sx + v[9], n * X * Y + X * sy + Y * sx + v[10],
+                            n * Y * Y + 2 * Y * sy + v[11]};
+    unsigned long long* acc = (unsigned long long*)(sp.acc + 8 * (size_t)k);
+    atomicAdd(&sp.count[k], v[0]);
+#pragma unroll
+    for (int f = 0; f < 8; f++) atomicAdd(acc + f, (unsigned long long)d[f]);
+  }
+}
+
 template <int TX, int TY, int NS>
 struct SweepTile {
   static constexpr int kSH = 4 * NS;                                 // label halo
@@ -731,6 +816,7 @@ struct SweepTile {
   // pixels of the tile whose label the launch's last sweep changed, as row bitmasks
   // over label-region columns (the change flags the launch writes)
   unsigned long long chg[TY][2];
+  DeltaTab delta;                     // statistics moves of the tile's pixels (deltas on)
 };
 
 // Bit masks over a label-region row (two 64-bit words, bit x of word x >> 6).
@@ -759,7 +845,8 @@ constexpr unsigned long long kOddBits = 0xAAAAAAAAAAAAAAAAull;
 template <int TX, int TY, int NS, int G>
 __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>& sm,
                                            const unsigned* lut_bits, int tx0, int ty0,
-                                           float s2, float potts, bool use_act, bool last) {
+                                           float s2, float potts, bool use_act, bool last,
+                                           bool deltas) {
   constexpr int kLX = SweepTile<TX, TY, NS>::kLX;
   constexpr int kLY = SweepTile<TX, TY, NS>::kLY;
   constexpr int kSH = SweepTile<TX, TY, NS>::kSH;
@@ -773,6 +860,7 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
   const int H = S.H, W = S.W;
   const float* __restrict__ img = S.img;
   const SweepRec* __restrict__ rec = S.sp.rec;
+  const SpDev& spd = S.sp;
   const int cap = S.sp.cap;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -929,10 +1017,13 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
       if (bl != C) {
         L[p] = bl;
         // a tile pixel changed by the launch's last sweep: its change flag (each pixel
-        // is scored once per sweep, so a changed pixel keeps its new label)
+        // is scored once per sweep, so a changed pixel keeps its new label); with
+        // deltas, the move of its statistics from C to bl
         const int ty = lyi + OFF - kSH, ax = lxi + OFF;
-        if (last && ty >= 0 && ty < TY && ax >= kSH && ax < kSH + TX)
-          atomicOr(&sm.chg[ty][ax >> 6], 1ull << (ax & 63));
+        if (ty >= 0 && ty < TY && ax >= kSH && ax < kSH + TX) {
+          if (last) atomicOr(&sm.chg[ty][ax >> 6], 1ull << (ax & 63));
+          if (deltas) delta_move(sm.delta, spd, C, bl, gx, gy, tx0, ty0, c0, c1, c2);
+        }
       }
     }
     __syncthreads();
@@ -952,7 +1043,7 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
 template <int TX, int TY, int NS>
 __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int parity, float s2,
                                            float potts, SweepTile<TX, TY, NS>& sm,
-                                           const unsigned* lut_bits, int mode, int stats) {
+                                           const unsigned* lut_bits, int mode, int deltas) {
   constexpr int kTX = TX, kTY = TY;
   constexpr int kSH = SweepTile<TX, TY, NS>::kSH;
   constexpr int kLX = SweepTile<TX, TY, NS>::kLX, kLY = SweepTile<TX, TY, NS>::kLY;
@@ -1076,14 +1167,25 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 2 * kTY; i += blockDim.x) (&sm.chg[0][0])[i] = 0ull;
+  if (deltas) {
+    for (int i = threadIdx.x; i < kDeltaTab; i += blockDim.x) {
+      sm.delta.key[i] = -1;
+#pragma unroll
+      for (int f = 0; f < 12; f++) sm.delta.v[i][f] = 0;
+    }
+  }
+  // (the listing barrier of the first pass orders these clears before any use)
   if (NS == 1) {
-    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0, true);
+    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0, true,
+                                       deltas != 0);
   } else {
-    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0, false);
+    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0, false,
+                                       deltas != 0);
     if (threadIdx.x < 4) cnt[threadIdx.x] = 0;   // fresh lists (the phases' last barrier
                                                  // ordered every read of the counts)
-    sweep_pass<TX, TY, NS, 3>(S, sm, lut_bits, tx0, ty0, s2, potts, false, true);
+    sweep_pass<TX, TY, NS, 3>(S, sm, lut_bits, tx0, ty0, s2, potts, false, true, deltas != 0);
   }
+  if (deltas) delta_flush(sm.delta, S.sp, tx0, ty0);   // after the last phase's barrier
   // write back the tile (a warp covers 32 consecutive pixels of a row; 16-wide tiles:
   // two rows), then the change words of the last sweep: word i of a tile row holds
   // tile columns 16 i .. 16 i + 15 = label-region columns kSH + 16 i ..
@@ -1108,7 +1210,7 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
 
 template <int TX, int TY, int NS>
 __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B, int parity,
-                                           float s2, float potts, int mode, int stats) {
+                                           float s2, float potts, int mode, int deltas) {
   __shared__ SweepTile<TX, TY, NS> sm;
   __shared__ unsigned lut_bits[8];
   if (threadIdx.x < 8) {
@@ -1126,33 +1228,21 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
   const Slot& S = slots[lo];
   const int tl = t - S.tile_base[v];
   const int tiles_x = (S.W + TX - 1) / TX;
-  if (stats == 1) {
-    // the clear_fields part of update_params (kb_clear_stats) for this tile's share of
-    // the ids; no sweep reads the counts or sums
-    const int ntiles = tiles_x * ((S.H + TY - 1) / TY);
-    const int cap = S.sp.cap, chunk = (cap + ntiles - 1) / ntiles;
-    const int k1 = min(cap, (tl + 1) * chunk);
-    for (int k = tl * chunk + threadIdx.x; k < k1; k += blockDim.x) {
-      S.sp.count[k] = 0;
-      long long* a = S.sp.acc + 8 * (size_t)k;
-#pragma unroll
-      for (int c = 0; c < 8; c++) a[c] = 0;
-    }
-  }
   sweep_tile<TX, TY, NS>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits, mode,
-                         stats);
+                         deltas);
 }
 
 // One block per tile of the batch (grid = the batch's total tile count), one sweep
 // (kb_sweep_t*) or two consecutive sweeps (kb_sweep2_t*) per launch.
 // mode 0: every border pixel (first sweep of an update_seg call); 1: active set.
-// stats 1: also clear the statistics (first launch of a call); 0: not.
+// deltas 1: move the statistics of every relabelled tile pixel (incremental
+// statistics: the sums of the labels at the call's start stay current); 0: not.
 #define STSPIX_SWEEP_KERNEL(name, TX, NS, MINB)                                          \
   __global__ void __launch_bounds__(256, MINB) name(const Slot* __restrict__ slots, int B, \
                                                     int parity, float s2, float potts,     \
-                                                    int mode, int stats) {                 \
+                                                    int mode, int deltas) {                \
     pdl_enter();                                                                          \
-    sweep_flat<TX, 32, NS>(slots, B, parity, s2, potts, mode, stats);                     \
+    sweep_flat<TX, 32, NS>(slots, B, parity, s2, potts, mode, deltas);                    \
   }
 STSPIX_SWEEP_KERNEL(kb_sweep_t32, 32, 1, 6)
 STSPIX_SWEEP_KERNEL(kb_sweep_t64, 64, 1, 6)
