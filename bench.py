@@ -461,6 +461,22 @@ def run_batch_mode(args, world, rank):
     stop.set()
     th.join(timeout=5)
     gpu_ms = bist_cuda._ctx(dev).last_batch_ms()
+    # the same batch with the persistent work-queue sweep in place of one block per tile
+    def one_batch_queue():
+        fq = [batch.Frame(img=im, sp_size=sp) for im, sp in imgs]
+        batch.process_batch(fq, sweep_queue=1, **cfg)
+        return fq
+
+    for _ in range(args.warmup):
+        one_batch_queue()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fq = one_batch_queue()
+    torch.cuda.synchronize()
+    elapsed_q = time.perf_counter() - t0
+    gpu_ms_q = bist_cuda._ctx(dev).last_batch_ms()
+    same_q = sum(int(torch.equal(a.labels, b.labels)) for a, b in zip(fr, fq))
     # plain per-frame path on the same frames (one untimed pass first: workspace
     # growth and tile tuning for the single-frame sizes)
     for im, sp in imgs:
@@ -487,6 +503,12 @@ def run_batch_mode(args, world, rank):
         "plain_per_frame_fps": b["n"] / plain,
         "batched_vs_plain": value / (b["n"] / plain),
         "frames_identical_to_plain": f"{same}/{b['n']}",
+        "work_queue_sweep": {"value": b["n"] * args.steps / elapsed_q, "unit": "frames/s",
+                             "batch_gpu_ms": gpu_ms_q,
+                             "frames_identical": f"{same_q}/{b['n']}",
+                             "note": "the same batch with the persistent work-queue sweep "
+                                     "(stspix_config.sweep_queue = 1) in place of one block "
+                                     "per tile"},
         "clocks": summarize_clocks(clk_lines),
     }
     print(json.dumps(line), flush=True)
@@ -787,6 +809,8 @@ def main():
     ap.add_argument("--sweep-tile", type=int, default=0, choices=[0, 16, 32, 64],
                     help="stream: single-sweep tile width (0 autotuned); profiler runs pin "
                          "the width the autotuner picks without the profiler")
+    ap.add_argument("--sweep-queue", type=int, default=0, choices=[0, 1],
+                    help="stream: 1 runs single sweeps as the persistent work-queue kernel")
     ap.add_argument("--no-group-sizes", action="store_true",
                     help="serve: batches take frames oldest first across sizes (default: the "
                          "oldest frame's size first)")
@@ -841,7 +865,8 @@ def main():
     cfg = dict(niters=w["niters"], sp_size=w["sp_size"], potts=w["potts"],
                sigma2_app=w["sigma2_app"], alpha=w["alpha"], split_alpha=w["split_alpha"],
                sm_period=w["sm_period"], prop_niters=w["prop_niters"],
-               sweep_schedule=args.sweep_schedule, sweep_tile=args.sweep_tile)
+               sweep_schedule=args.sweep_schedule, sweep_tile=args.sweep_tile,
+               sweep_queue=args.sweep_queue)
 
     # one video per stream (seed = rank * S + i), generated on the device; the host
     # copies feed the end-to-end leg
@@ -1101,6 +1126,7 @@ def main():
         "config": workload_config(),
         "run": {"streams_per_gpu": S, "lanes": NL, "batch_per_lane": B0,
                    "sweep_schedule": args.sweep_schedule, "sweep_tile": args.sweep_tile,
+                   "sweep_queue": args.sweep_queue,
                    "batch_graphs": not args.no_batch_graphs,
                    "step": "all %d frames of every stream; frame t of a lane's streams is "
                            "one batch" % T,

@@ -88,6 +88,9 @@ typedef struct stspix_config {
   int   sweep_tile;      /* tile width: 0 autotuned (default), or 16, 32, 64 (no
                             timing; schedules 0 and 1 then run single sweeps of that
                             width, schedule 2 two-sweep launches of that width)      */
+  int   sweep_queue;     /* single-sweep launches: 0 one block per tile (default), 1 a
+                            persistent work-queue kernel (one resident block set that
+                            takes tiles from an atomic counter); same labels         */
 } stspix_config;
 
 void stspix_default_config(stspix_config* cfg);

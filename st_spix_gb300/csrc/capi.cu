@@ -117,7 +117,8 @@ struct stspix_ctx {
   long long tunes = 0;
   int accumulator = 0;            // cfg.accumulator of the batch being run
   int* body_iters = nullptr;       // device: [0] fill-loop iterations run (launch count),
-                                   // [1] the fill compaction's block counter
+                                   // [1] the fill compaction's block counter, [2..3] the
+                                   // work-queue sweep's tile and block counters
   int* body_iters_host = nullptr;  // pinned
   long long body_iters_seen = 0;
   // bist_forward's stream state
@@ -413,6 +414,9 @@ void preload_kernels() {
       (const void*)kb_sweep2_t32,
       (const void*)kb_sweep2_t16,
       (const void*)kb_sweep2_t64,
+      (const void*)kb_sweepq_t32,
+      (const void*)kb_sweepq_t64,
+      (const void*)kb_sweepq_t16,
       (const void*)kb_copy_labels,
       (const void*)kb_read_params,
       (const void*)kb_save_prev,
@@ -650,6 +654,23 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   // Launch j reads the labels of parity j & 1 and writes the other buffer.
   auto sweep1 = [&](int v, int parity, int mode, int stats) {
     const unsigned g = (unsigned)std::max(1, L.tiles_upto[v][nb]);
+    if (cfg.sweep_queue) {
+      // persistent work queue: the blocks the SMs hold at once (6 per SM), at most one
+      // per tile
+      unsigned* q = (unsigned*)(ctx->body_iters + 2);
+      const unsigned gq = std::min<unsigned>(g, 6u * (unsigned)ctx->num_sms);
+      const int nt = (int)g;
+      if (v == 1)
+        LAUNCHG(kb_sweepq_t64, gq, 256, L.d, nb, nt, q, parity, cfg.sigma2_app, cfg.potts, mode,
+                stats);
+      else if (v == 2)
+        LAUNCHG(kb_sweepq_t16, gq, 256, L.d, nb, nt, q, parity, cfg.sigma2_app, cfg.potts, mode,
+                stats);
+      else
+        LAUNCHG(kb_sweepq_t32, gq, 256, L.d, nb, nt, q, parity, cfg.sigma2_app, cfg.potts, mode,
+                stats);
+      return;
+    }
     if (v == 1)
       LAUNCHG(kb_sweep_t64, g, 256, L.d, nb, parity, cfg.sigma2_app, cfg.potts, mode, stats);
     else if (v == 2)
@@ -1509,6 +1530,7 @@ void stspix_default_config(stspix_config* c) {
   c->accumulator = 0;
   c->sweep_schedule = 0;
   c->sweep_tile = 0;
+  c->sweep_queue = 0;
 }
 
 int stspix_version(void) { return 2; }
@@ -1534,12 +1556,12 @@ int stspix_create(stspix_ctx** out, int device) {
   }
   // slot tables for 256 frames per batch from the start: they never move for
   // batches up to that size, so the graphs that point at them stay valid
-  if (ensure_bcap(ctx, 256) != STSPIX_OK || cudaMalloc(&ctx->body_iters, 2 * sizeof(int)) != cudaSuccess ||
+  if (ensure_bcap(ctx, 256) != STSPIX_OK || cudaMalloc(&ctx->body_iters, 4 * sizeof(int)) != cudaSuccess ||
       cudaMallocHost(&ctx->body_iters_host, sizeof(int)) != cudaSuccess) {
     delete ctx;
     return STSPIX_ERR_NOMEM;
   }
-  cudaMemset(ctx->body_iters, 0, 2 * sizeof(int));
+  cudaMemset(ctx->body_iters, 0, 4 * sizeof(int));
   cudaEventCreate(&ctx->batch_ev[0]);
   cudaEventCreate(&ctx->batch_ev[1]);
   for (auto& e : ctx->tune_ev) cudaEventCreate(&e);

@@ -1232,6 +1232,66 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
                          deltas);
 }
 
+// Persistent work-queue form of the single-sweep launch: a resident set of blocks
+// (the SM count times the blocks an SM holds, at most the tile count) takes the
+// batch's tiles in index order from an atomic counter, queue[0], and sweeps each as
+// the one-block-per-tile kernel does (the same labels: a launch reads only the labels
+// at its start).  The last block to finish, counted in queue[1], sets both counters
+// back to zero for the next launch (stream order and the dependent-launch wait make
+// that store visible to it).  No block waits on another.
+template <int TX, int TY>
+__device__ __forceinline__ void sweep_queue(const Slot* __restrict__ slots, int B, int ntiles,
+                                            unsigned* queue, int parity, float s2, float potts,
+                                            int mode, int deltas) {
+  __shared__ SweepTile<TX, TY, 1> sm;
+  __shared__ unsigned lut_bits[8];
+  __shared__ int next;
+  if (threadIdx.x < 8) {
+    unsigned w = 0;
+    for (int b = 0; b < 32; b++) w |= (unsigned)(c_simple_lut[threadIdx.x * 32 + b] != 0) << b;
+    lut_bits[threadIdx.x] = w;
+  }
+  const int v = TX == 32 ? 0 : TX == 64 ? 1 : 2;   // which tile_base of the slots
+  for (;;) {
+    if (threadIdx.x == 0) next = (int)atomicAdd(&queue[0], 1u);
+    __syncthreads();
+    const int t = next;
+    if (t >= ntiles) break;
+    int lo = 0, hi = B - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (slots[mid].tile_base[v] <= t) lo = mid; else hi = mid - 1;
+    }
+    const Slot& S = slots[lo];
+    const int tl = t - S.tile_base[v];
+    const int tiles_x = (S.W + TX - 1) / TX;
+    sweep_tile<TX, TY, 1>(S, tl % tiles_x, tl / tiles_x, parity, s2, potts, sm, lut_bits, mode,
+                          deltas);
+    __syncthreads();          // the tile's shared memory and `next` are free again
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&queue[1], 1u) == gridDim.x - 1) {
+      queue[0] = 0u;
+      queue[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+#define STSPIX_SWEEPQ_KERNEL(name, TX, MINB)                                                \
+  __global__ void __launch_bounds__(256, MINB) name(const Slot* __restrict__ slots, int B,    \
+                                                    int ntiles, unsigned* queue, int parity,  \
+                                                    float s2, float potts, int mode,          \
+                                                    int deltas) {                             \
+    pdl_enter();                                                                             \
+    sweep_queue<TX, 32>(slots, B, ntiles, queue, parity, s2, potts, mode, deltas);           \
+  }
+STSPIX_SWEEPQ_KERNEL(kb_sweepq_t32, 32, 6)
+STSPIX_SWEEPQ_KERNEL(kb_sweepq_t64, 64, 6)
+STSPIX_SWEEPQ_KERNEL(kb_sweepq_t16, 16, 6)
+#undef STSPIX_SWEEPQ_KERNEL
+
 // One block per tile of the batch (grid = the batch's total tile count), one sweep
 // (kb_sweep_t*) or two consecutive sweeps (kb_sweep2_t*) per launch.
 // mode 0: every border pixel (first sweep of an update_seg call); 1: active set.

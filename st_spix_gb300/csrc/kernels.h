@@ -41,18 +41,26 @@ __global__ void kb_store_sample(const Slot* slots);
 __global__ void kb_find_border(const Slot* slots);
 // boundary sweep, one block per 32x32 / 64x32 / 16x32 tile of the batch
 __global__ void kb_sweep_t32(const Slot* slots, int B, int parity, float s2, float potts,
-                             int mode, int stats);
+                             int mode, int deltas);
 __global__ void kb_sweep_t64(const Slot* slots, int B, int parity, float s2, float potts,
-                             int mode, int stats);
+                             int mode, int deltas);
 __global__ void kb_sweep_t16(const Slot* slots, int B, int parity, float s2, float potts,
-                             int mode, int stats);
+                             int mode, int deltas);
+// the same single sweep as a persistent work-queue kernel (queue: 2 counters, zero
+// between launches)
+__global__ void kb_sweepq_t32(const Slot* slots, int B, int ntiles, unsigned* queue, int parity,
+                              float s2, float potts, int mode, int deltas);
+__global__ void kb_sweepq_t64(const Slot* slots, int B, int ntiles, unsigned* queue, int parity,
+                              float s2, float potts, int mode, int deltas);
+__global__ void kb_sweepq_t16(const Slot* slots, int B, int ntiles, unsigned* queue, int parity,
+                              float s2, float potts, int mode, int deltas);
 // two consecutive sweeps per launch (8-pixel halo)
 __global__ void kb_sweep2_t32(const Slot* slots, int B, int parity, float s2, float potts,
-                              int mode, int stats);
+                              int mode, int deltas);
 __global__ void kb_sweep2_t16(const Slot* slots, int B, int parity, float s2, float potts,
-                              int mode, int stats);
+                              int mode, int deltas);
 __global__ void kb_sweep2_t64(const Slot* slots, int B, int parity, float s2, float potts,
-                              int mode, int stats);
+                              int mode, int deltas);
 __global__ void kb_copy_labels(const Slot* slots);
 __global__ void kb_read_params(const Slot* slots);
 __global__ void kb_save_prev(const Slot* slots);

@@ -220,3 +220,9 @@ def test_uneven_batch_at_full_size_matches_oracle_and_plain_path():
         alone, p = bist_cuda.run_bass(cuda(img), sp_size=sp, **cfg)
         np.testing.assert_array_equal(alone.cpu().numpy(), lab)
         assert p.n == n
+    # the persistent work-queue sweep gives the same labels on the same batch
+    fq = [batch.Frame(img=cuda(img), sp_size=sp) for img, sp in imgs]
+    batch.process_batch(fq, sweep_queue=1, **cfg)
+    for a, b in zip(fr, fq):
+        assert b.status == 0
+        assert torch.equal(a.labels, b.labels)

@@ -101,3 +101,27 @@ def test_gpu_forced_sweep_tile_matches_oracle(tile, schedule):
                                      sweep_tile=tile, sweep_schedule=schedule)
         torch.cuda.current_stream().synchronize()
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tile", [0, 16, 32, 64])
+def test_gpu_work_queue_sweep_matches_oracle(tile):
+    """The persistent work-queue sweep (resident blocks taking tiles from an atomic
+    counter that resets itself after each launch) gives the oracle's labels, with the
+    autotuned width and every forced width, over many consecutive launches of one
+    context (a counter left non-zero would skip tiles of the next launch)."""
+    import torch
+    from st_spix_gb300 import bist_cuda
+    g = load("bist_video_48x64x3.npz")
+    st, ref, _ = O.bist_forward(g["vid"], g["flows"], O.default_config(niters=int(g["niters"])),
+                                True)
+    assert st == 0
+    with torch.cuda.stream(torch.cuda.Stream()):
+        for _ in range(2):
+            out = bist_cuda.bist_forward(torch.from_numpy(g["vid"]).cuda(),
+                                         torch.from_numpy(g["flows"]).cuda(), int(g["niters"]),
+                                         15, 0.5, 0.009 ** 2, float(np.log(0.5)), 0.0, True,
+                                         False, sweep_tile=tile, sweep_schedule=1,
+                                         sweep_queue=1)
+            torch.cuda.current_stream().synchronize()
+            np.testing.assert_array_equal(out.cpu().numpy(), ref)
