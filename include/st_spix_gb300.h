@@ -91,6 +91,11 @@ typedef struct stspix_config {
   int   sweep_queue;     /* single-sweep launches: 0 one block per tile (default), 1 a
                             persistent work-queue kernel (one resident block set that
                             takes tiles from an atomic counter); same labels         */
+  int   lab_ingest;      /* 0 frames used as given (default; the reference's
+                            bist_forward ignores its rgb2lab flag), 1 every frame is
+                            converted sRGB -> CIELAB (the reference's rgb2lab steps,
+                            first channel blue) once at ingest into an engine buffer,
+                            which the statistics and sweeps then read              */
 } stspix_config;
 
 void stspix_default_config(stspix_config* cfg);

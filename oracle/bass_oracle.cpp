@@ -1255,6 +1255,7 @@ void oracle_default_config(stspix_config* c) {
   c->sweep_schedule = 0;   // a launch schedule of the engine; the oracle sweeps one by one
   c->sweep_tile = 0;
   c->sweep_queue = 0;
+  c->lab_ingest = 0;
 }
 
 int oracle_hex_count(int H, int W, int sp_size) {

@@ -40,7 +40,8 @@ class Config(C.Structure):
                 ("merge_alpha", C.c_float), ("sigma2_size", C.c_float),
                 ("thresh_relabel", C.c_float), ("thresh_new", C.c_float),
                 ("accumulator", C.c_int), ("sweep_schedule", C.c_int),
-                ("sweep_tile", C.c_int), ("sweep_queue", C.c_int)]
+                ("sweep_tile", C.c_int), ("sweep_queue", C.c_int),
+                ("lab_ingest", C.c_int)]
 
 
 class ParamsC(C.Structure):

@@ -43,8 +43,9 @@ struct Buf {
 
 // Working buffers of one batch position.
 struct SlotWork {
-  std::vector<Buf> pix, sp;
-  int npix_cap = 0, sp_cap = 0;
+  std::vector<Buf> pix, sp, lab;
+  int npix_cap = 0, sp_cap = 0, lab_cap = 0;
+  float* lab_img = nullptr;        // CIELAB frame of stspix_config.lab_ingest (on demand)
   Slot s{};
 };
 
@@ -116,6 +117,7 @@ struct stspix_ctx {
   cudaEvent_t tune_ev[kSweepVariants + 1] = {};
   long long tunes = 0;
   int accumulator = 0;            // cfg.accumulator of the batch being run
+  int lab_ingest = 0;             // cfg.lab_ingest of the batch being run
   int* body_iters = nullptr;       // device: [0] fill-loop iterations run (launch count),
                                    // [1] the fill compaction's block counter, [2..3] the
                                    // work-queue sweep's tile and block counters
@@ -363,6 +365,18 @@ int ensure_slot(stspix_ctx* ctx, int i, int npix, int sp_cap) {
   return STSPIX_OK;
 }
 
+// The CIELAB frame buffer of slot position i (stspix_config.lab_ingest), npix pixels.
+int ensure_lab(stspix_ctx* ctx, int i, int npix) {
+  SlotWork& w = ctx->work[i];
+  if (npix <= w.lab_cap) return STSPIX_OK;
+  std::lock_guard<std::mutex> lk(g_device_mu);
+  CK(cudaDeviceSynchronize());
+  free_list(w.lab);
+  AL(w.lab, w.lab_img, 3 * (size_t)npix);
+  w.lab_cap = npix;
+  return STSPIX_OK;
+}
+
 // Graphs hold the slot-table and staging addresses: dropped when those move.
 void drop_fill_graphs(stspix_ctx* ctx) {
   for (auto& kv : ctx->fill_graphs) {
@@ -472,7 +486,8 @@ void preload_kernels() {
       (const void*)kb_accumulate_fp, (const void*)kb_accumulate_fp_store,
       (const void*)kb_accumulate_fp_clear, (const void*)k_label_stats,
       (const void*)k_label_stats_out,
-      (const void*)k_rgb2lab, (const void*)k_lab2rgb, (const void*)k_rescale_u8};
+      (const void*)k_rgb2lab, (const void*)k_lab2rgb, (const void*)k_rescale_u8,
+      (const void*)kb_lab_ingest};
     for (const void* f : fns) {
       cudaFuncAttributes a;
       cudaError_t e = cudaFuncGetAttributes(&a, f);
@@ -541,6 +556,11 @@ int slot_cap(const FrameDesc& f) {
 Slot make_slot(stspix_ctx* ctx, const FrameDesc& f, int cap) {
   Slot s = ctx->work[f.slot].s;
   s.img = f.img;
+  s.img_src = nullptr;
+  if (ctx->lab_ingest) {          // converted at ingest into the slot's CIELAB buffer
+    s.img_src = f.img;
+    s.img = ctx->work[f.slot].lab_img;
+  }
   s.seg = f.seg;
   s.H = f.H; s.W = f.W; s.npix = f.H * f.W;
   s.cap = cap;
@@ -1184,6 +1204,7 @@ int batch_head(stspix_ctx* ctx, cudaStream_t st, int stages, const List& La, con
     return r;
   ctx->cur_fam = STSPIX_FAM_OTHER;
   LAUNCHS(kb_scalars, La, La.B, (int)kOpBegin);
+  if (ctx->lab_ingest) LAUNCHB(kb_lab_ingest, La.max_npix, La, La.B);
   if ((stages & kStageShift) && (r = shift_fill(ctx, st, Lp))) return r;
   return bass_init(ctx, st, Lb);
 }
@@ -1295,11 +1316,13 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
   const int B = (int)fr.size();
   int r;
   ctx->accumulator = cfg.accumulator;
+  ctx->lab_ingest = cfg.lab_ingest ? 1 : 0;
   if ((r = ensure_bcap(ctx, B))) return r;
   std::vector<int> caps(B);
   for (int i = 0; i < B; i++) {
     caps[i] = slot_cap(fr[i]);
     if ((r = ensure_slot(ctx, fr[i].slot, fr[i].H * fr[i].W, caps[i]))) return r;
+    if (ctx->lab_ingest && (r = ensure_lab(ctx, fr[i].slot, fr[i].H * fr[i].W))) return r;
   }
   std::vector<Slot> all, bass, prop;
   for (int i = 0; i < B; i++) {
@@ -1576,7 +1599,7 @@ int stspix_destroy(stspix_ctx* ctx) {
   std::lock_guard<std::mutex> lk(g_device_mu);
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
-  for (auto& w : ctx->work) { free_list(w.pix); free_list(w.sp); }
+  for (auto& w : ctx->work) { free_list(w.pix); free_list(w.sp); free_list(w.lab); }
   drop_fill_graphs(ctx);
   free_list(ctx->ctl_bufs);
   cudaFree(ctx->body_iters);

@@ -121,7 +121,9 @@ struct Scalars {
 // frame's extent return).
 struct Slot {
   // frame
-  const float* img;        // [npix*3]
+  const float* img;        // [npix*3] the colours the path reads
+  const float* img_src;    // [npix*3] the caller's frame when it is converted to CIELAB
+                           // into img at ingest (stspix_config.lab_ingest), else null
   int* seg;                // working labels (the caller's output)
   int* seg_alt;            // ping-pong labels for the sweeps
   int H, W, npix;

@@ -2,7 +2,8 @@
 // st_spix/csrc/bist/rgb2lab.cu): sRGB -> CIELAB and back, and 8-bit frame ingest.
 // Not called by bist_forward in the reference (pyapi.cu:95-102), so the drop-in path
 // leaves frames as given; these serve callers that feed LAB, as the reference's
-// command-line pipeline does.
+// command-line pipeline does, and the opt-in ingest conversion of the batched path
+// (stspix_config.lab_ingest).
 //
 // The steps follow the reference exactly (they define the values callers compare
 // against): the first channel is read as blue (rgb2lab.cu:64-66), the arithmetic is
@@ -13,23 +14,22 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "engine.h"
 #include "pdl.h"
 
 namespace stspix {
 
-// first_blue: the first channel is blue (bist/rgb2lab.cu:64-66); 0: red (the legacy
-// prop/rgb2lab.cu:42-44 reads the channels in RGB order, otherwise identical).
-__global__ void k_rgb2lab(const float* __restrict__ rgb, float* __restrict__ lab, long long npix,
-                          int first_blue) {
-  pdl_enter();
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix) return;
-  const double c0 = (double)rgb[3 * t];
-  const double sG = (double)rgb[3 * t + 1];
-  const double c2 = (double)rgb[3 * t + 2];
+// One pixel: first_blue: the first channel is blue (bist/rgb2lab.cu:64-66); 0: red
+// (the legacy prop/rgb2lab.cu:42-44 reads the channels in RGB order, otherwise
+// identical).  Returns false (nothing written) for a pixel with a NaN channel.
+__device__ __forceinline__ bool rgb2lab_px(const float* __restrict__ in, float* __restrict__ out,
+                                           int first_blue) {
+  const double c0 = (double)in[0];
+  const double sG = (double)in[1];
+  const double c2 = (double)in[2];
   const double sB = first_blue ? c0 : c2;
   const double sR = first_blue ? c2 : c0;
-  if (sR != sR || sG != sG || sB != sB) return;
+  if (sR != sR || sG != sG || sB != sB) return false;
   auto lin = [](double c) {
     return c <= 0.04045 ? c / 12.92 : (double)powf((float)((c + 0.055) / 1.055), (float)2.4);
   };
@@ -45,9 +45,35 @@ __global__ void k_rgb2lab(const float* __restrict__ rgb, float* __restrict__ lab
   const float lval = (float)(116.0 * fy - 16.0);
   const float aval = (float)(500.0 * (fx - fy));
   const float bval = (float)(200.0 * (fy - fz));
-  lab[3 * t] = lval / (-100);
-  lab[3 * t + 1] = aval / 100;
-  lab[3 * t + 2] = bval / 100;
+  out[0] = lval / (-100);
+  out[1] = aval / 100;
+  out[2] = bval / 100;
+  return true;
+}
+
+__global__ void k_rgb2lab(const float* __restrict__ rgb, float* __restrict__ lab, long long npix,
+                          int first_blue) {
+  pdl_enter();
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npix) return;
+  rgb2lab_px(rgb + 3 * t, lab + 3 * t, first_blue);
+}
+
+// Ingest of a batch with stspix_config.lab_ingest: every frame's colours converted
+// once into the slot's engine buffer (img), which every later kernel reads.  A pixel
+// with a NaN channel keeps its input values (the reference leaves it unwritten).
+__global__ void kb_lab_ingest(const Slot* __restrict__ slots) {
+  pdl_enter();
+  const Slot& S = slots[blockIdx.y];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!S.img_src || t >= S.npix) return;
+  float* out = const_cast<float*>(S.img) + 3 * t;
+  const float* in = S.img_src + 3 * t;
+  if (!rgb2lab_px(in, out, 1)) {
+    out[0] = in[0];
+    out[1] = in[1];
+    out[2] = in[2];
+  }
 }
 
 __global__ void k_lab2rgb(const float* __restrict__ lab, float* __restrict__ rgb, long long npix) {

@@ -121,6 +121,7 @@ __global__ void kb_count_revived(const Slot* slots);
 
 // k_color.cu
 __global__ void k_rgb2lab(const float* rgb, float* lab, long long npix, int first_blue);
+__global__ void kb_lab_ingest(const Slot* slots);
 __global__ void k_lab2rgb(const float* lab, float* rgb, long long npix);
 __global__ void k_rescale_u8(const uint8_t* in, float* out, long long nvals, float mval);
 

@@ -39,3 +39,29 @@ def test_color_kernels_match_oracle():
     u8 = rng.integers(0, 256, size=(32, 48, 3)).astype(np.uint8)
     f = bist_cuda.rescale_u8(torch.from_numpy(u8).cuda()).cpu().numpy()
     np.testing.assert_array_equal(f, O.rescale_u8(u8))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("video_mode", [False, True])
+def test_lab_ingest_equals_converting_first(video_mode):
+    """stspix_config.lab_ingest converts every frame to CIELAB once at ingest: the
+    labels equal those of the engine on frames converted beforehand by the colour front
+    end, and the oracle's on the oracle's conversion of the same frames (the conversion
+    agrees with the oracle's to a few ulps of powf; the labels are compared exactly)."""
+    torch = pytest.importorskip("torch")
+    from st_spix_gb300 import bist_cuda
+    from tests.helpers import small_video
+    vid, flows = small_video(T=3)
+    gv, gf = torch.from_numpy(vid).cuda(), torch.from_numpy(flows).cuda()
+    args = (12, 15, 0.5, 0.009 ** 2, float(np.log(0.5)), 0.0, video_mode, False)
+    fused = bist_cuda.bist_forward(gv, gf, *args, lab_ingest=1).cpu().numpy()
+    lab = bist_cuda.rgb2lab(gv)
+    first = bist_cuda.bist_forward(lab, gf, *args).cpu().numpy()
+    np.testing.assert_array_equal(fused, first)
+    st, ref, _ = O.bist_forward(lab.cpu().numpy(), flows, O.default_config(niters=12),
+                                video_mode)
+    assert st == 0
+    np.testing.assert_array_equal(fused, ref)
+    # the default leaves frames as given (the reference ignores its rgb2lab flag)
+    plain = bist_cuda.bist_forward(gv, gf, *args).cpu().numpy()
+    assert not np.array_equal(plain, fused)
