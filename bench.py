@@ -1020,36 +1020,56 @@ def main():
     e_vid = [torch.empty_like(v) for v in dvid]
     e_flo = [torch.empty_like(f) for f in dflo]
 
-    # frames stream in: every frame's host->device copy is queued on the lane's copy-in
-    # stream ahead of the batches, batch t waits for frame t only, and frame t's labels
-    # go back on the copy-out stream while later batches run
+    # Frames stream in: each lane keeps the host->device copies of its next LOOKAHEAD
+    # frames queued on its copy-in stream (the steps form one continuous sequence of
+    # frames), so the copy engines serve the lanes' frames in step with the batches
+    # instead of one lane's whole step ahead of the others; batch t waits for frame t
+    # only, a frame buffer is refilled once the previous step's batches that read it are
+    # done, and frame t's labels go back on the copy-out stream while later batches run.
+    # The streams are synchronised once, after the last step.
+    LOOKAHEAD = 3
     in_streams = [torch.cuda.Stream(dev) for _ in range(NL)]
     out_streams = [torch.cuda.Stream(dev) for _ in range(NL)]
+    in_ev = [dict() for _ in range(NL)]          # (step, t) -> copy-in done
+    read_ev = [dict() for _ in range(NL)]        # t -> previous use of frame buffer t done
+
+    def enqueue(j, st, t):
+        with torch.cuda.stream(in_streams[j]):
+            # frame t is read by batch t, its flow by batch t + 1
+            dep = read_ev[j].get(min(t + 1, T - 1))
+            if dep is not None:
+                in_streams[j].wait_event(dep)
+            for i in lanes[j]:
+                e_vid[i][t].copy_(h_vid[i][t], non_blocking=True)
+                if t < T - 1:
+                    e_flo[i][t].copy_(h_flo[i][t], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(in_streams[j])
+            in_ev[j][(st, t)] = ev
 
     def e2e(j, st):
-        ev_in = [torch.cuda.Event() for _ in range(T)]
-        with torch.cuda.stream(in_streams[j]):
-            in_streams[j].wait_stream(cstreams[j])     # the previous step's reads are done
-            for t in range(T):
-                for i in lanes[j]:
-                    e_vid[i][t].copy_(h_vid[i][t], non_blocking=True)
-                    if t < T - 1:
-                        e_flo[i][t].copy_(h_flo[i][t], non_blocking=True)
-                ev_in[t].record(in_streams[j])
+        if st == 0:
+            for t in range(min(LOOKAHEAD, T)):
+                enqueue(j, 0, t)
 
         def before(t):
-            cstreams[j].wait_event(ev_in[t])
+            g = st * T + t + LOOKAHEAD
+            if g < args.steps * T:
+                enqueue(j, g // T, g % T)
+            cstreams[j].wait_event(in_ev[j].pop((st, t)))
 
         def after(t):
             ev = torch.cuda.Event()
             ev.record(cstreams[j])
+            read_ev[j][t] = ev
             out_streams[j].wait_event(ev)
             with torch.cuda.stream(out_streams[j]):
                 for i in lanes[j]:
                     h_out[i][t].copy_(dout[i][t], non_blocking=True)
         video_pass(j, e_vid, e_flo, dout, False, before, after)
-        out_streams[j].synchronize()
-        cstreams[j].synchronize()
+        if st == args.steps - 1:
+            out_streams[j].synchronize()
+            cstreams[j].synchronize()
 
     barrier()
     torch.cuda.synchronize()
