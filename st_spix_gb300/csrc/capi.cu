@@ -563,6 +563,8 @@ Slot make_slot(stspix_ctx* ctx, const FrameDesc& f, int cap) {
   }
   s.seg = f.seg;
   s.H = f.H; s.W = f.W; s.npix = f.H * f.W;
+  s.inv_w = 1.0 / (double)f.W;
+  s.inv_h = 1.0 / (double)f.H;
   s.cap = cap;
   s.sp.cap = cap;
   s.tmp.cap = cap;

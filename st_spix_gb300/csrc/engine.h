@@ -124,6 +124,7 @@ struct Slot {
   const float* img;        // [npix*3] the colours the path reads
   const float* img_src;    // [npix*3] the caller's frame when it is converted to CIELAB
                            // into img at ingest (stspix_config.lab_ingest), else null
+  double inv_w, inv_h;     // 1 / W, 1 / H (the hole fill's quotients, see fill_quot)
   int* seg;                // working labels (the caller's output)
   int* seg_alt;            // ping-pong labels for the sweeps
   int H, W, npix;

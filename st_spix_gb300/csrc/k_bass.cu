@@ -459,6 +459,10 @@ __device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in
 __global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
+  // ids above the largest in use were never live in this frame: their fields still hold
+  // the zeros the frame's set-up wrote (kb_init_bass_params, kb_write_params), which is
+  // what this kernel would write for them
+  if ((int)blockIdx.x * 32 > S.sc->max_spix) return;
   __shared__ double v_ps[3][32], v_raw[3][32], v_m[2][32], v_s[3][32], v_i[4][32];
   __shared__ float v_app[3][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -566,7 +570,8 @@ __global__ void kb_store_sample(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
-  FOR_SP(k, sp.cap) {
+  const int n = min(sp.cap, S.sc->max_spix + 1);     // ids above are never valid
+  FOR_SP(k, n) {
   if (!sp.valid[k]) continue;
   const long long* a = sp.acc + 8 * (size_t)k;
   double count = sp.count[k] * 1.0;

@@ -223,6 +223,20 @@ __global__ void kb_fill_border(const Slot* __restrict__ slots) {
   }
 }
 
+// (float)(num / d) for the fill's similarity (fill_missing.cu: a float pixel coordinate
+// minus a double centre, divided by the float frame size, in double, then stored in a
+// float), without the double division where it cannot matter: r = num * (1 / d) is
+// within 2 ulps of the double quotient, so unless r lies within 3 ulps of a float
+// rounding midpoint (the 29 bits below a float's mantissa equal to 2^28) both round to
+// the same float.  The rare rest divides.  GB300's FP64 rate is low, and two divisions
+// per candidate made the fill FP64-bound; the result is the same bit for bit.
+__device__ __forceinline__ float fill_quot(double num, double inv, double d) {
+  const double r = num * inv;
+  const unsigned lo29 = (unsigned)(__double_as_longlong(r) & ((1ll << 29) - 1));
+  if (fabs(r) >= 0x1p-120 && (lo29 > (1u << 28) + 3u || lo29 < (1u << 28) - 3u)) return (float)r;
+  return (float)(num / d);
+}
+
 __global__ void kb_fill_phase(const Slot* __restrict__ slots, int ph) {
   pdl_enter();
   SLOT_Y;
@@ -245,10 +259,11 @@ __global__ void kb_fill_phase(const Slot* __restrict__ slots, int ph) {
     if (y < H - 1) So = seg[idx + W];
     float bx = -999999;
     int bl = -1;
+    const double inv_w = S.inv_w, inv_h = S.inv_h, dW = 1.0f * W, dH = 1.0f * H;
     auto consider = [&](int lab) {
       const double* cp = centers + 2 * (size_t)lab;
-      float dx = (1.0f * x - cp[0]) / (1.0f * W);
-      float dy = (1.0f * y - cp[1]) / (1.0f * H);
+      float dx = fill_quot(1.0f * x - cp[0], inv_w, dW);
+      float dy = fill_quot(1.0f * y - cp[1], inv_h, dH);
       float sim = -dx * dx - dy * dy;
       if (sim > bx) { bx = sim; bl = lab; }
     };

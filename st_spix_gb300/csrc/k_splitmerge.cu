@@ -587,7 +587,9 @@ __device__ __forceinline__ void merge_decide_one(const SpDev& sp, const SmDev& s
 __global__ void kb_merge_decide(const Slot* __restrict__ slots, SmConsts K, float merge_alpha) {
   pdl_enter();
   SLOT_Y;
-  FOR_SP(k, S.sp.cap) merge_decide_one(S.sp, S.sm, S.sc, K, merge_alpha, k);
+  // only valid ids decide, and none lies above the largest id in use
+  const int n = min(S.sp.cap, S.sc->max_spix + 1);
+  FOR_SP(k, n) merge_decide_one(S.sp, S.sm, S.sc, K, merge_alpha, k);
 }
 
 // Merge set-up: candidate pairs unset, claims at +inf (cap + 2 entries).
