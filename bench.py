@@ -46,6 +46,7 @@ SWEEP_TRAFFIC_NCU = dict(bytes_per_launch=35236608,
                          source="ncu dram__bytes_read.sum + dram__bytes_write.sum, "
                                 "profiles/kb_sweep_bist_stream_480x854_T30.md")
 METRIC = "streamed frames/sec"
+SERVE_LANES = 3          # host lanes of the serving legs in the default run
 
 
 def gen_video(seed: int, T: int = None):
@@ -785,11 +786,12 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--streams", type=int, default=None,
-                    help="video streams per GPU (default 24; serve: 256); stream mode: frame "
+                    help="video streams per GPU (default 32; serve: 256); stream mode: frame "
                          "t of every stream of a lane runs as one batch")
     ap.add_argument("--lanes", type=int, default=None,
                     help="host threads per GPU, each with its own CUDA stream, engine "
-                         "context and share of the streams (default 3)")
+                         "context and share of the streams (default 4 in stream mode, "
+                         "else 3)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="stream",
                     choices=["stream", "serve", "batch", "precision", "image", "latency"],
@@ -824,9 +826,11 @@ def main():
                          "kernel of a graph that holds conditional nodes)")
     args = ap.parse_args()
     if args.streams is None:
-        args.streams = SERVE["streams"] if args.mode == "serve" else 24
+        args.streams = SERVE["streams"] if args.mode == "serve" else 32
     if args.lanes is None:
-        args.lanes = 3
+        # stream mode: 4 host lanes of 8 streams (24 on 3: 2377 frames/s, 32 on 4: 2471,
+        # 40 on 5: 2465); the serving form keeps 3
+        args.lanes = 4 if args.mode == "stream" else 3
     world, rank, local = dist_setup()
     args.local = local
     if args.impl == "reference":
@@ -1085,19 +1089,21 @@ def main():
     # 30 fps offering 85 % of the rate served under the config-3 backlog) -------------
     serving = None
     if not args.no_serve and world == 1:
-        full = serve_leg(args, dev, rank, SERVE["streams"], args.serve_frames, SERVE["fps"])
+        full = serve_leg(args, dev, rank, SERVE["streams"], args.serve_frames, SERVE["fps"],
+                         lanes=SERVE_LANES)
         served = full["serving"].get("frames_per_s") or 0.0
         # the largest load served as offered: start at 85 % of the config-3 served rate and
         # shrink until the served rate is within 5 % of the offered one (3 tries at most)
         n_sus, tries = max(1, int(0.85 * served / SERVE["fps"])), []
         for _ in range(3):
-            sus = serve_leg(args, dev, rank, n_sus, WORKLOAD["T"], SERVE["fps"])
+            sus = serve_leg(args, dev, rank, n_sus, WORKLOAD["T"], SERVE["fps"],
+                            lanes=SERVE_LANES)
             got = sus["serving"].get("frames_per_s") or 0.0
             tries.append({"streams": n_sus, "offered_fps": sus["offered_fps"], "served_fps": got})
             if got >= 0.95 * sus["offered_fps"] or n_sus == 1:
                 break
             n_sus = max(1, int(0.9 * n_sus * got / sus["offered_fps"]))
-        light = serve_leg(args, dev, rank, 4, WORKLOAD["T"], SERVE["fps"])
+        light = serve_leg(args, dev, rank, 4, WORKLOAD["T"], SERVE["fps"], lanes=SERVE_LANES)
         serving = {"config3": serving_summary(full, "256 streams, Poisson 30 fps each, %d frames "
                                                "per stream" % args.serve_frames),
                    "sustained": dict(serving_summary(sus, "%d streams, Poisson 30 fps each, %d "
