@@ -461,9 +461,9 @@ void preload_kernels() {
       (const void*)kb_shift_decode,
       (const void*)kb_count_labels,
       (const void*)kb_fill_begin,
-      (const void*)kb_fill_border,
+      (const void*)kb_fill_split,
       (const void*)kb_fill_phase,
-      (const void*)kb_fill_compact,
+      (const void*)kb_fill_end,
       (const void*)kb_cc_init,
       (const void*)kb_cc_hook,
       (const void*)kb_cc_compress,
@@ -1018,11 +1018,10 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
 }
 
 // The hole-fill loop of the propagated slots of table L as a graph: a WHILE node
-// whose body is one iteration (kb_fill_phase x 4, kb_fill_compact, added as kernel
-// nodes); kb_fill_compact's last block sets the condition.  Built once per (table,
-// size).
-// The loop body's kernel nodes (four parity phases, then the compaction, whose last
-// block sets `cond`) into graph `body`.
+// whose body is one iteration (kb_fill_phase x 4, added as kernel nodes); the fourth
+// phase's last block sets the condition.  Built once per (table, size).
+// The loop body's kernel nodes (four parity phases, the last of which closes the
+// iteration and sets `cond`) into graph `body`.
 cudaError_t add_fill_body(stspix_ctx* ctx, cudaGraph_t body, const List& L,
                           cudaGraphConditionalHandle cond) {
   const unsigned G = (unsigned)std::max(8, std::min(128, 2048 / std::max(L.B, 1)));
@@ -1045,15 +1044,17 @@ cudaError_t add_fill_body(stspix_ctx* ctx, cudaGraph_t body, const List& L,
     ce = cudaGraphAddKernelNode(&n, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp);
     prev = n;
   };
-  void* a_ph[4][2];
+  void* a_ph[4][7];
   for (int ph = 0; ph < 4; ph++) {
     a_ph[ph][0] = (void*)&table;
     a_ph[ph][1] = (void*)&ph_arg[ph];
+    a_ph[ph][2] = (void*)&B;
+    a_ph[ph][3] = (void*)&cond;
+    a_ph[ph][4] = (void*)&break_iter;
+    a_ph[ph][5] = (void*)&ctx->body_iters;
+    a_ph[ph][6] = (void*)&ctr;
     add((const void*)kb_fill_phase, grid, dim3(kThreads), a_ph[ph]);
   }
-  void* a_compact[] = {(void*)&table, (void*)&B, (void*)&cond, (void*)&break_iter,
-                       (void*)&ctx->body_iters, (void*)&ctr};
-  add((const void*)kb_fill_compact, grid, dim3(kThreads), a_compact);
   return ce;
 }
 
@@ -1101,11 +1102,22 @@ int fill_graph(stspix_ctx* ctx, const List& L, cudaGraphExec_t* out) {
   return STSPIX_OK;
 }
 
+int fill_loop(stspix_ctx* ctx, cudaStream_t st, const List& L);
+
 int run_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHS(kb_fill_begin, L, L.B);
-  // the first iteration's border flags (later ones come with the compaction)
+  // the hole list split by parity class
   const unsigned G = (unsigned)std::max(8, std::min(128, 2048 / std::max(L.B, 1)));
-  LAUNCHG(kb_fill_border, dim3(G, (unsigned)L.B), kThreads, L.d);
+  LAUNCHG(kb_fill_split, dim3(G, (unsigned)L.B), kThreads, L.d, 0);
+  LAUNCHG(kb_fill_split, dim3(G, (unsigned)L.B), kThreads, L.d, 1);
+  int r = fill_loop(ctx, st, L);
+  if (r) return r;
+  LAUNCHG(kb_fill_end, dim3(G, (unsigned)L.B), kThreads, L.d);
+  return STSPIX_OK;
+}
+
+// The WHILE loop of the fill (recorded into the running capture, or a cached graph).
+int fill_loop(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   if (ctx->capturing) {
     // inside a batch capture: the loop node goes into the graph being captured
     cudaStreamCaptureStatus cs;
@@ -1171,8 +1183,8 @@ int read_scalars(stspix_ctx* ctx, cudaStream_t st, int B) {
   CK(cudaMemcpyAsync(ctx->sc_host, ctx->sc, sizeof(Scalars) * (size_t)B, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(ctx->body_iters_host, ctx->body_iters, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  // kernels launched by the fill graphs: 5 per loop iteration
-  ctx->launches += 5 * ((long long)*ctx->body_iters_host - ctx->body_iters_seen);
+  // kernels launched by the fill graphs: 4 per loop iteration
+  ctx->launches += 4 * ((long long)*ctx->body_iters_host - ctx->body_iters_seen);
   ctx->body_iters_seen = *ctx->body_iters_host;
   CK(cudaGetLastError());
   prof_harvest(ctx);

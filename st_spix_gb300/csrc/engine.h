@@ -110,9 +110,11 @@ struct Scalars {
   int ninvalid;       // -1 pixels after the shift
   int tmp0, tmp1, tmp2;
   int nhole;          // length of the hole list of the fill
-  // hole-fill loop state: current / next list length, previous count, iteration,
-  // finished flag, which buffer holds the current list (0 smseg, 1 hits)
-  int fl_n, fl_next, fl_prev, fl_iter, fl_done, fl_cur;
+  // hole-fill loop state: holes left, previous count, iterations run, finished flag,
+  // holes filled in the running iteration; the hole list split by parity class
+  // (class counts, write cursors)
+  int fl_n, fl_prev, fl_iter, fl_done, fl_fill;
+  int fl_cnt[4], fl_pos[4];
 };
 
 // One frame of a batch: its inputs, outputs, workspace and scalars.  Kernels take

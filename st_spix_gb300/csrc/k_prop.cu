@@ -178,20 +178,26 @@ __global__ void kb_count_labels(const Slot* __restrict__ slots, int which) {
 
 // ---------------------------------------------------------------------------
 // Hole filling (fill_missing.cu:35-130, update_missing_seg_nn :288-441,
-// find_border_along_missing :617-647) over the list of hole pixels instead of the
-// frame.  One iteration = kb_fill_phase x 4 and kb_fill_compact (the border flags of
-// the first iteration by kb_fill_border before the loop); the host runs it as the body
-// of a CUDA-graph WHILE node whose condition kb_fill_compact's last block sets, so the
-// loop needs neither host round trips nor grid barriers.  Per iteration: the hole
-// count (the list length), the border flag of every hole (a 4-neighbour labelled at
-// the start of the iteration), four parity
-// phases in which a bordered hole takes the label of the neighbour whose centre is
-// nearest, then the holes left are compacted into the other list buffer.  Stop
-// rules as the reference: a count equal to the previous one is an error (it exits),
-// no holes left ends the loop, both after the iteration's phases; break_iter caps it.
-__device__ __forceinline__ const int* fill_list(const Slot& S) {
-  return S.sc->fl_cur ? S.hits : S.smseg;
-}
+// find_border_along_missing :617-647) over lists of hole pixels instead of the frame.
+// The reference's iteration: the hole count, the border flag of every hole (a
+// 4-neighbour labelled at the start of the iteration), then four parity phases in
+// which a bordered hole takes the label of the neighbour whose centre is nearest;
+// stop rules: a count equal to the previous one is an error (it exits), no holes
+// left ends the loop, both checked after the iteration's phases; break_iter caps it.
+//
+// Here the fill's hole list is split once into the four parity classes (kb_fill_split,
+// into the `hits` buffer), and an iteration is kb_fill_phase x 4, run as the body of a
+// CUDA-graph WHILE node whose condition the last block of the fourth phase sets (no
+// host round trips, no grid barriers).  A phase scans its class only.  The border
+// flags are not stored: a hole filled in this iteration carries a flag bit of the
+// iteration's parity in its label until its own class's phase of the next iteration
+// (or kb_fill_end) strips it, so "labelled at the start of the iteration" is "labelled
+// and not flagged with this iteration's parity" (a 4-neighbour always belongs to
+// another class, so a phase never reads a label of its own class written in the same
+// phase).  Candidates read the labels without flags.  The order of the holes in a list
+// does not matter (a phase's pixels are never 4-neighbours of each other).
+constexpr int kFillFlagOdd = 1 << 30, kFillFlagEven = 1 << 29;
+constexpr int kFillFlags = kFillFlagOdd | kFillFlagEven;
 
 __global__ void kb_fill_begin(const Slot* __restrict__ slots, int B) {
   pdl_enter();
@@ -199,27 +205,48 @@ __global__ void kb_fill_begin(const Slot* __restrict__ slots, int B) {
   if (i >= B) return;
   Scalars* sc = slots[i].sc;
   sc->fl_n = sc->nhole;
-  sc->fl_next = 0;
   sc->fl_prev = 1410065408;  // (int)10000000000 as the reference truncates it
   sc->fl_iter = 0;
   sc->fl_done = 0;
-  sc->fl_cur = 0;
+  sc->fl_fill = 0;
+  for (int c = 0; c < 4; c++) { sc->fl_cnt[c] = 0; sc->fl_pos[c] = 0; }
 }
 
-__global__ void kb_fill_border(const Slot* __restrict__ slots) {
+__device__ __forceinline__ int fill_class(int idx, int W) {
+  const int x = idx % W, y = idx / W;
+  return ((x & 1) << 1) | (y & 1);             // phase ph: x parity ph >> 1, y parity ph & 1
+}
+
+// pass 0: count the holes of each class; pass 1: write each class's holes into its
+// part of `hits` (offset = the counts of the classes before it).  Warp-aggregated.
+__global__ void kb_fill_split(const Slot* __restrict__ slots, int pass) {
   pdl_enter();
   SLOT_Y;
-  const Scalars* sc = S.sc;
-  if (sc->fl_done) return;
-  const int n = sc->fl_n, W = S.W, H = S.H;
-  const int* la = fill_list(S);
-  const int* seg = S.seg;
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-    const int idx = la[j];
-    const int x = idx % W, y = idx / W;
-    const bool b = (y > 0 && seg[idx - W] >= 0) || (x > 0 && seg[idx - 1] >= 0) ||
-                   (y < H - 1 && seg[idx + W] >= 0) || (x < W - 1 && seg[idx + 1] >= 0);
-    S.border[j] = b ? 1 : 0;
+  Scalars* sc = S.sc;
+  const int n = sc->nhole, W = S.W;
+  const int lane = threadIdx.x & 31;
+  int off[4] = {0, 0, 0, 0};
+  if (pass) {
+    off[1] = sc->fl_cnt[0];
+    off[2] = off[1] + sc->fl_cnt[1];
+    off[3] = off[2] + sc->fl_cnt[2];
+  }
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int j = base + threadIdx.x;
+    const bool in = j < n;
+    const int idx = in ? S.smseg[j] : 0;
+    const int c = in ? fill_class(idx, W) : -1;
+#pragma unroll
+    for (int cc = 0; cc < 4; cc++) {
+      const unsigned m = __ballot_sync(0xffffffffu, c == cc);
+      if (!m) continue;
+      const int leader = __ffs(m) - 1;
+      int at = 0;
+      if (lane == leader) at = atomicAdd(pass ? &sc->fl_pos[cc] : &sc->fl_cnt[cc], __popc(m));
+      at = __shfl_sync(0xffffffffu, at, leader);
+      if (pass && c == cc) S.hits[off[cc] + at + __popc(m & ((1u << lane) - 1))] = idx;
+    }
   }
 }
 
@@ -237,84 +264,74 @@ __device__ __forceinline__ float fill_quot(double num, double inv, double d) {
   return (float)(num / d);
 }
 
-__global__ void kb_fill_phase(const Slot* __restrict__ slots, int ph) {
-  pdl_enter();
-  SLOT_Y;
-  const Scalars* sc = S.sc;
-  if (sc->fl_done) return;
-  const int n = sc->fl_n, W = S.W, H = S.H;
-  const int xm = ph >> 1, ym = ph & 1;
-  const int* la = fill_list(S);
-  int* seg = S.seg;
-  const double* centers = S.centers;
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-    const int idx = la[j];
-    const int x = idx % W, y = idx / W;
-    if ((x & 1) != xm || (y & 1) != ym) continue;
-    if (!S.border[j] || seg[idx] != -1) continue;
-    int N = -1, So = -1, E = -1, Wl = -1;
-    if (x > 0) Wl = seg[idx - 1];
-    if (y > 0) N = seg[idx - W];
-    if (x < W - 1) E = seg[idx + 1];
-    if (y < H - 1) So = seg[idx + W];
-    float bx = -999999;
-    int bl = -1;
-    const double inv_w = S.inv_w, inv_h = S.inv_h, dW = 1.0f * W, dH = 1.0f * H;
-    auto consider = [&](int lab) {
-      const double* cp = centers + 2 * (size_t)lab;
-      float dx = fill_quot(1.0f * x - cp[0], inv_w, dW);
-      float dy = fill_quot(1.0f * y - cp[1], inv_h, dH);
-      float sim = -dx * dx - dy * dy;
-      if (sim > bx) { bx = sim; bl = lab; }
-    };
-    if (N >= 0) consider(N);
-    if (So >= 0 && So != N) consider(So);
-    if (Wl >= 0 && Wl != So && Wl != N) consider(Wl);
-    if (E >= 0 && E != Wl && E != So && E != N) consider(E);
-    seg[idx] = bl;
-  }
-}
-
-// Holes still unfilled go to the other list buffer (warp-aggregated append; the
-// order does not matter, see append_hole), each with its border flag for the next
-// iteration (a labelled 4-neighbour now, i.e. at the start of the next iteration).
-// The last block to finish (a device counter, no waiting) closes the iteration for
-// every slot: count, stop rules, list swap, and the loop condition.  *body_iters
-// counts the iterations run; ctr is reset for the next iteration.
-__global__ void kb_fill_compact(const Slot* __restrict__ slots, int B,
-                                cudaGraphConditionalHandle cond, int break_iter, int* body_iters,
-                                unsigned* ctr) {
+// One parity phase of one iteration.  ph 3 also closes the iteration: its last block
+// (a device counter, no waiting) applies the stop rules to every slot, counts the
+// iteration (*body_iters) and sets the loop condition.
+__global__ void kb_fill_phase(const Slot* __restrict__ slots, int ph, int B,
+                              cudaGraphConditionalHandle cond, int break_iter, int* body_iters,
+                              unsigned* ctr) {
   pdl_enter();
   SLOT_Y;
   Scalars* sc = S.sc;
   if (!sc->fl_done) {
-    const int n = sc->fl_n, W = S.W, H = S.H;
-    const int* la = fill_list(S);
-    int* lb = sc->fl_cur ? S.smseg : S.hits;
-    const int* seg = S.seg;
+    const int W = S.W, H = S.H;
+    const int cur = (sc->fl_iter & 1) ? kFillFlagOdd : kFillFlagEven;
+    const int off = ph == 0 ? 0 : ph == 1 ? sc->fl_cnt[0]
+                  : ph == 2 ? sc->fl_cnt[0] + sc->fl_cnt[1]
+                            : sc->fl_cnt[0] + sc->fl_cnt[1] + sc->fl_cnt[2];
+    const int n = sc->fl_cnt[ph];
+    const int* la = S.hits + off;
+    int* seg = S.seg;
+    const double* centers = S.centers;
+    const double inv_w = S.inv_w, inv_h = S.inv_h, dW = 1.0f * W, dH = 1.0f * H;
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
       const int j = base + threadIdx.x;
-      int idx = -1;
-      if (j < n) idx = la[j];
-      const bool keep = j < n && seg[idx] < 0;
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (!m) continue;
-      const int leader = __ffs(m) - 1;
-      int pos = 0;
-      if (lane == leader) pos = atomicAdd(&sc->fl_next, __popc(m));
-      pos = __shfl_sync(0xffffffffu, pos, leader);
-      if (keep) {
-        const int at = pos + __popc(m & ((1u << lane) - 1));
-        const int x = idx % W, y = idx / W;
-        const bool bd = (y > 0 && seg[idx - W] >= 0) || (x > 0 && seg[idx - 1] >= 0) ||
-                        (y < H - 1 && seg[idx + W] >= 0) || (x < W - 1 && seg[idx + 1] >= 0);
-        lb[at] = idx;
-        S.border[at] = bd ? 1 : 0;
+      bool filled_now = false;
+      if (j < n) {
+        const int idx = la[j];
+        const int v = seg[idx];
+        if (v != -1) {
+          // filled in an earlier iteration: its flag (the previous iteration's) goes
+          if (v & kFillFlags) seg[idx] = v & ~kFillFlags;
+        } else {
+          const int x = idx % W, y = idx / W;
+          int N = -1, So = -1, E = -1, Wl = -1;
+          if (x > 0) Wl = seg[idx - 1];
+          if (y > 0) N = seg[idx - W];
+          if (x < W - 1) E = seg[idx + 1];
+          if (y < H - 1) So = seg[idx + W];
+          // bordered: a neighbour labelled at the start of the iteration
+          auto at_start = [&](int u) { return u >= 0 && !(u & cur); };
+          if (at_start(N) || at_start(So) || at_start(Wl) || at_start(E)) {
+            N = N >= 0 ? (N & ~kFillFlags) : N;
+            So = So >= 0 ? (So & ~kFillFlags) : So;
+            Wl = Wl >= 0 ? (Wl & ~kFillFlags) : Wl;
+            E = E >= 0 ? (E & ~kFillFlags) : E;
+            float bx = -999999;
+            int bl = -1;
+            auto consider = [&](int lab) {
+              const double* cp = centers + 2 * (size_t)lab;
+              float dx = fill_quot(1.0f * x - cp[0], inv_w, dW);
+              float dy = fill_quot(1.0f * y - cp[1], inv_h, dH);
+              float sim = -dx * dx - dy * dy;
+              if (sim > bx) { bx = sim; bl = lab; }
+            };
+            if (N >= 0) consider(N);
+            if (So >= 0 && So != N) consider(So);
+            if (Wl >= 0 && Wl != So && Wl != N) consider(Wl);
+            if (E >= 0 && E != Wl && E != So && E != N) consider(E);
+            seg[idx] = bl | cur;
+            filled_now = true;
+          }
+        }
       }
+      const unsigned m = __ballot_sync(0xffffffffu, filled_now);
+      if (m && lane == __ffs(m) - 1) atomicAdd(&sc->fl_fill, __popc(m));
     }
   }
+  if (ph != 3) return;
   __shared__ int is_last;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -328,7 +345,7 @@ __global__ void kb_fill_compact(const Slot* __restrict__ slots, int B,
   for (int i = threadIdx.x; i < B; i += blockDim.x) {
     Scalars* si = slots[i].sc;
     if (si->fl_done) continue;
-    const int num_neg = si->fl_n;
+    const int num_neg = si->fl_n;           // holes at the start of this iteration
     si->fill_iters += 1;
     si->fl_iter += 1;
     if (num_neg == si->fl_prev) {
@@ -338,9 +355,8 @@ __global__ void kb_fill_compact(const Slot* __restrict__ slots, int B,
       si->fl_prev = num_neg;
       if (num_neg <= 0 || si->fl_iter >= break_iter) si->fl_done = 1;
     }
-    si->fl_n = si->fl_next;
-    si->fl_next = 0;
-    si->fl_cur ^= 1;
+    si->fl_n = num_neg - si->fl_fill;
+    si->fl_fill = 0;
     if (!si->fl_done) active = 1;
   }
   active = __syncthreads_or(active);
@@ -348,6 +364,19 @@ __global__ void kb_fill_compact(const Slot* __restrict__ slots, int B,
     *body_iters += 1;
     *ctr = 0u;
     cudaGraphSetConditional(cond, active ? 1u : 0u);
+  }
+}
+
+// After the loop: the flags of the last iterations' fills go.
+__global__ void kb_fill_end(const Slot* __restrict__ slots) {
+  pdl_enter();
+  SLOT_Y;
+  const int n = S.sc->nhole;
+  int* seg = S.seg;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int idx = S.hits[j];
+    const int v = seg[idx];
+    if (v >= 0 && (v & kFillFlags)) seg[idx] = v & ~kFillFlags;
   }
 }
 

@@ -95,10 +95,10 @@ __global__ void kb_shift(const Slot* slots);
 __global__ void kb_shift_decode(const Slot* slots);
 __global__ void kb_count_labels(const Slot* slots, int which);
 __global__ void kb_fill_begin(const Slot* slots, int B);
-__global__ void kb_fill_border(const Slot* slots);
-__global__ void kb_fill_phase(const Slot* slots, int ph);
-__global__ void kb_fill_compact(const Slot* slots, int B, cudaGraphConditionalHandle cond,
-                                int break_iter, int* body_iters, unsigned* ctr);
+__global__ void kb_fill_split(const Slot* slots, int pass);
+__global__ void kb_fill_phase(const Slot* slots, int ph, int B, cudaGraphConditionalHandle cond,
+                              int break_iter, int* body_iters, unsigned* ctr);
+__global__ void kb_fill_end(const Slot* slots);
 __global__ void kb_cc_init(const Slot* slots);
 __global__ void kb_cc_hook(const Slot* slots);
 __global__ void kb_cc_compress(const Slot* slots);
