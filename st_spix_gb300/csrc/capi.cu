@@ -1017,6 +1017,8 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   return STSPIX_OK;
 }
 
+constexpr int kFillUnroll = 2;
+
 // The hole-fill loop of the propagated slots of table L as a graph: a WHILE node
 // whose body is one iteration (kb_fill_phase x 4, added as kernel nodes); the fourth
 // phase's last block sets the condition.  Built once per (table, size).
@@ -1044,6 +1046,8 @@ cudaError_t add_fill_body(stspix_ctx* ctx, cudaGraph_t body, const List& L,
     ce = cudaGraphAddKernelNode(&n, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp);
     prev = n;
   };
+  // kFillUnroll iterations per execution of the body: fewer evaluations of the loop
+  // condition; an iteration after the loop's end finds every slot done and returns
   void* a_ph[4][7];
   for (int ph = 0; ph < 4; ph++) {
     a_ph[ph][0] = (void*)&table;
@@ -1053,8 +1057,9 @@ cudaError_t add_fill_body(stspix_ctx* ctx, cudaGraph_t body, const List& L,
     a_ph[ph][4] = (void*)&break_iter;
     a_ph[ph][5] = (void*)&ctx->body_iters;
     a_ph[ph][6] = (void*)&ctr;
-    add((const void*)kb_fill_phase, grid, dim3(kThreads), a_ph[ph]);
   }
+  for (int u = 0; u < kFillUnroll; u++)
+    for (int ph = 0; ph < 4; ph++) add((const void*)kb_fill_phase, grid, dim3(kThreads), a_ph[ph]);
   return ce;
 }
 
