@@ -666,7 +666,7 @@ __global__ void k_overlay(float* __restrict__ out, const float* __restrict__ img
 // Simple-point table (data, identical to the reference's bass_lut): bit i of the
 // index is set when 3x3 neighbour i (NW,N,NE,W,E,SW,S,SE) carries the candidate
 // label or lies outside the image.
-__constant__ unsigned char c_simple_lut[256] = {
+constexpr unsigned char kSimpleLut[256] = {
     0, 0, 1, 1, 0, 0, 1, 1, 1, 1, 0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 0, 0,
     0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0,
     0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
@@ -677,6 +677,19 @@ __constant__ unsigned char c_simple_lut[256] = {
     0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
     1, 0, 0, 0, 1, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 1,
     0, 1, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0, 1, 1, 1, 1, 0, 0, 1, 1, 0, 0};
+
+// The table as eight 32-bit words (bit b of word w = entry 32 w + b), computed from it at
+// compile time.
+struct SimpleBits {
+  unsigned w[8];
+};
+__host__ __device__ constexpr SimpleBits simple_bits() {
+  SimpleBits r{};
+  for (int i = 0; i < 256; i++)
+    if (kSimpleLut[i]) r.w[i >> 5] |= 1u << (i & 31);
+  return r;
+}
+__constant__ SimpleBits c_simple_bits = simple_bits();
 
 __device__ __forceinline__ void joint(float c0, float c1, float c2, int x, int y,
                                       const SweepRec& r, int k, float s2, float neigh_neq,
@@ -847,7 +860,21 @@ constexpr unsigned long long kOddBits = 0xAAAAAAAAAAAAAAAAull;
 // grown by G (phase k on the tile grown by G - k), then score them phase by phase in
 // shared memory.  OFF = label-region offset of the grown-by-G region; use_act: only
 // pixels flagged in sm.act (active-set sweeps).
-template <int TX, int TY, int NS, int G>
+// The 32-bit chunk ballots of a label-region row as its two 64-bit words.
+template <int kCK>
+__device__ __forceinline__ void pack_row(const unsigned (&b)[kCK], unsigned long long* w0,
+                                         unsigned long long* w1) {
+  unsigned long long lo = b[0], hi = 0;
+  if (kCK > 1) lo |= (unsigned long long)b[1 % kCK] << 32;
+  if (kCK > 2) hi = b[2 % kCK];
+  if (kCK > 3) hi |= (unsigned long long)b[3 % kCK] << 32;
+  *w0 = lo; *w1 = hi;
+}
+
+// STAGED: the label edges of the staged rows are already in sm.edE / sm.edS (computed
+// from the staging registers, rows in contiguous spans of kLY / 8 per warp) except the
+// lower edges of each span's last row, which need the next warp's first row.
+template <int TX, int TY, int NS, int G, bool STAGED>
 __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>& sm,
                                            const unsigned* lut_bits, int tx0, int ty0,
                                            float s2, float potts, bool use_act, bool last,
@@ -856,7 +883,7 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
   constexpr int kLY = SweepTile<TX, TY, NS>::kLY;
   constexpr int kSH = SweepTile<TX, TY, NS>::kSH;
   constexpr int OFF = kSH - G;
-  constexpr int kIX = TX + 2 * G, kIY = TY + 2 * G;
+  constexpr int kIY = TY + 2 * G;
   constexpr int kCK = (kLX + 31) / 32;
   static_assert(OFF >= 1, "every listed pixel has its 4 neighbours in the label region");
   int* L = sm.L;
@@ -877,29 +904,42 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
   // edge rows and columns count as border pixels as in the reference).  First the
   // edges of the label region, one warp per row in 32-pixel chunks (rows with no
   // change in reach are skipped in active-set sweeps).
-  for (int ay = OFF - 1 + warp; ay < OFF + kIY; ay += nwarps) {
-    if (use_act) {
-      const int an = min(ay + 1, kLY - 1);
-      if (!(sm.act[0][ay] | sm.act[1][ay] | sm.act[0][an] | sm.act[1][an])) continue;
-    }
-    unsigned e[kCK], d[kCK];
+  if (STAGED) {
+    constexpr int kSpan = kLY / 8;
+    const int ay = warp * kSpan + kSpan - 1;   // this warp's span's last row
+    if (ay + 1 < kLY) {
+      unsigned d[kCK];
 #pragma unroll
-    for (int c = 0; c < kCK; c++) {
-      const int x = lane + 32 * c;
-      const bool in = x < kLX;
-      const int v = in ? L[ay * kLX + x] : -1;
-      const int r = (x + 1 < kLX) ? L[ay * kLX + x + 1] : v;
-      const int dn = (in && ay + 1 < kLY) ? L[(ay + 1) * kLX + x] : v;
-      e[c] = __ballot_sync(0xffffffffu, v != r);
-      d[c] = __ballot_sync(0xffffffffu, v != dn);
+      for (int c = 0; c < kCK; c++) {
+        const int x = lane + 32 * c;
+        const bool in = x < kLX;
+        const int v = in ? L[ay * kLX + x] : -1;
+        const int dn = in ? L[(ay + 1) * kLX + x] : v;
+        d[c] = __ballot_sync(0xffffffffu, v != dn);
+      }
+      if (lane == 0) pack_row<kCK>(d, &sm.edS[0][ay], &sm.edS[1][ay]);
     }
-    if (lane == 0) {
-      unsigned long long e0 = e[0], e1 = 0, d0 = d[0], d1 = 0;
-      if (kCK > 1) { e0 |= (unsigned long long)e[1 % kCK] << 32; d0 |= (unsigned long long)d[1 % kCK] << 32; }
-      if (kCK > 2) { e1 = e[2 % kCK]; d1 = d[2 % kCK]; }
-      if (kCK > 3) { e1 |= (unsigned long long)e[3 % kCK] << 32; d1 |= (unsigned long long)d[3 % kCK] << 32; }
-      sm.edE[0][ay] = e0; sm.edE[1][ay] = e1;
-      sm.edS[0][ay] = d0; sm.edS[1][ay] = d1;
+  } else {
+    for (int ay = OFF - 1 + warp; ay < OFF + kIY; ay += nwarps) {
+      if (use_act) {
+        const int an = min(ay + 1, kLY - 1);
+        if (!(sm.act[0][ay] | sm.act[1][ay] | sm.act[0][an] | sm.act[1][an])) continue;
+      }
+      unsigned e[kCK], d[kCK];
+#pragma unroll
+      for (int c = 0; c < kCK; c++) {
+        const int x = lane + 32 * c;
+        const bool in = x < kLX;
+        const int v = in ? L[ay * kLX + x] : -1;
+        const int r = (x + 1 < kLX) ? L[ay * kLX + x + 1] : v;
+        const int dn = (in && ay + 1 < kLY) ? L[(ay + 1) * kLX + x] : v;
+        e[c] = __ballot_sync(0xffffffffu, v != r);
+        d[c] = __ballot_sync(0xffffffffu, v != dn);
+      }
+      if (lane == 0) {
+        pack_row<kCK>(e, &sm.edE[0][ay], &sm.edE[1][ay]);
+        pack_row<kCK>(d, &sm.edS[0][ay], &sm.edS[1][ay]);
+      }
     }
   }
   __syncthreads();
@@ -924,16 +964,21 @@ __device__ __forceinline__ void sweep_pass(const Slot& S, SweepTile<TX, TY, NS>&
       }
       const int cy = gy & 1;
       // the two classes of this row: (xo << 1) | cy, listed on the tile grown by
-      // G - class; x parity of a label-region column equals that of the image column
+      // G - class; x parity of a label-region column equals that of the image column.
+      // The column masks of the four classes are constants of the template.
+      constexpr unsigned long long A00 = range_word(kSH - G, kSH + TX + G, 0) & kEvenBits;
+      constexpr unsigned long long A01 = range_word(kSH - G, kSH + TX + G, 1) & kEvenBits;
+      constexpr unsigned long long B00 = range_word(kSH - G + 2, kSH + TX + G - 2, 0) & kOddBits;
+      constexpr unsigned long long B01 = range_word(kSH - G + 2, kSH + TX + G - 2, 1) & kOddBits;
+      constexpr unsigned long long A10 = range_word(kSH - G + 1, kSH + TX + G - 1, 0) & kEvenBits;
+      constexpr unsigned long long A11 = range_word(kSH - G + 1, kSH + TX + G - 1, 1) & kEvenBits;
+      constexpr unsigned long long B10 = range_word(kSH - G + 3, kSH + TX + G - 3, 0) & kOddBits;
+      constexpr unsigned long long B11 = range_word(kSH - G + 3, kSH + TX + G - 3, 1) & kOddBits;
       const int ga = G - cy, gb = G - (2 | cy);
       const int ry = ay - kSH;                   // row relative to the tile
       const bool ya = ry >= -ga && ry < TY + ga, yb = ry >= -gb && ry < TY + gb;
-      const unsigned long long k0 =
-          (ya ? range_word(kSH - ga, kSH + TX + ga, 0) & kEvenBits : 0ull) |
-          (yb ? range_word(kSH - gb, kSH + TX + gb, 0) & kOddBits : 0ull);
-      const unsigned long long k1 =
-          (ya ? range_word(kSH - ga, kSH + TX + ga, 1) & kEvenBits : 0ull) |
-          (yb ? range_word(kSH - gb, kSH + TX + gb, 1) & kOddBits : 0ull);
+      const unsigned long long k0 = (ya ? (cy ? A10 : A00) : 0ull) | (yb ? (cy ? B10 : B00) : 0ull);
+      const unsigned long long k1 = (ya ? (cy ? A11 : A01) : 0ull) | (yb ? (cy ? B11 : B01) : 0ull);
       const unsigned long long e0 = sm.edE[0][ay], e1 = sm.edE[1][ay];
       const unsigned long long b0 = e0 | (e0 << 1) | sm.edS[0][ay] | sm.edS[0][ay - 1];
       const unsigned long long b1 =
@@ -1070,11 +1115,12 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   // in 32-label chunks, every load issued before any is used, so the block waits for
   // one memory round trip (overlapping the change-flag loads of active-set sweeps).
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int kRW = (kLY + 7) / 8, kCK = (kLX + 31) / 32;
+  constexpr int kRW = kLY / 8, kCK = (kLX + 31) / 32;   // warp w: rows kRW w .. kRW w + kRW - 1
+  static_assert(kLY % 8 == 0, "label-region rows in whole warp spans");
   int lv[kRW][kCK];
 #pragma unroll
   for (int a = 0; a < kRW; a++) {
-    const int r = warp + 8 * a, gy = ry0 + r;
+    const int r = warp * kRW + a, gy = ry0 + r;
     const bool row_ok = r < kLY && gy >= 0 && gy < H;
 #pragma unroll
     for (int c = 0; c < kCK; c++) {
@@ -1132,7 +1178,7 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       // change, and there is none in the label region)
 #pragma unroll
       for (int a = 0; a < kRW; a++) {
-        const int rr = warp + 8 * a;
+        const int rr = warp * kRW + a;
 #pragma unroll
         for (int c = 0; c < kCK; c++) {
           const int x = lane + 32 * c;
@@ -1160,14 +1206,27 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
     // (the barrier after the label stores below orders these before the border pass)
   }
   // labels to shared memory (colours are not staged: the scored border pixels read
-  // theirs from global memory)
+  // theirs from global memory), and the label edges of the warp's rows from the
+  // registers: right neighbours by shuffles, lower neighbours from the next row of
+  // the span (the span's last row waits for the shared copy, see sweep_pass)
 #pragma unroll
   for (int a = 0; a < kRW; a++) {
-    const int r = warp + 8 * a;
+    const int r = warp * kRW + a;
+    unsigned e[kCK], d[kCK];
 #pragma unroll
     for (int c = 0; c < kCK; c++) {
       const int x = lane + 32 * c;
-      if (r < kLY && x < kLX) L[r * kLX + x] = lv[a][c];
+      const int v = lv[a][c];
+      if (x < kLX) L[r * kLX + x] = v;
+      int right = __shfl_down_sync(0xffffffffu, v, 1);
+      const int nxt = __shfl_sync(0xffffffffu, lv[a][c + 1 < kCK ? c + 1 : c], 0);
+      if (lane == 31) right = c + 1 < kCK ? nxt : v;
+      e[c] = __ballot_sync(0xffffffffu, x + 1 < kLX && v != right);
+      d[c] = __ballot_sync(0xffffffffu, x < kLX && a + 1 < kRW && v != lv[a + 1 < kRW ? a + 1 : a][c]);
+    }
+    if (lane == 0) {
+      pack_row<kCK>(e, &sm.edE[0][r], &sm.edE[1][r]);
+      if (a + 1 < kRW) pack_row<kCK>(d, &sm.edS[0][r], &sm.edS[1][r]);
     }
   }
   __syncthreads();
@@ -1181,14 +1240,15 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   }
   // (the listing barrier of the first pass orders these clears before any use)
   if (NS == 1) {
-    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0, true,
-                                       deltas != 0);
+    sweep_pass<TX, TY, NS, 4 * NS - 1, true>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0,
+                                             true, deltas != 0);
   } else {
-    sweep_pass<TX, TY, NS, 4 * NS - 1>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0, false,
-                                       deltas != 0);
+    sweep_pass<TX, TY, NS, 4 * NS - 1, true>(S, sm, lut_bits, tx0, ty0, s2, potts, mode != 0,
+                                             false, deltas != 0);
     if (threadIdx.x < 4) cnt[threadIdx.x] = 0;   // fresh lists (the phases' last barrier
                                                  // ordered every read of the counts)
-    sweep_pass<TX, TY, NS, 3>(S, sm, lut_bits, tx0, ty0, s2, potts, false, true, deltas != 0);
+    sweep_pass<TX, TY, NS, 3, false>(S, sm, lut_bits, tx0, ty0, s2, potts, false, true,
+                                     deltas != 0);
   }
   if (deltas) delta_flush(sm.delta, S.sp, tx0, ty0);   // after the last phase's barrier
   // write back the tile (a warp covers 32 consecutive pixels of a row; 16-wide tiles:
@@ -1218,11 +1278,7 @@ __device__ __forceinline__ void sweep_flat(const Slot* __restrict__ slots, int B
                                            float s2, float potts, int mode, int deltas) {
   __shared__ SweepTile<TX, TY, NS> sm;
   __shared__ unsigned lut_bits[8];
-  if (threadIdx.x < 8) {
-    unsigned w = 0;
-    for (int b = 0; b < 32; b++) w |= (unsigned)(c_simple_lut[threadIdx.x * 32 + b] != 0) << b;
-    lut_bits[threadIdx.x] = w;
-  }
+  if (threadIdx.x < 8) lut_bits[threadIdx.x] = c_simple_bits.w[threadIdx.x];
   const int v = TX == 32 ? 0 : TX == 64 ? 1 : 2;   // which tile_base of the slots
   const int t = blockIdx.x;
   int lo = 0, hi = B - 1;
@@ -1251,11 +1307,7 @@ __device__ __forceinline__ void sweep_queue(const Slot* __restrict__ slots, int 
   __shared__ SweepTile<TX, TY, 1> sm;
   __shared__ unsigned lut_bits[8];
   __shared__ int next;
-  if (threadIdx.x < 8) {
-    unsigned w = 0;
-    for (int b = 0; b < 32; b++) w |= (unsigned)(c_simple_lut[threadIdx.x * 32 + b] != 0) << b;
-    lut_bits[threadIdx.x] = w;
-  }
+  if (threadIdx.x < 8) lut_bits[threadIdx.x] = c_simple_bits.w[threadIdx.x];
   const int v = TX == 32 ? 0 : TX == 64 ? 1 : 2;   // which tile_base of the slots
   for (;;) {
     if (threadIdx.x == 0) next = (int)atomicAdd(&queue[0], 1u);
