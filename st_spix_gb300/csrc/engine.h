@@ -177,8 +177,10 @@ enum { kOpBegin = 0, kOpAfterHex = 1, kOpCompactN = 2, kOpCompactEnd = 3 };
 // h = trunc(t / 2^18) is an exact integer-valued float; l = t - h * 2^18 holds the bits
 // of t below 2^18 (same sign, |l| < 2^18) and is exact; h * 2^18 is an even integer, so
 // round(t) = h * 2^18 + round(l), ties included.
+// Values in [0, 1] (colours, their squares) take one conversion: t <= 2^shift < 2^32.
 __device__ __forceinline__ long long fx_q(float v, int shift) {
   const float t = v * (float)(1u << shift);
+  if (v >= 0.f && v <= 1.f) return (long long)__float2uint_rn(t);
   const float h = truncf(t * 0x1p-18f);
   const float l = t - h * 0x1p18f;
   return (long long)__float2int_rz(h) * 262144LL + (long long)__float2int_rn(l);

@@ -1118,14 +1118,26 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   constexpr int kRW = kLY / 8, kCK = (kLX + 31) / 32;   // warp w: rows kRW w .. kRW w + kRW - 1
   static_assert(kLY % 8 == 0, "label-region rows in whole warp spans");
   int lv[kRW][kCK];
+  if (rx0 >= 0 && ry0 >= 0 && rx0 + kLX <= W && ry0 + kLY <= H) {
+    // the label region lies inside the frame (most tiles): one row pointer per row,
+    // no per-label bounds but the region's width
+    const int* base = seg_in + (size_t)(ry0 + warp * kRW) * W + rx0 + lane;
 #pragma unroll
-  for (int a = 0; a < kRW; a++) {
-    const int r = warp * kRW + a, gy = ry0 + r;
-    const bool row_ok = r < kLY && gy >= 0 && gy < H;
+    for (int a = 0; a < kRW; a++) {
 #pragma unroll
-    for (int c = 0; c < kCK; c++) {
-      const int x = lane + 32 * c, gx = rx0 + x;
-      lv[a][c] = (row_ok && x < kLX && gx >= 0 && gx < W) ? seg_in[gy * W + gx] : -1;
+      for (int c = 0; c < kCK; c++)
+        lv[a][c] = (lane + 32 * c < kLX) ? base[(size_t)a * W + 32 * c] : -1;
+    }
+  } else {
+#pragma unroll
+    for (int a = 0; a < kRW; a++) {
+      const int r = warp * kRW + a, gy = ry0 + r;
+      const bool row_ok = r < kLY && gy >= 0 && gy < H;
+#pragma unroll
+      for (int c = 0; c < kCK; c++) {
+        const int x = lane + 32 * c, gx = rx0 + x;
+        lv[a][c] = (row_ok && x < kLX && gx >= 0 && gx < W) ? seg_in[gy * W + gx] : -1;
+      }
     }
   }
   // tile pixels of the staging layout: (a, c) -> label-region (r, x)
