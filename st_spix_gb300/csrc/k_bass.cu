@@ -469,8 +469,27 @@ __global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slo
   const SpDev& sp = S.sp;
   const int k = blockIdx.x * 32 + lane;
   const bool inr = k < sp.cap;
-  const int count_int = inr ? sp.count[k] : 0;
-  const uint8_t valid = inr ? sp.valid[k] : 0;
+  // every load of the id is issued before any is used (one memory round trip): the
+  // count and flags, and the fields this warp's part of the posterior reads
+  int count_int = 0;
+  uint8_t valid = 0, prop = 0;
+  float pc = 0.f;
+  long long a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0;
+  double q0 = 0, q1 = 0, q2 = 0, i0 = 0, i1 = 0, i2 = 0;
+  const long long* a = sp.acc + 8 * (size_t)k;
+  if (inr) {
+    count_int = sp.count[k];
+    valid = sp.valid[k];
+    if (w == 0) { a0 = a[0]; a1 = a[1]; a2 = a[2]; }
+    else if (w == 1) {
+      pc = sp.prior_count[k];
+      prop = sp.prop[k];
+      q0 = sp.sample_sigma_shape[3 * k]; q1 = sp.sample_sigma_shape[3 * k + 1];
+      q2 = sp.sample_sigma_shape[3 * k + 2];
+      i0 = sp.prior_icov[3 * k]; i1 = sp.prior_icov[3 * k + 1]; i2 = sp.prior_icov[3 * k + 2];
+    } else if (w == 2) { a0 = a[3]; a1 = a[4]; a2 = a[5]; a3 = a[6]; a4 = a[7]; }
+    if (w != 1) pc = sp.prior_count[k];
+  }
   const bool live = valid && count_int > 0;
   if (w == 0 && inr) {
     if (valid && count_int <= 0) sp.valid[k] = 0;
@@ -480,26 +499,24 @@ __global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slo
     }
   }
   if (!__syncthreads_or(live)) return;
-  const float pc = live ? sp.prior_count[k] : 0.f;
   const double count = count_int * 1.0;
   const double total_count = (double)count_int + pc * 50;
-  const long long* a = sp.acc + 8 * (size_t)k;
   if (live) {
     if (w == 0) {
       // colour means (fixed-point sums, R1)
+      const long long ac[3] = {a0, a1, a2};
       for (int c = 0; c < 3; c++) {
-        const float m = (float)(fx_unq(a[c], kFxAppShift) / count);
+        const float m = (float)(fx_unq(ac[c], kFxAppShift) / count);
         sp.mu_app[3 * k + c] = m;
         v_app[c][lane] = m;
       }
     } else if (w == 1) {
       // prior shape term (calc_simple_update with _add_sigma_smoothing)
       double px, py, pz;
-      if (sp.prop[k]) {
-        smooth_prior(sp.sample_sigma_shape[3 * k], sp.sample_sigma_shape[3 * k + 1],
-                     sp.sample_sigma_shape[3 * k + 2], (int)pc, pc, S.sp_size, &px, &py, &pz);
+      if (prop) {
+        smooth_prior(q0, q1, q2, (int)pc, pc, S.sp_size, &px, &py, &pz);
       } else {
-        px = sp.prior_icov[3 * k]; py = sp.prior_icov[3 * k + 1]; pz = sp.prior_icov[3 * k + 2];
+        px = i0; py = i1; pz = i2;
       }
       double pr_det = px * pz - py * py;
       if (!(pr_det > 0)) atomicExch(&S.sc->status, STSPIX_ERR_DEGENERATE);
@@ -509,12 +526,12 @@ __global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slo
       v_ps[2][lane] = pc / pr_det * pz;
     } else if (w == 2) {
       // shape mean and scatter
-      const double mx = a[3] / count, my = a[4] / count;
+      const double mx = a0 / count, my = a1 / count;
       sp.mu_shape[2 * k] = mx; sp.mu_shape[2 * k + 1] = my;
       v_m[0][lane] = mx; v_m[1][lane] = my;
-      v_raw[0][lane] = a[5] - count * mx * mx;
-      v_raw[1][lane] = a[6] - count * mx * my;
-      v_raw[2][lane] = a[7] - count * my * my;
+      v_raw[0][lane] = a2 - count * mx * mx;
+      v_raw[1][lane] = a3 - count * mx * my;
+      v_raw[2][lane] = a4 - count * my * my;
     }
   }
   __syncthreads();

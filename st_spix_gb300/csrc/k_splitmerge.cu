@@ -212,6 +212,53 @@ __device__ void bfs_bits(int t, int k, int x0, int y0, int bw, int bh, int W,
   }
 }
 
+// Boxes of at most 64 x 32 pixels (most superpixels): lane r holds row r of the box as
+// one 64-bit word of each field in registers; a layer is two shifts, a shuffle from the
+// rows above and below, and the masks, with no shared memory and no barrier.
+__device__ __forceinline__ void bfs_reg(int k, int x0, int y0, int bw, int bh, int W,
+                                        const int* __restrict__ seg, int* d1, int* d2) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long m = 0, f1 = 0, f2 = 0;
+  const int cpr = (bw + 31) >> 5;                 // 1 or 2 chunks of 32 pixels per row
+  for (int r = 0; r < bh; r++) {
+    for (int cx = 0; cx < cpr; cx++) {
+      const int xi = cx * 32 + lane;
+      bool in = false, s1 = false, s2 = false;
+      if (xi < bw) {
+        const int g = (y0 + r) * W + x0 + xi;
+        in = seg[g] == k;
+        if (in) { s1 = d1[g] == 1; s2 = d2[g] == 1; }
+      }
+      const unsigned bm = __ballot_sync(0xffffffffu, in);
+      const unsigned b1 = __ballot_sync(0xffffffffu, s1);
+      const unsigned b2 = __ballot_sync(0xffffffffu, s2);
+      if (lane == r) {
+        m |= (unsigned long long)bm << (32 * cx);
+        f1 |= (unsigned long long)b1 << (32 * cx);
+        f2 |= (unsigned long long)b2 << (32 * cx);
+      }
+    }
+  }
+  unsigned long long v1 = f1, v2 = f2;
+  const int area = bw * bh;
+  const int gb = (y0 + lane) * W + x0;
+  for (int L = 1; L <= area + 1; L++) {
+    unsigned long long u1 = __shfl_up_sync(0xffffffffu, f1, 1);
+    unsigned long long w1 = __shfl_down_sync(0xffffffffu, f1, 1);
+    unsigned long long u2 = __shfl_up_sync(0xffffffffu, f2, 1);
+    unsigned long long w2 = __shfl_down_sync(0xffffffffu, f2, 1);
+    if (lane == 0) { u1 = 0; u2 = 0; }
+    if (lane == 31) { w1 = 0; w2 = 0; }
+    const unsigned long long n1 = ((f1 << 1) | (f1 >> 1) | u1 | w1) & m & ~v1;
+    const unsigned long long n2 = ((f2 << 1) | (f2 >> 1) | u2 | w2) & m & ~v2;
+    f1 = n1; f2 = n2;
+    v1 |= n1; v2 |= n2;
+    for (unsigned long long b = n1; b; b &= b - 1) d1[gb + __ffsll((long long)b) - 1] = L + 1;
+    for (unsigned long long b = n2; b; b &= b - 1) d2[gb + __ffsll((long long)b) - 1] = L + 1;
+    if (!__any_sync(0xffffffffu, (n1 | n2) != 0ull)) break;
+  }
+}
+
 struct BfsWarpSmem {
   unsigned long long a[5][kWarpRows * kWarpWpr];
 };
@@ -232,6 +279,10 @@ __global__ void __launch_bounds__(128) kb_split_bfs(const Slot* __restrict__ slo
     const int bw = x1 - x0 + 1, bh = y1 - y0 + 1;
     if (bw > 64 * kWarpWpr || bh > kWarpRows) {
       if (lane == 0) S.sm.newid[atomicAdd(&S.sc->tmp2, 1)] = k;
+      continue;
+    }
+    if (bw <= 64 && bh <= 32) {
+      bfs_reg(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2);
       continue;
     }
     bfs_bits<32, kWarpRows * kWarpWpr / 32>(lane, k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2,
