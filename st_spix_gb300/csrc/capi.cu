@@ -162,6 +162,11 @@ std::mutex g_device_mu;
 const int kThreads = 256;
 const int kBfsBigSmem = 5 * 512 * 8 * 8;  // kb_split_bfs_big: 5 arrays of 512 rows x 8 words
 inline unsigned blocks_for(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
+// 64 x 32 tiles of the largest frame of a slot table (per-slot grids of the warp-block
+// kernels; blocks past a smaller frame's tiles return).
+inline unsigned tiles64(const List& L) {
+  return (unsigned)std::max(1, ((L.max_w + 63) / 64) * ((L.max_h + 31) / 32));
+}
 
 int fail(stspix_ctx* c, int code, const char* fmt, ...) {
   char buf[512];
@@ -464,7 +469,7 @@ void preload_kernels() {
       (const void*)kb_fill_split,
       (const void*)kb_fill_phase,
       (const void*)kb_fill_end,
-      (const void*)kb_cc_init,
+      (const void*)kb_cc_local,
       (const void*)kb_cc_hook,
       (const void*)kb_cc_compress,
       (const void*)kb_list_holes,
@@ -858,7 +863,7 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
   LAUNCHB(kb_split_clear, L.max_npix, L, nb);
   LAUNCHB(kb_split_seed, L.max_cap, L, nb, dir_b, dir_p);
   LAUNCHG(kb_bbox, dim3(blocks_for(L.max_sm), (unsigned)nb), kThreads, L.d);
-  LAUNCHG(kb_split_bfs, dim3(256, (unsigned)nb), 128, L.d);  // 1024 warps per slot
+  LAUNCHG(kb_split_bfs, dim3(256, (unsigned)nb), 128, L.d, dir_b, dir_p);  // 1024 warps per slot
   {
     cudaEvent_t pe_ = prof_begin(ctx, st);
     launch_k(kb_split_bfs_big, dim3(8, (unsigned)nb), dim3(256), kBfsBigSmem, st,
@@ -868,7 +873,7 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
   }
   LAUNCHB(kb_split_partition, L.max_npix, L, nb);
   LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
-  LAUNCHG(kb_sm_accumulate, dim3(blocks_for(L.max_sm), (unsigned)nb), kThreads, L.d, 1);
+  LAUNCHG(kb_sm_accumulate, dim3(tiles64(L), (unsigned)nb), kThreads, L.d, 1);
   LAUNCHB(kb_split_decide, L.max_cap, L, nb, K, cfg.split_alpha);
   LAUNCHG(kb_scan, (unsigned)nb, 1024, L.d, 1);
   LAUNCHB(kb_split_commit, L.max_cap, L, nb);
@@ -903,7 +908,7 @@ int run_merge(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
   LAUNCHB(kb_merge_clear, L.max_cap + 2, L, nb);
   LAUNCHB(kb_merge_candidates, L.max_npix, L, nb, dir_b, dir_p);
   LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
-  LAUNCHG(kb_sm_accumulate, dim3(blocks_for(L.max_sm), (unsigned)nb), kThreads, L.d, 0);
+  LAUNCHG(kb_sm_accumulate, dim3(tiles64(L), (unsigned)nb), kThreads, L.d, 0);
   LAUNCHB(kb_merge_single, L.max_cap, L, nb, K);
   LAUNCHB(kb_merge_decide, L.max_cap, L, nb, K, cfg.merge_alpha);
   LAUNCHB(kb_merge_flag, L.max_cap, L, nb);
@@ -1162,7 +1167,8 @@ int shift_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHG(kb_count_labels, dim3(blocks_for(L.max_sm), (unsigned)L.B), kThreads, L.d, 0);
   // fill, invalidate disconnected, fill
   if ((r = run_fill(ctx, st, L))) return r;
-  LAUNCHB(kb_cc_init, L.max_npix, L, L.B);
+  LAUNCHG(kb_cc_local, dim3((unsigned)(((L.max_w + 31) / 32) * ((L.max_h + 31) / 32)), (unsigned)L.B),
+          kThreads, L.d);
   LAUNCHB(kb_cc_hook, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_compress, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_size, L.max_npix, L, L.B);

@@ -51,10 +51,6 @@ struct __align__(16) SweepRec {
 __device__ __forceinline__ int spread_id(int j) { return blockIdx.x + gridDim.x * j; }
 #define FOR_SP(k, n)                                                              \
   for (int j_ = threadIdx.x, k = spread_id(j_); k < (n); j_ += blockDim.x, k = spread_id(j_))
-// Same over a batched launch whose x dimension alone covers the ids.
-__device__ __forceinline__ int spread_id_x(int j) { return blockIdx.x + gridDim.x * j; }
-#define FOR_SPX(k, n)                                                             \
-  for (int j_ = threadIdx.x, k = spread_id_x(j_); k < (n); j_ += blockDim.x, k = spread_id_x(j_))
 
 // Per-superpixel working state, structure of arrays, `cap` entries each.
 struct SpDev {
@@ -187,6 +183,14 @@ __device__ __forceinline__ long long fx_q(float v, int shift) {
 }
 __device__ __forceinline__ double fx_unq(long long q, int shift) {
   return ldexp((double)q, -shift);
+}
+// Full-warp sum of a 64-bit integer by 32-bit reductions: v = hi * 2^24 + lo with lo in
+// [0, 2^24), so the lo parts of 32 lanes stay below 2^29; |v| < 2^54 per lane.
+__device__ __forceinline__ long long warp_sum64(long long v) {
+  const unsigned lo = (unsigned)(v & 0xFFFFFF);
+  const int hi = (int)(v >> 24);
+  return (long long)__reduce_add_sync(0xffffffffu, hi) * (1LL << 24) +
+         (long long)__reduce_add_sync(0xffffffffu, lo);
 }
 
 }  // namespace stspix

@@ -255,14 +255,6 @@ __global__ void kb_init_prior_mu(const Slot* __restrict__ slots) {
 // scatter this replaces, with a set of atomics per run of a 32-pixel row, took 50 us
 // per 8-frame 480x854 batch against 43 us here).  Integer sums: the totals do not
 // depend on the grouping or the order of the adds.
-__device__ __forceinline__ long long warp_sum64(long long v) {
-  // |v| < 2^54 per lane: v = hi * 2^24 + lo, lo in [0, 2^24)
-  const unsigned lo = (unsigned)(v & 0xFFFFFF);
-  const int hi = (int)(v >> 24);
-  return (long long)__reduce_add_sync(0xffffffffu, hi) * (1LL << 24) +
-         (long long)__reduce_add_sync(0xffffffffu, lo);
-}
-
 __device__ __forceinline__ void block_stats(const Slot& S, int bx, int by) {
   const int lane = threadIdx.x & 31;
   const int H = S.H, W = S.W;

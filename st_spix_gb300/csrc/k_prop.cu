@@ -383,15 +383,6 @@ __global__ void kb_fill_end(const Slot* __restrict__ slots) {
 // ---------------------------------------------------------------------------
 // Disconnected regions (split_disconnected.cu:33-96): component roots by
 // union-find, sizes, largest region per label (R6), invalidate the rest.
-__global__ void kb_cc_init(const Slot* __restrict__ slots) {
-  pdl_enter();
-  SLOT_Y;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  S.d1[t] = S.seg[t] >= 0 ? t : -1;
-  if (t == 0) S.sc->nhole = 0;
-}
-
 // Connected components (8-connected, same label) by union-find with min-index
 // hooking: every tree's root is the smallest pixel index of its component, the
 // fixed point of find_spix_min (split_disconnected.cu:458-498).  Parents only
@@ -423,29 +414,89 @@ __device__ __forceinline__ bool uf_unite(int* parent, int a, int b) {
   return false;
 }
 
-// Unions with the earlier 8-neighbours; a diagonal one is skipped when a 4-path
-// through W or N already joins it (W-NW and N-NW, N-NE are united at those pixels).
+// The unions of pixel t: with the earlier 8-neighbours of the same label; a diagonal one
+// is skipped when a 4-path through W or N already joins it (W-NW and N-NW, N-NE are
+// united at those pixels).  Each union is made by the pass that owns it: a tile's own
+// pass (kb_cc_local, both pixels in one CC tile) or the cross-tile pass (kb_cc_hook);
+// union-find with min-index hooking reaches the same roots whatever the order.
+constexpr int kCcTile = 32;             // CC tiles of 32 x 32 pixels
+__device__ __forceinline__ bool cc_same_tile(int x, int y, int xn, int yn) {
+  return (x / kCcTile) == (xn / kCcTile) && (y / kCcTile) == (yn / kCcTile);
+}
+template <typename Unite>
+__device__ __forceinline__ void cc_unions(const int* __restrict__ seg, int t, int W, int L,
+                                          bool local, Unite unite) {
+  const int x = t % W, y = t / W;
+  auto own = [&](int xn, int yn) { return cc_same_tile(x, y, xn, yn) == local; };
+  const bool w = x > 0 && seg[t - 1] == L;
+  if (w && own(x - 1, y)) unite(t - 1);
+  if (y > 0) {
+    if (seg[t - W] == L) {
+      if (own(x, y - 1)) unite(t - W);
+    } else {
+      if (!w && x > 0 && seg[t - W - 1] == L && own(x - 1, y - 1)) unite(t - W - 1);
+      if (x < W - 1 && seg[t - W + 1] == L && own(x + 1, y - 1)) unite(t - W + 1);
+    }
+  }
+}
+
+// One block per 32 x 32 tile: parents of the tile's pixels by union-find in shared
+// memory over the unions inside the tile, then each pixel's global parent = its local
+// root (the smallest pixel index of its component within the tile: row-major order
+// within a tile is the frame's order).  Replaces the parent initialisation.
+__global__ void __launch_bounds__(256) kb_cc_local(const Slot* __restrict__ slots) {
+  pdl_enter();
+  SLOT_Y;
+  __shared__ int par[kCcTile * kCcTile];
+  const int W = S.W, H = S.H;
+  const int tiles_x = (W + kCcTile - 1) / kCcTile;
+  if ((int)blockIdx.x >= tiles_x * ((H + kCcTile - 1) / kCcTile)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) S.sc->nhole = 0;
+  const int tx0 = (blockIdx.x % tiles_x) * kCcTile, ty0 = (blockIdx.x / tiles_x) * kCcTile;
+  const int* seg = S.seg;
+  auto gidx = [&](int li) { return (ty0 + li / kCcTile) * W + tx0 + li % kCcTile; };
+  auto lidx = [&](int g) { return (g / W - ty0) * kCcTile + (g % W - tx0); };
+  for (int li = threadIdx.x; li < kCcTile * kCcTile; li += blockDim.x) {
+    const int x = tx0 + li % kCcTile, y = ty0 + li / kCcTile;
+    par[li] = (x < W && y < H && seg[gidx(li)] >= 0) ? li : -1;
+  }
+  __syncthreads();
+  bool ok = true;
+  for (int li = threadIdx.x; li < kCcTile * kCcTile; li += blockDim.x) {
+    const int x = tx0 + li % kCcTile, y = ty0 + li / kCcTile;
+    if (x >= W || y >= H) continue;
+    const int t = gidx(li);
+    const int L = seg[t];
+    if (L < 0) continue;
+    cc_unions(seg, t, W, L, true, [&](int tn) { ok &= uf_unite(par, li, lidx(tn)); });
+  }
+  __syncthreads();
+  for (int li = threadIdx.x; li < kCcTile * kCcTile; li += blockDim.x) {
+    const int x = tx0 + li % kCcTile, y = ty0 + li / kCcTile;
+    if (x >= W || y >= H) continue;
+    const int r = par[li] >= 0 ? uf_find(par, li) : -1;
+    if (par[li] >= 0 && r < 0) ok = false;
+    S.d1[gidx(li)] = r >= 0 ? gidx(r) : -1;
+  }
+  if (!ok) atomicExch(&S.sc->status, STSPIX_ERR_ITER_LIMIT);
+}
+
+// The unions across tile edges (only pixels on a tile's first row or first / last
+// column have neighbours in another tile), on the global parents.
 __global__ void kb_cc_hook(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.npix) return;
   const int W = S.W;
+  const int x = t % W, y = t / W;
+  const int lx = x % kCcTile, ly = y % kCcTile;
+  if (!(lx == 0 || ly == 0 || lx == kCcTile - 1)) return;
   const int* seg = S.seg;
   const int L = seg[t];
   if (L < 0) return;
-  const int x = t % W, y = t / W;
   bool ok = true;
-  const bool w = x > 0 && seg[t - 1] == L;
-  if (w) ok &= uf_unite(S.d1, t, t - 1);
-  if (y > 0) {
-    if (seg[t - W] == L) {
-      ok &= uf_unite(S.d1, t, t - W);
-    } else {
-      if (!w && x > 0 && seg[t - W - 1] == L) ok &= uf_unite(S.d1, t, t - W - 1);
-      if (x < W - 1 && seg[t - W + 1] == L) ok &= uf_unite(S.d1, t, t - W + 1);
-    }
-  }
+  cc_unions(seg, t, W, L, false, [&](int tn) { ok &= uf_unite(S.d1, t, tn); });
   if (!ok) atomicExch(&S.sc->status, STSPIX_ERR_ITER_LIMIT);
 }
 

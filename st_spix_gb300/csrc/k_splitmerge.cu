@@ -12,35 +12,32 @@ namespace stspix {
 
 
 // ---------------------------------------------------------------------------
-// Split seeds (init_split, split_merge.cu:803-844) for both directions.
+// Split seeds (init_split, split_merge.cu:803-844): seed s (0, 1) of superpixel k is
+// the pixel one step from its mean position along +direction (s = 0) or -direction
+// (s = 1), x for |direction| = 1 and y otherwise; -1 when that pixel is off the frame or
+// not of label k.
+__device__ __forceinline__ int split_seed_index(const Slot& S, int k, int s, int direction) {
+  const int dir = s == 0 ? direction : -direction;
+  int x = int(S.sp.mu_shape[2 * k]), y = int(S.sp.mu_shape[2 * k + 1]);
+  if (dir == 1 || dir == -1) x += dir; else y += dir;
+  const long long ind = (long long)y * S.W + x;
+  if (ind < 0 || ind > (long long)S.W * S.H - 1) return -1;
+  return S.seg[ind] == k ? (int)ind : -1;
+}
+
 __global__ void kb_split_seed(const Slot* __restrict__ slots, int dir_bass, int dir_prop) {
   pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
-  const int* __restrict__ seg = S.seg;
-  const int H = S.H, W = S.W;
   const int direction = S.mode ? dir_prop : dir_bass;
-  int* __restrict__ d1 = S.d1;
-  int* __restrict__ d2 = S.d2;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sp.cap) return;
   int* bb = S.bbox + 4 * (size_t)k;
   bb[0] = INT32_MAX; bb[1] = -1; bb[2] = INT32_MAX; bb[3] = -1;
   if (!S.sc->tmp0 /*split_on*/ || !sp.valid[k]) return;
   for (int s = 0; s < 2; s++) {
-    int dir = s == 0 ? direction : -direction;
-    int x, y;
-    if (dir == 1 || dir == -1) {
-      x = int(sp.mu_shape[2 * k]) + dir;
-      y = int(sp.mu_shape[2 * k + 1]);
-    } else {
-      x = int(sp.mu_shape[2 * k]);
-      y = int(sp.mu_shape[2 * k + 1]) + dir;
-    }
-    long long ind = (long long)y * W + x;
-    if (ind < 0 || ind > (long long)W * H - 1) continue;
-    if (seg[ind] != k) continue;
-    (s == 0 ? d1 : d2)[ind] = 1;
+    const int ind = split_seed_index(S, k, s, direction);
+    if (ind >= 0) (s == 0 ? S.d1 : S.d2)[ind] = 1;
   }
 }
 
@@ -104,10 +101,10 @@ __global__ void kb_bbox(const Slot* __restrict__ slots) {
 //     N = (F << 1 | F >> 1 | F[row-1] | F[row+1]) & M & ~V
 // per word, so a layer costs O(rows x words) however the superpixel is shaped;
 // each newly reached pixel gets distance L + 1 written once.
-// kb_split_bfs runs one warp per superpixel (boxes up to 128 x 128 pixels) and
-// lists larger boxes for kb_split_bfs_big (one block each, boxes up to 512 x 512
-// pixels; beyond that the same layers run on the global distances).
-constexpr int kWarpRows = 128, kWarpWpr = 2;    // warp: 128 rows x 2 words
+// kb_split_bfs runs one warp per superpixel with the box in registers (boxes up to
+// 128 x 128 pixels, bfs_reg) and lists larger boxes for kb_split_bfs_big (one block
+// each, the box in shared memory up to 512 x 512 pixels, bfs_bits; beyond that the same
+// layers run on the global distances).
 constexpr int kBigRows = 512, kBigWpr = 8;      // block: 512 rows x 8 words
 
 template <int NT>
@@ -212,64 +209,115 @@ __device__ void bfs_bits(int t, int k, int x0, int y0, int bw, int bh, int W,
   }
 }
 
-// Boxes of at most 64 x 32 pixels (most superpixels): lane r holds row r of the box as
-// one 64-bit word of each field in registers; a layer is two shifts, a shuffle from the
-// rows above and below, and the masks, with no shared memory and no barrier.
+// Boxes of at most 128 x 128 pixels (every superpixel of ordinary frames): the box is
+// held in registers, lane l holding rows R l .. R l + R - 1 (R = 1..4 by the box height)
+// as C 64-bit words each (C = 1, 2 by its width) of each field: label mask m, frontiers
+// f1, f2 and visited v1, v2.  A layer is shifts within a row, the rows above and below
+// from the lane's own rows or one shuffle, and the masks: no shared memory, no barrier.
+// The seeds come as pixel indices (split_seed_index), so the box's distances are not
+// read.
+template <int R, int C>
 __device__ __forceinline__ void bfs_reg(int k, int x0, int y0, int bw, int bh, int W,
-                                        const int* __restrict__ seg, int* d1, int* d2) {
+                                        const int* __restrict__ seg, int* d1, int* d2,
+                                        int seed1, int seed2) {
+  using u64 = unsigned long long;
   const int lane = threadIdx.x & 31;
-  unsigned long long m = 0, f1 = 0, f2 = 0;
-  const int cpr = (bw + 31) >> 5;                 // 1 or 2 chunks of 32 pixels per row
-  for (int r = 0; r < bh; r++) {
-    for (int cx = 0; cx < cpr; cx++) {
-      const int xi = cx * 32 + lane;
-      bool in = false, s1 = false, s2 = false;
-      if (xi < bw) {
-        const int g = (y0 + r) * W + x0 + xi;
-        in = seg[g] == k;
-        if (in) { s1 = d1[g] == 1; s2 = d2[g] == 1; }
+  u64 m[R][C], f1[R][C], f2[R][C], v1[R][C], v2[R][C];
+#pragma unroll
+  for (int j = 0; j < R; j++)
+#pragma unroll
+    for (int w = 0; w < C; w++) m[j][w] = 0;
+  // label mask: groups of 12 rows (R divides 12, so row rb + i sits in slot i % R of lane
+  // (rb + i) / R), each row as 2C coalesced 32-pixel chunks, the group's loads issued
+  // together
+  constexpr int G = 12;
+  for (int rb = 0; rb < bh; rb += G) {
+    int v[G][2 * C];
+#pragma unroll
+    for (int i = 0; i < G; i++)
+#pragma unroll
+      for (int cx = 0; cx < 2 * C; cx++) {
+        const int r = rb + i, xi = cx * 32 + lane;
+        v[i][cx] = (r < bh && xi < bw) ? seg[(size_t)(y0 + r) * W + x0 + xi] : -1;
       }
-      const unsigned bm = __ballot_sync(0xffffffffu, in);
-      const unsigned b1 = __ballot_sync(0xffffffffu, s1);
-      const unsigned b2 = __ballot_sync(0xffffffffu, s2);
-      if (lane == r) {
-        m |= (unsigned long long)bm << (32 * cx);
-        f1 |= (unsigned long long)b1 << (32 * cx);
-        f2 |= (unsigned long long)b2 << (32 * cx);
+#pragma unroll
+    for (int i = 0; i < G; i++)
+#pragma unroll
+      for (int cx = 0; cx < 2 * C; cx++) {
+        const unsigned b = __ballot_sync(0xffffffffu, v[i][cx] == k);
+        if (lane == (rb + i) / R) m[i % R][cx >> 1] |= (u64)b << (32 * (cx & 1));
+      }
+  }
+  {
+    // seed bits: the owning lane's row slot and word as masks (a conditional write into
+    // the arrays would put them in local memory)
+    const int r1 = seed1 >= 0 ? seed1 / W - y0 - lane * R : -1, c1 = seed1 >= 0 ? seed1 % W - x0 : 0;
+    const int r2 = seed2 >= 0 ? seed2 / W - y0 - lane * R : -1, c2 = seed2 >= 0 ? seed2 % W - x0 : 0;
+    const u64 b1 = 1ull << (c1 & 63), b2 = 1ull << (c2 & 63);
+#pragma unroll
+    for (int j = 0; j < R; j++)
+#pragma unroll
+      for (int w = 0; w < C; w++) {
+        f1[j][w] = b1 & (0ull - (u64)(r1 == j && (c1 >> 6) == w));
+        f2[j][w] = b2 & (0ull - (u64)(r2 == j && (c2 >> 6) == w));
+      }
+  }
+#pragma unroll
+  for (int j = 0; j < R; j++)
+#pragma unroll
+    for (int w = 0; w < C; w++) { v1[j][w] = f1[j][w]; v2[j][w] = f2[j][w]; }
+  auto layer = [&](u64 (&f)[R][C], u64 (&v)[R][C]) {
+    u64 n[R][C];
+#pragma unroll
+    for (int w = 0; w < C; w++) {
+      u64 up = __shfl_up_sync(0xffffffffu, f[R - 1][w], 1);
+      u64 dn = __shfl_down_sync(0xffffffffu, f[0][w], 1);
+      if (lane == 0) up = 0;
+      if (lane == 31) dn = 0;
+#pragma unroll
+      for (int j = 0; j < R; j++) {
+        u64 a = (f[j][w] << 1) | (f[j][w] >> 1);
+        if (w > 0) a |= f[j][w - 1] >> 63;
+        if (w < C - 1) a |= f[j][w + 1] << 63;
+        a |= j > 0 ? f[j - 1][w] : up;
+        a |= j < R - 1 ? f[j + 1][w] : dn;
+        n[j][w] = a & m[j][w] & ~v[j][w];
       }
     }
-  }
-  unsigned long long v1 = f1, v2 = f2;
+    u64 any = 0;
+#pragma unroll
+    for (int j = 0; j < R; j++)
+#pragma unroll
+      for (int w = 0; w < C; w++) { f[j][w] = n[j][w]; v[j][w] |= n[j][w]; any |= n[j][w]; }
+    return any;
+  };
+  auto write = [&](const u64 (&f)[R][C], int* d, int val) {
+#pragma unroll
+    for (int j = 0; j < R; j++)
+#pragma unroll
+      for (int w = 0; w < C; w++)
+        if (f[j][w]) {
+          int* row = d + (size_t)(y0 + lane * R + j) * W + x0 + 64 * w;
+          for (u64 b = f[j][w]; b; b &= b - 1) row[__ffsll((long long)b) - 1] = val;
+        }
+  };
   const int area = bw * bh;
-  const int gb = (y0 + lane) * W + x0;
   for (int L = 1; L <= area + 1; L++) {
-    unsigned long long u1 = __shfl_up_sync(0xffffffffu, f1, 1);
-    unsigned long long w1 = __shfl_down_sync(0xffffffffu, f1, 1);
-    unsigned long long u2 = __shfl_up_sync(0xffffffffu, f2, 1);
-    unsigned long long w2 = __shfl_down_sync(0xffffffffu, f2, 1);
-    if (lane == 0) { u1 = 0; u2 = 0; }
-    if (lane == 31) { w1 = 0; w2 = 0; }
-    const unsigned long long n1 = ((f1 << 1) | (f1 >> 1) | u1 | w1) & m & ~v1;
-    const unsigned long long n2 = ((f2 << 1) | (f2 >> 1) | u2 | w2) & m & ~v2;
-    f1 = n1; f2 = n2;
-    v1 |= n1; v2 |= n2;
-    for (unsigned long long b = n1; b; b &= b - 1) d1[gb + __ffsll((long long)b) - 1] = L + 1;
-    for (unsigned long long b = n2; b; b &= b - 1) d2[gb + __ffsll((long long)b) - 1] = L + 1;
-    if (!__any_sync(0xffffffffu, (n1 | n2) != 0ull)) break;
+    const u64 a1 = layer(f1, v1);
+    const u64 a2 = layer(f2, v2);
+    write(f1, d1, L + 1);
+    write(f2, d2, L + 1);
+    if (!__any_sync(0xffffffffu, (a1 | a2) != 0ull)) break;
   }
 }
 
-struct BfsWarpSmem {
-  unsigned long long a[5][kWarpRows * kWarpWpr];
-};
-
-__global__ void __launch_bounds__(128) kb_split_bfs(const Slot* __restrict__ slots) {
+__global__ void __launch_bounds__(128) kb_split_bfs(const Slot* __restrict__ slots, int dir_bass,
+                                                    int dir_prop) {
   pdl_enter();
   SLOT_Y;
   if (!S.sc->tmp0) return;
-  __shared__ BfsWarpSmem sm_all[4];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  BfsWarpSmem& sm = sm_all[warp];
+  const int direction = S.mode ? dir_prop : dir_bass;
   const int n = min(S.cap, S.sc->max_spix + 1);
   for (int k = blockIdx.x * 4 + warp; k < n; k += gridDim.x * 4) {
     if (!S.sp.valid[k]) continue;
@@ -277,17 +325,28 @@ __global__ void __launch_bounds__(128) kb_split_bfs(const Slot* __restrict__ slo
     const int x0 = bb[0], x1 = bb[1], y0 = bb[2], y1 = bb[3];
     if (x1 < x0 || y1 < y0) continue;
     const int bw = x1 - x0 + 1, bh = y1 - y0 + 1;
-    if (bw > 64 * kWarpWpr || bh > kWarpRows) {
+    if (bw > 128 || bh > 128) {
       if (lane == 0) S.sm.newid[atomicAdd(&S.sc->tmp2, 1)] = k;
       continue;
     }
-    if (bw <= 64 && bh <= 32) {
-      bfs_reg(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2);
-      continue;
+    const int s1 = split_seed_index(S, k, 0, direction);
+    const int s2 = split_seed_index(S, k, 1, direction);
+    const int R = (bh + 31) >> 5;
+    if (bw <= 64) {
+      switch (R) {
+        case 1: bfs_reg<1, 1>(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2, s1, s2); break;
+        case 2: bfs_reg<2, 1>(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2, s1, s2); break;
+        case 3: bfs_reg<3, 1>(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2, s1, s2); break;
+        default: bfs_reg<4, 1>(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2, s1, s2); break;
+      }
+    } else {
+      switch (R) {
+        case 1: bfs_reg<1, 2>(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2, s1, s2); break;
+        case 2: bfs_reg<2, 2>(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2, s1, s2); break;
+        case 3: bfs_reg<3, 2>(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2, s1, s2); break;
+        default: bfs_reg<4, 2>(k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2, s1, s2); break;
+      }
     }
-    bfs_bits<32, kWarpRows * kWarpWpr / 32>(lane, k, x0, y0, bw, bh, S.W, S.seg, S.d1, S.d2,
-                                            sm.a[0], sm.a[1], sm.a[2], sm.a[3], sm.a[4]);
-    __syncwarp();
   }
 }
 
@@ -368,52 +427,84 @@ __global__ void kb_sm_clear(const Slot* __restrict__ slots) {
 // split_merge_prop.cu:1942-2018): count, colour sums, square sums, invalid count.
 // split: labels = split labels, invalid counts against the shifted labels (prop
 // slots); merge: labels = current labels, ids < cap.
-__global__ void kb_sm_accumulate(const Slot* __restrict__ slots, int split) {
+// Grid: the 64 x 32 tiles of a slot; warp w of a block owns the tile's 32 x 8 block
+// (w & 1, w >> 1), a lane one column of it.  The warp takes the block's labels one at a
+// time (the label of the lowest lane that still has pixels): each lane sums its pixels of
+// that label, full-warp reductions add the lanes' sums, and one lane adds the totals with
+// one set of atomics.  The colours wait in shared memory, so a lane converts each of its
+// pixels once, in the round of its label, and holds no 64-bit terms between rounds.
+// Integer sums (R1): totals do not depend on the grouping.
+__global__ void __launch_bounds__(256) kb_sm_accumulate(const Slot* __restrict__ slots, int split) {
   pdl_enter();
   SLOT_Y;
-  const float* __restrict__ img = S.img;
-  const int* __restrict__ lab = split ? S.smseg : S.seg;
-  const int* __restrict__ shifted = (split && S.mode) ? S.shifted : nullptr;
+  __shared__ float cs[8][8][3][32];   // [warp][row][channel][lane]
   const int H = S.H, W = S.W;
+  const int tiles_x = (W + 63) / 64;
+  if ((int)blockIdx.x >= tiles_x * ((H + 31) / 32)) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gx = (blockIdx.x % tiles_x) * 64 + (warp & 1) * 32 + lane;
+  const int by = (blockIdx.x / tiles_x) * 32 + (warp >> 1) * 8;
+  const int* __restrict__ labp = split ? S.smseg : S.seg;
+  const int* __restrict__ shifted = (split && S.mode) ? S.shifted : nullptr;
+  const float* __restrict__ img = S.img;
   const int cap = split ? S.cap + 2 : S.cap;
   const SmDev& sm = S.sm;
-  constexpr int R = 16;
-  const int cpr = (W + R - 1) / R;
-  int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= H * cpr) return;
-  int y = tid / cpr, xs = (tid % cpr) * R, xe = min(W, xs + R);
-  const int* lrow = lab + (size_t)y * W;
-  const float* irow = img + (size_t)y * W * 3;
-  const int* shrow = shifted ? shifted + (size_t)y * W : nullptr;
-  int cur = -1, n = 0, ninv = 0;
-  long long s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
-  auto flush = [&]() {
-    if (cur < 0 || cur >= cap) return;
-    atomicAdd(&sm.count[cur], n);
-    if (shrow) atomicAdd(&sm.ninvalid[cur], ninv);
-    for (int c = 0; c < 3; c++) {
-      atomicAdd((unsigned long long*)&sm.s[3 * (size_t)cur + c], (unsigned long long)s[c]);
-      atomicAdd((unsigned long long*)&sm.sq[3 * (size_t)cur + c], (unsigned long long)q[c]);
-    }
-  };
-  for (int x = xs; x < xe; x++) {
-    int k = lrow[x];
-    if (k != cur) {
-      flush();
-      cur = k; n = 0; ninv = 0;
-      s[0] = s[1] = s[2] = q[0] = q[1] = q[2] = 0;
-    }
-    if (k >= 0) {
-      n++;
-      for (int c = 0; c < 3; c++) {
-        float v = irow[3 * x + c];
-        s[c] += fx_q(v, kFxAppShift);
-        q[c] += fx_q(v * v, kFxSqShift);
+  float (*cw)[3][32] = cs[warp];
+  int lab[8];
+  unsigned inv = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int gy = by + i;
+    const bool in = gx < W && gy < H;
+    const size_t g = (size_t)gy * W + gx;
+    lab[i] = in ? labp[g] : -1;
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) cw[i][ch][lane] = in ? img[3 * g + ch] : 0.f;
+    if (shifted && in && shifted[g] < 0) inv |= 1u << i;
+  }
+  __syncwarp();
+  unsigned pend = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+    if (lab[i] >= 0 && lab[i] < cap) pend |= 1u << i;
+  for (;;) {
+    const unsigned any = __ballot_sync(0xffffffffu, pend != 0);
+    if (!any) break;
+    const int src = __ffs(any) - 1;
+    int first = -1;
+#pragma unroll
+    for (int i = 7; i >= 0; i--)
+      if ((pend >> i) & 1u) first = lab[i];
+    const int k = __shfl_sync(0xffffffffu, first, src);
+    unsigned m = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) m |= (unsigned)(lab[i] == k) << i;
+    pend &= ~m;
+    long long s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+    for (unsigned mm = m; mm; mm &= mm - 1) {
+      const int i = __ffs(mm) - 1;
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) {
+        const float v = cw[i][ch][lane];
+        s[ch] += fx_q(v, kFxAppShift);
+        q[ch] += fx_q(v * v, kFxSqShift);
       }
-      if (shrow && shrow[x] < 0) ninv++;
+    }
+    const int N = __reduce_add_sync(0xffffffffu, __popc(m));
+    const int NI = shifted ? __reduce_add_sync(0xffffffffu, __popc(m & inv)) : 0;
+    long long St[3], Qt[3];
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) { St[ch] = warp_sum64(s[ch]); Qt[ch] = warp_sum64(q[ch]); }
+    if (lane == src) {
+      atomicAdd(&sm.count[k], N);
+      if (NI) atomicAdd(&sm.ninvalid[k], NI);
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) {
+        atomicAdd((unsigned long long*)&sm.s[3 * (size_t)k + ch], (unsigned long long)St[ch]);
+        atomicAdd((unsigned long long*)&sm.sq[3 * (size_t)k + ch], (unsigned long long)Qt[ch]);
+      }
     }
   }
-  flush();
 }
 
 // Marginal of one superpixel over the three colour channels, FP64: the

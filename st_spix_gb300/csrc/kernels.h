@@ -70,7 +70,7 @@ __global__ void kb_split_begin(const Slot* slots, int B);
 __global__ void kb_split_clear(const Slot* slots);
 __global__ void kb_split_seed(const Slot* slots, int dir_bass, int dir_prop);
 __global__ void kb_bbox(const Slot* slots);
-__global__ void kb_split_bfs(const Slot* slots);
+__global__ void kb_split_bfs(const Slot* slots, int dir_bass, int dir_prop);
 __global__ void kb_split_bfs_big(const Slot* slots);
 __global__ void kb_split_partition(const Slot* slots);
 __global__ void kb_sm_clear(const Slot* slots);
@@ -99,7 +99,7 @@ __global__ void kb_fill_split(const Slot* slots, int pass);
 __global__ void kb_fill_phase(const Slot* slots, int ph, int B, cudaGraphConditionalHandle cond,
                               int break_iter, int* body_iters, unsigned* ctr);
 __global__ void kb_fill_end(const Slot* slots);
-__global__ void kb_cc_init(const Slot* slots);
+__global__ void kb_cc_local(const Slot* slots);
 __global__ void kb_cc_hook(const Slot* slots);
 __global__ void kb_cc_compress(const Slot* slots);
 __global__ void kb_list_holes(const Slot* slots);
