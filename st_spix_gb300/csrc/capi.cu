@@ -73,7 +73,6 @@ struct List {
   Slot* d = nullptr;               // device table
   int B = 0;
   int max_npix = 0, max_cap = 0, max_nprev = 0, max_w = 0, max_h = 0;
-  long long max_acc = 0, max_sm = 0;
   bool any_prop = false;
   std::vector<int> tiles_upto[3];  // sweep tiles (32-, 64-, 16-wide) of the first i slots
   std::vector<long long> segs_upto;  // 32-pixel row segments of the first i slots
@@ -473,7 +472,6 @@ void preload_kernels() {
       (const void*)kb_cc_hook,
       (const void*)kb_cc_compress,
       (const void*)kb_list_holes,
-      (const void*)kb_cc_size,
       (const void*)kb_cc_best,
       (const void*)kb_cc_invalidate,
       (const void*)kb_shift_params,
@@ -616,8 +614,6 @@ List make_list(stspix_ctx* ctx, int off, const std::vector<Slot>& slots) {
     if (s.mode) L.max_nprev = std::max(L.max_nprev, (s.cap - 2) / 10);
     L.max_w = std::max(L.max_w, s.W);
     L.max_h = std::max(L.max_h, s.H);
-    L.max_acc = std::max(L.max_acc, (long long)s.H * ((s.W + 7) / 8));
-    L.max_sm = std::max(L.max_sm, (long long)s.H * ((s.W + 15) / 16));
     if (s.mode) L.any_prop = true;
   }
   return L;
@@ -659,7 +655,11 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   }
   if (ctx->accumulator) accumulate_fp(ctx, st, L, nb, ctx->accumulator);
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
-  LAUNCHG(kb_posterior, dim3((unsigned)((L.max_cap + 31) / 32), (unsigned)nb), 128, L.d);
+  // id groups of 32 per block, about four blocks per SM over the batch (a block loops
+  // when a slot has more groups in use)
+  const unsigned pg = (unsigned)std::min<long long>((L.max_cap + 31) / 32,
+                                                    std::max(32, (4 * ctx->num_sms + nb - 1) / nb));
+  LAUNCHG(kb_posterior, dim3(pg, (unsigned)nb), 128, L.d);
   return STSPIX_OK;
 }
 
@@ -862,7 +862,7 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
   LAUNCHS(kb_split_begin, L, nb);
   LAUNCHB(kb_split_clear, L.max_npix, L, nb);
   LAUNCHB(kb_split_seed, L.max_cap, L, nb, dir_b, dir_p);
-  LAUNCHG(kb_bbox, dim3(blocks_for(L.max_sm), (unsigned)nb), kThreads, L.d);
+  LAUNCHG(kb_bbox, dim3(tiles64(L), (unsigned)nb), kThreads, L.d);
   LAUNCHG(kb_split_bfs, dim3(256, (unsigned)nb), 128, L.d, dir_b, dir_p);  // 1024 warps per slot
   {
     cudaEvent_t pe_ = prof_begin(ctx, st);
@@ -888,10 +888,9 @@ int run_relabel(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   ctx->cur_fam = STSPIX_FAM_MERGE;
   LAUNCHB(kb_relabel_init, L.max_cap + 2, L, nb);
   LAUNCHB(kb_living, L.max_npix, L, nb);
-  const int chunk = 256;
-  dim3 g(blocks_for(L.max_cap), (unsigned)std::max(1, (L.max_nprev + chunk - 1) / chunk),
-         (unsigned)nb);
-  LAUNCHG(kb_relabel_compare, g, kThreads, L.d, chunk);
+  dim3 g(blocks_for(L.max_cap),
+         (unsigned)std::max(1, (L.max_nprev + kRelabelChunk - 1) / kRelabelChunk), (unsigned)nb);
+  LAUNCHG(kb_relabel_compare, g, kThreads, L.d);
   LAUNCHB(kb_relabel_mark, L.max_cap, L, nb, cfg.thresh_relabel, cfg.thresh_new);
   LAUNCHG(kb_scan, (unsigned)nb, 1024, L.d, 2);
   LAUNCHB(kb_relabel_ids, L.max_cap, L, nb);
@@ -1160,23 +1159,22 @@ int shift_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   int r;
   ctx->cur_fam = STSPIX_FAM_PROP;
   LAUNCHB(kb_prop_clear, std::max<long long>(L.max_npix, L.max_nprev), L, L.B);
-  LAUNCHG(kb_flow_pool, dim3(blocks_for(L.max_sm), (unsigned)L.B), kThreads, L.d);
+  LAUNCHG(kb_flow_pool, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d);
   LAUNCHB(kb_flow_mean, L.max_nprev, L, L.B);
   LAUNCHB(kb_shift, L.max_npix, L, L.B);
   LAUNCHB(kb_shift_decode, L.max_npix, L, L.B);
-  LAUNCHG(kb_count_labels, dim3(blocks_for(L.max_sm), (unsigned)L.B), kThreads, L.d, 0);
+  LAUNCHG(kb_count_labels, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d, 0);
   // fill, invalidate disconnected, fill
   if ((r = run_fill(ctx, st, L))) return r;
   LAUNCHG(kb_cc_local, dim3((unsigned)(((L.max_w + 31) / 32) * ((L.max_h + 31) / 32)), (unsigned)L.B),
           kThreads, L.d);
   LAUNCHB(kb_cc_hook, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_compress, L.max_npix, L, L.B);
-  LAUNCHB(kb_cc_size, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_best, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_invalidate, L.max_npix, L, L.B);
   LAUNCHB(kb_list_holes, L.max_npix, L, L.B);
   if ((r = run_fill(ctx, st, L))) return r;
-  LAUNCHG(kb_count_labels, dim3(blocks_for(L.max_sm), (unsigned)L.B), kThreads, L.d, 1);
+  LAUNCHG(kb_count_labels, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d, 1);
   LAUNCHB(kb_shift_params, L.max_nprev, L, L.B);
   return STSPIX_OK;
 }

@@ -32,6 +32,7 @@ constexpr int kMaxBatchGraphs = 64;       // captured batch steps kept per conte
 constexpr float kWideMargin = 1.05f;      // large batches: 64x32 unless 5 % slower
 constexpr int kPairMaxTiles = 2048;       // two-sweep launches only below this many 32x32 tiles
 constexpr int kSweepTileW[kSweepVariants] = {32, 64, 16};
+constexpr int kRelabelChunk = 64;         // previous superpixels per relabel-compare block
 
 // Packed record read by the boundary sweep: the fields calc_joint reads
 // (update_seg.cu:194-259), already converted to the types it uses.  The reference
@@ -46,9 +47,14 @@ struct __align__(16) SweepRec {
   float isx, isy, isz, pad;        // (float) inverse shape covariance
 };
 
-// Per-superpixel kernels spread consecutive ids over blocks (live ids are the low
-// ones, and the FP64 work per id is heavy on this part): id = block + grid * j.
-__device__ __forceinline__ int spread_id(int j) { return blockIdx.x + gridDim.x * j; }
+// Per-superpixel kernels with FP64 work: live ids are the low ones, and this part issues
+// FP64 slowly, at a cost per warp instruction whatever its active lanes.  So a warp takes
+// 32 consecutive ids (full lanes) and consecutive groups of 32 go to different blocks
+// (different SMs): thread j of block b takes id 32 (b + grid (j / 32)) + j % 32.  The id
+// grows with j, so the loop ends at the first id >= n.
+__device__ __forceinline__ int spread_id(int j) {
+  return (blockIdx.x + gridDim.x * (j >> 5)) * 32 + (j & 31);
+}
 #define FOR_SP(k, n)                                                              \
   for (int j_ = threadIdx.x, k = spread_id(j_); k < (n); j_ += blockDim.x, k = spread_id(j_))
 
@@ -191,6 +197,56 @@ __device__ __forceinline__ long long warp_sum64(long long v) {
   const int hi = (int)(v >> 24);
   return (long long)__reduce_add_sync(0xffffffffu, hi) * (1LL << 24) +
          (long long)__reduce_add_sync(0xffffffffu, lo);
+}
+
+// Full-warp sum of 32-bit unsigned values (any value per lane): hi = v >> 24 < 2^8 and
+// lo < 2^24 summed separately.
+__device__ __forceinline__ long long warp_sum_u32(unsigned v) {
+  return (long long)__reduce_add_sync(0xffffffffu, v >> 24) * (1LL << 24) +
+         (long long)__reduce_add_sync(0xffffffffu, v & 0xFFFFFFu);
+}
+// Colours in [0, 1] (the usual RGB input): their 2^28 fixed point is one conversion and
+// fits 32 bits, and so does a lane's sum of 8 (< 2^31); squares at 2^20 likewise, and a
+// warp's sum of 256 of those (< 2^29) fits one 32-bit reduction.
+__device__ __forceinline__ bool unit_colour(float v) { return v >= 0.f && v <= 1.f; }
+__device__ __forceinline__ unsigned fx_unit(float v, int shift) {
+  return __float2uint_rn(v * (float)(1u << shift));     // fx_q(v, shift) for v in [0, 1]
+}
+
+// Warp-block label sums.  A warp owns a 32 x 8 block of a frame, lane l its column l,
+// lab[i] the label of row i.  The warp takes the block's labels one at a time (the label
+// of the lowest lane with rows pending) and calls body(k, m, src) on every lane: m = the
+// lane's rows of label k, src = the lane that adds the warp's totals to the global sums.
+// pend = the rows to take (labels in range).  A block holds a few labels, so a few warp
+// reductions and one set of atomics per label serve its 256 pixels.
+template <typename Body>
+__device__ __forceinline__ void label_rounds(const int (&lab)[8], unsigned pend, Body body) {
+  for (;;) {
+    const unsigned any = __ballot_sync(0xffffffffu, pend != 0);
+    if (!any) break;
+    const int src = __ffs(any) - 1;
+    int first = -1;
+#pragma unroll
+    for (int i = 7; i >= 0; i--)
+      if ((pend >> i) & 1u) first = lab[i];
+    const int k = __shfl_sync(0xffffffffu, first, src);
+    unsigned m = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) m |= (unsigned)(lab[i] == k) << i;
+    pend &= ~m;
+    body(k, m, src);
+  }
+}
+
+// The 32 x 8 block of warp w of a block of the 64 x 32 tile grid of a W-wide frame:
+// its lane's column gx and first row by.  False for blocks past the frame's tiles.
+__device__ __forceinline__ bool warp_block(int W, int H, int& gx, int& by) {
+  const int tiles_x = (W + 63) / 64;
+  if ((int)blockIdx.x >= tiles_x * ((H + 31) / 32)) return false;
+  const int warp = threadIdx.x >> 5;
+  gx = (blockIdx.x % tiles_x) * 64 + (warp & 1) * 32 + (threadIdx.x & 31);
+  by = (blockIdx.x / tiles_x) * 32 + (warp >> 1) * 8;
+  return true;
 }
 
 }  // namespace stspix

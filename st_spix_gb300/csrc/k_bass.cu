@@ -255,7 +255,8 @@ __global__ void kb_init_prior_mu(const Slot* __restrict__ slots) {
 // scatter this replaces, with a set of atomics per run of a 32-pixel row, took 50 us
 // per 8-frame 480x854 batch against 43 us here).  Integer sums: the totals do not
 // depend on the grouping or the order of the adds.
-__device__ __forceinline__ void block_stats(const Slot& S, int bx, int by) {
+// cw: the warp's shared staging rows (colours other than unit ones).
+__device__ __forceinline__ void block_stats(const Slot& S, int bx, int by, float (*cw)[3][32]) {
   const int lane = threadIdx.x & 31;
   const int H = S.H, W = S.W;
   const SpDev& sp = S.sp;
@@ -263,6 +264,8 @@ __device__ __forceinline__ void block_stats(const Slot& S, int bx, int by) {
   const int gx = bx + lane;
   int lab[8];
   float c[8][3];
+  unsigned pend = 0;
+  bool unit = true;
 #pragma unroll
   for (int i = 0; i < 8; i++) {
     const int gy = by + i;
@@ -270,38 +273,19 @@ __device__ __forceinline__ void block_stats(const Slot& S, int bx, int by) {
     const size_t g = (size_t)gy * W + gx;
     lab[i] = in ? S.seg[g] : -1;
 #pragma unroll
-    for (int ch = 0; ch < 3; ch++) c[i][ch] = in ? S.img[3 * g + ch] : 0.f;
-  }
-  long long q[8][3];
-  unsigned pend = 0;
-#pragma unroll
-  for (int i = 0; i < 8; i++) {
-#pragma unroll
-    for (int ch = 0; ch < 3; ch++) q[i][ch] = fx_q(c[i][ch], kFxAppShift);
+    for (int ch = 0; ch < 3; ch++) {
+      c[i][ch] = in ? S.img[3 * g + ch] : 0.f;
+      unit &= unit_colour(c[i][ch]);
+    }
     if (lab[i] >= 0 && lab[i] < cap) pend |= 1u << i;
   }
-  for (;;) {
-    const unsigned any = __ballot_sync(0xffffffffu, pend != 0);
-    if (!any) break;
-    const int src = __ffs(any) - 1;
-    int first = -1;
-#pragma unroll
-    for (int i = 7; i >= 0; i--)
-      if ((pend >> i) & 1u) first = lab[i];
-    const int k = __shfl_sync(0xffffffffu, first, src);
-    unsigned m = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) m |= (unsigned)(lab[i] == k) << i;
-    pend &= ~m;              // every pixel of label k of this column is taken now
-    long long s0 = 0, s1 = 0, s2 = 0;
+  // the warp's totals of label k given its colour sums: count and position moments
+  // (relative to the block, so they fit 32 bits), one set of atomics
+  auto add = [&](int k, unsigned m, int src, long long S0, long long S1, long long S2) {
     int sy = 0, syy = 0;
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-      if ((m >> i) & 1u) {
-        s0 += q[i][0]; s1 += q[i][1]; s2 += q[i][2];
-        sy += i; syy += i * i;
-      }
-    }
+    for (int i = 0; i < 8; i++)
+      if ((m >> i) & 1u) { sy += i; syy += i * i; }
     const int n = __popc(m);
     const int N = __reduce_add_sync(0xffffffffu, n);
     const int SX = __reduce_add_sync(0xffffffffu, n * lane);
@@ -309,7 +293,6 @@ __device__ __forceinline__ void block_stats(const Slot& S, int bx, int by) {
     const int SY = __reduce_add_sync(0xffffffffu, sy);
     const int SYY = __reduce_add_sync(0xffffffffu, syy);
     const int SXY = __reduce_add_sync(0xffffffffu, lane * sy);
-    const long long S0 = warp_sum64(s0), S1 = warp_sum64(s1), S2 = warp_sum64(s2);
     if (lane == src) {
       const long long ln = N, X = bx, Y = by;
       unsigned long long* acc = (unsigned long long*)(sp.acc + 8 * (size_t)k);
@@ -323,7 +306,39 @@ __device__ __forceinline__ void block_stats(const Slot& S, int bx, int by) {
       atomicAdd(acc + 6, (unsigned long long)(ln * X * Y + X * SY + Y * SX + SXY));
       atomicAdd(acc + 7, (unsigned long long)(ln * Y * Y + 2 * Y * SY + SYY));
     }
+  };
+  if (__all_sync(0xffffffffu, unit)) {
+    unsigned q[8][3];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) q[i][ch] = fx_unit(c[i][ch], kFxAppShift);
+    label_rounds(lab, pend, [&](int k, unsigned m, int src) {
+      unsigned s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        if ((m >> i) & 1u) { s0 += q[i][0]; s1 += q[i][1]; s2 += q[i][2]; }
+      add(k, m, src, warp_sum_u32(s0), warp_sum_u32(s1), warp_sum_u32(s2));
+    });
+    return;
   }
+  // other colours: 64-bit sums, the colours wait in shared memory and a lane converts
+  // each of its pixels in the round of its label
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) cw[i][ch][lane] = c[i][ch];
+  __syncwarp();
+  label_rounds(lab, pend, [&](int k, unsigned m, int src) {
+    long long s0 = 0, s1 = 0, s2 = 0;
+    for (unsigned mm = m; mm; mm &= mm - 1) {
+      const int i = __ffs(mm) - 1;
+      s0 += fx_q(cw[i][0][lane], kFxAppShift);
+      s1 += fx_q(cw[i][1][lane], kFxAppShift);
+      s2 += fx_q(cw[i][2][lane], kFxAppShift);
+    }
+    add(k, m, src, warp_sum64(s0), warp_sum64(s1), warp_sum64(s2));
+  });
 }
 
 // Grid: the 64 x 32 tiles of the first B slots (a block finds its slot by binary
@@ -342,7 +357,9 @@ __global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ sl
   const int tl = t - S.tile_base[1];
   const int tiles_x = (S.W + 63) / 64;
   const int warp = threadIdx.x >> 5;
-  block_stats(S, (tl % tiles_x) * 64 + (warp & 1) * 32, (tl / tiles_x) * 32 + (warp >> 1) * 8);
+  __shared__ float cs[8][8][3][32];   // [warp][row][channel][lane]
+  block_stats(S, (tl % tiles_x) * 64 + (warp & 1) * 32, (tl / tiles_x) * 32 + (warp >> 1) * 8,
+              cs[warp]);
 }
 
 // Accumulator precision study: colour sums by per-pixel FP32 (mode 1, as the
@@ -448,18 +465,12 @@ __device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in
 // mean and scatter; then warps 0-2 one smoothed covariance entry each, then warps 0-2
 // one inverse entry each and warp 3 the log determinant.  Every value is the same
 // expression as a single-thread evaluation, exchanged through shared memory.
-__global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slots) {
-  pdl_enter();
-  SLOT_Y;
-  // ids above the largest in use were never live in this frame: their fields still hold
-  // the zeros the frame's set-up wrote (kb_init_bass_params, kb_write_params), which is
-  // what this kernel would write for them
-  if ((int)blockIdx.x * 32 > S.sc->max_spix) return;
+__device__ __forceinline__ void posterior_ids(const Slot& S, int k0) {
   __shared__ double v_ps[3][32], v_raw[3][32], v_m[2][32], v_s[3][32], v_i[4][32];
   __shared__ float v_app[3][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const SpDev& sp = S.sp;
-  const int k = blockIdx.x * 32 + lane;
+  const int k = k0 + lane;
   const bool inr = k < sp.cap;
   // every load of the id is issued before any is used (one memory round trip): the
   // count and flags, and the fields this warp's part of the posterior reads
@@ -559,6 +570,19 @@ __global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slo
     r.count = count_int;
     sp.rec[k] = r;
   }
+}
+
+// Grid: x blocks per slot, each taking the slot's 32-id groups x, x + gridDim.x, ...
+// up to the largest id in use.  Ids above it were never live in this frame: their
+// fields still hold the zeros the frame's set-up wrote (kb_init_bass_params,
+// kb_write_params), which is what the posterior would write for them.  A group's
+// barriers are block-uniform, and the first barrier of the next group follows every
+// read of the previous one's shared values.
+__global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slots) {
+  pdl_enter();
+  SLOT_Y;
+  const int last = min(S.sp.cap - 1, S.sc->max_spix);
+  for (int g = blockIdx.x; g * 32 <= last; g += gridDim.x) posterior_ids(S, g * 32);
 }
 
 // clear_fields + the helper memset (update_params.cu:54-88, :26): zero the counts

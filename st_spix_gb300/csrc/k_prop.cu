@@ -10,9 +10,6 @@
 namespace stspix {
 
 // ---------------------------------------------------------------------------
-// Mean flow per superpixel (sp_downsample_kernel / normz_downsample_kernel,
-// sp_pooling.cu:27-71), R1 fixed point.  Runs of equal labels in a row are
-// aggregated before the atomics.
 // Clear the per-previous-superpixel sums and the warp targets of every slot.
 __global__ void kb_prop_clear(const Slot* __restrict__ slots) {
   pdl_enter();
@@ -34,39 +31,44 @@ __global__ void kb_prop_clear(const Slot* __restrict__ slots) {
   if (i == 0) { S.sc->ninvalid = 0; S.sc->nhole = 0; }
 }
 
-__global__ void kb_flow_pool(const Slot* __restrict__ slots) {
+// Mean flow per superpixel (sp_downsample_kernel / normz_downsample_kernel,
+// sp_pooling.cu:27-71), R1 fixed point: pixel counts and flow sums of the previous
+// labels by warp-block label rounds.
+__global__ void __launch_bounds__(256) kb_flow_pool(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  const int* __restrict__ lab = S.prev_labels;
-  const float* __restrict__ flow = S.flow;
   const int H = S.H, W = S.W, n = S.n_prev;
-  int* __restrict__ cnt = S.cnt_pool;
-  long long* __restrict__ fs = S.fs;
-  constexpr int R = 16;
-  const int cpr = (W + R - 1) / R;
-  int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= H * cpr) return;
-  int y = tid / cpr, xs = (tid % cpr) * R, xe = min(W, xs + R);
-  const int* lrow = lab + (size_t)y * W;
-  const float* frow = flow + (size_t)y * W * 2;
-  int cur = -1, c = 0;
-  long long sx = 0, sy = 0;
-  for (int x = xs; x <= xe; x++) {
-    int k = x < xe ? lrow[x] : -2;
-    if (k != cur) {
-      if (cur >= 0 && cur < n) {
-        atomicAdd(&cnt[cur], c);
-        atomicAdd((unsigned long long*)&fs[2 * (size_t)cur], (unsigned long long)sx);
-        atomicAdd((unsigned long long*)&fs[2 * (size_t)cur + 1], (unsigned long long)sy);
-      }
-      cur = k; c = 0; sx = sy = 0;
-    }
-    if (x < xe && k >= 0) {
-      c++;
-      sx += fx_q(frow[2 * x], kFxFlowShift);
-      sy += fx_q(frow[2 * x + 1], kFxFlowShift);
-    }
+  int gx, by;
+  if (!warp_block(W, H, gx, by)) return;
+  const int lane = threadIdx.x & 31;
+  const int* __restrict__ lab_prev = S.prev_labels;
+  const float* __restrict__ flow = S.flow;
+  int lab[8];
+  long long qx[8], qy[8];
+  unsigned pend = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int gy = by + i;
+    const bool in = gx < W && gy < H;
+    const size_t g = (size_t)gy * W + gx;
+    lab[i] = in ? lab_prev[g] : -1;
+    qx[i] = in ? fx_q(flow[2 * g], kFxFlowShift) : 0;
+    qy[i] = in ? fx_q(flow[2 * g + 1], kFxFlowShift) : 0;
+    if (lab[i] >= 0 && lab[i] < n) pend |= 1u << i;
   }
+  label_rounds(lab, pend, [&](int k, unsigned m, int src) {
+    long long sx = 0, sy = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+      if ((m >> i) & 1u) { sx += qx[i]; sy += qy[i]; }
+    const int N = __reduce_add_sync(0xffffffffu, __popc(m));
+    const long long SX = warp_sum64(sx), SY = warp_sum64(sy);
+    if (lane == src) {
+      atomicAdd(&S.cnt_pool[k], N);
+      atomicAdd((unsigned long long*)&S.fs[2 * (size_t)k], (unsigned long long)SX);
+      atomicAdd((unsigned long long*)&S.fs[2 * (size_t)k + 1], (unsigned long long)SY);
+    }
+  });
 }
 
 // normz + centres = mu_shape + mean flow (shift_and_fill.cu:140-150).
@@ -116,64 +118,64 @@ __global__ void kb_shift(const Slot* __restrict__ slots) {
 
 // decode_kernel (shift_labels.cu:128-164) + copy to `filled` + hole count.
 // Append pixel t to the slot's hole list (smseg, count sc->nhole) when `hole`;
-// warp-aggregated.  The list order depends on scheduling; the fill's result does
-// not (a parity phase updates pixels that are never 4-neighbours of each other).
-// With count_invalid the holes are also counted into sc->ninvalid (the hole count
-// after the shift, which the iteration ladder reads).
+// block-aggregated: one atomic per block (every thread of the block calls it).  The
+// list order depends on scheduling; the fill's result does not (a parity phase updates
+// pixels that are never 4-neighbours of each other).  With count_invalid the holes are
+// also counted into sc->ninvalid (the hole count after the shift, which the iteration
+// ladder reads).
 __device__ __forceinline__ void append_hole(const Slot& S, int t, bool hole, bool count_invalid) {
-  const unsigned act = __activemask();
-  const unsigned m = __ballot_sync(act, hole);
-  if (!m) return;
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(m) - 1;
-  int base = 0;
-  if (lane == leader) {
-    base = atomicAdd(&S.sc->nhole, __popc(m));
-    if (count_invalid) atomicAdd(&S.sc->ninvalid, __popc(m));
+  __shared__ int woff[32];
+  __shared__ int base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned m = __ballot_sync(0xffffffffu, hole);
+  if (lane == 0) woff[warp] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) { const int c = woff[w]; woff[w] = tot; tot += c; }
+    base = tot ? atomicAdd(&S.sc->nhole, tot) : 0;
+    if (tot && count_invalid) atomicAdd(&S.sc->ninvalid, tot);
   }
-  base = __shfl_sync(act, base, leader);
-  if (hole) S.smseg[base + __popc(m & ((1u << lane) - 1))] = t;
+  __syncthreads();
+  if (hole) S.smseg[base + woff[warp] + __popc(m & ((1u << lane) - 1))] = t;
 }
 
 __global__ void kb_shift_decode(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  const int* __restrict__ hits = S.hits;
-  const unsigned long long* __restrict__ best = S.best;
-  int* __restrict__ shifted = S.shifted;
-  int* __restrict__ filled = S.seg;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int v = hits[t] > 0 ? (int)(unsigned int)best[t] : -1;
-  shifted[t] = v;
-  filled[t] = v;
-  append_hole(S, t, v < 0, true);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int)(blockIdx.x * blockDim.x) >= S.npix) return;   // block-uniform
+  const bool in = t < S.npix;
+  int v = -1;
+  if (in) {
+    v = S.hits[t] > 0 ? (int)(unsigned int)S.best[t] : -1;
+    S.shifted[t] = v;
+    S.seg[t] = v;
+  }
+  append_hole(S, t, in && v < 0, true);
 }
 
-// Per-label pixel counts (get_spix_sizes, seg_utils.cu:56-75).
-// which 0: counts after the shift (cs), 1: after the fill (cf).  One 16-pixel
-// row run per thread; runs of equal labels are counted before the atomic.
-__global__ void kb_count_labels(const Slot* __restrict__ slots, int which) {
+// Per-label pixel counts (get_spix_sizes, seg_utils.cu:56-75), by warp-block label
+// rounds.  which 0: counts after the shift (cs), 1: after the fill (cf).
+__global__ void __launch_bounds__(256) kb_count_labels(const Slot* __restrict__ slots, int which) {
   pdl_enter();
   SLOT_Y;
-  constexpr int R = 16;
-  const int W = S.W, n = S.n_prev;
-  const int cpr = (W + R - 1) / R;
-  int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= S.H * cpr) return;
-  int y = tid / cpr, xs = (tid % cpr) * R, xe = min(W, xs + R);
-  const int* lrow = S.seg + (size_t)y * W;
+  const int H = S.H, W = S.W, n = S.n_prev;
+  int gx, by;
+  if (!warp_block(W, H, gx, by)) return;
   int* cnt = which ? S.cf : S.cs;
-  int cur = -1, c = 0;
-  for (int x = xs; x <= xe; x++) {
-    int k = x < xe ? lrow[x] : -2;
-    if (k != cur) {
-      if (cur >= 0 && cur < n) atomicAdd(&cnt[cur], c);
-      cur = k;
-      c = 0;
-    }
-    c++;
+  int lab[8];
+  unsigned pend = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int gy = by + i;
+    lab[i] = (gx < W && gy < H) ? S.seg[(size_t)gy * W + gx] : -1;
+    if (lab[i] >= 0 && lab[i] < n) pend |= 1u << i;
   }
+  label_rounds(lab, pend, [&](int k, unsigned m, int src) {
+    const int N = __reduce_add_sync(0xffffffffu, __popc(m));
+    if ((int)(threadIdx.x & 31) == src) atomicAdd(&cnt[k], N);
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -500,21 +502,19 @@ __global__ void kb_cc_hook(const Slot* __restrict__ slots) {
   if (!ok) atomicExch(&S.sc->status, STSPIX_ERR_ITER_LIMIT);
 }
 
+// Every pixel's parent := its root, and the component sizes: the lanes of a warp with
+// the same root (a warp's pixels are consecutive, so few roots) add their count once.
 __global__ void kb_cc_compress(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  if (S.d1[t] >= 0) S.d1[t] = uf_find(S.d1, t);
-}
-
-__global__ void kb_cc_size(const Slot* __restrict__ slots) {
-  pdl_enter();
-  SLOT_Y;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int r = S.d1[t];
-  if (r >= 0) atomicAdd(&S.d2[r], 1);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int r = -1;
+  if (t < S.npix && S.d1[t] >= 0) {
+    r = uf_find(S.d1, t);
+    S.d1[t] = r;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, r);
+  if (r >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&S.d2[r], __popc(peers));
 }
 
 __global__ void kb_cc_best(const Slot* __restrict__ slots) {
@@ -553,9 +553,9 @@ __global__ void kb_cc_invalidate(const Slot* __restrict__ slots) {
 __global__ void kb_list_holes(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  append_hole(S, t, S.seg[t] < 0, false);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int)(blockIdx.x * blockDim.x) >= S.npix) return;   // block-uniform
+  append_hole(S, t, t < S.npix && S.seg[t] < 0, false);
 }
 
 // invalid_counts / prior_counts update (shift_and_fill.cu:300-330).
@@ -664,39 +664,50 @@ __global__ void kb_living(const Slot* __restrict__ slots) {
   if (v >= 0 && v <= S.sc->max_spix) S.living[v] = 1;
 }
 
-// find_most_similar_spix (relabel.cu:201-276): grid (s, candidate chunk).
-__global__ void kb_relabel_compare(const Slot* __restrict__ slots, int chunk) {
+// find_most_similar_spix (relabel.cu:201-276): grid (s, candidate chunk of
+// kRelabelChunk previous superpixels).  A block stages its chunk's prior colours and
+// skip flags in shared memory, then every thread scans the chunk for its s.
+__global__ void kb_relabel_compare(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Z;
   if (!S.mode) return;
   const SpDev& sp = S.sp;
-  const float* __restrict__ prev_prior_mu_app = S.pprev.prior_mu_app;
   const int n_prev = S.n_prev;
-  const Scalars* __restrict__ sc = S.sc;
+  const int c0 = blockIdx.y * kRelabelChunk;
+  if (c0 >= n_prev) return;
+  const int nspix = S.sc->max_spix + 1;
+  if ((int)(blockIdx.x * blockDim.x) >= min(nspix, sp.cap)) return;   // block-uniform
   const uint8_t* __restrict__ living = S.living;
-  unsigned long long* __restrict__ best = S.rbest;
-  float* __restrict__ ss = S.ss;
-  if ((int)blockIdx.y * chunk >= n_prev) return;
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nspix = sc->max_spix + 1;
+  const float* __restrict__ prev_prior_mu_app = S.pprev.prior_mu_app;
+  __shared__ float cmu[3][kRelabelChunk];
+  __shared__ uint8_t cskip[kRelabelChunk];
+  const int nc = min(n_prev - c0, kRelabelChunk);
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    const int c = c0 + i;
+    cskip[i] = c < nspix && living[c];
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) cmu[ch][i] = prev_prior_mu_app[3 * c + ch];
+  }
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nspix || s >= sp.cap || !living[s]) return;
-  int c0 = blockIdx.y * chunk, c1 = min(n_prev, c0 + chunk);
   const float mx = sp.mu_app[3 * s], my = sp.mu_app[3 * s + 1], mz = sp.mu_app[3 * s + 2];
   unsigned long long b = ~0ull;
-  for (int c = c0; c < c1; c++) {
-    bool same = (c == s);
-    if (c < nspix && living[c] && !same) continue;
-    float dx = mx - prev_prior_mu_app[3 * c];
-    float dy = my - prev_prior_mu_app[3 * c + 1];
-    float dz = mz - prev_prior_mu_app[3 * c + 2];
-    float delta = (dx * dx + dy * dy + dz * dz);
-    if (same) ss[s] = delta;
+  for (int i = 0; i < nc; i++) {
+    const int c = c0 + i;
+    const bool same = (c == s);
+    if (cskip[i] && !same) continue;
+    const float dx = mx - cmu[0][i];
+    const float dy = my - cmu[1][i];
+    const float dz = mz - cmu[2][i];
+    const float delta = (dx * dx + dy * dy + dz * dz);
+    if (same) S.ss[s] = delta;
     if (delta < 10000.f) {
-      unsigned long long key = ((unsigned long long)__float_as_uint(delta) << 32) | (unsigned)c;
+      const unsigned long long key = ((unsigned long long)__float_as_uint(delta) << 32) | (unsigned)c;
       if (key < b) b = key;
     }
   }
-  if (b != ~0ull) atomicMin(&best[s], b);
+  if (b != ~0ull) atomicMin(&S.rbest[s], b);
 }
 
 // mark_for_relabel (relabel.cu:126-192): revive flags and mint flags.

@@ -63,34 +63,37 @@ __global__ void kb_split_begin(const Slot* __restrict__ slots, int B) {
 }
 
 // ---------------------------------------------------------------------------
-// Bounding box of every superpixel (for the split BFS), one 16-pixel row run per
-// thread.
-__global__ void kb_bbox(const Slot* __restrict__ slots) {
+// Bounding box of every superpixel (for the split BFS), by warp-block label rounds:
+// a label's columns in the block are the lanes that hold it, its rows the union of
+// their row masks; one set of min / max atomics per (block, label).
+__global__ void __launch_bounds__(256) kb_bbox(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
   if (!S.sc->tmp0) return;
-  constexpr int R = 16;
-  const int W = S.W, cap = S.cap;
-  const int cpr = (W + R - 1) / R;
-  int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= S.H * cpr) return;
-  int y = tid / cpr, xs = (tid % cpr) * R, xe = min(W, xs + R);
-  const int* lrow = S.seg + (size_t)y * W;
-  int cur = -1, x0 = xs;
-  for (int x = xs; x <= xe; x++) {
-    int k = x < xe ? lrow[x] : -2;
-    if (k != cur) {
-      if (cur >= 0 && cur < cap) {
-        int* bb = S.bbox + 4 * (size_t)cur;
-        atomicMin(&bb[0], x0);
-        atomicMax(&bb[1], x - 1);
-        atomicMin(&bb[2], y);
-        atomicMax(&bb[3], y);
-      }
-      cur = k;
-      x0 = x;
-    }
+  const int H = S.H, W = S.W, cap = S.cap;
+  int gx, by;
+  if (!warp_block(W, H, gx, by)) return;
+  const int lane = threadIdx.x & 31;
+  const int bx = gx - lane;
+  int lab[8];
+  unsigned pend = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int gy = by + i;
+    lab[i] = (gx < W && gy < H) ? S.seg[(size_t)gy * W + gx] : -1;
+    if (lab[i] >= 0 && lab[i] < cap) pend |= 1u << i;
   }
+  label_rounds(lab, pend, [&](int k, unsigned m, int src) {
+    const unsigned cols = __ballot_sync(0xffffffffu, m != 0);
+    const unsigned rows = __reduce_or_sync(0xffffffffu, m);
+    if (lane == src) {
+      int* bb = S.bbox + 4 * (size_t)k;
+      atomicMin(&bb[0], bx + __ffs(cols) - 1);
+      atomicMax(&bb[1], bx + 31 - __clz(cols));
+      atomicMin(&bb[2], by + __ffs(rows) - 1);
+      atomicMax(&bb[3], by + 31 - __clz(rows));
+    }
+  });
 }
 
 // Split BFS (calc_split_candidate, split_merge.cu:758-800): distances from the two
@@ -431,19 +434,17 @@ __global__ void kb_sm_clear(const Slot* __restrict__ slots) {
 // (w & 1, w >> 1), a lane one column of it.  The warp takes the block's labels one at a
 // time (the label of the lowest lane that still has pixels): each lane sums its pixels of
 // that label, full-warp reductions add the lanes' sums, and one lane adds the totals with
-// one set of atomics.  The colours wait in shared memory, so a lane converts each of its
-// pixels once, in the round of its label, and holds no 64-bit terms between rounds.
+// one set of atomics.  Unit colours (all of the warp's in [0, 1]) are summed in 32 bits;
+// other colours wait in shared memory and a lane converts each pixel in its label's round.
 // Integer sums (R1): totals do not depend on the grouping.
 __global__ void __launch_bounds__(256) kb_sm_accumulate(const Slot* __restrict__ slots, int split) {
   pdl_enter();
   SLOT_Y;
   __shared__ float cs[8][8][3][32];   // [warp][row][channel][lane]
   const int H = S.H, W = S.W;
-  const int tiles_x = (W + 63) / 64;
-  if ((int)blockIdx.x >= tiles_x * ((H + 31) / 32)) return;
+  int gx, by;
+  if (!warp_block(W, H, gx, by)) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gx = (blockIdx.x % tiles_x) * 64 + (warp & 1) * 32 + lane;
-  const int by = (blockIdx.x / tiles_x) * 32 + (warp >> 1) * 8;
   const int* __restrict__ labp = split ? S.smseg : S.seg;
   const int* __restrict__ shifted = (split && S.mode) ? S.shifted : nullptr;
   const float* __restrict__ img = S.img;
@@ -451,7 +452,9 @@ __global__ void __launch_bounds__(256) kb_sm_accumulate(const Slot* __restrict__
   const SmDev& sm = S.sm;
   float (*cw)[3][32] = cs[warp];
   int lab[8];
-  unsigned inv = 0;
+  float c[8][3];
+  unsigned inv = 0, pend = 0;
+  bool unit = true;
 #pragma unroll
   for (int i = 0; i < 8; i++) {
     const int gy = by + i;
@@ -459,27 +462,61 @@ __global__ void __launch_bounds__(256) kb_sm_accumulate(const Slot* __restrict__
     const size_t g = (size_t)gy * W + gx;
     lab[i] = in ? labp[g] : -1;
 #pragma unroll
-    for (int ch = 0; ch < 3; ch++) cw[i][ch][lane] = in ? img[3 * g + ch] : 0.f;
+    for (int ch = 0; ch < 3; ch++) {
+      c[i][ch] = in ? img[3 * g + ch] : 0.f;
+      unit &= unit_colour(c[i][ch]);
+    }
     if (shifted && in && shifted[g] < 0) inv |= 1u << i;
+    if (lab[i] >= 0 && lab[i] < cap) pend |= 1u << i;
   }
-  __syncwarp();
-  unsigned pend = 0;
+  auto add = [&](int k, unsigned m, int src, const long long (&St)[3], const long long (&Qt)[3]) {
+    const int N = __reduce_add_sync(0xffffffffu, __popc(m));
+    const int NI = shifted ? __reduce_add_sync(0xffffffffu, __popc(m & inv)) : 0;
+    if (lane == src) {
+      atomicAdd(&sm.count[k], N);
+      if (NI) atomicAdd(&sm.ninvalid[k], NI);
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) {
+        atomicAdd((unsigned long long*)&sm.s[3 * (size_t)k + ch], (unsigned long long)St[ch]);
+        atomicAdd((unsigned long long*)&sm.sq[3 * (size_t)k + ch], (unsigned long long)Qt[ch]);
+      }
+    }
+  };
+  if (__all_sync(0xffffffffu, unit)) {
+    unsigned qs[8][3], qq[8][3];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) {
+        qs[i][ch] = fx_unit(c[i][ch], kFxAppShift);
+        qq[i][ch] = fx_unit(c[i][ch] * c[i][ch], kFxSqShift);
+      }
+    label_rounds(lab, pend, [&](int k, unsigned m, int src) {
+      unsigned s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        if ((m >> i) & 1u) {
+#pragma unroll
+          for (int ch = 0; ch < 3; ch++) { s[ch] += qs[i][ch]; q[ch] += qq[i][ch]; }
+        }
+      long long St[3], Qt[3];
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) {
+        St[ch] = warp_sum_u32(s[ch]);
+        Qt[ch] = (long long)__reduce_add_sync(0xffffffffu, q[ch]);
+      }
+      add(k, m, src, St, Qt);
+    });
+    return;
+  }
+  // other colours: 64-bit sums, the colours wait in shared memory and a lane converts
+  // each of its pixels in the round of its label
 #pragma unroll
   for (int i = 0; i < 8; i++)
-    if (lab[i] >= 0 && lab[i] < cap) pend |= 1u << i;
-  for (;;) {
-    const unsigned any = __ballot_sync(0xffffffffu, pend != 0);
-    if (!any) break;
-    const int src = __ffs(any) - 1;
-    int first = -1;
 #pragma unroll
-    for (int i = 7; i >= 0; i--)
-      if ((pend >> i) & 1u) first = lab[i];
-    const int k = __shfl_sync(0xffffffffu, first, src);
-    unsigned m = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) m |= (unsigned)(lab[i] == k) << i;
-    pend &= ~m;
+    for (int ch = 0; ch < 3; ch++) cw[i][ch][lane] = c[i][ch];
+  __syncwarp();
+  label_rounds(lab, pend, [&](int k, unsigned m, int src) {
     long long s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
     for (unsigned mm = m; mm; mm &= mm - 1) {
       const int i = __ffs(mm) - 1;
@@ -490,21 +527,11 @@ __global__ void __launch_bounds__(256) kb_sm_accumulate(const Slot* __restrict__
         q[ch] += fx_q(v * v, kFxSqShift);
       }
     }
-    const int N = __reduce_add_sync(0xffffffffu, __popc(m));
-    const int NI = shifted ? __reduce_add_sync(0xffffffffu, __popc(m & inv)) : 0;
     long long St[3], Qt[3];
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) { St[ch] = warp_sum64(s[ch]); Qt[ch] = warp_sum64(q[ch]); }
-    if (lane == src) {
-      atomicAdd(&sm.count[k], N);
-      if (NI) atomicAdd(&sm.ninvalid[k], NI);
-#pragma unroll
-      for (int ch = 0; ch < 3; ch++) {
-        atomicAdd((unsigned long long*)&sm.s[3 * (size_t)k + ch], (unsigned long long)St[ch]);
-        atomicAdd((unsigned long long*)&sm.sq[3 * (size_t)k + ch], (unsigned long long)Qt[ch]);
-      }
-    }
-  }
+    add(k, m, src, St, Qt);
+  });
 }
 
 // Marginal of one superpixel over the three colour channels, FP64: the

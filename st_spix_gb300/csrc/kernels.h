@@ -103,7 +103,6 @@ __global__ void kb_cc_local(const Slot* slots);
 __global__ void kb_cc_hook(const Slot* slots);
 __global__ void kb_cc_compress(const Slot* slots);
 __global__ void kb_list_holes(const Slot* slots);
-__global__ void kb_cc_size(const Slot* slots);
 __global__ void kb_cc_best(const Slot* slots);
 __global__ void kb_cc_invalidate(const Slot* slots);
 __global__ void kb_shift_params(const Slot* slots);
@@ -111,7 +110,7 @@ __global__ void kb_write_params(const Slot* slots);
 __global__ void kb_mark_active(const Slot* slots);
 __global__ void kb_relabel_init(const Slot* slots);
 __global__ void kb_living(const Slot* slots);
-__global__ void kb_relabel_compare(const Slot* slots, int chunk);
+__global__ void kb_relabel_compare(const Slot* slots);
 __global__ void kb_relabel_mark(const Slot* slots, float thresh_replace, float thresh_new);
 __global__ void kb_relabel_ids(const Slot* slots);
 __global__ void kb_relabel_params(const Slot* slots);
