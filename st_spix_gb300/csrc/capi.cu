@@ -322,7 +322,7 @@ constexpr long long kPixBytes = 1 + 5 * 4 + 8 + 4 + 2;        // border, d1 d2 s
 constexpr long long kSpDevBytes = 4 + 1 + 1 + 4 + 4 + 4 + 12 + 16 + 24 + 8 + 12 + 16 + 24 + 24 + 24 +
                                   64 + (long long)sizeof(SweepRec);
 constexpr long long kSmBytes = 4 + 24 + 24 + 4 + 4 + 4 + 4 + 4 + 1 + 8;
-constexpr long long kAuxBytes = 5 * 1 + 6 * 4 + 16 + 8 + 4 + 16 + 8 + 8;
+constexpr long long kAuxBytes = 5 * 1 + 6 * 4 + 16 + 8 + 4 + 16 + 8 + 8 + 72 + 4 + 1;
 constexpr long long kParamBytes = 12 + 12 + 16 + 24 + 4 + 16 + 24 + 24 + 4 + 4 + 4 + 4 + 4;
 
 // Make sure slot position i holds npix pixels and sp_cap superpixels.  Growing
@@ -364,6 +364,7 @@ int ensure_slot(stspix_ctx* ctx, int i, int npix, int sp_cap) {
     AL(L, s.fs, 2 * c2); AL(L, s.fds, 2 * c2); AL(L, s.ss, c2);
     AL(L, s.centers, 2 * c2); AL(L, s.rbest, c2); AL(L, s.ccbest, c2);
     AL(L, s.bbox, 4 * c2);
+    AL(L, s.snap, 9 * c2); AL(L, s.post_ids, c2); AL(L, s.recchg, c2);
     w.sp_cap = cap;
   }
   return STSPIX_OK;
@@ -424,6 +425,7 @@ void preload_kernels() {
       (const void*)kb_clear_stats,
       (const void*)kb_accumulate,
       (const void*)kb_posterior,
+      (const void*)kb_post_list,
       (const void*)kb_store_sample,
       (const void*)kb_find_border,
       (const void*)kb_sweep_t32,
@@ -646,8 +648,10 @@ void accumulate_fp(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, int 
 
 // stats_ready: the last sweep of the preceding update_seg already cleared and added
 // the statistics of the first nb slots (see update_seg).
+// incremental: only the ids whose sums changed since their last posterior (kb_post_list);
+// only where nothing but sweeps ran since the previous posterior of every slot.
 int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
-                  bool stats_ready = false) {
+                  bool stats_ready = false, bool incremental = false) {
   ctx->cur_fam = STSPIX_FAM_STATS;
   if (!stats_ready) {
     LAUNCHB(kb_clear_stats, L.max_cap, L, nb);
@@ -655,8 +659,9 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   }
   if (ctx->accumulator) accumulate_fp(ctx, st, L, nb, ctx->accumulator);
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
-  // id groups of 32 per block, about four blocks per SM over the batch (a block loops
-  // when a slot has more groups in use)
+  LAUNCHB(kb_post_list, L.max_cap, L, nb, incremental ? 1 : 0);
+  // groups of 32 listed ids, about four blocks per SM over the batch (a block loops
+  // when a slot lists more groups)
   const unsigned pg = (unsigned)std::min<long long>((L.max_cap + 31) / 32,
                                                     std::max(32, (4 * ctx->num_sms + nb - 1) / nb));
   LAUNCHG(kb_posterior, dim3(pg, (unsigned)nb), 128, L.d);
@@ -671,11 +676,19 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
 // current labels and the next update_params skips its clear and accumulate passes.
 // Not while tuning (the trial launches rerun the same sweep).  *fused tells whether
 // that happened.
+// first_active: the first sweep is an active-set sweep too (mode 2): only the
+// previous call's last-sweep changes (change plane 1) and the pixels next to a label
+// whose record the posterior between the calls changed can decide differently.  For
+// calls that follow one with *chg_ok set, with only an incremental posterior between.
+// *chg_ok: this call ran no tuning trials and an even number of launches, so change
+// plane 1 holds its last sweep's changes.
 int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
-               const stspix_config& cfg, bool need_border, bool fuse_stats, bool* fused) {
+               const stspix_config& cfg, bool need_border, bool fuse_stats, bool* fused,
+               bool first_active = false, bool* chg_ok = nullptr) {
   ctx->cur_fam = STSPIX_FAM_SWEEP;
   const int nseg = cfg.niters_seg;
   *fused = false;
+  if (chg_ok) *chg_ok = false;
   // the first sweep of the call scores every border pixel; the later ones only the
   // active set next to the previous sweep's changes (same labels, see kb_sweep_t*).
   // Launch j reads the labels of parity j & 1 and writes the other buffer.
@@ -838,16 +851,19 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
       return STSPIX_OK;
     }
   }
-  const bool fuse = fuse_stats && done == 0;   // no tuning trials in this call
+  const bool untuned = done == 0;             // no tuning trials in this call
+  const bool fuse = fuse_stats && untuned;
   while (done < nseg) {
     const bool pair = v2 >= 0 && nseg - done >= 2;
     const int deltas = fuse ? 1 : 0;
-    if (pair) sweep2(v2, launch & 1, done > 0 ? 1 : 0, deltas);
-    else sweep1(v1, launch & 1, done > 0 ? 1 : 0, deltas);
+    const int mode = done > 0 ? 1 : (first_active && untuned ? 2 : 0);
+    if (pair) sweep2(v2, launch & 1, mode, deltas);
+    else sweep1(v1, launch & 1, mode, deltas);
     done += pair ? 2 : 1;
     launch++;
   }
   *fused = fuse;
+  if (chg_ok) *chg_ok = untuned && launch > 0 && (launch & 1) == 0;
   if (launch & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;
@@ -931,15 +947,21 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector
   // pass); the int64 accumulator only
   bool stats_ready = false;
   const bool fuse = ctx->accumulator == 0;
+  bool chg_ok = false;      // the previous update_seg left its last changes in plane 1
   for (int idx = 0; idx < maxn; idx++) {
     while (nb > 0 && nit[nb - 1] <= idx) nb--;
     if (stop_after >= 0 && idx == stop_after) {
       if (extra_update && (r = update_params(ctx, st, L, nb))) return r;
       return STSPIX_OK;
     }
-    if ((r = update_params(ctx, st, L, nb, stats_ready))) return r;
+    // after the first iteration only the sweeps ran since every slot's last posterior
+    if ((r = update_params(ctx, st, L, nb, stats_ready, idx > 0))) return r;
     stats_ready = false;
+    // the first sweep is an active-set one when only sweeps and that incremental
+    // posterior ran since the previous update_seg
+    bool first_active = idx > 0 && chg_ok;
     if (idx > cfg.sm_start) {
+      if (idx % P == 0 || idx % P == P / 2) first_active = false;
       if (idx % P == 0) {
         count_b += 1;
         count_p += 1;
@@ -957,7 +979,8 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector
     const bool merge_next = nx < maxn && nx > cfg.sm_start && nx % P == P / 2;
     const bool fuse_now = fuse && nx < maxn && !(stop_after >= 0 && nx == stop_after);
     bool fused = false;
-    if ((r = update_seg(ctx, st, L, nb, cfg, merge_next || stop_after >= 0, fuse_now, &fused)))
+    if ((r = update_seg(ctx, st, L, nb, cfg, merge_next || stop_after >= 0, fuse_now, &fused,
+                        first_active, &chg_ok)))
       return r;
     stats_ready = fused;
   }
@@ -967,7 +990,7 @@ int bass_loop(stspix_ctx* ctx, cudaStream_t st, const List& L, const std::vector
   }
   // final update_params + store_sample; slots that finished earlier were untouched
   // since, so running theirs here is the same as running it right after their loop
-  if ((r = update_params(ctx, st, L, L.B))) return r;
+  if ((r = update_params(ctx, st, L, L.B, false, maxn > 0))) return r;
   ctx->cur_fam = STSPIX_FAM_POSTERIOR;
   LAUNCHB(kb_store_sample, L.max_cap, L, L.B);
   return STSPIX_OK;

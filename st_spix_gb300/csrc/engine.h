@@ -46,6 +46,7 @@ struct __align__(16) SweepRec {
   int count;                       // pixel count
   float isx, isy, isz, pad;        // (float) inverse shape covariance
 };
+static_assert(sizeof(SweepRec) == 48, "three 16-byte words");
 
 // Per-superpixel kernels with FP64 work: live ids are the low ones, and this part issues
 // FP64 slowly, at a cost per warp instruction whatever its active lanes.  So a warp takes
@@ -117,6 +118,8 @@ struct Scalars {
   // (class counts, write cursors)
   int fl_n, fl_prev, fl_iter, fl_done, fl_fill;
   int fl_cnt[4], fl_pos[4];
+  // posterior work list: ids listed, blocks of the posterior launch done
+  int npost, post_done;
 };
 
 // One frame of a batch: its inputs, outputs, workspace and scalars.  Kernels take
@@ -161,6 +164,9 @@ struct Slot {
   double* centers;
   unsigned long long *rbest, *ccbest;
   int* bbox;               // [4*(cap+2)]: x0, x1, y0, y1 per superpixel (split BFS)
+  long long* snap;         // [9*(cap+2)]: count and the 8 sums each id's posterior last saw
+  uint8_t* recchg;         // [cap+2]: the last posterior changed the id's SweepRec
+  int* post_ids;           // [cap+2]: ids of the running posterior (kb_post_list)
   Scalars* sc;
   int tile_base[3];        // first sweep tile of this slot in the batch (32-, 64-, 16-wide)
 };

@@ -465,13 +465,13 @@ __device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in
 // mean and scatter; then warps 0-2 one smoothed covariance entry each, then warps 0-2
 // one inverse entry each and warp 3 the log determinant.  Every value is the same
 // expression as a single-thread evaluation, exchanged through shared memory.
-__device__ __forceinline__ void posterior_ids(const Slot& S, int k0) {
+// k: this lane's id (-1: none).
+__device__ __forceinline__ void posterior_ids(const Slot& S, int k) {
   __shared__ double v_ps[3][32], v_raw[3][32], v_m[2][32], v_s[3][32], v_i[4][32];
   __shared__ float v_app[3][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const SpDev& sp = S.sp;
-  const int k = k0 + lane;
-  const bool inr = k < sp.cap;
+  const bool inr = k >= 0 && k < sp.cap;
   // every load of the id is issued before any is used (one memory round trip): the
   // count and flags, and the fields this warp's part of the posterior reads
   int count_int = 0;
@@ -568,21 +568,84 @@ __device__ __forceinline__ void posterior_ids(const Slot& S, int k0) {
     r.frac = (mx != fx ? 1 : 0) | (my != fy ? 2 : 0);
     r.isx = (float)ix; r.isy = (float)iy; r.isz = (float)iz; r.pad = 0.f;
     r.count = count_int;
+    // the sweeps of the next update score again only the pixels next to a changed record
+    const uint4* o = (const uint4*)&sp.rec[k];
+    const uint4* nw = (const uint4*)&r;
+    bool same = true;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const uint4 a = o[q], b = nw[q];
+      same &= a.x == b.x && a.y == b.y && a.z == b.z && a.w == b.w;
+    }
+    if (!same) S.recchg[k] = 1;
     sp.rec[k] = r;
   }
 }
 
-// Grid: x blocks per slot, each taking the slot's 32-id groups x, x + gridDim.x, ...
-// up to the largest id in use.  Ids above it were never live in this frame: their
-// fields still hold the zeros the frame's set-up wrote (kb_init_bass_params,
-// kb_write_params), which is what the posterior would write for them.  A group's
-// barriers are block-uniform, and the first barrier of the next group follows every
-// read of the previous one's shared values.
-__global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slots) {
+// The posterior's work list (ids 0 .. max_spix, below cap): every id, or with
+// `incremental` only the ids whose count or sums differ from those its posterior last
+// saw.  Between two posteriors of the outer loop only the sweeps run, which change no
+// other input of the posterior (priors, flags and the sample covariance change in the
+// split, merge and relabel steps and at the frame's set-up, whose posteriors are full),
+// so an id with equal sums would get the values it already holds (the same
+// expressions of the same inputs).  Listed ids record their sums; the list's order
+// varies, each id's result does not.
+__global__ void kb_post_list(const Slot* __restrict__ slots, int incremental) {
   pdl_enter();
   SLOT_Y;
   const int last = min(S.sp.cap - 1, S.sc->max_spix);
-  for (int g = blockIdx.x; g * 32 <= last; g += gridDim.x) posterior_ids(S, g * 32);
+  if ((int)(blockIdx.x * blockDim.x) > last) return;     // block-uniform
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  bool want = false;
+  if (k <= last) {
+    S.recchg[k] = 0;                       // set by kb_posterior when the record changes
+    const long long* a = S.sp.acc + 8 * (size_t)k;
+    long long* snap = S.snap + 9 * (size_t)k;
+    long long cur[9];
+#pragma unroll
+    for (int f = 0; f < 8; f++) cur[f] = a[f];
+    cur[8] = S.sp.count[k];
+    want = !incremental;
+    if (incremental) {
+#pragma unroll
+      for (int f = 0; f < 9; f++) want |= cur[f] != snap[f];
+    }
+    if (want) {
+#pragma unroll
+      for (int f = 0; f < 9; f++) snap[f] = cur[f];
+    }
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&S.sc->npost, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (want) S.post_ids[base + __popc(m & ((1u << lane) - 1))] = k;
+}
+
+// Grid: x blocks per slot, each taking groups of 32 listed ids x, x + gridDim.x, ...
+// A group's barriers are block-uniform, and the first barrier of the next group follows
+// every read of the previous one's shared values.  The last block of a slot to finish
+// clears the list for the next posterior (every block read the list length first).
+__global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slots) {
+  pdl_enter();
+  SLOT_Y;
+  Scalars* sc = S.sc;
+  const int n = *(volatile int*)&sc->npost;
+  for (int g = blockIdx.x; g * 32 < n; g += gridDim.x) {
+    const int i = g * 32 + (threadIdx.x & 31);
+    posterior_ids(S, i < n ? S.post_ids[i] : -1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&sc->post_done, 1) == (int)gridDim.x - 1) {
+      sc->npost = 0;
+      sc->post_done = 0;
+      __threadfence();
+    }
+  }
 }
 
 // clear_fields + the helper memset (update_params.cu:54-88, :26): zero the counts
@@ -1180,6 +1243,25 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
   if (mode) {
     unsigned long long* a0 = sm.act[0];
     unsigned long long* a1 = sm.act[1];
+    if (mode == 2) {
+      // first sweep after an incremental posterior: besides the previous sweep's changes,
+      // every pixel whose label or 4-neighbour's label got a new record may decide
+      // differently.  The label-region pixels whose label's record changed, as row
+      // bitmasks (from the staging registers; sm.edE is free until the edges below).
+      const int cap = S.sp.cap;
+#pragma unroll
+      for (int a = 0; a < kRW; a++) {
+        const int rr = warp * kRW + a;
+        unsigned q[kCK];
+#pragma unroll
+        for (int c = 0; c < kCK; c++) {
+          const int v = lv[a][c];
+          q[c] = __ballot_sync(0xffffffffu, v >= 0 && v < cap && S.recchg[v] != 0);
+        }
+        if (lane == 0) pack_row<kCK>(q, &sm.edE[0][rr], &sm.edE[1][rr]);
+      }
+      __syncthreads();
+    }
     // each row of the label region: its change bits from the previous sweep's plane
     // (kNW 16-bit words starting at word rx0 >> 4, shifted by the region's offset in
     // the first word), then dilated by the reach horizontally
@@ -1205,6 +1287,15 @@ __device__ __forceinline__ void sweep_tile(const Slot& S, int bx, int by, int pa
       }
       unsigned long long f0 = (lo >> off) | (hi << (64 - off));
       unsigned long long f1 = hi >> off;
+      if (mode == 2) {
+        // changed records seed the active set one pixel further out (a pixel reads the
+        // records of its 4-neighbours' labels)
+        unsigned long long q0 = sm.edE[0][r], q1 = sm.edE[1][r];
+        if (r > 0) { q0 |= sm.edE[0][r - 1]; q1 |= sm.edE[1][r - 1]; }
+        if (r + 1 < kLY) { q0 |= sm.edE[0][r + 1]; q1 |= sm.edE[1][r + 1]; }
+        f0 |= q0 | (q0 << 1) | (q0 >> 1) | (q1 << 63);
+        f1 |= q1 | (q1 << 1) | (q1 >> 1) | (q0 >> 63);
+      }
       if (kLX < 64) { f0 &= (1ull << (kLX & 63)) - 1ull; f1 = 0; }
       else if (kLX < 128) { f1 &= (1ull << ((kLX - 64) & 63)) - 1ull; }
       nz = (f0 | f1) != 0;
@@ -1462,6 +1553,7 @@ __global__ void kb_scalars(const Slot* __restrict__ slots, int B, int op) {
       sc->fill_iters = 0;
       sc->ninvalid = 0;
       sc->tmp0 = sc->tmp1 = sc->tmp2 = 0;
+      sc->npost = sc->post_done = 0;
       sc->nspix = 0;
       if (S.mode) { sc->max_spix = S.n_prev - 1; sc->nbuf_logical = 10 * S.n_prev; }
       else { sc->max_spix = 0; sc->nbuf_logical = 30 * S.nraw; }
