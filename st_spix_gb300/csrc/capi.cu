@@ -161,6 +161,8 @@ std::mutex g_device_mu;
 const int kThreads = 256;
 const int kBfsBigSmem = 5 * 512 * 8 * 8;  // kb_split_bfs_big: 5 arrays of 512 rows x 8 words
 inline unsigned blocks_for(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
+// Threads of a FOR_PIX kernel over n pixels.
+inline long long pix_units(long long n) { return (n + kPixPerThread - 1) / kPixPerThread; }
 // 64 x 32 tiles of the largest frame of a slot table (per-slot grids of the warp-block
 // kernels; blocks past a smaller frame's tiles return).
 inline unsigned tiles64(const List& L) {
@@ -843,10 +845,10 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
     ctx->sweep_choice[key] = v1 | ((v2 + 1) << 8);
     ctx->tunes++;
     if (done >= nseg) {
-      if (launch & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
+      if (launch & 1) LAUNCHB(kb_copy_labels, pix_units(L.max_npix), L, nb);
       if (need_border) {
         ctx->cur_fam = STSPIX_FAM_MERGE;
-        LAUNCHB(kb_find_border, L.max_npix, L, nb);
+        LAUNCHB(kb_find_border, pix_units(L.max_npix), L, nb);
       }
       return STSPIX_OK;
     }
@@ -864,10 +866,10 @@ int update_seg(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   }
   *fused = fuse;
   if (chg_ok) *chg_ok = untuned && launch > 0 && (launch & 1) == 0;
-  if (launch & 1) LAUNCHB(kb_copy_labels, L.max_npix, L, nb);
+  if (launch & 1) LAUNCHB(kb_copy_labels, pix_units(L.max_npix), L, nb);
   if (need_border) {
     ctx->cur_fam = STSPIX_FAM_MERGE;
-    LAUNCHB(kb_find_border, L.max_npix, L, nb);
+    LAUNCHB(kb_find_border, pix_units(L.max_npix), L, nb);
   }
   return STSPIX_OK;
 }
@@ -876,7 +878,7 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
               const stspix_config& cfg, int dir_b, int dir_p) {
   ctx->cur_fam = STSPIX_FAM_SPLIT;
   LAUNCHS(kb_split_begin, L, nb);
-  LAUNCHB(kb_split_clear, L.max_npix, L, nb);
+  LAUNCHB(kb_split_clear, pix_units(L.max_npix), L, nb);
   LAUNCHB(kb_split_seed, L.max_cap, L, nb, dir_b, dir_p);
   LAUNCHG(kb_bbox, dim3(tiles64(L), (unsigned)nb), kThreads, L.d);
   LAUNCHG(kb_split_bfs, dim3(256, (unsigned)nb), 128, L.d, dir_b, dir_p);  // 1024 warps per slot
@@ -887,13 +889,13 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
     ctx->launches++;
     prof_end(ctx, st, pe_, "kb_split_bfs_big");
   }
-  LAUNCHB(kb_split_partition, L.max_npix, L, nb);
+  LAUNCHB(kb_split_partition, pix_units(L.max_npix), L, nb);
   LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
   LAUNCHG(kb_sm_accumulate, dim3(tiles64(L), (unsigned)nb), kThreads, L.d, 1);
   LAUNCHB(kb_split_decide, L.max_cap, L, nb, K, cfg.split_alpha);
   LAUNCHG(kb_scan, (unsigned)nb, 1024, L.d, 1);
   LAUNCHB(kb_split_commit, L.max_cap, L, nb);
-  LAUNCHB(kb_split_apply, L.max_npix, L, nb);
+  LAUNCHB(kb_split_apply, pix_units(L.max_npix), L, nb);
   LAUNCHS(kb_split_end, L, nb);
   return STSPIX_OK;
 }
@@ -911,7 +913,7 @@ int run_relabel(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   LAUNCHG(kb_scan, (unsigned)nb, 1024, L.d, 2);
   LAUNCHB(kb_relabel_ids, L.max_cap, L, nb);
   LAUNCHB(kb_relabel_params, L.max_cap, L, nb);
-  LAUNCHB(kb_relabel_apply, L.max_npix, L, nb);
+  LAUNCHB(kb_relabel_apply, pix_units(L.max_npix), L, nb);
   LAUNCHB(kb_count_revived, L.max_cap, L, nb);
   LAUNCHS(kb_relabel_end, L, nb);
   return STSPIX_OK;
@@ -921,14 +923,14 @@ int run_merge(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
               const stspix_config& cfg, int dir_b, int dir_p) {
   ctx->cur_fam = STSPIX_FAM_MERGE;
   LAUNCHB(kb_merge_clear, L.max_cap + 2, L, nb);
-  LAUNCHB(kb_merge_candidates, L.max_npix, L, nb, dir_b, dir_p);
+  LAUNCHB(kb_merge_candidates, pix_units(L.max_npix), L, nb, dir_b, dir_p);
   LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
   LAUNCHG(kb_sm_accumulate, dim3(tiles64(L), (unsigned)nb), kThreads, L.d, 0);
   LAUNCHB(kb_merge_single, L.max_cap, L, nb, K);
   LAUNCHB(kb_merge_decide, L.max_cap, L, nb, K, cfg.merge_alpha);
   LAUNCHB(kb_merge_flag, L.max_cap, L, nb);
   LAUNCHB(kb_merge_remove, L.max_cap, L, nb);
-  LAUNCHB(kb_merge_apply, L.max_npix, L, nb);
+  LAUNCHB(kb_merge_apply, pix_units(L.max_npix), L, nb);
   return STSPIX_OK;
 }
 
@@ -1019,7 +1021,7 @@ int compact(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHG(kb_scan, (unsigned)L.B, 1024, L.d, 3);
   LAUNCHB(kb_compact_gather, L.max_cap, L, L.B);
   LAUNCHB(kb_compact_scatter, L.max_cap, L, L.B);
-  LAUNCHB(kb_remap, L.max_npix, L, L.B, 1);
+  LAUNCHB(kb_remap, pix_units(L.max_npix), L, L.B, 1);
   LAUNCHS(kb_scalars, L, L.B, (int)kOpCompactEnd);
   return STSPIX_OK;
 }
@@ -1033,14 +1035,14 @@ int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHB(kb_clear_flags, L.max_cap + 2, L, L.B);
   LAUNCHB(kb_mark_present, L.max_npix, L, L.B, 0);
   LAUNCHG(kb_scan, (unsigned)L.B, 1024, L.d, 0);
-  LAUNCHB(kb_remap, L.max_npix, L, L.B, 0);
+  LAUNCHB(kb_remap, pix_units(L.max_npix), L, L.B, 0);
   LAUNCHS(kb_scalars, L, L.B, (int)kOpAfterHex);
   LAUNCHB(kb_init_bass_params, L.max_cap, L, L.B);
   LAUNCHB(kb_clear_stats, L.max_cap, L, L.B);
   LAUNCHG(kb_accumulate, acc_blocks(ctx, L, L.B), 256, L.d, L.B);
   if (ctx->accumulator) accumulate_fp(ctx, st, L, L.B, ctx->accumulator);
   LAUNCHB(kb_init_prior_mu, L.max_cap, L, L.B);
-  LAUNCHB(kb_find_border, L.max_npix, L, L.B);
+  LAUNCHB(kb_find_border, pix_units(L.max_npix), L, L.B);
   return STSPIX_OK;
 }
 
@@ -1181,10 +1183,10 @@ int shift_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   if (L.B <= 0) return STSPIX_OK;
   int r;
   ctx->cur_fam = STSPIX_FAM_PROP;
-  LAUNCHB(kb_prop_clear, std::max<long long>(L.max_npix, L.max_nprev), L, L.B);
+  LAUNCHB(kb_prop_clear, pix_units(std::max<long long>(L.max_npix, L.max_nprev)), L, L.B);
   LAUNCHG(kb_flow_pool, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d);
   LAUNCHB(kb_flow_mean, L.max_nprev, L, L.B);
-  LAUNCHB(kb_shift, L.max_npix, L, L.B);
+  LAUNCHB(kb_shift, pix_units(L.max_npix), L, L.B);
   LAUNCHB(kb_shift_decode, L.max_npix, L, L.B);
   LAUNCHG(kb_count_labels, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d, 0);
   // fill, invalidate disconnected, fill
@@ -1193,8 +1195,8 @@ int shift_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
           kThreads, L.d);
   LAUNCHB(kb_cc_hook, L.max_npix, L, L.B);
   LAUNCHB(kb_cc_compress, L.max_npix, L, L.B);
-  LAUNCHB(kb_cc_best, L.max_npix, L, L.B);
-  LAUNCHB(kb_cc_invalidate, L.max_npix, L, L.B);
+  LAUNCHB(kb_cc_best, pix_units(L.max_npix), L, L.B);
+  LAUNCHB(kb_cc_invalidate, pix_units(L.max_npix), L, L.B);
   LAUNCHB(kb_list_holes, L.max_npix, L, L.B);
   if ((r = run_fill(ctx, st, L))) return r;
   LAUNCHG(kb_count_labels, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d, 1);
@@ -1264,7 +1266,7 @@ int batch_tail(stspix_ctx* ctx, cudaStream_t st, const List& Lp, const List& Ls,
   if ((r = bass_loop(ctx, st, Ls, nit_sorted, cfg, K, -1, 0))) return r;
   if ((r = compact(ctx, st, Ls))) return r;
   LAUNCHB(kb_read_params, Ls.max_cap, Ls, Ls.B);
-  LAUNCHB(kb_save_prev, Ls.max_npix, Ls, Ls.B);
+  LAUNCHB(kb_save_prev, pix_units(Ls.max_npix), Ls, Ls.B);
   return STSPIX_OK;
 }
 
@@ -1479,7 +1481,7 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
   if (stop_after < 0) {
     if ((r = compact(ctx, st, Ls))) return r;
     LAUNCHB(kb_read_params, Ls.max_cap, Ls, Ls.B);
-    LAUNCHB(kb_save_prev, Ls.max_npix, Ls, Ls.B);
+    LAUNCHB(kb_save_prev, pix_units(Ls.max_npix), Ls, Ls.B);
   }
   return finish();
 }

@@ -175,6 +175,14 @@ struct Slot {
 enum { kOpBegin = 0, kOpAfterHex = 1, kOpCompactN = 2, kOpCompactEnd = 3 };
 
 #define SLOT_Y const Slot& S = slots[blockIdx.y]
+// Light per-pixel kernels: thread i of block b takes the pixels
+// kPixPerThread * blockDim.x * b + i + blockDim.x * j (j < kPixPerThread), coalesced, so
+// a launch has a quarter of the blocks of one pixel per thread (block scheduling and the
+// per-block set-up dominate passes this light).  Grids: pix_units(n) threads.
+constexpr int kPixPerThread = 4;
+#define FOR_PIX(t, n)                                                                    \
+  for (int j_ = 0, t = (int)blockIdx.x * (kPixPerThread * (int)blockDim.x) + (int)threadIdx.x; \
+       j_ < kPixPerThread && t < (n); j_++, t += (int)blockDim.x)
 #define SLOT_Z const Slot& S = slots[blockIdx.z]
 
 // ---------------------------------------------------------------------------

@@ -85,12 +85,13 @@ __global__ void kb_init_hex(const Slot* __restrict__ slots) {
 __global__ void kb_mark_present(const Slot* __restrict__ slots, int mode) {
   pdl_enter();
   SLOT_Y;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= S.npix) return;
-  int lo = mode == 0 ? 0 : S.lo;
-  int hi = mode == 0 ? S.nraw - 1 : min(S.sc->max_spix, S.cap - 1);
-  int v = S.seg[i];
-  if (v >= lo && v <= hi) S.flags[v - lo] = 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lo = mode == 0 ? 0 : S.lo;
+  const int hi = mode == 0 ? S.nraw - 1 : min(S.sc->max_spix, S.cap - 1);
+  const int v = i < S.npix ? S.seg[i] : -1;
+  // one store per distinct label of the warp (a warp's pixels are consecutive)
+  const unsigned peers = __match_any_sync(0xffffffffu, v);
+  if (v >= lo && v <= hi && (int)(threadIdx.x & 31) == __ffs(peers) - 1) S.flags[v - lo] = 1;
 }
 
 // One block per slot: exclusive scan of n byte flags (n up to a few 10^5), each
@@ -130,11 +131,11 @@ __global__ void kb_scan(const Slot* __restrict__ slots, int mode) {
 __global__ void kb_remap(const Slot* __restrict__ slots, int mode) {
   pdl_enter();
   SLOT_Y;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= S.npix) return;
-  int lo = mode == 0 ? 0 : S.lo;
-  int v = S.seg[i];
-  if (v >= lo) S.seg[i] = lo + S.excl[v - lo];
+  const int lo = mode == 0 ? 0 : S.lo;
+  FOR_PIX(i, S.npix) {
+    const int v = S.seg[i];
+    if (v >= lo) S.seg[i] = lo + S.excl[v - lo];
+  }
 }
 
 // fill_new_params_from_old (compact_spix.cu:220-265): gather moved fields.
@@ -705,15 +706,15 @@ __global__ void k_find_border(const int* __restrict__ seg, uint8_t* __restrict__
 __global__ void kb_find_border(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= S.npix) return;
   const int W = S.W, H = S.H;
   const int* seg = S.seg;
-  int x = idx % W, y = idx / W;
-  if (y < 1 || x < 1 || y >= H - 1 || x >= W - 1) { S.border[idx] = 1; return; }
-  int C = seg[idx];
-  S.border[idx] = (C != seg[idx - W] || C != seg[idx + W] || C != seg[idx + 1] ||
-                   C != seg[idx - 1]) ? 1 : 0;
+  FOR_PIX(idx, S.npix) {
+    const int x = idx % W, y = idx / W;
+    if (y < 1 || x < 1 || y >= H - 1 || x >= W - 1) { S.border[idx] = 1; continue; }
+    const int C = seg[idx];
+    S.border[idx] = (C != seg[idx - W] || C != seg[idx + W] || C != seg[idx + 1] ||
+                     C != seg[idx - 1]) ? 1 : 0;
+  }
 }
 
 __global__ void k_find_border_end(const int* __restrict__ seg, uint8_t* __restrict__ border,
@@ -1582,15 +1583,14 @@ __global__ void kb_clear_flags(const Slot* __restrict__ slots) {
 __global__ void kb_save_prev(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (S.resident_labels && i < S.npix) S.resident_labels[i] = S.seg[i];
+  if (!S.resident_labels) return;
+  FOR_PIX(i, S.npix) S.resident_labels[i] = S.seg[i];
 }
 
 __global__ void kb_copy_labels(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < S.npix) S.seg[i] = S.seg_alt[i];
+  FOR_PIX(i, S.npix) S.seg[i] = S.seg_alt[i];
 }
 
 __global__ void k_dump_state(SpDev sp, stspix_state_dump d) {

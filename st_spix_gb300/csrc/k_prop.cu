@@ -14,21 +14,22 @@ namespace stspix {
 __global__ void kb_prop_clear(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < S.n_prev) {
-    S.cnt_pool[i] = 0;
-    S.cs[i] = 0;
-    S.cf[i] = 0;
-    S.fs[2 * i] = 0;
-    S.fs[2 * i + 1] = 0;
-    S.ccbest[i] = 0;
+  FOR_PIX(i, max(S.npix, S.n_prev)) {
+    if (i < S.n_prev) {
+      S.cnt_pool[i] = 0;
+      S.cs[i] = 0;
+      S.cf[i] = 0;
+      S.fs[2 * (size_t)i] = 0;
+      S.fs[2 * (size_t)i + 1] = 0;
+      S.ccbest[i] = 0;
+    }
+    if (i < S.npix) {
+      S.hits[i] = 0;
+      S.best[i] = ~0ull;
+      S.d2[i] = 0;
+    }
+    if (i == 0) { S.sc->ninvalid = 0; S.sc->nhole = 0; }
   }
-  if (i < S.npix) {
-    S.hits[i] = 0;
-    S.best[i] = ~0ull;
-    S.d2[i] = 0;
-  }
-  if (i == 0) { S.sc->ninvalid = 0; S.sc->nhole = 0; }
 }
 
 // Mean flow per superpixel (sp_downsample_kernel / normz_downsample_kernel,
@@ -101,19 +102,19 @@ __global__ void kb_shift(const Slot* __restrict__ slots) {
   const float* __restrict__ fds = S.fds;
   int* __restrict__ hits = S.hits;
   unsigned long long* __restrict__ best = S.best;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= H * W) return;
-  int k = lab[t];
-  if (k < 0 || k >= n) return;
-  int size = cnt[k];
-  int fw = (int)roundf(fds[2 * k]);
-  int fh = (int)roundf(fds[2 * k + 1]);
-  int w = t % W + fw, h = t / W + fh;
-  if (w < 0 || w >= W || h < 0 || h >= H) return;
-  int d = h * W + w;
-  atomicAdd(&hits[d], 1);
-  unsigned long long key = ((unsigned long long)(unsigned int)size << 32) | (unsigned int)k;
-  atomicMin(&best[d], key);
+  FOR_PIX(t, H * W) {
+    const int k = lab[t];
+    if (k < 0 || k >= n) continue;
+    const int size = cnt[k];
+    const int fw = (int)roundf(fds[2 * k]);
+    const int fh = (int)roundf(fds[2 * k + 1]);
+    const int w = t % W + fw, h = t / W + fh;
+    if (w < 0 || w >= W || h < 0 || h >= H) continue;
+    const int d = h * W + w;
+    atomicAdd(&hits[d], 1);
+    const unsigned long long key = ((unsigned long long)(unsigned int)size << 32) | (unsigned int)k;
+    atomicMin(&best[d], key);
+  }
 }
 
 // decode_kernel (shift_labels.cu:128-164) + copy to `filled` + hole count.
@@ -525,13 +526,14 @@ __global__ void kb_cc_best(const Slot* __restrict__ slots) {
   const int* __restrict__ size = S.d2;
   const int nlab = S.n_prev;
   unsigned long long* __restrict__ best = S.ccbest;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix || root[t] != t) return;
-  int L = seg[t];
-  if (L < 0 || L >= nlab) return;
-  unsigned long long key = ((unsigned long long)(unsigned int)size[t] << 32) |
-                           (unsigned long long)(0xffffffffu - (unsigned int)t);
-  atomicMax(&best[L], key);
+  FOR_PIX(t, S.npix) {
+    if (root[t] != t) continue;
+    const int L = seg[t];
+    if (L < 0 || L >= nlab) continue;
+    const unsigned long long key = ((unsigned long long)(unsigned int)size[t] << 32) |
+                                   (unsigned long long)(0xffffffffu - (unsigned int)t);
+    atomicMax(&best[L], key);
+  }
 }
 
 __global__ void kb_cc_invalidate(const Slot* __restrict__ slots) {
@@ -541,12 +543,12 @@ __global__ void kb_cc_invalidate(const Slot* __restrict__ slots) {
   const int* __restrict__ root = S.d1;
   const int nlab = S.n_prev;
   const unsigned long long* __restrict__ best = S.ccbest;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int L = seg[t];
-  if (L < 0 || L >= nlab) return;
-  unsigned int win = 0xffffffffu - (unsigned int)(best[L] & 0xffffffffull);
-  if ((unsigned int)root[t] != win) seg[t] = -1;
+  FOR_PIX(t, S.npix) {
+    const int L = seg[t];
+    if (L < 0 || L >= nlab) continue;
+    const unsigned int win = 0xffffffffu - (unsigned int)(best[L] & 0xffffffffull);
+    if ((unsigned int)root[t] != win) seg[t] = -1;
+  }
 }
 
 // Hole list of the second fill: every -1 pixel after the invalidation.
@@ -658,10 +660,12 @@ __global__ void kb_living(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int v = S.seg[t];
-  if (v >= 0 && v <= S.sc->max_spix) S.living[v] = 1;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = t < S.npix ? S.seg[t] : -1;
+  // one store per distinct label of the warp (a warp's pixels are consecutive)
+  const unsigned peers = __match_any_sync(0xffffffffu, v);
+  if (v >= 0 && v <= S.sc->max_spix && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+    S.living[v] = 1;
 }
 
 // find_most_similar_spix (relabel.cu:201-276): grid (s, candidate chunk of
@@ -793,12 +797,12 @@ __global__ void kb_relabel_apply(const Slot* __restrict__ slots) {
   int* __restrict__ seg = S.seg;
   const int cap = S.cap;
   const int* __restrict__ rid = S.rid;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int v = seg[t];
-  if (v < 0 || v >= cap) return;
-  int n = rid[v];
-  if (n >= 0 && n < cap) seg[t] = n;
+  FOR_PIX(t, S.npix) {
+    const int v = seg[t];
+    if (v < 0 || v >= cap) continue;
+    const int n = rid[v];
+    if (n >= 0 && n < cap) seg[t] = n;
+  }
 }
 
 __global__ void kb_relabel_end(const Slot* __restrict__ slots, int B) {

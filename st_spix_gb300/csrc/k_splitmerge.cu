@@ -45,10 +45,10 @@ __global__ void kb_split_seed(const Slot* __restrict__ slots, int dir_bass, int 
 __global__ void kb_split_clear(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  S.d1[t] = -1;
-  S.d2[t] = -1;
+  FOR_PIX(t, S.npix) {
+    S.d1[t] = -1;
+    S.d2[t] = -1;
+  }
 }
 
 __global__ void kb_split_begin(const Slot* __restrict__ slots, int B) {
@@ -406,11 +406,12 @@ __global__ void __launch_bounds__(256) kb_split_bfs_big(const Slot* __restrict__
 __global__ void kb_split_partition(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int v = S.seg[t];
-  if (S.d1[t] > S.d2[t]) v += S.sc->tmp1;
-  S.smseg[t] = v;
+  const int off = S.sc->tmp1;
+  FOR_PIX(t, S.npix) {
+    int v = S.seg[t];
+    if (S.d1[t] > S.d2[t]) v += off;
+    S.smseg[t] = v;
+  }
 }
 
 // Clear the split/merge sums (cap + 2 entries).
@@ -648,19 +649,19 @@ __global__ void kb_split_apply(const Slot* __restrict__ slots) {
   const Scalars* __restrict__ sc = S.sc;
   const uint8_t* __restrict__ accept = S.accept;
   const int prop_mode = S.mode;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int k = seg[t];
-  if (k < 0 || k >= sp.cap) return;
-  uint8_t fl = accept[k];
-  if (!fl) return;
-  int s = sm.newid[k];
-  if (s < 0) return;
-  int k2 = k + sc->tmp1;
-  if (!prop_mode || (fl & 8)) {
-    if (smseg[t] == k2) seg[t] = s;
-  } else {
-    if (smseg[t] == k) seg[t] = s;
+  FOR_PIX(t, S.npix) {
+    const int k = seg[t];
+    if (k < 0 || k >= sp.cap) continue;
+    const uint8_t fl = accept[k];
+    if (!fl) continue;
+    const int s = sm.newid[k];
+    if (s < 0) continue;
+    const int k2 = k + sc->tmp1;
+    if (!prop_mode || (fl & 8)) {
+      if (smseg[t] == k2) seg[t] = s;
+    } else {
+      if (smseg[t] == k) seg[t] = s;
+    }
   }
 }
 
@@ -688,24 +689,25 @@ __global__ void kb_merge_candidates(const Slot* __restrict__ slots, int dir_bass
   const uint8_t* __restrict__ prop = S.sp.prop;
   const int cap = S.cap;
   int* __restrict__ pair = S.sm.pair;
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= H * W || !border[idx]) return;
-  int x = idx % W, y = idx / W;
-  int C = seg[idx];
-  if (C < 0 || C >= cap) return;
-  int Wl = -1;
-  if (!prop_mode) {
-    if (direction == 1) { if (y >= 0 && y < H - 1) Wl = seg[idx + W]; }
-    else { if (x > 0 && x < W) Wl = seg[idx - 1]; }
-    if (Wl >= cap) Wl = -1;
-    if (Wl >= 0 && C != Wl) atomicMax(&pair[C], Wl);
-  } else {
-    if (direction == 1) { if (y > 1 && y < H - 2) Wl = seg[idx + W]; }
-    else { if (x > 1 && x < W - 2) Wl = seg[idx - 1]; }
-    if (Wl >= cap) Wl = -1;
-    bool pC = prop[C];
-    bool pW = (Wl >= 0) ? prop[Wl] : false;
-    if (Wl >= 0 && C != Wl && pC != pW) atomicMax(&pair[C], Wl);
+  FOR_PIX(idx, H * W) {
+    if (!border[idx]) continue;
+    const int x = idx % W, y = idx / W;
+    const int C = seg[idx];
+    if (C < 0 || C >= cap) continue;
+    int Wl = -1;
+    if (!prop_mode) {
+      if (direction == 1) { if (y >= 0 && y < H - 1) Wl = seg[idx + W]; }
+      else { if (x > 0 && x < W) Wl = seg[idx - 1]; }
+      if (Wl >= cap) Wl = -1;
+      if (Wl >= 0 && C != Wl) atomicMax(&pair[C], Wl);
+    } else {
+      if (direction == 1) { if (y > 1 && y < H - 2) Wl = seg[idx + W]; }
+      else { if (x > 1 && x < W - 2) Wl = seg[idx - 1]; }
+      if (Wl >= cap) Wl = -1;
+      const bool pC = prop[C];
+      const bool pW = (Wl >= 0) ? prop[Wl] : false;
+      if (Wl >= 0 && C != Wl && pC != pW) atomicMax(&pair[C], Wl);
+    }
   }
 }
 
@@ -831,11 +833,11 @@ __global__ void kb_merge_apply(const Slot* __restrict__ slots) {
   int* __restrict__ seg = S.seg;
   const int cap = S.cap;
   const SmDev& sm = S.sm;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int k = seg[t];
-  if (k < 0 || k >= cap) return;
-  if (sm.flag[k] & 4) seg[t] = sm.target[k];
+  FOR_PIX(t, S.npix) {
+    const int k = seg[t];
+    if (k < 0 || k >= cap) continue;
+    if (sm.flag[k] & 4) seg[t] = sm.target[k];
+  }
 }
 
 }  // namespace stspix
