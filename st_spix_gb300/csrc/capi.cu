@@ -905,7 +905,7 @@ int run_relabel(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
                 const stspix_config& cfg) {
   ctx->cur_fam = STSPIX_FAM_MERGE;
   LAUNCHB(kb_relabel_init, L.max_cap + 2, L, nb);
-  LAUNCHB(kb_living, L.max_npix, L, nb);
+  LAUNCHB(kb_living, pix_units(L.max_npix), L, nb);
   dim3 g(blocks_for(L.max_cap),
          (unsigned)std::max(1, (L.max_nprev + kRelabelChunk - 1) / kRelabelChunk), (unsigned)nb);
   LAUNCHG(kb_relabel_compare, g, kThreads, L.d);
@@ -1017,7 +1017,7 @@ int compact(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   ctx->cur_fam = STSPIX_FAM_OTHER;
   LAUNCHB(kb_clear_flags, L.max_cap + 2, L, L.B);
   LAUNCHS(kb_scalars, L, L.B, (int)kOpCompactN);
-  LAUNCHB(kb_mark_present, L.max_npix, L, L.B, 1);
+  LAUNCHB(kb_mark_present, pix_units(L.max_npix), L, L.B, 1);
   LAUNCHG(kb_scan, (unsigned)L.B, 1024, L.d, 3);
   LAUNCHB(kb_compact_gather, L.max_cap, L, L.B);
   LAUNCHB(kb_compact_scatter, L.max_cap, L, L.B);
@@ -1030,10 +1030,10 @@ int compact(stspix_ctx* ctx, cudaStream_t st, const List& L) {
 int bass_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   if (L.B <= 0) return STSPIX_OK;
   ctx->cur_fam = STSPIX_FAM_OTHER;
-  LAUNCHB(kb_init_hex, L.max_npix, L, L.B);
+  LAUNCHG(kb_init_hex, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d);
   // compact the hex ids (extract_unique_ids + compactify, bass.cu:251-252)
   LAUNCHB(kb_clear_flags, L.max_cap + 2, L, L.B);
-  LAUNCHB(kb_mark_present, L.max_npix, L, L.B, 0);
+  LAUNCHB(kb_mark_present, pix_units(L.max_npix), L, L.B, 0);
   LAUNCHG(kb_scan, (unsigned)L.B, 1024, L.d, 0);
   LAUNCHB(kb_remap, pix_units(L.max_npix), L, L.B, 0);
   LAUNCHS(kb_scalars, L, L.B, (int)kOpAfterHex);
@@ -1187,17 +1187,17 @@ int shift_fill(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   LAUNCHG(kb_flow_pool, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d);
   LAUNCHB(kb_flow_mean, L.max_nprev, L, L.B);
   LAUNCHB(kb_shift, pix_units(L.max_npix), L, L.B);
-  LAUNCHB(kb_shift_decode, L.max_npix, L, L.B);
+  LAUNCHB(kb_shift_decode, pix_units(L.max_npix), L, L.B);
   LAUNCHG(kb_count_labels, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d, 0);
   // fill, invalidate disconnected, fill
   if ((r = run_fill(ctx, st, L))) return r;
   LAUNCHG(kb_cc_local, dim3((unsigned)(((L.max_w + 31) / 32) * ((L.max_h + 31) / 32)), (unsigned)L.B),
           kThreads, L.d);
-  LAUNCHB(kb_cc_hook, L.max_npix, L, L.B);
-  LAUNCHB(kb_cc_compress, L.max_npix, L, L.B);
+  LAUNCHB(kb_cc_hook, (long long)((L.max_w + 31) / 32) * ((L.max_h + 31) / 32) * (32 + 2 * 31), L, L.B);
+  LAUNCHB(kb_cc_compress, pix_units(L.max_npix), L, L.B);
   LAUNCHB(kb_cc_best, pix_units(L.max_npix), L, L.B);
   LAUNCHB(kb_cc_invalidate, pix_units(L.max_npix), L, L.B);
-  LAUNCHB(kb_list_holes, L.max_npix, L, L.B);
+  LAUNCHB(kb_list_holes, pix_units(L.max_npix), L, L.B);
   if ((r = run_fill(ctx, st, L))) return r;
   LAUNCHG(kb_count_labels, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d, 1);
   LAUNCHB(kb_shift_params, L.max_nprev, L, L.B);
@@ -1209,7 +1209,7 @@ int prop_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   if (L.B <= 0) return STSPIX_OK;
   ctx->cur_fam = STSPIX_FAM_OTHER;
   LAUNCHB(kb_write_params, L.max_cap, L, L.B);
-  LAUNCHB(kb_mark_active, L.max_npix, L, L.B);
+  LAUNCHB(kb_mark_active, pix_units(L.max_npix), L, L.B);
   return STSPIX_OK;
 }
 

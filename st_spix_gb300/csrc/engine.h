@@ -183,6 +183,12 @@ constexpr int kPixPerThread = 4;
 #define FOR_PIX(t, n)                                                                    \
   for (int j_ = 0, t = (int)blockIdx.x * (kPixPerThread * (int)blockDim.x) + (int)threadIdx.x; \
        j_ < kPixPerThread && t < (n); j_++, t += (int)blockDim.x)
+// Block-uniform form, for bodies with warp or block collectives: every thread of a block
+// runs the same iterations (t - threadIdx.x is the block's first pixel of the iteration),
+// so t may be >= n in the last one.
+#define FOR_PIX_ALL(t, n)                                                                \
+  for (int j_ = 0, t = (int)blockIdx.x * (kPixPerThread * (int)blockDim.x) + (int)threadIdx.x; \
+       j_ < kPixPerThread && t - (int)threadIdx.x < (n); j_++, t += (int)blockDim.x)
 #define SLOT_Z const Slot& S = slots[blockIdx.z]
 
 // ---------------------------------------------------------------------------

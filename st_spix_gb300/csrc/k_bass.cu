@@ -24,9 +24,9 @@ namespace stspix {
 // coordinates below x + y + 3s, the FP32 squared distance errs by less than
 // ~5e-6 s (x + y + 6s) + 1e-7 d2 px^2; the margin below exceeds twice that, so
 // every FP64 minimiser passes the filter and the label is the reference's.
-__device__ __forceinline__ int hex_label(int x, int y, double Hh, double w, int nx, int ny) {
-  const int r0 = (int)floor(y / (1.5 * Hh));
-  const int c0 = (int)floor(x / w);
+// r0, c0: the search window's centre row floor(y / (1.5 Hh)) and column floor(x / w).
+__device__ __forceinline__ int hex_label_rc(int x, int y, double Hh, double w, int nx, int ny,
+                                           int r0, int c0) {
   const float wf = (float)w, hf = (float)(1.5 * Hh), half = (float)(0.5 * w);
   const float xf = (float)x, yf = (float)y;
   float mn = 3.0e38f;
@@ -61,6 +61,9 @@ __device__ __forceinline__ int hex_label(int x, int y, double Hh, double w, int 
   }
   return best;
 }
+__device__ __forceinline__ int hex_label(int x, int y, double Hh, double w, int nx, int ny) {
+  return hex_label_rc(x, y, Hh, w, nx, ny, (int)floor(y / (1.5 * Hh)), (int)floor(x / w));
+}
 
 __global__ void k_init_hex(int* __restrict__ seg, int H, int W, double Hh, double w, int nx,
                            int ny) {
@@ -70,12 +73,28 @@ __global__ void k_init_hex(int* __restrict__ seg, int H, int W, double Hh, doubl
   seg[idx] = hex_label(idx % W, idx / W, Hh, w, nx, ny);
 }
 
-__global__ void kb_init_hex(const Slot* __restrict__ slots) {
+// Grid: the 64 x 32 tiles of a slot.  The window row depends on y only and the window
+// column on x only, so a block computes those of its 32 rows and 64 columns once (two
+// FP64 divisions per row or column instead of per pixel; this part issues FP64 slowly).
+__global__ void __launch_bounds__(256) kb_init_hex(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= S.npix) return;
-  S.seg[idx] = hex_label(idx % S.W, idx / S.W, S.hex_h, S.hex_w, S.hex_nx, S.hex_ny);
+  __shared__ int r0s[32], c0s[64];
+  const int W = S.W, H = S.H;
+  const int tiles_x = (W + 63) / 64;
+  if ((int)blockIdx.x >= tiles_x * ((H + 31) / 32)) return;
+  const int tx0 = (blockIdx.x % tiles_x) * 64, ty0 = (blockIdx.x / tiles_x) * 32;
+  const double Hh = S.hex_h, w = S.hex_w;
+  if (threadIdx.x < 32) r0s[threadIdx.x] = (int)floor((ty0 + (int)threadIdx.x) / (1.5 * Hh));
+  else if (threadIdx.x < 96) c0s[threadIdx.x - 32] = (int)floor((tx0 + (int)threadIdx.x - 32) / w);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 64 * 32; i += blockDim.x) {
+    const int lx = i & 63, ly = i >> 6;
+    const int x = tx0 + lx, y = ty0 + ly;
+    if (x < W && y < H)
+      S.seg[(size_t)y * W + x] =
+          hex_label_rc(x, y, Hh, w, S.hex_nx, S.hex_ny, r0s[ly], c0s[lx]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -85,13 +104,14 @@ __global__ void kb_init_hex(const Slot* __restrict__ slots) {
 __global__ void kb_mark_present(const Slot* __restrict__ slots, int mode) {
   pdl_enter();
   SLOT_Y;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lo = mode == 0 ? 0 : S.lo;
   const int hi = mode == 0 ? S.nraw - 1 : min(S.sc->max_spix, S.cap - 1);
-  const int v = i < S.npix ? S.seg[i] : -1;
-  // one store per distinct label of the warp (a warp's pixels are consecutive)
-  const unsigned peers = __match_any_sync(0xffffffffu, v);
-  if (v >= lo && v <= hi && (int)(threadIdx.x & 31) == __ffs(peers) - 1) S.flags[v - lo] = 1;
+  FOR_PIX_ALL(i, S.npix) {
+    const int v = i < S.npix ? S.seg[i] : -1;
+    // one store per distinct label of the warp (a warp's pixels are consecutive)
+    const unsigned peers = __match_any_sync(0xffffffffu, v);
+    if (v >= lo && v <= hi && (int)(threadIdx.x & 31) == __ffs(peers) - 1) S.flags[v - lo] = 1;
+  }
 }
 
 // One block per slot: exclusive scan of n byte flags (n up to a few 10^5), each

@@ -139,21 +139,22 @@ __device__ __forceinline__ void append_hole(const Slot& S, int t, bool hole, boo
   }
   __syncthreads();
   if (hole) S.smseg[base + woff[warp] + __popc(m & ((1u << lane) - 1))] = t;
+  __syncthreads();          // woff and base are free for the block's next call
 }
 
 __global__ void kb_shift_decode(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if ((int)(blockIdx.x * blockDim.x) >= S.npix) return;   // block-uniform
-  const bool in = t < S.npix;
-  int v = -1;
-  if (in) {
-    v = S.hits[t] > 0 ? (int)(unsigned int)S.best[t] : -1;
-    S.shifted[t] = v;
-    S.seg[t] = v;
+  FOR_PIX_ALL(t, S.npix) {
+    const bool in = t < S.npix;
+    int v = -1;
+    if (in) {
+      v = S.hits[t] > 0 ? (int)(unsigned int)S.best[t] : -1;
+      S.shifted[t] = v;
+      S.seg[t] = v;
+    }
+    append_hole(S, t, in && v < 0, true);
   }
-  append_hole(S, t, in && v < 0, true);
 }
 
 // Per-label pixel counts (get_spix_sizes, seg_utils.cu:56-75), by warp-block label
@@ -484,17 +485,23 @@ __global__ void __launch_bounds__(256) kb_cc_local(const Slot* __restrict__ slot
   if (!ok) atomicExch(&S.sc->status, STSPIX_ERR_ITER_LIMIT);
 }
 
-// The unions across tile edges (only pixels on a tile's first row or first / last
-// column have neighbours in another tile), on the global parents.
+// The unions across tile edges, on the global parents.  Only pixels on a tile's first
+// row or first / last column have neighbours in another tile: kCcEdge per tile, thread
+// u taking edge pixel u % kCcEdge of tile u / kCcEdge.
+constexpr int kCcEdge = kCcTile + 2 * (kCcTile - 1);
 __global__ void kb_cc_hook(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  const int W = S.W;
-  const int x = t % W, y = t / W;
-  const int lx = x % kCcTile, ly = y % kCcTile;
-  if (!(lx == 0 || ly == 0 || lx == kCcTile - 1)) return;
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  const int W = S.W, H = S.H;
+  const int tiles_x = (W + kCcTile - 1) / kCcTile;
+  const int tile = u / kCcEdge, e = u % kCcEdge;
+  if (tile >= tiles_x * ((H + kCcTile - 1) / kCcTile)) return;
+  const int lx = e < kCcTile ? e : (e < 2 * kCcTile - 1 ? 0 : kCcTile - 1);
+  const int ly = e < kCcTile ? 0 : (e < 2 * kCcTile - 1 ? e - kCcTile + 1 : e - 2 * kCcTile + 2);
+  const int x = (tile % tiles_x) * kCcTile + lx, y = (tile / tiles_x) * kCcTile + ly;
+  if (x >= W || y >= H) return;
+  const int t = y * W + x;
   const int* seg = S.seg;
   const int L = seg[t];
   if (L < 0) return;
@@ -508,14 +515,15 @@ __global__ void kb_cc_hook(const Slot* __restrict__ slots) {
 __global__ void kb_cc_compress(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  int r = -1;
-  if (t < S.npix && S.d1[t] >= 0) {
-    r = uf_find(S.d1, t);
-    S.d1[t] = r;
+  FOR_PIX_ALL(t, S.npix) {
+    int r = -1;
+    if (t < S.npix && S.d1[t] >= 0) {
+      r = uf_find(S.d1, t);
+      S.d1[t] = r;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, r);
+    if (r >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&S.d2[r], __popc(peers));
   }
-  const unsigned peers = __match_any_sync(0xffffffffu, r);
-  if (r >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&S.d2[r], __popc(peers));
 }
 
 __global__ void kb_cc_best(const Slot* __restrict__ slots) {
@@ -555,9 +563,7 @@ __global__ void kb_cc_invalidate(const Slot* __restrict__ slots) {
 __global__ void kb_list_holes(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if ((int)(blockIdx.x * blockDim.x) >= S.npix) return;   // block-uniform
-  append_hole(S, t, t < S.npix && S.seg[t] < 0, false);
+  FOR_PIX_ALL(t, S.npix) append_hole(S, t, t < S.npix && S.seg[t] < 0, false);
 }
 
 // invalid_counts / prior_counts update (shift_and_fill.cu:300-330).
@@ -632,10 +638,15 @@ __global__ void kb_mark_active(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.npix) return;
-  int v = S.seg[t];
-  if (v >= 0 && v < sp.cap) { sp.valid[v] = 1; sp.prop[v] = 1; }
+  FOR_PIX_ALL(t, S.npix) {
+    const int v = t < S.npix ? S.seg[t] : -1;
+    // one store per distinct label of the warp (a warp's pixels are consecutive)
+    const unsigned peers = __match_any_sync(0xffffffffu, v);
+    if (v >= 0 && v < sp.cap && (int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+      sp.valid[v] = 1;
+      sp.prop[v] = 1;
+    }
+  }
 }
 
 
@@ -660,12 +671,13 @@ __global__ void kb_living(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
   if (!S.mode) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int v = t < S.npix ? S.seg[t] : -1;
-  // one store per distinct label of the warp (a warp's pixels are consecutive)
-  const unsigned peers = __match_any_sync(0xffffffffu, v);
-  if (v >= 0 && v <= S.sc->max_spix && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
-    S.living[v] = 1;
+  const int ms = S.sc->max_spix;
+  FOR_PIX_ALL(t, S.npix) {
+    const int v = t < S.npix ? S.seg[t] : -1;
+    // one store per distinct label of the warp (a warp's pixels are consecutive)
+    const unsigned peers = __match_any_sync(0xffffffffu, v);
+    if (v >= 0 && v <= ms && (int)(threadIdx.x & 31) == __ffs(peers) - 1) S.living[v] = 1;
+  }
 }
 
 // find_most_similar_spix (relabel.cu:201-276): grid (s, candidate chunk of
