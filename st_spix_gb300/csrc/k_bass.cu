@@ -106,11 +106,10 @@ __global__ void kb_mark_present(const Slot* __restrict__ slots, int mode) {
   SLOT_Y;
   const int lo = mode == 0 ? 0 : S.lo;
   const int hi = mode == 0 ? S.nraw - 1 : min(S.sc->max_spix, S.cap - 1);
-  FOR_PIX_ALL(i, S.npix) {
-    const int v = i < S.npix ? S.seg[i] : -1;
-    // one store per distinct label of the warp (a warp's pixels are consecutive)
-    const unsigned peers = __match_any_sync(0xffffffffu, v);
-    if (v >= lo && v <= hi && (int)(threadIdx.x & 31) == __ffs(peers) - 1) S.flags[v - lo] = 1;
+  FOR_PIX(i, S.npix) {
+    // one store per run of equal labels (the run's first pixel)
+    const int v = S.seg[i];
+    if (v >= lo && v <= hi && (i == 0 || S.seg[i - 1] != v)) S.flags[v - lo] = 1;
   }
 }
 

@@ -444,43 +444,78 @@ __device__ __forceinline__ void cc_unions(const int* __restrict__ seg, int t, in
   }
 }
 
-// One block per 32 x 32 tile: parents of the tile's pixels by union-find in shared
-// memory over the unions inside the tile, then each pixel's global parent = its local
-// root (the smallest pixel index of its component within the tile: row-major order
-// within a tile is the frame's order).  Replaces the parent initialisation.
+// One block per 32 x 32 tile, a warp per tile row (tile rows are 32 pixels): each
+// pixel's parent starts as the first pixel of its run of equal labels in the row (one
+// ballot, no atomics), then union-find in shared memory (min-index hooking) joins the
+// runs.  A pixel p = (x, y) of label L unites, inside the tile, with
+//   N  when N has label L, unless the left pixel and NW both have label L (the left
+//      pixel is in p's run and NW in N's run, so the left pixel's union joins them);
+//   NW when neither the left pixel nor N has label L and NW has;
+//   NE when N does not have label L and NE has
+// (the 8-connected rule of cc_unions with the W unions given by the runs).  At the
+// tile's first column the left pixel is in another tile: no skip there, and the pairs
+// across tile edges are kb_cc_hook's.  Then each pixel's global parent = its local root
+// (the smallest pixel index of its component in the tile: row-major order within a
+// tile is the frame's order).  Replaces the parent initialisation.
 __global__ void __launch_bounds__(256) kb_cc_local(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
+  static_assert(kCcTile == 32, "a tile row is a warp");
+  constexpr int kRows = kCcTile / 8;        // rows per warp
+  __shared__ int lab[kCcTile][kCcTile];
   __shared__ int par[kCcTile * kCcTile];
   const int W = S.W, H = S.H;
   const int tiles_x = (W + kCcTile - 1) / kCcTile;
   if ((int)blockIdx.x >= tiles_x * ((H + kCcTile - 1) / kCcTile)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) S.sc->nhole = 0;
   const int tx0 = (blockIdx.x % tiles_x) * kCcTile, ty0 = (blockIdx.x / tiles_x) * kCcTile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int x = tx0 + lane;
   const int* seg = S.seg;
-  auto gidx = [&](int li) { return (ty0 + li / kCcTile) * W + tx0 + li % kCcTile; };
-  auto lidx = [&](int g) { return (g / W - ty0) * kCcTile + (g % W - tx0); };
-  for (int li = threadIdx.x; li < kCcTile * kCcTile; li += blockDim.x) {
-    const int x = tx0 + li % kCcTile, y = ty0 + li / kCcTile;
-    par[li] = (x < W && y < H && seg[gidx(li)] >= 0) ? li : -1;
+  int v[kRows];
+#pragma unroll
+  for (int a = 0; a < kRows; a++) {
+    const int y = ty0 + warp * kRows + a;
+    v[a] = (x < W && y < H) ? seg[(size_t)y * W + x] : -1;
+  }
+#pragma unroll
+  for (int a = 0; a < kRows; a++) {
+    const int ly = warp * kRows + a;
+    lab[ly][lane] = v[a];
+    const int left = __shfl_up_sync(0xffffffffu, v[a], 1);
+    const unsigned cont = __ballot_sync(0xffffffffu, lane > 0 && v[a] >= 0 && v[a] == left);
+    const unsigned starts = ~cont & (0xffffffffu >> (31 - lane));   // run starts at lanes <= lane
+    par[ly * kCcTile + lane] = v[a] >= 0 ? ly * kCcTile + (31 - __clz(starts)) : -1;
   }
   __syncthreads();
   bool ok = true;
-  for (int li = threadIdx.x; li < kCcTile * kCcTile; li += blockDim.x) {
-    const int x = tx0 + li % kCcTile, y = ty0 + li / kCcTile;
-    if (x >= W || y >= H) continue;
-    const int t = gidx(li);
-    const int L = seg[t];
-    if (L < 0) continue;
-    cc_unions(seg, t, W, L, true, [&](int tn) { ok &= uf_unite(par, li, lidx(tn)); });
+#pragma unroll
+  for (int a = 0; a < kRows; a++) {
+    const int ly = warp * kRows + a;
+    const int L = v[a];
+    if (L < 0 || ly == 0) continue;
+    const int li = ly * kCcTile + lane;
+    const int n = lab[ly - 1][lane];
+    const bool w = lane > 0 && lab[ly][lane - 1] == L;
+    const int nw = lane > 0 ? lab[ly - 1][lane - 1] : -1;
+    const int ne = lane < kCcTile - 1 ? lab[ly - 1][lane + 1] : -1;
+    if (n == L) {
+      if (!(w && nw == L)) ok &= uf_unite(par, li, li - kCcTile);
+    } else {
+      if (!w && nw == L) ok &= uf_unite(par, li, li - kCcTile - 1);
+      if (ne == L) ok &= uf_unite(par, li, li - kCcTile + 1);
+    }
   }
   __syncthreads();
-  for (int li = threadIdx.x; li < kCcTile * kCcTile; li += blockDim.x) {
-    const int x = tx0 + li % kCcTile, y = ty0 + li / kCcTile;
+#pragma unroll
+  for (int a = 0; a < kRows; a++) {
+    const int ly = warp * kRows + a;
+    const int y = ty0 + ly;
     if (x >= W || y >= H) continue;
+    const int li = ly * kCcTile + lane;
     const int r = par[li] >= 0 ? uf_find(par, li) : -1;
     if (par[li] >= 0 && r < 0) ok = false;
-    S.d1[gidx(li)] = r >= 0 ? gidx(r) : -1;
+    S.d1[(size_t)y * W + x] = r >= 0 ? (ty0 + r / kCcTile) * W + tx0 + r % kCcTile : -1;
   }
   if (!ok) atomicExch(&S.sc->status, STSPIX_ERR_ITER_LIMIT);
 }
@@ -638,11 +673,10 @@ __global__ void kb_mark_active(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
-  FOR_PIX_ALL(t, S.npix) {
-    const int v = t < S.npix ? S.seg[t] : -1;
-    // one store per distinct label of the warp (a warp's pixels are consecutive)
-    const unsigned peers = __match_any_sync(0xffffffffu, v);
-    if (v >= 0 && v < sp.cap && (int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+  FOR_PIX(t, S.npix) {
+    // one store per run of equal labels (the run's first pixel)
+    const int v = S.seg[t];
+    if (v >= 0 && v < sp.cap && (t == 0 || S.seg[t - 1] != v)) {
       sp.valid[v] = 1;
       sp.prop[v] = 1;
     }
@@ -672,11 +706,10 @@ __global__ void kb_living(const Slot* __restrict__ slots) {
   SLOT_Y;
   if (!S.mode) return;
   const int ms = S.sc->max_spix;
-  FOR_PIX_ALL(t, S.npix) {
-    const int v = t < S.npix ? S.seg[t] : -1;
-    // one store per distinct label of the warp (a warp's pixels are consecutive)
-    const unsigned peers = __match_any_sync(0xffffffffu, v);
-    if (v >= 0 && v <= ms && (int)(threadIdx.x & 31) == __ffs(peers) - 1) S.living[v] = 1;
+  FOR_PIX(t, S.npix) {
+    // one store per run of equal labels (the run's first pixel)
+    const int v = S.seg[t];
+    if (v >= 0 && v <= ms && (t == 0 || S.seg[t - 1] != v)) S.living[v] = 1;
   }
 }
 
