@@ -218,7 +218,7 @@ __device__ void bfs_bits(int t, int k, int x0, int y0, int bw, int bh, int W,
 // f1, f2 and visited v1, v2.  A layer is shifts within a row, the rows above and below
 // from the lane's own rows or one shuffle, and the masks: no shared memory, no barrier.
 // The seeds come as pixel indices (split_seed_index), so the box's distances are not
-// read.
+// read; only the comparison d1 > d2 is written, once, at the end.
 template <int R, int C>
 __device__ __forceinline__ void bfs_reg(int k, int x0, int y0, int bw, int bh, int W,
                                         const int* __restrict__ seg, int* d1, int* d2,
@@ -294,27 +294,52 @@ __device__ __forceinline__ void bfs_reg(int k, int x0, int y0, int bw, int bh, i
       for (int w = 0; w < C; w++) { f[j][w] = n[j][w]; v[j][w] |= n[j][w]; any |= n[j][w]; }
     return any;
   };
-  auto write = [&](const u64 (&f)[R][C], int* d, int val) {
+  // The split's only use of the distances is d1 > d2 (kb_split_partition): true where seed
+  // 1 reaches a pixel and seed 2 reaches it strictly later or never.  early2: pixels seed 2
+  // reached in a layer where seed 1 had not (yet) reached them, seed 2 itself included.
+  u64 early2[R][C];
 #pragma unroll
-    for (int j = 0; j < R; j++)
+  for (int j = 0; j < R; j++)
 #pragma unroll
-      for (int w = 0; w < C; w++)
-        if (f[j][w]) {
-          int* row = d + (size_t)(y0 + lane * R + j) * W + x0 + 64 * w;
-          for (u64 b = f[j][w]; b; b &= b - 1) row[__ffsll((long long)b) - 1] = val;
-        }
-  };
+    for (int w = 0; w < C; w++) early2[j][w] = f2[j][w] & ~f1[j][w];
   const int area = bw * bh;
   for (int L = 1; L <= area + 1; L++) {
     const u64 a1 = layer(f1, v1);
     const u64 a2 = layer(f2, v2);
-    write(f1, d1, L + 1);
-    write(f2, d2, L + 1);
+#pragma unroll
+    for (int j = 0; j < R; j++)
+#pragma unroll
+      for (int w = 0; w < C; w++) early2[j][w] |= f2[j][w] & ~v1[j][w];
     if (!__any_sync(0xffffffffu, (a1 | a2) != 0ull)) break;
+  }
+  // Distances that give the same comparison: d2 keeps -1 but 1 at seed 2 (kb_split_seed),
+  // so d1 := 2 on the pixels with d1 > d2 and d1 := -1 at seed 1 when it has not.
+#pragma unroll
+  for (int j = 0; j < R; j++)
+#pragma unroll
+    for (int w = 0; w < C; w++) {
+      const u64 second = v1[j][w] & (~v2[j][w] | early2[j][w]);
+      if (second) {
+        int* row = d1 + (size_t)(y0 + lane * R + j) * W + x0 + 64 * w;
+        for (u64 b = second; b; b &= b - 1) row[__ffsll((long long)b) - 1] = 2;
+      }
+    }
+  if (seed1 >= 0) {
+    // the seed's word selected by masks (an indexed read would put the arrays in local
+    // memory)
+    const int r1 = seed1 / W - y0 - lane * R, c1 = seed1 % W - x0;
+    u64 word = 0;
+#pragma unroll
+    for (int j = 0; j < R; j++)
+#pragma unroll
+      for (int w = 0; w < C; w++)
+        word |= (v1[j][w] & (~v2[j][w] | early2[j][w])) &
+                (0ull - (u64)(r1 == j && (c1 >> 6) == w));
+    if (r1 >= 0 && r1 < R && !((word >> (c1 & 63)) & 1ull)) d1[seed1] = -1;
   }
 }
 
-__global__ void __launch_bounds__(128) kb_split_bfs(const Slot* __restrict__ slots, int dir_bass,
+__global__ void __launch_bounds__(128, 4) kb_split_bfs(const Slot* __restrict__ slots, int dir_bass,
                                                     int dir_prop) {
   pdl_enter();
   SLOT_Y;
