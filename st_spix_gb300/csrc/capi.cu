@@ -324,7 +324,7 @@ constexpr long long kPixBytes = 1 + 5 * 4 + 8 + 4 + 2;        // border, d1 d2 s
 constexpr long long kSpDevBytes = 4 + 1 + 1 + 4 + 4 + 4 + 12 + 16 + 24 + 8 + 12 + 16 + 24 + 24 + 24 +
                                   64 + (long long)sizeof(SweepRec);
 constexpr long long kSmBytes = 4 + 24 + 24 + 4 + 4 + 4 + 4 + 4 + 1 + 8;
-constexpr long long kAuxBytes = 5 * 1 + 6 * 4 + 16 + 8 + 4 + 16 + 8 + 8 + 72 + 4 + 1;
+constexpr long long kAuxBytes = 5 * 1 + 6 * 4 + 16 + 8 + 4 + 16 + 8 + 8 + 72 + 4 + 1 + 24;
 constexpr long long kParamBytes = 12 + 12 + 16 + 24 + 4 + 16 + 24 + 24 + 4 + 4 + 4 + 4 + 4;
 
 // Make sure slot position i holds npix pixels and sp_cap superpixels.  Growing
@@ -367,6 +367,7 @@ int ensure_slot(stspix_ctx* ctx, int i, int npix, int sp_cap) {
     AL(L, s.centers, 2 * c2); AL(L, s.rbest, c2); AL(L, s.ccbest, c2);
     AL(L, s.bbox, 4 * c2);
     AL(L, s.snap, 9 * c2); AL(L, s.post_ids, c2); AL(L, s.recchg, c2);
+    AL(L, s.pscache, 3 * c2);
     w.sp_cap = cap;
   }
   return STSPIX_OK;
@@ -666,7 +667,7 @@ int update_params(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
   // when a slot lists more groups)
   const unsigned pg = (unsigned)std::min<long long>((L.max_cap + 31) / 32,
                                                     std::max(32, (4 * ctx->num_sms + nb - 1) / nb));
-  LAUNCHG(kb_posterior, dim3(pg, (unsigned)nb), 128, L.d);
+  LAUNCHG(kb_posterior, dim3(pg, (unsigned)nb), 128, L.d, incremental ? 1 : 0);
   return STSPIX_OK;
 }
 

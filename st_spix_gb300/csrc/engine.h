@@ -166,6 +166,7 @@ struct Slot {
   int* bbox;               // [4*(cap+2)]: x0, x1, y0, y1 per superpixel (split BFS)
   long long* snap;         // [9*(cap+2)]: count and the 8 sums each id's posterior last saw
   uint8_t* recchg;         // [cap+2]: the last posterior changed the id's SweepRec
+  double* pscache;         // [3*(cap+2)]: the prior shape term of the last full posterior
   int* post_ids;           // [cap+2]: ids of the running posterior (kb_post_list)
   Scalars* sc;
   int tile_base[3];        // first sweep tile of this slot in the batch (32-, 64-, 16-wide)

@@ -364,7 +364,7 @@ __device__ __forceinline__ void block_stats(const Slot& S, int bx, int by, float
 // Grid: the 64 x 32 tiles of the first B slots (a block finds its slot by binary
 // search over the slots' first tiles); warp w takes the tile's 32 x 8 block
 // (w & 1, w >> 1).
-__global__ void __launch_bounds__(256) kb_accumulate(const Slot* __restrict__ slots, int B) {
+__global__ void __launch_bounds__(256, 4) kb_accumulate(const Slot* __restrict__ slots, int B) {
   pdl_enter();
   if (B <= 0) return;
   const int t = blockIdx.x;
@@ -485,8 +485,10 @@ __device__ __forceinline__ void smooth_prior(double in_x, double in_y, double in
 // mean and scatter; then warps 0-2 one smoothed covariance entry each, then warps 0-2
 // one inverse entry each and warp 3 the log determinant.  Every value is the same
 // expression as a single-thread evaluation, exchanged through shared memory.
-// k: this lane's id (-1: none).
-__device__ __forceinline__ void posterior_ids(const Slot& S, int k) {
+// k: this lane's id (-1: none).  cached: the prior shape term is read from S.pscache,
+// which the last full posterior wrote (incremental posteriors: the priors, flags and
+// sample covariance it depends on change only in the steps followed by a full one).
+__device__ __forceinline__ void posterior_ids(const Slot& S, int k, bool cached) {
   __shared__ double v_ps[3][32], v_raw[3][32], v_m[2][32], v_s[3][32], v_i[4][32];
   __shared__ float v_app[3][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -506,10 +508,15 @@ __device__ __forceinline__ void posterior_ids(const Slot& S, int k) {
     if (w == 0) { a0 = a[0]; a1 = a[1]; a2 = a[2]; }
     else if (w == 1) {
       pc = sp.prior_count[k];
-      prop = sp.prop[k];
-      q0 = sp.sample_sigma_shape[3 * k]; q1 = sp.sample_sigma_shape[3 * k + 1];
-      q2 = sp.sample_sigma_shape[3 * k + 2];
-      i0 = sp.prior_icov[3 * k]; i1 = sp.prior_icov[3 * k + 1]; i2 = sp.prior_icov[3 * k + 2];
+      if (cached) {
+        q0 = S.pscache[3 * (size_t)k]; q1 = S.pscache[3 * (size_t)k + 1];
+        q2 = S.pscache[3 * (size_t)k + 2];
+      } else {
+        prop = sp.prop[k];
+        q0 = sp.sample_sigma_shape[3 * k]; q1 = sp.sample_sigma_shape[3 * k + 1];
+        q2 = sp.sample_sigma_shape[3 * k + 2];
+        i0 = sp.prior_icov[3 * k]; i1 = sp.prior_icov[3 * k + 1]; i2 = sp.prior_icov[3 * k + 2];
+      }
     } else if (w == 2) { a0 = a[3]; a1 = a[4]; a2 = a[5]; a3 = a[6]; a4 = a[7]; }
     if (w != 1) pc = sp.prior_count[k];
   }
@@ -535,18 +542,23 @@ __device__ __forceinline__ void posterior_ids(const Slot& S, int k) {
       }
     } else if (w == 1) {
       // prior shape term (calc_simple_update with _add_sigma_smoothing)
-      double px, py, pz;
-      if (prop) {
-        smooth_prior(q0, q1, q2, (int)pc, pc, S.sp_size, &px, &py, &pz);
+      if (cached) {
+        v_ps[0][lane] = q0; v_ps[1][lane] = q1; v_ps[2][lane] = q2;
       } else {
-        px = i0; py = i1; pz = i2;
+        double px, py, pz;
+        if (prop) {
+          smooth_prior(q0, q1, q2, (int)pc, pc, S.sp_size, &px, &py, &pz);
+        } else {
+          px = i0; py = i1; pz = i2;
+        }
+        double pr_det = px * pz - py * py;
+        if (!(pr_det > 0)) atomicExch(&S.sc->status, STSPIX_ERR_DEGENERATE);
+        pr_det = sqrt(pr_det);
+        const double t0 = pc / pr_det * px, t1 = pc / pr_det * py, t2 = pc / pr_det * pz;
+        v_ps[0][lane] = t0; v_ps[1][lane] = t1; v_ps[2][lane] = t2;
+        S.pscache[3 * (size_t)k] = t0; S.pscache[3 * (size_t)k + 1] = t1;
+        S.pscache[3 * (size_t)k + 2] = t2;
       }
-      double pr_det = px * pz - py * py;
-      if (!(pr_det > 0)) atomicExch(&S.sc->status, STSPIX_ERR_DEGENERATE);
-      pr_det = sqrt(pr_det);
-      v_ps[0][lane] = pc / pr_det * px;
-      v_ps[1][lane] = pc / pr_det * py;
-      v_ps[2][lane] = pc / pr_det * pz;
     } else if (w == 2) {
       // shape mean and scatter
       const double mx = a0 / count, my = a1 / count;
@@ -648,14 +660,15 @@ __global__ void kb_post_list(const Slot* __restrict__ slots, int incremental) {
 // A group's barriers are block-uniform, and the first barrier of the next group follows
 // every read of the previous one's shared values.  The last block of a slot to finish
 // clears the list for the next posterior (every block read the list length first).
-__global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slots) {
+__global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slots,
+                                                    int incremental) {
   pdl_enter();
   SLOT_Y;
   Scalars* sc = S.sc;
   const int n = *(volatile int*)&sc->npost;
   for (int g = blockIdx.x; g * 32 < n; g += gridDim.x) {
     const int i = g * 32 + (threadIdx.x & 31);
-    posterior_ids(S, i < n ? S.post_ids[i] : -1);
+    posterior_ids(S, i < n ? S.post_ids[i] : -1, incremental != 0);
   }
   __syncthreads();
   if (threadIdx.x == 0) {

@@ -463,7 +463,7 @@ __global__ void kb_sm_clear(const Slot* __restrict__ slots) {
 // one set of atomics.  Unit colours (all of the warp's in [0, 1]) are summed in 32 bits;
 // other colours wait in shared memory and a lane converts each pixel in its label's round.
 // Integer sums (R1): totals do not depend on the grouping.
-__global__ void __launch_bounds__(256) kb_sm_accumulate(const Slot* __restrict__ slots, int split) {
+__global__ void __launch_bounds__(256, 4) kb_sm_accumulate(const Slot* __restrict__ slots, int split) {
   pdl_enter();
   SLOT_Y;
   __shared__ float cs[8][8][3][32];   // [warp][row][channel][lane]

@@ -29,7 +29,7 @@ __global__ void kb_init_bass_params(const Slot* slots);
 __global__ void kb_init_prior_mu(const Slot* slots);
 __global__ void kb_clear_stats(const Slot* slots);
 __global__ void kb_accumulate(const Slot* slots, int B);
-__global__ void kb_posterior(const Slot* slots);
+__global__ void kb_posterior(const Slot* slots, int incremental);
 __global__ void kb_post_list(const Slot* slots, int incremental);
 __global__ void kb_accumulate_fp(const Slot* slots, int mode);
 __global__ void kb_accumulate_fp_store(const Slot* slots, int mode);
