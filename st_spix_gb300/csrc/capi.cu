@@ -893,7 +893,8 @@ int run_split(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
   LAUNCHB(kb_split_partition, pix_units(L.max_npix), L, nb);
   LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
   LAUNCHG(kb_sm_accumulate, dim3(tiles64(L), (unsigned)nb), kThreads, L.d, 1);
-  LAUNCHB(kb_split_decide, L.max_cap, L, nb, K, cfg.split_alpha);
+  LAUNCHG(kb_split_decide, dim3((unsigned)((L.max_cap + 31) / 32), (unsigned)nb), 128, L.d, K,
+          cfg.split_alpha);
   LAUNCHG(kb_scan, (unsigned)nb, 1024, L.d, 1);
   LAUNCHB(kb_split_commit, L.max_cap, L, nb);
   LAUNCHB(kb_split_apply, pix_units(L.max_npix), L, nb);
@@ -927,8 +928,9 @@ int run_merge(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb, const SmC
   LAUNCHB(kb_merge_candidates, pix_units(L.max_npix), L, nb, dir_b, dir_p);
   LAUNCHB(kb_sm_clear, L.max_cap + 2, L, nb);
   LAUNCHG(kb_sm_accumulate, dim3(tiles64(L), (unsigned)nb), kThreads, L.d, 0);
-  LAUNCHB(kb_merge_single, L.max_cap, L, nb, K);
-  LAUNCHB(kb_merge_decide, L.max_cap, L, nb, K, cfg.merge_alpha);
+  LAUNCHG(kb_merge_single, dim3((unsigned)((L.max_cap + 31) / 32), (unsigned)nb), 128, L.d, K);
+  LAUNCHG(kb_merge_decide, dim3((unsigned)((L.max_cap + 31) / 32), (unsigned)nb), 128, L.d, K,
+          cfg.merge_alpha);
   LAUNCHB(kb_merge_flag, L.max_cap, L, nb);
   LAUNCHB(kb_merge_remove, L.max_cap, L, nb);
   LAUNCHB(kb_merge_apply, pix_units(L.max_npix), L, nb);

@@ -565,42 +565,87 @@ __global__ void __launch_bounds__(256, 4) kb_sm_accumulate(const Slot* __restric
 // the identical lgamma(a_n) terms cancelled and log b_0 - log b_n evaluated as
 // -log1p((b_n - b_0) / b_0); b_n = b_0 + 0.5 (sum v^2 - (sum v)^2 / n)
 // (:480-501).  `clamp` is the merge path's b_n < 0 -> 0.1 rule.
-__device__ __forceinline__ double total_marginal(double n, const SmConsts& K, const long long* s,
-                                                 const long long* sq, bool clamp) {
+// In two parts, so the decision kernels can spread one id's terms over warps: a channel's
+// log ratio, and the sum over the channels in this order.
+__device__ __forceinline__ double marginal_lr(double n, const SmConsts& K, long long s, long long sq,
+                                              bool clamp) {
+  const double S = fx_unq(s, kFxAppShift), Q = fx_unq(sq, kFxSqShift);
+  const double d = 0.5 * (Q - S * S / n);
+  return (clamp && K.b0 + d < 0) ? K.log_01_b0 : log1p(d / K.b0);
+}
+__device__ __forceinline__ double marginal_sum(double n, const SmConsts& K, double lr0, double lr1,
+                                               double lr2, double logn) {
   const double a_n = 1e4 + n / 2;
   double t = 0;
-  for (int c = 0; c < 3; c++) {
-    double S = fx_unq(s[c], kFxAppShift), Q = fx_unq(sq[c], kFxSqShift);
-    double d = 0.5 * (Q - S * S / n);
-    double lr = (clamp && K.b0 + d < 0) ? K.log_01_b0 : log1p(d / K.b0);
-    t += -a_n * lr;
-  }
-  return t + 3 * (-0.5 * log(n) - n * K.lc);
+  t += -a_n * lr0;
+  t += -a_n * lr1;
+  t += -a_n * lr2;
+  return t + 3 * (-0.5 * logn - n * K.lc);
 }
 __device__ __forceinline__ bool near_tie(double h) { return fabs(h + 2.0) < 1e-6; }
 
 // update_split_flag (split_merge_orig.cu:900-986) / update_split_flag_p
 // (split_merge_prop.cu:3026-3149): decision only; ids by scan afterwards (R2).
-__device__ __forceinline__ void split_decide_one(const SpDev& sp, const SmDev& sm, Scalars* sc,
-                                                 const SmConsts& K, float split_alpha,
-                                                 int prop_mode, uint8_t* __restrict__ accept,
-                                                 int k) {
-  accept[k] = 0;
-  if (!sc->tmp0 || !sp.valid[k]) return;
-  const int off = sc->tmp1;
-  int s = k + off;
-  if (s >= sc->nbuf_logical || s >= sp.cap + 2) return;
-  double count_f = sp.count[k], count_k = sm.count[k], count_s = sm.count[s];
-  if (count_f < 1 || count_k < 1 || count_s < 1) return;
-  if (count_f != count_k + count_s) return;
-  long long sq_f[3];
-  for (int c = 0; c < 3; c++) sq_f[c] = sm.sq[3 * (size_t)k + c] + sm.sq[3 * (size_t)s + c];
-  double mk = total_marginal(count_k, K, &sm.s[3 * (size_t)k], &sm.sq[3 * (size_t)k], false);
-  double ms = total_marginal(count_s, K, &sm.s[3 * (size_t)s], &sm.sq[3 * (size_t)s], false);
-  double mf = total_marginal(count_f, K, sp.acc + 8 * (size_t)k, sq_f, false);
-  double h = mk + ms - mf + split_alpha;
+// One block per 32 consecutive ids, the FP64 terms of an id spread over the 4 warps (this
+// part issues FP64 slowly; each warp runs on its own scheduler): warp m < 3 the three
+// channel log ratios of marginal m (0: k's half, 1: s's half, 2: the whole superpixel),
+// warp 3 the three log counts; warp 0 then adds them in marginal_sum's order and
+// decides.  Every value is the same expression as a single-thread evaluation.
+__global__ void __launch_bounds__(128) kb_split_decide(const Slot* __restrict__ slots, SmConsts K,
+                                                       float split_alpha) {
+  pdl_enter();
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const SmDev& sm = S.sm;
+  Scalars* sc = S.sc;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  if ((int)blockIdx.x * 32 >= sp.cap) return;             // block-uniform
+  __shared__ double t_lr[3][3][32], t_log[3][32];
+  // the preconditions, evaluated alike by every warp
+  bool ok = false;
+  int s = 0;
+  double cnt[3] = {0, 0, 0};                                // k's half, s's half, whole
+  if (k < sp.cap) {
+    if (w == 0) S.accept[k] = 0;
+    if (sc->tmp0 && sp.valid[k]) {
+      s = k + sc->tmp1;
+      if (s < sc->nbuf_logical && s < sp.cap + 2) {
+        cnt[2] = sp.count[k];
+        cnt[0] = sm.count[k];
+        cnt[1] = sm.count[s];
+        ok = cnt[2] >= 1 && cnt[0] >= 1 && cnt[1] >= 1 && cnt[2] == cnt[0] + cnt[1];
+      }
+    }
+  }
+  if (!__syncthreads_or(ok)) return;
+  if (ok) {
+    if (w < 3) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        long long sv, qv;
+        if (w == 0) { sv = sm.s[3 * (size_t)k + c]; qv = sm.sq[3 * (size_t)k + c]; }
+        else if (w == 1) { sv = sm.s[3 * (size_t)s + c]; qv = sm.sq[3 * (size_t)s + c]; }
+        else { sv = sp.acc[8 * (size_t)k + c]; qv = sm.sq[3 * (size_t)k + c] + sm.sq[3 * (size_t)s + c]; }
+        const double nm = w == 0 ? cnt[0] : (w == 1 ? cnt[1] : cnt[2]);
+        t_lr[w][c][lane] = marginal_lr(nm, K, sv, qv, false);
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < 3; m++) t_log[m][lane] = log(cnt[m]);
+    }
+  }
+  __syncthreads();
+  if (w != 0 || !ok) return;
+  double mm[3];
+#pragma unroll
+  for (int m = 0; m < 3; m++)
+    mm[m] = marginal_sum(cnt[m], K, t_lr[m][0][lane], t_lr[m][1][lane], t_lr[m][2][lane],
+                         t_log[m][lane]);
+  const double count_k = cnt[0], count_s = cnt[1];
+  double h = mm[0] + mm[1] - mm[2] + split_alpha;
   uint8_t fl = 1;
-  if (prop_mode) {
+  if (S.mode) {
     bool is_prop = sp.prop[k];
     int ninv_k = sm.ninvalid[k], ninv_s = sm.ninvalid[s];
     bool prop_k = (ninv_k <= ninv_s);
@@ -613,13 +658,7 @@ __device__ __forceinline__ void split_decide_one(const SpDev& sp, const SmDev& s
     if (prop_k) fl |= 16;              // keep prior count on k
   }
   if (near_tie(h)) atomicAdd(&sc->near_ties, 1);
-  if (h > -2) accept[k] = fl;
-}
-
-__global__ void kb_split_decide(const Slot* __restrict__ slots, SmConsts K, float split_alpha) {
-  pdl_enter();
-  SLOT_Y;
-  FOR_SP(k, S.sp.cap) split_decide_one(S.sp, S.sm, S.sc, K, split_alpha, S.mode, S.accept, k);
+  if (h > -2) S.accept[k] = fl;
 }
 
 // Split commit: new id = max_spix + 1 + rank (R2), prior counts.
@@ -737,40 +776,81 @@ __global__ void kb_merge_candidates(const Slot* __restrict__ slots, int dir_bass
 }
 
 // Single-superpixel marginal, present only when k has its own candidate
-// (calc_merge_stats_step0 computes b_n only then; split_merge_orig.cu:456-520).
-__global__ void kb_merge_single(const Slot* __restrict__ slots, SmConsts K) {
+// (calc_merge_stats_step0 computes b_n only then; split_merge_orig.cu:456-520).  One block
+// per 32 ids: warps 0-2 one channel's log ratio each, warp 3 the log count, warp 0 adds.
+__global__ void __launch_bounds__(128) kb_merge_single(const Slot* __restrict__ slots, SmConsts K) {
   pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
   const SmDev& sm = S.sm;
-  FOR_SP(k, sp.cap) {
-    sm.flag[k] = 0;
-    if (!sp.valid[k] || sm.pair[k] < 0) continue;
-    sm.msingle[k] = total_marginal(sp.count[k], K, sp.acc + 8 * (size_t)k,
-                                   &sm.sq[3 * (size_t)k], true);
-    sm.flag[k] = 16;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  if ((int)blockIdx.x * 32 >= sp.cap) return;             // block-uniform
+  __shared__ double t_lr[3][32], t_log[32];
+  bool ok = false;
+  double n = 0;
+  if (k < sp.cap) {
+    if (w == 0) sm.flag[k] = 0;
+    ok = sp.valid[k] && sm.pair[k] >= 0;
+    if (ok) n = sp.count[k];
   }
+  if (!__syncthreads_or(ok)) return;
+  if (ok) {
+    if (w < 3) t_lr[w][lane] = marginal_lr(n, K, sp.acc[8 * (size_t)k + w], sm.sq[3 * (size_t)k + w], true);
+    else t_log[lane] = log(n);
+  }
+  __syncthreads();
+  if (w != 0 || !ok) return;
+  sm.msingle[k] = marginal_sum(n, K, t_lr[0][lane], t_lr[1][lane], t_lr[2][lane], t_log[lane]);
+  sm.flag[k] = 16;
 }
 
-// calc_merge_stats_step2 + update_merge_flag (split_merge_orig.cu:555-656), R3.
-__device__ __forceinline__ void merge_decide_one(const SpDev& sp, const SmDev& sm, Scalars* sc,
-                                                 const SmConsts& K, float merge_alpha, int k) {
-  if (!sp.valid[k]) return;
-  int f = sm.pair[k];
-  if (f < 0 || !sp.valid[f]) return;
-  double count_k = sp.count[k];
-  double count_f = sp.count[k] + sp.count[f];
-  if (count_k < 1 || count_f < 1) return;
-  long long s_f[3], sq_f[3];
-  for (int c = 0; c < 3; c++) {
-    s_f[c] = sp.acc[8 * (size_t)k + c] + sp.acc[8 * (size_t)f + c];
-    sq_f[c] = sm.sq[3 * (size_t)k + c] + sm.sq[3 * (size_t)f + c];
+// calc_merge_stats_step2 + update_merge_flag (split_merge_orig.cu:555-656), R3.  One
+// block per 32 ids (only valid ids decide, and none lies above the largest id in use):
+// warps 0-2 one channel's log ratio of the merged pair each, warp 3 the log count, warp 0
+// adds and decides.
+__global__ void __launch_bounds__(128) kb_merge_decide(const Slot* __restrict__ slots, SmConsts K,
+                                                       float merge_alpha) {
+  pdl_enter();
+  SLOT_Y;
+  const SpDev& sp = S.sp;
+  const SmDev& sm = S.sm;
+  Scalars* sc = S.sc;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  const int n_ids = min(sp.cap, sc->max_spix + 1);
+  if ((int)blockIdx.x * 32 >= n_ids) return;              // block-uniform
+  __shared__ double t_lr[3][32], t_log[32];
+  bool ok = false;
+  int f = -1;
+  double count_k = 0, count_f = 0;
+  if (k < n_ids && sp.valid[k]) {
+    f = sm.pair[k];
+    if (f >= 0 && sp.valid[f]) {
+      count_k = sp.count[k];
+      count_f = sp.count[k] + sp.count[f];
+      ok = count_k >= 1 && count_f >= 1;
+    }
   }
+  if (!__syncthreads_or(ok)) return;
+  const bool calc = ok && (sm.flag[f] & 16);
+  if (calc) {
+    if (w < 3) {
+      const long long sv = sp.acc[8 * (size_t)k + w] + sp.acc[8 * (size_t)f + w];
+      const long long qv = sm.sq[3 * (size_t)k + w] + sm.sq[3 * (size_t)f + w];
+      t_lr[w][lane] = marginal_lr(count_f, K, sv, qv, true);
+    } else {
+      t_log[lane] = log(count_f);
+    }
+  }
+  __syncthreads();
+  if (w != 0 || !ok) return;
   double h;
-  if (!(sm.flag[f] & 16)) {
+  if (!calc) {
     h = -INFINITY;
   } else {
-    double m_merged = total_marginal(count_f, K, s_f, sq_f, true);
+    const double m_merged =
+        marginal_sum(count_f, K, t_lr[0][lane], t_lr[1][lane], t_lr[2][lane], t_log[lane]);
     h = m_merged - (K.log_alpha + sm.msingle[k] + sm.msingle[f]) + merge_alpha;
   }
   if (near_tie(h)) atomicAdd(&sc->near_ties, 1);
@@ -778,14 +858,6 @@ __device__ __forceinline__ void merge_decide_one(const SpDev& sp, const SmDev& s
     sm.flag[k] |= 1;  // only thread k writes flag[k] here; readers use bit 16 only
     atomicMin(&sm.claim[f], k);
   }
-}
-
-__global__ void kb_merge_decide(const Slot* __restrict__ slots, SmConsts K, float merge_alpha) {
-  pdl_enter();
-  SLOT_Y;
-  // only valid ids decide, and none lies above the largest id in use
-  const int n = min(S.sp.cap, S.sc->max_spix + 1);
-  FOR_SP(k, n) merge_decide_one(S.sp, S.sm, S.sc, K, merge_alpha, k);
 }
 
 // Merge set-up: candidate pairs unset, claims at +inf (cap + 2 entries).

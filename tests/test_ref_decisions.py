@@ -24,9 +24,11 @@ pytestmark = [pytest.mark.gpu,
 S2 = 0.009 ** 2
 LOG_ALPHA = float(np.log(0.5))
 # absolute agreement of the FP32 reference ratio with the FP64 oracle ratio, and the
-# band around the -2 threshold inside which the two may decide differently
-RATIO_ATOL = 0.25
-NEAR = 0.25
+# band around the -2 threshold inside which the two may decide differently.  The
+# reference's colour sums are FP32 atomics whose order varies from run to run, so its
+# ratio does too: runs on GB300 gave errors up to 0.26 on the 480x854 case.
+RATIO_ATOL = 0.5
+NEAR = 0.5
 _ref = {}
 
 
