@@ -264,18 +264,16 @@ __global__ void kb_init_prior_mu(const Slot* __restrict__ slots) {
 
 // ---------------------------------------------------------------------------
 // Sufficient statistics (sum_by_label, update_params.cu:89-130), R1.  A warp owns a
-// 32 x 8 block of a frame: lane = column, and it holds the block's 8 labels and
-// fixed-point colours of its column in registers (every load issued before any is
-// used).  The warp then takes the block's labels one at a time (the first pending
-// label of the lowest lane that still has one): each lane sums its pixels of that
-// label, the warp adds the lanes' sums with full-warp reductions (colour sums in
+// 32 x 8 block of a frame: lane = column, and it holds the block's 8 labels and colours
+// of its column in registers (every load issued before any is used).  The warp then
+// takes the block's labels one at a time (label_rounds): each lane sums its pixels of
+// that label, the warp adds the lanes' sums with full-warp reductions (colour sums in
 // 24-bit parts, positions relative to the block so they fit 32 bits) and one lane adds
 // the label's totals to its global sums with one set of 64-bit atomics.  A block holds
-// a few labels, so a few reductions and atomic sets serve 256 pixels (the row-segment
-// scatter this replaces, with a set of atomics per run of a 32-pixel row, took 50 us
-// per 8-frame 480x854 batch against 43 us here).  Integer sums: the totals do not
-// depend on the grouping or the order of the adds.
-// cw: the warp's shared staging rows (colours other than unit ones).
+// a few labels, so a few reductions and atomic sets serve 256 pixels.  Colours in
+// [0, 1] are summed in 32 bits (one conversion each); others wait in the warp's shared
+// staging rows `cw` and are converted and summed in 64 bits in their label's round.
+// Integer sums: the totals do not depend on the grouping or the order of the adds.
 __device__ __forceinline__ void block_stats(const Slot& S, int bx, int by, float (*cw)[3][32]) {
   const int lane = threadIdx.x & 31;
   const int H = S.H, W = S.W;
