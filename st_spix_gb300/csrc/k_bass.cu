@@ -651,7 +651,8 @@ __global__ void kb_post_list(const Slot* __restrict__ slots, int incremental) {
   int base = 0;
   if (lane == leader) base = atomicAdd(&S.sc->npost, __popc(m));
   base = __shfl_sync(0xffffffffu, base, leader);
-  if (want) S.post_ids[base + __popc(m & ((1u << lane) - 1))] = k;
+  const int pos = base + __popc(m & ((1u << lane) - 1));
+  if (want && pos < S.sp.cap) S.post_ids[pos] = k;     // at most cap ids are listed
 }
 
 // Grid: x blocks per slot, each taking groups of 32 listed ids x, x + gridDim.x, ...
@@ -663,7 +664,7 @@ __global__ void __launch_bounds__(128) kb_posterior(const Slot* __restrict__ slo
   pdl_enter();
   SLOT_Y;
   Scalars* sc = S.sc;
-  const int n = *(volatile int*)&sc->npost;
+  const int n = min(*(volatile int*)&sc->npost, S.sp.cap);
   for (int g = blockIdx.x; g * 32 < n; g += gridDim.x) {
     const int i = g * 32 + (threadIdx.x & 31);
     posterior_ids(S, i < n ? S.post_ids[i] : -1, incremental != 0);
