@@ -907,7 +907,7 @@ int run_relabel(stspix_ctx* ctx, cudaStream_t st, const List& L, int nb,
                 const stspix_config& cfg) {
   ctx->cur_fam = STSPIX_FAM_MERGE;
   LAUNCHB(kb_relabel_init, L.max_cap + 2, L, nb);
-  LAUNCHB(kb_living, pix_units(L.max_npix), L, nb);
+  LAUNCHG(kb_living, dim3(tiles64(L), (unsigned)nb), kThreads, L.d);
   dim3 g(blocks_for(L.max_cap),
          (unsigned)std::max(1, (L.max_nprev + kRelabelChunk - 1) / kRelabelChunk), (unsigned)nb);
   LAUNCHG(kb_relabel_compare, g, kThreads, L.d);
@@ -1212,7 +1212,7 @@ int prop_init(stspix_ctx* ctx, cudaStream_t st, const List& L) {
   if (L.B <= 0) return STSPIX_OK;
   ctx->cur_fam = STSPIX_FAM_OTHER;
   LAUNCHB(kb_write_params, L.max_cap, L, L.B);
-  LAUNCHB(kb_mark_active, pix_units(L.max_npix), L, L.B);
+  LAUNCHG(kb_mark_active, dim3(tiles64(L), (unsigned)L.B), kThreads, L.d);
   return STSPIX_OK;
 }
 

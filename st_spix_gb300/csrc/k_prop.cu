@@ -673,14 +673,23 @@ __global__ void kb_mark_active(const Slot* __restrict__ slots) {
   pdl_enter();
   SLOT_Y;
   const SpDev& sp = S.sp;
-  FOR_PIX(t, S.npix) {
-    // one store per run of equal labels (the run's first pixel)
-    const int v = S.seg[t];
-    if (v >= 0 && v < sp.cap && (t == 0 || S.seg[t - 1] != v)) {
-      sp.valid[v] = 1;
-      sp.prop[v] = 1;
-    }
+  int gx, by;
+  if (!warp_block(S.W, S.H, gx, by)) return;
+  // one store pair per label of a warp's 32 x 8 block (many blocks share a label)
+  int lab[8];
+  unsigned pend = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int gy = by + i;
+    lab[i] = (gx < S.W && gy < S.H) ? S.seg[(size_t)gy * S.W + gx] : -1;
+    if (lab[i] >= 0 && lab[i] < sp.cap) pend |= 1u << i;
   }
+  label_rounds(lab, pend, [&](int k, unsigned, int src) {
+    if ((int)(threadIdx.x & 31) == src) {
+      sp.valid[k] = 1;
+      sp.prop[k] = 1;
+    }
+  });
 }
 
 
@@ -706,11 +715,20 @@ __global__ void kb_living(const Slot* __restrict__ slots) {
   SLOT_Y;
   if (!S.mode) return;
   const int ms = S.sc->max_spix;
-  FOR_PIX(t, S.npix) {
-    // one store per run of equal labels (the run's first pixel)
-    const int v = S.seg[t];
-    if (v >= 0 && v <= ms && (t == 0 || S.seg[t - 1] != v)) S.living[v] = 1;
+  int gx, by;
+  if (!warp_block(S.W, S.H, gx, by)) return;
+  // one store per label of a warp's 32 x 8 block (many blocks share a label)
+  int lab[8];
+  unsigned pend = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int gy = by + i;
+    lab[i] = (gx < S.W && gy < S.H) ? S.seg[(size_t)gy * S.W + gx] : -1;
+    if (lab[i] >= 0 && lab[i] <= ms) pend |= 1u << i;
   }
+  label_rounds(lab, pend, [&](int k, unsigned, int src) {
+    if ((int)(threadIdx.x & 31) == src) S.living[k] = 1;
+  });
 }
 
 // find_most_similar_spix (relabel.cu:201-276): grid (s, candidate chunk of
