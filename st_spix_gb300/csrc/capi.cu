@@ -1424,10 +1424,9 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
   // as a CUDA graph once its launch sequence repeats
   if ((stages & kStageSeg) && stop_after < 0 && !split_dir && !ctx->prof_on && ctx->graphs_on) {
     const std::string key = batch_signature(fr, caps, nit, stages, cfg);
-    if ((r = run_graphed(ctx, st, key + "h", [&](cudaStream_t s) {
-           return batch_head(ctx, s, stages, La, Lb, Lp);
-         })))
-      return r;
+    r = run_graphed(ctx, st, key + "h",
+                    [&](cudaStream_t s) { return batch_head(ctx, s, stages, La, Lb, Lp); });
+    if (r) return r;
     if (need_ladder) {
       if ((r = read_scalars(ctx, st, B))) return r;
       for (int i = 0; i < B; i++) {
@@ -1441,10 +1440,10 @@ int run_batch(stspix_ctx* ctx, cudaStream_t st, std::vector<FrameDesc>& fr,
     bool own = false;
     const List Ls = sort_table(nit_sorted, &own);
     const std::string tkey = need_ladder ? batch_signature(fr, caps, nit, stages, cfg) : key;
-    if ((r = run_graphed(ctx, st, tkey + "t", [&](cudaStream_t s) {
-           return batch_tail(ctx, s, Lp, Ls, own, nit_sorted, cfg);
-         })))
-      return r;
+    r = run_graphed(ctx, st, tkey + "t", [&](cudaStream_t s) {
+      return batch_tail(ctx, s, Lp, Ls, own, nit_sorted, cfg);
+    });
+    if (r) return r;
     return finish();
   }
   if ((r = upload(ctx, st, La, 0)) || (r = upload(ctx, st, Lb, 1)) || (r = upload(ctx, st, Lp, 2)))
